@@ -1,0 +1,295 @@
+/*
+ * h264r.h — C ABI of the GB300 H.264 macroblock-reconstruction engine.
+ *
+ * The host side (entropy decoding, slice headers, reference lists, motion
+ * vector derivation, DPB bookkeeping) stays serial on the CPU and emits, per
+ * decoded picture, the compact records declared here.  The engine turns the
+ * records into decoded samples on the GPU:
+ *   8.5  dequantisation and 4x4 / 8x8 / DC inverse transforms
+ *   8.4.2 quarter-sample luma and eighth-sample chroma motion compensation
+ *        with default / explicit / implicit weighted prediction
+ *   8.3  intra prediction (4x4, 8x8, 16x16, chroma, I_PCM)
+ *   8.7  deblocking
+ *
+ * It replaces, for that path, the per-macroblock reconstruction calls the
+ * reference decoder makes from its slice-data loop
+ * (h264_video_decoder_demo/H264SliceData.cpp:222-227, 333-338, 389-487) and
+ * the per-picture deblocking call
+ * (h264_video_decoder_demo/H264PictureBase.cpp:707 ->
+ *  H264PictureDeblockingFilterProcess.cpp:76).
+ *
+ * Conventions follow the reference decoder: every entry point returns 0 on
+ * success and a negative error code on failure (CommonFunction.h:40-47);
+ * h264r_last_error() gives a one-line reason.  No call traps or hangs: device
+ * side waits are bounded and surface as H264R_ERR_DEVICE_TIMEOUT.
+ *
+ * All integer fields are little-endian host order; structures are packed to
+ * the sizes asserted below so that the same bytes can be copied to the GPU.
+ */
+#ifndef H264R_H
+#define H264R_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define H264R_ABI_VERSION 1
+
+/* ---- error codes ------------------------------------------------------ */
+#define H264R_OK                 0
+#define H264R_ERR_INVALID_ARG   -1   /* null pointer, size out of range        */
+#define H264R_ERR_BAD_RECORD    -2   /* record field out of range (validator)  */
+#define H264R_ERR_UNSUPPORTED   -3   /* coding tool outside the engine's scope */
+#define H264R_ERR_CUDA          -4   /* CUDA runtime error                      */
+#define H264R_ERR_NO_MEMORY     -5   /* device/pinned allocation failed         */
+#define H264R_ERR_BUDGET        -6   /* admission refused: DPB memory budget    */
+#define H264R_ERR_DEVICE_TIMEOUT -7  /* a bounded device-side wait expired      */
+#define H264R_ERR_BUSY          -8   /* no free slot / queue full               */
+
+/* ---- macroblock record ------------------------------------------------- */
+/* mb type classes (derived from mb_type / MbPartPredMode, 7.4.5)          */
+#define H264R_MB_INTER   0   /* P/B, including P_Skip and B_Skip          */
+#define H264R_MB_I4x4    1
+#define H264R_MB_I8x8    2
+#define H264R_MB_I16x16  3
+#define H264R_MB_IPCM    4
+#define H264R_MB_NONE    5   /* not decoded (its slice was lost): samples
+                                stay zero; see the deblocking stop rule    */
+
+/* h264r_mb.flags */
+#define H264R_MBF_T8x8        0x01  /* transform_size_8x8_flag               */
+#define H264R_MBF_FIELD       0x02  /* mb_field_decoding_flag (MBAFF)        */
+#define H264R_MBF_CIP         0x04  /* constrained_intra_pred_flag           */
+
+#define H264R_NONE 0xFFFFFFFFu
+
+/*
+ * One record per macroblock, indexed by mbAddr (raster order for non-MBAFF
+ * pictures, pair order for MBAFF).  Restates the reconstruction-relevant
+ * subset of CH264MacroBlock (H264MacroBlock.h:110-252): 18,200 bytes there,
+ * 32 bytes here plus the variable-size motion / coefficient payloads.
+ */
+typedef struct h264r_mb {
+    uint8_t  type;          /* H264R_MB_*                                    */
+    uint8_t  flags;         /* H264R_MBF_*                                   */
+    uint8_t  qpy;           /* QPY, 0..51 (8-bit video: QP'Y == QPY)         */
+    uint8_t  i16_mode;      /* Intra16x16PredMode 0..3                       */
+    uint8_t  chroma_mode;   /* intra_chroma_pred_mode 0..3                   */
+    uint8_t  nz8x8;         /* bit b: 8x8 luma block b has non-zero levels   */
+    uint16_t nz4x4;         /* bit b: 4x4 luma block b (luma4x4BlkIdx order)
+                               has non-zero levels                           */
+    uint16_t slice;         /* slice number within the picture               */
+    uint16_t reserved;
+    uint32_t ipred[2];      /* Intra4x4PredMode[16] (4 bits each, block 0 in
+                               the low nibble of ipred[0]) or
+                               Intra8x8PredMode[4] in ipred[0] bits 0..15     */
+    uint32_t coef;          /* byte offset into the coefficient pool, or
+                               H264R_NONE when the MB has no levels          */
+    uint32_t aux;           /* inter: byte offset into the motion pool;
+                               I_PCM: index of its 384-byte sample block      */
+    uint32_t reserved2;
+} h264r_mb;
+
+/*
+ * Coefficient payload of one macroblock, at h264r_mb.coef (4-byte aligned):
+ *   uint32 mask        which blocks are present:
+ *                        bits 0..15  4x4 luma block (luma4x4BlkIdx) levels
+ *                                    (Intra16x16: the AC list, scan pos 1..15)
+ *                        bits 0..3   8x8 luma block (when H264R_MBF_T8x8)
+ *                        bit  16     Intra16x16 luma DC
+ *                        bits 17,18  Cb / Cr chroma DC (4:2:0: 4 levels)
+ *                        bits 19..22 Cb AC blocks 0..3 (scan pos 1..15)
+ *                        bits 23..26 Cr AC blocks 0..3
+ *   uint16 sig[...]    per present block, in mask bit order: one significance
+ *                      word (bit i = scan position i non-zero), four words
+ *                      for an 8x8 block (positions 0..63)
+ *   (pad to 4 bytes)
+ *   int16  level[...]  the non-zero levels, block after block, ascending scan
+ *                      position
+ * Levels are in coded scan order (zig-zag, or field scan for field MBs), as
+ * the reference stores them in LumaLevel4x4 / LumaLevel8x8 /
+ * Intra16x16DCLevel / Intra16x16ACLevel / ChromaDCLevel / ChromaACLevel.
+ */
+#define H264R_CM_LUMA_DC  (1u << 16)
+#define H264R_CM_CB_DC    (1u << 17)
+#define H264R_CM_CR_DC    (1u << 18)
+#define H264R_CM_CB_AC0   19
+#define H264R_CM_CR_AC0   23
+
+/*
+ * Motion payload of one inter macroblock, at h264r_mb.aux (4-byte aligned):
+ *   uint16 shape       bits 0..1: 0 16x16, 1 16x8, 2 8x16, 3 8x8
+ *                      bits 2+2q..3+2q: sub-partition of 8x8 quadrant q
+ *                                       (0 8x8, 1 8x4, 2 4x8, 3 4x4)
+ *   uint16 count       number of h264r_part entries that follow
+ *   h264r_part part[count]   ordered by (mbPartIdx, subMbPartIdx)
+ * B_Skip / B_Direct_16x16 / B_Direct_8x8 quadrants are described as 4x4
+ * sub-partitions, which is how the reference predicts them
+ * (H264InterPrediction.cpp:475-486).
+ */
+typedef struct h264r_part {
+    int16_t  mv[2][2];      /* [list][x,y] luma motion vector, 1/4 sample    */
+    int8_t   ref[2];        /* motion-compensation reference per list, -1 if
+                               the list is unused; bits 0..4 DPB slot,
+                               bit 5 field reference, bit 6 bottom field      */
+    int8_t   dref[2];       /* reference identity used by the deblocking
+                               filter's bS rules, -1 for none (see DESIGN)    */
+    uint16_t wt;            /* index into the picture's weight table         */
+    uint16_t reserved;
+} h264r_part;
+
+#define H264R_REF_SLOT(r)   ((r) & 31)
+#define H264R_REF_FIELD     0x20
+#define H264R_REF_BOTTOM    0x40
+
+/* Weighted-prediction parameters of one partition (8.4.2.3, 8.4.3). */
+typedef struct h264r_weight {
+    int8_t   weighted;      /* 0: default prediction 8.4.2.3.1;
+                               1: weighted prediction 8.4.2.3.2             */
+    int8_t   log_wd[3];     /* logWD for Y, Cb, Cr                           */
+    int16_t  w0[3], w1[3];  /* weights                                       */
+    int16_t  o0[3], o1[3];  /* offsets (already scaled by bit depth)        */
+    int16_t  reserved[2];
+} h264r_weight;
+
+/* Per-slice parameters used by reconstruction and deblocking. */
+typedef struct h264r_slice {
+    int8_t   chroma_qp_offset[2];   /* chroma_qp_index_offset,
+                                       second_chroma_qp_index_offset        */
+    int8_t   filter_offset_a;       /* FilterOffsetA = alpha offset << 1     */
+    int8_t   filter_offset_b;       /* FilterOffsetB                         */
+    uint8_t  disable_deblocking_filter_idc;
+    uint8_t  slice_type;            /* 0 P, 1 B, 2 I, 3 SP, 4 SI             */
+    uint8_t  reserved[2];
+} h264r_slice;
+
+#define H264R_STRUCT_FRAME   0
+#define H264R_STRUCT_TOP     1
+#define H264R_STRUCT_BOTTOM  2
+
+/* One decoded picture's worth of records (host or device pointers). */
+typedef struct h264r_picture {
+    uint16_t width_mbs;        /* PicWidthInMbs                              */
+    uint16_t height_mbs;       /* FrameHeightInMbs                           */
+    uint8_t  structure;        /* H264R_STRUCT_*                             */
+    uint8_t  mbaff;            /* MbaffFrameFlag                             */
+    uint8_t  dst_slot;         /* DPB slot that receives the samples         */
+    uint8_t  deblock;          /* 1: run the 8.7 deblocking filter           */
+    uint16_t num_slices;
+    uint16_t num_weights;
+    uint32_t num_mbs;          /* PicSizeInMbs                               */
+    uint32_t motion_bytes;
+    uint32_t coef_bytes;
+    uint32_t num_pcm;
+    uint8_t  scaling4x4[6][16];/* ScalingList4x4, coded (zig-zag) order      */
+    uint8_t  scaling8x8[6][64];/* ScalingList8x8                             */
+    const h264r_mb     *mbs;
+    const h264r_slice  *slices;
+    const h264r_weight *weights;
+    const uint8_t      *motion;
+    const uint8_t      *coef;
+    const uint8_t      *pcm;    /* 384 bytes per I_PCM MB: 256 Y, 64 Cb, 64 Cr */
+} h264r_picture;
+
+/* ---- engine objects ----------------------------------------------------- */
+typedef struct h264r_ctx h264r_ctx;
+typedef struct h264r_stream h264r_stream;
+
+typedef struct h264r_cfg {
+    int      device;             /* CUDA device ordinal                      */
+    uint64_t dpb_budget_bytes;   /* admission budget for all stream DPBs;
+                                    0 = 90% of free device memory            */
+    uint32_t max_batch_pictures; /* pictures per batched launch (0: 64)      */
+    uint32_t flags;              /* reserved, 0                              */
+} h264r_cfg;
+
+typedef struct h264r_stream_cfg {
+    uint16_t width_mbs;
+    uint16_t height_mbs;         /* frame height in MBs                      */
+    uint16_t dpb_slots;          /* number of picture buffers (<= 32)        */
+    uint16_t reserved;
+} h264r_stream_cfg;
+
+/*
+ * Create / destroy an engine context on one GPU.
+ * Replaces: the reference's per-decoder state set up in
+ * CH264VideoDecoder::open (H264VideoDecoder.cpp:56-80).
+ */
+int  h264r_ctx_create(const h264r_cfg *cfg, h264r_ctx **out);
+int  h264r_ctx_destroy(h264r_ctx *ctx);
+const char *h264r_last_error(const h264r_ctx *ctx);
+
+/*
+ * Open a stream: allocate its device-resident DPB (dpb_slots pictures in the
+ * reference's single-allocation Y/Cb/Cr layout, H264PictureBase.cpp:162-181).
+ * Replaces: CH264PicturesGOP's 16 CH264Picture buffers
+ * (H264PicturesGOP.cpp:27-50).  Fails with H264R_ERR_BUDGET when the DPB
+ * would exceed the context's memory budget.
+ */
+int  h264r_stream_open(h264r_ctx *ctx, const h264r_stream_cfg *cfg, h264r_stream **out);
+int  h264r_stream_close(h264r_stream *s);
+uint64_t h264r_stream_dpb_bytes(const h264r_stream_cfg *cfg);
+
+/*
+ * Reconstruct one picture from host-resident records: copies the records to
+ * the device (through pinned staging), runs inter + intra reconstruction and
+ * deblocking into DPB slot pic->dst_slot, and returns once the work is
+ * enqueued on the stream.  Replaces the reconstruction dispatch of
+ * CH264SliceData::slice_data (H264SliceData.cpp:389-487, skip paths 222-227
+ * and 333-338) plus CH264PictureBase::Deblocking_filter_process
+ * (H264PictureDeblockingFilterProcess.cpp:76).
+ */
+int  h264r_submit_picture(h264r_stream *s, const h264r_picture *pic);
+
+/*
+ * Same as h264r_submit_picture, but every pointer in pic (mbs, slices,
+ * weights, motion, coef, pcm) is already device memory.  Used when the
+ * records are staged on the GPU ahead of time.
+ */
+int  h264r_submit_picture_device(h264r_stream *s, const h264r_picture *pic);
+
+/*
+ * Batched reconstruction: n independent pictures (of any streams in the same
+ * context; no picture may reference another picture of the same batch) in
+ * one fused launch sequence.  Pointers are device memory.
+ */
+int  h264r_submit_batch_device(h264r_ctx *ctx, int n, h264r_stream *const *streams,
+                               const h264r_picture *pics);
+
+/*
+ * Copy a decoded picture (DPB slot) to host planes at coded size: luma
+ * width_mbs*16 x height_mbs*16, chroma half in each direction.  Replaces the
+ * borrowed CH264Picture the reference hands to its output callback
+ * (H264VideoDecoder.cpp:383-435).  Enqueued; call h264r_stream_sync before
+ * reading the planes.
+ */
+int  h264r_output(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *cr);
+/* Upload host planes into a DPB slot (initial state / tests). */
+int  h264r_load_slot(h264r_stream *s, int slot, const uint8_t *y, const uint8_t *cb, const uint8_t *cr);
+/* Device address of a DPB slot's Y plane (Cb, Cr follow contiguously). */
+int  h264r_slot_device_ptr(h264r_stream *s, int slot, void **dev_y);
+int  h264r_stream_sync(h264r_stream *s);
+int  h264r_ctx_sync(h264r_ctx *ctx);
+/* The CUDA stream the engine enqueues this stream's work on (cudaStream_t). */
+void *h264r_stream_cuda_stream(h264r_stream *s);
+
+/* Validate a picture's records on the host (ranges, offsets, payload sizes).
+ * Returns 0 or H264R_ERR_BAD_RECORD / H264R_ERR_UNSUPPORTED. */
+int  h264r_validate_picture(const h264r_picture *pic, int dpb_slots);
+
+/* Number of engine kernels launched so far by this context. */
+uint64_t h264r_ctx_kernel_launches(const h264r_ctx *ctx);
+
+/* Device timing of the kernels of the last submitted picture / batch, in ms:
+ * t[0] inter, t[1] intra, t[2] deblock (0 when timing is disabled). */
+int  h264r_ctx_set_timing(h264r_ctx *ctx, int enable);
+int  h264r_ctx_last_timing(h264r_ctx *ctx, float t[3]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* H264R_H */
