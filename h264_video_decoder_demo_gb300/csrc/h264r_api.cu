@@ -1,0 +1,692 @@
+// h264r_api.cu — host side of the reconstruction engine behind the C ABI of
+// include/h264r.h: contexts, streams with device-resident DPBs, record
+// staging (pinned host -> device) and the launch sequence
+//   k_inter -> k_intra (only when the batch has intra MBs) -> k_bs -> k_deblock
+// on the stream's CUDA stream.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "h264r_device.cuh"
+
+namespace h264r {
+__global__ void k_inter(const PicDesc *__restrict__ pics, int npics, LaunchState st);
+__global__ void k_intra(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st);
+__global__ void k_bs(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
+__global__ void k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st);
+}  // namespace h264r
+
+using h264r::PicDesc;
+using h264r::LaunchState;
+
+static_assert(sizeof(h264r_mb) == 32, "h264r_mb layout");
+static_assert(sizeof(h264r_part) == 16, "h264r_part layout");
+static_assert(sizeof(h264r_weight) == 32, "h264r_weight layout");
+static_assert(sizeof(h264r_slice) == 8, "h264r_slice layout");
+
+namespace {
+
+constexpr int kRing = 4;                 // in-flight launches per stream
+constexpr uint64_t kAlign = 256;
+constexpr unsigned long long kSpinLimit = 1ull << 25;  // ~ seconds of 64 ns sleeps
+
+inline uint64_t align_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
+
+// Per-launch scratch: PicDesc array, wavefront tickets, progress counters,
+// bS tables.  Host mirror in pinned memory, device copy uploaded per launch.
+struct LaunchBuf {
+    uint8_t *host = nullptr;      // pinned: PicDesc array, tickets, progress
+    uint64_t host_cap = 0;
+    uint8_t *dev = nullptr;       // its device copy
+    uint64_t dev_cap = 0;
+    uint8_t *bs = nullptr;        // device, bS tables
+    uint64_t bs_cap = 0;
+    uint8_t *rec_host = nullptr;  // pinned staging for host-resident records
+    uint64_t rec_host_cap = 0;
+    uint8_t *rec_dev = nullptr;   // device copy of the records
+    uint64_t rec_dev_cap = 0;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+};
+
+}  // namespace
+
+struct h264r_ctx {
+    int device = 0;
+    uint64_t budget = 0, used = 0;
+    uint32_t max_batch = 64;
+    int *d_error = nullptr;
+    int *h_error = nullptr;  // pinned
+    std::atomic<uint64_t> launches{0};
+    bool timing = false;
+    float last_ms[3] = {0, 0, 0};
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaStream_t batch_stream = nullptr;
+    LaunchBuf batch_ring[kRing];
+    int batch_next = 0;
+    std::mutex mu;
+    char err[256] = {0};
+};
+
+struct h264r_stream {
+    h264r_ctx *ctx = nullptr;
+    h264r_stream_cfg cfg{};
+    uint64_t slot_bytes = 0;
+    uint8_t *dpb = nullptr;
+    cudaStream_t cs = nullptr;
+    LaunchBuf ring[kRing];
+    int next = 0;
+};
+
+static void set_err(h264r_ctx *ctx, const char *fmt, ...)
+{
+    if (!ctx) return;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(ctx->err, sizeof(ctx->err), fmt, ap);
+    va_end(ap);
+}
+
+#define CUDA_OR(ctx, expr)                                                                  \
+    do {                                                                                    \
+        cudaError_t e_ = (expr);                                                            \
+        if (e_ != cudaSuccess) {                                                            \
+            set_err((ctx), "%s: %s", #expr, cudaGetErrorString(e_));                        \
+            return H264R_ERR_CUDA;                                                          \
+        }                                                                                   \
+    } while (0)
+
+extern "C" uint64_t h264r_stream_dpb_bytes(const h264r_stream_cfg *cfg)
+{
+    if (!cfg) return 0;
+    uint64_t W = (uint64_t)cfg->width_mbs * 16, H = (uint64_t)cfg->height_mbs * 16;
+    uint64_t slot = align_up(W * H * 3 / 2 + 4 * W + 64, kAlign);
+    return slot * cfg->dpb_slots;
+}
+
+static uint64_t slot_bytes_of(const h264r_stream_cfg &c)
+{
+    uint64_t W = (uint64_t)c.width_mbs * 16, H = (uint64_t)c.height_mbs * 16;
+    return align_up(W * H * 3 / 2 + 4 * W + 64, kAlign);
+}
+
+extern "C" int h264r_ctx_create(const h264r_cfg *cfg, h264r_ctx **out)
+{
+    if (!out) return H264R_ERR_INVALID_ARG;
+    *out = nullptr;
+    h264r_ctx *ctx = new (std::nothrow) h264r_ctx();
+    if (!ctx) return H264R_ERR_NO_MEMORY;
+    ctx->device = cfg ? cfg->device : 0;
+    if (cfg && cfg->max_batch_pictures) ctx->max_batch = cfg->max_batch_pictures;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) {
+        fprintf(stderr, "h264r_ctx_create: cudaSetDevice(%d): %s\n", ctx->device, cudaGetErrorString(e));
+        delete ctx;
+        return H264R_ERR_CUDA;
+    }
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    ctx->budget = (cfg && cfg->dpb_budget_bytes) ? cfg->dpb_budget_bytes : (uint64_t)(free_b * 0.9);
+    if (cudaMalloc(&ctx->d_error, sizeof(int)) != cudaSuccess || cudaMallocHost(&ctx->h_error, sizeof(int)) != cudaSuccess ||
+        cudaMemset(ctx->d_error, 0, sizeof(int)) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->batch_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return H264R_ERR_CUDA;
+    }
+    for (auto &ev : ctx->ev) cudaEventCreate(&ev);
+    for (auto &b : ctx->batch_ring) cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming);
+    *ctx->h_error = 0;
+    *out = ctx;
+    return H264R_OK;
+}
+
+static void free_buf(LaunchBuf &b)
+{
+    if (b.host) cudaFreeHost(b.host);
+    if (b.dev) cudaFree(b.dev);
+    if (b.bs) cudaFree(b.bs);
+    if (b.rec_host) cudaFreeHost(b.rec_host);
+    if (b.rec_dev) cudaFree(b.rec_dev);
+    if (b.done) cudaEventDestroy(b.done);
+    b = LaunchBuf();
+}
+
+extern "C" int h264r_ctx_destroy(h264r_ctx *ctx)
+{
+    if (!ctx) return H264R_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->batch_stream);
+    for (auto &b : ctx->batch_ring) free_buf(b);
+    for (auto &ev : ctx->ev) cudaEventDestroy(ev);
+    cudaStreamDestroy(ctx->batch_stream);
+    cudaFree(ctx->d_error);
+    cudaFreeHost(ctx->h_error);
+    delete ctx;
+    return H264R_OK;
+}
+
+extern "C" const char *h264r_last_error(const h264r_ctx *ctx) { return ctx ? ctx->err : "no context"; }
+
+extern "C" uint64_t h264r_ctx_kernel_launches(const h264r_ctx *ctx) { return ctx ? ctx->launches.load() : 0; }
+
+extern "C" int h264r_ctx_set_timing(h264r_ctx *ctx, int enable)
+{
+    if (!ctx) return H264R_ERR_INVALID_ARG;
+    ctx->timing = enable != 0;
+    return H264R_OK;
+}
+
+extern "C" int h264r_ctx_last_timing(h264r_ctx *ctx, float t[3])
+{
+    if (!ctx || !t) return H264R_ERR_INVALID_ARG;
+    if (ctx->timing) {
+        CUDA_OR(ctx, cudaEventSynchronize(ctx->ev[3]));
+        cudaEventElapsedTime(&ctx->last_ms[0], ctx->ev[0], ctx->ev[1]);
+        cudaEventElapsedTime(&ctx->last_ms[1], ctx->ev[1], ctx->ev[2]);
+        cudaEventElapsedTime(&ctx->last_ms[2], ctx->ev[2], ctx->ev[3]);
+    }
+    memcpy(t, ctx->last_ms, sizeof(ctx->last_ms));
+    return H264R_OK;
+}
+
+extern "C" int h264r_stream_open(h264r_ctx *ctx, const h264r_stream_cfg *cfg, h264r_stream **out)
+{
+    if (!ctx || !cfg || !out) return H264R_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (cfg->width_mbs == 0 || cfg->height_mbs == 0 || cfg->width_mbs > 512 || cfg->height_mbs > 512 || cfg->dpb_slots == 0 ||
+        cfg->dpb_slots > 32) {
+        set_err(ctx, "h264r_stream_open: bad geometry %ux%u MBs, %u slots", cfg->width_mbs, cfg->height_mbs, cfg->dpb_slots);
+        return H264R_ERR_INVALID_ARG;
+    }
+    uint64_t bytes = h264r_stream_dpb_bytes(cfg);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (ctx->used + bytes > ctx->budget) {
+        set_err(ctx, "h264r_stream_open: DPB of %llu bytes exceeds the remaining budget (%llu of %llu used)",
+                (unsigned long long)bytes, (unsigned long long)ctx->used, (unsigned long long)ctx->budget);
+        return H264R_ERR_BUDGET;
+    }
+    h264r_stream *s = new (std::nothrow) h264r_stream();
+    if (!s) return H264R_ERR_NO_MEMORY;
+    s->ctx = ctx;
+    s->cfg = *cfg;
+    s->slot_bytes = slot_bytes_of(*cfg);
+    cudaSetDevice(ctx->device);
+    if (cudaMalloc(&s->dpb, bytes) != cudaSuccess) {
+        set_err(ctx, "h264r_stream_open: cudaMalloc(%llu) failed", (unsigned long long)bytes);
+        delete s;
+        return H264R_ERR_NO_MEMORY;
+    }
+    // the reference starts every picture buffer cleared (H264PictureBase.cpp:162-181)
+    cudaMemset(s->dpb, 0, bytes);
+    cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking);
+    for (auto &b : s->ring) cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming);
+    cudaDeviceSynchronize();
+    ctx->used += bytes;
+    *out = s;
+    return H264R_OK;
+}
+
+extern "C" int h264r_stream_close(h264r_stream *s)
+{
+    if (!s) return H264R_ERR_INVALID_ARG;
+    h264r_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(s->cs);
+    for (auto &b : s->ring) free_buf(b);
+    cudaStreamDestroy(s->cs);
+    cudaFree(s->dpb);
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        ctx->used -= h264r_stream_dpb_bytes(&s->cfg);
+    }
+    delete s;
+    return H264R_OK;
+}
+
+extern "C" void *h264r_stream_cuda_stream(h264r_stream *s) { return s ? (void *)s->cs : nullptr; }
+
+extern "C" int h264r_slot_device_ptr(h264r_stream *s, int slot, void **dev_y)
+{
+    if (!s || !dev_y || slot < 0 || slot >= s->cfg.dpb_slots) return H264R_ERR_INVALID_ARG;
+    *dev_y = s->dpb + (uint64_t)slot * s->slot_bytes;
+    return H264R_OK;
+}
+
+// ---------------------------------------------------------------- validator
+static int parts_count(uint32_t shape)
+{
+    int mp = shape & 3;
+    if (mp == 0) return 1;
+    if (mp != 3) return 2;
+    int n = 0;
+    for (int q = 0; q < 4; q++) {
+        int sc = (shape >> (2 + 2 * q)) & 3;
+        n += (sc == 0) ? 1 : (sc == 3 ? 4 : 2);
+    }
+    return n;
+}
+
+extern "C" int h264r_validate_picture(const h264r_picture *pic, int dpb_slots)
+{
+    if (!pic || !pic->mbs || !pic->slices || !pic->weights) return H264R_ERR_INVALID_ARG;
+    if (pic->structure != H264R_STRUCT_FRAME) return H264R_ERR_UNSUPPORTED;
+    if (pic->width_mbs == 0 || pic->height_mbs == 0 || pic->num_mbs != (uint32_t)pic->width_mbs * pic->height_mbs)
+        return H264R_ERR_BAD_RECORD;
+    if (pic->mbaff && (pic->height_mbs & 1)) return H264R_ERR_BAD_RECORD;
+    if (pic->dst_slot >= dpb_slots || pic->num_slices == 0 || pic->num_weights == 0) return H264R_ERR_BAD_RECORD;
+    if ((pic->motion_bytes && !pic->motion) || (pic->coef_bytes && !pic->coef) || (pic->num_pcm && !pic->pcm))
+        return H264R_ERR_INVALID_ARG;
+    for (uint32_t i = 0; i < pic->num_weights; i++)
+        for (int c = 0; c < 3; c++)
+            if (pic->weights[i].log_wd[c] < 0 || pic->weights[i].log_wd[c] > 7) return H264R_ERR_BAD_RECORD;
+    for (uint32_t i = 0; i < pic->num_slices; i++)
+        if (pic->slices[i].disable_deblocking_filter_idc > 2 || pic->slices[i].slice_type > 4 ||
+            pic->slices[i].filter_offset_a < -12 || pic->slices[i].filter_offset_a > 12 ||
+            pic->slices[i].filter_offset_b < -12 || pic->slices[i].filter_offset_b > 12)
+            return H264R_ERR_BAD_RECORD;
+    for (uint32_t a = 0; a < pic->num_mbs; a++) {
+        const h264r_mb &m = pic->mbs[a];
+        if (m.type > H264R_MB_NONE || m.qpy > 51 || m.slice >= pic->num_slices || m.i16_mode > 3 || m.chroma_mode > 3)
+            return H264R_ERR_BAD_RECORD;
+        if (m.coef != H264R_NONE) {
+            if ((m.coef & 3) || (uint64_t)m.coef + 4 > pic->coef_bytes) return H264R_ERR_BAD_RECORD;
+            uint32_t mask;
+            memcpy(&mask, pic->coef + m.coef, 4);
+            if (mask >> 27) return H264R_ERR_BAD_RECORD;
+            int t8 = (m.flags & H264R_MBF_T8x8) != 0;
+            if (t8 && (mask & 0xFFF0u)) return H264R_ERR_BAD_RECORD;
+            uint64_t nw = __builtin_popcount(mask) + (t8 ? 3 * __builtin_popcount(mask & 15u) : 0);
+            uint64_t voff = (4 + 2 * nw + 3) & ~3ull;
+            if (m.coef + voff > pic->coef_bytes) return H264R_ERR_BAD_RECORD;
+            uint64_t nl = 0;
+            for (uint64_t w = 0; w < nw; w++) {
+                uint16_t s;
+                memcpy(&s, pic->coef + m.coef + 4 + 2 * w, 2);
+                nl += __builtin_popcount(s);
+            }
+            if (m.coef + voff + 2 * nl > pic->coef_bytes) return H264R_ERR_BAD_RECORD;
+        }
+        if (m.type == H264R_MB_INTER) {
+            if (m.aux == H264R_NONE || (m.aux & 3) || (uint64_t)m.aux + 4 > pic->motion_bytes) return H264R_ERR_BAD_RECORD;
+            uint16_t hdr[2];
+            memcpy(hdr, pic->motion + m.aux, 4);
+            if (hdr[1] != parts_count(hdr[0]) || (uint64_t)m.aux + 4 + 16ull * hdr[1] > pic->motion_bytes) return H264R_ERR_BAD_RECORD;
+            for (int e = 0; e < hdr[1]; e++) {
+                h264r_part p;
+                memcpy(&p, pic->motion + m.aux + 4 + 16 * e, 16);
+                if (p.wt >= pic->num_weights) return H264R_ERR_BAD_RECORD;
+                for (int l = 0; l < 2; l++) {
+                    if (p.ref[l] >= 0 && (H264R_REF_SLOT(p.ref[l]) >= dpb_slots || H264R_REF_SLOT(p.ref[l]) == pic->dst_slot))
+                        return H264R_ERR_BAD_RECORD;
+                    if (p.ref[l] >= 0 && (p.ref[l] & H264R_REF_FIELD) && !((m.flags & H264R_MBF_FIELD) && pic->mbaff))
+                        return H264R_ERR_BAD_RECORD;
+                }
+            }
+        } else if (m.type == H264R_MB_IPCM) {
+            if (m.aux >= pic->num_pcm) return H264R_ERR_BAD_RECORD;
+        }
+    }
+    return H264R_OK;
+}
+
+// ---------------------------------------------------------------- launching
+static int ensure(h264r_ctx *ctx, uint8_t **p, uint64_t *cap, uint64_t need, bool pinned)
+{
+    if (need <= *cap) return H264R_OK;
+    uint64_t n = align_up(need + need / 4, 1 << 16);
+    if (*p) {
+        if (pinned) cudaFreeHost(*p);
+        else cudaFree(*p);
+        *p = nullptr;
+    }
+    cudaError_t e = pinned ? cudaMallocHost(p, n) : cudaMalloc(p, n);
+    if (e != cudaSuccess) {
+        *cap = 0;
+        set_err(ctx, "allocation of %llu bytes failed: %s", (unsigned long long)n, cudaGetErrorString(e));
+        return H264R_ERR_NO_MEMORY;
+    }
+    *cap = n;
+    return H264R_OK;
+}
+
+static int wait_slot(h264r_ctx *ctx, LaunchBuf &b)
+{
+    if (b.pending) {
+        CUDA_OR(ctx, cudaEventSynchronize(b.done));
+        b.pending = false;
+    }
+    return H264R_OK;
+}
+
+static bool all_flat(const h264r_picture *pic)
+{
+    for (int i = 0; i < 6; i++)
+        for (int k = 0; k < 16; k++)
+            if (pic->scaling4x4[i][k] != 16) return false;
+    for (int i = 0; i < 6; i++)
+        for (int k = 0; k < 64; k++)
+            if (pic->scaling8x8[i][k] != 16) return false;
+    return true;
+}
+
+struct BatchItem {
+    h264r_stream *s;
+    const h264r_picture *pic;  // pointers are device memory
+    const uint8_t *scaling_dev;
+    bool has_intra;
+};
+
+// Build the PicDesc array + counters in b.host, upload, run the kernels.
+static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vector<BatchItem> &items, bool any_intra)
+{
+    const int n = (int)items.size();
+    uint64_t rows = 0, mbs = 0;
+    for (auto &it : items) {
+        uint32_t uh = it.pic->mbaff ? it.pic->height_mbs / 2 : it.pic->height_mbs;
+        rows += uh;
+        mbs += it.pic->num_mbs;
+    }
+    const uint64_t desc_bytes = align_up(sizeof(PicDesc) * n, kAlign);
+    const uint64_t ticket_off = desc_bytes;
+    const uint64_t prog_off = ticket_off + kAlign;
+    const uint64_t total = prog_off + align_up(8 * rows + 8, kAlign);
+    int rc = ensure(ctx, &b.host, &b.host_cap, total, true);
+    if (rc) return rc;
+    rc = ensure(ctx, &b.dev, &b.dev_cap, total, false);
+    if (rc) return rc;
+    rc = ensure(ctx, &b.bs, &b.bs_cap, mbs * h264r::kBsBytes + 16, false);
+    if (rc) return rc;
+    memset(b.host, 0, total);
+    PicDesc *d = (PicDesc *)b.host;
+    uint64_t mb_base = 0, row_base = 0, prog = 0;
+    for (int i = 0; i < n; i++) {
+        const h264r_picture *pic = items[i].pic;
+        h264r_stream *s = items[i].s;
+        PicDesc &p = d[i];
+        p.wmb = pic->width_mbs;
+        p.hmb = pic->height_mbs;
+        p.W = p.wmb * 16;
+        p.H = p.hmb * 16;
+        p.Wc = p.W / 2;
+        p.Hc = p.H / 2;
+        p.mbaff = pic->mbaff;
+        p.deblock = pic->deblock;
+        p.num_mbs = pic->num_mbs;
+        p.num_slices = pic->num_slices;
+        p.num_weights = pic->num_weights;
+        p.num_pcm = pic->num_pcm;
+        p.motion_bytes = pic->motion_bytes;
+        p.coef_bytes = pic->coef_bytes;
+        p.mbs = pic->mbs;
+        p.slices = pic->slices;
+        p.weights = pic->weights;
+        p.motion = pic->motion;
+        p.coef = pic->coef;
+        p.pcm = pic->pcm;
+        p.scaling = items[i].scaling_dev;
+        p.flat_scaling = all_flat(pic) ? 1 : 0;
+        p.dpb = s->dpb;
+        p.slot_bytes = s->slot_bytes;
+        p.nslots = s->cfg.dpb_slots;
+        p.dst = s->dpb + (uint64_t)pic->dst_slot * s->slot_bytes;
+        p.bs = b.bs + mb_base * h264r::kBsBytes;
+        p.units_w = pic->width_mbs;
+        p.units_h = pic->mbaff ? pic->height_mbs / 2 : pic->height_mbs;
+        p.progress = (int *)(b.dev + prog_off) + prog;
+        p.mb_base = (uint32_t)mb_base;
+        p.row_base = (uint32_t)row_base;
+        p.deblock_stop = 0xFFFFFFFFu;
+        mb_base += pic->num_mbs;
+        row_base += p.units_h;
+        prog += 2 * p.units_h;
+    }
+    CUDA_OR(ctx, cudaMemcpyAsync(b.dev, b.host, total, cudaMemcpyHostToDevice, cs));
+    LaunchState st;
+    st.error = ctx->d_error;
+    st.ticket = (unsigned int *)(b.dev + ticket_off);
+    st.spin_limit = kSpinLimit;
+    const PicDesc *dd = (const PicDesc *)b.dev;
+    bool any_deblock = false;
+    for (auto &it : items) any_deblock = any_deblock || it.pic->deblock;
+    if (ctx->timing) cudaEventRecord(ctx->ev[0], cs);
+    h264r::k_inter<<<(unsigned)mbs, 256, 0, cs>>>(dd, n, st);
+    ctx->launches++;
+    if (ctx->timing) cudaEventRecord(ctx->ev[1], cs);
+    if (any_intra) {
+        h264r::k_intra<<<(unsigned)rows, 32, 0, cs>>>(dd, n, (uint32_t)rows, st);
+        ctx->launches++;
+    }
+    if (ctx->timing) cudaEventRecord(ctx->ev[2], cs);
+    if (any_deblock) {
+        h264r::k_bs<<<(unsigned)((mbs + 3) / 4), 128, 0, cs>>>(dd, n, (uint32_t)mbs, st);
+        h264r::k_deblock<<<(unsigned)rows, 32, 0, cs>>>(dd, n, (uint32_t)rows, st);
+        ctx->launches += 2;
+    }
+    if (ctx->timing) cudaEventRecord(ctx->ev[3], cs);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_err(ctx, "kernel launch: %s", cudaGetErrorString(e));
+        return H264R_ERR_CUDA;
+    }
+    CUDA_OR(ctx, cudaEventRecord(b.done, cs));
+    b.pending = true;
+    return H264R_OK;
+}
+
+static bool has_intra_mbs(const h264r_picture *pic)
+{
+    for (uint32_t a = 0; a < pic->num_mbs; a++) {
+        int t = pic->mbs[a].type;
+        if (t == H264R_MB_I4x4 || t == H264R_MB_I8x8 || t == H264R_MB_I16x16) return true;
+    }
+    return false;
+}
+
+extern "C" int h264r_submit_picture(h264r_stream *s, const h264r_picture *pic)
+{
+    if (!s || !pic) return H264R_ERR_INVALID_ARG;
+    h264r_ctx *ctx = s->ctx;
+    int rc = h264r_validate_picture(pic, s->cfg.dpb_slots);
+    if (rc) {
+        set_err(ctx, "h264r_submit_picture: records rejected by the validator (%d)", rc);
+        return rc;
+    }
+    if (pic->width_mbs != s->cfg.width_mbs || pic->height_mbs != s->cfg.height_mbs) {
+        set_err(ctx, "h264r_submit_picture: picture size differs from the stream's");
+        return H264R_ERR_INVALID_ARG;
+    }
+    cudaSetDevice(ctx->device);
+    LaunchBuf &b = s->ring[s->next];
+    s->next = (s->next + 1) % kRing;
+    rc = wait_slot(ctx, b);
+    if (rc) return rc;
+    // pack the records: mbs | slices | weights | motion | coef | pcm | scaling
+    uint64_t off[7], sz[7] = {sizeof(h264r_mb) * pic->num_mbs, sizeof(h264r_slice) * pic->num_slices,
+                              sizeof(h264r_weight) * pic->num_weights, pic->motion_bytes, pic->coef_bytes,
+                              384ull * pic->num_pcm, 480};
+    uint64_t tot = 0;
+    for (int i = 0; i < 7; i++) {
+        off[i] = tot;
+        tot = align_up(tot + sz[i], kAlign);
+    }
+    rc = ensure(ctx, &b.rec_host, &b.rec_host_cap, tot, true);
+    if (rc) return rc;
+    rc = ensure(ctx, &b.rec_dev, &b.rec_dev_cap, tot, false);
+    if (rc) return rc;
+    const void *src[6] = {pic->mbs, pic->slices, pic->weights, pic->motion, pic->coef, pic->pcm};
+    for (int i = 0; i < 6; i++)
+        if (sz[i]) memcpy(b.rec_host + off[i], src[i], sz[i]);
+    memcpy(b.rec_host + off[6], pic->scaling4x4, 96);
+    memcpy(b.rec_host + off[6] + 96, pic->scaling8x8, 384);
+    CUDA_OR(ctx, cudaMemcpyAsync(b.rec_dev, b.rec_host, tot, cudaMemcpyHostToDevice, s->cs));
+    h264r_picture dp = *pic;
+    dp.mbs = (const h264r_mb *)(b.rec_dev + off[0]);
+    dp.slices = (const h264r_slice *)(b.rec_dev + off[1]);
+    dp.weights = (const h264r_weight *)(b.rec_dev + off[2]);
+    dp.motion = b.rec_dev + off[3];
+    dp.coef = b.rec_dev + off[4];
+    dp.pcm = b.rec_dev + off[5];
+    std::vector<BatchItem> items(1);
+    items[0].s = s;
+    items[0].pic = &dp;
+    items[0].scaling_dev = b.rec_dev + off[6];
+    items[0].has_intra = has_intra_mbs(pic);
+    return launch(ctx, s->cs, b, items, items[0].has_intra);
+}
+
+// Device-resident records: the scaling lists are read from the host struct
+// and staged with the launch buffer.
+static int submit_device(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, int n, h264r_stream *const *streams,
+                         const h264r_picture *pics)
+{
+    // scaling lists of every picture go into the record staging area
+    uint64_t tot = align_up(480ull * n, kAlign);
+    int rc = ensure(ctx, &b.rec_host, &b.rec_host_cap, tot, true);
+    if (rc) return rc;
+    rc = ensure(ctx, &b.rec_dev, &b.rec_dev_cap, tot, false);
+    if (rc) return rc;
+    std::vector<BatchItem> items(n);
+    bool any_intra = false;
+    for (int i = 0; i < n; i++) {
+        memcpy(b.rec_host + 480ull * i, pics[i].scaling4x4, 96);
+        memcpy(b.rec_host + 480ull * i + 96, pics[i].scaling8x8, 384);
+        items[i].s = streams[i];
+        items[i].pic = &pics[i];
+        items[i].scaling_dev = b.rec_dev + 480ull * i;
+        // device records: the intra kernel is always launched (it exits
+        // immediately on rows without intra MBs)
+        items[i].has_intra = true;
+        any_intra = true;
+    }
+    CUDA_OR(ctx, cudaMemcpyAsync(b.rec_dev, b.rec_host, tot, cudaMemcpyHostToDevice, cs));
+    return launch(ctx, cs, b, items, any_intra);
+}
+
+static int check_device_pic(h264r_stream *s, const h264r_picture *pic)
+{
+    if (!s || !pic || !pic->mbs || !pic->slices || !pic->weights) return H264R_ERR_INVALID_ARG;
+    if (pic->structure != H264R_STRUCT_FRAME) return H264R_ERR_UNSUPPORTED;
+    if (pic->width_mbs != s->cfg.width_mbs || pic->height_mbs != s->cfg.height_mbs ||
+        pic->num_mbs != (uint32_t)pic->width_mbs * pic->height_mbs || pic->dst_slot >= s->cfg.dpb_slots ||
+        (pic->mbaff && (pic->height_mbs & 1)))
+        return H264R_ERR_INVALID_ARG;
+    return H264R_OK;
+}
+
+extern "C" int h264r_submit_picture_device(h264r_stream *s, const h264r_picture *pic)
+{
+    int rc = check_device_pic(s, pic);
+    if (rc) {
+        if (s) set_err(s->ctx, "h264r_submit_picture_device: bad picture (%d)", rc);
+        return rc;
+    }
+    h264r_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    LaunchBuf &b = s->ring[s->next];
+    s->next = (s->next + 1) % kRing;
+    rc = wait_slot(ctx, b);
+    if (rc) return rc;
+    h264r_stream *const arr[1] = {s};
+    return submit_device(ctx, s->cs, b, 1, arr, pic);
+}
+
+extern "C" int h264r_submit_batch_device(h264r_ctx *ctx, int n, h264r_stream *const *streams, const h264r_picture *pics)
+{
+    if (!ctx || n <= 0 || !streams || !pics) return H264R_ERR_INVALID_ARG;
+    if ((uint32_t)n > ctx->max_batch) {
+        set_err(ctx, "h264r_submit_batch_device: %d pictures exceed the batch limit %u", n, ctx->max_batch);
+        return H264R_ERR_BUSY;
+    }
+    for (int i = 0; i < n; i++) {
+        if (!streams[i] || streams[i]->ctx != ctx) return H264R_ERR_INVALID_ARG;
+        int rc = check_device_pic(streams[i], &pics[i]);
+        if (rc) {
+            set_err(ctx, "h264r_submit_batch_device: picture %d rejected (%d)", i, rc);
+            return rc;
+        }
+    }
+    cudaSetDevice(ctx->device);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    LaunchBuf &b = ctx->batch_ring[ctx->batch_next];
+    ctx->batch_next = (ctx->batch_next + 1) % kRing;
+    int rc = wait_slot(ctx, b);
+    if (rc) return rc;
+    // the batch runs on the context's batch stream, after any work already
+    // queued on the member streams, and the member streams wait for it
+    cudaEvent_t ev;
+    cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    for (int i = 0; i < n; i++) {
+        cudaEventRecord(ev, streams[i]->cs);
+        cudaStreamWaitEvent(ctx->batch_stream, ev, 0);
+    }
+    rc = submit_device(ctx, ctx->batch_stream, b, n, streams, pics);
+    if (rc == H264R_OK) {
+        cudaEventRecord(ev, ctx->batch_stream);
+        for (int i = 0; i < n; i++) cudaStreamWaitEvent(streams[i]->cs, ev, 0);
+    }
+    cudaEventDestroy(ev);
+    return rc;
+}
+
+extern "C" int h264r_output(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *cr)
+{
+    if (!s || slot < 0 || slot >= s->cfg.dpb_slots || !y || !cb || !cr) return H264R_ERR_INVALID_ARG;
+    h264r_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    const uint64_t W = s->cfg.width_mbs * 16ull, H = s->cfg.height_mbs * 16ull;
+    const uint8_t *base = s->dpb + (uint64_t)slot * s->slot_bytes;
+    CUDA_OR(ctx, cudaMemcpyAsync(y, base, W * H, cudaMemcpyDeviceToHost, s->cs));
+    CUDA_OR(ctx, cudaMemcpyAsync(cb, base + W * H, W * H / 4, cudaMemcpyDeviceToHost, s->cs));
+    CUDA_OR(ctx, cudaMemcpyAsync(cr, base + W * H + W * H / 4, W * H / 4, cudaMemcpyDeviceToHost, s->cs));
+    return H264R_OK;
+}
+
+extern "C" int h264r_load_slot(h264r_stream *s, int slot, const uint8_t *y, const uint8_t *cb, const uint8_t *cr)
+{
+    if (!s || slot < 0 || slot >= s->cfg.dpb_slots || !y || !cb || !cr) return H264R_ERR_INVALID_ARG;
+    h264r_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    const uint64_t W = s->cfg.width_mbs * 16ull, H = s->cfg.height_mbs * 16ull;
+    uint8_t *base = s->dpb + (uint64_t)slot * s->slot_bytes;
+    CUDA_OR(ctx, cudaMemcpyAsync(base, y, W * H, cudaMemcpyHostToDevice, s->cs));
+    CUDA_OR(ctx, cudaMemcpyAsync(base + W * H, cb, W * H / 4, cudaMemcpyHostToDevice, s->cs));
+    CUDA_OR(ctx, cudaMemcpyAsync(base + W * H + W * H / 4, cr, W * H / 4, cudaMemcpyHostToDevice, s->cs));
+    // pageable sources: the copy may still read them after return
+    CUDA_OR(ctx, cudaStreamSynchronize(s->cs));
+    return H264R_OK;
+}
+
+static int check_device_error(h264r_ctx *ctx, cudaStream_t cs)
+{
+    CUDA_OR(ctx, cudaMemcpyAsync(ctx->h_error, ctx->d_error, sizeof(int), cudaMemcpyDeviceToHost, cs));
+    CUDA_OR(ctx, cudaStreamSynchronize(cs));
+    int e = *ctx->h_error;
+    if (e != 0) {
+        set_err(ctx, "device reported error %d (%s)", e, e == H264R_ERR_DEVICE_TIMEOUT ? "bounded wait expired" : "bad record");
+        cudaMemsetAsync(ctx->d_error, 0, sizeof(int), cs);
+        cudaStreamSynchronize(cs);
+        return e;
+    }
+    return H264R_OK;
+}
+
+extern "C" int h264r_stream_sync(h264r_stream *s)
+{
+    if (!s) return H264R_ERR_INVALID_ARG;
+    cudaSetDevice(s->ctx->device);
+    CUDA_OR(s->ctx, cudaStreamSynchronize(s->cs));
+    return check_device_error(s->ctx, s->cs);
+}
+
+extern "C" int h264r_ctx_sync(h264r_ctx *ctx)
+{
+    if (!ctx) return H264R_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    CUDA_OR(ctx, cudaDeviceSynchronize());
+    return check_device_error(ctx, ctx->batch_stream);
+}

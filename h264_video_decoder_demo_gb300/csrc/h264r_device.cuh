@@ -1,0 +1,577 @@
+// h264r_device.cuh — device-side building blocks of the reconstruction
+// engine: tables, record access, inverse transforms, interpolation, weighted
+// prediction, intra predictors, neighbour derivation and deblocking rules.
+//
+// Every function restates one process of the reference decoder
+// (jfu222/h264_video_decoder_demo, paths relative to its
+// h264_video_decoder_demo/ directory) bit for bit, including the places
+// where the reference departs from the H.264 text ("quirk").
+#pragma once
+
+#include <cstdint>
+#include "../../include/h264r.h"
+
+#define H264R_CLIP3(lo, hi, v) ((v) < (lo) ? (lo) : ((v) > (hi) ? (hi) : (v)))
+
+namespace h264r {
+
+__device__ __forceinline__ int clip1(int v) { return min(max(v, 0), 255); }
+
+// ---------------------------------------------------------------- tables
+// scan index -> raster index (row*4+col / row*8+col), Table 8-12/8-13
+// (H264PictureBase.cpp:4542, 4597)
+__device__ const uint8_t kZigzag4x4[16] = {0, 1, 4, 8, 5, 2, 3, 6, 9, 12, 13, 10, 7, 11, 14, 15};
+__device__ const uint8_t kField4x4[16] = {0, 4, 1, 8, 12, 5, 9, 13, 2, 6, 10, 14, 3, 7, 11, 15};
+__device__ const uint8_t kZigzag8x8[64] = {
+    0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5,
+    12, 19, 26, 33, 40, 48, 41, 34, 27, 20, 13, 6, 7, 14, 21, 28,
+    35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51,
+    58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63};
+__device__ const uint8_t kField8x8[64] = {
+    0, 8, 16, 1, 9, 24, 32, 17, 2, 25, 40, 48, 56, 33, 10, 3,
+    18, 41, 49, 57, 26, 11, 4, 19, 34, 42, 50, 58, 27, 12, 5, 20,
+    35, 43, 51, 59, 28, 13, 6, 21, 36, 44, 52, 60, 29, 14, 22, 37,
+    45, 53, 61, 30, 7, 15, 38, 46, 54, 62, 23, 31, 39, 47, 55, 63};
+// normAdjust (scaling_functions, H264PictureBase.cpp:4900-4951)
+__device__ const uint8_t kV4[6][3] = {{10, 16, 13}, {11, 18, 14}, {13, 20, 16}, {14, 23, 18}, {16, 25, 20}, {18, 29, 23}};
+__device__ const uint8_t kV8[6][6] = {{20, 18, 32, 19, 25, 24}, {22, 19, 35, 21, 28, 26}, {26, 23, 42, 24, 33, 31},
+                                      {28, 25, 45, 26, 35, 33}, {32, 28, 51, 30, 40, 38}, {36, 32, 58, 34, 46, 43}};
+// Table 8-15 (H264PictureBase.cpp:4773-4778)
+__device__ const uint8_t kQpc[52] = {
+    0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25,
+    26, 27, 28, 29, 29, 30, 31, 32, 32, 33, 34, 34, 35, 35, 36, 36, 37, 37, 37, 38, 38, 38, 39, 39, 39, 39};
+// Tables 8-16 / 8-17 (H264PictureDeblockingFilterProcess.cpp:1330-1409)
+__device__ const uint8_t kAlpha[52] = {
+    0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 4, 4, 5, 6, 7, 8, 9, 10, 12, 13,
+    15, 17, 20, 22, 25, 28, 32, 36, 40, 45, 50, 56, 63, 71, 80, 90, 101, 113, 127, 144, 162, 182, 203, 226, 255, 255};
+__device__ const uint8_t kBeta[52] = {
+    0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4,
+    6, 6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13, 14, 14, 15, 15, 16, 16, 17, 17, 18, 18};
+__device__ const uint8_t kTc0[3][52] = {
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1,
+     1, 1, 1, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 4, 4, 4, 5, 6, 6, 7, 8, 9, 10, 11, 13},
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1,
+     1, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 4, 4, 5, 5, 6, 7, 8, 8, 10, 11, 12, 13, 15, 17},
+    {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 1,
+     1, 2, 2, 2, 2, 3, 3, 3, 4, 4, 4, 5, 6, 6, 7, 8, 9, 10, 11, 13, 14, 16, 18, 20, 23, 25}};
+// luma4x4BlkIdx -> 4x4-block column / row (6.4.3)
+__device__ const uint8_t kBlkX[16] = {0, 1, 0, 1, 2, 3, 2, 3, 0, 1, 0, 1, 2, 3, 2, 3};
+__device__ const uint8_t kBlkY[16] = {0, 0, 1, 1, 0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 3, 3};
+
+// ---------------------------------------------------------------- picture
+// Device view of one picture of a batch (built by the host for every launch).
+struct PicDesc {
+    int wmb, hmb;            // frame size in MBs
+    int W, H, Wc, Hc;        // frame size in samples
+    int mbaff, deblock;
+    uint32_t num_mbs, num_slices, num_weights, num_pcm;
+    uint32_t motion_bytes, coef_bytes;
+    const h264r_mb *mbs;
+    const h264r_slice *slices;
+    const h264r_weight *weights;
+    const uint8_t *motion;
+    const uint8_t *coef;
+    const uint8_t *pcm;
+    const uint8_t *scaling;  // 96 bytes ScalingList4x4 then 384 bytes ScalingList8x8
+    uint8_t *dst;            // destination slot: Y, then Cb, then Cr
+    const uint8_t *dpb;      // slot 0 of the stream's DPB
+    uint64_t slot_bytes;
+    int nslots;
+    int flat_scaling;        // every scaling list is flat 16
+    uint8_t *bs;             // deblocking strengths, kBsBytes per MB
+    int *progress;           // per unit row progress counters (2 * units_h)
+    uint32_t mb_base;        // first global MB index of this picture in the batch
+    uint32_t row_base;       // first global unit row of this picture in the batch
+    uint32_t units_w, units_h;  // wavefront grid: MBs (or MB pairs) per row, rows
+    uint32_t deblock_stop;   // first failing bS derivation key (0xFFFFFFFF: none)
+};
+
+// Engine-wide device state for one launch.
+struct LaunchState {
+    int *error;              // first error code (0 ok)
+    unsigned int *ticket;    // wavefront row tickets [2]
+    unsigned long long spin_limit;
+};
+
+// bS table layout per MB (bytes): luma vertical 4 edges x 16 rows, luma
+// horizontal 4 edges x 16 cols, extra MBAFF top edge x 16, chroma vertical
+// 2 x 8, chroma horizontal 2 x 8, chroma extra top edge x 8.  A value of
+// 0xFF marks the place where the reference's bS derivation fails.
+constexpr int kBsLumaV = 0, kBsLumaH = 64, kBsLumaTop2 = 128, kBsChromaV = 144, kBsChromaH = 160,
+              kBsChromaTop2 = 176, kBsBytes = 192;
+
+__device__ __forceinline__ uint8_t *plane_y(const PicDesc &p) { return p.dst; }
+__device__ __forceinline__ uint8_t *plane_c(const PicDesc &p, int pl)
+{
+    return p.dst + (size_t)p.W * p.H + (size_t)pl * p.Wc * p.Hc;
+}
+
+// Inverse_macroblock_scanning_process (H264PictureBase.cpp:2503)
+__device__ __forceinline__ void mb_origin(const PicDesc &p, int addr, int &x, int &y, int &dy)
+{
+    if (!p.mbaff) {
+        x = (addr % p.wmb) * 16;
+        y = (addr / p.wmb) * 16;
+        dy = 1;
+    } else {
+        int pair = addr >> 1;
+        x = (pair % p.wmb) * 16;
+        int y0 = (pair / p.wmb) * 32;
+        if (p.mbs[addr].flags & H264R_MBF_FIELD) {
+            y = y0 + (addr & 1);
+            dy = 2;
+        } else {
+            y = y0 + (addr & 1) * 16;
+            dy = 1;
+        }
+    }
+}
+
+__device__ __forceinline__ int field_mb(const PicDesc &p, int addr)
+{
+    return p.mbaff && (p.mbs[addr].flags & H264R_MBF_FIELD);
+}
+
+__device__ __forceinline__ int chroma_row0(int y) { return (y >> 4) * 8 + (y & 1); }
+
+__device__ __forceinline__ int chroma_qp(int qpy, int offset) { return kQpc[H264R_CLIP3(0, 51, qpy + offset)]; }
+
+__device__ __forceinline__ bool is_intra_type(int t) { return t == H264R_MB_I4x4 || t == H264R_MB_I8x8 || t == H264R_MB_I16x16; }
+
+// ---------------------------------------------------------------- scaling
+__device__ __forceinline__ int scan_pos_of(const uint8_t *scan, int n, int raster)
+{
+    for (int k = 0; k < n; k++)
+        if (scan[k] == raster) return k;
+    return 0;
+}
+
+// LevelScale4x4(m, i, j) of scaling list `list` (8.5.9)
+__device__ __forceinline__ int level_scale4(const PicDesc &p, int list, int field, int m, int i, int j)
+{
+    int ws = 16;
+    if (!p.flat_scaling) ws = p.scaling[list * 16 + scan_pos_of(field ? kField4x4 : kZigzag4x4, 16, i * 4 + j)];
+    int v = ((i & 1) == 0 && (j & 1) == 0) ? kV4[m][0] : (((i & 1) && (j & 1)) ? kV4[m][1] : kV4[m][2]);
+    return ws * v;
+}
+
+__device__ __forceinline__ int level_scale8(const PicDesc &p, int list, int field, int m, int i, int j)
+{
+    int ws = 16;
+    if (!p.flat_scaling) ws = p.scaling[96 + list * 64 + scan_pos_of(field ? kField8x8 : kZigzag8x8, 64, i * 8 + j)];
+    int v;
+    if (i % 4 == 0 && j % 4 == 0) v = kV8[m][0];
+    else if (i % 2 == 1 && j % 2 == 1) v = kV8[m][1];
+    else if (i % 4 == 2 && j % 4 == 2) v = kV8[m][2];
+    else if ((i % 4 == 0 && j % 2 == 1) || (i % 2 == 1 && j % 4 == 0)) v = kV8[m][3];
+    else if ((i % 4 == 0 && j % 4 == 2) || (i % 4 == 2 && j % 4 == 0)) v = kV8[m][4];
+    else v = kV8[m][5];
+    return ws * v;
+}
+
+// ---------------------------------------------------------------- transforms
+// 8.5.12 on a 4x4 array already in raster order (Scaling_and_transformation_
+// process_for_residual_4x4_blocks, H264PictureBase.cpp:4106-4266)
+__device__ __forceinline__ void idct4x4(const PicDesc &p, int32_t c[16], int field, int qp, int ls_list, bool dc_pass,
+                                        int32_t r[16])
+{
+    int32_t d[16];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            int32_t v = c[i * 4 + j];
+            if (i == 0 && j == 0 && dc_pass) {
+                d[0] = v;
+            } else if (v == 0) {
+                d[i * 4 + j] = 0;
+            } else {
+                int ls = level_scale4(p, ls_list, field, qp % 6, i, j);
+                if (qp >= 24) d[i * 4 + j] = (v * ls) << (qp / 6 - 4);
+                else d[i * 4 + j] = (v * ls + (1 << (3 - qp / 6))) >> (4 - qp / 6);
+            }
+        }
+    int32_t f[16];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        int e0 = d[i * 4 + 0] + d[i * 4 + 2], e1 = d[i * 4 + 0] - d[i * 4 + 2];
+        int e2 = (d[i * 4 + 1] >> 1) - d[i * 4 + 3], e3 = d[i * 4 + 1] + (d[i * 4 + 3] >> 1);
+        f[i * 4 + 0] = e0 + e3; f[i * 4 + 1] = e1 + e2; f[i * 4 + 2] = e1 - e2; f[i * 4 + 3] = e0 - e3;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        int g0 = f[0 * 4 + j] + f[2 * 4 + j], g1 = f[0 * 4 + j] - f[2 * 4 + j];
+        int g2 = (f[1 * 4 + j] >> 1) - f[3 * 4 + j], g3 = f[1 * 4 + j] + (f[3 * 4 + j] >> 1);
+        r[0 * 4 + j] = (g0 + g3 + 32) >> 6;
+        r[1 * 4 + j] = (g1 + g2 + 32) >> 6;
+        r[2 * 4 + j] = (g1 - g2 + 32) >> 6;
+        r[3 * 4 + j] = (g0 - g3 + 32) >> 6;
+    }
+}
+
+// one 8-point pass of 8.5.13.2
+__device__ __forceinline__ void idct8_1d(int x0, int x1, int x2, int x3, int x4, int x5, int x6, int x7, int o[8])
+{
+    int e0 = x0 + x4;
+    int e1 = -x3 + x5 - x7 - (x7 >> 1);
+    int e2 = x0 - x4;
+    int e3 = x1 + x7 - x3 - (x3 >> 1);
+    int e4 = (x2 >> 1) - x6;
+    int e5 = -x1 + x7 + x5 + (x5 >> 1);
+    int e6 = x2 + (x6 >> 1);
+    int e7 = x3 + x5 + x1 + (x1 >> 1);
+    int f0 = e0 + e6, f1 = e1 + (e7 >> 2), f2 = e2 + e4, f3 = e3 + (e5 >> 2);
+    int f4 = e2 - e4, f5 = (e3 >> 2) - e5, f6 = e0 - e6, f7 = e7 - (e1 >> 2);
+    o[0] = f0 + f7; o[1] = f2 + f5; o[2] = f4 + f3; o[3] = f6 + f1;
+    o[4] = f6 - f1; o[5] = f4 - f3; o[6] = f2 - f5; o[7] = f0 - f7;
+}
+
+// 8.5.13 (H264PictureBase.cpp:4270-4403); c and r in raster order; in place allowed
+__device__ __forceinline__ void idct8x8(const PicDesc &p, int32_t *c, int field, int qp, int ls_list, int32_t *r)
+{
+    int32_t d[64];
+    for (int i = 0; i < 8; i++)
+        for (int j = 0; j < 8; j++) {
+            int32_t v = c[i * 8 + j];
+            if (v == 0) { d[i * 8 + j] = 0; continue; }
+            int ls = level_scale8(p, ls_list, field, qp % 6, i, j);
+            if (qp >= 36) d[i * 8 + j] = (v * ls) << (qp / 6 - 6);
+            else d[i * 8 + j] = (v * ls + (1 << (5 - qp / 6))) >> (6 - qp / 6);
+        }
+    int o[8];
+    for (int i = 0; i < 8; i++) {
+        idct8_1d(d[i * 8 + 0], d[i * 8 + 1], d[i * 8 + 2], d[i * 8 + 3], d[i * 8 + 4], d[i * 8 + 5], d[i * 8 + 6], d[i * 8 + 7], o);
+        for (int j = 0; j < 8; j++) d[i * 8 + j] = o[j];
+    }
+    for (int j = 0; j < 8; j++) {
+        idct8_1d(d[0 * 8 + j], d[1 * 8 + j], d[2 * 8 + j], d[3 * 8 + j], d[4 * 8 + j], d[5 * 8 + j], d[6 * 8 + j], d[7 * 8 + j], o);
+        for (int i = 0; i < 8; i++) r[i * 8 + j] = (o[i] + 32) >> 6;
+    }
+}
+
+// 8.5.10 Intra16x16 DC (H264PictureBase.cpp:4993-5088): c raster -> dcY raster
+__device__ __forceinline__ void luma_dc(const PicDesc &p, const int32_t c[16], int field, int qp, int32_t dcY[16])
+{
+    int32_t g[16];
+    for (int j = 0; j < 4; j++) {
+        g[0 * 4 + j] = c[0 * 4 + j] + c[1 * 4 + j] + c[2 * 4 + j] + c[3 * 4 + j];
+        g[1 * 4 + j] = c[0 * 4 + j] + c[1 * 4 + j] - c[2 * 4 + j] - c[3 * 4 + j];
+        g[2 * 4 + j] = c[0 * 4 + j] - c[1 * 4 + j] - c[2 * 4 + j] + c[3 * 4 + j];
+        g[3 * 4 + j] = c[0 * 4 + j] - c[1 * 4 + j] + c[2 * 4 + j] - c[3 * 4 + j];
+    }
+    int ls = level_scale4(p, 0, field, qp % 6, 0, 0);
+    for (int i = 0; i < 4; i++) {
+        int f0 = g[i * 4 + 0] + g[i * 4 + 1] + g[i * 4 + 2] + g[i * 4 + 3];
+        int f1 = g[i * 4 + 0] + g[i * 4 + 1] - g[i * 4 + 2] - g[i * 4 + 3];
+        int f2 = g[i * 4 + 0] - g[i * 4 + 1] - g[i * 4 + 2] + g[i * 4 + 3];
+        int f3 = g[i * 4 + 0] - g[i * 4 + 1] + g[i * 4 + 2] - g[i * 4 + 3];
+        int f[4] = {f0, f1, f2, f3};
+        for (int j = 0; j < 4; j++) {
+            if (qp >= 36) dcY[i * 4 + j] = (f[j] * ls) << (qp / 6 - 6);
+            else dcY[i * 4 + j] = (f[j] * ls + (1 << (5 - qp / 6))) >> (6 - qp / 6);
+        }
+    }
+}
+
+// 8.5.11 chroma DC 4:2:0 (H264PictureBase.cpp:3989-4044); quirk: the
+// LevelScale4x4 of the MB's luma list (0 intra / 3 inter) is used
+__device__ __forceinline__ void chroma_dc(const PicDesc &p, const int32_t lv[4], int field, int qpc, int ls_list, int32_t dcC[4])
+{
+    int e00 = lv[0] + lv[2], e01 = lv[1] + lv[3], e10 = lv[0] - lv[2], e11 = lv[1] - lv[3];
+    int f[4] = {e00 + e01, e00 - e01, e10 + e11, e10 - e11};
+    int ls = level_scale4(p, ls_list, field, qpc % 6, 0, 0);
+    for (int i = 0; i < 4; i++) dcC[i] = ((f[i] * ls) << (qpc / 6)) >> 5;
+}
+
+// ---------------------------------------------------------------- coefficients
+// Payload decode: the block list a lane owns.  Returns the number of
+// significance words of the block ahead of it.
+struct CoefView {
+    uint32_t mask;
+    const uint16_t *sig;
+    const int16_t *lv;
+    int t8;
+};
+
+__device__ __forceinline__ bool coef_view(const PicDesc &p, const h264r_mb &m, CoefView &v)
+{
+    v.mask = 0;
+    v.t8 = (m.flags & H264R_MBF_T8x8) != 0;
+    if (m.coef == H264R_NONE) return true;
+    if ((m.coef & 3) || (uint64_t)m.coef + 4 > p.coef_bytes) return false;
+    const uint8_t *base = p.coef + m.coef;
+    v.mask = *(const uint32_t *)base;
+    if (v.mask >> 27) return false;
+    int nw = __popc(v.mask) + (v.t8 ? 3 * __popc(v.mask & 15u) : 0);
+    v.sig = (const uint16_t *)(base + 4);
+    v.lv = (const int16_t *)(base + ((4 + 2 * nw + 3) & ~3));
+    return true;
+}
+
+// word index and level index of block bit b (all blocks before it)
+__device__ __forceinline__ void coef_block(const CoefView &v, int b, int &word, int &level)
+{
+    uint32_t before = v.mask & ((1u << b) - 1u);
+    word = __popc(before) + (v.t8 ? 3 * __popc(before & 15u) : 0);
+    level = 0;
+    for (int w = 0; w < word; w++) level += __popc((uint32_t)v.sig[w]);
+}
+
+// scan list of a 16-position block bit b into raster array c (zeroed first)
+__device__ __forceinline__ void coef_list16(const CoefView &v, int b, int field, int32_t c[16])
+{
+#pragma unroll
+    for (int i = 0; i < 16; i++) c[i] = 0;
+    if (!(v.mask & (1u << b))) return;
+    int w, l;
+    coef_block(v, b, w, l);
+    uint32_t s = v.sig[w];
+    const uint8_t *scan = field ? kField4x4 : kZigzag4x4;
+    while (s) {
+        int k = __ffs(s) - 1;
+        s &= s - 1;
+        c[scan[k]] = v.lv[l++];
+    }
+}
+
+// ---------------------------------------------------------------- motion
+// entry index covering 4x4 block (bx, by) for a motion payload shape
+__device__ __forceinline__ int part_of_block(uint32_t shape, int bx, int by)
+{
+    int mp = shape & 3;
+    if (mp == 0) return 0;
+    if (mp == 1) return by >> 1;
+    if (mp == 2) return bx >> 1;
+    int q = (by >> 1) * 2 + (bx >> 1), base = 0;
+    for (int i = 0; i < q; i++) {
+        int sc = (shape >> (2 + 2 * i)) & 3;
+        base += (sc == 0) ? 1 : (sc == 3 ? 4 : 2);
+    }
+    int sc = (shape >> (2 + 2 * q)) & 3, sx = bx & 1, sy = by & 1;
+    if (sc == 0) return base;
+    if (sc == 1) return base + sy;
+    if (sc == 2) return base + sx;
+    return base + sy * 2 + sx;
+}
+
+// ---------------------------------------------------------------- MC
+struct RefView {
+    const uint8_t *y, *cb, *cr;
+    int ystride, cstride, xmax, xmaxc;
+};
+
+// frame reference, or field of a frame for MBAFF field MBs; quirk: x is
+// clamped to the doubled field-view width (H264InterPrediction.cpp:2363)
+__device__ __forceinline__ RefView ref_view(const PicDesc &p, int ref)
+{
+    RefView r;
+    const uint8_t *base = p.dpb + (uint64_t)(ref & 31) * p.slot_bytes;
+    const uint8_t *cb = base + (size_t)p.W * p.H, *cr = cb + (size_t)p.Wc * p.Hc;
+    if (ref & H264R_REF_FIELD) {
+        int bot = (ref & H264R_REF_BOTTOM) ? 1 : 0;
+        r.y = base + bot * p.W;
+        r.cb = cb + bot * p.Wc;
+        r.cr = cr + bot * p.Wc;
+        r.ystride = 2 * p.W;
+        r.cstride = 2 * p.Wc;
+        r.xmax = 2 * p.W - 1;
+        r.xmaxc = 2 * p.Wc - 1;
+    } else {
+        r.y = base; r.cb = cb; r.cr = cr;
+        r.ystride = p.W; r.cstride = p.Wc;
+        r.xmax = p.W - 1; r.xmaxc = p.Wc - 1;
+    }
+    return r;
+}
+
+// 8.4.2.2.1 Luma_sample_interpolation_process (H264InterPrediction.cpp:2344-2480)
+__device__ __forceinline__ int luma_sample(const RefView &r, int ymax, int xi, int yi, int xf, int yf)
+{
+#define S(dx, dy) ((int)__ldg(r.y + (size_t)H264R_CLIP3(0, ymax, yi + (dy)) * r.ystride + H264R_CLIP3(0, r.xmax, xi + (dx))))
+#define TAP(a, b, c_, d, e, f) ((a) - 5 * (b) + 20 * (c_) + 20 * (d) - 5 * (e) + (f))
+    int G = S(0, 0);
+    if ((xf | yf) == 0) return G;
+    if (yf == 0) {  // a, b, c
+        int b = clip1((TAP(S(-2, 0), S(-1, 0), G, S(1, 0), S(2, 0), S(3, 0)) + 16) >> 5);
+        if (xf == 2) return b;
+        return xf == 1 ? (G + b + 1) >> 1 : (S(1, 0) + b + 1) >> 1;
+    }
+    if (xf == 0) {  // d, h, n
+        int h = clip1((TAP(S(0, -2), S(0, -1), G, S(0, 1), S(0, 2), S(0, 3)) + 16) >> 5);
+        if (yf == 2) return h;
+        return yf == 1 ? (G + h + 1) >> 1 : (S(0, 1) + h + 1) >> 1;
+    }
+    if (xf == 2 || yf == 2) {  // f, i, j, k, q
+        int cc = TAP(S(-2, -2), S(-2, -1), S(-2, 0), S(-2, 1), S(-2, 2), S(-2, 3));
+        int dd = TAP(S(-1, -2), S(-1, -1), S(-1, 0), S(-1, 1), S(-1, 2), S(-1, 3));
+        int h1 = TAP(S(0, -2), S(0, -1), G, S(0, 1), S(0, 2), S(0, 3));
+        int m1 = TAP(S(1, -2), S(1, -1), S(1, 0), S(1, 1), S(1, 2), S(1, 3));
+        int ee = TAP(S(2, -2), S(2, -1), S(2, 0), S(2, 1), S(2, 2), S(2, 3));
+        int ff = TAP(S(3, -2), S(3, -1), S(3, 0), S(3, 1), S(3, 2), S(3, 3));
+        int j = clip1((TAP(cc, dd, h1, m1, ee, ff) + 512) >> 10);
+        if (xf == 2 && yf == 2) return j;
+        if (xf == 2) {  // f (yf 1) / q (yf 3)
+            int row = yf == 1 ? 0 : 1;
+            int b = clip1((TAP(S(-2, row), S(-1, row), S(0, row), S(1, row), S(2, row), S(3, row)) + 16) >> 5);
+            return (b + j + 1) >> 1;
+        }
+        // i (xf 1) / k (xf 3)
+        int hh = clip1(((xf == 1 ? h1 : m1) + 16) >> 5);
+        return (hh + j + 1) >> 1;
+    }
+    // e, g, p, r: average of a horizontal and a vertical half sample
+    int row = yf == 1 ? 0 : 1, col = xf == 1 ? 0 : 1;
+    int b = clip1((TAP(S(-2, row), S(-1, row), S(0, row), S(1, row), S(2, row), S(3, row)) + 16) >> 5);
+    int h = clip1((TAP(S(col, -2), S(col, -1), S(col, 0), S(col, 1), S(col, 2), S(col, 3)) + 16) >> 5);
+    return (b + h + 1) >> 1;
+#undef S
+#undef TAP
+}
+
+// 8.4.2.2.2 (H264InterPrediction.cpp:2485-2522)
+__device__ __forceinline__ int chroma_sample(const uint8_t *pl, int stride, int xmax, int ymax, int xi, int yi, int xf, int yf)
+{
+    int xa = H264R_CLIP3(0, xmax, xi), xb = H264R_CLIP3(0, xmax, xi + 1);
+    int ya = H264R_CLIP3(0, ymax, yi), yb = H264R_CLIP3(0, ymax, yi + 1);
+    int A = __ldg(pl + (size_t)ya * stride + xa), B = __ldg(pl + (size_t)ya * stride + xb);
+    int C = __ldg(pl + (size_t)yb * stride + xa), D = __ldg(pl + (size_t)yb * stride + xb);
+    return ((8 - xf) * (8 - yf) * A + xf * (8 - yf) * B + (8 - xf) * yf * C + xf * yf * D + 32) >> 6;
+}
+
+// 8.4.2.3 (H264InterPrediction.cpp:2526-2829); quirk: explicit weights with
+// only list 1 in use apply w0/o0 to luma
+__device__ __forceinline__ int weigh(const h264r_weight &w, int comp, bool use0, bool use1, int p0, int p1)
+{
+    if (!use0 && !use1) return 0;
+    if (!w.weighted) {
+        if (use0 && use1) return (p0 + p1 + 1) >> 1;
+        return use0 ? p0 : p1;
+    }
+    int lw = w.log_wd[comp];
+    if (use0 && use1)
+        return clip1(((p0 * w.w0[comp] + p1 * w.w1[comp] + (1 << lw)) >> (lw + 1)) + ((w.o0[comp] + w.o1[comp] + 1) >> 1));
+    int pv = use0 ? p0 : p1;
+    int ww, oo;
+    if (use0 || comp == 0) { ww = w.w0[comp]; oo = w.o0[comp]; }
+    else { ww = w.w1[comp]; oo = w.o1[comp]; }
+    if (lw >= 1) return clip1(((pv * ww + (1 << (lw - 1))) >> lw) + oo);
+    return clip1(pv * ww + oo);
+}
+
+// ---------------------------------------------------------------- neighbours
+__device__ __forceinline__ bool avail_mb(const PicDesc &p, int cur, int n)
+{
+    return n >= 0 && n <= cur && p.mbs[n].slice == p.mbs[cur].slice;
+}
+
+// 6.4.12.1 (getMbAddrN_non_MBAFF_frames, H264PictureBase.cpp:2878)
+__device__ __forceinline__ int nb_loc_frame(const PicDesc &p, int cur, int xN, int yN, int maxW, int maxH, int &xW, int &yW)
+{
+    int W = p.wmb, n;
+    if (xN < 0 && yN < 0) n = (cur % W == 0) ? -1 : cur - W - 1;
+    else if (xN < 0 && yN < maxH) n = (cur % W == 0) ? -1 : cur - 1;
+    else if (xN < maxW && yN < 0) n = cur - W;
+    else if (xN < maxW && yN < maxH) n = cur;
+    else if (xN >= maxW && yN < 0) n = ((cur + 1) % W == 0) ? -1 : cur - W + 1;
+    else return -1;
+    if (n != cur && !avail_mb(p, cur, n)) return -1;
+    xW = (xN + maxW) % maxW;
+    yW = (yN + maxH) % maxH;
+    return n;
+}
+
+// 6.4.12.2, Table 6-4 (getMbAddrN_MBAFF_frames, H264PictureBase.cpp:2984-3395)
+__device__ inline int nb_loc_mbaff(const PicDesc &p, int cur, int xN, int yN, int maxW, int maxH, int &xW, int &yW)
+{
+    const int W = p.wmb, pair = cur / 2;
+    const h264r_mb *mbs = p.mbs;
+    int A = 2 * (pair - 1), B = 2 * (pair - W), C = 2 * (pair - W + 1), D = 2 * (pair - W - 1);
+    const int sl = mbs[cur].slice;
+    if (A < 0 || A > cur || mbs[A].slice != sl || pair % W == 0) A = -2;
+    if (B < 0 || B > cur || mbs[B].slice != sl) B = -2;
+    if (C < 0 || C > cur || mbs[C].slice != sl || (pair + 1) % W == 0) C = -2;
+    if (D < 0 || D > cur || mbs[D].slice != sl || pair % W == 0) D = -2;
+#define FRM(a) (!(mbs[a].flags & H264R_MBF_FIELD))
+    const bool frame = FRM(cur), top = (cur % 2) == 0;
+    int n = -1, yM = 0;
+    if (xN < 0 && yN < 0) {
+        if (frame) {
+            if (top) { n = D + 1; yM = yN; }
+            else if (A >= 0) {
+                if (FRM(A)) { n = A; yM = yN; } else { n = A + 1; yM = (yN + maxH) >> 1; }
+            }
+        } else {
+            if (top) {
+                if (D >= 0) { if (FRM(D)) { n = D + 1; yM = 2 * yN; } else { n = D; yM = yN; } }
+            } else { n = D + 1; yM = yN; }
+        }
+    } else if (xN < 0 && yN < maxH) {
+        if (A >= 0) {
+            if (frame) {
+                if (top) {
+                    if (FRM(A)) { n = A; yM = yN; } else { n = (yN % 2 == 0) ? A : A + 1; yM = yN >> 1; }
+                } else {
+                    if (FRM(A)) { n = A + 1; yM = yN; } else { n = (yN % 2 == 0) ? A : A + 1; yM = (yN + maxH) >> 1; }
+                }
+            } else {
+                if (top) {
+                    if (FRM(A)) {
+                        if (yN < maxH / 2) { n = A; yM = yN << 1; } else { n = A + 1; yM = (yN << 1) - maxH; }
+                    } else { n = A; yM = yN; }
+                } else {
+                    if (FRM(A)) {
+                        if (yN < maxH / 2) { n = A; yM = (yN << 1) + 1; } else { n = A + 1; yM = (yN << 1) + 1 - maxH; }
+                    } else { n = A + 1; yM = yN; }
+                }
+            }
+        }
+    } else if (xN < maxW && yN < 0) {
+        if (frame) {
+            if (top) { n = B + 1; yM = yN; } else { n = cur - 1; yM = yN; }
+        } else {
+            if (top) {
+                if (B >= 0) { if (FRM(B)) { n = B + 1; yM = 2 * yN; } else { n = B; yM = yN; } }
+            } else { n = B + 1; yM = yN; }
+        }
+    } else if (xN < maxW && yN < maxH) {
+        n = cur; yM = yN;
+    } else if (xN >= maxW && yN < 0) {
+        if (frame) {
+            if (top) { n = C + 1; yM = yN; } else n = -1;
+        } else {
+            if (top) {
+                if (C >= 0) { if (FRM(C)) { n = C + 1; yM = 2 * yN; } else { n = C; yM = yN; } }
+            } else { n = C + 1; yM = yN; }
+        }
+    }
+#undef FRM
+    if (n < 0) return -1;
+    xW = (xN + maxW) % maxW;
+    yW = (yM + maxH) % maxH;
+    return n;
+}
+
+__device__ __forceinline__ int nb_loc(const PicDesc &p, int cur, int xN, int yN, int maxW, int maxH, int &xW, int &yW)
+{
+    if (!p.mbaff) return nb_loc_frame(p, cur, xN, yN, maxW, maxH, xW, yW);
+    return nb_loc_mbaff(p, cur, xN, yN, maxW, maxH, xW, yW);
+}
+
+// Address of neighbouring constructed sample p[xN, yN] of MB cur, or null
+// when it is "not available for Intra prediction" (mbAddrN unavailable, or
+// an inter MB under constrained_intra_pred_flag).
+__device__ __forceinline__ const uint8_t *intra_nb_ptr(const PicDesc &p, int cur, int isChroma, int pl, int xN, int yN)
+{
+    int maxW = isChroma ? 8 : 16;
+    int xW, yW;
+    int n = nb_loc(p, cur, xN, yN, maxW, maxW, xW, yW);
+    if (n < 0) return nullptr;
+    const h264r_mb &mn = p.mbs[n];
+    if (n != cur && mn.type == H264R_MB_INTER && (mn.flags & H264R_MBF_CIP)) return nullptr;
+    int x, y, dy;
+    mb_origin(p, n, x, y, dy);
+    if (!isChroma) return plane_y(p) + (size_t)(y + dy * yW) * p.W + x + xW;
+    return plane_c(p, pl) + (size_t)(chroma_row0(y) + dy * yW) * p.Wc + x / 2 + xW;
+}
+
+}  // namespace h264r

@@ -1,0 +1,1075 @@
+// h264r_kernels.cu — the reconstruction kernels (sm_103a).
+//
+//  k_inter     inter MBs (8.4 MC + 8.4.2.3 weighting + 8.5 residual), I_PCM
+//              and undecoded MBs; fully parallel over the MBs of a batch.
+//  k_intra     intra MBs (8.3 + 8.5) as an anti-diagonal wavefront: one warp
+//              per MB row (MB-pair row for MBAFF), each row trailing the row
+//              above by two units (the top-right neighbour).
+//  k_bs        8.7.2.1 boundary strengths of every edge sample row, fully
+//              parallel (bS depends on records only, not on samples).
+//  k_deblock   8.7 filtering in the reference's raster order as a wavefront
+//              (each MB's top edge filter needs the MB above-right done).
+//
+// Cross-row waits spin on per-row progress counters with an iteration
+// limit; on expiry the kernel records H264R_ERR_DEVICE_TIMEOUT and returns.
+#include "h264r_device.cuh"
+
+namespace h264r {
+
+// ------------------------------------------------------------ batch lookup
+__device__ __forceinline__ int find_pic_by_mb(const PicDesc *pics, int npics, uint32_t g)
+{
+    int lo = 0, hi = npics - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pics[mid].mb_base <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int find_pic_by_row(const PicDesc *pics, int npics, uint32_t g)
+{
+    int lo = 0, hi = npics - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pics[mid].row_base <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void set_error(const LaunchState &st, int code) { atomicCAS(st.error, 0, code); }
+
+__device__ __forceinline__ int ld_acquire(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Wait (whole warp) until *flag >= target.  Returns false on timeout or when
+// another block reported an error.
+__device__ bool wait_progress(const LaunchState &st, const int *flag, int target)
+{
+    bool ok = true;
+    if ((threadIdx.x & 31) == 0) {
+        unsigned long long n = 0;
+        while (ld_acquire(flag) < target) {
+            if (*(volatile int *)st.error != 0) { ok = false; break; }
+            if (++n > st.spin_limit) {
+                set_error(st, H264R_ERR_DEVICE_TIMEOUT);
+                ok = false;
+                break;
+            }
+            __nanosleep(64);
+        }
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __syncwarp();
+    return ok;
+}
+
+// ======================================================================
+// K1: inter macroblocks, I_PCM, undecoded macroblocks
+// ======================================================================
+__global__ void __launch_bounds__(256) k_inter(const PicDesc *__restrict__ pics, int npics, LaunchState st)
+{
+    __shared__ PicDesc sp;
+    __shared__ h264r_mb sm;
+    __shared__ int32_t res[384];
+    __shared__ __align__(16) uint8_t out[384];
+    __shared__ uint32_t s_shape, s_count;
+    const int t = threadIdx.x;
+    const uint32_t g = blockIdx.x;
+    if (t == 0) {
+        int pi = find_pic_by_mb(pics, npics, g);
+        sp = pics[pi];
+    }
+    __syncthreads();
+    const PicDesc &p = sp;
+    const int addr = (int)(g - p.mb_base);
+    if (addr >= (int)p.num_mbs) return;
+    if (t == 0) sm = p.mbs[addr];
+    __syncthreads();
+    const h264r_mb m = sm;
+    if (m.type != H264R_MB_INTER && m.type != H264R_MB_IPCM && m.type != H264R_MB_NONE) return;
+    int x, y, dy;
+    mb_origin(p, addr, x, y, dy);
+    const int field = field_mb(p, addr);
+
+    if (m.type == H264R_MB_NONE) {
+        for (int i = t; i < 384; i += 256) out[i] = 0;
+    } else if (m.type == H264R_MB_IPCM) {
+        if (m.aux >= p.num_pcm) { if (t == 0) set_error(st, H264R_ERR_BAD_RECORD); return; }
+        const uint8_t *s = p.pcm + (size_t)m.aux * 384;
+        for (int i = t; i < 384; i += 256) out[i] = s[i];
+    } else {
+        // ---- prediction
+        if (t == 0) {
+            bool bad = (m.aux & 3) || (uint64_t)m.aux + 4 > p.motion_bytes;
+            uint32_t hdr = bad ? 0 : *(const uint32_t *)(p.motion + m.aux);
+            s_shape = hdr & 0xFFFF;
+            s_count = hdr >> 16;
+            if (bad || (uint64_t)m.aux + 4 + 16ull * s_count > p.motion_bytes) {
+                set_error(st, H264R_ERR_BAD_RECORD);
+                s_count = 0;
+            }
+        }
+        for (int i = t; i < 384; i += 256) res[i] = 0;
+        __syncthreads();
+        if (s_count == 0) return;
+        const h264r_part *parts = (const h264r_part *)(p.motion + m.aux + 4);
+        const int bottom_mb = p.mbaff ? (addr & 1) : 0;
+        const int yAL0 = field ? (y - (y & 1)) / 2 : y;
+        const int ymax = field ? p.H / 2 - 1 : p.H - 1;
+        const int ymaxc = field ? p.Hc / 2 - 1 : p.Hc - 1;
+        {
+            // luma sample t
+            const int lx = t & 15, ly = t >> 4;
+            int e = part_of_block(s_shape, lx >> 2, ly >> 2);
+            if (e >= (int)s_count) e = 0;
+            const h264r_part pp = parts[e];
+            const h264r_weight w = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
+            int v[2] = {0, 0};
+            bool use[2] = {pp.ref[0] >= 0, pp.ref[1] >= 0};
+#pragma unroll
+            for (int l = 0; l < 2; l++) {
+                if (!use[l]) continue;
+                RefView rv = ref_view(p, pp.ref[l]);
+                int mvx = pp.mv[l][0], mvy = pp.mv[l][1];
+                v[l] = luma_sample(rv, ymax, x + lx + (mvx >> 2), yAL0 + ly + (mvy >> 2), mvx & 3, mvy & 3);
+            }
+            out[t] = (uint8_t)weigh(w, 0, use[0], use[1], v[0], v[1]);
+        }
+        if (t < 128) {
+            // chroma sample: plane t>>6, row (t&63)>>3, col t&7
+            const int pl = t >> 6, cy = (t & 63) >> 3, cx = t & 7;
+            int e = part_of_block(s_shape, cx >> 1, cy >> 1);
+            if (e >= (int)s_count) e = 0;
+            const h264r_part pp = parts[e];
+            const h264r_weight w = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
+            int v[2] = {0, 0};
+            bool use[2] = {pp.ref[0] >= 0, pp.ref[1] >= 0};
+#pragma unroll
+            for (int l = 0; l < 2; l++) {
+                if (!use[l]) continue;
+                RefView rv = ref_view(p, pp.ref[l]);
+                int mvx = pp.mv[l][0], mvy = pp.mv[l][1];
+                if (field) {  // Table 8-10 (H264InterPrediction.cpp:2006-2047)
+                    int refbot = (pp.ref[l] & H264R_REF_BOTTOM) ? 1 : 0;
+                    if (!refbot && bottom_mb) mvy += 2;
+                    else if (refbot && !bottom_mb) mvy -= 2;
+                }
+                const uint8_t *plane = pl ? rv.cr : rv.cb;
+                v[l] = chroma_sample(plane, rv.cstride, rv.xmaxc, ymaxc, x / 2 + cx + (mvx >> 3), yAL0 / 2 + cy + (mvy >> 3),
+                                     mvx & 7, mvy & 7);
+            }
+            out[256 + t] = (uint8_t)weigh(w, 1 + pl, use[0], use[1], v[0], v[1]);
+        }
+        // ---- residual (H264InterPrediction.cpp:22-407)
+        if (m.coef != H264R_NONE) {
+            CoefView cv;
+            if (!coef_view(p, m, cv)) {
+                if (t == 0) set_error(st, H264R_ERR_BAD_RECORD);
+            } else if (cv.t8) {
+                if (t < 4 && (cv.mask & (1u << t))) {
+                    int32_t c[64];
+                    for (int i = 0; i < 64; i++) c[i] = 0;
+                    int w, l;
+                    coef_block(cv, t, w, l);
+                    const uint8_t *scan = field ? kField8x8 : kZigzag8x8;
+                    for (int q = 0; q < 4; q++) {
+                        uint32_t s = cv.sig[w + q];
+                        while (s) {
+                            int k = __ffs(s) - 1;
+                            s &= s - 1;
+                            c[scan[16 * q + k]] = cv.lv[l++];
+                        }
+                    }
+                    idct8x8(p, c, field, m.qpy, 1, c);
+                    int bx = (t & 1) * 8, by = (t >> 1) * 8;
+                    for (int i = 0; i < 8; i++)
+                        for (int j = 0; j < 8; j++) res[(by + i) * 16 + bx + j] = c[i * 8 + j];
+                }
+            } else if (t < 16) {
+                if (cv.mask & (1u << t)) {
+                    int32_t c[16], r[16];
+                    coef_list16(cv, t, field, c);
+                    idct4x4(p, c, field, m.qpy, 3, false, r);
+                    int bx = kBlkX[t] * 4, by = kBlkY[t] * 4;
+                    for (int i = 0; i < 4; i++)
+                        for (int j = 0; j < 4; j++) res[(by + i) * 16 + bx + j] = r[i * 4 + j];
+                }
+            }
+            if (t >= 32 && t < 40 && cv.mask != 0) {
+                // chroma block: plane pl, block b
+                const int pl = (t - 32) >> 2, b = (t - 32) & 3;
+                const int qpc = chroma_qp(m.qpy, p.slices[m.slice].chroma_qp_offset[pl]);
+                int32_t dcl[16], dc4[4], dcC[4];
+                coef_list16(cv, 17 + pl, 0, dcl);  // DC list: positions 0..3 in zig-zag order map to raster 0,1,4,8
+                dc4[0] = dcl[0]; dc4[1] = dcl[1]; dc4[2] = dcl[4]; dc4[3] = dcl[8];
+                chroma_dc(p, dc4, field, qpc, 3, dcC);
+                int32_t c[16], r[16];
+                coef_list16(cv, (pl ? H264R_CM_CR_AC0 : H264R_CM_CB_AC0) + b, field, c);
+                c[0] = dcC[b];
+                idct4x4(p, c, field, qpc, 3, true, r);
+                int bx = (b & 1) * 4, by = (b >> 1) * 4;
+                for (int i = 0; i < 4; i++)
+                    for (int j = 0; j < 4; j++) res[256 + pl * 64 + (by + i) * 8 + bx + j] = r[i * 4 + j];
+            }
+        }
+        __syncthreads();
+        out[t] = (uint8_t)clip1(out[t] + res[t]);
+        if (t < 128) out[256 + t] = (uint8_t)clip1(out[256 + t] + res[256 + t]);
+    }
+    __syncthreads();
+    // ---- store: 16 luma rows of 16 bytes, 2 x 8 chroma rows of 8 bytes
+    if (t < 16) {
+        uint4 v = *(const uint4 *)(out + t * 16);
+        *(uint4 *)(plane_y(p) + (size_t)(y + t * dy) * p.W + x) = v;
+    } else if (t < 32) {
+        const int pl = (t - 16) >> 3, r = (t - 16) & 7;
+        uint2 v = *(const uint2 *)(out + 256 + pl * 64 + r * 8);
+        *(uint2 *)(plane_c(p, pl) + (size_t)(chroma_row0(y) + r * dy) * p.Wc + x / 2) = v;
+    }
+}
+
+// ======================================================================
+// K2: intra macroblocks, wavefront
+// ======================================================================
+struct IntraSmem {
+    int32_t res[384];     // residual: luma raster 16x16, Cb 8x8, Cr 8x8
+    int32_t dc[16];       // Intra16x16 DC
+    int nb[40];           // neighbouring samples (-1: not available)
+    int nbf[40];          // filtered (8x8) neighbours
+};
+
+// 4x4 prediction sample (x, y) from nb = {p[-1,-1], p[-1,0..3], p[0..7,-1]}
+// (Intra_4x4_sample_prediction, H264PictureBase.cpp:1062-1419); returns -1
+// when the mode's samples are not available (prediction not written).
+__device__ int pred4x4_sample(int mode, const int *nb, int x, int y)
+{
+#define L(i) nb[1 + (i)]
+#define T(i) nb[5 + (i)]
+#define C nb[0]
+    bool top = T(0) >= 0 && T(1) >= 0 && T(2) >= 0 && T(3) >= 0;
+    bool top8 = top && T(4) >= 0 && T(5) >= 0 && T(6) >= 0 && T(7) >= 0;
+    bool left = L(0) >= 0 && L(1) >= 0 && L(2) >= 0 && L(3) >= 0;
+    bool corner = C >= 0;
+    auto pt = [&](int xx, int yy) -> int { return yy < 0 ? (xx < 0 ? C : T(xx)) : L(yy); };
+    switch (mode) {
+    case 0: return top ? T(x) : -1;
+    case 1: return left ? L(y) : -1;
+    case 2:
+        if (top && left) return (T(0) + T(1) + T(2) + T(3) + L(0) + L(1) + L(2) + L(3) + 4) >> 3;
+        if (left) return (L(0) + L(1) + L(2) + L(3) + 2) >> 2;
+        if (top) return (T(0) + T(1) + T(2) + T(3) + 2) >> 2;
+        return 128;
+    case 3:
+        if (!top8) return -1;
+        if (x == 3 && y == 3) return (T(6) + 3 * T(7) + 2) >> 2;
+        return (T(x + y) + 2 * T(x + y + 1) + T(x + y + 2) + 2) >> 2;
+    case 4:
+        if (!(top && left && corner)) return -1;
+        if (x > y) return (pt(x - y - 2, -1) + 2 * pt(x - y - 1, -1) + pt(x - y, -1) + 2) >> 2;
+        if (x < y) return (pt(-1, y - x - 2) + 2 * pt(-1, y - x - 1) + pt(-1, y - x) + 2) >> 2;
+        return (T(0) + 2 * C + L(0) + 2) >> 2;
+    case 5: {
+        if (!(top && left && corner)) return -1;
+        int z = 2 * x - y;
+        if (z >= 0 && (z & 1) == 0) return (pt(x - (y >> 1) - 1, -1) + pt(x - (y >> 1), -1) + 1) >> 1;
+        if (z >= 0) return (pt(x - (y >> 1) - 2, -1) + 2 * pt(x - (y >> 1) - 1, -1) + pt(x - (y >> 1), -1) + 2) >> 2;
+        if (z == -1) return (L(0) + 2 * C + T(0) + 2) >> 2;
+        return (pt(-1, y - 1) + 2 * pt(-1, y - 2) + pt(-1, y - 3) + 2) >> 2;
+    }
+    case 6: {
+        if (!(top && left && corner)) return -1;
+        int z = 2 * y - x;
+        if (z >= 0 && (z & 1) == 0) return (pt(-1, y - (x >> 1) - 1) + pt(-1, y - (x >> 1)) + 1) >> 1;
+        if (z >= 0) return (pt(-1, y - (x >> 1) - 2) + 2 * pt(-1, y - (x >> 1) - 1) + pt(-1, y - (x >> 1)) + 2) >> 2;
+        if (z == -1) return (L(0) + 2 * C + T(0) + 2) >> 2;
+        return (pt(x - 1, -1) + 2 * pt(x - 2, -1) + pt(x - 3, -1) + 2) >> 2;
+    }
+    case 7:
+        if (!top8) return -1;
+        if ((y & 1) == 0) return (T(x + (y >> 1)) + T(x + (y >> 1) + 1) + 1) >> 1;
+        return (T(x + (y >> 1)) + 2 * T(x + (y >> 1) + 1) + T(x + (y >> 1) + 2) + 2) >> 2;
+    case 8: {
+        if (!left) return -1;
+        int z = x + 2 * y;
+        if (z <= 4 && (z & 1) == 0) return (L(y + (x >> 1)) + L(y + (x >> 1) + 1) + 1) >> 1;
+        if (z < 5) return (L(y + (x >> 1)) + 2 * L(y + (x >> 1) + 1) + L(y + (x >> 1) + 2) + 2) >> 2;
+        if (z == 5) return (L(2) + 3 * L(3) + 2) >> 2;
+        return L(3);
+    }
+    }
+    return -1;
+#undef L
+#undef T
+#undef C
+}
+
+// 8x8 prediction sample from filtered nb = {p'[-1,-1], p'[-1,0..7], p'[0..15,-1]}
+// (Intra_8x8_sample_prediction, H264PictureBase.cpp:1600-1846)
+__device__ int pred8x8_sample(int mode, const int *nb, int x, int y)
+{
+#define L(i) nb[1 + (i)]
+#define T(i) nb[9 + (i)]
+#define C nb[0]
+    bool top = true, topr = true, left = true;
+    for (int i = 0; i < 8; i++) { top = top && T(i) >= 0; left = left && L(i) >= 0; }
+    topr = top;
+    for (int i = 8; i < 16; i++) topr = topr && T(i) >= 0;
+    bool corner = C >= 0;
+    auto pt = [&](int xx, int yy) -> int { return yy < 0 ? (xx < 0 ? C : T(xx)) : L(yy); };
+    switch (mode) {
+    case 0: return top ? T(x) : -1;
+    case 1: return left ? L(y) : -1;
+    case 2: {
+        int st = 0, sl = 0;
+        for (int i = 0; i < 8; i++) { st += top ? T(i) : 0; sl += left ? L(i) : 0; }
+        if (top && left) return (st + sl + 8) >> 4;
+        if (left) return (sl + 4) >> 3;
+        if (top) return (st + 4) >> 3;
+        return 128;
+    }
+    case 3:
+        if (!topr) return -1;
+        if (x == 7 && y == 7) return (T(14) + 3 * T(15) + 2) >> 2;
+        return (T(x + y) + 2 * T(x + y + 1) + T(x + y + 2) + 2) >> 2;
+    case 4:
+        if (!(top && left && corner)) return -1;
+        if (x > y) return (pt(x - y - 2, -1) + 2 * pt(x - y - 1, -1) + pt(x - y, -1) + 2) >> 2;
+        if (x < y) return (pt(-1, y - x - 2) + 2 * pt(-1, y - x - 1) + pt(-1, y - x) + 2) >> 2;
+        return (T(0) + 2 * C + L(0) + 2) >> 2;
+    case 5: {
+        if (!(top && left && corner)) return -1;
+        int z = 2 * x - y;
+        if (z >= 0 && (z & 1) == 0) return (pt(x - (y >> 1) - 1, -1) + pt(x - (y >> 1), -1) + 1) >> 1;
+        if (z >= 0) return (pt(x - (y >> 1) - 2, -1) + 2 * pt(x - (y >> 1) - 1, -1) + pt(x - (y >> 1), -1) + 2) >> 2;
+        if (z == -1) return (L(0) + 2 * C + T(0) + 2) >> 2;
+        return (pt(-1, y - 2 * x - 1) + 2 * pt(-1, y - 2 * x - 2) + pt(-1, y - 2 * x - 3) + 2) >> 2;
+    }
+    case 6: {
+        if (!(top && left && corner)) return -1;
+        int z = 2 * y - x;
+        if (z >= 0 && (z & 1) == 0) return (pt(-1, y - (x >> 1) - 1) + pt(-1, y - (x >> 1)) + 1) >> 1;
+        if (z >= 0) return (pt(-1, y - (x >> 1) - 2) + 2 * pt(-1, y - (x >> 1) - 1) + pt(-1, y - (x >> 1)) + 2) >> 2;
+        if (z == -1) return (L(0) + 2 * C + T(0) + 2) >> 2;
+        return (pt(x - 2 * y - 1, -1) + 2 * pt(x - 2 * y - 2, -1) + pt(x - 2 * y - 3, -1) + 2) >> 2;
+    }
+    case 7:
+        if (!topr) return -1;
+        if ((y & 1) == 0) return (T(x + (y >> 1)) + T(x + (y >> 1) + 1) + 1) >> 1;
+        return (T(x + (y >> 1)) + 2 * T(x + (y >> 1) + 1) + T(x + (y >> 1) + 2) + 2) >> 2;
+    case 8: {
+        if (!left) return -1;
+        int z = x + 2 * y;
+        if (z <= 12 && (z & 1) == 0) return (L(y + (x >> 1)) + L(y + (x >> 1) + 1) + 1) >> 1;
+        if (z < 13) return (L(y + (x >> 1)) + 2 * L(y + (x >> 1) + 1) + L(y + (x >> 1) + 2) + 2) >> 2;
+        if (z == 13) return (L(6) + 3 * L(7) + 2) >> 2;
+        return L(7);
+    }
+    }
+    return -1;
+#undef L
+#undef T
+#undef C
+}
+
+__device__ __forceinline__ int ldcg_u8(const uint8_t *ptr) { return (int)__ldcg(ptr); }
+
+// Reconstruct one intra MB with one warp (lane = threadIdx.x & 31).
+__device__ void intra_mb(const PicDesc &p, int addr, IntraSmem &s, const LaunchState &st)
+{
+    const int lane = threadIdx.x & 31;
+    const h264r_mb m = p.mbs[addr];
+    int x, y, dy;
+    mb_origin(p, addr, x, y, dy);
+    const int field = field_mb(p, addr);
+    const int qp = m.qpy;
+    uint8_t *Y = plane_y(p);
+    // ---- residuals
+    for (int i = lane; i < 384; i += 32) s.res[i] = 0;
+    CoefView cv;
+    if (!coef_view(p, m, cv)) {
+        if (lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
+        cv.mask = 0;
+    }
+    __syncwarp();
+    if (m.type == H264R_MB_I16x16) {
+        if (lane == 0) {
+            int32_t c[16];
+            coef_list16(cv, 16, field, c);
+            luma_dc(p, c, field, qp, s.dc);
+        }
+        __syncwarp();
+    }
+    if (m.type == H264R_MB_I8x8) {
+        if (lane < 4 && (cv.mask & (1u << lane))) {
+            int32_t c[64];
+            for (int i = 0; i < 64; i++) c[i] = 0;
+            int w, l;
+            coef_block(cv, lane, w, l);
+            const uint8_t *scan = field ? kField8x8 : kZigzag8x8;
+            for (int q = 0; q < 4; q++) {
+                uint32_t sg = cv.sig[w + q];
+                while (sg) {
+                    int k = __ffs(sg) - 1;
+                    sg &= sg - 1;
+                    c[scan[16 * q + k]] = cv.lv[l++];
+                }
+            }
+            idct8x8(p, c, field, qp, 0, c);
+            int bx = (lane & 1) * 8, by = (lane >> 1) * 8;
+            for (int i = 0; i < 8; i++)
+                for (int j = 0; j < 8; j++) s.res[(by + i) * 16 + bx + j] = c[i * 8 + j];
+        }
+    } else if (lane < 16) {
+        bool i16 = m.type == H264R_MB_I16x16;
+        if ((cv.mask & (1u << lane)) || (i16 && s.dc[kBlkY[lane] * 4 + kBlkX[lane]] != 0)) {
+            int32_t c[16], r[16];
+            coef_list16(cv, lane, field, c);
+            if (i16) c[0] = s.dc[kBlkY[lane] * 4 + kBlkX[lane]];
+            idct4x4(p, c, field, qp, 0, i16, r);
+            int bx = kBlkX[lane] * 4, by = kBlkY[lane] * 4;
+            for (int i = 0; i < 4; i++)
+                for (int j = 0; j < 4; j++) s.res[(by + i) * 16 + bx + j] = r[i * 4 + j];
+        }
+    }
+    if (lane >= 16 && lane < 24 && cv.mask != 0) {
+        const int pl = (lane - 16) >> 2, b = (lane - 16) & 3;
+        const int qpc = chroma_qp(qp, p.slices[m.slice].chroma_qp_offset[pl]);
+        int32_t dcl[16], dc4[4], dcC[4];
+        coef_list16(cv, 17 + pl, 0, dcl);
+        dc4[0] = dcl[0]; dc4[1] = dcl[1]; dc4[2] = dcl[4]; dc4[3] = dcl[8];
+        chroma_dc(p, dc4, field, qpc, 0, dcC);
+        int32_t c[16], r[16];
+        coef_list16(cv, (pl ? H264R_CM_CR_AC0 : H264R_CM_CB_AC0) + b, field, c);
+        c[0] = dcC[b];
+        idct4x4(p, c, field, qpc, 0, true, r);
+        int bx = (b & 1) * 4, by = (b >> 1) * 4;
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) s.res[256 + pl * 64 + (by + i) * 8 + bx + j] = r[i * 4 + j];
+    }
+    __syncwarp();
+    // ---- luma prediction + reconstruction
+    if (m.type == H264R_MB_I4x4) {
+        for (int b = 0; b < 16; b++) {
+            const int xO = kBlkX[b] * 4, yO = kBlkY[b] * 4;
+            if (lane < 13) {
+                int nx = lane < 5 ? -1 : lane - 5, ny = lane < 5 ? lane - 1 : -1;
+                int v = -1;
+                if (!(nx > 3 && (b == 3 || b == 11))) {
+                    const uint8_t *ptr = intra_nb_ptr(p, addr, 0, 0, xO + nx, yO + ny);
+                    if (ptr) v = ldcg_u8(ptr);
+                }
+                s.nb[lane] = v;
+            }
+            __syncwarp();
+            if (lane == 0 && s.nb[9] < 0 && s.nb[10] < 0 && s.nb[11] < 0 && s.nb[12] < 0 && s.nb[8] >= 0)
+                s.nb[9] = s.nb[10] = s.nb[11] = s.nb[12] = s.nb[8];
+            __syncwarp();
+            if (lane < 16) {
+                int i = lane >> 2, j = lane & 3;
+                int mode = (m.ipred[b >> 3] >> (4 * (b & 7))) & 15;
+                int pv = pred4x4_sample(mode, s.nb, j, i);
+                if (pv < 0) pv = 0;  // prediction not written: the cleared buffer
+                Y[(size_t)(y + (yO + i) * dy) * p.W + x + xO + j] = (uint8_t)clip1(pv + s.res[(yO + i) * 16 + xO + j]);
+            }
+            __threadfence_block();
+            __syncwarp();
+        }
+    } else if (m.type == H264R_MB_I8x8) {
+        for (int b = 0; b < 4; b++) {
+            const int xO = (b & 1) * 8, yO = (b >> 1) * 8;
+            // 25 samples: p[-1,-1], p[-1,0..7], p[0..15,-1]
+            if (lane < 25) {
+                int nx = lane < 9 ? -1 : lane - 9, ny = lane < 9 ? lane - 1 : -1;
+                const uint8_t *ptr = intra_nb_ptr(p, addr, 0, 0, xO + nx, yO + ny);
+                s.nb[lane] = ptr ? ldcg_u8(ptr) : -1;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                int *q = s.nb;  // q[0] corner, q[1..8] left, q[9..24] top
+                bool all = true;
+                for (int i = 17; i < 25; i++) all = all && q[i] < 0;
+                if (all && q[16] >= 0)
+                    for (int i = 17; i < 25; i++) q[i] = q[16];
+                int *f = s.nbf;
+                for (int i = 0; i < 25; i++) f[i] = -1;
+                bool top16 = true;
+                for (int i = 9; i < 25; i++) top16 = top16 && q[i] >= 0;
+                // 8.3.2.2.1 reference sample filtering (H264PictureBase.cpp:1540-1600)
+                if (top16) {
+                    f[9] = (q[0] >= 0) ? (q[0] + 2 * q[9] + q[10] + 2) >> 2 : (3 * q[9] + q[10] + 2) >> 2;
+                    for (int i = 10; i < 24; i++) f[i] = (q[i - 1] + 2 * q[i] + q[i + 1] + 2) >> 2;
+                    f[24] = (q[23] + 3 * q[24] + 2) >> 2;
+                }
+                if (q[0] >= 0) {
+                    if (q[9] < 0 || q[1] < 0) {
+                        if (q[9] >= 0) f[0] = (3 * q[0] + q[9] + 2) >> 2;
+                        else if (q[1] >= 0) f[0] = (3 * q[0] + q[1] + 2) >> 2;
+                        else f[0] = q[0];
+                    } else {
+                        f[0] = (q[9] + 2 * q[0] + q[1] + 2) >> 2;
+                    }
+                }
+                bool left8 = true;
+                for (int i = 1; i < 9; i++) left8 = left8 && q[i] >= 0;
+                if (left8) {
+                    f[1] = (q[0] >= 0) ? (q[0] + 2 * q[1] + q[2] + 2) >> 2 : (3 * q[1] + q[2] + 2) >> 2;
+                    for (int i = 2; i < 8; i++) f[i] = (q[i - 1] + 2 * q[i] + q[i + 1] + 2) >> 2;
+                    f[8] = (q[7] + 3 * q[8] + 2) >> 2;
+                }
+            }
+            __syncwarp();
+            int mode = (m.ipred[0] >> (4 * b)) & 15;
+            for (int k = lane; k < 64; k += 32) {
+                int i = k >> 3, j = k & 7;
+                int pv = pred8x8_sample(mode, s.nbf, j, i);
+                if (pv < 0) pv = 0;
+                Y[(size_t)(y + (yO + i) * dy) * p.W + x + xO + j] = (uint8_t)clip1(pv + s.res[(yO + i) * 16 + xO + j]);
+            }
+            __threadfence_block();
+            __syncwarp();
+        }
+    } else {
+        // Intra_16x16: 33 samples p[-1,-1], p[-1,0..15], p[0..15,-1]
+        for (int k = lane; k < 33; k += 32) {
+            int nx = k < 17 ? -1 : k - 17, ny = k < 17 ? k - 1 : -1;
+            const uint8_t *ptr = intra_nb_ptr(p, addr, 0, 0, nx, ny);
+            s.nb[k] = ptr ? ldcg_u8(ptr) : -1;
+        }
+        __syncwarp();
+        const int *q = s.nb;
+        bool ta = true, la = true;
+        for (int i = 0; i < 16; i++) { ta = ta && q[17 + i] >= 0; la = la && q[1 + i] >= 0; }
+        const int mode = m.i16_mode;
+        int a = 0, bb = 0, cc = 0, dcv = 128;
+        if (mode == 2) {
+            int stp = 0, slf = 0;
+            for (int i = 0; i < 16; i++) { stp += q[17 + i]; slf += q[1 + i]; }
+            if (ta && la) dcv = (stp + slf + 16) >> 5;
+            else if (la) dcv = (slf + 8) >> 4;
+            else if (ta) dcv = (stp + 8) >> 4;
+        } else if (mode == 3) {
+            // quirk: p[-1,-1] is not required; when unavailable -1 enters H, V
+            int H = 0, V = 0;
+            for (int i = 0; i <= 7; i++) {
+                H += (i + 1) * (q[17 + 8 + i] - (6 - i >= 0 ? q[17 + 6 - i] : q[0]));
+                V += (i + 1) * (q[1 + 8 + i] - (6 - i >= 0 ? q[1 + 6 - i] : q[0]));
+            }
+            a = 16 * (q[1 + 15] + q[17 + 15]);
+            bb = (5 * H + 32) >> 6;
+            cc = (5 * V + 32) >> 6;
+        }
+        for (int k = lane; k < 256; k += 32) {
+            int i = k >> 4, j = k & 15, pv;
+            if (mode == 0) pv = ta ? q[17 + j] : 0;
+            else if (mode == 1) pv = la ? q[1 + i] : 0;
+            else if (mode == 2) pv = dcv;
+            else if (mode == 3) pv = (ta && la) ? clip1((a + bb * (j - 7) + cc * (i - 7) + 16) >> 5) : 0;
+            else pv = 0;
+            Y[(size_t)(y + i * dy) * p.W + x + j] = (uint8_t)clip1(pv + s.res[k]);
+        }
+        __threadfence_block();
+        __syncwarp();
+    }
+    // ---- chroma (Intra_chroma_sample_prediction_for_YUV420_or_YUV422,
+    //      H264PictureBase.cpp:2076-2385); quirk: DC treats value 0 as unavailable
+    for (int k = lane; k < 34; k += 32) {
+        int pl = k / 17, i = k % 17;
+        int nx = i < 9 ? -1 : i - 9, ny = i < 9 ? i - 1 : -1;
+        const uint8_t *ptr = intra_nb_ptr(p, addr, 1, pl, nx, ny);
+        s.nb[k] = ptr ? ldcg_u8(ptr) : -1;
+    }
+    __syncwarp();
+    const int cmode = m.chroma_mode;
+    const int xc = x / 2, yc = chroma_row0(y);
+    for (int k = lane; k < 128; k += 32) {
+        const int pl = k >> 6, i = (k & 63) >> 3, j = k & 7;
+        const int *q = s.nb + pl * 17;  // q[0] corner, q[1..8] left, q[9..16] top
+        int pv = 0;
+        if (cmode == 0) {
+            int xO = j & 4, yO = i & 4;
+            bool t4 = q[9 + xO] > 0 && q[10 + xO] > 0 && q[11 + xO] > 0 && q[12 + xO] > 0;
+            bool l4 = q[1 + yO] > 0 && q[2 + yO] > 0 && q[3 + yO] > 0 && q[4 + yO] > 0;
+            int stp = t4 ? q[9 + xO] + q[10 + xO] + q[11 + xO] + q[12 + xO] : 0;
+            int slf = l4 ? q[1 + yO] + q[2 + yO] + q[3 + yO] + q[4 + yO] : 0;
+            if ((xO == 0 && yO == 0) || (xO > 0 && yO > 0)) {
+                pv = (t4 && l4) ? (stp + slf + 4) >> 3 : l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
+            } else if (xO > 0) {
+                pv = t4 ? (stp + 2) >> 2 : l4 ? (slf + 2) >> 2 : 128;
+            } else {
+                pv = l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
+            }
+        } else if (cmode == 1) {
+            bool ok = true;
+            for (int u = 0; u < 8; u++) ok = ok && q[1 + u] >= 0;
+            pv = ok ? q[1 + i] : 0;
+        } else if (cmode == 2) {
+            bool ok = true;
+            for (int u = 0; u < 8; u++) ok = ok && q[9 + u] >= 0;
+            pv = ok ? q[9 + j] : 0;
+        } else if (cmode == 3) {
+            bool ok = q[0] >= 0;
+            for (int u = 0; u < 8; u++) ok = ok && q[9 + u] >= 0 && q[1 + u] >= 0;
+            if (ok) {
+                int H = 0, V = 0;
+                for (int u = 0; u <= 3; u++) {
+                    H += (u + 1) * (q[9 + 4 + u] - (2 - u >= 0 ? q[9 + 2 - u] : q[0]));
+                    V += (u + 1) * (q[1 + 4 + u] - (2 - u >= 0 ? q[1 + 2 - u] : q[0]));
+                }
+                int a = 16 * (q[1 + 7] + q[9 + 7]);
+                int b2 = (34 * H + 32) >> 6, c2 = (34 * V + 32) >> 6;
+                pv = clip1((a + b2 * (j - 3) + c2 * (i - 3) + 16) >> 5);
+            }
+        }
+        uint8_t *C = plane_c(p, pl);
+        C[(size_t)(yc + i * dy) * p.Wc + xc + j] = (uint8_t)clip1(pv + s.res[256 + pl * 64 + i * 8 + j]);
+    }
+    __threadfence_block();
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(32) k_intra(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st)
+{
+    __shared__ IntraSmem s;
+    __shared__ uint32_t s_row;
+    const int lane = threadIdx.x;
+    if (lane == 0) s_row = atomicAdd(&st.ticket[0], 1u);
+    __syncwarp();
+    const uint32_t g = s_row;
+    if (g >= total_rows) return;
+    const int pi = find_pic_by_row(pics, npics, g);
+    const PicDesc &p = pics[pi];
+    const int row = (int)(g - p.row_base);
+    const int uw = (int)p.units_w;
+    const int per = p.mbaff ? 2 : 1;
+    int *prog = p.progress;
+    for (int u = 0; u < uw; u++) {
+        if (row > 0 && !wait_progress(st, prog + row - 1, min(u + 2, uw))) return;
+        for (int k = 0; k < per; k++) {
+            int addr = p.mbaff ? 2 * (row * uw + u) + k : row * uw + u;
+            int t = p.mbs[addr].type;
+            if (is_intra_type(t)) intra_mb(p, addr, s, st);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence();
+            st_release(prog + row, u + 1);
+        }
+    }
+}
+
+// ======================================================================
+// K3a: boundary strengths
+// ======================================================================
+struct BlkMotion {
+    int mv[2][2];
+    int pf[2];
+    int id[2];
+};
+
+__device__ __forceinline__ void get_motion(const PicDesc &p, int addr, int xq, int yq, BlkMotion &o)
+{
+    const h264r_mb &m = p.mbs[addr];
+    o.mv[0][0] = o.mv[0][1] = o.mv[1][0] = o.mv[1][1] = 0;
+    o.pf[0] = o.pf[1] = 0;
+    o.id[0] = o.id[1] = -1;
+    if (m.type != H264R_MB_INTER || m.aux == H264R_NONE) return;
+    uint32_t hdr = *(const uint32_t *)(p.motion + m.aux);
+    int e = part_of_block(hdr & 0xFFFF, xq >> 2, yq >> 2);
+    if (e >= (int)(hdr >> 16)) return;
+    const h264r_part pp = ((const h264r_part *)(p.motion + m.aux + 4))[e];
+    for (int l = 0; l < 2; l++) {
+        o.mv[l][0] = pp.mv[l][0];
+        o.mv[l][1] = pp.mv[l][1];
+        o.pf[l] = pp.ref[l] >= 0;
+        o.id[l] = pp.dref[l];
+    }
+}
+
+// 8.7.2.1 (Derivation_process_for_the_luma_content_dependent_boundary_
+// filtering_strength, H264PictureDeblockingFilterProcess.cpp:994-1310).
+// Returns 0xFF where the reference's derivation fails (it reaches the
+// partition lookup of a macroblock that was never decoded).
+__device__ int derive_bs(const PicDesc &p, int mbP, int mbQ, int xp, int yp, int xq, int yq, int vertical)
+{
+    const h264r_mb P = p.mbs[mbP], Q = p.mbs[mbQ];
+    const int mbaff = p.mbaff;
+    int fP = (P.flags & H264R_MBF_FIELD) && mbaff, fQ = (Q.flags & H264R_MBF_FIELD) && mbaff;
+    int mixed = mbaff && mbP != mbQ && fP != fQ;
+    bool intraP = is_intra_type(P.type), intraQ = is_intra_type(Q.type);
+    int stP = p.slices[P.slice].slice_type, stQ = p.slices[Q.slice].slice_type;
+    bool spP = stP == 3 || stP == 4, spQ = stQ == 3 || stQ == 4;
+    if (mbP != mbQ) {
+        if ((!fP && !fQ && (intraP || intraQ)) || (!fP && !fQ && (spP || spQ)) || (mbaff && vertical && (intraP || intraQ)) ||
+            (mbaff && vertical && (spP || spQ)))
+            return 4;
+    }
+    if ((!mixed && (intraP || intraQ)) || (!mixed && (spP || spQ)) || (mixed && !vertical && (intraP || intraQ)) ||
+        (mixed && !vertical && (spP || spQ)))
+        return 3;
+    int bp4 = 8 * (yp / 8) + 4 * (xp / 8) + 2 * ((yp % 8) / 4) + ((xp % 8) / 4);
+    int bq4 = 8 * (yq / 8) + 4 * (xq / 8) + 2 * ((yq % 8) / 4) + ((xq % 8) / 4);
+    int bp8 = 2 * (yp / 8) + (xp / 8), bq8 = 2 * (yq / 8) + (xq / 8);
+    int nzP = (P.flags & H264R_MBF_T8x8) ? ((P.nz8x8 >> bp8) & 1) : ((P.nz4x4 >> bp4) & 1);
+    int nzQ = (Q.flags & H264R_MBF_T8x8) ? ((Q.nz8x8 >> bq8) & 1) : ((Q.nz4x4 >> bq4) & 1);
+    if (nzP || nzQ) return 2;
+    if (P.type == H264R_MB_NONE || Q.type == H264R_MB_NONE) return 0xFF;
+    if (mixed) return 1;
+    const int lim = fQ ? 2 : 4;
+    BlkMotion a, b;
+    get_motion(p, mbP, xp, yp, a);
+    get_motion(p, mbQ, xq, yq, b);
+#define DIFF(u, v) (abs((u)[0] - (v)[0]) >= 4 || abs((u)[1] - (v)[1]) >= lim)
+    int r0p = a.id[0], r1p = a.id[1], r0q = b.id[0], r1q = b.id[1];
+    int np = a.pf[0] + a.pf[1], nq = b.pf[0] + b.pf[1];
+    if (!(((r0p == r0q && r1p == r1q) || (r0p == r1q && r1p == r0q)) && np == nq)) return 1;
+    if (a.pf[0] && !a.pf[1] && b.pf[0] && !b.pf[1] && DIFF(a.mv[0], b.mv[0])) return 1;
+    if (a.pf[0] && !a.pf[1] && !b.pf[0] && b.pf[1] && DIFF(a.mv[0], b.mv[1])) return 1;
+    if (!a.pf[0] && a.pf[1] && b.pf[0] && !b.pf[1] && DIFF(a.mv[1], b.mv[0])) return 1;
+    if (!a.pf[0] && a.pf[1] && !b.pf[0] && b.pf[1] && DIFF(a.mv[1], b.mv[1])) return 1;
+    if (a.pf[0] && a.pf[1] && r0p != r1p && b.pf[0] && b.pf[1] && ((r0q == r0p && r1q == r1p) || (r0q == r1p && r1q == r0p))) {
+        if (r0q == r0p && (DIFF(a.mv[0], b.mv[0]) || DIFF(a.mv[1], b.mv[1]))) return 1;
+        else if (r0q == r1p && (DIFF(a.mv[1], b.mv[0]) || DIFF(a.mv[0], b.mv[1]))) return 1;
+    }
+    // quirk: parsed as (A || B) && C || D (1289-1298)
+    if (a.pf[0] && a.pf[1] && r0p == r1p && b.pf[0] && b.pf[1] && r0q == r1q && r0q == r0p) {
+        if (((DIFF(a.mv[0], b.mv[0]) || DIFF(a.mv[1], b.mv[1])) && DIFF(a.mv[0], b.mv[1])) || DIFF(a.mv[1], b.mv[0])) return 1;
+    }
+#undef DIFF
+    return 0;
+}
+
+// Per-MB filter controls of Deblocking_filter_process (76-160)
+struct EdgeCtl {
+    int mbA, mbB, field, left, top, internal, t8, leftMixed, topDouble;
+};
+
+__device__ __forceinline__ EdgeCtl edge_ctl(const PicDesc &p, int cur)
+{
+    EdgeCtl e;
+    const h264r_mb m = p.mbs[cur];
+    int xW, yW;
+    e.mbA = nb_loc(p, cur, -1, 0, 16, 16, xW, yW);
+    e.mbB = nb_loc(p, cur, 0, -1, 16, 16, xW, yW);
+    const int W = p.wmb, mbaff = p.mbaff;
+    e.field = mbaff && (m.flags & H264R_MBF_FIELD);
+    int idc = p.slices[m.slice].disable_deblocking_filter_idc;
+    e.internal = idc != 1;
+    e.left = !((!mbaff && cur % W == 0) || (mbaff && (cur >> 1) % W == 0) || idc == 1 || (idc == 2 && e.mbA < 0));
+    e.top = !((!mbaff && cur < W) || (mbaff && (cur >> 1) < W && e.field) || (mbaff && (cur >> 1) < W && !e.field && (cur % 2) == 0) ||
+              idc == 1 || (idc == 2 && e.mbB < 0));
+    e.t8 = (m.flags & H264R_MBF_T8x8) != 0;
+    e.leftMixed = mbaff && cur >= 2 && !e.field && (p.mbs[cur - 2].flags & H264R_MBF_FIELD);
+    e.topDouble = mbaff && (cur % 2) == 0 && cur >= 2 * W && !e.field && (p.mbs[cur - 2 * W + 1].flags & H264R_MBF_FIELD);
+    return e;
+}
+
+// bS of row/col k of one edge (8.7.1 p-side rules, 639-805); e = edge
+// offset in samples of the component; mbN: neighbour handed to the filter
+__device__ __forceinline__ int edge_bs(const PicDesc &p, int cur, int chroma, int vertical, int e, int mbN, int leftMbEdge, int k)
+{
+    int xE = vertical ? e : k, yE = vertical ? k : e;
+    int mbP = cur, xp0, yp0, xq0, yq0;
+    if (vertical) {
+        xp0 = xE - 1;
+        if (xp0 < 0) {
+            if (mbN >= 0) mbP = leftMbEdge ? mbN + (yE % 2) : mbN;
+            xp0 += chroma ? 8 : 16;
+        }
+        yp0 = yE; xq0 = xE; yq0 = yE;
+    } else {
+        xp0 = xE;
+        yp0 = (yE - 1) - (yE % 2);
+        if (yp0 < 0) {
+            if (mbN >= 0) mbP = mbN;
+            yp0 += chroma ? 8 : 16;
+        }
+        xq0 = xE; yq0 = yE - (yE % 2);
+    }
+    int sx = chroma ? 2 : 1;
+    return derive_bs(p, mbP, cur, xp0 * sx, yp0 * sx, xq0 * sx, yq0 * sx, vertical);
+}
+
+// edge sequence numbers in the reference's per-MB filtering order
+enum { SEQ_LV0 = 0, SEQ_LV4, SEQ_LV8, SEQ_LV12, SEQ_LH0, SEQ_LH0B, SEQ_LH4, SEQ_LH8, SEQ_LH12,
+       SEQ_CBV0, SEQ_CRV0, SEQ_CBV4, SEQ_CRV4, SEQ_CBH0, SEQ_CRH0, SEQ_CBH0B, SEQ_CRH0B, SEQ_CBH4, SEQ_CRH4 };
+
+__device__ __forceinline__ uint32_t stop_key(int mb, int seq, int k) { return ((uint32_t)mb << 10) | ((uint32_t)seq << 4) | (uint32_t)k; }
+
+__global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st)
+{
+    // one warp per MB; 4 MBs per block
+    const uint32_t g = blockIdx.x * 4 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (g >= total_mbs) return;
+    const int pi = find_pic_by_mb(pics, npics, g);
+    PicDesc *pp = const_cast<PicDesc *>(&pics[pi]);
+    const PicDesc &p = pics[pi];
+    const int cur = (int)(g - p.mb_base);
+    if (!p.deblock) return;
+    EdgeCtl c = edge_ctl(p, cur);
+    uint8_t *out = p.bs + (size_t)cur * kBsBytes;
+    uint32_t mystop = 0xFFFFFFFFu;
+    // luma vertical (4 edges x 16 rows): items 0..63
+    for (int it = lane; it < 64; it += 32) {
+        int ei = it >> 4, k = it & 15, e = ei * 4;
+        bool on = (ei == 0) ? c.left : (c.internal && (ei == 2 || !c.t8));
+        int bs = on ? edge_bs(p, cur, 0, 1, e, c.mbA, ei == 0 ? c.leftMixed : 0, k) : 0;
+        if (bs == 0xFF) mystop = min(mystop, stop_key(cur, SEQ_LV0 + ei, k));
+        out[kBsLumaV + it] = (uint8_t)bs;
+    }
+    // luma horizontal: items 0..63 (+16 for the MBAFF second top edge)
+    for (int it = lane; it < 80; it += 32) {
+        int bs = 0, seq, k;
+        if (it < 64) {
+            int ei = it >> 4, e = ei * 4;
+            k = it & 15;
+            bool on = (ei == 0) ? c.top : (c.internal && (ei == 2 || !c.t8));
+            if (on) {
+                if (ei == 0 && c.topDouble) bs = edge_bs(p, cur, 0, 0, 0, c.mbB - 1, 0, k);
+                else bs = edge_bs(p, cur, 0, 0, e, c.mbB, 0, k);
+            }
+            seq = ei == 0 ? SEQ_LH0 : SEQ_LH4 + ei - 1;
+            out[kBsLumaH + it] = (uint8_t)bs;
+        } else {
+            k = it - 64;
+            if (c.top && c.topDouble) bs = edge_bs(p, cur, 0, 0, 1, c.mbB, 0, k);
+            seq = SEQ_LH0B;
+            out[kBsLumaTop2 + k] = (uint8_t)bs;
+        }
+        if (bs == 0xFF) mystop = min(mystop, stop_key(cur, seq, k));
+    }
+    // chroma: vertical 2 edges x 8 rows, horizontal 2 x 8, extra top 8;
+    // Cb and Cr share the strengths but are separate steps of the order
+    for (int it = lane; it < 40; it += 32) {
+        int bs = 0, seqcb, k;
+        if (it < 16) {
+            int ei = it >> 3;
+            k = it & 7;
+            bool on = ei == 0 ? c.left : c.internal;
+            if (on) bs = edge_bs(p, cur, 1, 1, ei * 4, c.mbA, ei == 0 ? c.leftMixed : 0, k);
+            seqcb = ei == 0 ? SEQ_CBV0 : SEQ_CBV4;
+            out[kBsChromaV + it] = (uint8_t)bs;
+        } else if (it < 32) {
+            int ei = (it - 16) >> 3;
+            k = it & 7;
+            bool on = ei == 0 ? c.top : c.internal;
+            if (on) bs = edge_bs(p, cur, 1, 0, ei == 0 ? 0 : 4, c.mbB, 0, k);
+            seqcb = ei == 0 ? SEQ_CBH0 : SEQ_CBH4;
+            out[kBsChromaH + (it - 16)] = (uint8_t)bs;
+        } else {
+            k = it - 32;
+            if (c.top && c.topDouble) bs = edge_bs(p, cur, 1, 0, 1, c.mbB, 0, k);
+            seqcb = SEQ_CBH0B;
+            out[kBsChromaTop2 + k] = (uint8_t)bs;
+        }
+        if (bs == 0xFF) mystop = min(mystop, stop_key(cur, seqcb, k));
+    }
+    for (int o = 16; o > 0; o >>= 1) mystop = min(mystop, __shfl_xor_sync(0xffffffffu, mystop, o));
+    if (lane == 0 && mystop != 0xFFFFFFFFu) atomicMin(&pp->deblock_stop, mystop);
+}
+
+// ======================================================================
+// K3b: deblocking wavefront
+// ======================================================================
+// filter one line (8.7.2.3 / 8.7.2.4, H264PictureDeblockingFilterProcess.cpp:1373-1522)
+__device__ __forceinline__ void filter_line(int *pv, int *qv, int bS, bool chroma, int indexA, int alpha, int beta)
+{
+    if (!(bS != 0 && abs(pv[0] - qv[0]) < alpha && abs(pv[1] - pv[0]) < beta && abs(qv[1] - qv[0]) < beta)) return;
+    int ap = abs(pv[2] - pv[0]), aq = abs(qv[2] - qv[0]);
+    int np0 = pv[0], np1 = pv[1], np2 = pv[2], nq0 = qv[0], nq1 = qv[1], nq2 = qv[2];
+    if (bS < 4) {
+        int tc0 = kTc0[bS - 1][indexA];
+        int tc = chroma ? tc0 + 1 : tc0 + (ap < beta) + (aq < beta);
+        int delta = H264R_CLIP3(-tc, tc, ((((qv[0] - pv[0]) << 2) + (pv[1] - qv[1]) + 4) >> 3));
+        np0 = clip1(pv[0] + delta);
+        nq0 = clip1(qv[0] - delta);
+        if (!chroma && ap < beta) np1 = (uint8_t)(pv[1] + H264R_CLIP3(-tc0, tc0, (pv[2] + ((pv[0] + qv[0] + 1) >> 1) - (pv[1] << 1)) >> 1));
+        if (!chroma && aq < beta) nq1 = (uint8_t)(qv[1] + H264R_CLIP3(-tc0, tc0, (qv[2] + ((pv[0] + qv[0] + 1) >> 1) - (qv[1] << 1)) >> 1));
+    } else {
+        bool sm = abs(pv[0] - qv[0]) < ((alpha >> 2) + 2);
+        if (!chroma && ap < beta && sm) {
+            np0 = (pv[2] + 2 * pv[1] + 2 * pv[0] + 2 * qv[0] + qv[1] + 4) >> 3;
+            np1 = (pv[2] + pv[1] + pv[0] + qv[0] + 2) >> 2;
+            np2 = (2 * pv[3] + 3 * pv[2] + pv[1] + pv[0] + qv[0] + 4) >> 3;
+        } else {
+            np0 = (2 * pv[1] + pv[0] + qv[1] + 2) >> 2;
+        }
+        if (!chroma && aq < beta && sm) {
+            nq0 = (pv[1] + 2 * pv[0] + 2 * qv[0] + 2 * qv[1] + qv[2] + 4) >> 3;
+            nq1 = (pv[0] + qv[0] + qv[1] + qv[2] + 2) >> 2;
+            nq2 = (2 * qv[3] + 3 * qv[2] + qv[1] + qv[0] + pv[0] + 4) >> 3;
+        } else {
+            nq0 = (2 * qv[1] + qv[0] + pv[1] + 2) >> 2;
+        }
+    }
+    pv[0] = np0; pv[1] = np1; pv[2] = np2;
+    qv[0] = nq0; qv[1] = nq1; qv[2] = nq2;
+}
+
+// One edge step, one line per active lane (8.7.1, 639-840).  comp: 0 luma,
+// 1 Cb, 2 Cr; k: line index of this lane; bs: its strength.
+__device__ __forceinline__ void edge_line(const PicDesc &p, int cur, int comp, int vertical, int e, int mbN, int leftMbEdge,
+                                          int fieldMode, int k, int bs)
+{
+    if (bs == 0) return;
+    const bool chroma = comp != 0;
+    uint8_t *plane = comp == 0 ? plane_y(p) : plane_c(p, comp - 1);
+    const int stride = chroma ? p.Wc : p.W;
+    const int ddy = 1 + fieldMode;
+    int xI, yI, dyI;
+    mb_origin(p, cur, xI, yI, dyI);
+    int xP = chroma ? xI / 2 : xI, yP = chroma ? (yI + 1) / 2 : yI;
+    int xE = vertical ? e : k, yE = vertical ? k : e;
+    size_t qi[4], pi[4];
+    for (int i = 0; i < 4; i++) {
+        if (vertical) {
+            qi[i] = (size_t)(yP + ddy * yE) * stride + (xP + xE + i);
+            pi[i] = (size_t)(yP + ddy * yE) * stride + (xP + xE - i - 1);
+        } else {
+            qi[i] = (size_t)(yP + ddy * (yE + i) - (yE % 2)) * stride + (xP + xE);
+            pi[i] = (size_t)(yP + ddy * (yE - i - 1) - (yE % 2)) * stride + (xP + xE);
+        }
+    }
+    // p-side MB (same rule as edge_bs)
+    int mbP = cur;
+    if (vertical) {
+        if (xE - 1 < 0 && mbN >= 0) mbP = leftMbEdge ? mbN + (yE % 2) : mbN;
+    } else {
+        if ((yE - 1) - (yE % 2) < 0 && mbN >= 0) mbP = mbN;
+    }
+    const h264r_mb P = p.mbs[mbP], Q = p.mbs[cur];
+    const h264r_slice sq = p.slices[Q.slice];
+    int qPp, qPq;
+    if (!chroma) {
+        qPp = P.type == H264R_MB_IPCM ? 0 : P.qpy;
+        qPq = Q.type == H264R_MB_IPCM ? 0 : Q.qpy;
+    } else {
+        int off = sq.chroma_qp_offset[comp - 1];
+        qPp = chroma_qp(P.type == H264R_MB_IPCM ? 0 : P.qpy, off);
+        qPq = chroma_qp(Q.type == H264R_MB_IPCM ? 0 : Q.qpy, off);
+    }
+    int qPav = (qPp + qPq + 1) >> 1;
+    int indexA = H264R_CLIP3(0, 51, qPav + sq.filter_offset_a);
+    int indexB = H264R_CLIP3(0, 51, qPav + sq.filter_offset_b);
+    int alpha = kAlpha[indexA], beta = kBeta[indexB];
+    int pv[4], qv[4];
+    for (int i = 0; i < 4; i++) {
+        pv[i] = __ldcg(plane + pi[i]);
+        qv[i] = __ldcg(plane + qi[i]);
+    }
+    filter_line(pv, qv, bs, chroma, indexA, alpha, beta);
+    for (int i = 0; i < 3; i++) {
+        plane[qi[i]] = (uint8_t)qv[i];
+        plane[pi[i]] = (uint8_t)pv[i];
+    }
+}
+
+// Deblock one MB with one warp: lanes 0..15 luma lines, 16..23 Cb, 24..31 Cr.
+__device__ void deblock_mb(const PicDesc &p, int cur)
+{
+    const int lane = threadIdx.x & 31;
+    const EdgeCtl c = edge_ctl(p, cur);
+    const uint8_t *bs = p.bs + (size_t)cur * kBsBytes;
+    const uint32_t stop = p.deblock_stop;
+    const bool luma = lane < 16;
+    const int k = luma ? lane : (lane & 7);
+    const int comp = luma ? 0 : (lane < 24 ? 1 : 2);
+    // a step runs only when it comes before the reference's early return
+    auto allowed = [&](int seq, int kk) -> bool { return stop_key(cur, seq, kk) < stop; };
+    const int cseq = comp == 2 ? 1 : 0;  // Cr steps follow the Cb step of the same edge
+    // ---- vertical edges
+    if (luma) {
+        if (c.left && allowed(SEQ_LV0, k)) edge_line(p, cur, 0, 1, 0, c.mbA, c.leftMixed, c.field, k, bs[kBsLumaV + k]);
+        __syncwarp(0x0000FFFFu);
+        if (c.internal) {
+            if (!c.t8 && allowed(SEQ_LV4, k)) edge_line(p, cur, 0, 1, 4, c.mbA, 0, c.field, k, bs[kBsLumaV + 16 + k]);
+            __syncwarp(0x0000FFFFu);
+            if (allowed(SEQ_LV8, k)) edge_line(p, cur, 0, 1, 8, c.mbA, 0, c.field, k, bs[kBsLumaV + 32 + k]);
+            __syncwarp(0x0000FFFFu);
+            if (!c.t8 && allowed(SEQ_LV12, k)) edge_line(p, cur, 0, 1, 12, c.mbA, 0, c.field, k, bs[kBsLumaV + 48 + k]);
+        }
+    } else {
+        if (c.left && allowed(SEQ_CBV0 + cseq, k)) edge_line(p, cur, comp, 1, 0, c.mbA, c.leftMixed, c.field, k, bs[kBsChromaV + k]);
+        __syncwarp(0xFFFF0000u);
+        if (c.internal && allowed(SEQ_CBV4 + cseq, k)) edge_line(p, cur, comp, 1, 4, c.mbA, 0, c.field, k, bs[kBsChromaV + 8 + k]);
+    }
+    __syncwarp();
+    // ---- horizontal edges
+    if (luma) {
+        if (c.top) {
+            if (c.topDouble) {
+                if (allowed(SEQ_LH0, k)) edge_line(p, cur, 0, 0, 0, c.mbB - 1, 0, 1, k, bs[kBsLumaH + k]);
+                __syncwarp(0x0000FFFFu);
+                if (allowed(SEQ_LH0B, k)) edge_line(p, cur, 0, 0, 1, c.mbB, 0, 1, k, bs[kBsLumaTop2 + k]);
+            } else if (allowed(SEQ_LH0, k)) {
+                edge_line(p, cur, 0, 0, 0, c.mbB, 0, c.field, k, bs[kBsLumaH + k]);
+            }
+        }
+        __syncwarp(0x0000FFFFu);
+        if (c.internal) {
+            if (!c.t8 && allowed(SEQ_LH4, k)) edge_line(p, cur, 0, 0, 4, c.mbB, 0, c.field, k, bs[kBsLumaH + 16 + k]);
+            __syncwarp(0x0000FFFFu);
+            if (allowed(SEQ_LH8, k)) edge_line(p, cur, 0, 0, 8, c.mbB, 0, c.field, k, bs[kBsLumaH + 32 + k]);
+            __syncwarp(0x0000FFFFu);
+            if (!c.t8 && allowed(SEQ_LH12, k)) edge_line(p, cur, 0, 0, 12, c.mbB, 0, c.field, k, bs[kBsLumaH + 48 + k]);
+        }
+    } else {
+        if (c.top) {
+            if (c.topDouble) {
+                if (allowed(SEQ_CBH0 + cseq, k)) edge_line(p, cur, comp, 0, 0, c.mbB, 0, 1, k, bs[kBsChromaH + k]);
+                __syncwarp(0xFFFF0000u);
+                if (allowed(SEQ_CBH0B + cseq, k)) edge_line(p, cur, comp, 0, 1, c.mbB, 0, 1, k, bs[kBsChromaTop2 + k]);
+            } else if (allowed(SEQ_CBH0 + cseq, k)) {
+                edge_line(p, cur, comp, 0, 0, c.mbB, 0, c.field, k, bs[kBsChromaH + k]);
+            }
+        }
+        __syncwarp(0xFFFF0000u);
+        if (c.internal && allowed(SEQ_CBH4 + cseq, k)) edge_line(p, cur, comp, 0, 4, c.mbB, 0, c.field, k, bs[kBsChromaH + 8 + k]);
+    }
+    __threadfence_block();
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(32) k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st)
+{
+    __shared__ uint32_t s_row;
+    const int lane = threadIdx.x;
+    if (lane == 0) s_row = atomicAdd(&st.ticket[1], 1u);
+    __syncwarp();
+    const uint32_t g = s_row;
+    if (g >= total_rows) return;
+    const int pi = find_pic_by_row(pics, npics, g);
+    const PicDesc &p = pics[pi];
+    if (!p.deblock) return;
+    const int row = (int)(g - p.row_base);
+    const int uw = (int)p.units_w;
+    const int per = p.mbaff ? 2 : 1;
+    int *prog = p.progress + p.units_h;
+    const uint32_t stop_mb = p.deblock_stop >> 10;
+    for (int u = 0; u < uw; u++) {
+        if (row > 0 && !wait_progress(st, prog + row - 1, min(u + 2, uw))) return;
+        for (int k = 0; k < per; k++) {
+            int addr = p.mbaff ? 2 * (row * uw + u) + k : row * uw + u;
+            if ((uint32_t)addr <= stop_mb) deblock_mb(p, addr);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence();
+            st_release(prog + row, u + 1);
+        }
+    }
+}
+
+}  // namespace h264r

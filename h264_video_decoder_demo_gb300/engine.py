@@ -1,0 +1,274 @@
+"""Python binding of the engine's C ABI (include/h264r.h) over ctypes.
+
+The CUDA engine lives in libh264r.so next to this file (built in-tree by
+h264_video_decoder_demo_gb300.build).  There is no fallback: when the library
+is missing, loading fails with an error that says how to build it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import records as R
+
+_LIB = None
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libh264r.so")
+
+# every symbol include/h264r.h and include/h264r_synth.h declare
+EXPORTS = [
+    "h264r_ctx_create", "h264r_ctx_destroy", "h264r_last_error", "h264r_stream_open",
+    "h264r_stream_close", "h264r_stream_dpb_bytes", "h264r_submit_picture",
+    "h264r_submit_picture_device", "h264r_submit_batch_device", "h264r_output",
+    "h264r_load_slot", "h264r_slot_device_ptr", "h264r_stream_sync", "h264r_ctx_sync",
+    "h264r_stream_cuda_stream", "h264r_validate_picture", "h264r_ctx_kernel_launches",
+    "h264r_ctx_set_timing", "h264r_ctx_last_timing",
+    "h264r_synth_create", "h264r_synth_dpb_slots", "h264r_synth_next", "h264r_synth_destroy",
+]
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("h264r error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    """Load libh264r.so (once) and declare the C signatures."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libh264r.so is not built: run `python -m h264_video_decoder_demo_gb300.build` "
+                          "(or __graft_entry__.build()) first")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i32, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64
+    P = ctypes.POINTER
+    sig = {
+        "h264r_ctx_create": (i32, [P(R.CCfg), P(vp)]),
+        "h264r_ctx_destroy": (i32, [vp]),
+        "h264r_last_error": (ctypes.c_char_p, [vp]),
+        "h264r_stream_open": (i32, [vp, P(R.CStreamCfg), P(vp)]),
+        "h264r_stream_close": (i32, [vp]),
+        "h264r_stream_dpb_bytes": (u64, [P(R.CStreamCfg)]),
+        "h264r_submit_picture": (i32, [vp, P(R.CPicture)]),
+        "h264r_submit_picture_device": (i32, [vp, P(R.CPicture)]),
+        "h264r_submit_batch_device": (i32, [vp, i32, P(vp), P(R.CPicture)]),
+        "h264r_output": (i32, [vp, i32, vp, vp, vp]),
+        "h264r_load_slot": (i32, [vp, i32, vp, vp, vp]),
+        "h264r_slot_device_ptr": (i32, [vp, i32, P(vp)]),
+        "h264r_stream_sync": (i32, [vp]),
+        "h264r_ctx_sync": (i32, [vp]),
+        "h264r_stream_cuda_stream": (vp, [vp]),
+        "h264r_validate_picture": (i32, [P(R.CPicture), i32]),
+        "h264r_ctx_kernel_launches": (u64, [vp]),
+        "h264r_ctx_set_timing": (i32, [vp, i32]),
+        "h264r_ctx_last_timing": (i32, [vp, P(ctypes.c_float)]),
+        "h264r_synth_create": (i32, [P(R.CSynthCfg), P(vp)]),
+        "h264r_synth_dpb_slots": (i32, [vp]),
+        "h264r_synth_next": (i32, [vp, P(R.CPicture), P(i32)]),
+        "h264r_synth_destroy": (i32, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = L
+    return L
+
+
+def validate(pic, dpb_slots):
+    c = pic.to_c()
+    return lib().h264r_validate_picture(ctypes.byref(c), dpb_slots)
+
+
+class Context:
+    """An engine context on one GPU (h264r_ctx)."""
+
+    def __init__(self, device=0, dpb_budget_bytes=0, max_batch=64):
+        cfg = R.CCfg(device, dpb_budget_bytes, max_batch, 0)
+        h = ctypes.c_void_p()
+        rc = lib().h264r_ctx_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != 0:
+            raise EngineError(rc, "h264r_ctx_create failed")
+        self.h = h
+
+    def check(self, rc, what):
+        if rc != 0:
+            raise EngineError(rc, "%s: %s" % (what, lib().h264r_last_error(self.h).decode()))
+        return rc
+
+    def last_error(self):
+        return lib().h264r_last_error(self.h).decode()
+
+    def kernel_launches(self):
+        return int(lib().h264r_ctx_kernel_launches(self.h))
+
+    def set_timing(self, on):
+        self.check(lib().h264r_ctx_set_timing(self.h, 1 if on else 0), "set_timing")
+
+    def last_timing(self):
+        t = (ctypes.c_float * 3)()
+        self.check(lib().h264r_ctx_last_timing(self.h, t), "last_timing")
+        return list(t)
+
+    def sync(self):
+        return self.check(lib().h264r_ctx_sync(self.h), "ctx_sync")
+
+    def submit_batch_device(self, streams, cpics):
+        n = len(streams)
+        arr = (ctypes.c_void_p * n)(*[s.h.value for s in streams])
+        pics = (R.CPicture * n)(*cpics)
+        return lib().h264r_submit_batch_device(self.h, n, arr, pics)
+
+    def close(self):
+        if self.h:
+            lib().h264r_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Stream:
+    """A stream with a device-resident DPB (h264r_stream)."""
+
+    def __init__(self, ctx, width_mbs, height_mbs, dpb_slots):
+        self.ctx = ctx
+        self.width_mbs, self.height_mbs, self.dpb_slots = width_mbs, height_mbs, dpb_slots
+        cfg = R.CStreamCfg(width_mbs, height_mbs, dpb_slots, 0)
+        h = ctypes.c_void_p()
+        rc = lib().h264r_stream_open(ctx.h, ctypes.byref(cfg), ctypes.byref(h))
+        ctx.check(rc, "stream_open")
+        self.h = h
+
+    @property
+    def plane_bytes(self):
+        return self.width_mbs * self.height_mbs * 384
+
+    def submit(self, pic):
+        """Reconstruct a picture from host records (Picture)."""
+        c = pic.to_c()
+        return self.ctx.check(lib().h264r_submit_picture(self.h, ctypes.byref(c)), "submit_picture")
+
+    def submit_device(self, cpic):
+        return self.ctx.check(lib().h264r_submit_picture_device(self.h, ctypes.byref(cpic)), "submit_picture_device")
+
+    def output(self, slot, out=None):
+        """Decoded planes of a DPB slot as one uint8 array (Y, Cb, Cr)."""
+        W, H = self.width_mbs * 16, self.height_mbs * 16
+        if out is None:
+            out = np.empty(W * H * 3 // 2, np.uint8)
+        base = out.ctypes.data
+        self.ctx.check(lib().h264r_output(self.h, slot, base, base + W * H, base + W * H + W * H // 4), "output")
+        self.sync()
+        return out
+
+    def output_async(self, slot, out):
+        W, H = self.width_mbs * 16, self.height_mbs * 16
+        base = out.ctypes.data
+        return self.ctx.check(lib().h264r_output(self.h, slot, base, base + W * H, base + W * H + W * H // 4), "output")
+
+    def load_slot(self, slot, planes):
+        W, H = self.width_mbs * 16, self.height_mbs * 16
+        planes = np.ascontiguousarray(planes, np.uint8)
+        base = planes.ctypes.data
+        self.ctx.check(lib().h264r_load_slot(self.h, slot, base, base + W * H, base + W * H + W * H // 4), "load_slot")
+
+    def slot_ptr(self, slot):
+        p = ctypes.c_void_p()
+        self.ctx.check(lib().h264r_slot_device_ptr(self.h, slot, ctypes.byref(p)), "slot_ptr")
+        return p.value
+
+    def cuda_stream(self):
+        return lib().h264r_stream_cuda_stream(self.h)
+
+    def sync(self):
+        return self.ctx.check(lib().h264r_stream_sync(self.h), "stream_sync")
+
+    def close(self):
+        if self.h:
+            lib().h264r_stream_close(self.h)
+            self.h = None
+
+
+class Synth:
+    """Seeded synthetic stream generator (include/h264r_synth.h)."""
+
+    GOP_IPPP, GOP_IBBP = 0, 1
+    WP_NONE, WP_EXPLICIT, WP_IMPLICIT = 0, 1, 2
+
+    def __init__(self, **kw):
+        cfg = R.CSynthCfg()
+        defaults = dict(seed=1, width_mbs=22, height_mbs=18, num_pictures=8, gop_length=15,
+                        gop_kind=0, num_refs=1, transform8x8=0, weighted=0, min_partition=2,
+                        intra_percent=10, skip_percent=10, qp_min=20, qp_max=36,
+                        edge_mv_percent=0, mv_range=64, filter_offset_max=0, coef_density=40)
+        defaults.update(kw)
+        for k, v in defaults.items():
+            setattr(cfg, k, v)
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        rc = lib().h264r_synth_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != 0:
+            raise EngineError(rc, "h264r_synth_create")
+        self.h = h
+
+    @property
+    def dpb_slots(self):
+        return lib().h264r_synth_dpb_slots(self.h)
+
+    def __iter__(self):
+        return self
+
+    def __next__(self):
+        c = R.CPicture()
+        grp = ctypes.c_int()
+        rc = lib().h264r_synth_next(self.h, ctypes.byref(c), ctypes.byref(grp))
+        if rc == 1:
+            raise StopIteration
+        if rc != 0:
+            raise EngineError(rc, "h264r_synth_next")
+        pic = R.Picture.from_c(c)
+        pic.group = grp.value
+        return pic
+
+    def close(self):
+        if self.h:
+            lib().h264r_synth_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# named workloads: the reference's benchmark configurations as synthetic
+# record streams (shapes, sizes and value distributions of each config)
+WORKLOADS = {
+    # CIF 352x288, 8 pictures IPPP, Baseline CAVLC, 1 ref, QP 20..36, 10% I4x4
+    "cif_ippp": dict(width_mbs=22, height_mbs=18, num_pictures=8, gop_kind=0, num_refs=1,
+                     transform8x8=0, weighted=0, min_partition=2, intra_percent=10,
+                     skip_percent=5, qp_min=20, qp_max=36, mv_range=64, filter_offset_max=0),
+    # 1080p High: 1920x1088, 30 pictures, GOP 15 IBBP, 8x8 transform, partitions
+    # to 4x4, 4 refs, explicit weights, MVs +-256 qpel with 5% past the edges,
+    # QP 22..40, alpha/beta offsets +-6
+    "1080p_high": dict(width_mbs=120, height_mbs=68, num_pictures=30, gop_length=15, gop_kind=1,
+                       num_refs=4, transform8x8=1, weighted=1, min_partition=3, intra_percent=5,
+                       skip_percent=10, qp_min=22, qp_max=40, edge_mv_percent=5, mv_range=256,
+                       filter_offset_max=6, coef_density=40),
+    "720p_high": dict(width_mbs=80, height_mbs=45, num_pictures=60, gop_length=15, gop_kind=1,
+                      num_refs=4, transform8x8=1, weighted=2, min_partition=3, intra_percent=5,
+                      skip_percent=10, qp_min=22, qp_max=40, edge_mv_percent=5, mv_range=256,
+                      filter_offset_max=6, coef_density=40),
+}
+
+
+def synth(name, seed=1, **over):
+    kw = dict(WORKLOADS[name])
+    kw.update(over)
+    return Synth(seed=seed, **kw)

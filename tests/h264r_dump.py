@@ -4,25 +4,15 @@ views of the record structures declared in include/h264r.h.
 Test infrastructure: used by the fixture generator, the CPU tests and the GPU
 parity tests.
 """
+import os
 import struct
+import sys
 
 import numpy as np
 
-MB_DTYPE = np.dtype([
-    ("type", "u1"), ("flags", "u1"), ("qpy", "u1"), ("i16_mode", "u1"),
-    ("chroma_mode", "u1"), ("nz8x8", "u1"), ("nz4x4", "<u2"), ("slice", "<u2"),
-    ("reserved", "<u2"), ("ipred", "<u4", (2,)), ("coef", "<u4"), ("aux", "<u4"),
-    ("reserved2", "<u4")])
-SLICE_DTYPE = np.dtype([
-    ("chroma_qp_offset", "i1", (2,)), ("filter_offset_a", "i1"), ("filter_offset_b", "i1"),
-    ("disable_deblocking_filter_idc", "u1"), ("slice_type", "u1"), ("reserved", "u1", (2,))])
-WEIGHT_DTYPE = np.dtype([
-    ("weighted", "i1"), ("log_wd", "i1", (3,)), ("w0", "<i2", (3,)), ("w1", "<i2", (3,)),
-    ("o0", "<i2", (3,)), ("o1", "<i2", (3,)), ("reserved", "<i2", (2,))])
-PART_DTYPE = np.dtype([
-    ("mv", "<i2", (2, 2)), ("ref", "i1", (2,)), ("dref", "i1", (2,)), ("wt", "<u2"), ("reserved", "<u2")])
-assert MB_DTYPE.itemsize == 32 and SLICE_DTYPE.itemsize == 8
-assert WEIGHT_DTYPE.itemsize == 32 and PART_DTYPE.itemsize == 16
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+from h264_video_decoder_demo_gb300.records import MB_DTYPE, PART_DTYPE, SLICE_DTYPE, WEIGHT_DTYPE  # noqa: E402
 
 MAGIC = b"H264RDMP"
 PIC_TAG = 0x31434950
@@ -35,40 +25,24 @@ HDR_SIZE = _HDR1.size + 96 + 384 + _HDR2.size
 HAS_PRE, HAS_POST = 1, 2
 
 
-class Picture:
-    """One picture's records (+ optional reference planes)."""
+from h264_video_decoder_demo_gb300.records import Picture as _RecPicture  # noqa: E402
+
+
+class Picture(_RecPicture):
+    """Records of one picture plus the dump's reference planes."""
 
     def __init__(self):
-        self.width_mbs = self.height_mbs = 0
-        self.structure = self.mbaff = self.dst_slot = 0
-        self.deblock = 1
-        self.scaling4x4 = np.full((6, 16), 16, np.uint8)
-        self.scaling8x8 = np.full((6, 64), 16, np.uint8)
-        self.mbs = np.zeros(0, MB_DTYPE)
-        self.slices = np.zeros(0, SLICE_DTYPE)
-        self.weights = np.zeros(1, WEIGHT_DTYPE)
-        self.motion = np.zeros(0, np.uint8)
-        self.coef = np.zeros(0, np.uint8)
-        self.pcm = np.zeros(0, np.uint8)
+        super().__init__()
         self.poc = self.pic_num_cnt = 0
         self.pre = None
         self.post = None
 
-    @property
-    def plane_bytes(self):
-        return self.width_mbs * self.height_mbs * 384
-
-    def parts(self, addr):
-        """(shape, parts ndarray) of an inter MB's motion payload."""
-        off = int(self.mbs[addr]["aux"])
-        shape, count = struct.unpack_from("<HH", self.motion.tobytes(), off)
-        parts = np.frombuffer(self.motion.tobytes(), PART_DTYPE, count, off + 4)
-        return shape, parts
-
 
 def read_dump(path, max_pictures=None):
+    import gzip
     pics = []
-    with open(path, "rb") as f:
+    opener = gzip.open if path.endswith(".gz") else open
+    with opener(path, "rb") as f:
         if f.read(8) != MAGIC:
             raise ValueError("not a record dump")
         f.read(8)
