@@ -5,6 +5,7 @@
 // on the stream's CUDA stream.
 #include <cuda_runtime.h>
 
+#include <array>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -65,8 +66,10 @@ struct h264r_ctx {
     int *h_error = nullptr;  // pinned
     std::atomic<uint64_t> launches{0};
     bool timing = false;
-    float last_ms[3] = {0, 0, 0};
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double total_ms[3] = {0, 0, 0};
+    int timed_launches = 0;
+    std::vector<std::array<cudaEvent_t, 4>> ev_free, ev_pending;
+    std::mutex timing_mu;
     cudaStream_t batch_stream = nullptr;
     LaunchBuf batch_ring[kRing];
     int batch_next = 0;
@@ -138,7 +141,6 @@ extern "C" int h264r_ctx_create(const h264r_cfg *cfg, h264r_ctx **out)
         delete ctx;
         return H264R_ERR_CUDA;
     }
-    for (auto &ev : ctx->ev) cudaEventCreate(&ev);
     for (auto &b : ctx->batch_ring) cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming);
     *ctx->h_error = 0;
     *out = ctx;
@@ -162,7 +164,9 @@ extern "C" int h264r_ctx_destroy(h264r_ctx *ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->batch_stream);
     for (auto &b : ctx->batch_ring) free_buf(b);
-    for (auto &ev : ctx->ev) cudaEventDestroy(ev);
+    for (auto *pool : {&ctx->ev_free, &ctx->ev_pending})
+        for (auto &q : *pool)
+            for (auto e : q) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->batch_stream);
     cudaFree(ctx->d_error);
     cudaFreeHost(ctx->h_error);
@@ -174,24 +178,56 @@ extern "C" const char *h264r_last_error(const h264r_ctx *ctx) { return ctx ? ctx
 
 extern "C" uint64_t h264r_ctx_kernel_launches(const h264r_ctx *ctx) { return ctx ? ctx->launches.load() : 0; }
 
-extern "C" int h264r_ctx_set_timing(h264r_ctx *ctx, int enable)
+static int drain_timing(h264r_ctx *ctx)
 {
-    if (!ctx) return H264R_ERR_INVALID_ARG;
-    ctx->timing = enable != 0;
+    std::lock_guard<std::mutex> lk(ctx->timing_mu);
+    for (auto &q : ctx->ev_pending) {
+        CUDA_OR(ctx, cudaEventSynchronize(q[3]));
+        float ms;
+        for (int k = 0; k < 3; k++) {
+            cudaEventElapsedTime(&ms, q[k], q[k + 1]);
+            ctx->total_ms[k] += ms;
+        }
+        ctx->timed_launches++;
+        ctx->ev_free.push_back(q);
+    }
+    ctx->ev_pending.clear();
     return H264R_OK;
 }
 
-extern "C" int h264r_ctx_last_timing(h264r_ctx *ctx, float t[3])
+extern "C" int h264r_ctx_set_timing(h264r_ctx *ctx, int enable)
+{
+    if (!ctx) return H264R_ERR_INVALID_ARG;
+    int rc = drain_timing(ctx);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(ctx->timing_mu);
+    ctx->timing = enable != 0;
+    ctx->total_ms[0] = ctx->total_ms[1] = ctx->total_ms[2] = 0;
+    ctx->timed_launches = 0;
+    return H264R_OK;
+}
+
+extern "C" int h264r_ctx_last_timing(h264r_ctx *ctx, float t[3], int *launches)
 {
     if (!ctx || !t) return H264R_ERR_INVALID_ARG;
-    if (ctx->timing) {
-        CUDA_OR(ctx, cudaEventSynchronize(ctx->ev[3]));
-        cudaEventElapsedTime(&ctx->last_ms[0], ctx->ev[0], ctx->ev[1]);
-        cudaEventElapsedTime(&ctx->last_ms[1], ctx->ev[1], ctx->ev[2]);
-        cudaEventElapsedTime(&ctx->last_ms[2], ctx->ev[2], ctx->ev[3]);
-    }
-    memcpy(t, ctx->last_ms, sizeof(ctx->last_ms));
+    int rc = drain_timing(ctx);
+    if (rc) return rc;
+    for (int k = 0; k < 3; k++) t[k] = (float)ctx->total_ms[k];
+    if (launches) *launches = ctx->timed_launches;
     return H264R_OK;
+}
+
+static std::array<cudaEvent_t, 4> *take_events(h264r_ctx *ctx)
+{
+    std::lock_guard<std::mutex> lk(ctx->timing_mu);
+    if (ctx->ev_free.empty()) {
+        std::array<cudaEvent_t, 4> q;
+        for (auto &e : q) cudaEventCreate(&e);
+        ctx->ev_free.push_back(q);
+    }
+    ctx->ev_pending.push_back(ctx->ev_free.back());
+    ctx->ev_free.pop_back();
+    return &ctx->ev_pending.back();
 }
 
 extern "C" int h264r_stream_open(h264r_ctx *ctx, const h264r_stream_cfg *cfg, h264r_stream **out)
@@ -310,6 +346,15 @@ extern "C" int h264r_validate_picture(const h264r_picture *pic, int dpb_slots)
                 nl += __builtin_popcount(s);
             }
             if (m.coef + voff + 2 * nl > pic->coef_bytes) return H264R_ERR_BAD_RECORD;
+            // chroma DC of 4:2:0 has scan positions 0..3 only
+            for (int b = 17; b <= 18; b++) {
+                if (!(mask & (1u << b))) continue;
+                uint32_t before = mask & ((1u << b) - 1u);
+                uint64_t w = __builtin_popcount(before) + (t8 ? 3 * __builtin_popcount(before & 15u) : 0);
+                uint16_t sg;
+                memcpy(&sg, pic->coef + m.coef + 4 + 2 * w, 2);
+                if (sg & 0xFFF0u) return H264R_ERR_BAD_RECORD;
+            }
         }
         if (m.type == H264R_MB_INTER) {
             if (m.aux == H264R_NONE || (m.aux & 3) || (uint64_t)m.aux + 4 > pic->motion_bytes) return H264R_ERR_BAD_RECORD;
@@ -453,21 +498,23 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
     const PicDesc *dd = (const PicDesc *)b.dev;
     bool any_deblock = false;
     for (auto &it : items) any_deblock = any_deblock || it.pic->deblock;
-    if (ctx->timing) cudaEventRecord(ctx->ev[0], cs);
+    std::array<cudaEvent_t, 4> ev{};
+    if (ctx->timing) ev = *take_events(ctx);
+    if (ctx->timing) cudaEventRecord(ev[0], cs);
     h264r::k_inter<<<(unsigned)mbs, 256, 0, cs>>>(dd, n, st);
     ctx->launches++;
-    if (ctx->timing) cudaEventRecord(ctx->ev[1], cs);
+    if (ctx->timing) cudaEventRecord(ev[1], cs);
     if (any_intra) {
         h264r::k_intra<<<(unsigned)rows, 32, 0, cs>>>(dd, n, (uint32_t)rows, st);
         ctx->launches++;
     }
-    if (ctx->timing) cudaEventRecord(ctx->ev[2], cs);
+    if (ctx->timing) cudaEventRecord(ev[2], cs);
     if (any_deblock) {
         h264r::k_bs<<<(unsigned)((mbs + 3) / 4), 128, 0, cs>>>(dd, n, (uint32_t)mbs, st);
         h264r::k_deblock<<<(unsigned)rows, 32, 0, cs>>>(dd, n, (uint32_t)rows, st);
         ctx->launches += 2;
     }
-    if (ctx->timing) cudaEventRecord(ctx->ev[3], cs);
+    if (ctx->timing) cudaEventRecord(ev[3], cs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_err(ctx, "kernel launch: %s", cudaGetErrorString(e));
@@ -570,6 +617,7 @@ static int submit_device(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, int n, h
 static int check_device_pic(h264r_stream *s, const h264r_picture *pic)
 {
     if (!s || !pic || !pic->mbs || !pic->slices || !pic->weights) return H264R_ERR_INVALID_ARG;
+    if (pic->num_slices == 0 || pic->num_weights == 0) return H264R_ERR_BAD_RECORD;
     if (pic->structure != H264R_STRUCT_FRAME) return H264R_ERR_UNSUPPORTED;
     if (pic->width_mbs != s->cfg.width_mbs || pic->height_mbs != s->cfg.height_mbs ||
         pic->num_mbs != (uint32_t)pic->width_mbs * pic->height_mbs || pic->dst_slot >= s->cfg.dpb_slots ||
@@ -689,4 +737,160 @@ extern "C" int h264r_ctx_sync(h264r_ctx *ctx)
     cudaSetDevice(ctx->device);
     CUDA_OR(ctx, cudaDeviceSynchronize());
     return check_device_error(ctx, ctx->batch_stream);
+}
+
+// ---------------------------------------------------------------- host batch
+extern "C" int h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *streams, const h264r_picture *pics)
+{
+    if (!ctx || n <= 0 || !streams || !pics) return H264R_ERR_INVALID_ARG;
+    if ((uint32_t)n > ctx->max_batch) {
+        set_err(ctx, "h264r_submit_batch: %d pictures exceed the batch limit %u", n, ctx->max_batch);
+        return H264R_ERR_BUSY;
+    }
+    for (int i = 0; i < n; i++) {
+        if (!streams[i] || streams[i]->ctx != ctx) return H264R_ERR_INVALID_ARG;
+        int rc = h264r_validate_picture(&pics[i], streams[i]->cfg.dpb_slots);
+        if (rc == H264R_OK && (pics[i].width_mbs != streams[i]->cfg.width_mbs || pics[i].height_mbs != streams[i]->cfg.height_mbs))
+            rc = H264R_ERR_INVALID_ARG;
+        if (rc) {
+            set_err(ctx, "h264r_submit_batch: picture %d rejected (%d)", i, rc);
+            return rc;
+        }
+    }
+    cudaSetDevice(ctx->device);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    LaunchBuf &b = ctx->batch_ring[ctx->batch_next];
+    ctx->batch_next = (ctx->batch_next + 1) % kRing;
+    int rc = wait_slot(ctx, b);
+    if (rc) return rc;
+    // pack every picture's records, then one host -> device copy
+    std::vector<std::array<uint64_t, 7>> offs(n);
+    uint64_t tot = 0;
+    for (int i = 0; i < n; i++) {
+        const h264r_picture *pic = &pics[i];
+        uint64_t sz[7] = {sizeof(h264r_mb) * pic->num_mbs, sizeof(h264r_slice) * pic->num_slices,
+                          sizeof(h264r_weight) * pic->num_weights, pic->motion_bytes, pic->coef_bytes,
+                          384ull * pic->num_pcm, 480};
+        for (int k = 0; k < 7; k++) {
+            offs[i][k] = tot;
+            tot = align_up(tot + sz[k], kAlign);
+        }
+    }
+    rc = ensure(ctx, &b.rec_host, &b.rec_host_cap, tot, true);
+    if (rc) return rc;
+    rc = ensure(ctx, &b.rec_dev, &b.rec_dev_cap, tot, false);
+    if (rc) return rc;
+    std::vector<h264r_picture> dp(pics, pics + n);
+    std::vector<BatchItem> items(n);
+    bool any_intra = false;
+    for (int i = 0; i < n; i++) {
+        const h264r_picture *pic = &pics[i];
+        const void *src[6] = {pic->mbs, pic->slices, pic->weights, pic->motion, pic->coef, pic->pcm};
+        uint64_t sz[6] = {sizeof(h264r_mb) * pic->num_mbs, sizeof(h264r_slice) * pic->num_slices,
+                          sizeof(h264r_weight) * pic->num_weights, pic->motion_bytes, pic->coef_bytes, 384ull * pic->num_pcm};
+        for (int k = 0; k < 6; k++)
+            if (sz[k]) memcpy(b.rec_host + offs[i][k], src[k], sz[k]);
+        memcpy(b.rec_host + offs[i][6], pic->scaling4x4, 96);
+        memcpy(b.rec_host + offs[i][6] + 96, pic->scaling8x8, 384);
+        dp[i].mbs = (const h264r_mb *)(b.rec_dev + offs[i][0]);
+        dp[i].slices = (const h264r_slice *)(b.rec_dev + offs[i][1]);
+        dp[i].weights = (const h264r_weight *)(b.rec_dev + offs[i][2]);
+        dp[i].motion = b.rec_dev + offs[i][3];
+        dp[i].coef = b.rec_dev + offs[i][4];
+        dp[i].pcm = b.rec_dev + offs[i][5];
+        items[i].s = streams[i];
+        items[i].pic = &dp[i];
+        items[i].scaling_dev = b.rec_dev + offs[i][6];
+        items[i].has_intra = has_intra_mbs(pic);
+        any_intra = any_intra || items[i].has_intra;
+    }
+    cudaEvent_t ev;
+    cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    for (int i = 0; i < n; i++) {
+        cudaEventRecord(ev, streams[i]->cs);
+        cudaStreamWaitEvent(ctx->batch_stream, ev, 0);
+    }
+    rc = H264R_OK;
+    if (cudaMemcpyAsync(b.rec_dev, b.rec_host, tot, cudaMemcpyHostToDevice, ctx->batch_stream) != cudaSuccess) {
+        set_err(ctx, "h264r_submit_batch: record upload failed");
+        rc = H264R_ERR_CUDA;
+    }
+    if (rc == H264R_OK) rc = launch(ctx, ctx->batch_stream, b, items, any_intra);
+    if (rc == H264R_OK) {
+        cudaEventRecord(ev, ctx->batch_stream);
+        for (int i = 0; i < n; i++) cudaStreamWaitEvent(streams[i]->cs, ev, 0);
+    }
+    cudaEventDestroy(ev);
+    return rc;
+}
+
+// ---------------------------------------------------------------- accounting
+extern "C" int h264r_picture_bytes(const h264r_picture *pic, uint64_t out[4])
+{
+    if (!pic || !out || !pic->mbs) return H264R_ERR_INVALID_ARG;
+    uint64_t k1 = 0, k2 = 0, k3 = 0, rec = 0;
+    rec = sizeof(h264r_mb) * (uint64_t)pic->num_mbs + pic->motion_bytes + pic->coef_bytes + 384ull * pic->num_pcm +
+          sizeof(h264r_slice) * pic->num_slices + sizeof(h264r_weight) * pic->num_weights;
+    auto coef_len = [&](const h264r_mb &m) -> uint64_t {
+        if (m.coef == H264R_NONE || (uint64_t)m.coef + 4 > pic->coef_bytes) return 0;
+        uint32_t mask;
+        memcpy(&mask, pic->coef + m.coef, 4);
+        int t8 = (m.flags & H264R_MBF_T8x8) != 0;
+        uint64_t nw = __builtin_popcount(mask) + (t8 ? 3 * __builtin_popcount(mask & 15u) : 0);
+        uint64_t nl = 0;
+        for (uint64_t w = 0; w < nw && m.coef + 4 + 2 * w + 2 <= pic->coef_bytes; w++) {
+            uint16_t s;
+            memcpy(&s, pic->coef + m.coef + 4 + 2 * w, 2);
+            nl += __builtin_popcount(s);
+        }
+        return ((4 + 2 * nw + 3) & ~3ull) + 2 * nl;
+    };
+    for (uint32_t a = 0; a < pic->num_mbs; a++) {
+        const h264r_mb &m = pic->mbs[a];
+        uint64_t own = sizeof(h264r_mb) + coef_len(m);
+        if (m.type == H264R_MB_INTER && m.aux != H264R_NONE && (uint64_t)m.aux + 4 <= pic->motion_bytes) {
+            uint16_t hdr[2];
+            memcpy(hdr, pic->motion + m.aux, 4);
+            own += 4 + 16ull * hdr[1];
+            int mp = hdr[0] & 3;
+            for (int e = 0; e < hdr[1] && (uint64_t)m.aux + 4 + 16ull * (e + 1) <= pic->motion_bytes; e++) {
+                h264r_part p;
+                memcpy(&p, pic->motion + m.aux + 4 + 16 * e, 16);
+                int w = 16, h = 16;
+                if (mp == 1) h = 8;
+                else if (mp == 2) w = 8;
+                else if (mp == 3) {
+                    // quadrant of entry e
+                    int base = 0, q = 0, sc = 0;
+                    for (q = 0; q < 4; q++) {
+                        sc = (hdr[0] >> (2 + 2 * q)) & 3;
+                        int cnt = (sc == 0) ? 1 : (sc == 3 ? 4 : 2);
+                        if (e < base + cnt) break;
+                        base += cnt;
+                    }
+                    w = (sc == 0 || sc == 1) ? 8 : 4;
+                    h = (sc == 0 || sc == 2) ? 8 : 4;
+                }
+                for (int l = 0; l < 2; l++) {
+                    if (p.ref[l] < 0) continue;
+                    int fx = p.mv[l][0] & 3, fy = p.mv[l][1] & 3, cx = p.mv[l][0] & 7, cy = p.mv[l][1] & 7;
+                    own += (uint64_t)(w + (fx ? 5 : 0)) * (h + (fy ? 5 : 0));
+                    own += 2ull * (w / 2 + (cx ? 1 : 0)) * (h / 2 + (cy ? 1 : 0));
+                }
+            }
+            k1 += own + 384;
+        } else if (m.type == H264R_MB_IPCM) {
+            k1 += own + 384 + 384;
+        } else if (m.type == H264R_MB_NONE) {
+            k1 += own + 384;
+        } else {
+            k2 += own + 384;
+        }
+        if (pic->deblock) k3 += 768 + sizeof(h264r_mb);
+    }
+    out[0] = k1;
+    out[1] = k2;
+    out[2] = k3;
+    out[3] = rec;
+    return H264R_OK;
 }

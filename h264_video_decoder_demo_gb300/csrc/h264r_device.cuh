@@ -291,6 +291,7 @@ struct CoefView {
     const uint16_t *sig;
     const int16_t *lv;
     int t8;
+    int max_levels;  // levels that fit in the payload buffer
 };
 
 __device__ __forceinline__ bool coef_view(const PicDesc &p, const h264r_mb &m, CoefView &v)
@@ -303,8 +304,11 @@ __device__ __forceinline__ bool coef_view(const PicDesc &p, const h264r_mb &m, C
     v.mask = *(const uint32_t *)base;
     if (v.mask >> 27) return false;
     int nw = __popc(v.mask) + (v.t8 ? 3 * __popc(v.mask & 15u) : 0);
+    uint64_t voff = (uint64_t)m.coef + ((4 + 2 * nw + 3) & ~3);
+    if (voff > p.coef_bytes) return false;
     v.sig = (const uint16_t *)(base + 4);
-    v.lv = (const int16_t *)(base + ((4 + 2 * nw + 3) & ~3));
+    v.lv = (const int16_t *)(p.coef + voff);
+    v.max_levels = (int)((p.coef_bytes - voff) / 2);
     return true;
 }
 
@@ -327,7 +331,7 @@ __device__ __forceinline__ void coef_list16(const CoefView &v, int b, int field,
     coef_block(v, b, w, l);
     uint32_t s = v.sig[w];
     const uint8_t *scan = field ? kField4x4 : kZigzag4x4;
-    while (s) {
+    while (s && l < v.max_levels) {
         int k = __ffs(s) - 1;
         s &= s - 1;
         c[scan[k]] = v.lv[l++];
@@ -365,7 +369,9 @@ struct RefView {
 __device__ __forceinline__ RefView ref_view(const PicDesc &p, int ref)
 {
     RefView r;
-    const uint8_t *base = p.dpb + (uint64_t)(ref & 31) * p.slot_bytes;
+    int slot = ref & 31;
+    if (slot >= p.nslots) slot = 0;  // out-of-range slots are rejected on the host; stay in bounds regardless
+    const uint8_t *base = p.dpb + (uint64_t)slot * p.slot_bytes;
     const uint8_t *cb = base + (size_t)p.W * p.H, *cr = cb + (size_t)p.Wc * p.Hc;
     if (ref & H264R_REF_FIELD) {
         int bot = (ref & H264R_REF_BOTTOM) ? 1 : 0;

@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(256) k_inter(const PicDesc *__restrict__ pics,
                     const uint8_t *scan = field ? kField8x8 : kZigzag8x8;
                     for (int q = 0; q < 4; q++) {
                         uint32_t s = cv.sig[w + q];
-                        while (s) {
+                        while (s && l < cv.max_levels) {
                             int k = __ffs(s) - 1;
                             s &= s - 1;
                             c[scan[16 * q + k]] = cv.lv[l++];
@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(256) k_inter(const PicDesc *__restrict__ pics,
             if (t >= 32 && t < 40 && cv.mask != 0) {
                 // chroma block: plane pl, block b
                 const int pl = (t - 32) >> 2, b = (t - 32) & 3;
-                const int qpc = chroma_qp(m.qpy, p.slices[m.slice].chroma_qp_offset[pl]);
+                const int qpc = chroma_qp(m.qpy, p.slices[min((uint32_t)m.slice, p.num_slices - 1)].chroma_qp_offset[pl]);
                 int32_t dcl[16], dc4[4], dcC[4];
                 coef_list16(cv, 17 + pl, 0, dcl);  // DC list: positions 0..3 in zig-zag order map to raster 0,1,4,8
                 dc4[0] = dcl[0]; dc4[1] = dcl[1]; dc4[2] = dcl[4]; dc4[3] = dcl[8];
@@ -420,7 +420,7 @@ __device__ void intra_mb(const PicDesc &p, int addr, IntraSmem &s, const LaunchS
             const uint8_t *scan = field ? kField8x8 : kZigzag8x8;
             for (int q = 0; q < 4; q++) {
                 uint32_t sg = cv.sig[w + q];
-                while (sg) {
+                while (sg && l < cv.max_levels) {
                     int k = __ffs(sg) - 1;
                     sg &= sg - 1;
                     c[scan[16 * q + k]] = cv.lv[l++];
@@ -445,7 +445,7 @@ __device__ void intra_mb(const PicDesc &p, int addr, IntraSmem &s, const LaunchS
     }
     if (lane >= 16 && lane < 24 && cv.mask != 0) {
         const int pl = (lane - 16) >> 2, b = (lane - 16) & 3;
-        const int qpc = chroma_qp(qp, p.slices[m.slice].chroma_qp_offset[pl]);
+        const int qpc = chroma_qp(qp, p.slices[min((uint32_t)m.slice, p.num_slices - 1)].chroma_qp_offset[pl]);
         int32_t dcl[16], dc4[4], dcC[4];
         coef_list16(cv, 17 + pl, 0, dcl);
         dc4[0] = dcl[0]; dc4[1] = dcl[1]; dc4[2] = dcl[4]; dc4[3] = dcl[8];
@@ -684,10 +684,10 @@ __device__ __forceinline__ void get_motion(const PicDesc &p, int addr, int xq, i
     o.mv[0][0] = o.mv[0][1] = o.mv[1][0] = o.mv[1][1] = 0;
     o.pf[0] = o.pf[1] = 0;
     o.id[0] = o.id[1] = -1;
-    if (m.type != H264R_MB_INTER || m.aux == H264R_NONE) return;
+    if (m.type != H264R_MB_INTER || m.aux == H264R_NONE || (m.aux & 3) || (uint64_t)m.aux + 4 > p.motion_bytes) return;
     uint32_t hdr = *(const uint32_t *)(p.motion + m.aux);
     int e = part_of_block(hdr & 0xFFFF, xq >> 2, yq >> 2);
-    if (e >= (int)(hdr >> 16)) return;
+    if (e >= (int)(hdr >> 16) || (uint64_t)m.aux + 4 + 16ull * (e + 1) > p.motion_bytes) return;
     const h264r_part pp = ((const h264r_part *)(p.motion + m.aux + 4))[e];
     for (int l = 0; l < 2; l++) {
         o.mv[l][0] = pp.mv[l][0];
@@ -708,7 +708,8 @@ __device__ int derive_bs(const PicDesc &p, int mbP, int mbQ, int xp, int yp, int
     int fP = (P.flags & H264R_MBF_FIELD) && mbaff, fQ = (Q.flags & H264R_MBF_FIELD) && mbaff;
     int mixed = mbaff && mbP != mbQ && fP != fQ;
     bool intraP = is_intra_type(P.type), intraQ = is_intra_type(Q.type);
-    int stP = p.slices[P.slice].slice_type, stQ = p.slices[Q.slice].slice_type;
+    int stP = p.slices[min((uint32_t)P.slice, p.num_slices - 1)].slice_type;
+    int stQ = p.slices[min((uint32_t)Q.slice, p.num_slices - 1)].slice_type;
     bool spP = stP == 3 || stP == 4, spQ = stQ == 3 || stQ == 4;
     if (mbP != mbQ) {
         if ((!fP && !fQ && (intraP || intraQ)) || (!fP && !fQ && (spP || spQ)) || (mbaff && vertical && (intraP || intraQ)) ||
@@ -764,7 +765,7 @@ __device__ __forceinline__ EdgeCtl edge_ctl(const PicDesc &p, int cur)
     e.mbB = nb_loc(p, cur, 0, -1, 16, 16, xW, yW);
     const int W = p.wmb, mbaff = p.mbaff;
     e.field = mbaff && (m.flags & H264R_MBF_FIELD);
-    int idc = p.slices[m.slice].disable_deblocking_filter_idc;
+    int idc = p.slices[min((uint32_t)m.slice, p.num_slices - 1)].disable_deblocking_filter_idc;
     e.internal = idc != 1;
     e.left = !((!mbaff && cur % W == 0) || (mbaff && (cur >> 1) % W == 0) || idc == 1 || (idc == 2 && e.mbA < 0));
     e.top = !((!mbaff && cur < W) || (mbaff && (cur >> 1) < W && e.field) || (mbaff && (cur >> 1) < W && !e.field && (cur % 2) == 0) ||
@@ -950,7 +951,7 @@ __device__ __forceinline__ void edge_line(const PicDesc &p, int cur, int comp, i
         if ((yE - 1) - (yE % 2) < 0 && mbN >= 0) mbP = mbN;
     }
     const h264r_mb P = p.mbs[mbP], Q = p.mbs[cur];
-    const h264r_slice sq = p.slices[Q.slice];
+    const h264r_slice sq = p.slices[min((uint32_t)Q.slice, p.num_slices - 1)];
     int qPp, qPq;
     if (!chroma) {
         qPp = P.type == H264R_MB_IPCM ? 0 : P.qpy;

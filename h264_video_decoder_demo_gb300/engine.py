@@ -23,6 +23,7 @@ EXPORTS = [
     "h264r_stream_cuda_stream", "h264r_validate_picture", "h264r_ctx_kernel_launches",
     "h264r_ctx_set_timing", "h264r_ctx_last_timing",
     "h264r_synth_create", "h264r_synth_dpb_slots", "h264r_synth_next", "h264r_synth_destroy",
+    "h264r_submit_batch", "h264r_picture_bytes",
 ]
 
 
@@ -62,7 +63,9 @@ def lib():
         "h264r_validate_picture": (i32, [P(R.CPicture), i32]),
         "h264r_ctx_kernel_launches": (u64, [vp]),
         "h264r_ctx_set_timing": (i32, [vp, i32]),
-        "h264r_ctx_last_timing": (i32, [vp, P(ctypes.c_float)]),
+        "h264r_ctx_last_timing": (i32, [vp, P(ctypes.c_float), P(i32)]),
+        "h264r_submit_batch": (i32, [vp, i32, P(vp), P(R.CPicture)]),
+        "h264r_picture_bytes": (i32, [P(R.CPicture), P(ctypes.c_uint64)]),
         "h264r_synth_create": (i32, [P(R.CSynthCfg), P(vp)]),
         "h264r_synth_dpb_slots": (i32, [vp]),
         "h264r_synth_next": (i32, [vp, P(R.CPicture), P(i32)]),
@@ -74,6 +77,16 @@ def lib():
         f.argtypes = args
     _LIB = L
     return L
+
+
+def picture_bytes(pic):
+    """Algorithmic bytes [inter, intra, deblock, records] of a Picture."""
+    c = pic.to_c()
+    out = (ctypes.c_uint64 * 4)()
+    rc = lib().h264r_picture_bytes(ctypes.byref(c), out)
+    if rc != 0:
+        raise EngineError(rc, "h264r_picture_bytes")
+    return list(out)
 
 
 def validate(pic, dpb_slots):
@@ -107,12 +120,21 @@ class Context:
         self.check(lib().h264r_ctx_set_timing(self.h, 1 if on else 0), "set_timing")
 
     def last_timing(self):
+        """(summed ms of [inter, intra, deblock], launch sequences) since set_timing(True)."""
         t = (ctypes.c_float * 3)()
-        self.check(lib().h264r_ctx_last_timing(self.h, t), "last_timing")
-        return list(t)
+        n = ctypes.c_int()
+        self.check(lib().h264r_ctx_last_timing(self.h, t, ctypes.byref(n)), "last_timing")
+        return list(t), n.value
 
     def sync(self):
         return self.check(lib().h264r_ctx_sync(self.h), "ctx_sync")
+
+    def submit_batch(self, streams, pics):
+        """Batched reconstruction from host records (list of Picture)."""
+        n = len(streams)
+        arr = (ctypes.c_void_p * n)(*[s.h.value for s in streams])
+        cpics = (R.CPicture * n)(*[p.to_c() for p in pics])
+        return self.check(lib().h264r_submit_batch(self.h, n, arr, cpics), "submit_batch")
 
     def submit_batch_device(self, streams, cpics):
         n = len(streams)

@@ -260,6 +260,25 @@ int  h264r_submit_batch_device(h264r_ctx *ctx, int n, h264r_stream *const *strea
                                const h264r_picture *pics);
 
 /*
+ * Batched reconstruction from host-resident records: the records of all n
+ * pictures are packed into pinned staging memory and copied to the device
+ * in one transfer, then reconstructed in one fused launch sequence (same
+ * rules as h264r_submit_batch_device).
+ */
+int  h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *streams, const h264r_picture *pics);
+
+/*
+ * Algorithmic bytes of one picture per engine stage, for roofline
+ * accounting: out[0] inter stage (records read + reference samples + 384
+ * output bytes per inter / I_PCM MB), out[1] intra stage (records + 384 per
+ * intra MB), out[2] deblocking (768 per MB + 32 record bytes), out[3] all
+ * record bytes.  Reference samples per partition and list:
+ * (w + 5*[xFrac!=0]) * (h + 5*[yFrac!=0]) luma plus
+ * 2 * (w/2 + [xFracC!=0]) * (h/2 + [yFracC!=0]) chroma.  Host pointers.
+ */
+int  h264r_picture_bytes(const h264r_picture *pic, uint64_t out[4]);
+
+/*
  * Copy a decoded picture (DPB slot) to host planes at coded size: luma
  * width_mbs*16 x height_mbs*16, chroma half in each direction.  Replaces the
  * borrowed CH264Picture the reference hands to its output callback
@@ -283,10 +302,14 @@ int  h264r_validate_picture(const h264r_picture *pic, int dpb_slots);
 /* Number of engine kernels launched so far by this context. */
 uint64_t h264r_ctx_kernel_launches(const h264r_ctx *ctx);
 
-/* Device timing of the kernels of the last submitted picture / batch, in ms:
- * t[0] inter, t[1] intra, t[2] deblock (0 when timing is disabled). */
+/* Device timing of the engine's kernels, measured with CUDA events on the
+ * stream each kernel runs on.  h264r_ctx_set_timing(ctx, 1) clears the
+ * totals and starts recording; h264r_ctx_last_timing waits for the recorded
+ * launches and returns the summed milliseconds since then: t[0] inter,
+ * t[1] intra, t[2] deblocking (bS + filter); *launches receives the number
+ * of launch sequences summed. */
 int  h264r_ctx_set_timing(h264r_ctx *ctx, int enable);
-int  h264r_ctx_last_timing(h264r_ctx *ctx, float t[3]);
+int  h264r_ctx_last_timing(h264r_ctx *ctx, float t[3], int *launches);
 
 #ifdef __cplusplus
 }
