@@ -1,0 +1,437 @@
+#!/usr/bin/env python3
+"""Benchmark: 1080p decoded frames/s of the GB300 reconstruction engine.
+
+Workload (the reference's 1080p High configuration as seeded synthetic
+record streams): S independent streams of 1920x1088, 30 pictures each, GOP
+15 IBBP, 8x8 transforms, partitions down to 4x4, 4 reference pictures,
+explicit weighted prediction, MVs +-256 quarter samples with 5% past the
+picture edges, QP 22..40, alpha/beta offsets +-6.  Seeds 1000 + stream.
+
+One step reconstructs every picture of every stream (30 * S frames): the
+pictures of all streams that do not reference each other go into one
+batched launch sequence (inter -> intra wavefront -> bS -> deblocking
+wavefront), batches in decoding order.
+
+  value     records resident in HBM, batched path, CUDA events on the
+            engine's batch stream
+  e2e       host records through h264r_submit_batch (pinned staging + H2D)
+            and every decoded frame copied back to pinned host memory
+  plain_fps one picture per launch sequence with a host sync after each
+  cpu_baseline  the CPU oracle (a restatement of the reference's
+            reconstruction) on a bounded sample, one host core
+  --impl reference  that CPU implementation with every host core
+
+Prints one JSON line (rank 0).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+METRIC = "1080p decoded fps (bit-exact): batched/served vs plain GPU path; p99 frame ms"
+WORKLOAD = "1080p_high"
+FRAME_BYTES = 1920 * 1088 * 3 // 2
+SEED_BASE = 1000  # configuration index 1 * 1000
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--streams", type=int, default=16)
+    ap.add_argument("--pictures", type=int, default=30)
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (quick runs)")
+    return ap.parse_args()
+
+
+def gen_streams(n, pictures, seed0):
+    """Records of n seeded streams (generated in parallel; the generator is C)."""
+    import h264_video_decoder_demo_gb300 as h
+    h.lib()
+    out = [None] * n
+    slots = [0] * n
+    errors = []
+
+    def work(i):
+        try:
+            g = h.synth(WORKLOAD, seed=seed0 + i, num_pictures=pictures)
+            out[i] = list(g)
+            slots[i] = g.dpb_slots
+            g.close()
+        except Exception as exc:  # surfaced below
+            errors.append(exc)
+
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(n)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if errors:
+        raise errors[0]
+    return out, slots
+
+
+def oracle_sample(pics, slots, seconds, check=None):
+    """Time the CPU oracle on pictures in decoding order (one thread) until
+    `seconds` of work; optionally compare each picture with check(i)."""
+    from oracle_cpu import OracleDPB
+    p0 = pics[0]
+    dpb = OracleDPB(p0.width_mbs, p0.height_mbs, slots)
+    n, t0, exact = 0, time.perf_counter(), True
+    for i, p in enumerate(pics):
+        rc, _ = dpb.reconstruct(p)
+        if rc != 0:
+            raise RuntimeError("oracle error %d" % rc)
+        n += 1
+        if check is not None:
+            exact = exact and check(i, dpb.planes(p.dst_slot))
+        if time.perf_counter() - t0 > seconds:
+            break
+    return n, time.perf_counter() - t0, exact
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.proc = None
+        self.device = device
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except (ValueError, IndexError):
+                continue
+            for k, name in enumerate(names):
+                if len(f) > 3 + k and f[3 + k].lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if args.impl == "engine" else "gloo")
+    return world, rank, local, dist
+
+
+def run_reference(args, rank):
+    """The CPU implementation of the path (the oracle port) on every host core."""
+    if rank != 0:
+        return None
+    cores = os.cpu_count() or 1
+    pics, slots = gen_streams(cores, args.pictures, SEED_BASE)
+    from oracle_cpu import OracleDPB
+    dpbs = [OracleDPB(p[0].width_mbs, p[0].height_mbs, s) for p, s in zip(pics, slots)]
+    cursor = [0] * cores
+
+    def step():
+        def work(i):
+            k = cursor[i] % len(pics[i])
+            if k == 0:
+                dpbs[i] = OracleDPB(pics[i][0].width_mbs, pics[i][0].height_mbs, slots[i])
+            rc, _ = dpbs[i].reconstruct(pics[i][k])
+            if rc != 0:
+                raise RuntimeError("oracle error %d" % rc)
+            cursor[i] += 1
+        th = [threading.Thread(target=work, args=(i,)) for i in range(cores)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    fps = cores * args.steps / dt
+    sample = "%d streams x %d pictures of %s, one 1080p picture per core per step" % (cores, args.steps, WORKLOAD)
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(fps, 3), "unit": "frames/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * dt / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (seeded 1080p High records; CPU restatement of the reference's reconstruction)",
+        "config": {"workload": WORKLOAD, "streams": cores, "pictures_per_stream": args.pictures, "threads": cores},
+        "cpu_baseline": {"value": round(fps, 3), "unit": "frames/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": round(fps, 3), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def run_engine(args, world, rank, local, dist):
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import h264_video_decoder_demo_gb300 as h
+    from h264_video_decoder_demo_gb300 import records as R
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    S = args.streams
+    streams_pics, slots = gen_streams(S, args.pictures, SEED_BASE + 100 * rank)
+    ngroups = max(p.group for p in streams_pics[0]) + 1
+    ctx = h.Context(local, max_batch=4 * S)
+    streams = [h.Stream(ctx, 120, 68, slots[i]) for i in range(S)]
+
+    # ---- records resident in HBM
+    keep = []
+    cpics = []  # per stream, per picture: CPicture with device pointers
+    algo = np.zeros(4, np.int64)  # bytes per step: inter, intra, deblock, records
+    rec_bytes = 0
+    for i in range(S):
+        row = []
+        for p in streams_pics[i]:
+            algo += np.array(h.engine.picture_bytes(p), np.int64)
+            c = p.to_c()
+            parts = []
+            for name in R.Picture._ARRAYS:
+                a = np.ascontiguousarray(getattr(p, name)).view(np.uint8).reshape(-1)
+                t = torch.from_numpy(a.copy()).to(dev) if a.size else torch.empty(1, dtype=torch.uint8, device=dev)
+                keep.append(t)
+                setattr(c, name, t.data_ptr())
+                rec_bytes += a.size
+            row.append(c)
+        cpics.append(row)
+    batches = []
+    for g in range(ngroups):
+        ss, cc = [], []
+        for i in range(S):
+            for k, p in enumerate(streams_pics[i]):
+                if p.group == g:
+                    ss.append(streams[i])
+                    cc.append(cpics[i][k])
+        batches.append((ss, cc))
+    frames_per_step = S * args.pictures
+    cs = torch.cuda.ExternalStream(ctx.cuda_stream(), device=dev)
+
+    def step(evs=None):
+        for bi, (ss, cc) in enumerate(batches):
+            if evs is not None:
+                evs[bi][0].record(cs)
+            rc = ctx.submit_batch_device(ss, cc)
+            if rc != 0:
+                raise RuntimeError("submit_batch_device: %d %s" % (rc, ctx.last_error()))
+            if evs is not None:
+                evs[bi][1].record(cs)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+
+    # ---- timed region
+    launches0 = ctx.kernel_launches()
+    batch_evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in batches]
+                 for _ in range(args.steps)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.set_timing(True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        start.record(cs)
+        for k in range(args.steps):
+            step(batch_evs[k])
+        end.record(cs)
+        torch.cuda.synchronize()
+    ctx.sync()
+    if dist:
+        dist.barrier()
+    elapsed_ms = start.elapsed_time(end)
+    launches = ctx.kernel_launches() - launches0
+    ktimes, nlaunch = ctx.last_timing()
+    ctx.set_timing(False)
+    if dist:
+        t = torch.tensor([elapsed_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    lat = sorted(b[0].elapsed_time(b[1]) for stepev in batch_evs for b in stepev)
+    value = world * frames_per_step * args.steps / (elapsed_ms / 1000.0)
+
+    # ---- roofline of the dominant kernel
+    names = ["k_inter", "k_intra", "k_deblock"]
+    dom = int(np.argmax(ktimes))
+    per_kernel_bytes = algo[:3] * args.steps
+    achieved = per_kernel_bytes[dom] / (ktimes[dom] / 1000.0) / 1e9 if ktimes[dom] > 0 else 0.0
+    peak, peak_kind = peak_hbm()
+    tr = ncu_traffic().get(names[dom])
+    traffic = None
+    if tr and "bytes_per_frame" in tr:
+        traffic = int(tr["bytes_per_frame"] * frames_per_step / len(batches))
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
+                "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                "algorithmic_bytes_per_launch": int(per_kernel_bytes[dom] / (args.steps * len(batches))),
+                "kernel_ms_per_step": [round(t / args.steps, 3) for t in ktimes]}
+
+    extra = {}
+    if rank == 0:
+        # ---- plain path: one picture per launch sequence, host sync after each
+        s0 = h.Stream(ctx, 120, 68, slots[0])
+        for c in cpics[0][:3]:
+            s0.submit_device(c)
+            s0.sync()
+        t0 = time.perf_counter()
+        nplain = 0
+        for rep in range(2):
+            for c in cpics[0]:
+                s0.submit_device(c)
+                s0.sync()
+                nplain += 1
+        plain_fps = nplain / (time.perf_counter() - t0)
+        # ---- bit-exactness of stream 0 against the CPU oracle (also the CPU baseline sample)
+        s0.close()
+        s1 = h.Stream(ctx, 120, 68, slots[0])
+        gpu_frames = []
+        for p in streams_pics[0]:
+            s1.submit(p)
+            gpu_frames.append(s1.output(p.dst_slot).copy())
+        s1.close()
+        if args.skip_cpu:
+            cpu = None
+            exact = None
+        else:
+            n, dt, exact = oracle_sample(streams_pics[0], slots[0], 20.0,
+                                         check=lambda i, planes: bool(np.array_equal(gpu_frames[i], planes)))
+            cpu = {"value": round(n / dt, 3), "unit": "frames/s", "cores": 1, "kind": "port",
+                   "sample": "%d pictures of stream 0 (%s, seed %d) in decoding order" % (n, WORKLOAD, SEED_BASE)}
+        # ---- end to end: host records, pinned staging + H2D, every frame back to pinned host memory
+        pinned = [[torch.empty(FRAME_BYTES, dtype=torch.uint8, pin_memory=True).numpy() for _ in range(3)] for _ in range(S)]
+        e2e_steps = 2
+        h2d = int(sum(p.record_bytes for ps in streams_pics for p in ps))
+        torch.cuda.synchronize()
+        ctx.sync()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            for g in range(ngroups):
+                ss, pp, bufs = [], [], []
+                for i in range(S):
+                    k = 0
+                    for p in streams_pics[i]:
+                        if p.group == g:
+                            ss.append(streams[i])
+                            pp.append(p)
+                            bufs.append(pinned[i][k % 3])
+                            k += 1
+                ctx.submit_batch(ss, pp)
+                for st, p, buf in zip(ss, pp, bufs):
+                    st.output_async(p.dst_slot, buf)
+            for st in streams:
+                st.sync()
+        ctx.sync()
+        e2e_dt = time.perf_counter() - t0
+        e2e = {"value": round(frames_per_step * e2e_steps / e2e_dt, 2), "unit": "frames/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": frames_per_step * FRAME_BYTES}
+        extra = {"plain_fps": round(plain_fps, 2), "cpu_baseline": cpu, "e2e": e2e, "bit_exact_sample": exact}
+
+    for s in streams:
+        s.close()
+    ctx.close()
+    if rank != 0:
+        return None
+    mbs = 120 * 68
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(elapsed_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (seeded 1080p High record streams, shapes and distributions of the reference's 1080p config)",
+        "config": {"workload": WORKLOAD, "streams_per_gpu": S, "pictures_per_stream": args.pictures,
+                   "batches_per_step": len(batches), "frames_per_step": frames_per_step,
+                   "coded_size": "1920x1088", "gop": "15, IBBP", "refs": 4, "weighted_prediction": "explicit",
+                   "l2": "inputs larger than L2 (%.0f MB of records + %.0f MB of DPB per GPU)" %
+                         (rec_bytes / 1e6, sum(slots) * FRAME_BYTES / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "mb_per_s": round(value * mbs, 1),
+        "p50_frame_ms": round(statistics.median(lat), 3), "p99_frame_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
+        "frame_latency_note": "device time of the batched launch sequence that reconstructs the frame",
+        "roofline": roofline,
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    out.update(extra)
+    if out.get("plain_fps"):
+        out["batched_over_plain"] = round(value / world / out["plain_fps"], 2)
+    return out
+
+
+def main():
+    args = parse()
+    world, rank, local, dist = dist_setup(args)
+    if args.impl == "reference":
+        res = run_reference(args, rank)
+    else:
+        res = run_engine(args, world, rank, local, dist)
+    if res is not None and rank == 0:
+        print(json.dumps(res), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -286,6 +286,8 @@ extern "C" int h264r_stream_close(h264r_stream *s)
 
 extern "C" void *h264r_stream_cuda_stream(h264r_stream *s) { return s ? (void *)s->cs : nullptr; }
 
+extern "C" void *h264r_ctx_cuda_stream(h264r_ctx *ctx) { return ctx ? (void *)ctx->batch_stream : nullptr; }
+
 extern "C" int h264r_slot_device_ptr(h264r_stream *s, int slot, void **dev_y)
 {
     if (!s || !dev_y || slot < 0 || slot >= s->cfg.dpb_slots) return H264R_ERR_INVALID_ARG;

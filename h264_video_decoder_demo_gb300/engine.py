@@ -6,12 +6,14 @@ is missing, loading fails with an error that says how to build it.
 """
 import ctypes
 import os
+import threading
 
 import numpy as np
 
 from . import records as R
 
 _LIB = None
+_LIB_LOCK = threading.Lock()
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libh264r.so")
 
 # every symbol include/h264r.h and include/h264r_synth.h declare
@@ -23,7 +25,7 @@ EXPORTS = [
     "h264r_stream_cuda_stream", "h264r_validate_picture", "h264r_ctx_kernel_launches",
     "h264r_ctx_set_timing", "h264r_ctx_last_timing",
     "h264r_synth_create", "h264r_synth_dpb_slots", "h264r_synth_next", "h264r_synth_destroy",
-    "h264r_submit_batch", "h264r_picture_bytes",
+    "h264r_submit_batch", "h264r_picture_bytes", "h264r_ctx_cuda_stream",
 ]
 
 
@@ -38,6 +40,13 @@ def lib():
     global _LIB
     if _LIB is not None:
         return _LIB
+    with _LIB_LOCK:
+        if _LIB is None:
+            _LIB = _load()
+    return _LIB
+
+
+def _load():
     if not os.path.exists(LIB_PATH):
         raise ImportError("libh264r.so is not built: run `python -m h264_video_decoder_demo_gb300.build` "
                           "(or __graft_entry__.build()) first")
@@ -60,6 +69,7 @@ def lib():
         "h264r_stream_sync": (i32, [vp]),
         "h264r_ctx_sync": (i32, [vp]),
         "h264r_stream_cuda_stream": (vp, [vp]),
+        "h264r_ctx_cuda_stream": (vp, [vp]),
         "h264r_validate_picture": (i32, [P(R.CPicture), i32]),
         "h264r_ctx_kernel_launches": (u64, [vp]),
         "h264r_ctx_set_timing": (i32, [vp, i32]),
@@ -75,7 +85,6 @@ def lib():
         f = getattr(L, name)
         f.restype = res
         f.argtypes = args
-    _LIB = L
     return L
 
 
@@ -128,6 +137,10 @@ class Context:
 
     def sync(self):
         return self.check(lib().h264r_ctx_sync(self.h), "ctx_sync")
+
+    def cuda_stream(self):
+        """cudaStream_t (int) of the context's batch stream."""
+        return lib().h264r_ctx_cuda_stream(self.h)
 
     def submit_batch(self, streams, pics):
         """Batched reconstruction from host records (list of Picture)."""

@@ -294,6 +294,8 @@ int  h264r_stream_sync(h264r_stream *s);
 int  h264r_ctx_sync(h264r_ctx *ctx);
 /* The CUDA stream the engine enqueues this stream's work on (cudaStream_t). */
 void *h264r_stream_cuda_stream(h264r_stream *s);
+/* The CUDA stream batched launches of the context run on (cudaStream_t). */
+void *h264r_ctx_cuda_stream(h264r_ctx *ctx);
 
 /* Validate a picture's records on the host (ranges, offsets, payload sizes).
  * Returns 0 or H264R_ERR_BAD_RECORD / H264R_ERR_UNSUPPORTED. */
