@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--streams", type=int, default=16)
     ap.add_argument("--pictures", type=int, default=30)
+    ap.add_argument("--pipelines", type=int, default=2, help="concurrent batch pipelines over disjoint stream sets")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (quick runs)")
     return ap.parse_args()
 
@@ -260,27 +261,34 @@ def run_engine(args, world, rank, local, dist):
                 rec_bytes += a.size
             row.append(c)
         cpics.append(row)
-    batches = []
+    # two pipelines over disjoint stream sets: the batches of one overlap
+    # the other's (each batch runs on its first member's CUDA stream)
+    npipe = max(1, min(args.pipelines, S))
+    sets = [list(range(j, S, npipe)) for j in range(npipe)]
+    batches = []  # (pipeline, streams, device pictures, host pictures)
     for g in range(ngroups):
-        ss, cc = [], []
-        for i in range(S):
-            for k, p in enumerate(streams_pics[i]):
-                if p.group == g:
-                    ss.append(streams[i])
-                    cc.append(cpics[i][k])
-        batches.append((ss, cc))
+        for j, idxs in enumerate(sets):
+            ss, cc, hp = [], [], []
+            for i in idxs:
+                for k, p in enumerate(streams_pics[i]):
+                    if p.group == g:
+                        ss.append(streams[i])
+                        cc.append(cpics[i][k])
+                        hp.append(p)
+            batches.append((j, ss, cc, hp))
     frames_per_step = S * args.pictures
-    cs = torch.cuda.ExternalStream(ctx.cuda_stream(), device=dev)
+    pipes = [torch.cuda.ExternalStream(streams[idxs[0]].cuda_stream(), device=dev) for idxs in sets]
+    cs = pipes[0]
 
     def step(evs=None):
-        for bi, (ss, cc) in enumerate(batches):
+        for bi, (j, ss, cc, _) in enumerate(batches):
             if evs is not None:
-                evs[bi][0].record(cs)
+                evs[bi][0].record(pipes[j])
             rc = ctx.submit_batch_device(ss, cc)
             if rc != 0:
                 raise RuntimeError("submit_batch_device: %d %s" % (rc, ctx.last_error()))
             if evs is not None:
-                evs[bi][1].record(cs)
+                evs[bi][1].record(pipes[j])
 
     for _ in range(args.warmup):
         step()
@@ -297,8 +305,14 @@ def run_engine(args, world, rank, local, dist):
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         start.record(cs)
+        for q in pipes[1:]:
+            q.wait_event(start)
         for k in range(args.steps):
             step(batch_evs[k])
+        for q in pipes[1:]:
+            ev = torch.cuda.Event()
+            ev.record(q)
+            cs.wait_event(ev)
         end.record(cs)
         torch.cuda.synchronize()
     ctx.sync()
@@ -369,19 +383,13 @@ def run_engine(args, world, rank, local, dist):
         ctx.sync()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            for g in range(ngroups):
-                ss, pp, bufs = [], [], []
-                for i in range(S):
-                    k = 0
-                    for p in streams_pics[i]:
-                        if p.group == g:
-                            ss.append(streams[i])
-                            pp.append(p)
-                            bufs.append(pinned[i][k % 3])
-                            k += 1
+            for j, ss, _, pp in batches:
                 ctx.submit_batch(ss, pp)
-                for st, p, buf in zip(ss, pp, bufs):
-                    st.output_async(p.dst_slot, buf)
+                seen = {}
+                for st, p in zip(ss, pp):
+                    k = seen.get(id(st), 0)
+                    seen[id(st)] = k + 1
+                    st.output_async(p.dst_slot, pinned[streams.index(st)][k % 3])
             for st in streams:
                 st.sync()
         ctx.sync()
@@ -406,6 +414,7 @@ def run_engine(args, world, rank, local, dist):
                    "coded_size": "1920x1088", "gop": "15, IBBP", "refs": 4, "weighted_prediction": "explicit",
                    "l2": "inputs larger than L2 (%.0f MB of records + %.0f MB of DPB per GPU)" %
                          (rec_bytes / 1e6, sum(slots) * FRAME_BYTES / 1e6),
+                   "pipelines": npipe,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "mb_per_s": round(value * mbs, 1),
         "p50_frame_ms": round(statistics.median(lat), 3), "p99_frame_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),

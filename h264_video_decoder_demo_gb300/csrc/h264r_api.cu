@@ -17,7 +17,7 @@
 #include "h264r_device.cuh"
 
 namespace h264r {
-__global__ void k_inter(const PicDesc *__restrict__ pics, int npics, LaunchState st);
+__global__ void k_inter(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
 __global__ void k_intra(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st);
 __global__ void k_bs(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
 __global__ void k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st);
@@ -503,7 +503,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
     std::array<cudaEvent_t, 4> ev{};
     if (ctx->timing) ev = *take_events(ctx);
     if (ctx->timing) cudaEventRecord(ev[0], cs);
-    h264r::k_inter<<<(unsigned)mbs, 256, 0, cs>>>(dd, n, st);
+    h264r::k_inter<<<(unsigned)((mbs + 3) / 4), 128, 0, cs>>>(dd, n, (uint32_t)mbs, st);
     ctx->launches++;
     if (ctx->timing) cudaEventRecord(ev[1], cs);
     if (any_intra) {
@@ -666,18 +666,21 @@ extern "C" int h264r_submit_batch_device(h264r_ctx *ctx, int n, h264r_stream *co
     ctx->batch_next = (ctx->batch_next + 1) % kRing;
     int rc = wait_slot(ctx, b);
     if (rc) return rc;
-    // the batch runs on the context's batch stream, after any work already
-    // queued on the member streams, and the member streams wait for it
+    // the batch runs on the CUDA stream of its first member, after any work
+    // already queued on the other members, which then wait for it
+    cudaStream_t cs = streams[0]->cs;
     cudaEvent_t ev;
     cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-    for (int i = 0; i < n; i++) {
+    for (int i = 1; i < n; i++) {
+        if (streams[i]->cs == cs) continue;
         cudaEventRecord(ev, streams[i]->cs);
-        cudaStreamWaitEvent(ctx->batch_stream, ev, 0);
+        cudaStreamWaitEvent(cs, ev, 0);
     }
-    rc = submit_device(ctx, ctx->batch_stream, b, n, streams, pics);
+    rc = submit_device(ctx, cs, b, n, streams, pics);
     if (rc == H264R_OK) {
-        cudaEventRecord(ev, ctx->batch_stream);
-        for (int i = 0; i < n; i++) cudaStreamWaitEvent(streams[i]->cs, ev, 0);
+        cudaEventRecord(ev, cs);
+        for (int i = 1; i < n; i++)
+            if (streams[i]->cs != cs) cudaStreamWaitEvent(streams[i]->cs, ev, 0);
     }
     cudaEventDestroy(ev);
     return rc;
@@ -806,21 +809,24 @@ extern "C" int h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *st
         items[i].has_intra = has_intra_mbs(pic);
         any_intra = any_intra || items[i].has_intra;
     }
+    cudaStream_t cs = streams[0]->cs;
     cudaEvent_t ev;
     cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-    for (int i = 0; i < n; i++) {
+    for (int i = 1; i < n; i++) {
+        if (streams[i]->cs == cs) continue;
         cudaEventRecord(ev, streams[i]->cs);
-        cudaStreamWaitEvent(ctx->batch_stream, ev, 0);
+        cudaStreamWaitEvent(cs, ev, 0);
     }
     rc = H264R_OK;
-    if (cudaMemcpyAsync(b.rec_dev, b.rec_host, tot, cudaMemcpyHostToDevice, ctx->batch_stream) != cudaSuccess) {
+    if (cudaMemcpyAsync(b.rec_dev, b.rec_host, tot, cudaMemcpyHostToDevice, cs) != cudaSuccess) {
         set_err(ctx, "h264r_submit_batch: record upload failed");
         rc = H264R_ERR_CUDA;
     }
-    if (rc == H264R_OK) rc = launch(ctx, ctx->batch_stream, b, items, any_intra);
+    if (rc == H264R_OK) rc = launch(ctx, cs, b, items, any_intra);
     if (rc == H264R_OK) {
-        cudaEventRecord(ev, ctx->batch_stream);
-        for (int i = 0; i < n; i++) cudaStreamWaitEvent(streams[i]->cs, ev, 0);
+        cudaEventRecord(ev, cs);
+        for (int i = 1; i < n; i++)
+            if (streams[i]->cs != cs) cudaStreamWaitEvent(streams[i]->cs, ev, 0);
     }
     cudaEventDestroy(ev);
     return rc;

@@ -580,4 +580,37 @@ __device__ __forceinline__ const uint8_t *intra_nb_ptr(const PicDesc &p, int cur
     return plane_c(p, pl) + (size_t)(chroma_row0(y) + dy * yW) * p.Wc + x / 2 + xW;
 }
 
+// ---------------------------------------------------------------- byte packing
+__device__ __forceinline__ void unpack16(uint4 v, int *d)
+{
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int i = 0; i < 16; i++) d[i] = (w[i >> 2] >> (8 * (i & 3))) & 255;
+}
+
+__device__ __forceinline__ uint4 pack16(const int *s)
+{
+    uint32_t w[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int i = 0; i < 16; i++) w[i >> 2] |= (uint32_t)(s[i] & 255) << (8 * (i & 3));
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+__device__ __forceinline__ void unpack8(uint2 v, int *d)
+{
+#pragma unroll
+    for (int i = 0; i < 8; i++) d[i] = ((i < 4 ? v.x : v.y) >> (8 * (i & 3))) & 255;
+}
+
+__device__ __forceinline__ uint2 pack8(const int *s)
+{
+    uint32_t a = 0, b = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        a |= (uint32_t)(s[i] & 255) << (8 * i);
+        b |= (uint32_t)(s[4 + i] & 255) << (8 * i);
+    }
+    return make_uint2(a, b);
+}
+
 }  // namespace h264r

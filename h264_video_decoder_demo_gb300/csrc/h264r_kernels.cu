@@ -61,13 +61,15 @@ __device__ bool wait_progress(const LaunchState &st, const int *flag, int target
     if ((threadIdx.x & 31) == 0) {
         unsigned long long n = 0;
         while (ld_acquire(flag) < target) {
-            if (*(volatile int *)st.error != 0) { ok = false; break; }
             if (++n > st.spin_limit) {
                 set_error(st, H264R_ERR_DEVICE_TIMEOUT);
                 ok = false;
                 break;
             }
-            __nanosleep(64);
+            if (n > 64) {
+                if (*(volatile int *)st.error != 0) { ok = false; break; }
+                __nanosleep(32);
+            }
         }
     }
     ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -78,88 +80,250 @@ __device__ bool wait_progress(const LaunchState &st, const int *flag, int target
 // ======================================================================
 // K1: inter macroblocks, I_PCM, undecoded macroblocks
 // ======================================================================
-__global__ void __launch_bounds__(256) k_inter(const PicDesc *__restrict__ pics, int npics, LaunchState st)
+// One warp per MB, 4 MBs per block.  Lane l predicts rows 2*(l&1), +1 of
+// 4x4 block l>>1 (raster order within the MB) from a 7x9 window of the
+// reference staged in shared memory, and the 2x2 chroma samples of block
+// l&15 for plane l>>4; residuals come from lanes owning whole blocks.
+constexpr int kInterWarps = 4;
+
+struct InterWarpSmem {
+    uint8_t win[32][64];   // per-lane luma reference window, 7 rows x 9 cols
+    int32_t res[384];      // residual: luma raster 16x16, Cb 8x8, Cr 8x8
+    int32_t t8[4][64];     // 8x8 transform work area
+    __align__(16) uint8_t out[384];
+};
+
+#define TAP6(a, b, c_, d, e, f) ((a) - 5 * (b) + 20 * (c_) + 20 * (d) - 5 * (e) + (f))
+
+// 8.4.2.2.1 for a 2x4 group of samples (rows i0..i0+1, cols 0..3 of the
+// window origin) from win[(r+2)*9 + (c+2)], r in -2..4, c in -2..6.  The
+// centre sample j uses horizontal taps first: the taps are exact integers,
+// so the order of the two 6-tap passes does not change j1.
+__device__ __forceinline__ void mc_luma_2x4(const uint8_t *win, int xf, int yf, int out[8])
 {
-    __shared__ PicDesc sp;
-    __shared__ h264r_mb sm;
-    __shared__ int32_t res[384];
-    __shared__ __align__(16) uint8_t out[384];
-    __shared__ uint32_t s_shape, s_count;
-    const int t = threadIdx.x;
-    const uint32_t g = blockIdx.x;
-    if (t == 0) {
-        int pi = find_pic_by_mb(pics, npics, g);
-        sp = pics[pi];
+#define WV(r, c) ((int)win[((r) + 2) * 9 + (c) + 2])
+    if ((xf | yf) == 0) {
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) out[i * 4 + j] = WV(i, j);
+        return;
     }
-    __syncthreads();
-    const PicDesc &p = sp;
+    if (yf == 0) {
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                int b = clip1((TAP6(WV(i, j - 2), WV(i, j - 1), WV(i, j), WV(i, j + 1), WV(i, j + 2), WV(i, j + 3)) + 16) >> 5);
+                out[i * 4 + j] = xf == 2 ? b : ((xf == 1 ? WV(i, j) : WV(i, j + 1)) + b + 1) >> 1;
+            }
+        return;
+    }
+    if (xf == 0) {
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                int h = clip1((TAP6(WV(i - 2, j), WV(i - 1, j), WV(i, j), WV(i + 1, j), WV(i + 2, j), WV(i + 3, j)) + 16) >> 5);
+                out[i * 4 + j] = yf == 2 ? h : ((yf == 1 ? WV(i, j) : WV(i + 1, j)) + h + 1) >> 1;
+            }
+        return;
+    }
+    if (xf == 2 || yf == 2) {
+        int hb1[7][4];  // horizontal 6-tap sums at rows -2..4
+#pragma unroll
+        for (int r = -2; r <= 4; r++)
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                hb1[r + 2][j] = TAP6(WV(r, j - 2), WV(r, j - 1), WV(r, j), WV(r, j + 1), WV(r, j + 2), WV(r, j + 3));
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                int jv = clip1((TAP6(hb1[i][j], hb1[i + 1][j], hb1[i + 2][j], hb1[i + 3][j], hb1[i + 4][j], hb1[i + 5][j]) + 512) >> 10);
+                int o;
+                if (xf == 2 && yf == 2) {
+                    o = jv;
+                } else if (xf == 2) {  // f (row i) / q (row i+1)
+                    int b = clip1((hb1[i + 2 + (yf == 3 ? 1 : 0)][j] + 16) >> 5);
+                    o = (b + jv + 1) >> 1;
+                } else {  // i (col j) / k (col j+1)
+                    int c = j + (xf == 3 ? 1 : 0);
+                    int hh = clip1((TAP6(WV(i - 2, c), WV(i - 1, c), WV(i, c), WV(i + 1, c), WV(i + 2, c), WV(i + 3, c)) + 16) >> 5);
+                    o = (hh + jv + 1) >> 1;
+                }
+                out[i * 4 + j] = o;
+            }
+        return;
+    }
+    // e, g, p, r
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            int r = i + (yf == 3 ? 1 : 0), c = j + (xf == 3 ? 1 : 0);
+            int b = clip1((TAP6(WV(r, j - 2), WV(r, j - 1), WV(r, j), WV(r, j + 1), WV(r, j + 2), WV(r, j + 3)) + 16) >> 5);
+            int h = clip1((TAP6(WV(i - 2, c), WV(i - 1, c), WV(i, c), WV(i + 1, c), WV(i + 2, c), WV(i + 3, c)) + 16) >> 5);
+            out[i * 4 + j] = (b + h + 1) >> 1;
+        }
+#undef WV
+}
+
+__global__ void __launch_bounds__(32 * kInterWarps) k_inter(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st)
+{
+    __shared__ InterWarpSmem smem[kInterWarps];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t g = blockIdx.x * kInterWarps + wid;
+    if (g >= total_mbs) return;
+    InterWarpSmem &s = smem[wid];
+    const PicDesc p = pics[find_pic_by_mb(pics, npics, g)];
     const int addr = (int)(g - p.mb_base);
-    if (addr >= (int)p.num_mbs) return;
-    if (t == 0) sm = p.mbs[addr];
-    __syncthreads();
-    const h264r_mb m = sm;
+    const h264r_mb m = p.mbs[addr];
     if (m.type != H264R_MB_INTER && m.type != H264R_MB_IPCM && m.type != H264R_MB_NONE) return;
     int x, y, dy;
     mb_origin(p, addr, x, y, dy);
     const int field = field_mb(p, addr);
 
     if (m.type == H264R_MB_NONE) {
-        for (int i = t; i < 384; i += 256) out[i] = 0;
+        for (int i = lane; i < 96; i += 32) ((uint32_t *)s.out)[i] = 0;
     } else if (m.type == H264R_MB_IPCM) {
-        if (m.aux >= p.num_pcm) { if (t == 0) set_error(st, H264R_ERR_BAD_RECORD); return; }
-        const uint8_t *s = p.pcm + (size_t)m.aux * 384;
-        for (int i = t; i < 384; i += 256) out[i] = s[i];
+        if (m.aux >= p.num_pcm) { if (lane == 0) set_error(st, H264R_ERR_BAD_RECORD); return; }
+        const uint32_t *src = (const uint32_t *)(p.pcm + (size_t)m.aux * 384);
+        for (int i = lane; i < 96; i += 32) ((uint32_t *)s.out)[i] = __ldg(src + i);
     } else {
-        // ---- prediction
-        if (t == 0) {
-            bool bad = (m.aux & 3) || (uint64_t)m.aux + 4 > p.motion_bytes;
-            uint32_t hdr = bad ? 0 : *(const uint32_t *)(p.motion + m.aux);
-            s_shape = hdr & 0xFFFF;
-            s_count = hdr >> 16;
-            if (bad || (uint64_t)m.aux + 4 + 16ull * s_count > p.motion_bytes) {
-                set_error(st, H264R_ERR_BAD_RECORD);
-                s_count = 0;
-            }
+        bool bad = (m.aux & 3) || (uint64_t)m.aux + 4 > p.motion_bytes;
+        const uint32_t hdr = bad ? 0 : __ldg((const uint32_t *)(p.motion + m.aux));
+        const uint32_t shape = hdr & 0xFFFF, count = hdr >> 16;
+        if (bad || count == 0 || (uint64_t)m.aux + 4 + 16ull * count > p.motion_bytes) {
+            if (lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
+            return;
         }
-        for (int i = t; i < 384; i += 256) res[i] = 0;
-        __syncthreads();
-        if (s_count == 0) return;
         const h264r_part *parts = (const h264r_part *)(p.motion + m.aux + 4);
         const int bottom_mb = p.mbaff ? (addr & 1) : 0;
         const int yAL0 = field ? (y - (y & 1)) / 2 : y;
         const int ymax = field ? p.H / 2 - 1 : p.H - 1;
         const int ymaxc = field ? p.Hc / 2 - 1 : p.Hc - 1;
-        {
-            // luma sample t
-            const int lx = t & 15, ly = t >> 4;
-            int e = part_of_block(s_shape, lx >> 2, ly >> 2);
-            if (e >= (int)s_count) e = 0;
-            const h264r_part pp = parts[e];
-            const h264r_weight w = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
-            int v[2] = {0, 0};
-            bool use[2] = {pp.ref[0] >= 0, pp.ref[1] >= 0};
-#pragma unroll
-            for (int l = 0; l < 2; l++) {
-                if (!use[l]) continue;
-                RefView rv = ref_view(p, pp.ref[l]);
-                int mvx = pp.mv[l][0], mvy = pp.mv[l][1];
-                v[l] = luma_sample(rv, ymax, x + lx + (mvx >> 2), yAL0 + ly + (mvy >> 2), mvx & 3, mvy & 3);
+        // ---- residual first (lanes owning whole blocks), into s.res
+        for (int i = lane; i < 384; i += 32) s.res[i] = 0;
+        __syncwarp();
+        if (m.coef != H264R_NONE) {
+            CoefView cv;
+            if (!coef_view(p, m, cv)) {
+                if (lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
+                cv.mask = 0;
             }
-            out[t] = (uint8_t)weigh(w, 0, use[0], use[1], v[0], v[1]);
+            if (cv.t8) {
+                // 8 lanes per 8x8 block: lane = 8*b + row (8.5.13)
+                const int b = lane >> 3, r = lane & 7;
+                if (cv.mask & (1u << b)) {
+                    int w, l;
+                    coef_block(cv, b, w, l);
+                    const uint8_t *scan = field ? kField8x8 : kZigzag8x8;
+                    int32_t d[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                    for (int q = 0; q < 4; q++) {
+                        uint32_t sg = cv.sig[w + q];
+                        while (sg && l < cv.max_levels) {
+                            int kk = __ffs(sg) - 1;
+                            sg &= sg - 1;
+                            int v = cv.lv[l++];
+                            int rp = scan[16 * q + kk];
+                            if ((rp >> 3) == r) {
+                                int jj = rp & 7;
+                                int ls = level_scale8(p, 1, field, m.qpy % 6, r, jj);
+                                d[jj] = (m.qpy >= 36) ? (v * ls) << (m.qpy / 6 - 6) : (v * ls + (1 << (5 - m.qpy / 6))) >> (6 - m.qpy / 6);
+                            }
+                        }
+                    }
+                    int o[8];
+                    idct8_1d(d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], o);
+#pragma unroll
+                    for (int jj = 0; jj < 8; jj++) s.t8[b][r * 8 + jj] = o[jj];
+                }
+                __syncwarp();
+                if (cv.mask & (1u << b)) {
+                    const int c = r;  // now: column
+                    int o[8];
+                    idct8_1d(s.t8[b][0 * 8 + c], s.t8[b][1 * 8 + c], s.t8[b][2 * 8 + c], s.t8[b][3 * 8 + c], s.t8[b][4 * 8 + c],
+                             s.t8[b][5 * 8 + c], s.t8[b][6 * 8 + c], s.t8[b][7 * 8 + c], o);
+                    const int bx = (b & 1) * 8, by = (b >> 1) * 8;
+#pragma unroll
+                    for (int ii = 0; ii < 8; ii++) s.res[(by + ii) * 16 + bx + c] = (o[ii] + 32) >> 6;
+                }
+            } else if (lane < 16) {
+                if (cv.mask & (1u << lane)) {
+                    int32_t c[16], r[16];
+                    coef_list16(cv, lane, field, c);
+                    idct4x4(p, c, field, m.qpy, 3, false, r);
+                    const int bx = kBlkX[lane] * 4, by = kBlkY[lane] * 4;
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+#pragma unroll
+                        for (int j = 0; j < 4; j++) s.res[(by + i) * 16 + bx + j] = r[i * 4 + j];
+                }
+            }
+            if (lane >= 16 && lane < 24 && (cv.mask >> 17)) {
+                const int pl = (lane - 16) >> 2, b = (lane - 16) & 3;
+                const int qpc = chroma_qp(m.qpy, p.slices[min((uint32_t)m.slice, p.num_slices - 1)].chroma_qp_offset[pl]);
+                int32_t dcl[16], dc4[4], dcC[4];
+                coef_list16(cv, 17 + pl, 0, dcl);
+                dc4[0] = dcl[0]; dc4[1] = dcl[1]; dc4[2] = dcl[4]; dc4[3] = dcl[8];
+                chroma_dc(p, dc4, field, qpc, 3, dcC);
+                int32_t c[16], r[16];
+                coef_list16(cv, (pl ? H264R_CM_CR_AC0 : H264R_CM_CB_AC0) + b, field, c);
+                c[0] = dcC[b];
+                idct4x4(p, c, field, qpc, 3, true, r);
+                const int bx = (b & 1) * 4, by = (b >> 1) * 4;
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int j = 0; j < 4; j++) s.res[256 + pl * 64 + (by + i) * 8 + bx + j] = r[i * 4 + j];
+            }
+            __syncwarp();
         }
-        if (t < 128) {
-            // chroma sample: plane t>>6, row (t&63)>>3, col t&7
-            const int pl = t >> 6, cy = (t & 63) >> 3, cx = t & 7;
-            int e = part_of_block(s_shape, cx >> 1, cy >> 1);
-            if (e >= (int)s_count) e = 0;
+        // ---- luma prediction: 4x4 block lane>>1 (raster), rows 2*(lane&1), +1
+        {
+            const int blk = lane >> 1, bx = blk & 3, by = blk >> 2, r0 = 2 * (lane & 1);
+            int e = part_of_block(shape, bx, by);
+            if (e >= (int)count) e = 0;
             const h264r_part pp = parts[e];
             const h264r_weight w = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
-            int v[2] = {0, 0};
+            int v[2][8];
             bool use[2] = {pp.ref[0] >= 0, pp.ref[1] >= 0};
+            uint8_t *win = s.win[lane];
 #pragma unroll
             for (int l = 0; l < 2; l++) {
                 if (!use[l]) continue;
-                RefView rv = ref_view(p, pp.ref[l]);
+                const RefView rv = ref_view(p, pp.ref[l]);
+                const int mvx = pp.mv[l][0], mvy = pp.mv[l][1];
+                const int xi = x + bx * 4 + (mvx >> 2), yi = yAL0 + by * 4 + r0 + (mvy >> 2);
+                for (int rr = 0; rr < 7; rr++) {
+                    const uint8_t *row = rv.y + (size_t)H264R_CLIP3(0, ymax, yi + rr - 2) * rv.ystride;
+#pragma unroll
+                    for (int cc = 0; cc < 9; cc++) win[rr * 9 + cc] = __ldg(row + H264R_CLIP3(0, rv.xmax, xi + cc - 2));
+                }
+                mc_luma_2x4(win, mvx & 3, mvy & 3, v[l]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int oy = by * 4 + r0 + i, ox = bx * 4 + j;
+                    s.out[oy * 16 + ox] = (uint8_t)clip1(weigh(w, 0, use[0], use[1], v[0][i * 4 + j], v[1][i * 4 + j]) + s.res[oy * 16 + ox]);
+                }
+        }
+        // ---- chroma prediction: plane lane>>4, 2x2 samples of 4x4 block lane&15 (raster)
+        {
+            const int pl = lane >> 4, blk = lane & 15, bx = blk & 3, by = blk >> 2;
+            int e = part_of_block(shape, bx, by);
+            if (e >= (int)count) e = 0;
+            const h264r_part pp = parts[e];
+            const h264r_weight w = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
+            bool use[2] = {pp.ref[0] >= 0, pp.ref[1] >= 0};
+            int v[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+#pragma unroll
+            for (int l = 0; l < 2; l++) {
+                if (!use[l]) continue;
+                const RefView rv = ref_view(p, pp.ref[l]);
                 int mvx = pp.mv[l][0], mvy = pp.mv[l][1];
                 if (field) {  // Table 8-10 (H264InterPrediction.cpp:2006-2047)
                     int refbot = (pp.ref[l] & H264R_REF_BOTTOM) ? 1 : 0;
@@ -167,78 +331,32 @@ __global__ void __launch_bounds__(256) k_inter(const PicDesc *__restrict__ pics,
                     else if (refbot && !bottom_mb) mvy -= 2;
                 }
                 const uint8_t *plane = pl ? rv.cr : rv.cb;
-                v[l] = chroma_sample(plane, rv.cstride, rv.xmaxc, ymaxc, x / 2 + cx + (mvx >> 3), yAL0 / 2 + cy + (mvy >> 3),
-                                     mvx & 7, mvy & 7);
+                const int xi = x / 2 + bx * 2 + (mvx >> 3), yi = yAL0 / 2 + by * 2 + (mvy >> 3);
+#pragma unroll
+                for (int i = 0; i < 2; i++)
+#pragma unroll
+                    for (int j = 0; j < 2; j++)
+                        v[l][i * 2 + j] = chroma_sample(plane, rv.cstride, rv.xmaxc, ymaxc, xi + j, yi + i, mvx & 7, mvy & 7);
             }
-            out[256 + t] = (uint8_t)weigh(w, 1 + pl, use[0], use[1], v[0], v[1]);
-        }
-        // ---- residual (H264InterPrediction.cpp:22-407)
-        if (m.coef != H264R_NONE) {
-            CoefView cv;
-            if (!coef_view(p, m, cv)) {
-                if (t == 0) set_error(st, H264R_ERR_BAD_RECORD);
-            } else if (cv.t8) {
-                if (t < 4 && (cv.mask & (1u << t))) {
-                    int32_t c[64];
-                    for (int i = 0; i < 64; i++) c[i] = 0;
-                    int w, l;
-                    coef_block(cv, t, w, l);
-                    const uint8_t *scan = field ? kField8x8 : kZigzag8x8;
-                    for (int q = 0; q < 4; q++) {
-                        uint32_t s = cv.sig[w + q];
-                        while (s && l < cv.max_levels) {
-                            int k = __ffs(s) - 1;
-                            s &= s - 1;
-                            c[scan[16 * q + k]] = cv.lv[l++];
-                        }
-                    }
-                    idct8x8(p, c, field, m.qpy, 1, c);
-                    int bx = (t & 1) * 8, by = (t >> 1) * 8;
-                    for (int i = 0; i < 8; i++)
-                        for (int j = 0; j < 8; j++) res[(by + i) * 16 + bx + j] = c[i * 8 + j];
+#pragma unroll
+            for (int i = 0; i < 2; i++)
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    const int oy = by * 2 + i, ox = bx * 2 + j, o = 256 + pl * 64 + oy * 8 + ox;
+                    s.out[o] = (uint8_t)clip1(weigh(w, 1 + pl, use[0], use[1], v[0][i * 2 + j], v[1][i * 2 + j]) + s.res[o - 0]);
                 }
-            } else if (t < 16) {
-                if (cv.mask & (1u << t)) {
-                    int32_t c[16], r[16];
-                    coef_list16(cv, t, field, c);
-                    idct4x4(p, c, field, m.qpy, 3, false, r);
-                    int bx = kBlkX[t] * 4, by = kBlkY[t] * 4;
-                    for (int i = 0; i < 4; i++)
-                        for (int j = 0; j < 4; j++) res[(by + i) * 16 + bx + j] = r[i * 4 + j];
-                }
-            }
-            if (t >= 32 && t < 40 && cv.mask != 0) {
-                // chroma block: plane pl, block b
-                const int pl = (t - 32) >> 2, b = (t - 32) & 3;
-                const int qpc = chroma_qp(m.qpy, p.slices[min((uint32_t)m.slice, p.num_slices - 1)].chroma_qp_offset[pl]);
-                int32_t dcl[16], dc4[4], dcC[4];
-                coef_list16(cv, 17 + pl, 0, dcl);  // DC list: positions 0..3 in zig-zag order map to raster 0,1,4,8
-                dc4[0] = dcl[0]; dc4[1] = dcl[1]; dc4[2] = dcl[4]; dc4[3] = dcl[8];
-                chroma_dc(p, dc4, field, qpc, 3, dcC);
-                int32_t c[16], r[16];
-                coef_list16(cv, (pl ? H264R_CM_CR_AC0 : H264R_CM_CB_AC0) + b, field, c);
-                c[0] = dcC[b];
-                idct4x4(p, c, field, qpc, 3, true, r);
-                int bx = (b & 1) * 4, by = (b >> 1) * 4;
-                for (int i = 0; i < 4; i++)
-                    for (int j = 0; j < 4; j++) res[256 + pl * 64 + (by + i) * 8 + bx + j] = r[i * 4 + j];
-            }
         }
-        __syncthreads();
-        out[t] = (uint8_t)clip1(out[t] + res[t]);
-        if (t < 128) out[256 + t] = (uint8_t)clip1(out[256 + t] + res[256 + t]);
     }
-    __syncthreads();
+    __syncwarp();
     // ---- store: 16 luma rows of 16 bytes, 2 x 8 chroma rows of 8 bytes
-    if (t < 16) {
-        uint4 v = *(const uint4 *)(out + t * 16);
-        *(uint4 *)(plane_y(p) + (size_t)(y + t * dy) * p.W + x) = v;
-    } else if (t < 32) {
-        const int pl = (t - 16) >> 3, r = (t - 16) & 7;
-        uint2 v = *(const uint2 *)(out + 256 + pl * 64 + r * 8);
-        *(uint2 *)(plane_c(p, pl) + (size_t)(chroma_row0(y) + r * dy) * p.Wc + x / 2) = v;
+    if (lane < 16) {
+        *(uint4 *)(plane_y(p) + (size_t)(y + lane * dy) * p.W + x) = *(const uint4 *)(s.out + lane * 16);
+    } else {
+        const int pl = (lane - 16) >> 3, r = (lane - 16) & 7;
+        *(uint2 *)(plane_c(p, pl) + (size_t)(chroma_row0(y) + r * dy) * p.Wc + x / 2) = *(const uint2 *)(s.out + 256 + pl * 64 + r * 8);
     }
 }
+#undef TAP6
 
 // ======================================================================
 // K2: intra macroblocks, wavefront
@@ -639,9 +757,283 @@ __device__ void intra_mb(const PicDesc &p, int addr, IntraSmem &s, const LaunchS
     __syncwarp();
 }
 
+// ---------------------------------------------------------------- frame fast path
+// Non-MBAFF intra MB with its neighbourhood staged in shared memory: the
+// left column, top row (with the top-right MB's samples) and corner are
+// loaded once; the 4x4 / 8x8 blocks predict from and write into the tile;
+// the MB is stored once.  Neighbour availability follows
+// getMbAddrN_non_MBAFF_frames and the Intra_4x4/8x8 block rules.
+struct IntraTile {
+    int l[17][25];     // luma rows -1..15 (index +1), cols -1..23 (index +1)
+    int c[2][9][9];    // chroma rows -1..7, cols -1..7
+};
+
+// luma neighbour p[xN, yN] (relative to the MB) of a block, -1 when not
+// available; tr_ok: block rule for samples inside the MB to the top right
+__device__ __forceinline__ int tile_nb(const IntraTile &t, int xN, int yN, bool inside_tr_ok)
+{
+    if (yN >= 0 && xN >= 16) return -1;
+    if (yN >= 0 && xN >= 0 && !inside_tr_ok) return -1;
+    return t.l[yN + 1][xN + 1];
+}
+
+__device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTile &t, const LaunchState &st)
+{
+    const int lane = threadIdx.x & 31;
+    const h264r_mb m = p.mbs[addr];
+    const int W = p.W, Wc = p.Wc, wmb = p.wmb;
+    const int mx = addr % wmb, my = addr / wmb;
+    const int x = mx * 16, y = my * 16;
+    const int qp = m.qpy;
+    uint8_t *Y = plane_y(p);
+    // ---- neighbour MBs (6.4.9 / getMbAddrN_non_MBAFF_frames) and CIP
+    auto usable = [&](int n) -> bool {
+        if (n < 0 || n > addr) return false;
+        const h264r_mb &q = p.mbs[n];
+        if (q.slice != m.slice) return false;
+        return !(q.type == H264R_MB_INTER && (q.flags & H264R_MBF_CIP));
+    };
+    const bool A = mx > 0 && usable(addr - 1);
+    const bool B = my > 0 && usable(addr - wmb);
+    const bool Cc = my > 0 && mx + 1 < wmb && usable(addr - wmb + 1);
+    const bool D = mx > 0 && my > 0 && usable(addr - wmb - 1);
+    // ---- stage the neighbourhood (luma: corner, 16 left, 24 top; chroma: corner, 8 left, 8 top)
+    for (int i = lane; i < 41 + 34; i += 32) {
+        if (i < 41) {
+            int v = -1;
+            if (i == 0) { if (D) v = __ldcg(Y + (size_t)(y - 1) * W + x - 1); t.l[0][0] = v; }
+            else if (i < 17) { if (A) v = __ldcg(Y + (size_t)(y + i - 1) * W + x - 1); t.l[i][0] = v; }
+            else {
+                int xx = i - 17;  // 0..23
+                bool ok = xx < 16 ? B : Cc;
+                if (ok) v = __ldcg(Y + (size_t)(y - 1) * W + x + xx);
+                t.l[0][xx + 1] = v;
+            }
+        } else {
+            int j = i - 41, pl = j / 17, q = j % 17, v = -1;
+            const uint8_t *C = plane_c(p, pl);
+            const int xc = x / 2, yc = y / 2;
+            if (q == 0) { if (D) v = __ldcg(C + (size_t)(yc - 1) * Wc + xc - 1); t.c[pl][0][0] = v; }
+            else if (q < 9) { if (A) v = __ldcg(C + (size_t)(yc + q - 1) * Wc + xc - 1); t.c[pl][q][0] = v; }
+            else { if (B) v = __ldcg(C + (size_t)(yc - 1) * Wc + xc + q - 9); t.c[pl][0][q - 8] = v; }
+        }
+    }
+    // ---- residuals (same as intra_mb)
+    for (int i = lane; i < 384; i += 32) s.res[i] = 0;
+    CoefView cv;
+    if (!coef_view(p, m, cv)) {
+        if (lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
+        cv.mask = 0;
+    }
+    __syncwarp();
+    if (m.type == H264R_MB_I16x16) {
+        if (lane == 0) {
+            int32_t c[16];
+            coef_list16(cv, 16, 0, c);
+            luma_dc(p, c, 0, qp, s.dc);
+        }
+        __syncwarp();
+    }
+    if (m.type == H264R_MB_I8x8) {
+        if (lane < 4 && (cv.mask & (1u << lane))) {
+            int32_t c[64];
+            for (int i = 0; i < 64; i++) c[i] = 0;
+            int w, l;
+            coef_block(cv, lane, w, l);
+            for (int q = 0; q < 4; q++) {
+                uint32_t sg = cv.sig[w + q];
+                while (sg && l < cv.max_levels) {
+                    int kk = __ffs(sg) - 1;
+                    sg &= sg - 1;
+                    c[kZigzag8x8[16 * q + kk]] = cv.lv[l++];
+                }
+            }
+            idct8x8(p, c, 0, qp, 0, c);
+            int bx = (lane & 1) * 8, by = (lane >> 1) * 8;
+            for (int i = 0; i < 8; i++)
+                for (int j = 0; j < 8; j++) s.res[(by + i) * 16 + bx + j] = c[i * 8 + j];
+        }
+    } else if (lane < 16) {
+        bool i16 = m.type == H264R_MB_I16x16;
+        if ((cv.mask & (1u << lane)) || (i16 && s.dc[kBlkY[lane] * 4 + kBlkX[lane]] != 0)) {
+            int32_t c[16], r[16];
+            coef_list16(cv, lane, 0, c);
+            if (i16) c[0] = s.dc[kBlkY[lane] * 4 + kBlkX[lane]];
+            idct4x4(p, c, 0, qp, 0, i16, r);
+            int bx = kBlkX[lane] * 4, by = kBlkY[lane] * 4;
+            for (int i = 0; i < 4; i++)
+                for (int j = 0; j < 4; j++) s.res[(by + i) * 16 + bx + j] = r[i * 4 + j];
+        }
+    }
+    if (lane >= 16 && lane < 24 && cv.mask != 0) {
+        const int pl = (lane - 16) >> 2, b = (lane - 16) & 3;
+        const int qpc = chroma_qp(qp, p.slices[min((uint32_t)m.slice, p.num_slices - 1)].chroma_qp_offset[pl]);
+        int32_t dcl[16], dc4[4], dcC[4];
+        coef_list16(cv, 17 + pl, 0, dcl);
+        dc4[0] = dcl[0]; dc4[1] = dcl[1]; dc4[2] = dcl[4]; dc4[3] = dcl[8];
+        chroma_dc(p, dc4, 0, qpc, 0, dcC);
+        int32_t c[16], r[16];
+        coef_list16(cv, (pl ? H264R_CM_CR_AC0 : H264R_CM_CB_AC0) + b, 0, c);
+        c[0] = dcC[b];
+        idct4x4(p, c, 0, qpc, 0, true, r);
+        int bx = (b & 1) * 4, by = (b >> 1) * 4;
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) s.res[256 + pl * 64 + (by + i) * 8 + bx + j] = r[i * 4 + j];
+    }
+    __syncwarp();
+    // ---- luma
+    if (m.type == H264R_MB_I4x4) {
+        for (int b = 0; b < 16; b++) {
+            const int xO = kBlkX[b] * 4, yO = kBlkY[b] * 4;
+            if (lane < 16) {
+                int nb[13];
+                nb[0] = tile_nb(t, xO - 1, yO - 1, true);
+                for (int i = 0; i < 4; i++) nb[1 + i] = tile_nb(t, xO - 1, yO + i, true);
+                for (int i = 0; i < 8; i++) nb[5 + i] = tile_nb(t, xO + i, yO - 1, !(i > 3 && (b == 3 || b == 11)));
+                if (nb[9] < 0 && nb[10] < 0 && nb[11] < 0 && nb[12] < 0 && nb[8] >= 0) nb[9] = nb[10] = nb[11] = nb[12] = nb[8];
+                const int i = lane >> 2, j = lane & 3;
+                const int mode = (m.ipred[b >> 3] >> (4 * (b & 7))) & 15;
+                int pv = pred4x4_sample(mode, nb, j, i);
+                if (pv < 0) pv = 0;  // prediction not written: the cleared buffer
+                t.l[yO + i + 1][xO + j + 1] = clip1(pv + s.res[(yO + i) * 16 + xO + j]);
+            }
+            __syncwarp();
+        }
+    } else if (m.type == H264R_MB_I8x8) {
+        for (int b = 0; b < 4; b++) {
+            const int xO = (b & 1) * 8, yO = (b >> 1) * 8;
+            if (lane < 25) {
+                int nx = lane < 9 ? -1 : lane - 9, ny = lane < 9 ? lane - 1 : -1;
+                s.nb[lane] = tile_nb(t, xO + nx, yO + ny, true);
+            }
+            __syncwarp();
+            if (lane == 0) {
+                int *q = s.nb;
+                bool all = true;
+                for (int i = 17; i < 25; i++) all = all && q[i] < 0;
+                if (all && q[16] >= 0)
+                    for (int i = 17; i < 25; i++) q[i] = q[16];
+                int *f = s.nbf;
+                for (int i = 0; i < 25; i++) f[i] = -1;
+                bool top16 = true;
+                for (int i = 9; i < 25; i++) top16 = top16 && q[i] >= 0;
+                if (top16) {
+                    f[9] = (q[0] >= 0) ? (q[0] + 2 * q[9] + q[10] + 2) >> 2 : (3 * q[9] + q[10] + 2) >> 2;
+                    for (int i = 10; i < 24; i++) f[i] = (q[i - 1] + 2 * q[i] + q[i + 1] + 2) >> 2;
+                    f[24] = (q[23] + 3 * q[24] + 2) >> 2;
+                }
+                if (q[0] >= 0) {
+                    if (q[9] < 0 || q[1] < 0) {
+                        if (q[9] >= 0) f[0] = (3 * q[0] + q[9] + 2) >> 2;
+                        else if (q[1] >= 0) f[0] = (3 * q[0] + q[1] + 2) >> 2;
+                        else f[0] = q[0];
+                    } else {
+                        f[0] = (q[9] + 2 * q[0] + q[1] + 2) >> 2;
+                    }
+                }
+                bool left8 = true;
+                for (int i = 1; i < 9; i++) left8 = left8 && q[i] >= 0;
+                if (left8) {
+                    f[1] = (q[0] >= 0) ? (q[0] + 2 * q[1] + q[2] + 2) >> 2 : (3 * q[1] + q[2] + 2) >> 2;
+                    for (int i = 2; i < 8; i++) f[i] = (q[i - 1] + 2 * q[i] + q[i + 1] + 2) >> 2;
+                    f[8] = (q[7] + 3 * q[8] + 2) >> 2;
+                }
+            }
+            __syncwarp();
+            const int mode = (m.ipred[0] >> (4 * b)) & 15;
+            for (int kk = lane; kk < 64; kk += 32) {
+                int i = kk >> 3, j = kk & 7;
+                int pv = pred8x8_sample(mode, s.nbf, j, i);
+                if (pv < 0) pv = 0;
+                t.l[yO + i + 1][xO + j + 1] = clip1(pv + s.res[(yO + i) * 16 + xO + j]);
+            }
+            __syncwarp();
+        }
+    } else {
+        // Intra_16x16 (H264PictureBase.cpp:1847-2059)
+        const int *top = &t.l[0][1];
+        bool ta = B, la = A;
+        const int mode = m.i16_mode;
+        int a = 0, bb = 0, cc = 0, dcv = 128;
+        if (mode == 2) {
+            int stp = 0, slf = 0;
+            for (int i = 0; i < 16; i++) { stp += top[i]; slf += t.l[1 + i][0]; }
+            if (ta && la) dcv = (stp + slf + 16) >> 5;
+            else if (la) dcv = (slf + 8) >> 4;
+            else if (ta) dcv = (stp + 8) >> 4;
+        } else if (mode == 3) {
+            // quirk: p[-1,-1] is not required; when unavailable -1 enters H, V
+            int H = 0, V = 0;
+            for (int i = 0; i <= 7; i++) {
+                H += (i + 1) * (top[8 + i] - (6 - i >= 0 ? top[6 - i] : t.l[0][0]));
+                V += (i + 1) * (t.l[1 + 8 + i][0] - (6 - i >= 0 ? t.l[1 + 6 - i][0] : t.l[0][0]));
+            }
+            a = 16 * (t.l[16][0] + top[15]);
+            bb = (5 * H + 32) >> 6;
+            cc = (5 * V + 32) >> 6;
+        }
+        for (int kk = lane; kk < 256; kk += 32) {
+            int i = kk >> 4, j = kk & 15, pv;
+            if (mode == 0) pv = ta ? top[j] : 0;
+            else if (mode == 1) pv = la ? t.l[1 + i][0] : 0;
+            else if (mode == 2) pv = dcv;
+            else if (mode == 3) pv = (ta && la) ? clip1((a + bb * (j - 7) + cc * (i - 7) + 16) >> 5) : 0;
+            else pv = 0;
+            t.l[1 + i][1 + j] = clip1(pv + s.res[kk]);
+        }
+        __syncwarp();
+    }
+    // ---- chroma; quirk: DC treats a neighbouring value 0 as unavailable
+    const int cmode = m.chroma_mode;
+    for (int kk = lane; kk < 128; kk += 32) {
+        const int pl = kk >> 6, i = (kk & 63) >> 3, j = kk & 7;
+        int q[17];
+        q[0] = t.c[pl][0][0];
+        for (int u = 0; u < 8; u++) { q[1 + u] = t.c[pl][1 + u][0]; q[9 + u] = t.c[pl][0][1 + u]; }
+        int pv = 0;
+        if (cmode == 0) {
+            int xO = j & 4, yO = i & 4;
+            bool t4 = q[9 + xO] > 0 && q[10 + xO] > 0 && q[11 + xO] > 0 && q[12 + xO] > 0;
+            bool l4 = q[1 + yO] > 0 && q[2 + yO] > 0 && q[3 + yO] > 0 && q[4 + yO] > 0;
+            int stp = t4 ? q[9 + xO] + q[10 + xO] + q[11 + xO] + q[12 + xO] : 0;
+            int slf = l4 ? q[1 + yO] + q[2 + yO] + q[3 + yO] + q[4 + yO] : 0;
+            if ((xO == 0 && yO == 0) || (xO > 0 && yO > 0)) pv = (t4 && l4) ? (stp + slf + 4) >> 3 : l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
+            else if (xO > 0) pv = t4 ? (stp + 2) >> 2 : l4 ? (slf + 2) >> 2 : 128;
+            else pv = l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
+        } else if (cmode == 1) {
+            pv = A ? q[1 + i] : 0;
+        } else if (cmode == 2) {
+            pv = B ? q[9 + j] : 0;
+        } else if (cmode == 3) {
+            if (A && B && D) {
+                int H = 0, V = 0;
+                for (int u = 0; u <= 3; u++) {
+                    H += (u + 1) * (q[9 + 4 + u] - (2 - u >= 0 ? q[9 + 2 - u] : q[0]));
+                    V += (u + 1) * (q[1 + 4 + u] - (2 - u >= 0 ? q[1 + 2 - u] : q[0]));
+                }
+                int a = 16 * (q[1 + 7] + q[9 + 7]);
+                int b2 = (34 * H + 32) >> 6, c2 = (34 * V + 32) >> 6;
+                pv = clip1((a + b2 * (j - 3) + c2 * (i - 3) + 16) >> 5);
+            }
+        }
+        s.res[256 + kk] = clip1(pv + s.res[256 + kk]);  // reconstructed chroma, in place
+    }
+    __syncwarp();
+    // ---- store the MB: 16 luma rows of 16 bytes, 2 x 8 chroma rows of 8 bytes
+    if (lane < 16) {
+        *(uint4 *)(Y + (size_t)(y + lane) * W + x) = pack16(&t.l[1 + lane][1]);
+    } else {
+        const int pl = (lane - 16) >> 3, r = (lane - 16) & 7;
+        *(uint2 *)(plane_c(p, pl) + (size_t)(y / 2 + r) * Wc + x / 2) = pack8(&s.res[256 + pl * 64 + r * 8]);
+    }
+    __threadfence_block();
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(32) k_intra(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st)
 {
     __shared__ IntraSmem s;
+    __shared__ IntraTile tile;
     __shared__ uint32_t s_row;
     const int lane = threadIdx.x;
     if (lane == 0) s_row = atomicAdd(&st.ticket[0], 1u);
@@ -649,24 +1041,35 @@ __global__ void __launch_bounds__(32) k_intra(const PicDesc *__restrict__ pics, 
     const uint32_t g = s_row;
     if (g >= total_rows) return;
     const int pi = find_pic_by_row(pics, npics, g);
-    const PicDesc &p = pics[pi];
+    const PicDesc p = pics[pi];
     const int row = (int)(g - p.row_base);
     const int uw = (int)p.units_w;
     const int per = p.mbaff ? 2 : 1;
     int *prog = p.progress;
+    // Units without intra MBs were completed by k_inter: progress is only
+    // published before this row waits and after each intra unit.
+    int posted = 0;
     for (int u = 0; u < uw; u++) {
+        bool any = false;
+        for (int k = 0; k < per; k++) {
+            int addr = p.mbaff ? 2 * (row * uw + u) + k : row * uw + u;
+            any = any || is_intra_type(p.mbs[addr].type);
+        }
+        if (!any) continue;
+        if (lane == 0 && posted < u) st_release(prog + row, u);
+        posted = u;
         if (row > 0 && !wait_progress(st, prog + row - 1, min(u + 2, uw))) return;
         for (int k = 0; k < per; k++) {
             int addr = p.mbaff ? 2 * (row * uw + u) + k : row * uw + u;
-            int t = p.mbs[addr].type;
-            if (is_intra_type(t)) intra_mb(p, addr, s, st);
+            if (!is_intra_type(p.mbs[addr].type)) continue;
+            if (p.mbaff) intra_mb(p, addr, s, st);
+            else intra_mb_frame(p, addr, s, tile, st);
         }
         __syncwarp();
-        if (lane == 0) {
-            __threadfence();
-            st_release(prog + row, u + 1);
-        }
+        if (lane == 0) st_release(prog + row, u + 1);
+        posted = u + 1;
     }
+    if (lane == 0 && posted < uw) st_release(prog + row, uw);
 }
 
 // ======================================================================
@@ -1043,6 +1446,256 @@ __device__ void deblock_mb(const PicDesc &p, int cur)
     __syncwarp();
 }
 
+// ---------------------------------------------------------------- frame fast path
+// Non-MBAFF pictures: one warp filters one MB row with the MB, its left
+// neighbour's last columns and the MB above's last rows staged in shared
+// memory; one load and one store per MB instead of a global round trip per
+// edge step.  Same edge order, strengths and stop rule as deblock_mb.
+struct DbTile {
+    int l[20][20];     // luma rows -4..15, cols -4..15
+    int c[2][12][12];  // chroma rows -4..7, cols -4..7
+};
+
+// filter the line through q0 (p_i = q0[-(i+1)*step], q_i = q0[i*step])
+__device__ __forceinline__ void filter_tile_line(int *q0, int step, int bS, bool chroma, int indexA, int alpha, int beta)
+{
+    int pv[4], qv[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        qv[i] = q0[i * step];
+        pv[i] = q0[-(i + 1) * step];
+    }
+    filter_line(pv, qv, bS, chroma, indexA, alpha, beta);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        q0[i * step] = qv[i];
+        q0[-(i + 1) * step] = pv[i];
+    }
+}
+
+__device__ __forceinline__ void edge_params(const PicDesc &p, int mbP, int cur, int comp, int &indexA, int &alpha, int &beta)
+{
+    const h264r_mb P = p.mbs[mbP], Q = p.mbs[cur];
+    const h264r_slice sq = p.slices[min((uint32_t)Q.slice, p.num_slices - 1)];
+    int qPp, qPq;
+    if (comp == 0) {
+        qPp = P.type == H264R_MB_IPCM ? 0 : P.qpy;
+        qPq = Q.type == H264R_MB_IPCM ? 0 : Q.qpy;
+    } else {
+        int off = sq.chroma_qp_offset[comp - 1];
+        qPp = chroma_qp(P.type == H264R_MB_IPCM ? 0 : P.qpy, off);
+        qPq = chroma_qp(Q.type == H264R_MB_IPCM ? 0 : Q.qpy, off);
+    }
+    int qPav = (qPp + qPq + 1) >> 1;
+    indexA = H264R_CLIP3(0, 51, qPav + sq.filter_offset_a);
+    int indexB = H264R_CLIP3(0, 51, qPav + sq.filter_offset_b);
+    alpha = kAlpha[indexA];
+    beta = kBeta[indexB];
+}
+
+// data of one MB step that does not depend on the wavefront, prefetched
+// while the previous MB of the row is being filtered
+struct DbPrefetch {
+    uint4 luma;       // this lane's luma row (lanes 0..15)
+    uint2 chroma;     // this lane's chroma row (lanes 16..31)
+    uint8_t bv[4], bh[4];  // this lane's strengths: vertical / horizontal edges
+    uint4 mq, ma, mb; // first 16 bytes of the records of the MB, its left and top MB
+    uint2 sq;         // slice parameters of the MB
+};
+
+__device__ __forceinline__ void db_prefetch(const PicDesc &p, int row, int u, int lane, DbPrefetch &f)
+{
+    const int uw = (int)p.units_w, cur = row * uw + u;
+    const int x0 = u * 16, y0 = row * 16;
+    const uint8_t *bs = p.bs + (size_t)cur * kBsBytes;
+    if (lane < 16) {
+        f.luma = __ldcg((const uint4 *)(plane_y(p) + (size_t)(y0 + lane) * p.W + x0));
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            f.bv[e] = __ldcg(bs + kBsLumaV + 16 * e + lane);
+            f.bh[e] = __ldcg(bs + kBsLumaH + 16 * e + lane);
+        }
+    } else {
+        const int comp = lane < 24 ? 0 : 1, k = lane & 7;
+        f.chroma = __ldcg((const uint2 *)(plane_c(p, comp) + (size_t)(y0 / 2 + k) * p.Wc + x0 / 2));
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+            f.bv[e] = __ldcg(bs + kBsChromaV + 8 * e + k);
+            f.bh[e] = __ldcg(bs + kBsChromaH + 8 * e + k);
+        }
+    }
+    const uint4 *recs = (const uint4 *)p.mbs;  // h264r_mb is 32 bytes = 2 x uint4
+    f.mq = __ldg(recs + 2 * cur);
+    f.ma = u > 0 ? __ldg(recs + 2 * (cur - 1)) : f.mq;
+    f.mb = row > 0 ? __ldg(recs + 2 * (cur - uw)) : f.mq;
+    f.sq = __ldg((const uint2 *)p.slices + min((uint32_t)(f.mq.z & 0xFFFF), p.num_slices - 1));
+}
+
+__device__ __forceinline__ int rec_type(uint4 r) { return r.x & 255; }
+__device__ __forceinline__ int rec_flags(uint4 r) { return (r.x >> 8) & 255; }
+__device__ __forceinline__ int rec_qpy(uint4 r) { return (r.x >> 16) & 255; }
+__device__ __forceinline__ int rec_slice(uint4 r) { return r.z & 0xFFFF; }
+
+// alpha / beta / indexA of an edge from the p and q records (8.7.2.2)
+__device__ __forceinline__ void edge_params_rec(uint2 sraw, uint4 P, uint4 Q, int comp, int &indexA, int &alpha, int &beta)
+{
+    h264r_slice sq;
+    memcpy(&sq, &sraw, sizeof(sq));
+    int qyp = rec_type(P) == H264R_MB_IPCM ? 0 : rec_qpy(P);
+    int qyq = rec_type(Q) == H264R_MB_IPCM ? 0 : rec_qpy(Q);
+    int qPp = qyp, qPq = qyq;
+    if (comp) {
+        int off = sq.chroma_qp_offset[comp - 1];
+        qPp = chroma_qp(qyp, off);
+        qPq = chroma_qp(qyq, off);
+    }
+    int qPav = (qPp + qPq + 1) >> 1;
+    indexA = H264R_CLIP3(0, 51, qPav + sq.filter_offset_a);
+    int indexB = H264R_CLIP3(0, 51, qPav + sq.filter_offset_b);
+    alpha = kAlpha[indexA];
+    beta = kBeta[indexB];
+}
+
+__device__ void deblock_row_frame(const PicDesc &p, int row, DbTile &t, const LaunchState &st)
+{
+    const int lane = threadIdx.x & 31;
+    const int uw = (int)p.units_w, W = p.W, Wc = p.Wc;
+    int *prog = p.progress + p.units_h;
+    uint8_t *Y = plane_y(p);
+    const uint32_t stop = p.deblock_stop, stop_mb = stop >> 10;
+    const bool luma = lane < 16;
+    const int k = luma ? lane : (lane & 7);          // line index
+    const int comp = luma ? 0 : (lane < 24 ? 1 : 2);
+    const int cseq = comp == 2 ? 1 : 0;
+    uint8_t *C = luma ? nullptr : plane_c(p, comp - 1);
+    int(*ct)[12] = luma ? nullptr : t.c[comp - 1];
+    DbPrefetch nxt;
+    db_prefetch(p, row, 0, lane, nxt);
+    for (int u = 0; u < uw; u++) {
+        const int cur = row * uw + u;
+        const DbPrefetch f = nxt;
+        if (u + 1 < uw) db_prefetch(p, row, u + 1, lane, nxt);
+        if (row > 0 && !wait_progress(st, prog + row - 1, min(u + 2, uw))) return;
+        if ((uint32_t)cur <= stop_mb) {
+            const int x0 = u * 16, y0 = row * 16;
+            // the four rows above: final for this MB once the wait returned
+            uint4 above_l = make_uint4(0, 0, 0, 0);
+            uint2 above_c = make_uint2(0, 0);
+            if (row > 0) {
+                if (lane < 4) above_l = __ldcg((const uint4 *)(Y + (size_t)(y0 - 4 + lane) * W + x0));
+                else if (lane < 12) above_c = __ldcg((const uint2 *)(plane_c(p, (lane - 4) >> 2) + (size_t)(y0 / 2 - 4 + ((lane - 4) & 3)) * Wc + x0 / 2));
+            }
+            // left neighbour columns 12..15 (this warp's previous MB) -> -4..-1, then the MB itself
+            if (luma) {
+                if (u > 0) {
+#pragma unroll
+                    for (int i = 0; i < 4; i++) t.l[k + 4][i] = t.l[k + 4][16 + i];
+                }
+                unpack16(f.luma, &t.l[k + 4][4]);
+            } else {
+                if (u > 0) {
+#pragma unroll
+                    for (int i = 0; i < 4; i++) ct[k + 4][i] = ct[k + 4][8 + i];
+                }
+                unpack8(f.chroma, &ct[k + 4][4]);
+            }
+            if (row > 0) {
+                if (lane < 4) unpack16(above_l, &t.l[lane][4]);
+                else if (lane < 12) unpack8(above_c, &t.c[(lane - 4) >> 2][(lane - 4) & 3][4]);
+            }
+            __syncwarp();
+            // filter controls (Deblocking_filter_process 90-160, non-MBAFF)
+            const int sl = rec_slice(f.mq);
+            const int idc = (f.sq.y >> 0) & 255;  // disable_deblocking_filter_idc (byte 4 of h264r_slice)
+            const bool hasA = u > 0 && rec_slice(f.ma) == sl;
+            const bool hasB = row > 0 && rec_slice(f.mb) == sl;
+            const bool left = u > 0 && idc != 1 && !(idc == 2 && !hasA);
+            const bool top = row > 0 && idc != 1 && !(idc == 2 && !hasB);
+            const bool internal = idc != 1;
+            const bool t8 = (rec_flags(f.mq) & H264R_MBF_T8x8) != 0;
+            auto allowed = [&](int seq, int kk) -> bool { return stop_key(cur, seq, kk) < stop; };
+            int iA, al, be;
+            // ---- vertical edges (each lane owns one line)
+            if (luma) {
+                int *line = &t.l[k + 4][4];
+                if (left && f.bv[0] && allowed(SEQ_LV0, k)) {
+                    edge_params_rec(f.sq, hasA ? f.ma : f.mq, f.mq, 0, iA, al, be);
+                    filter_tile_line(line, 1, f.bv[0], false, iA, al, be);
+                }
+                if (internal) {
+                    edge_params_rec(f.sq, f.mq, f.mq, 0, iA, al, be);
+                    if (!t8 && f.bv[1] && allowed(SEQ_LV4, k)) filter_tile_line(line + 4, 1, f.bv[1], false, iA, al, be);
+                    if (f.bv[2] && allowed(SEQ_LV8, k)) filter_tile_line(line + 8, 1, f.bv[2], false, iA, al, be);
+                    if (!t8 && f.bv[3] && allowed(SEQ_LV12, k)) filter_tile_line(line + 12, 1, f.bv[3], false, iA, al, be);
+                }
+            } else {
+                int *line = &ct[k + 4][4];
+                if (left && f.bv[0] && allowed(SEQ_CBV0 + cseq, k)) {
+                    edge_params_rec(f.sq, hasA ? f.ma : f.mq, f.mq, comp, iA, al, be);
+                    filter_tile_line(line, 1, f.bv[0], true, iA, al, be);
+                }
+                if (internal && f.bv[1] && allowed(SEQ_CBV4 + cseq, k)) {
+                    edge_params_rec(f.sq, f.mq, f.mq, comp, iA, al, be);
+                    filter_tile_line(line + 4, 1, f.bv[1], true, iA, al, be);
+                }
+            }
+            __syncwarp();
+            // ---- horizontal edges (each lane owns one column)
+            if (luma) {
+                int *col = &t.l[4][k + 4];
+                if (top && f.bh[0] && allowed(SEQ_LH0, k)) {
+                    edge_params_rec(f.sq, hasB ? f.mb : f.mq, f.mq, 0, iA, al, be);
+                    filter_tile_line(col, 20, f.bh[0], false, iA, al, be);
+                }
+                if (internal) {
+                    edge_params_rec(f.sq, f.mq, f.mq, 0, iA, al, be);
+                    if (!t8 && f.bh[1] && allowed(SEQ_LH4, k)) filter_tile_line(col + 4 * 20, 20, f.bh[1], false, iA, al, be);
+                    if (f.bh[2] && allowed(SEQ_LH8, k)) filter_tile_line(col + 8 * 20, 20, f.bh[2], false, iA, al, be);
+                    if (!t8 && f.bh[3] && allowed(SEQ_LH12, k)) filter_tile_line(col + 12 * 20, 20, f.bh[3], false, iA, al, be);
+                }
+            } else {
+                int *col = &ct[4][k + 4];
+                if (top && f.bh[0] && allowed(SEQ_CBH0 + cseq, k)) {
+                    edge_params_rec(f.sq, hasB ? f.mb : f.mq, f.mq, comp, iA, al, be);
+                    filter_tile_line(col, 12, f.bh[0], true, iA, al, be);
+                }
+                if (internal && f.bh[1] && allowed(SEQ_CBH4 + cseq, k)) {
+                    edge_params_rec(f.sq, f.mq, f.mq, comp, iA, al, be);
+                    filter_tile_line(col + 4 * 12, 12, f.bh[1], true, iA, al, be);
+                }
+            }
+            __syncwarp();
+            // ---- write back: the MB, the left MB's last 3 columns, the MB above's last 3 rows
+            if (luma) {
+                *(uint4 *)(Y + (size_t)(y0 + k) * W + x0) = pack16(&t.l[k + 4][4]);
+                if (u > 0) {
+                    uint8_t *d = Y + (size_t)(y0 + k) * W + x0 - 3;
+                    d[0] = (uint8_t)t.l[k + 4][1];
+                    d[1] = (uint8_t)t.l[k + 4][2];
+                    d[2] = (uint8_t)t.l[k + 4][3];
+                }
+            } else {
+                *(uint2 *)(C + (size_t)(y0 / 2 + k) * Wc + x0 / 2) = pack8(&ct[k + 4][4]);
+                if (u > 0) {
+                    uint8_t *d = C + (size_t)(y0 / 2 + k) * Wc + x0 / 2 - 3;
+                    d[0] = (uint8_t)ct[k + 4][1];
+                    d[1] = (uint8_t)ct[k + 4][2];
+                    d[2] = (uint8_t)ct[k + 4][3];
+                }
+            }
+            if (row > 0) {
+                if (lane < 3) *(uint4 *)(Y + (size_t)(y0 - 3 + lane) * W + x0) = pack16(&t.l[1 + lane][4]);
+                else if (lane < 9) {
+                    const int pl = (lane - 3) / 3, rr = (lane - 3) % 3;
+                    *(uint2 *)(plane_c(p, pl) + (size_t)(y0 / 2 - 3 + rr) * Wc + x0 / 2) = pack8(&t.c[pl][1 + rr][4]);
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) st_release(prog + row, u + 1);
+    }
+}
+
 __global__ void __launch_bounds__(32) k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st)
 {
     __shared__ uint32_t s_row;
@@ -1052,9 +1705,14 @@ __global__ void __launch_bounds__(32) k_deblock(const PicDesc *__restrict__ pics
     const uint32_t g = s_row;
     if (g >= total_rows) return;
     const int pi = find_pic_by_row(pics, npics, g);
-    const PicDesc &p = pics[pi];
+    const PicDesc p = pics[pi];
     if (!p.deblock) return;
     const int row = (int)(g - p.row_base);
+    if (!p.mbaff) {
+        __shared__ DbTile tile;
+        deblock_row_frame(p, row, tile, st);
+        return;
+    }
     const int uw = (int)p.units_w;
     const int per = p.mbaff ? 2 : 1;
     int *prog = p.progress + p.units_h;
@@ -1066,10 +1724,7 @@ __global__ void __launch_bounds__(32) k_deblock(const PicDesc *__restrict__ pics
             if ((uint32_t)addr <= stop_mb) deblock_mb(p, addr);
         }
         __syncwarp();
-        if (lane == 0) {
-            __threadfence();
-            st_release(prog + row, u + 1);
-        }
+        if (lane == 0) st_release(prog + row, u + 1);
     }
 }
 

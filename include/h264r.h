@@ -254,7 +254,10 @@ int  h264r_submit_picture_device(h264r_stream *s, const h264r_picture *pic);
 /*
  * Batched reconstruction: n independent pictures (of any streams in the same
  * context; no picture may reference another picture of the same batch) in
- * one fused launch sequence.  Pointers are device memory.
+ * one fused launch sequence.  Pointers are device memory.  The batch runs on
+ * the CUDA stream of streams[0] after the work already queued on the other
+ * member streams, and their later work waits for it; batches over disjoint
+ * sets of streams with different first members therefore overlap.
  */
 int  h264r_submit_batch_device(h264r_ctx *ctx, int n, h264r_stream *const *streams,
                                const h264r_picture *pics);
@@ -294,7 +297,7 @@ int  h264r_stream_sync(h264r_stream *s);
 int  h264r_ctx_sync(h264r_ctx *ctx);
 /* The CUDA stream the engine enqueues this stream's work on (cudaStream_t). */
 void *h264r_stream_cuda_stream(h264r_stream *s);
-/* The CUDA stream batched launches of the context run on (cudaStream_t). */
+/* The context's own CUDA stream (used by h264r_ctx_sync), cudaStream_t. */
 void *h264r_ctx_cuda_stream(h264r_ctx *ctx);
 
 /* Validate a picture's records on the host (ranges, offsets, payload sizes).
