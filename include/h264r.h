@@ -136,7 +136,10 @@ typedef struct h264r_part {
                                the list is unused; bits 0..4 DPB slot,
                                bit 5 field reference, bit 6 bottom field      */
     int8_t   dref[2];       /* reference identity used by the deblocking
-                               filter's bS rules, -1 for none (see DESIGN)    */
+                               filter's bS rules, -1 for none: the picture-
+                               level list entry the reference compares
+                               (H264PictureDeblockingFilterProcess.cpp:
+                               1175-1178), which can differ from ref[]      */
     uint16_t wt;            /* index into the picture's weight table         */
     uint16_t reserved;
 } h264r_part;
