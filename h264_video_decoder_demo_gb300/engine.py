@@ -26,6 +26,7 @@ EXPORTS = [
     "h264r_ctx_set_timing", "h264r_ctx_last_timing",
     "h264r_synth_create", "h264r_synth_dpb_slots", "h264r_synth_next", "h264r_synth_destroy",
     "h264r_submit_batch", "h264r_picture_bytes", "h264r_ctx_cuda_stream",
+    "h264r_deblock_picture_noalloc",
 ]
 
 
@@ -70,6 +71,7 @@ def _load():
         "h264r_ctx_sync": (i32, [vp]),
         "h264r_stream_cuda_stream": (vp, [vp]),
         "h264r_ctx_cuda_stream": (vp, [vp]),
+        "h264r_deblock_picture_noalloc": (i32, [P(R.CPicture), vp, vp]),
         "h264r_validate_picture": (i32, [P(R.CPicture), i32]),
         "h264r_ctx_kernel_launches": (u64, [vp]),
         "h264r_ctx_set_timing": (i32, [vp, i32]),

@@ -48,6 +48,7 @@ extern "C" {
 #define H264R_ERR_BUDGET        -6   /* admission refused: DPB memory budget    */
 #define H264R_ERR_DEVICE_TIMEOUT -7  /* a bounded device-side wait expired      */
 #define H264R_ERR_BUSY          -8   /* no free slot / queue full               */
+#define H264R_ERR_TOO_LARGE     -9   /* exceeds a fixed maximum size            */
 
 /* ---- macroblock record ------------------------------------------------- */
 /* mb type classes (derived from mb_type / MbPartPredMode, 7.4.5)          */
@@ -302,6 +303,34 @@ int  h264r_ctx_sync(h264r_ctx *ctx);
 void *h264r_stream_cuda_stream(h264r_stream *s);
 /* The context's own CUDA stream (used by h264r_ctx_sync), cudaStream_t. */
 void *h264r_ctx_cuda_stream(h264r_ctx *ctx);
+
+/*
+ * Deblock one picture in place without allocating any device memory.
+ * No counterpart in the reference: it exists for callers that cannot let a
+ * library allocate on the GPU — processes that hand all device memory to a
+ * pool of their own up front, and real-time decode loops that must not stall
+ * other streams (cudaMalloc and cudaFree synchronise the device).
+ *
+ * pic: records of a reconstructed picture, every pointer device memory (as
+ *      for h264r_submit_picture_device); pic->deblock is ignored.
+ * planes: device address of the picture's samples, Y then Cb then Cr
+ *      contiguous at coded size (the engine's DPB slot layout); filtered in
+ *      place.  cuda_stream: the cudaStream_t to run on (0: legacy default).
+ * The scratch it needs (bS table, wavefront counters) is one static device
+ * array compiled into the library, sized for pictures of at most
+ * H264R_NOALLOC_MAX_MBS macroblocks and H264R_NOALLOC_MAX_MB_ROWS MB rows
+ * (1920x1088 fits); larger pictures return H264R_ERR_TOO_LARGE.  Every GPU
+ * that loads the library holds that array (about 1.6 MB) until the process
+ * exits.  The first call on a device resolves the array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.  All calls in a process share the one array:
+ * calls that overlap on the GPU race and corrupt each other, so do not run
+ * two at once.  The call waits for its stream and returns 0 or the device
+ * error (H264R_ERR_DEVICE_TIMEOUT / H264R_ERR_BAD_RECORD).
+ */
+#define H264R_NOALLOC_MAX_MBS     8192
+#define H264R_NOALLOC_MAX_MB_ROWS 256
+int  h264r_deblock_picture_noalloc(const h264r_picture *pic, uint8_t *planes, void *cuda_stream);
 
 /* Validate a picture's records on the host (ranges, offsets, payload sizes).
  * Returns 0 or H264R_ERR_BAD_RECORD / H264R_ERR_UNSUPPORTED. */
