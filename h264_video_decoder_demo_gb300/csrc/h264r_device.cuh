@@ -93,12 +93,22 @@ struct LaunchState {
     unsigned long long spin_limit;
 };
 
-// bS table layout per MB (bytes): luma vertical 4 edges x 16 rows, luma
-// horizontal 4 edges x 16 cols, extra MBAFF top edge x 16, chroma vertical
-// 2 x 8, chroma horizontal 2 x 8, chroma extra top edge x 8.  A value of
-// 0xFF marks the place where the reference's bS derivation fails.
+// bS table layout per MB (bytes), line-major so that one load gives a line
+// its strengths for every edge: luma vertical [16 rows][4 edges], luma
+// horizontal [16 cols][4 edges], extra MBAFF top edge [16], chroma vertical
+// [8 rows][2 edges], chroma horizontal [8 cols][2 edges], chroma extra top
+// edge [8].  A value of 0xFF marks the place where the reference's bS
+// derivation fails.  Edges not filtered (disable_deblocking_filter_idc,
+// picture borders, 8x8-transform internal edges) hold 0.
+// Frame (non-MBAFF) pictures also get the filter thresholds of each edge
+// class at kBsParams: [component][left, top, internal] words of
+// alpha | beta << 8 | tC0(bS 1..3) << 16, 21, 26 (8.7.2.2).
 constexpr int kBsLumaV = 0, kBsLumaH = 64, kBsLumaTop2 = 128, kBsChromaV = 144, kBsChromaH = 160,
-              kBsChromaTop2 = 176, kBsBytes = 192;
+              kBsChromaTop2 = 176, kBsParams = 192, kBsBytes = 256;
+__device__ __forceinline__ constexpr int bs_lv(int e, int k) { return kBsLumaV + 4 * k + e; }
+__device__ __forceinline__ constexpr int bs_lh(int e, int k) { return kBsLumaH + 4 * k + e; }
+__device__ __forceinline__ constexpr int bs_cv(int e, int k) { return kBsChromaV + 2 * k + e; }
+__device__ __forceinline__ constexpr int bs_ch(int e, int k) { return kBsChromaH + 2 * k + e; }
 
 __device__ __forceinline__ uint8_t *plane_y(const PicDesc &p) { return p.dst; }
 __device__ __forceinline__ uint8_t *plane_c(const PicDesc &p, int pl)

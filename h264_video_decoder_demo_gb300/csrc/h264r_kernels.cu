@@ -1211,6 +1211,28 @@ enum { SEQ_LV0 = 0, SEQ_LV4, SEQ_LV8, SEQ_LV12, SEQ_LH0, SEQ_LH0B, SEQ_LH4, SEQ_
 
 __device__ __forceinline__ uint32_t stop_key(int mb, int seq, int k) { return ((uint32_t)mb << 10) | ((uint32_t)seq << 4) | (uint32_t)k; }
 
+// indexA / alpha / beta of an edge between MBs mbP and cur (8.7.2.2,
+// H264PictureDeblockingFilterProcess.cpp:1314-1369)
+__device__ __forceinline__ void edge_params(const PicDesc &p, int mbP, int cur, int comp, int &indexA, int &alpha, int &beta)
+{
+    const h264r_mb P = p.mbs[mbP], Q = p.mbs[cur];
+    const h264r_slice sq = p.slices[min((uint32_t)Q.slice, p.num_slices - 1)];
+    int qPp, qPq;
+    if (comp == 0) {
+        qPp = P.type == H264R_MB_IPCM ? 0 : P.qpy;
+        qPq = Q.type == H264R_MB_IPCM ? 0 : Q.qpy;
+    } else {
+        int off = sq.chroma_qp_offset[comp - 1];
+        qPp = chroma_qp(P.type == H264R_MB_IPCM ? 0 : P.qpy, off);
+        qPq = chroma_qp(Q.type == H264R_MB_IPCM ? 0 : Q.qpy, off);
+    }
+    int qPav = (qPp + qPq + 1) >> 1;
+    indexA = H264R_CLIP3(0, 51, qPav + sq.filter_offset_a);
+    int indexB = H264R_CLIP3(0, 51, qPav + sq.filter_offset_b);
+    alpha = kAlpha[indexA];
+    beta = kBeta[indexB];
+}
+
 __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st)
 {
     // one warp per MB; 4 MBs per block
@@ -1231,7 +1253,7 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
         bool on = (ei == 0) ? c.left : (c.internal && (ei == 2 || !c.t8));
         int bs = on ? edge_bs(p, cur, 0, 1, e, c.mbA, ei == 0 ? c.leftMixed : 0, k) : 0;
         if (bs == 0xFF) mystop = min(mystop, stop_key(cur, SEQ_LV0 + ei, k));
-        out[kBsLumaV + it] = (uint8_t)bs;
+        out[bs_lv(ei, k)] = (uint8_t)bs;
     }
     // luma horizontal: items 0..63 (+16 for the MBAFF second top edge)
     for (int it = lane; it < 80; it += 32) {
@@ -1245,7 +1267,7 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
                 else bs = edge_bs(p, cur, 0, 0, e, c.mbB, 0, k);
             }
             seq = ei == 0 ? SEQ_LH0 : SEQ_LH4 + ei - 1;
-            out[kBsLumaH + it] = (uint8_t)bs;
+            out[bs_lh(ei, k)] = (uint8_t)bs;
         } else {
             k = it - 64;
             if (c.top && c.topDouble) bs = edge_bs(p, cur, 0, 0, 1, c.mbB, 0, k);
@@ -1264,14 +1286,14 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
             bool on = ei == 0 ? c.left : c.internal;
             if (on) bs = edge_bs(p, cur, 1, 1, ei * 4, c.mbA, ei == 0 ? c.leftMixed : 0, k);
             seqcb = ei == 0 ? SEQ_CBV0 : SEQ_CBV4;
-            out[kBsChromaV + it] = (uint8_t)bs;
+            out[bs_cv(ei, k)] = (uint8_t)bs;
         } else if (it < 32) {
             int ei = (it - 16) >> 3;
             k = it & 7;
             bool on = ei == 0 ? c.top : c.internal;
             if (on) bs = edge_bs(p, cur, 1, 0, ei == 0 ? 0 : 4, c.mbB, 0, k);
             seqcb = ei == 0 ? SEQ_CBH0 : SEQ_CBH4;
-            out[kBsChromaH + (it - 16)] = (uint8_t)bs;
+            out[bs_ch(ei, k)] = (uint8_t)bs;
         } else {
             k = it - 32;
             if (c.top && c.topDouble) bs = edge_bs(p, cur, 1, 0, 1, c.mbB, 0, k);
@@ -1279,6 +1301,18 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
             out[kBsChromaTop2 + k] = (uint8_t)bs;
         }
         if (bs == 0xFF) mystop = min(mystop, stop_key(cur, seqcb, k));
+    }
+    // thresholds of each edge class for the frame fast path of k_deblock
+    if (!p.mbaff && lane < 9) {
+        const int comp = lane / 3, kind = lane % 3;  // kind: 0 left, 1 top, 2 internal
+        int mbP = cur;
+        if (kind == 0 && c.mbA >= 0) mbP = c.mbA;
+        if (kind == 1 && c.mbB >= 0) mbP = c.mbB;
+        int iA, al, be;
+        edge_params(p, mbP, cur, comp, iA, al, be);
+        const uint32_t w = (uint32_t)al | ((uint32_t)be << 8) | ((uint32_t)kTc0[0][iA] << 16) |
+                           ((uint32_t)kTc0[1][iA] << 21) | ((uint32_t)kTc0[2][iA] << 26);
+        *(uint32_t *)(out + kBsParams + 16 * comp + 4 * kind) = w;
     }
     for (int o = 16; o > 0; o >>= 1) mystop = min(mystop, __shfl_xor_sync(0xffffffffu, mystop, o));
     if (lane == 0 && mystop != 0xFFFFFFFFu) atomicMin(&pp->deblock_stop, mystop);
@@ -1395,304 +1429,314 @@ __device__ void deblock_mb(const PicDesc &p, int cur)
     const int cseq = comp == 2 ? 1 : 0;  // Cr steps follow the Cb step of the same edge
     // ---- vertical edges
     if (luma) {
-        if (c.left && allowed(SEQ_LV0, k)) edge_line(p, cur, 0, 1, 0, c.mbA, c.leftMixed, c.field, k, bs[kBsLumaV + k]);
+        if (c.left && allowed(SEQ_LV0, k)) edge_line(p, cur, 0, 1, 0, c.mbA, c.leftMixed, c.field, k, bs[bs_lv(0, k)]);
         __syncwarp(0x0000FFFFu);
         if (c.internal) {
-            if (!c.t8 && allowed(SEQ_LV4, k)) edge_line(p, cur, 0, 1, 4, c.mbA, 0, c.field, k, bs[kBsLumaV + 16 + k]);
+            if (!c.t8 && allowed(SEQ_LV4, k)) edge_line(p, cur, 0, 1, 4, c.mbA, 0, c.field, k, bs[bs_lv(1, k)]);
             __syncwarp(0x0000FFFFu);
-            if (allowed(SEQ_LV8, k)) edge_line(p, cur, 0, 1, 8, c.mbA, 0, c.field, k, bs[kBsLumaV + 32 + k]);
+            if (allowed(SEQ_LV8, k)) edge_line(p, cur, 0, 1, 8, c.mbA, 0, c.field, k, bs[bs_lv(2, k)]);
             __syncwarp(0x0000FFFFu);
-            if (!c.t8 && allowed(SEQ_LV12, k)) edge_line(p, cur, 0, 1, 12, c.mbA, 0, c.field, k, bs[kBsLumaV + 48 + k]);
+            if (!c.t8 && allowed(SEQ_LV12, k)) edge_line(p, cur, 0, 1, 12, c.mbA, 0, c.field, k, bs[bs_lv(3, k)]);
         }
     } else {
-        if (c.left && allowed(SEQ_CBV0 + cseq, k)) edge_line(p, cur, comp, 1, 0, c.mbA, c.leftMixed, c.field, k, bs[kBsChromaV + k]);
+        if (c.left && allowed(SEQ_CBV0 + cseq, k)) edge_line(p, cur, comp, 1, 0, c.mbA, c.leftMixed, c.field, k, bs[bs_cv(0, k)]);
         __syncwarp(0xFFFF0000u);
-        if (c.internal && allowed(SEQ_CBV4 + cseq, k)) edge_line(p, cur, comp, 1, 4, c.mbA, 0, c.field, k, bs[kBsChromaV + 8 + k]);
+        if (c.internal && allowed(SEQ_CBV4 + cseq, k)) edge_line(p, cur, comp, 1, 4, c.mbA, 0, c.field, k, bs[bs_cv(1, k)]);
     }
     __syncwarp();
     // ---- horizontal edges
     if (luma) {
         if (c.top) {
             if (c.topDouble) {
-                if (allowed(SEQ_LH0, k)) edge_line(p, cur, 0, 0, 0, c.mbB - 1, 0, 1, k, bs[kBsLumaH + k]);
+                if (allowed(SEQ_LH0, k)) edge_line(p, cur, 0, 0, 0, c.mbB - 1, 0, 1, k, bs[bs_lh(0, k)]);
                 __syncwarp(0x0000FFFFu);
                 if (allowed(SEQ_LH0B, k)) edge_line(p, cur, 0, 0, 1, c.mbB, 0, 1, k, bs[kBsLumaTop2 + k]);
             } else if (allowed(SEQ_LH0, k)) {
-                edge_line(p, cur, 0, 0, 0, c.mbB, 0, c.field, k, bs[kBsLumaH + k]);
+                edge_line(p, cur, 0, 0, 0, c.mbB, 0, c.field, k, bs[bs_lh(0, k)]);
             }
         }
         __syncwarp(0x0000FFFFu);
         if (c.internal) {
-            if (!c.t8 && allowed(SEQ_LH4, k)) edge_line(p, cur, 0, 0, 4, c.mbB, 0, c.field, k, bs[kBsLumaH + 16 + k]);
+            if (!c.t8 && allowed(SEQ_LH4, k)) edge_line(p, cur, 0, 0, 4, c.mbB, 0, c.field, k, bs[bs_lh(1, k)]);
             __syncwarp(0x0000FFFFu);
-            if (allowed(SEQ_LH8, k)) edge_line(p, cur, 0, 0, 8, c.mbB, 0, c.field, k, bs[kBsLumaH + 32 + k]);
+            if (allowed(SEQ_LH8, k)) edge_line(p, cur, 0, 0, 8, c.mbB, 0, c.field, k, bs[bs_lh(2, k)]);
             __syncwarp(0x0000FFFFu);
-            if (!c.t8 && allowed(SEQ_LH12, k)) edge_line(p, cur, 0, 0, 12, c.mbB, 0, c.field, k, bs[kBsLumaH + 48 + k]);
+            if (!c.t8 && allowed(SEQ_LH12, k)) edge_line(p, cur, 0, 0, 12, c.mbB, 0, c.field, k, bs[bs_lh(3, k)]);
         }
     } else {
         if (c.top) {
             if (c.topDouble) {
-                if (allowed(SEQ_CBH0 + cseq, k)) edge_line(p, cur, comp, 0, 0, c.mbB, 0, 1, k, bs[kBsChromaH + k]);
+                if (allowed(SEQ_CBH0 + cseq, k)) edge_line(p, cur, comp, 0, 0, c.mbB, 0, 1, k, bs[bs_ch(0, k)]);
                 __syncwarp(0xFFFF0000u);
                 if (allowed(SEQ_CBH0B + cseq, k)) edge_line(p, cur, comp, 0, 1, c.mbB, 0, 1, k, bs[kBsChromaTop2 + k]);
             } else if (allowed(SEQ_CBH0 + cseq, k)) {
-                edge_line(p, cur, comp, 0, 0, c.mbB, 0, c.field, k, bs[kBsChromaH + k]);
+                edge_line(p, cur, comp, 0, 0, c.mbB, 0, c.field, k, bs[bs_ch(0, k)]);
             }
         }
         __syncwarp(0xFFFF0000u);
-        if (c.internal && allowed(SEQ_CBH4 + cseq, k)) edge_line(p, cur, comp, 0, 4, c.mbB, 0, c.field, k, bs[kBsChromaH + 8 + k]);
+        if (c.internal && allowed(SEQ_CBH4 + cseq, k)) edge_line(p, cur, comp, 0, 4, c.mbB, 0, c.field, k, bs[bs_ch(1, k)]);
     }
     __threadfence_block();
     __syncwarp();
 }
 
 // ---------------------------------------------------------------- frame fast path
-// Non-MBAFF pictures: one warp filters one MB row with the MB, its left
-// neighbour's last columns and the MB above's last rows staged in shared
-// memory; one load and one store per MB instead of a global round trip per
-// edge step.  Same edge order, strengths and stop rule as deblock_mb.
-struct DbTile {
-    int l[20][20];     // luma rows -4..15, cols -4..15
-    int c[2][12][12];  // chroma rows -4..7, cols -4..7
+// Non-MBAFF pictures: one warp filters a pair of MB rows, the second row
+// trailing the first by two MBs (in the reference's raster order a MB's top
+// edge comes after the left edge of the MB above-right).  Lanes 0..15 work
+// on the first row of the pair, 16..31 on the second; in each half a lane
+// owns one luma line and one chroma line (Cb for lanes 0..7 of the half, Cr
+// for 8..15).  A line is filtered in registers across all edges of one
+// direction, and the MB passes through shared memory once, between its
+// vertical and horizontal edges.  The vertical edges of a MB touch only its
+// own MB row, so they run before the wait for the row above.  The second
+// row takes the first row's bottom lines from a small ring in shared memory
+// instead of a global round trip.  Strengths and thresholds come from k_bs.
+constexpr int kDbLumaHalf = 368;    // ints per half: rows -4..15 x stride 17 (+ bank offset 16)
+constexpr int kDbChromaGroup = 169; // ints per (half, plane): rows -4..7 x stride 12 (+ bank offset 9)
+
+struct DbPairSmem {
+    int l[2][kDbLumaHalf];
+    int c[4][kDbChromaGroup];
+    uint4 ring_l[3][4];      // first row: luma rows 12..15 of the MB in column % 3
+    uint2 ring_c[3][2][4];   // first row: chroma rows 4..7, per plane
 };
 
-// filter the line through q0 (p_i = q0[-(i+1)*step], q_i = q0[i*step])
-__device__ __forceinline__ void filter_tile_line(int *q0, int step, int bS, bool chroma, int indexA, int alpha, int beta)
-{
-    int pv[4], qv[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        qv[i] = q0[i * step];
-        pv[i] = q0[-(i + 1) * step];
-    }
-    filter_line(pv, qv, bS, chroma, indexA, alpha, beta);
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        q0[i * step] = qv[i];
-        q0[-(i + 1) * step] = pv[i];
-    }
-}
-
-__device__ __forceinline__ void edge_params(const PicDesc &p, int mbP, int cur, int comp, int &indexA, int &alpha, int &beta)
-{
-    const h264r_mb P = p.mbs[mbP], Q = p.mbs[cur];
-    const h264r_slice sq = p.slices[min((uint32_t)Q.slice, p.num_slices - 1)];
-    int qPp, qPq;
-    if (comp == 0) {
-        qPp = P.type == H264R_MB_IPCM ? 0 : P.qpy;
-        qPq = Q.type == H264R_MB_IPCM ? 0 : Q.qpy;
-    } else {
-        int off = sq.chroma_qp_offset[comp - 1];
-        qPp = chroma_qp(P.type == H264R_MB_IPCM ? 0 : P.qpy, off);
-        qPq = chroma_qp(Q.type == H264R_MB_IPCM ? 0 : Q.qpy, off);
-    }
-    int qPav = (qPp + qPq + 1) >> 1;
-    indexA = H264R_CLIP3(0, 51, qPav + sq.filter_offset_a);
-    int indexB = H264R_CLIP3(0, 51, qPav + sq.filter_offset_b);
-    alpha = kAlpha[indexA];
-    beta = kBeta[indexB];
-}
-
-// data of one MB step that does not depend on the wavefront, prefetched
-// while the previous MB of the row is being filtered
-struct DbPrefetch {
-    uint4 luma;       // this lane's luma row (lanes 0..15)
-    uint2 chroma;     // this lane's chroma row (lanes 16..31)
-    uint8_t bv[4], bh[4];  // this lane's strengths: vertical / horizontal edges
-    uint4 mq, ma, mb; // first 16 bytes of the records of the MB, its left and top MB
-    uint2 sq;         // slice parameters of the MB
+// what one lane needs of one MB, none of it written by the wavefront
+struct DbLine {
+    uint4 luma;              // the lane's luma line of the MB
+    uint2 chroma;            // the lane's chroma line
+    uint32_t lv, lh;         // luma strengths of the line, byte e = edge e
+    uint32_t cv, ch;         // chroma strengths, bytes 0, 1
+    uint4 pl, pc;            // thresholds (left, top, internal): luma, the lane's chroma plane
 };
 
-__device__ __forceinline__ void db_prefetch(const PicDesc &p, int row, int u, int lane, DbPrefetch &f)
+__device__ __forceinline__ void db_fetch(const PicDesc &p, int row, int u, int k, int comp, int ck, DbLine &f)
 {
-    const int uw = (int)p.units_w, cur = row * uw + u;
-    const int x0 = u * 16, y0 = row * 16;
+    const int cur = row * (int)p.units_w + u;
     const uint8_t *bs = p.bs + (size_t)cur * kBsBytes;
-    if (lane < 16) {
-        f.luma = __ldcg((const uint4 *)(plane_y(p) + (size_t)(y0 + lane) * p.W + x0));
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-            f.bv[e] = __ldcg(bs + kBsLumaV + 16 * e + lane);
-            f.bh[e] = __ldcg(bs + kBsLumaH + 16 * e + lane);
-        }
-    } else {
-        const int comp = lane < 24 ? 0 : 1, k = lane & 7;
-        f.chroma = __ldcg((const uint2 *)(plane_c(p, comp) + (size_t)(y0 / 2 + k) * p.Wc + x0 / 2));
-#pragma unroll
-        for (int e = 0; e < 2; e++) {
-            f.bv[e] = __ldcg(bs + kBsChromaV + 8 * e + k);
-            f.bh[e] = __ldcg(bs + kBsChromaH + 8 * e + k);
-        }
-    }
-    const uint4 *recs = (const uint4 *)p.mbs;  // h264r_mb is 32 bytes = 2 x uint4
-    f.mq = __ldg(recs + 2 * cur);
-    f.ma = u > 0 ? __ldg(recs + 2 * (cur - 1)) : f.mq;
-    f.mb = row > 0 ? __ldg(recs + 2 * (cur - uw)) : f.mq;
-    f.sq = __ldg((const uint2 *)p.slices + min((uint32_t)(f.mq.z & 0xFFFF), p.num_slices - 1));
+    f.luma = __ldcg((const uint4 *)(plane_y(p) + (size_t)(row * 16 + k) * p.W + u * 16));
+    f.chroma = __ldcg((const uint2 *)(plane_c(p, comp) + (size_t)(row * 8 + ck) * p.Wc + u * 8));
+    f.lv = __ldcg((const uint32_t *)(bs + bs_lv(0, k)));
+    f.lh = __ldcg((const uint32_t *)(bs + bs_lh(0, k)));
+    f.cv = __ldcg((const uint16_t *)(bs + bs_cv(0, ck)));
+    f.ch = __ldcg((const uint16_t *)(bs + bs_ch(0, ck)));
+    f.pl = __ldcg((const uint4 *)(bs + kBsParams));
+    f.pc = __ldcg((const uint4 *)(bs + kBsParams + 16 + 16 * comp));
 }
 
-__device__ __forceinline__ int rec_type(uint4 r) { return r.x & 255; }
-__device__ __forceinline__ int rec_flags(uint4 r) { return (r.x >> 8) & 255; }
-__device__ __forceinline__ int rec_qpy(uint4 r) { return (r.x >> 16) & 255; }
-__device__ __forceinline__ int rec_slice(uint4 r) { return r.z & 0xFFFF; }
-
-// alpha / beta / indexA of an edge from the p and q records (8.7.2.2)
-__device__ __forceinline__ void edge_params_rec(uint2 sraw, uint4 P, uint4 Q, int comp, int &indexA, int &alpha, int &beta)
+// Clear the strengths of the steps at or after the point where the
+// reference's bS derivation fails (only pictures with undecoded MBs).
+__device__ __forceinline__ void db_mask_stop(int cur, uint32_t stop, int k, int comp, int ck, DbLine &f)
 {
-    h264r_slice sq;
-    memcpy(&sq, &sraw, sizeof(sq));
-    int qyp = rec_type(P) == H264R_MB_IPCM ? 0 : rec_qpy(P);
-    int qyq = rec_type(Q) == H264R_MB_IPCM ? 0 : rec_qpy(Q);
-    int qPp = qyp, qPq = qyq;
-    if (comp) {
-        int off = sq.chroma_qp_offset[comp - 1];
-        qPp = chroma_qp(qyp, off);
-        qPq = chroma_qp(qyq, off);
+    const uint32_t stop_mb = stop >> 10;
+    if ((uint32_t)cur < stop_mb) return;
+    if ((uint32_t)cur > stop_mb) {
+        f.lv = f.lh = f.cv = f.ch = 0;
+        return;
     }
-    int qPav = (qPp + qPq + 1) >> 1;
-    indexA = H264R_CLIP3(0, 51, qPav + sq.filter_offset_a);
-    int indexB = H264R_CLIP3(0, 51, qPav + sq.filter_offset_b);
-    alpha = kAlpha[indexA];
-    beta = kBeta[indexB];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        if (stop_key(cur, SEQ_LV0 + e, k) >= stop) f.lv &= ~(0xFFu << (8 * e));
+        if (stop_key(cur, e == 0 ? SEQ_LH0 : SEQ_LH4 + e - 1, k) >= stop) f.lh &= ~(0xFFu << (8 * e));
+    }
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+        if (stop_key(cur, (e == 0 ? SEQ_CBV0 : SEQ_CBV4) + comp, ck) >= stop) f.cv &= ~(0xFFu << (8 * e));
+        if (stop_key(cur, (e == 0 ? SEQ_CBH0 : SEQ_CBH4) + comp, ck) >= stop) f.ch &= ~(0xFFu << (8 * e));
+    }
 }
 
-__device__ void deblock_row_frame(const PicDesc &p, int row, DbTile &t, const LaunchState &st)
+__device__ __forceinline__ int db_tc0(uint32_t prm, int bS) { return (prm >> (11 + 5 * bS)) & 31; }
+
+// 8.7.2.3 / 8.7.2.4 on the luma line v with q0 at index Q
+// (Filtering_process_for_edges_with_bS_less_than_4 / _equal_to_4,
+// H264PictureDeblockingFilterProcess.cpp:1373-1522).  bS 4 occurs on MB
+// edges only.
+template <int Q, bool MBEDGE, int N>
+__device__ __forceinline__ void db_luma(int (&v)[N], int bS, uint32_t prm)
+{
+    const int alpha = prm & 255, beta = (prm >> 8) & 255;
+    const int p0 = v[Q - 1], p1 = v[Q - 2], p2 = v[Q - 3], q0 = v[Q], q1 = v[Q + 1], q2 = v[Q + 2];
+    if (bS == 0 || abs(p0 - q0) >= alpha || abs(p1 - p0) >= beta || abs(q1 - q0) >= beta) return;
+    const bool ap = abs(p2 - p0) < beta, aq = abs(q2 - q0) < beta;
+    if (MBEDGE && bS == 4) {
+        const int p3 = v[Q - 4], q3 = v[Q + 3];
+        const bool sm = abs(p0 - q0) < ((alpha >> 2) + 2);
+        if (ap && sm) {
+            v[Q - 1] = (p2 + 2 * p1 + 2 * p0 + 2 * q0 + q1 + 4) >> 3;
+            v[Q - 2] = (p2 + p1 + p0 + q0 + 2) >> 2;
+            v[Q - 3] = (2 * p3 + 3 * p2 + p1 + p0 + q0 + 4) >> 3;
+        } else {
+            v[Q - 1] = (2 * p1 + p0 + q1 + 2) >> 2;
+        }
+        if (aq && sm) {
+            v[Q] = (p1 + 2 * p0 + 2 * q0 + 2 * q1 + q2 + 4) >> 3;
+            v[Q + 1] = (p0 + q0 + q1 + q2 + 2) >> 2;
+            v[Q + 2] = (2 * q3 + 3 * q2 + q1 + q0 + p0 + 4) >> 3;
+        } else {
+            v[Q] = (2 * q1 + q0 + p1 + 2) >> 2;
+        }
+        return;
+    }
+    const int tc0 = db_tc0(prm, bS);
+    const int tc = tc0 + ap + aq;
+    const int delta = H264R_CLIP3(-tc, tc, (((q0 - p0) << 2) + (p1 - q1) + 4) >> 3);
+    v[Q - 1] = clip1(p0 + delta);
+    v[Q] = clip1(q0 - delta);
+    if (ap) v[Q - 2] = (p1 + H264R_CLIP3(-tc0, tc0, (p2 + ((p0 + q0 + 1) >> 1) - (p1 << 1)) >> 1)) & 255;
+    if (aq) v[Q + 1] = (q1 + H264R_CLIP3(-tc0, tc0, (q2 + ((p0 + q0 + 1) >> 1) - (q1 << 1)) >> 1)) & 255;
+}
+
+// chroma line (chromaStyleFilteringFlag = 1): only p0 and q0 change
+template <int Q, bool MBEDGE, int N>
+__device__ __forceinline__ void db_chroma(int (&v)[N], int bS, uint32_t prm)
+{
+    const int alpha = prm & 255, beta = (prm >> 8) & 255;
+    const int p0 = v[Q - 1], p1 = v[Q - 2], q0 = v[Q], q1 = v[Q + 1];
+    if (bS == 0 || abs(p0 - q0) >= alpha || abs(p1 - p0) >= beta || abs(q1 - q0) >= beta) return;
+    if (MBEDGE && bS == 4) {
+        v[Q - 1] = (2 * p1 + p0 + q1 + 2) >> 2;
+        v[Q] = (2 * q1 + q0 + p1 + 2) >> 2;
+        return;
+    }
+    const int tc = db_tc0(prm, bS) + 1;
+    const int delta = H264R_CLIP3(-tc, tc, (((q0 - p0) << 2) + (p1 - q1) + 4) >> 3);
+    v[Q - 1] = clip1(p0 + delta);
+    v[Q] = clip1(q0 - delta);
+}
+
+__device__ __forceinline__ uint32_t pack4(int a, int b, int c, int d)
+{
+    return (uint32_t)(a & 255) | ((uint32_t)(b & 255) << 8) | ((uint32_t)(c & 255) << 16) | ((uint32_t)(d & 255) << 24);
+}
+
+__device__ void deblock_pair_frame(const PicDesc &p, int pair, DbPairSmem &s, const LaunchState &st)
 {
     const int lane = threadIdx.x & 31;
-    const int uw = (int)p.units_w, W = p.W, Wc = p.Wc;
+    const int h = lane >> 4, k = lane & 15, comp = k >> 3, ck = k & 7;
+    const int uw = (int)p.units_w, rows = (int)p.units_h, W = p.W, Wc = p.Wc;
+    const int row = 2 * pair + h;
+    const bool row_ok = row < rows;
+    const bool has_second = 2 * pair + 1 < rows;
+    const int steps = has_second ? uw + 2 : uw;
     int *prog = p.progress + p.units_h;
     uint8_t *Y = plane_y(p);
-    const uint32_t stop = p.deblock_stop, stop_mb = stop >> 10;
-    const bool luma = lane < 16;
-    const int k = luma ? lane : (lane & 7);          // line index
-    const int comp = luma ? 0 : (lane < 24 ? 1 : 2);
-    const int cseq = comp == 2 ? 1 : 0;
-    uint8_t *C = luma ? nullptr : plane_c(p, comp - 1);
-    int(*ct)[12] = luma ? nullptr : t.c[comp - 1];
-    DbPrefetch nxt;
-    db_prefetch(p, row, 0, lane, nxt);
-    for (int u = 0; u < uw; u++) {
-        const int cur = row * uw + u;
-        const DbPrefetch f = nxt;
-        if (u + 1 < uw) db_prefetch(p, row, u + 1, lane, nxt);
-        if (row > 0 && !wait_progress(st, prog + row - 1, min(u + 2, uw))) return;
-        if ((uint32_t)cur <= stop_mb) {
-            const int x0 = u * 16, y0 = row * 16;
-            // the four rows above: final for this MB once the wait returned
-            uint4 above_l = make_uint4(0, 0, 0, 0);
-            uint2 above_c = make_uint2(0, 0);
-            if (row > 0) {
-                if (lane < 4) above_l = __ldcg((const uint4 *)(Y + (size_t)(y0 - 4 + lane) * W + x0));
-                else if (lane < 12) above_c = __ldcg((const uint2 *)(plane_c(p, (lane - 4) >> 2) + (size_t)(y0 / 2 - 4 + ((lane - 4) & 3)) * Wc + x0 / 2));
-            }
-            // left neighbour columns 12..15 (this warp's previous MB) -> -4..-1, then the MB itself
-            if (luma) {
-                if (u > 0) {
+    uint8_t *C = plane_c(p, comp);
+    int *tl = s.l[h];
+    int *tc = s.c[2 * h + comp];
+    int left[4] = {0, 0, 0, 0}, cleft[4] = {0, 0, 0, 0};
+    DbLine nxt;
+    if (row_ok && h == 0) db_fetch(p, row, 0, k, comp, ck, nxt);
+    for (int step = 0; step < steps; step++) {
+        const int u = step - 2 * h;                 // this half's MB column
+        const bool act = row_ok && u >= 0 && u < uw;
+        DbLine f = nxt;
+        if (row_ok && u + 1 >= 0 && u + 1 < uw) db_fetch(p, row, u + 1, k, comp, ck, nxt);
+        const int x0 = u * 16, y0 = row * 16;
+        if (act) {
+            db_mask_stop(row * uw + u, p.deblock_stop, k, comp, ck, f);
+            // ---- vertical edges, in registers
+            int v[20];
+            int w[12];
 #pragma unroll
-                    for (int i = 0; i < 4; i++) t.l[k + 4][i] = t.l[k + 4][16 + i];
+            for (int i = 0; i < 4; i++) { v[i] = left[i]; w[i] = cleft[i]; }
+            unpack16(f.luma, &v[4]);
+            unpack8(f.chroma, &w[4]);
+            db_luma<4, true>(v, f.lv & 255, f.pl.x);
+            db_luma<8, false>(v, (f.lv >> 8) & 255, f.pl.z);
+            db_luma<12, false>(v, (f.lv >> 16) & 255, f.pl.z);
+            db_luma<16, false>(v, f.lv >> 24, f.pl.z);
+            db_chroma<4, true>(w, f.cv & 255, f.pc.x);
+            db_chroma<8, false>(w, (f.cv >> 8) & 255, f.pc.z);
+            if (u > 0) {
+                // the left MB's last columns are final now
+                const uint32_t lw = pack4(v[0], v[1], v[2], v[3]);
+                const uint32_t cw = pack4(w[0], w[1], w[2], w[3]);
+                *(uint32_t *)(Y + (size_t)(y0 + k) * W + x0 - 4) = lw;
+                *(uint32_t *)(C + (size_t)(y0 / 2 + ck) * Wc + x0 / 2 - 4) = cw;
+                if (h == 0) {
+                    const int slot = (u - 1) % 3;
+                    if (k >= 12) s.ring_l[slot][k - 12].w = lw;
+                    if (ck >= 4) s.ring_c[slot][comp][ck - 4].y = cw;
                 }
-                unpack16(f.luma, &t.l[k + 4][4]);
-            } else {
-                if (u > 0) {
+            }
 #pragma unroll
-                    for (int i = 0; i < 4; i++) ct[k + 4][i] = ct[k + 4][8 + i];
-                }
-                unpack8(f.chroma, &ct[k + 4][4]);
-            }
-            if (row > 0) {
-                if (lane < 4) unpack16(above_l, &t.l[lane][4]);
-                else if (lane < 12) unpack8(above_c, &t.c[(lane - 4) >> 2][(lane - 4) & 3][4]);
-            }
-            __syncwarp();
-            // filter controls (Deblocking_filter_process 90-160, non-MBAFF)
-            const int sl = rec_slice(f.mq);
-            const int idc = (f.sq.y >> 0) & 255;  // disable_deblocking_filter_idc (byte 4 of h264r_slice)
-            const bool hasA = u > 0 && rec_slice(f.ma) == sl;
-            const bool hasB = row > 0 && rec_slice(f.mb) == sl;
-            const bool left = u > 0 && idc != 1 && !(idc == 2 && !hasA);
-            const bool top = row > 0 && idc != 1 && !(idc == 2 && !hasB);
-            const bool internal = idc != 1;
-            const bool t8 = (rec_flags(f.mq) & H264R_MBF_T8x8) != 0;
-            auto allowed = [&](int seq, int kk) -> bool { return stop_key(cur, seq, kk) < stop; };
-            int iA, al, be;
-            // ---- vertical edges (each lane owns one line)
-            if (luma) {
-                int *line = &t.l[k + 4][4];
-                if (left && f.bv[0] && allowed(SEQ_LV0, k)) {
-                    edge_params_rec(f.sq, hasA ? f.ma : f.mq, f.mq, 0, iA, al, be);
-                    filter_tile_line(line, 1, f.bv[0], false, iA, al, be);
-                }
-                if (internal) {
-                    edge_params_rec(f.sq, f.mq, f.mq, 0, iA, al, be);
-                    if (!t8 && f.bv[1] && allowed(SEQ_LV4, k)) filter_tile_line(line + 4, 1, f.bv[1], false, iA, al, be);
-                    if (f.bv[2] && allowed(SEQ_LV8, k)) filter_tile_line(line + 8, 1, f.bv[2], false, iA, al, be);
-                    if (!t8 && f.bv[3] && allowed(SEQ_LV12, k)) filter_tile_line(line + 12, 1, f.bv[3], false, iA, al, be);
+            for (int j = 0; j < 16; j++) tl[(k + 4) * 17 + j] = v[4 + j];
+#pragma unroll
+            for (int j = 0; j < 8; j++) tc[(ck + 4) * 12 + j] = w[4 + j];
+        }
+        // ---- the row above: final once its warp is two MBs ahead
+        const int u0 = step;  // first row's MB column
+        if (2 * pair > 0 && u0 < uw && !wait_progress(st, prog + 2 * pair - 1, min(u0 + 2, uw))) return;
+        if (act && row > 0) {
+            if (h == 0) {
+                if (k < 4) {
+                    const uint4 a = __ldcg((const uint4 *)(Y + (size_t)(y0 - 4 + k) * W + x0));
+                    unpack16(a, &tl[k * 17]);
+                } else if (k < 12) {
+                    const int pl = (k - 4) >> 2, r = (k - 4) & 3;
+                    const uint2 a = __ldcg((const uint2 *)(plane_c(p, pl) + (size_t)(y0 / 2 - 4 + r) * Wc + x0 / 2));
+                    unpack8(a, &s.c[pl][r * 12]);
                 }
             } else {
-                int *line = &ct[k + 4][4];
-                if (left && f.bv[0] && allowed(SEQ_CBV0 + cseq, k)) {
-                    edge_params_rec(f.sq, hasA ? f.ma : f.mq, f.mq, comp, iA, al, be);
-                    filter_tile_line(line, 1, f.bv[0], true, iA, al, be);
-                }
-                if (internal && f.bv[1] && allowed(SEQ_CBV4 + cseq, k)) {
-                    edge_params_rec(f.sq, f.mq, f.mq, comp, iA, al, be);
-                    filter_tile_line(line + 4, 1, f.bv[1], true, iA, al, be);
-                }
-            }
-            __syncwarp();
-            // ---- horizontal edges (each lane owns one column)
-            if (luma) {
-                int *col = &t.l[4][k + 4];
-                if (top && f.bh[0] && allowed(SEQ_LH0, k)) {
-                    edge_params_rec(f.sq, hasB ? f.mb : f.mq, f.mq, 0, iA, al, be);
-                    filter_tile_line(col, 20, f.bh[0], false, iA, al, be);
-                }
-                if (internal) {
-                    edge_params_rec(f.sq, f.mq, f.mq, 0, iA, al, be);
-                    if (!t8 && f.bh[1] && allowed(SEQ_LH4, k)) filter_tile_line(col + 4 * 20, 20, f.bh[1], false, iA, al, be);
-                    if (f.bh[2] && allowed(SEQ_LH8, k)) filter_tile_line(col + 8 * 20, 20, f.bh[2], false, iA, al, be);
-                    if (!t8 && f.bh[3] && allowed(SEQ_LH12, k)) filter_tile_line(col + 12 * 20, 20, f.bh[3], false, iA, al, be);
-                }
-            } else {
-                int *col = &ct[4][k + 4];
-                if (top && f.bh[0] && allowed(SEQ_CBH0 + cseq, k)) {
-                    edge_params_rec(f.sq, hasB ? f.mb : f.mq, f.mq, comp, iA, al, be);
-                    filter_tile_line(col, 12, f.bh[0], true, iA, al, be);
-                }
-                if (internal && f.bh[1] && allowed(SEQ_CBH4 + cseq, k)) {
-                    edge_params_rec(f.sq, f.mq, f.mq, comp, iA, al, be);
-                    filter_tile_line(col + 4 * 12, 12, f.bh[1], true, iA, al, be);
-                }
-            }
-            __syncwarp();
-            // ---- write back: the MB, the left MB's last 3 columns, the MB above's last 3 rows
-            if (luma) {
-                *(uint4 *)(Y + (size_t)(y0 + k) * W + x0) = pack16(&t.l[k + 4][4]);
-                if (u > 0) {
-                    uint8_t *d = Y + (size_t)(y0 + k) * W + x0 - 3;
-                    d[0] = (uint8_t)t.l[k + 4][1];
-                    d[1] = (uint8_t)t.l[k + 4][2];
-                    d[2] = (uint8_t)t.l[k + 4][3];
-                }
-            } else {
-                *(uint2 *)(C + (size_t)(y0 / 2 + k) * Wc + x0 / 2) = pack8(&ct[k + 4][4]);
-                if (u > 0) {
-                    uint8_t *d = C + (size_t)(y0 / 2 + k) * Wc + x0 / 2 - 3;
-                    d[0] = (uint8_t)ct[k + 4][1];
-                    d[1] = (uint8_t)ct[k + 4][2];
-                    d[2] = (uint8_t)ct[k + 4][3];
-                }
-            }
-            if (row > 0) {
-                if (lane < 3) *(uint4 *)(Y + (size_t)(y0 - 3 + lane) * W + x0) = pack16(&t.l[1 + lane][4]);
-                else if (lane < 9) {
-                    const int pl = (lane - 3) / 3, rr = (lane - 3) % 3;
-                    *(uint2 *)(plane_c(p, pl) + (size_t)(y0 / 2 - 3 + rr) * Wc + x0 / 2) = pack8(&t.c[pl][1 + rr][4]);
+                const int slot = u % 3;
+                if (k < 4) unpack16(s.ring_l[slot][k], &tl[k * 17]);
+                else if (k < 12) {
+                    const int pl = (k - 4) >> 2, r = (k - 4) & 3;
+                    unpack8(s.ring_c[slot][pl][r], &s.c[2 + pl][r * 12]);
                 }
             }
         }
         __syncwarp();
-        if (lane == 0) st_release(prog + row, u + 1);
+        // ---- horizontal edges, in registers (the lane owns a column)
+        if (act) {
+            int v[20];
+            int w[12];
+#pragma unroll
+            for (int i = 0; i < 20; i++) v[i] = tl[i * 17 + k];
+#pragma unroll
+            for (int i = 0; i < 12; i++) w[i] = tc[i * 12 + ck];
+            db_luma<4, true>(v, f.lh & 255, f.pl.y);
+            db_luma<8, false>(v, (f.lh >> 8) & 255, f.pl.z);
+            db_luma<12, false>(v, (f.lh >> 16) & 255, f.pl.z);
+            db_luma<16, false>(v, f.lh >> 24, f.pl.z);
+            db_chroma<4, true>(w, f.ch & 255, f.pc.y);
+            db_chroma<8, false>(w, (f.ch >> 8) & 255, f.pc.z);
+#pragma unroll
+            for (int i = 1; i < 19; i++) tl[i * 17 + k] = v[i];
+            tc[3 * 12 + ck] = w[3];
+            tc[4 * 12 + ck] = w[4];
+            tc[7 * 12 + ck] = w[7];
+            tc[8 * 12 + ck] = w[8];
+        }
+        __syncwarp();
+        // ---- store the MB and the three rows above it
+        if (act) {
+            const uint4 lr = pack16(&tl[(k + 4) * 17]);
+            const uint2 cr = pack8(&tc[(ck + 4) * 12]);
+            *(uint4 *)(Y + (size_t)(y0 + k) * W + x0) = lr;
+            *(uint2 *)(C + (size_t)(y0 / 2 + ck) * Wc + x0 / 2) = cr;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                left[i] = tl[(k + 4) * 17 + 12 + i];
+                cleft[i] = tc[(ck + 4) * 12 + 4 + i];
+            }
+            if (h == 0) {
+                if (k >= 12) s.ring_l[u % 3][k - 12] = lr;
+                if (ck >= 4) s.ring_c[u % 3][comp][ck - 4] = cr;
+            }
+            if (row > 0) {
+                if (k < 3) *(uint4 *)(Y + (size_t)(y0 - 3 + k) * W + x0) = pack16(&tl[(1 + k) * 17]);
+                else if (k < 9) {
+                    const int pl = (k - 3) / 3, r = (k - 3) % 3;
+                    *(uint2 *)(plane_c(p, pl) + (size_t)(y0 / 2 - 3 + r) * Wc + x0 / 2) = pack8(&s.c[2 * h + pl][(1 + r) * 12]);
+                }
+            }
+        }
+        __syncwarp();
+        // the second row publishes its progress (the next pair waits on it)
+        if (lane == 0 && has_second && step >= 2) st_release(prog + 2 * pair + 1, step - 1);
     }
 }
 
@@ -1709,8 +1753,9 @@ __global__ void __launch_bounds__(32) k_deblock(const PicDesc *__restrict__ pics
     if (!p.deblock) return;
     const int row = (int)(g - p.row_base);
     if (!p.mbaff) {
-        __shared__ DbTile tile;
-        deblock_row_frame(p, row, tile, st);
+        // rows are handled in pairs by the warp of the even row
+        __shared__ DbPairSmem pair_smem;
+        if ((row & 1) == 0) deblock_pair_frame(p, row >> 1, pair_smem, st);
         return;
     }
     const int uw = (int)p.units_w;

@@ -11,6 +11,9 @@
 // the library holds until the process exits.
 #include <cuda_runtime.h>
 
+#include <cstddef>
+#include <cstdint>
+
 #include <mutex>
 
 #include "h264r_device.cuh"
@@ -34,10 +37,11 @@ struct NoAllocScratch {
     int error;                                // device error word of the call
     unsigned int ticket[2];                   // wavefront row tickets
     int progress[2 * kNoAllocMaxRows];        // wavefront progress counters
-    uint8_t bs[kNoAllocMaxMbs * h264r::kBsBytes];  // boundary strengths
+    alignas(256) uint8_t bs[kNoAllocMaxMbs * h264r::kBsBytes];  // boundary strengths (read with 16-byte loads)
 };
+static_assert(offsetof(NoAllocScratch, bs) % 256 == 0, "the bS table must start on a 256-byte boundary");
 
-// The scratch: ~1.6 MB per device, shared by every call in the process.
+// The scratch: ~2.1 MB per device, shared by every call in the process.
 static __device__ __align__(256) NoAllocScratch g_scratch;
 
 // Device address of g_scratch, resolved once per device with that device
@@ -61,7 +65,7 @@ __global__ void k_noalloc_init(PicDesc d, NoAllocScratch *s)
 
 extern "C" int h264r_deblock_picture_noalloc(const h264r_picture *pic, uint8_t *planes, void *cuda_stream)
 {
-    if (!pic || !planes || !pic->mbs || !pic->slices) return H264R_ERR_INVALID_ARG;
+    if (!pic || !planes || !pic->mbs || !pic->slices || ((uintptr_t)planes & 15)) return H264R_ERR_INVALID_ARG;
     if (pic->structure != H264R_STRUCT_FRAME) return H264R_ERR_UNSUPPORTED;
     if (pic->width_mbs == 0 || pic->height_mbs == 0 || pic->num_slices == 0 ||
         pic->num_mbs != (uint32_t)pic->width_mbs * pic->height_mbs || (pic->mbaff && (pic->height_mbs & 1)))

@@ -314,13 +314,13 @@ void *h264r_ctx_cuda_stream(h264r_ctx *ctx);
  * pic: records of a reconstructed picture, every pointer device memory (as
  *      for h264r_submit_picture_device); pic->deblock is ignored.
  * planes: device address of the picture's samples, Y then Cb then Cr
- *      contiguous at coded size (the engine's DPB slot layout); filtered in
- *      place.  cuda_stream: the cudaStream_t to run on (0: legacy default).
+ *      contiguous at coded size (the engine's DPB slot layout), 16-byte
+ *      aligned; filtered in place.  cuda_stream: the cudaStream_t to run on (0: legacy default).
  * The scratch it needs (bS table, wavefront counters) is one static device
  * array compiled into the library, sized for pictures of at most
  * H264R_NOALLOC_MAX_MBS macroblocks and H264R_NOALLOC_MAX_MB_ROWS MB rows
  * (1920x1088 fits); larger pictures return H264R_ERR_TOO_LARGE.  Every GPU
- * that loads the library holds that array (about 1.6 MB) until the process
+ * that loads the library holds that array (about 2.1 MB) until the process
  * exits.  The first call on a device resolves the array's device address
  * (cudaGetSymbolAddress, with that device current); make that first call
  * before any stream capture.  All calls in a process share the one array:
