@@ -48,6 +48,8 @@ struct LaunchBuf {
     uint64_t dev_cap = 0;
     uint8_t *bs = nullptr;        // device, bS tables
     uint64_t bs_cap = 0;
+    uint8_t *ires = nullptr;      // device, intra residuals (768 bytes per MB)
+    uint64_t ires_cap = 0;
     uint8_t *rec_host = nullptr;  // pinned staging for host-resident records
     uint64_t rec_host_cap = 0;
     uint8_t *rec_dev = nullptr;   // device copy of the records
@@ -152,6 +154,7 @@ static void free_buf(LaunchBuf &b)
     if (b.host) cudaFreeHost(b.host);
     if (b.dev) cudaFree(b.dev);
     if (b.bs) cudaFree(b.bs);
+    if (b.ires) cudaFree(b.ires);
     if (b.rec_host) cudaFreeHost(b.rec_host);
     if (b.rec_dev) cudaFree(b.rec_dev);
     if (b.done) cudaEventDestroy(b.done);
@@ -448,6 +451,10 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
     if (rc) return rc;
     rc = ensure(ctx, &b.bs, &b.bs_cap, mbs * h264r::kBsBytes + 16, false);
     if (rc) return rc;
+    if (any_intra) {
+        rc = ensure(ctx, &b.ires, &b.ires_cap, mbs * 768 + 16, false);
+        if (rc) return rc;
+    }
     memset(b.host, 0, total);
     PicDesc *d = (PicDesc *)b.host;
     uint64_t mb_base = 0, row_base = 0, prog = 0;
@@ -482,6 +489,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
         p.nslots = s->cfg.dpb_slots;
         p.dst = s->dpb + (uint64_t)pic->dst_slot * s->slot_bytes;
         p.bs = b.bs + mb_base * h264r::kBsBytes;
+        p.ires = any_intra ? (int16_t *)b.ires + mb_base * 384 : nullptr;
         p.units_w = pic->width_mbs;
         p.units_h = pic->mbaff ? pic->height_mbs / 2 : pic->height_mbs;
         p.progress = (int *)(b.dev + prog_off) + prog;

@@ -79,6 +79,7 @@ struct PicDesc {
     int nslots;
     int flat_scaling;        // every scaling list is flat 16
     uint8_t *bs;             // deblocking strengths, kBsBytes per MB
+    int16_t *ires;           // intra MBs' residuals, 384 per MB (null: no intra MB)
     int *progress;           // per unit row progress counters (2 * units_h)
     uint32_t mb_base;        // first global MB index of this picture in the batch
     uint32_t row_base;       // first global unit row of this picture in the batch

@@ -78,6 +78,216 @@ __device__ bool wait_progress(const LaunchState &st, const int *flag, int target
 }
 
 // ======================================================================
+// Residual of one macroblock (8.5), whole warp
+// ======================================================================
+// The significance words of the payload are spread over the lanes and a
+// warp prefix sum gives the level index each word starts at; every block
+// then scatters its levels, already scaled (8.5.12.1 / 8.5.13.1), into the
+// residual tile, and the inverse transforms run in place.  No per-lane
+// arrays are indexed at run time.
+
+// 8.5.12.2 on a 4x4 block of the tile (row stride `st`), including the
+// final (x + 32) >> 6 (H264PictureBase.cpp:4229-4260)
+__device__ __forceinline__ void itrans4_tile(int32_t *b, int st)
+{
+    int32_t f[16];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int d0 = b[i * st], d1 = b[i * st + 1], d2 = b[i * st + 2], d3 = b[i * st + 3];
+        const int e0 = d0 + d2, e1 = d0 - d2, e2 = (d1 >> 1) - d3, e3 = d1 + (d3 >> 1);
+        f[i * 4 + 0] = e0 + e3; f[i * 4 + 1] = e1 + e2; f[i * 4 + 2] = e1 - e2; f[i * 4 + 3] = e0 - e3;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int g0 = f[j] + f[8 + j], g1 = f[j] - f[8 + j];
+        const int g2 = (f[4 + j] >> 1) - f[12 + j], g3 = f[4 + j] + (f[12 + j] >> 1);
+        b[0 * st + j] = (g0 + g3 + 32) >> 6;
+        b[1 * st + j] = (g1 + g2 + 32) >> 6;
+        b[2 * st + j] = (g1 - g2 + 32) >> 6;
+        b[3 * st + j] = (g0 - g3 + 32) >> 6;
+    }
+}
+
+__device__ __forceinline__ int norm4_class(int i, int j) { return ((i & 1) == 0 && (j & 1) == 0) ? 0 : (((i & 1) && (j & 1)) ? 1 : 2); }
+
+__device__ __forceinline__ int norm8_class(int i, int j)
+{
+    if (i % 4 == 0 && j % 4 == 0) return 0;
+    if (i % 2 == 1 && j % 2 == 1) return 1;
+    if (i % 4 == 2 && j % 4 == 2) return 2;
+    if ((i % 4 == 0 && j % 2 == 1) || (i % 2 == 1 && j % 4 == 0)) return 3;
+    if ((i % 4 == 0 && j % 4 == 2) || (i % 4 == 2 && j % 4 == 0)) return 4;
+    return 5;
+}
+
+// scaled coefficient of a 4x4 block (LevelScale4x4 from scan position k)
+__device__ __forceinline__ int scale4(const PicDesc &p, int list, int k, int raster, int qp, int v)
+{
+    const int ws = p.flat_scaling ? 16 : p.scaling[list * 16 + k];
+    const int ls = ws * kV4[qp % 6][norm4_class(raster >> 2, raster & 3)];
+    return qp >= 24 ? (v * ls) << (qp / 6 - 4) : (v * ls + (1 << (3 - qp / 6))) >> (4 - qp / 6);
+}
+
+__device__ __forceinline__ int scale8(const PicDesc &p, int list, int k, int raster, int qp, int v)
+{
+    const int ws = p.flat_scaling ? 16 : p.scaling[96 + list * 64 + k];
+    const int ls = ws * kV8[qp % 6][norm8_class(raster >> 3, raster & 7)];
+    return qp >= 36 ? (v * ls) << (qp / 6 - 6) : (v * ls + (1 << (5 - qp / 6))) >> (6 - qp / 6);
+}
+
+// res: 384 ints (luma 16x16 raster, Cb 8x8, Cr 8x8); dcs: 32 ints of
+// scratch.  ls4 / ls8: LevelScale lists of the luma blocks (intra 0 / 0,
+// inter 3 / 1); the chroma blocks use ls4 as well (quirk: the reference
+// scales chroma with the LevelScale4x4 it computed last, the luma one,
+// H264PictureBase.cpp:3752-3940).  Returns false for a malformed payload
+// (the residual is then zero).
+__device__ bool mb_residual(const PicDesc &p, const h264r_mb &m, int field, int ls4, int ls8, int32_t *res, int32_t *dcs)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int i = 0; i < 12; i++) res[lane + 32 * i] = 0;
+    CoefView cv;
+    bool ok = coef_view(p, m, cv);
+    const uint32_t mask = ok ? cv.mask : 0u;
+    if (mask == 0) {
+        __syncwarp();
+        return ok;
+    }
+    const int t8 = cv.t8;
+    const int nw = __popc(mask) + (t8 ? 3 * __popc(mask & 15u) : 0);
+    const uint32_t sw = lane < nw ? (uint32_t)cv.sig[lane] : 0u;
+    const int cnt = __popc(sw);
+    int inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc += t;
+    }
+    const int off = inc - cnt;
+    if (__shfl_sync(FULL, inc, 31) > cv.max_levels) {
+        __syncwarp();
+        return false;
+    }
+    auto word_of = [&](int bit) -> int {
+        const uint32_t before = mask & ((1u << bit) - 1u);
+        return __popc(before) + (t8 ? 3 * __popc(before & 15u) : 0);
+    };
+    const int qp = m.qpy;
+    const bool i16 = m.type == H264R_MB_I16x16;
+    const uint8_t *scan4 = field ? kField4x4 : kZigzag4x4;
+    const int16_t *lv = cv.lv;
+    // ---- Intra16x16 DC (8.5.10)
+    if (i16) {
+        const int w = word_of(16) & 31;
+        const uint32_t sg = (mask & H264R_CM_LUMA_DC) ? __shfl_sync(FULL, sw, w) : 0u;
+        const int o = __shfl_sync(FULL, off, w);
+        if (lane < 16) {
+            const int k = lane;
+            dcs[scan4[k]] = ((sg >> k) & 1) ? lv[o + __popc(sg & ((1u << k) - 1u))] : 0;
+        }
+        __syncwarp();
+        if (lane == 0) luma_dc(p, dcs, field, qp, dcs + 16);
+        __syncwarp();
+    }
+    // ---- luma levels
+    if (t8) {
+        const int b = lane >> 3, r = lane & 7;
+        const int w = (word_of(b) + (r >> 1)) & 31;
+        const uint32_t sg = __shfl_sync(FULL, sw, w);
+        const int o = __shfl_sync(FULL, off, w);
+        if (mask & (1u << b)) {
+            const int half = (r & 1) * 8;
+            int l = o + __popc(sg & ((1u << half) - 1u));
+            uint32_t bits = (sg >> half) & 255u;
+            const uint8_t *scan8 = field ? kField8x8 : kZigzag8x8;
+            const int bx = (b & 1) * 8, by = (b >> 1) * 8;
+            while (bits) {
+                const int t = __ffs(bits) - 1;
+                bits &= bits - 1;
+                const int k = 16 * (r >> 1) + half + t, rp = scan8[k];
+                res[(by + (rp >> 3)) * 16 + bx + (rp & 7)] = scale8(p, ls8, k, rp, qp, lv[l++]);
+            }
+        }
+    } else {
+        const int b = lane & 15;
+        const int w = word_of(b) & 31;
+        const uint32_t sg = __shfl_sync(FULL, sw, w);
+        const int o = __shfl_sync(FULL, off, w);
+        if (lane < 16) {
+            const int bx = kBlkX[b] * 4, by = kBlkY[b] * 4;
+            if (mask & (1u << b)) {
+                int l = o;
+                uint32_t bits = sg & 0xFFFFu;
+                while (bits) {
+                    const int k = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    const int rp = scan4[k];
+                    res[(by + (rp >> 2)) * 16 + bx + (rp & 3)] = scale4(p, ls4, k, rp, qp, lv[l++]);
+                }
+            }
+            if (i16) res[by * 16 + bx] = dcs[16 + kBlkY[b] * 4 + kBlkX[b]];
+        }
+    }
+    // ---- chroma levels (lanes 16..23: plane (lane-16)>>2, block (lane-16)&3)
+    const int pl = ((lane - 16) >> 2) & 1, cb = (lane - 16) & 3;
+    const bool chroma_lane = lane >= 16 && lane < 24;
+    const int wdc = word_of(17 + pl) & 31, wac = word_of(H264R_CM_CB_AC0 + 4 * pl + cb) & 31;
+    const uint32_t sdc = __shfl_sync(FULL, sw, wdc), sac = __shfl_sync(FULL, sw, wac);
+    const int odc = __shfl_sync(FULL, off, wdc), oac = __shfl_sync(FULL, off, wac);
+    const bool any_chroma = (mask >> 17) != 0;
+    if (chroma_lane && any_chroma) {
+        const int qpc = chroma_qp(qp, p.slices[min((uint32_t)m.slice, p.num_slices - 1)].chroma_qp_offset[pl]);
+        int32_t dc4[4] = {0, 0, 0, 0}, dcC[4];
+        if (mask & (1u << (17 + pl))) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) dc4[k] = ((sdc >> k) & 1) ? lv[odc + __popc(sdc & ((1u << k) - 1u))] : 0;
+        }
+        chroma_dc(p, dc4, field, qpc, ls4, dcC);
+        int32_t *blk = res + 256 + pl * 64 + (cb >> 1) * 32 + (cb & 1) * 4;
+        if (mask & (1u << (H264R_CM_CB_AC0 + 4 * pl + cb))) {
+            int l = oac;
+            uint32_t bits = sac & 0xFFFFu;  // AC list: positions 1..15 (a level at 0 is replaced by DC below)
+            while (bits) {
+                const int k = __ffs(bits) - 1;
+                bits &= bits - 1;
+                const int rp = scan4[k];
+                blk[(rp >> 2) * 8 + (rp & 3)] = scale4(p, ls4, k, rp, qpc, lv[l++]);
+            }
+        }
+        blk[0] = cb == 0 ? dcC[0] : cb == 1 ? dcC[1] : cb == 2 ? dcC[2] : dcC[3];
+    }
+    __syncwarp();
+    // ---- inverse transforms in place
+    if (t8) {
+        const int b = lane >> 3, r = lane & 7;
+        const int bx = (b & 1) * 8, by = (b >> 1) * 8;
+        const bool on = (mask >> b) & 1;
+        int o8[8];
+        if (on) {
+            int32_t *row = res + (by + r) * 16 + bx;
+            idct8_1d(row[0], row[1], row[2], row[3], row[4], row[5], row[6], row[7], o8);
+#pragma unroll
+            for (int j = 0; j < 8; j++) row[j] = o8[j];
+        }
+        __syncwarp();
+        if (on) {
+            int32_t *col = res + by * 16 + bx + r;
+            idct8_1d(col[0], col[16], col[32], col[48], col[64], col[80], col[96], col[112], o8);
+#pragma unroll
+            for (int i = 0; i < 8; i++) col[i * 16] = (o8[i] + 32) >> 6;
+        }
+    } else if (lane < 16) {
+        const int b = lane;
+        const int bx = kBlkX[b] * 4, by = kBlkY[b] * 4;
+        if (((mask >> b) & 1) || (i16 && dcs[16 + kBlkY[b] * 4 + kBlkX[b]] != 0)) itrans4_tile(res + by * 16 + bx, 16);
+    }
+    if (chroma_lane && any_chroma) itrans4_tile(res + 256 + pl * 64 + (cb >> 1) * 32 + (cb & 1) * 4, 8);
+    __syncwarp();
+    return ok;
+}
+
+// ======================================================================
 // K1: inter macroblocks, I_PCM, undecoded macroblocks
 // ======================================================================
 // One warp per MB, 4 MBs per block.  Lane l predicts rows 2*(l&1), +1 of
@@ -87,21 +297,89 @@ __device__ bool wait_progress(const LaunchState &st, const int *flag, int target
 constexpr int kInterWarps = 4;
 
 struct InterWarpSmem {
-    uint8_t win[32][64];   // per-lane luma reference window, 7 rows x 9 cols
+    uint32_t win[32][21];  // per-lane luma reference window, 7 rows x 12 bytes
     int32_t res[384];      // residual: luma raster 16x16, Cb 8x8, Cr 8x8
-    int32_t t8[4][64];     // 8x8 transform work area
+    int32_t dcs[32];       // Intra16x16 DC work area
     __align__(16) uint8_t out[384];
 };
 
 #define TAP6(a, b, c_, d, e, f) ((a) - 5 * (b) + 20 * (c_) + 20 * (d) - 5 * (e) + (f))
 
+// Reference window of one lane: rows yi-2..yi+4, columns xi-2..xi+6 of a
+// luma plane, clamped at the picture edges like luma_sample (8.4.2.2.1,
+// H264InterPrediction.cpp:2344-2363), as 7 rows of 12 bytes (byte c+2 of
+// row r+2 holds sample (xi+c, yi+r)).  Away from the edges each row is three
+// aligned 32-bit loads and two funnel shifts; the loads may read up to three
+// bytes past the window, which stay inside the picture allocation.
+__device__ __forceinline__ void load_luma_window(const RefView &rv, int ymax, int xi, int yi, uint32_t *win)
+{
+    const int x0 = xi - 2, y0 = yi - 2;
+    if (x0 >= 0 && xi + 6 <= rv.xmax && y0 >= 0 && yi + 4 <= ymax) {
+        const int sh = (x0 & 3) * 8;
+        const uint8_t *row = rv.y + (size_t)y0 * rv.ystride + (x0 & ~3);
+#pragma unroll
+        for (int r = 0; r < 7; r++) {
+            const uint32_t *q = (const uint32_t *)(row + (size_t)r * rv.ystride);
+            const uint32_t a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+            win[3 * r] = __funnelshift_r(a, b, sh);
+            win[3 * r + 1] = __funnelshift_r(b, c, sh);
+            win[3 * r + 2] = c >> sh;
+        }
+        return;
+    }
+    for (int r = 0; r < 7; r++) {
+        const uint8_t *row = rv.y + (size_t)H264R_CLIP3(0, ymax, y0 + r) * rv.ystride;
+        uint32_t w[3] = {0, 0, 0};
+#pragma unroll
+        for (int c = 0; c < 9; c++) w[c >> 2] |= (uint32_t)__ldg(row + H264R_CLIP3(0, rv.xmax, x0 + c)) << (8 * (c & 3));
+        win[3 * r] = w[0];
+        win[3 * r + 1] = w[1];
+        win[3 * r + 2] = w[2];
+    }
+}
+
+// 8.4.2.2.2 for the 2x2 chroma samples at (xi, yi) .. (xi+1, yi+1)
+// (Chroma_sample_interpolation_process, H264InterPrediction.cpp:2485-2522):
+// the 3x3 neighbourhood is held in three registers.
+__device__ __forceinline__ void chroma_2x2(const uint8_t *pl, int stride, int xmax, int ymax, int xi, int yi, int xf, int yf, int out[4])
+{
+    uint32_t rw[3];
+    if (xi >= 0 && xi + 2 <= xmax && yi >= 0 && yi + 2 <= ymax) {
+        const int sh = (xi & 3) * 8;
+        const uint8_t *row = pl + (size_t)yi * stride + (xi & ~3);
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+            const uint32_t *q = (const uint32_t *)(row + (size_t)r * stride);
+            rw[r] = __funnelshift_r(__ldg(q), __ldg(q + 1), sh);
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+            const uint8_t *row = pl + (size_t)H264R_CLIP3(0, ymax, yi + r) * stride;
+            uint32_t w = 0;
+#pragma unroll
+            for (int c = 0; c < 3; c++) w |= (uint32_t)__ldg(row + H264R_CLIP3(0, xmax, xi + c)) << (8 * c);
+            rw[r] = w;
+        }
+    }
+    const int w00 = (8 - xf) * (8 - yf), w01 = xf * (8 - yf), w10 = (8 - xf) * yf, w11 = xf * yf;
+#define CB(r, c) ((int)((rw[r] >> (8 * (c))) & 255))
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+            out[i * 2 + j] = (w00 * CB(i, j) + w01 * CB(i, j + 1) + w10 * CB(i + 1, j) + w11 * CB(i + 1, j + 1) + 32) >> 6;
+#undef CB
+}
+
 // 8.4.2.2.1 for a 2x4 group of samples (rows i0..i0+1, cols 0..3 of the
-// window origin) from win[(r+2)*9 + (c+2)], r in -2..4, c in -2..6.  The
+// window origin) from the window bytes win[(r+2)*12 + (c+2)], r in -2..4,
+// c in -2..6.  The
 // centre sample j uses horizontal taps first: the taps are exact integers,
 // so the order of the two 6-tap passes does not change j1.
 __device__ __forceinline__ void mc_luma_2x4(const uint8_t *win, int xf, int yf, int out[8])
 {
-#define WV(r, c) ((int)win[((r) + 2) * 9 + (c) + 2])
+#define WV(r, c) ((int)win[((r) + 2) * 12 + (c) + 2])
     if ((xf | yf) == 0) {
 #pragma unroll
         for (int i = 0; i < 2; i++)
@@ -179,10 +457,26 @@ __global__ void __launch_bounds__(32 * kInterWarps) k_inter(const PicDesc *__res
     const PicDesc p = pics[find_pic_by_mb(pics, npics, g)];
     const int addr = (int)(g - p.mb_base);
     const h264r_mb m = p.mbs[addr];
+    const int field = field_mb(p, addr);
+    if (is_intra_type(m.type)) {
+        // intra MB: only its residual, for the intra wavefront (k_intra).
+        // Stored clamped to [-255, 255]: Clip1(pred + r) is the same for
+        // every r beyond that range.
+        if (p.ires) {
+            if (!mb_residual(p, m, field, 0, 0, s.res, s.dcs) && lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
+            uint32_t *dst = (uint32_t *)(p.ires + (size_t)addr * 384);
+#pragma unroll
+            for (int t = 0; t < 6; t++) {
+                const int i = lane + 32 * t;
+                const int a = H264R_CLIP3(-255, 255, s.res[2 * i]), b = H264R_CLIP3(-255, 255, s.res[2 * i + 1]);
+                dst[i] = ((uint32_t)a & 0xFFFFu) | ((uint32_t)b << 16);
+            }
+        }
+        return;
+    }
     if (m.type != H264R_MB_INTER && m.type != H264R_MB_IPCM && m.type != H264R_MB_NONE) return;
     int x, y, dy;
     mb_origin(p, addr, x, y, dy);
-    const int field = field_mb(p, addr);
 
     if (m.type == H264R_MB_NONE) {
         for (int i = lane; i < 96; i += 32) ((uint32_t *)s.out)[i] = 0;
@@ -203,83 +497,8 @@ __global__ void __launch_bounds__(32 * kInterWarps) k_inter(const PicDesc *__res
         const int yAL0 = field ? (y - (y & 1)) / 2 : y;
         const int ymax = field ? p.H / 2 - 1 : p.H - 1;
         const int ymaxc = field ? p.Hc / 2 - 1 : p.Hc - 1;
-        // ---- residual first (lanes owning whole blocks), into s.res
-        for (int i = lane; i < 384; i += 32) s.res[i] = 0;
-        __syncwarp();
-        if (m.coef != H264R_NONE) {
-            CoefView cv;
-            if (!coef_view(p, m, cv)) {
-                if (lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
-                cv.mask = 0;
-            }
-            if (cv.t8) {
-                // 8 lanes per 8x8 block: lane = 8*b + row (8.5.13)
-                const int b = lane >> 3, r = lane & 7;
-                if (cv.mask & (1u << b)) {
-                    int w, l;
-                    coef_block(cv, b, w, l);
-                    const uint8_t *scan = field ? kField8x8 : kZigzag8x8;
-                    int32_t d[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                    for (int q = 0; q < 4; q++) {
-                        uint32_t sg = cv.sig[w + q];
-                        while (sg && l < cv.max_levels) {
-                            int kk = __ffs(sg) - 1;
-                            sg &= sg - 1;
-                            int v = cv.lv[l++];
-                            int rp = scan[16 * q + kk];
-                            if ((rp >> 3) == r) {
-                                int jj = rp & 7;
-                                int ls = level_scale8(p, 1, field, m.qpy % 6, r, jj);
-                                d[jj] = (m.qpy >= 36) ? (v * ls) << (m.qpy / 6 - 6) : (v * ls + (1 << (5 - m.qpy / 6))) >> (6 - m.qpy / 6);
-                            }
-                        }
-                    }
-                    int o[8];
-                    idct8_1d(d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], o);
-#pragma unroll
-                    for (int jj = 0; jj < 8; jj++) s.t8[b][r * 8 + jj] = o[jj];
-                }
-                __syncwarp();
-                if (cv.mask & (1u << b)) {
-                    const int c = r;  // now: column
-                    int o[8];
-                    idct8_1d(s.t8[b][0 * 8 + c], s.t8[b][1 * 8 + c], s.t8[b][2 * 8 + c], s.t8[b][3 * 8 + c], s.t8[b][4 * 8 + c],
-                             s.t8[b][5 * 8 + c], s.t8[b][6 * 8 + c], s.t8[b][7 * 8 + c], o);
-                    const int bx = (b & 1) * 8, by = (b >> 1) * 8;
-#pragma unroll
-                    for (int ii = 0; ii < 8; ii++) s.res[(by + ii) * 16 + bx + c] = (o[ii] + 32) >> 6;
-                }
-            } else if (lane < 16) {
-                if (cv.mask & (1u << lane)) {
-                    int32_t c[16], r[16];
-                    coef_list16(cv, lane, field, c);
-                    idct4x4(p, c, field, m.qpy, 3, false, r);
-                    const int bx = kBlkX[lane] * 4, by = kBlkY[lane] * 4;
-#pragma unroll
-                    for (int i = 0; i < 4; i++)
-#pragma unroll
-                        for (int j = 0; j < 4; j++) s.res[(by + i) * 16 + bx + j] = r[i * 4 + j];
-                }
-            }
-            if (lane >= 16 && lane < 24 && (cv.mask >> 17)) {
-                const int pl = (lane - 16) >> 2, b = (lane - 16) & 3;
-                const int qpc = chroma_qp(m.qpy, p.slices[min((uint32_t)m.slice, p.num_slices - 1)].chroma_qp_offset[pl]);
-                int32_t dcl[16], dc4[4], dcC[4];
-                coef_list16(cv, 17 + pl, 0, dcl);
-                dc4[0] = dcl[0]; dc4[1] = dcl[1]; dc4[2] = dcl[4]; dc4[3] = dcl[8];
-                chroma_dc(p, dc4, field, qpc, 3, dcC);
-                int32_t c[16], r[16];
-                coef_list16(cv, (pl ? H264R_CM_CR_AC0 : H264R_CM_CB_AC0) + b, field, c);
-                c[0] = dcC[b];
-                idct4x4(p, c, field, qpc, 3, true, r);
-                const int bx = (b & 1) * 4, by = (b >> 1) * 4;
-#pragma unroll
-                for (int i = 0; i < 4; i++)
-#pragma unroll
-                    for (int j = 0; j < 4; j++) s.res[256 + pl * 64 + (by + i) * 8 + bx + j] = r[i * 4 + j];
-            }
-            __syncwarp();
-        }
+        // ---- residual (8.5) into s.res
+        if (!mb_residual(p, m, field, 3, 1, s.res, s.dcs) && lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
         // ---- luma prediction: 4x4 block lane>>1 (raster), rows 2*(lane&1), +1
         {
             const int blk = lane >> 1, bx = blk & 3, by = blk >> 2, r0 = 2 * (lane & 1);
@@ -289,19 +508,15 @@ __global__ void __launch_bounds__(32 * kInterWarps) k_inter(const PicDesc *__res
             const h264r_weight w = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
             int v[2][8];
             bool use[2] = {pp.ref[0] >= 0, pp.ref[1] >= 0};
-            uint8_t *win = s.win[lane];
+            uint32_t *win = s.win[lane];
 #pragma unroll
             for (int l = 0; l < 2; l++) {
                 if (!use[l]) continue;
                 const RefView rv = ref_view(p, pp.ref[l]);
                 const int mvx = pp.mv[l][0], mvy = pp.mv[l][1];
                 const int xi = x + bx * 4 + (mvx >> 2), yi = yAL0 + by * 4 + r0 + (mvy >> 2);
-                for (int rr = 0; rr < 7; rr++) {
-                    const uint8_t *row = rv.y + (size_t)H264R_CLIP3(0, ymax, yi + rr - 2) * rv.ystride;
-#pragma unroll
-                    for (int cc = 0; cc < 9; cc++) win[rr * 9 + cc] = __ldg(row + H264R_CLIP3(0, rv.xmax, xi + cc - 2));
-                }
-                mc_luma_2x4(win, mvx & 3, mvy & 3, v[l]);
+                load_luma_window(rv, ymax, xi, yi, win);  // the lane's own window: no warp barrier
+                mc_luma_2x4((const uint8_t *)win, mvx & 3, mvy & 3, v[l]);
             }
 #pragma unroll
             for (int i = 0; i < 2; i++)
@@ -332,11 +547,7 @@ __global__ void __launch_bounds__(32 * kInterWarps) k_inter(const PicDesc *__res
                 }
                 const uint8_t *plane = pl ? rv.cr : rv.cb;
                 const int xi = x / 2 + bx * 2 + (mvx >> 3), yi = yAL0 / 2 + by * 2 + (mvy >> 3);
-#pragma unroll
-                for (int i = 0; i < 2; i++)
-#pragma unroll
-                    for (int j = 0; j < 2; j++)
-                        v[l][i * 2 + j] = chroma_sample(plane, rv.cstride, rv.xmaxc, ymaxc, xi + j, yi + i, mvx & 7, mvy & 7);
+                chroma_2x2(plane, rv.cstride, rv.xmaxc, ymaxc, xi, yi, mvx & 7, mvy & 7, v[l]);
             }
 #pragma unroll
             for (int i = 0; i < 2; i++)
@@ -363,7 +574,6 @@ __global__ void __launch_bounds__(32 * kInterWarps) k_inter(const PicDesc *__res
 // ======================================================================
 struct IntraSmem {
     int32_t res[384];     // residual: luma raster 16x16, Cb 8x8, Cr 8x8
-    int32_t dc[16];       // Intra16x16 DC
     int nb[40];           // neighbouring samples (-1: not available)
     int nbf[40];          // filtered (8x8) neighbours
 };
@@ -503,6 +713,20 @@ __device__ int pred8x8_sample(int mode, const int *nb, int x, int y)
 
 __device__ __forceinline__ int ldcg_u8(const uint8_t *ptr) { return (int)__ldcg(ptr); }
 
+// The MB's residual, computed by k_inter, into res (int32 per sample).
+__device__ __forceinline__ void load_intra_residual(const PicDesc &p, int addr, int32_t *res)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t *src = (const uint32_t *)(p.ires + (size_t)addr * 384);
+#pragma unroll
+    for (int t = 0; t < 6; t++) {
+        const int i = lane + 32 * t;
+        const uint32_t w = __ldcg(src + i);
+        res[2 * i] = (int16_t)(w & 0xFFFFu);
+        res[2 * i + 1] = (int16_t)(w >> 16);
+    }
+}
+
 // Reconstruct one intra MB with one warp (lane = threadIdx.x & 31).
 __device__ void intra_mb(const PicDesc &p, int addr, IntraSmem &s, const LaunchState &st)
 {
@@ -511,71 +735,9 @@ __device__ void intra_mb(const PicDesc &p, int addr, IntraSmem &s, const LaunchS
     int x, y, dy;
     mb_origin(p, addr, x, y, dy);
     const int field = field_mb(p, addr);
-    const int qp = m.qpy;
     uint8_t *Y = plane_y(p);
-    // ---- residuals
-    for (int i = lane; i < 384; i += 32) s.res[i] = 0;
-    CoefView cv;
-    if (!coef_view(p, m, cv)) {
-        if (lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
-        cv.mask = 0;
-    }
-    __syncwarp();
-    if (m.type == H264R_MB_I16x16) {
-        if (lane == 0) {
-            int32_t c[16];
-            coef_list16(cv, 16, field, c);
-            luma_dc(p, c, field, qp, s.dc);
-        }
-        __syncwarp();
-    }
-    if (m.type == H264R_MB_I8x8) {
-        if (lane < 4 && (cv.mask & (1u << lane))) {
-            int32_t c[64];
-            for (int i = 0; i < 64; i++) c[i] = 0;
-            int w, l;
-            coef_block(cv, lane, w, l);
-            const uint8_t *scan = field ? kField8x8 : kZigzag8x8;
-            for (int q = 0; q < 4; q++) {
-                uint32_t sg = cv.sig[w + q];
-                while (sg && l < cv.max_levels) {
-                    int k = __ffs(sg) - 1;
-                    sg &= sg - 1;
-                    c[scan[16 * q + k]] = cv.lv[l++];
-                }
-            }
-            idct8x8(p, c, field, qp, 0, c);
-            int bx = (lane & 1) * 8, by = (lane >> 1) * 8;
-            for (int i = 0; i < 8; i++)
-                for (int j = 0; j < 8; j++) s.res[(by + i) * 16 + bx + j] = c[i * 8 + j];
-        }
-    } else if (lane < 16) {
-        bool i16 = m.type == H264R_MB_I16x16;
-        if ((cv.mask & (1u << lane)) || (i16 && s.dc[kBlkY[lane] * 4 + kBlkX[lane]] != 0)) {
-            int32_t c[16], r[16];
-            coef_list16(cv, lane, field, c);
-            if (i16) c[0] = s.dc[kBlkY[lane] * 4 + kBlkX[lane]];
-            idct4x4(p, c, field, qp, 0, i16, r);
-            int bx = kBlkX[lane] * 4, by = kBlkY[lane] * 4;
-            for (int i = 0; i < 4; i++)
-                for (int j = 0; j < 4; j++) s.res[(by + i) * 16 + bx + j] = r[i * 4 + j];
-        }
-    }
-    if (lane >= 16 && lane < 24 && cv.mask != 0) {
-        const int pl = (lane - 16) >> 2, b = (lane - 16) & 3;
-        const int qpc = chroma_qp(qp, p.slices[min((uint32_t)m.slice, p.num_slices - 1)].chroma_qp_offset[pl]);
-        int32_t dcl[16], dc4[4], dcC[4];
-        coef_list16(cv, 17 + pl, 0, dcl);
-        dc4[0] = dcl[0]; dc4[1] = dcl[1]; dc4[2] = dcl[4]; dc4[3] = dcl[8];
-        chroma_dc(p, dc4, field, qpc, 0, dcC);
-        int32_t c[16], r[16];
-        coef_list16(cv, (pl ? H264R_CM_CR_AC0 : H264R_CM_CB_AC0) + b, field, c);
-        c[0] = dcC[b];
-        idct4x4(p, c, field, qpc, 0, true, r);
-        int bx = (b & 1) * 4, by = (b >> 1) * 4;
-        for (int i = 0; i < 4; i++)
-            for (int j = 0; j < 4; j++) s.res[256 + pl * 64 + (by + i) * 8 + bx + j] = r[i * 4 + j];
-    }
+    // ---- residual (computed by k_inter)
+    load_intra_residual(p, addr, s.res);
     __syncwarp();
     // ---- luma prediction + reconstruction
     if (m.type == H264R_MB_I4x4) {
@@ -784,7 +946,6 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     const int W = p.W, Wc = p.Wc, wmb = p.wmb;
     const int mx = addr % wmb, my = addr / wmb;
     const int x = mx * 16, y = my * 16;
-    const int qp = m.qpy;
     uint8_t *Y = plane_y(p);
     // ---- neighbour MBs (6.4.9 / getMbAddrN_non_MBAFF_frames) and CIP
     auto usable = [&](int n) -> bool {
@@ -797,6 +958,8 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     const bool B = my > 0 && usable(addr - wmb);
     const bool Cc = my > 0 && mx + 1 < wmb && usable(addr - wmb + 1);
     const bool D = mx > 0 && my > 0 && usable(addr - wmb - 1);
+    // ---- residual (computed by k_inter)
+    load_intra_residual(p, addr, s.res);
     // ---- stage the neighbourhood (luma: corner, 16 left, 24 top; chroma: corner, 8 left, 8 top)
     for (int i = lane; i < 41 + 34; i += 32) {
         if (i < 41) {
@@ -817,68 +980,6 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
             else if (q < 9) { if (A) v = __ldcg(C + (size_t)(yc + q - 1) * Wc + xc - 1); t.c[pl][q][0] = v; }
             else { if (B) v = __ldcg(C + (size_t)(yc - 1) * Wc + xc + q - 9); t.c[pl][0][q - 8] = v; }
         }
-    }
-    // ---- residuals (same as intra_mb)
-    for (int i = lane; i < 384; i += 32) s.res[i] = 0;
-    CoefView cv;
-    if (!coef_view(p, m, cv)) {
-        if (lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
-        cv.mask = 0;
-    }
-    __syncwarp();
-    if (m.type == H264R_MB_I16x16) {
-        if (lane == 0) {
-            int32_t c[16];
-            coef_list16(cv, 16, 0, c);
-            luma_dc(p, c, 0, qp, s.dc);
-        }
-        __syncwarp();
-    }
-    if (m.type == H264R_MB_I8x8) {
-        if (lane < 4 && (cv.mask & (1u << lane))) {
-            int32_t c[64];
-            for (int i = 0; i < 64; i++) c[i] = 0;
-            int w, l;
-            coef_block(cv, lane, w, l);
-            for (int q = 0; q < 4; q++) {
-                uint32_t sg = cv.sig[w + q];
-                while (sg && l < cv.max_levels) {
-                    int kk = __ffs(sg) - 1;
-                    sg &= sg - 1;
-                    c[kZigzag8x8[16 * q + kk]] = cv.lv[l++];
-                }
-            }
-            idct8x8(p, c, 0, qp, 0, c);
-            int bx = (lane & 1) * 8, by = (lane >> 1) * 8;
-            for (int i = 0; i < 8; i++)
-                for (int j = 0; j < 8; j++) s.res[(by + i) * 16 + bx + j] = c[i * 8 + j];
-        }
-    } else if (lane < 16) {
-        bool i16 = m.type == H264R_MB_I16x16;
-        if ((cv.mask & (1u << lane)) || (i16 && s.dc[kBlkY[lane] * 4 + kBlkX[lane]] != 0)) {
-            int32_t c[16], r[16];
-            coef_list16(cv, lane, 0, c);
-            if (i16) c[0] = s.dc[kBlkY[lane] * 4 + kBlkX[lane]];
-            idct4x4(p, c, 0, qp, 0, i16, r);
-            int bx = kBlkX[lane] * 4, by = kBlkY[lane] * 4;
-            for (int i = 0; i < 4; i++)
-                for (int j = 0; j < 4; j++) s.res[(by + i) * 16 + bx + j] = r[i * 4 + j];
-        }
-    }
-    if (lane >= 16 && lane < 24 && cv.mask != 0) {
-        const int pl = (lane - 16) >> 2, b = (lane - 16) & 3;
-        const int qpc = chroma_qp(qp, p.slices[min((uint32_t)m.slice, p.num_slices - 1)].chroma_qp_offset[pl]);
-        int32_t dcl[16], dc4[4], dcC[4];
-        coef_list16(cv, 17 + pl, 0, dcl);
-        dc4[0] = dcl[0]; dc4[1] = dcl[1]; dc4[2] = dcl[4]; dc4[3] = dcl[8];
-        chroma_dc(p, dc4, 0, qpc, 0, dcC);
-        int32_t c[16], r[16];
-        coef_list16(cv, (pl ? H264R_CM_CR_AC0 : H264R_CM_CB_AC0) + b, 0, c);
-        c[0] = dcC[b];
-        idct4x4(p, c, 0, qpc, 0, true, r);
-        int bx = (b & 1) * 4, by = (b >> 1) * 4;
-        for (int i = 0; i < 4; i++)
-            for (int j = 0; j < 4; j++) s.res[256 + pl * 64 + (by + i) * 8 + bx + j] = r[i * 4 + j];
     }
     __syncwarp();
     // ---- luma
