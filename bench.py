@@ -377,21 +377,29 @@ def run_engine(args, world, rank, local, dist):
                    "sample": "%d pictures of stream 0 (%s, seed %d) in decoding order" % (n, WORKLOAD, SEED_BASE)}
         # ---- end to end: host records, pinned staging + H2D, every frame back to pinned host memory
         pinned = [[torch.empty(FRAME_BYTES, dtype=torch.uint8, pin_memory=True).numpy() for _ in range(3)] for _ in range(S)]
-        e2e_steps = 2
+        e2e_steps = 3
         h2d = int(sum(p.record_bytes for ps in streams_pics for p in ps))
-        torch.cuda.synchronize()
-        ctx.sync()
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
+        sidx = {id(st): i for i, st in enumerate(streams)}
+
+        def e2e_step():
             for j, ss, _, pp in batches:
-                ctx.submit_batch(ss, pp)
+                rc = ctx.submit_batch(ss, pp)
+                if rc != 0:
+                    raise RuntimeError("submit_batch: %d %s" % (rc, ctx.last_error()))
                 seen = {}
                 for st, p in zip(ss, pp):
                     k = seen.get(id(st), 0)
                     seen[id(st)] = k + 1
-                    st.output_async(p.dst_slot, pinned[streams.index(st)][k % 3])
+                    st.output_async(p.dst_slot, pinned[sidx[id(st)]][k % 3])
             for st in streams:
                 st.sync()
+
+        e2e_step()  # untimed: sizes the pinned staging of the launch ring
+        torch.cuda.synchronize()
+        ctx.sync()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
         ctx.sync()
         e2e_dt = time.perf_counter() - t0
         e2e = {"value": round(frames_per_step * e2e_steps / e2e_dt, 2), "unit": "frames/s",

@@ -7,11 +7,15 @@
 
 #include <array>
 #include <atomic>
+#include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
+#include <memory>
 #include <mutex>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "h264r_device.cuh"
@@ -60,8 +64,77 @@ struct LaunchBuf {
 
 }  // namespace
 
+// Host worker threads of a context: validation and packing of the records
+// of a host-submitted batch run on them and on the calling thread, so that
+// the host prepares the next batch at the pace the GPU consumes them.
+class WorkerPool {
+public:
+    explicit WorkerPool(int n)
+    {
+        for (int i = 0; i < n; i++) th_.emplace_back([this] { loop(); });
+    }
+    ~WorkerPool()
+    {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+    // fn(0) .. fn(n-1), on the workers and the calling thread; returns when all are done
+    void run(int n, const std::function<void(int)> &fn)
+    {
+        if (n <= 1 || th_.empty()) {
+            for (int i = 0; i < n; i++) fn(i);
+            return;
+        }
+        std::unique_lock<std::mutex> lk(mu_);
+        fn_ = &fn;
+        n_ = n;
+        next_ = 0;
+        pending_ = n;
+        cv_.notify_all();
+        while (pending_ > 0) {
+            if (next_ < n_) {
+                const int i = next_++;
+                lk.unlock();
+                fn(i);
+                lk.lock();
+                --pending_;
+            } else {
+                done_.wait(lk);
+            }
+        }
+        fn_ = nullptr;
+    }
+
+private:
+    void loop()
+    {
+        std::unique_lock<std::mutex> lk(mu_);
+        for (;;) {
+            cv_.wait(lk, [this] { return stop_ || (fn_ && next_ < n_); });
+            if (stop_) return;
+            const int i = next_++;
+            const std::function<void(int)> *f = fn_;
+            lk.unlock();
+            (*f)(i);
+            lk.lock();
+            if (--pending_ == 0) done_.notify_all();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int)> *fn_ = nullptr;
+    int n_ = 0, next_ = 0, pending_ = 0;
+    bool stop_ = false;
+};
+
 struct h264r_ctx {
     int device = 0;
+    std::unique_ptr<WorkerPool> pool;
     uint64_t budget = 0, used = 0;
     uint32_t max_batch = 64;
     int *d_error = nullptr;
@@ -145,6 +218,12 @@ extern "C" int h264r_ctx_create(const h264r_cfg *cfg, h264r_ctx **out)
     }
     for (auto &b : ctx->batch_ring) cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming);
     *ctx->h_error = 0;
+    const unsigned hw = std::thread::hardware_concurrency();
+    ctx->pool.reset(new (std::nothrow) WorkerPool(hw > 2 ? (int)std::min(hw - 1u, 15u) : 0));
+    if (!ctx->pool) {
+        h264r_ctx_destroy(ctx);
+        return H264R_ERR_NO_MEMORY;
+    }
     *out = ctx;
     return H264R_OK;
 }
@@ -760,23 +839,15 @@ extern "C" int h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *st
         set_err(ctx, "h264r_submit_batch: %d pictures exceed the batch limit %u", n, ctx->max_batch);
         return H264R_ERR_BUSY;
     }
-    for (int i = 0; i < n; i++) {
-        if (!streams[i] || streams[i]->ctx != ctx) return H264R_ERR_INVALID_ARG;
-        int rc = h264r_validate_picture(&pics[i], streams[i]->cfg.dpb_slots);
-        if (rc == H264R_OK && (pics[i].width_mbs != streams[i]->cfg.width_mbs || pics[i].height_mbs != streams[i]->cfg.height_mbs))
-            rc = H264R_ERR_INVALID_ARG;
-        if (rc) {
-            set_err(ctx, "h264r_submit_batch: picture %d rejected (%d)", i, rc);
-            return rc;
-        }
-    }
+    for (int i = 0; i < n; i++)
+        if (!streams[i] || streams[i]->ctx != ctx || !pics[i].mbs) return H264R_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);
     std::lock_guard<std::mutex> lk(ctx->mu);
     LaunchBuf &b = ctx->batch_ring[ctx->batch_next];
     ctx->batch_next = (ctx->batch_next + 1) % kRing;
     int rc = wait_slot(ctx, b);
     if (rc) return rc;
-    // pack every picture's records, then one host -> device copy
+    // layout of the packed records of every picture, then one host -> device copy
     std::vector<std::array<uint64_t, 7>> offs(n);
     uint64_t tot = 0;
     for (int i = 0; i < n; i++) {
@@ -793,11 +864,17 @@ extern "C" int h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *st
     if (rc) return rc;
     rc = ensure(ctx, &b.rec_dev, &b.rec_dev_cap, tot, false);
     if (rc) return rc;
+    // validate and pack the pictures on the host workers
     std::vector<h264r_picture> dp(pics, pics + n);
     std::vector<BatchItem> items(n);
-    bool any_intra = false;
-    for (int i = 0; i < n; i++) {
+    std::vector<int> prc(n, H264R_OK);
+    ctx->pool->run(n, [&](int i) {
         const h264r_picture *pic = &pics[i];
+        int r = h264r_validate_picture(pic, streams[i]->cfg.dpb_slots);
+        if (r == H264R_OK && (pic->width_mbs != streams[i]->cfg.width_mbs || pic->height_mbs != streams[i]->cfg.height_mbs))
+            r = H264R_ERR_INVALID_ARG;
+        prc[i] = r;
+        if (r) return;
         const void *src[6] = {pic->mbs, pic->slices, pic->weights, pic->motion, pic->coef, pic->pcm};
         uint64_t sz[6] = {sizeof(h264r_mb) * pic->num_mbs, sizeof(h264r_slice) * pic->num_slices,
                           sizeof(h264r_weight) * pic->num_weights, pic->motion_bytes, pic->coef_bytes, 384ull * pic->num_pcm};
@@ -815,6 +892,13 @@ extern "C" int h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *st
         items[i].pic = &dp[i];
         items[i].scaling_dev = b.rec_dev + offs[i][6];
         items[i].has_intra = has_intra_mbs(pic);
+    });
+    bool any_intra = false;
+    for (int i = 0; i < n; i++) {
+        if (prc[i]) {
+            set_err(ctx, "h264r_submit_batch: picture %d rejected (%d)", i, prc[i]);
+            return prc[i];
+        }
         any_intra = any_intra || items[i].has_intra;
     }
     cudaStream_t cs = streams[0]->cs;

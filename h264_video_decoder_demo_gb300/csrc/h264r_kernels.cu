@@ -41,6 +41,11 @@ __device__ __forceinline__ int find_pic_by_row(const PicDesc *pics, int npics, u
 
 __device__ __forceinline__ void set_error(const LaunchState &st, int code) { atomicCAS(st.error, 0, code); }
 
+__device__ __forceinline__ uint32_t pack4(int a, int b, int c, int d)
+{
+    return (uint32_t)(a & 255) | ((uint32_t)(b & 255) << 8) | ((uint32_t)(c & 255) << 16) | ((uint32_t)(d & 255) << 24);
+}
+
 __device__ __forceinline__ int ld_acquire(const int *p)
 {
     int v;
@@ -294,7 +299,7 @@ __device__ bool mb_residual(const PicDesc &p, const h264r_mb &m, int field, int 
 // 4x4 block l>>1 (raster order within the MB) from a 7x9 window of the
 // reference staged in shared memory, and the 2x2 chroma samples of block
 // l&15 for plane l>>4; residuals come from lanes owning whole blocks.
-constexpr int kInterWarps = 4;
+constexpr int kInterWarps = 4;  // 6 blocks (24 warps) per SM: registers capped at 80
 
 struct InterWarpSmem {
     uint32_t win[32][21];  // per-lane luma reference window, 7 rows x 12 bytes
@@ -390,7 +395,7 @@ __device__ __forceinline__ void mc_luma_2x4(const uint8_t *win, int xf, int yf, 
     if (yf == 0) {
 #pragma unroll
         for (int i = 0; i < 2; i++)
-#pragma unroll
+#pragma unroll 1
             for (int j = 0; j < 4; j++) {
                 int b = clip1((TAP6(WV(i, j - 2), WV(i, j - 1), WV(i, j), WV(i, j + 1), WV(i, j + 2), WV(i, j + 3)) + 16) >> 5);
                 out[i * 4 + j] = xf == 2 ? b : ((xf == 1 ? WV(i, j) : WV(i, j + 1)) + b + 1) >> 1;
@@ -400,7 +405,7 @@ __device__ __forceinline__ void mc_luma_2x4(const uint8_t *win, int xf, int yf, 
     if (xf == 0) {
 #pragma unroll
         for (int i = 0; i < 2; i++)
-#pragma unroll
+#pragma unroll 1
             for (int j = 0; j < 4; j++) {
                 int h = clip1((TAP6(WV(i - 2, j), WV(i - 1, j), WV(i, j), WV(i + 1, j), WV(i + 2, j), WV(i + 3, j)) + 16) >> 5);
                 out[i * 4 + j] = yf == 2 ? h : ((yf == 1 ? WV(i, j) : WV(i + 1, j)) + h + 1) >> 1;
@@ -408,22 +413,22 @@ __device__ __forceinline__ void mc_luma_2x4(const uint8_t *win, int xf, int yf, 
         return;
     }
     if (xf == 2 || yf == 2) {
-        int hb1[7][4];  // horizontal 6-tap sums at rows -2..4
+        // column by column: the horizontal 6-tap sums of rows -2..4 of one
+        // column give j at rows 0 and 1 of that column
+#pragma unroll 1
+        for (int j = 0; j < 4; j++) {
+            int hb1[7];
 #pragma unroll
-        for (int r = -2; r <= 4; r++)
+            for (int r = -2; r <= 4; r++)
+                hb1[r + 2] = TAP6(WV(r, j - 2), WV(r, j - 1), WV(r, j), WV(r, j + 1), WV(r, j + 2), WV(r, j + 3));
 #pragma unroll
-            for (int j = 0; j < 4; j++)
-                hb1[r + 2][j] = TAP6(WV(r, j - 2), WV(r, j - 1), WV(r, j), WV(r, j + 1), WV(r, j + 2), WV(r, j + 3));
-#pragma unroll
-        for (int i = 0; i < 2; i++)
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                int jv = clip1((TAP6(hb1[i][j], hb1[i + 1][j], hb1[i + 2][j], hb1[i + 3][j], hb1[i + 4][j], hb1[i + 5][j]) + 512) >> 10);
+            for (int i = 0; i < 2; i++) {
+                int jv = clip1((TAP6(hb1[i], hb1[i + 1], hb1[i + 2], hb1[i + 3], hb1[i + 4], hb1[i + 5]) + 512) >> 10);
                 int o;
                 if (xf == 2 && yf == 2) {
                     o = jv;
                 } else if (xf == 2) {  // f (row i) / q (row i+1)
-                    int b = clip1((hb1[i + 2 + (yf == 3 ? 1 : 0)][j] + 16) >> 5);
+                    int b = clip1(((yf == 3 ? hb1[i + 3] : hb1[i + 2]) + 16) >> 5);
                     o = (b + jv + 1) >> 1;
                 } else {  // i (col j) / k (col j+1)
                     int c = j + (xf == 3 ? 1 : 0);
@@ -432,12 +437,13 @@ __device__ __forceinline__ void mc_luma_2x4(const uint8_t *win, int xf, int yf, 
                 }
                 out[i * 4 + j] = o;
             }
+        }
         return;
     }
     // e, g, p, r
 #pragma unroll
     for (int i = 0; i < 2; i++)
-#pragma unroll
+#pragma unroll 1
         for (int j = 0; j < 4; j++) {
             int r = i + (yf == 3 ? 1 : 0), c = j + (xf == 3 ? 1 : 0);
             int b = clip1((TAP6(WV(r, j - 2), WV(r, j - 1), WV(r, j), WV(r, j + 1), WV(r, j + 2), WV(r, j + 3)) + 16) >> 5);
@@ -447,7 +453,7 @@ __device__ __forceinline__ void mc_luma_2x4(const uint8_t *win, int xf, int yf, 
 #undef WV
 }
 
-__global__ void __launch_bounds__(32 * kInterWarps) k_inter(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st)
+__global__ void __launch_bounds__(32 * kInterWarps, 6) k_inter(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st)
 {
     __shared__ InterWarpSmem smem[kInterWarps];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -458,23 +464,27 @@ __global__ void __launch_bounds__(32 * kInterWarps) k_inter(const PicDesc *__res
     const int addr = (int)(g - p.mb_base);
     const h264r_mb m = p.mbs[addr];
     const int field = field_mb(p, addr);
-    if (is_intra_type(m.type)) {
+    const bool intra = is_intra_type(m.type);
+    if (intra && !p.ires) return;
+    // ---- residual (8.5) into s.res: one call site for intra and inter MBs
+    // (the code of this kernel is kept compact: instruction fetch, not
+    // arithmetic or memory, is what its warps wait on)
+    if (intra || m.type == H264R_MB_INTER) {
+        if (!mb_residual(p, m, field, intra ? 0 : 3, intra ? 0 : 1, s.res, s.dcs) && lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
+    }
+    if (intra) {
         // intra MB: only its residual, for the intra wavefront (k_intra).
         // Stored clamped to [-255, 255]: Clip1(pred + r) is the same for
         // every r beyond that range.
-        if (p.ires) {
-            if (!mb_residual(p, m, field, 0, 0, s.res, s.dcs) && lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
-            uint32_t *dst = (uint32_t *)(p.ires + (size_t)addr * 384);
+        uint32_t *dst = (uint32_t *)(p.ires + (size_t)addr * 384);
 #pragma unroll
-            for (int t = 0; t < 6; t++) {
-                const int i = lane + 32 * t;
-                const int a = H264R_CLIP3(-255, 255, s.res[2 * i]), b = H264R_CLIP3(-255, 255, s.res[2 * i + 1]);
-                dst[i] = ((uint32_t)a & 0xFFFFu) | ((uint32_t)b << 16);
-            }
+        for (int t = 0; t < 6; t++) {
+            const int i = lane + 32 * t;
+            const int a = H264R_CLIP3(-255, 255, s.res[2 * i]), b = H264R_CLIP3(-255, 255, s.res[2 * i + 1]);
+            dst[i] = ((uint32_t)a & 0xFFFFu) | ((uint32_t)b << 16);
         }
         return;
     }
-    if (m.type != H264R_MB_INTER && m.type != H264R_MB_IPCM && m.type != H264R_MB_NONE) return;
     int x, y, dy;
     mb_origin(p, addr, x, y, dy);
 
@@ -497,8 +507,6 @@ __global__ void __launch_bounds__(32 * kInterWarps) k_inter(const PicDesc *__res
         const int yAL0 = field ? (y - (y & 1)) / 2 : y;
         const int ymax = field ? p.H / 2 - 1 : p.H - 1;
         const int ymaxc = field ? p.Hc / 2 - 1 : p.Hc - 1;
-        // ---- residual (8.5) into s.res
-        if (!mb_residual(p, m, field, 3, 1, s.res, s.dcs) && lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
         // ---- luma prediction: 4x4 block lane>>1 (raster), rows 2*(lane&1), +1
         {
             const int blk = lane >> 1, bx = blk & 3, by = blk >> 2, r0 = 2 * (lane & 1);
@@ -506,25 +514,29 @@ __global__ void __launch_bounds__(32 * kInterWarps) k_inter(const PicDesc *__res
             if (e >= (int)count) e = 0;
             const h264r_part pp = parts[e];
             const h264r_weight w = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
-            int v[2][8];
-            bool use[2] = {pp.ref[0] >= 0, pp.ref[1] >= 0};
+            const bool use0 = pp.ref[0] >= 0, use1 = pp.ref[1] >= 0;
+            uint32_t va0 = 0, va1 = 0, vb0 = 0, vb1 = 0;  // predictions of list 0 / 1, 8 bytes each
             uint32_t *win = s.win[lane];
-#pragma unroll
+#pragma unroll 1
             for (int l = 0; l < 2; l++) {
-                if (!use[l]) continue;
-                const RefView rv = ref_view(p, pp.ref[l]);
-                const int mvx = pp.mv[l][0], mvy = pp.mv[l][1];
+                if (!(l ? use1 : use0)) continue;
+                const int ref = l ? pp.ref[1] : pp.ref[0];
+                const int mvx = l ? pp.mv[1][0] : pp.mv[0][0], mvy = l ? pp.mv[1][1] : pp.mv[0][1];
+                const RefView rv = ref_view(p, ref);
                 const int xi = x + bx * 4 + (mvx >> 2), yi = yAL0 + by * 4 + r0 + (mvy >> 2);
                 load_luma_window(rv, ymax, xi, yi, win);  // the lane's own window: no warp barrier
-                mc_luma_2x4((const uint8_t *)win, mvx & 3, mvy & 3, v[l]);
+                int o[8];
+                mc_luma_2x4((const uint8_t *)win, mvx & 3, mvy & 3, o);
+                const uint32_t w0 = pack4(o[0], o[1], o[2], o[3]), w1 = pack4(o[4], o[5], o[6], o[7]);
+                if (l) { vb0 = w0; vb1 = w1; } else { va0 = w0; va1 = w1; }
             }
-#pragma unroll
-            for (int i = 0; i < 2; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const int oy = by * 4 + r0 + i, ox = bx * 4 + j;
-                    s.out[oy * 16 + ox] = (uint8_t)clip1(weigh(w, 0, use[0], use[1], v[0][i * 4 + j], v[1][i * 4 + j]) + s.res[oy * 16 + ox]);
-                }
+#pragma unroll 1
+            for (int t = 0; t < 8; t++) {
+                const int i = t >> 2, j = t & 3;
+                const int oy = by * 4 + r0 + i, ox = bx * 4 + j;
+                const int a = ((i ? va1 : va0) >> (8 * j)) & 255, b = ((i ? vb1 : vb0) >> (8 * j)) & 255;
+                s.out[oy * 16 + ox] = (uint8_t)clip1(weigh(w, 0, use0, use1, a, b) + s.res[oy * 16 + ox]);
+            }
         }
         // ---- chroma prediction: plane lane>>4, 2x2 samples of 4x4 block lane&15 (raster)
         {
@@ -533,29 +545,33 @@ __global__ void __launch_bounds__(32 * kInterWarps) k_inter(const PicDesc *__res
             if (e >= (int)count) e = 0;
             const h264r_part pp = parts[e];
             const h264r_weight w = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
-            bool use[2] = {pp.ref[0] >= 0, pp.ref[1] >= 0};
-            int v[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
-#pragma unroll
+            const bool use0 = pp.ref[0] >= 0, use1 = pp.ref[1] >= 0;
+            uint32_t ca = 0, cb = 0;  // 2x2 predictions of list 0 / 1
+#pragma unroll 1
             for (int l = 0; l < 2; l++) {
-                if (!use[l]) continue;
-                const RefView rv = ref_view(p, pp.ref[l]);
-                int mvx = pp.mv[l][0], mvy = pp.mv[l][1];
+                if (!(l ? use1 : use0)) continue;
+                const int ref = l ? pp.ref[1] : pp.ref[0];
+                const RefView rv = ref_view(p, ref);
+                int mvx = l ? pp.mv[1][0] : pp.mv[0][0], mvy = l ? pp.mv[1][1] : pp.mv[0][1];
                 if (field) {  // Table 8-10 (H264InterPrediction.cpp:2006-2047)
-                    int refbot = (pp.ref[l] & H264R_REF_BOTTOM) ? 1 : 0;
+                    int refbot = (ref & H264R_REF_BOTTOM) ? 1 : 0;
                     if (!refbot && bottom_mb) mvy += 2;
                     else if (refbot && !bottom_mb) mvy -= 2;
                 }
                 const uint8_t *plane = pl ? rv.cr : rv.cb;
                 const int xi = x / 2 + bx * 2 + (mvx >> 3), yi = yAL0 / 2 + by * 2 + (mvy >> 3);
-                chroma_2x2(plane, rv.cstride, rv.xmaxc, ymaxc, xi, yi, mvx & 7, mvy & 7, v[l]);
+                int o[4];
+                chroma_2x2(plane, rv.cstride, rv.xmaxc, ymaxc, xi, yi, mvx & 7, mvy & 7, o);
+                const uint32_t wv = pack4(o[0], o[1], o[2], o[3]);
+                if (l) cb = wv; else ca = wv;
             }
-#pragma unroll
-            for (int i = 0; i < 2; i++)
-#pragma unroll
-                for (int j = 0; j < 2; j++) {
-                    const int oy = by * 2 + i, ox = bx * 2 + j, o = 256 + pl * 64 + oy * 8 + ox;
-                    s.out[o] = (uint8_t)clip1(weigh(w, 1 + pl, use[0], use[1], v[0][i * 2 + j], v[1][i * 2 + j]) + s.res[o - 0]);
-                }
+#pragma unroll 1
+            for (int t = 0; t < 4; t++) {
+                const int i = t >> 1, j = t & 1;
+                const int oy = by * 2 + i, ox = bx * 2 + j, o = 256 + pl * 64 + oy * 8 + ox;
+                const int a = (ca >> (8 * t)) & 255, b = (cb >> (8 * t)) & 255;
+                s.out[o] = (uint8_t)clip1(weigh(w, 1 + pl, use0, use1, a, b) + s.res[o]);
+            }
         }
     }
     __syncwarp();
@@ -1707,10 +1723,6 @@ __device__ __forceinline__ void db_chroma(int (&v)[N], int bS, uint32_t prm)
     v[Q] = clip1(q0 - delta);
 }
 
-__device__ __forceinline__ uint32_t pack4(int a, int b, int c, int d)
-{
-    return (uint32_t)(a & 255) | ((uint32_t)(b & 255) << 8) | ((uint32_t)(c & 255) << 16) | ((uint32_t)(d & 255) << 24);
-}
 
 __device__ void deblock_pair_frame(const PicDesc &p, int pair, DbPairSmem &s, const LaunchState &st)
 {
