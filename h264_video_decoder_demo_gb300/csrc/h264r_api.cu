@@ -24,7 +24,7 @@ namespace h264r {
 __global__ void k_inter(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
 __global__ void k_intra(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st);
 __global__ void k_bs(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
-__global__ void k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st);
+__global__ void k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st);
 }  // namespace h264r
 
 using h264r::PicDesc;
@@ -536,7 +536,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
     }
     memset(b.host, 0, total);
     PicDesc *d = (PicDesc *)b.host;
-    uint64_t mb_base = 0, row_base = 0, prog = 0;
+    uint64_t mb_base = 0, row_base = 0, prog = 0, db_base = 0;
     for (int i = 0; i < n; i++) {
         const h264r_picture *pic = items[i].pic;
         h264r_stream *s = items[i].s;
@@ -574,6 +574,9 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
         p.progress = (int *)(b.dev + prog_off) + prog;
         p.mb_base = (uint32_t)mb_base;
         p.row_base = (uint32_t)row_base;
+        p.db_units = h264r::deblock_units(p.mbaff, p.units_h);
+        p.db_base = (uint32_t)db_base;
+        db_base += p.db_units;
         p.deblock_stop = 0xFFFFFFFFu;
         mb_base += pic->num_mbs;
         row_base += p.units_h;
@@ -600,7 +603,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
     if (ctx->timing) cudaEventRecord(ev[2], cs);
     if (any_deblock) {
         h264r::k_bs<<<(unsigned)((mbs + 3) / 4), 128, 0, cs>>>(dd, n, (uint32_t)mbs, st);
-        h264r::k_deblock<<<(unsigned)rows, 32, 0, cs>>>(dd, n, (uint32_t)rows, st);
+        h264r::k_deblock<<<(unsigned)db_base, 32, 0, cs>>>(dd, n, (uint32_t)db_base, st);
         ctx->launches += 2;
     }
     if (ctx->timing) cudaEventRecord(ev[3], cs);

@@ -84,8 +84,14 @@ struct PicDesc {
     uint32_t mb_base;        // first global MB index of this picture in the batch
     uint32_t row_base;       // first global unit row of this picture in the batch
     uint32_t units_w, units_h;  // wavefront grid: MBs (or MB pairs) per row, rows
+    uint32_t db_base, db_units; // first deblocking ticket of this picture in the batch, ticket count
     uint32_t deblock_stop;   // first failing bS derivation key (0xFFFFFFFF: none)
 };
+
+// Deblocking tickets of a picture: frame pictures give one ticket to the
+// luma and one to the chroma warp of every pair of MB rows; MBAFF pictures
+// one per MB-pair row.
+__host__ __device__ inline uint32_t deblock_units(int mbaff, uint32_t units_h) { return mbaff ? units_h : 2u * ((units_h + 1u) / 2u); }
 
 // Engine-wide device state for one launch.
 struct LaunchState {

@@ -39,6 +39,17 @@ __device__ __forceinline__ int find_pic_by_row(const PicDesc *pics, int npics, u
     return lo;
 }
 
+__device__ __forceinline__ int find_pic_by_db(const PicDesc *pics, int npics, uint32_t g)
+{
+    int lo = 0, hi = npics - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pics[mid].db_base <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 __device__ __forceinline__ void set_error(const LaunchState &st, int code) { atomicCAS(st.error, 0, code); }
 
 __device__ __forceinline__ uint32_t pack4(int a, int b, int c, int d)
@@ -1598,71 +1609,28 @@ __device__ void deblock_mb(const PicDesc &p, int cur)
 }
 
 // ---------------------------------------------------------------- frame fast path
-// Non-MBAFF pictures: one warp filters a pair of MB rows, the second row
-// trailing the first by two MBs (in the reference's raster order a MB's top
-// edge comes after the left edge of the MB above-right).  Lanes 0..15 work
-// on the first row of the pair, 16..31 on the second; in each half a lane
-// owns one luma line and one chroma line (Cb for lanes 0..7 of the half, Cr
-// for 8..15).  A line is filtered in registers across all edges of one
-// direction, and the MB passes through shared memory once, between its
-// vertical and horizontal edges.  The vertical edges of a MB touch only its
-// own MB row, so they run before the wait for the row above.  The second
-// row takes the first row's bottom lines from a small ring in shared memory
-// instead of a global round trip.  Strengths and thresholds come from k_bs.
-constexpr int kDbLumaHalf = 368;    // ints per half: rows -4..15 x stride 17 (+ bank offset 16)
-constexpr int kDbChromaGroup = 169; // ints per (half, plane): rows -4..7 x stride 12 (+ bank offset 9)
-
-struct DbPairSmem {
-    int l[2][kDbLumaHalf];
-    int c[4][kDbChromaGroup];
-    uint4 ring_l[3][4];      // first row: luma rows 12..15 of the MB in column % 3
-    uint2 ring_c[3][2][4];   // first row: chroma rows 4..7, per plane
+// Non-MBAFF pictures.  Luma and chroma are filtered by separate warps (the
+// planes never interact), each warp taking a pair of MB rows: lanes 0..15
+// work on the first row, 16..31 on the second, which trails the first by
+// two MBs (in the reference's raster order a MB's top edge comes after the
+// left edge of the MB above-right).  A luma lane owns one line of the MB;
+// a chroma lane one line of Cb (lanes 0..7 of the half) or Cr (8..15).  A
+// line is filtered in registers across all edges of one direction, and the
+// MB passes through a byte tile in shared memory once, between its vertical
+// and horizontal edges.  The vertical edges of a MB touch only its own MB
+// row, so they run before the wait for the row above.  The second row takes
+// the first row's bottom lines from a ring in shared memory.  Strengths and
+// thresholds come from k_bs.  Progress of a pair's second row is published
+// per plane: luma at the odd row index, chroma at the even one.
+struct DbLumaSmem {
+    __align__(16) uint8_t t[2][20][16];  // per half: rows -4..15 of the MB
+    uint4 ring[3][4];                    // first row: rows 12..15 of the MB in column % 3
 };
 
-// what one lane needs of one MB, none of it written by the wavefront
-struct DbLine {
-    uint4 luma;              // the lane's luma line of the MB
-    uint2 chroma;            // the lane's chroma line
-    uint32_t lv, lh;         // luma strengths of the line, byte e = edge e
-    uint32_t cv, ch;         // chroma strengths, bytes 0, 1
-    uint4 pl, pc;            // thresholds (left, top, internal): luma, the lane's chroma plane
+struct DbChromaSmem {
+    __align__(16) uint8_t t[2][2][12][8];  // per half and plane: rows -4..7 of the MB
+    uint2 ring[3][2][4];                   // first row: rows 4..7, per plane
 };
-
-__device__ __forceinline__ void db_fetch(const PicDesc &p, int row, int u, int k, int comp, int ck, DbLine &f)
-{
-    const int cur = row * (int)p.units_w + u;
-    const uint8_t *bs = p.bs + (size_t)cur * kBsBytes;
-    f.luma = __ldcg((const uint4 *)(plane_y(p) + (size_t)(row * 16 + k) * p.W + u * 16));
-    f.chroma = __ldcg((const uint2 *)(plane_c(p, comp) + (size_t)(row * 8 + ck) * p.Wc + u * 8));
-    f.lv = __ldcg((const uint32_t *)(bs + bs_lv(0, k)));
-    f.lh = __ldcg((const uint32_t *)(bs + bs_lh(0, k)));
-    f.cv = __ldcg((const uint16_t *)(bs + bs_cv(0, ck)));
-    f.ch = __ldcg((const uint16_t *)(bs + bs_ch(0, ck)));
-    f.pl = __ldcg((const uint4 *)(bs + kBsParams));
-    f.pc = __ldcg((const uint4 *)(bs + kBsParams + 16 + 16 * comp));
-}
-
-// Clear the strengths of the steps at or after the point where the
-// reference's bS derivation fails (only pictures with undecoded MBs).
-__device__ __forceinline__ void db_mask_stop(int cur, uint32_t stop, int k, int comp, int ck, DbLine &f)
-{
-    const uint32_t stop_mb = stop >> 10;
-    if ((uint32_t)cur < stop_mb) return;
-    if ((uint32_t)cur > stop_mb) {
-        f.lv = f.lh = f.cv = f.ch = 0;
-        return;
-    }
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-        if (stop_key(cur, SEQ_LV0 + e, k) >= stop) f.lv &= ~(0xFFu << (8 * e));
-        if (stop_key(cur, e == 0 ? SEQ_LH0 : SEQ_LH4 + e - 1, k) >= stop) f.lh &= ~(0xFFu << (8 * e));
-    }
-#pragma unroll
-    for (int e = 0; e < 2; e++) {
-        if (stop_key(cur, (e == 0 ? SEQ_CBV0 : SEQ_CBV4) + comp, ck) >= stop) f.cv &= ~(0xFFu << (8 * e));
-        if (stop_key(cur, (e == 0 ? SEQ_CBH0 : SEQ_CBH4) + comp, ck) >= stop) f.ch &= ~(0xFFu << (8 * e));
-    }
-}
 
 __device__ __forceinline__ int db_tc0(uint32_t prm, int bS) { return (prm >> (11 + 5 * bS)) & 31; }
 
@@ -1723,154 +1691,235 @@ __device__ __forceinline__ void db_chroma(int (&v)[N], int bS, uint32_t prm)
     v[Q] = clip1(q0 - delta);
 }
 
+// Lane 0 polls the row above only when the last value it saw is behind.
+__device__ __forceinline__ bool db_wait(const LaunchState &st, const int *flag, int target, int &seen)
+{
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0 && seen < target) {
+        unsigned long long n = 0;
+        while ((seen = ld_acquire(flag)) < target) {
+            if (++n > st.spin_limit) {
+                set_error(st, H264R_ERR_DEVICE_TIMEOUT);
+                ok = 0;
+                break;
+            }
+            if (n > 64) {
+                if (*(volatile int *)st.error != 0) { ok = 0; break; }
+                __nanosleep(32);
+            }
+        }
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __syncwarp();
+    return ok != 0;
+}
 
-__device__ void deblock_pair_frame(const PicDesc &p, int pair, DbPairSmem &s, const LaunchState &st)
+__device__ void deblock_pair_luma(const PicDesc &p, int pair, DbLumaSmem &s, const LaunchState &st)
 {
     const int lane = threadIdx.x & 31;
-    const int h = lane >> 4, k = lane & 15, comp = k >> 3, ck = k & 7;
-    const int uw = (int)p.units_w, rows = (int)p.units_h, W = p.W, Wc = p.Wc;
+    const int h = lane >> 4, k = lane & 15;
+    const int uw = (int)p.units_w, rows = (int)p.units_h, W = p.W;
     const int row = 2 * pair + h;
     const bool row_ok = row < rows;
     const bool has_second = 2 * pair + 1 < rows;
     const int steps = has_second ? uw + 2 : uw;
     int *prog = p.progress + p.units_h;
     uint8_t *Y = plane_y(p);
-    uint8_t *C = plane_c(p, comp);
-    int *tl = s.l[h];
-    int *tc = s.c[2 * h + comp];
-    int left[4] = {0, 0, 0, 0}, cleft[4] = {0, 0, 0, 0};
-    DbLine nxt;
-    if (row_ok && h == 0) db_fetch(p, row, 0, k, comp, ck, nxt);
+    uint8_t(*t)[16] = s.t[h];
+    const uint32_t stop = p.deblock_stop;
+    int left[4] = {0, 0, 0, 0};
+    int seen = 0;
+    // prefetched per MB: the lane's line, its strengths (byte e: edge e), the thresholds
+    uint4 nl = make_uint4(0, 0, 0, 0), npl = nl;
+    uint32_t nlv = 0, nlh = 0;
+    auto fetch = [&](int u) {
+        const int cur = row * uw + u;
+        const uint8_t *bs = p.bs + (size_t)cur * kBsBytes;
+        nl = __ldcg((const uint4 *)(Y + (size_t)(row * 16 + k) * W + u * 16));
+        nlv = __ldcg((const uint32_t *)(bs + bs_lv(0, k)));
+        nlh = __ldcg((const uint32_t *)(bs + bs_lh(0, k)));
+        npl = __ldcg((const uint4 *)(bs + kBsParams));
+    };
+    if (row_ok && h == 0) fetch(0);
     for (int step = 0; step < steps; step++) {
-        const int u = step - 2 * h;                 // this half's MB column
+        const int u = step - 2 * h;
         const bool act = row_ok && u >= 0 && u < uw;
-        DbLine f = nxt;
-        if (row_ok && u + 1 >= 0 && u + 1 < uw) db_fetch(p, row, u + 1, k, comp, ck, nxt);
+        const uint4 line = nl, prm = npl;
+        uint32_t lv = nlv, lh = nlh;
+        if (row_ok && u + 1 >= 0 && u + 1 < uw) fetch(u + 1);
         const int x0 = u * 16, y0 = row * 16;
         if (act) {
-            db_mask_stop(row * uw + u, p.deblock_stop, k, comp, ck, f);
-            // ---- vertical edges, in registers
-            int v[20];
-            int w[12];
+            const int cur = row * uw + u;
+            if ((uint32_t)cur >= (stop >> 10)) {  // the reference's bS derivation fails at or before this MB
+                if ((uint32_t)cur > (stop >> 10)) lv = lh = 0;
+                else {
 #pragma unroll
-            for (int i = 0; i < 4; i++) { v[i] = left[i]; w[i] = cleft[i]; }
-            unpack16(f.luma, &v[4]);
-            unpack8(f.chroma, &w[4]);
-            db_luma<4, true>(v, f.lv & 255, f.pl.x);
-            db_luma<8, false>(v, (f.lv >> 8) & 255, f.pl.z);
-            db_luma<12, false>(v, (f.lv >> 16) & 255, f.pl.z);
-            db_luma<16, false>(v, f.lv >> 24, f.pl.z);
-            db_chroma<4, true>(w, f.cv & 255, f.pc.x);
-            db_chroma<8, false>(w, (f.cv >> 8) & 255, f.pc.z);
+                    for (int e = 0; e < 4; e++) {
+                        if (stop_key(cur, SEQ_LV0 + e, k) >= stop) lv &= ~(0xFFu << (8 * e));
+                        if (stop_key(cur, e == 0 ? SEQ_LH0 : SEQ_LH4 + e - 1, k) >= stop) lh &= ~(0xFFu << (8 * e));
+                    }
+                }
+            }
+            int v[20];
+#pragma unroll
+            for (int i = 0; i < 4; i++) v[i] = left[i];
+            unpack16(line, &v[4]);
+            db_luma<4, true>(v, lv & 255, prm.x);
+            db_luma<8, false>(v, (lv >> 8) & 255, prm.z);
+            db_luma<12, false>(v, (lv >> 16) & 255, prm.z);
+            db_luma<16, false>(v, lv >> 24, prm.z);
             if (u > 0) {
                 // the left MB's last columns are final now
                 const uint32_t lw = pack4(v[0], v[1], v[2], v[3]);
-                const uint32_t cw = pack4(w[0], w[1], w[2], w[3]);
                 *(uint32_t *)(Y + (size_t)(y0 + k) * W + x0 - 4) = lw;
-                *(uint32_t *)(C + (size_t)(y0 / 2 + ck) * Wc + x0 / 2 - 4) = cw;
-                if (h == 0) {
-                    const int slot = (u - 1) % 3;
-                    if (k >= 12) s.ring_l[slot][k - 12].w = lw;
-                    if (ck >= 4) s.ring_c[slot][comp][ck - 4].y = cw;
-                }
+                if (h == 0 && k >= 12) s.ring[(u - 1) % 3][k - 12].w = lw;
             }
-#pragma unroll
-            for (int j = 0; j < 16; j++) tl[(k + 4) * 17 + j] = v[4 + j];
-#pragma unroll
-            for (int j = 0; j < 8; j++) tc[(ck + 4) * 12 + j] = w[4 + j];
+            *(uint4 *)&t[k + 4][0] = pack16(&v[4]);
         }
         // ---- the row above: final once its warp is two MBs ahead
-        const int u0 = step;  // first row's MB column
-        if (2 * pair > 0 && u0 < uw && !wait_progress(st, prog + 2 * pair - 1, min(u0 + 2, uw))) return;
-        if (act && row > 0) {
-            if (h == 0) {
-                if (k < 4) {
-                    const uint4 a = __ldcg((const uint4 *)(Y + (size_t)(y0 - 4 + k) * W + x0));
-                    unpack16(a, &tl[k * 17]);
-                } else if (k < 12) {
-                    const int pl = (k - 4) >> 2, r = (k - 4) & 3;
-                    const uint2 a = __ldcg((const uint2 *)(plane_c(p, pl) + (size_t)(y0 / 2 - 4 + r) * Wc + x0 / 2));
-                    unpack8(a, &s.c[pl][r * 12]);
-                }
-            } else {
-                const int slot = u % 3;
-                if (k < 4) unpack16(s.ring_l[slot][k], &tl[k * 17]);
-                else if (k < 12) {
-                    const int pl = (k - 4) >> 2, r = (k - 4) & 3;
-                    unpack8(s.ring_c[slot][pl][r], &s.c[2 + pl][r * 12]);
-                }
-            }
-        }
+        if (2 * pair > 0 && step < uw && !db_wait(st, prog + 2 * pair - 1, min(step + 2, uw), seen)) return;
+        if (act && row > 0 && k < 4)
+            *(uint4 *)&t[k][0] = h == 0 ? __ldcg((const uint4 *)(Y + (size_t)(y0 - 4 + k) * W + x0)) : s.ring[u % 3][k];
         __syncwarp();
-        // ---- horizontal edges, in registers (the lane owns a column)
+        // ---- horizontal edges: the lane owns a column
         if (act) {
             int v[20];
-            int w[12];
 #pragma unroll
-            for (int i = 0; i < 20; i++) v[i] = tl[i * 17 + k];
+            for (int i = 0; i < 20; i++) v[i] = t[i][k];
+            db_luma<4, true>(v, lh & 255, prm.y);
+            db_luma<8, false>(v, (lh >> 8) & 255, prm.z);
+            db_luma<12, false>(v, (lh >> 16) & 255, prm.z);
+            db_luma<16, false>(v, lh >> 24, prm.z);
 #pragma unroll
-            for (int i = 0; i < 12; i++) w[i] = tc[i * 12 + ck];
-            db_luma<4, true>(v, f.lh & 255, f.pl.y);
-            db_luma<8, false>(v, (f.lh >> 8) & 255, f.pl.z);
-            db_luma<12, false>(v, (f.lh >> 16) & 255, f.pl.z);
-            db_luma<16, false>(v, f.lh >> 24, f.pl.z);
-            db_chroma<4, true>(w, f.ch & 255, f.pc.y);
-            db_chroma<8, false>(w, (f.ch >> 8) & 255, f.pc.z);
-#pragma unroll
-            for (int i = 1; i < 19; i++) tl[i * 17 + k] = v[i];
-            tc[3 * 12 + ck] = w[3];
-            tc[4 * 12 + ck] = w[4];
-            tc[7 * 12 + ck] = w[7];
-            tc[8 * 12 + ck] = w[8];
+            for (int i = 1; i < 19; i++) t[i][k] = (uint8_t)v[i];
         }
         __syncwarp();
         // ---- store the MB and the three rows above it
         if (act) {
-            const uint4 lr = pack16(&tl[(k + 4) * 17]);
-            const uint2 cr = pack8(&tc[(ck + 4) * 12]);
+            const uint4 lr = *(const uint4 *)&t[k + 4][0];
             *(uint4 *)(Y + (size_t)(y0 + k) * W + x0) = lr;
-            *(uint2 *)(C + (size_t)(y0 / 2 + ck) * Wc + x0 / 2) = cr;
 #pragma unroll
-            for (int i = 0; i < 4; i++) {
-                left[i] = tl[(k + 4) * 17 + 12 + i];
-                cleft[i] = tc[(ck + 4) * 12 + 4 + i];
-            }
-            if (h == 0) {
-                if (k >= 12) s.ring_l[u % 3][k - 12] = lr;
-                if (ck >= 4) s.ring_c[u % 3][comp][ck - 4] = cr;
-            }
-            if (row > 0) {
-                if (k < 3) *(uint4 *)(Y + (size_t)(y0 - 3 + k) * W + x0) = pack16(&tl[(1 + k) * 17]);
-                else if (k < 9) {
-                    const int pl = (k - 3) / 3, r = (k - 3) % 3;
-                    *(uint2 *)(plane_c(p, pl) + (size_t)(y0 / 2 - 3 + r) * Wc + x0 / 2) = pack8(&s.c[2 * h + pl][(1 + r) * 12]);
-                }
-            }
+            for (int i = 0; i < 4; i++) left[i] = (lr.w >> (8 * i)) & 255;
+            if (h == 0 && k >= 12) s.ring[u % 3][k - 12] = lr;
+            if (row > 0 && k < 3) *(uint4 *)(Y + (size_t)(y0 - 3 + k) * W + x0) = *(const uint4 *)&t[1 + k][0];
         }
         __syncwarp();
-        // the second row publishes its progress (the next pair waits on it)
         if (lane == 0 && has_second && step >= 2) st_release(prog + 2 * pair + 1, step - 1);
     }
 }
 
-__global__ void __launch_bounds__(32) k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st)
+__device__ void deblock_pair_chroma(const PicDesc &p, int pair, DbChromaSmem &s, const LaunchState &st)
+{
+    const int lane = threadIdx.x & 31;
+    const int h = lane >> 4, k = lane & 15, comp = k >> 3, ck = k & 7;
+    const int uw = (int)p.units_w, rows = (int)p.units_h, Wc = p.Wc;
+    const int row = 2 * pair + h;
+    const bool row_ok = row < rows;
+    const bool has_second = 2 * pair + 1 < rows;
+    const int steps = has_second ? uw + 2 : uw;
+    int *prog = p.progress + p.units_h;
+    uint8_t *C = plane_c(p, comp);
+    uint8_t(*t)[8] = s.t[h][comp];
+    const uint32_t stop = p.deblock_stop;
+    int left[4] = {0, 0, 0, 0};
+    int seen = 0;
+    uint2 nl = make_uint2(0, 0);
+    uint4 npc = make_uint4(0, 0, 0, 0);
+    uint32_t ncv = 0, nch = 0;
+    auto fetch = [&](int u) {
+        const int cur = row * uw + u;
+        const uint8_t *bs = p.bs + (size_t)cur * kBsBytes;
+        nl = __ldcg((const uint2 *)(C + (size_t)(row * 8 + ck) * Wc + u * 8));
+        ncv = __ldcg((const uint16_t *)(bs + bs_cv(0, ck)));
+        nch = __ldcg((const uint16_t *)(bs + bs_ch(0, ck)));
+        npc = __ldcg((const uint4 *)(bs + kBsParams + 16 + 16 * comp));
+    };
+    if (row_ok && h == 0) fetch(0);
+    for (int step = 0; step < steps; step++) {
+        const int u = step - 2 * h;
+        const bool act = row_ok && u >= 0 && u < uw;
+        const uint2 line = nl;
+        const uint4 prm = npc;
+        uint32_t cv = ncv, ch = nch;
+        if (row_ok && u + 1 >= 0 && u + 1 < uw) fetch(u + 1);
+        const int x0 = u * 8, y0 = row * 8;
+        if (act) {
+            const int cur = row * uw + u;
+            if ((uint32_t)cur >= (stop >> 10)) {
+                if ((uint32_t)cur > (stop >> 10)) cv = ch = 0;
+                else {
+#pragma unroll
+                    for (int e = 0; e < 2; e++) {
+                        if (stop_key(cur, (e == 0 ? SEQ_CBV0 : SEQ_CBV4) + comp, ck) >= stop) cv &= ~(0xFFu << (8 * e));
+                        if (stop_key(cur, (e == 0 ? SEQ_CBH0 : SEQ_CBH4) + comp, ck) >= stop) ch &= ~(0xFFu << (8 * e));
+                    }
+                }
+            }
+            int w[12];
+#pragma unroll
+            for (int i = 0; i < 4; i++) w[i] = left[i];
+            unpack8(line, &w[4]);
+            db_chroma<4, true>(w, cv & 255, prm.x);
+            db_chroma<8, false>(w, (cv >> 8) & 255, prm.z);
+            if (u > 0) {
+                const uint32_t cw = pack4(w[0], w[1], w[2], w[3]);
+                *(uint32_t *)(C + (size_t)(y0 + ck) * Wc + x0 - 4) = cw;
+                if (h == 0 && ck >= 4) s.ring[(u - 1) % 3][comp][ck - 4].y = cw;
+            }
+            *(uint2 *)&t[ck + 4][0] = pack8(&w[4]);
+        }
+        if (2 * pair > 0 && step < uw && !db_wait(st, prog + 2 * pair - 2, min(step + 2, uw), seen)) return;
+        if (act && row > 0 && ck < 4)
+            *(uint2 *)&t[ck][0] = h == 0 ? __ldcg((const uint2 *)(C + (size_t)(y0 - 4 + ck) * Wc + x0)) : s.ring[u % 3][comp][ck];
+        __syncwarp();
+        if (act) {
+            int w[12];
+#pragma unroll
+            for (int i = 0; i < 12; i++) w[i] = t[i][ck];
+            db_chroma<4, true>(w, ch & 255, prm.y);
+            db_chroma<8, false>(w, (ch >> 8) & 255, prm.z);
+            t[3][ck] = (uint8_t)w[3];
+            t[4][ck] = (uint8_t)w[4];
+            t[7][ck] = (uint8_t)w[7];
+            t[8][ck] = (uint8_t)w[8];
+        }
+        __syncwarp();
+        if (act) {
+            const uint2 cr = *(const uint2 *)&t[ck + 4][0];
+            *(uint2 *)(C + (size_t)(y0 + ck) * Wc + x0) = cr;
+#pragma unroll
+            for (int i = 0; i < 4; i++) left[i] = (cr.y >> (8 * i)) & 255;
+            if (h == 0 && ck >= 4) s.ring[u % 3][comp][ck - 4] = cr;
+            if (row > 0 && ck < 3) *(uint2 *)(C + (size_t)(y0 - 3 + ck) * Wc + x0) = *(const uint2 *)&t[1 + ck][0];
+        }
+        __syncwarp();
+        if (lane == 0 && has_second && step >= 2) st_release(prog + 2 * pair, step - 1);
+    }
+}
+
+__global__ void __launch_bounds__(32) k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st)
 {
     __shared__ uint32_t s_row;
     const int lane = threadIdx.x;
     if (lane == 0) s_row = atomicAdd(&st.ticket[1], 1u);
     __syncwarp();
     const uint32_t g = s_row;
-    if (g >= total_rows) return;
-    const int pi = find_pic_by_row(pics, npics, g);
+    if (g >= total_units) return;
+    const int pi = find_pic_by_db(pics, npics, g);
     const PicDesc p = pics[pi];
     if (!p.deblock) return;
-    const int row = (int)(g - p.row_base);
+    const int unit = (int)(g - p.db_base);
     if (!p.mbaff) {
-        // rows are handled in pairs by the warp of the even row
-        __shared__ DbPairSmem pair_smem;
-        if ((row & 1) == 0) deblock_pair_frame(p, row >> 1, pair_smem, st);
+        // even tickets: luma of MB-row pair unit/2; odd: its chroma
+        __shared__ union {
+            DbLumaSmem l;
+            DbChromaSmem c;
+        } pair_smem;
+        if ((unit & 1) == 0) deblock_pair_luma(p, unit >> 1, pair_smem.l, st);
+        else deblock_pair_chroma(p, unit >> 1, pair_smem.c, st);
         return;
     }
+    const int row = unit;
     const int uw = (int)p.units_w;
     const int per = p.mbaff ? 2 : 1;
     int *prog = p.progress + p.units_h;

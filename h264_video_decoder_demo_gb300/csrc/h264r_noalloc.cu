@@ -20,7 +20,7 @@
 
 namespace h264r {
 __global__ void k_bs(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
-__global__ void k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st);
+__global__ void k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st);
 }  // namespace h264r
 
 using h264r::PicDesc;
@@ -116,6 +116,8 @@ extern "C" int h264r_deblock_picture_noalloc(const h264r_picture *pic, uint8_t *
     d.progress = s->progress;
     d.units_w = pic->width_mbs;
     d.units_h = rows;
+    d.db_base = 0;
+    d.db_units = h264r::deblock_units(d.mbaff, rows);
     d.deblock_stop = 0xFFFFFFFFu;
 
     cudaStream_t cs = (cudaStream_t)cuda_stream;
@@ -125,7 +127,7 @@ extern "C" int h264r_deblock_picture_noalloc(const h264r_picture *pic, uint8_t *
     st.spin_limit = kNoAllocSpinLimit;
     k_noalloc_init<<<1, 256, 0, cs>>>(d, s);
     h264r::k_bs<<<(pic->num_mbs + 3) / 4, 128, 0, cs>>>(&s->desc, 1, pic->num_mbs, st);
-    h264r::k_deblock<<<rows, 32, 0, cs>>>(&s->desc, 1, rows, st);
+    h264r::k_deblock<<<d.db_units, 32, 0, cs>>>(&s->desc, 1, d.db_units, st);
     if (cudaGetLastError() != cudaSuccess) return H264R_ERR_CUDA;
     int herr = 0;
     if (cudaMemcpyAsync(&herr, &s->error, sizeof(int), cudaMemcpyDeviceToHost, cs) != cudaSuccess) return H264R_ERR_CUDA;
