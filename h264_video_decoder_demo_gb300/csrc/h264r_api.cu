@@ -260,6 +260,12 @@ extern "C" const char *h264r_last_error(const h264r_ctx *ctx) { return ctx ? ctx
 
 extern "C" uint64_t h264r_ctx_kernel_launches(const h264r_ctx *ctx) { return ctx ? ctx->launches.load() : 0; }
 
+extern "C" int h264r_ctx_device(const h264r_ctx *ctx) { return ctx ? ctx->device : H264R_ERR_INVALID_ARG; }
+
+extern "C" uint64_t h264r_ctx_dpb_budget(const h264r_ctx *ctx) { return ctx ? ctx->budget : 0; }
+
+extern "C" int h264r_ctx_max_batch(const h264r_ctx *ctx) { return ctx ? (int)ctx->max_batch : H264R_ERR_INVALID_ARG; }
+
 static int drain_timing(h264r_ctx *ctx)
 {
     std::lock_guard<std::mutex> lk(ctx->timing_mu);

@@ -1,0 +1,546 @@
+// h264r_server.cu — continuous-batching server (include/h264r_server.h).
+//
+// Host code only.  One scheduler thread per server owns every call into the
+// engine; the API calls (open / push / end / poll) only touch the server's
+// queues under its mutex, so a parser thread per stream can feed it.
+//
+// A picture moves through three queues of its stream:
+//   host_q  records validated and packed in host memory (push)
+//   dev_q   records uploaded into one of the stream's device slots
+//           (pinned staging + an H2D copy on the server's upload stream)
+//   flight  launched in a batch; done when the event recorded after its
+//           launch (and its output copy) completes
+// Each pass of the scheduler admits waiting streams whose DPB fits the
+// budget, retires finished pictures, uploads queued records, and launches
+// one batch with the next dependency group of every stream that has one
+// uploaded: continuous batching, with at most three batches in flight.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "../../include/h264r_server.h"
+
+namespace {
+
+constexpr uint64_t kAlign = 256;
+constexpr int kMaxBatchesInFlight = 3;
+constexpr int kMaxGroupsInFlight = 2;  // per stream
+
+uint64_t align_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
+
+double now_ms()
+{
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Slot {
+    uint8_t *host = nullptr;  // pinned staging
+    uint8_t *dev = nullptr;   // device records
+    uint64_t cap = 0;
+    bool busy = false;
+};
+
+struct Item {
+    std::vector<uint8_t> blob;  // packed records: mbs | slices | weights | motion | coef | pcm
+    uint64_t off[6] = {0, 0, 0, 0, 0, 0};
+    h264r_picture pic{};        // sizes, flags and scaling lists (pointers set on upload)
+    int group = 0;
+    uint64_t tag = 0;
+    uint8_t *out = nullptr;
+    double t_push = 0;
+    int slot = -1;
+    cudaEvent_t uploaded = nullptr, done = nullptr;
+};
+
+struct SStream {
+    int id = 0;
+    h264r_stream_cfg cfg{};
+    uint64_t dpb = 0;
+    h264r_stream *s = nullptr;
+    bool admitted = false, ended = false, finished = false;
+    int status = 0;
+    int pending = 0;  // pushed, not yet polled
+    std::deque<Item *> host_q, dev_q, flight;
+    std::vector<Slot> slots;
+    int groups_in_flight() const
+    {
+        int n = 0, last = -1;
+        bool first = true;
+        for (const Item *it : flight) {
+            if (first || it->group != last) n++;
+            last = it->group;
+            first = false;
+        }
+        return n;
+    }
+};
+
+}  // namespace
+
+struct h264r_server {
+    h264r_ctx *ctx = nullptr;
+    int device = 0;
+    uint64_t budget = 0;
+    int max_batch = 64, depth = 4;
+    std::mutex mu;
+    std::condition_variable wake, done_cv;
+    std::map<int, SStream *> streams;
+    std::deque<SStream *> waiting;
+    std::deque<h264r_server_done> done_q;
+    std::vector<double> lat;
+    h264r_server_stats st{};
+    std::deque<cudaEvent_t> batch_done;
+    std::vector<cudaEvent_t> ev_pool;
+    cudaStream_t up = nullptr;
+    std::thread th;
+    bool stop = false;
+    int next_id = 0;
+    size_t rr = 0;
+};
+
+namespace {
+
+cudaEvent_t take_event(h264r_server *srv)
+{
+    if (!srv->ev_pool.empty()) {
+        cudaEvent_t e = srv->ev_pool.back();
+        srv->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    return e;
+}
+
+void give_event(h264r_server *srv, cudaEvent_t &e)
+{
+    if (e) srv->ev_pool.push_back(e);
+    e = nullptr;
+}
+
+void report(h264r_server *srv, SStream *S, Item *it, int status)
+{
+    h264r_server_done d;
+    d.stream = S->id;
+    d.status = status;
+    d.tag = it->tag;
+    d.latency_ms = now_ms() - it->t_push;
+    srv->done_q.push_back(d);
+    if (status == 0) srv->lat.push_back(d.latency_ms);
+    srv->st.pictures_done++;
+    if (it->slot >= 0) S->slots[it->slot].busy = false;
+    give_event(srv, it->uploaded);
+    give_event(srv, it->done);
+    delete it;
+    srv->done_cv.notify_all();
+}
+
+// A stream that hit an error: every picture it still holds is reported with
+// the error, and it closes like a finished stream.
+void fail_stream(h264r_server *srv, SStream *S, int status)
+{
+    if (S->s) h264r_stream_sync(S->s);
+    S->status = status;
+    for (auto *q : {&S->flight, &S->dev_q, &S->host_q}) {
+        while (!q->empty()) {
+            report(srv, S, q->front(), status);
+            q->pop_front();
+        }
+    }
+}
+
+void close_stream(h264r_server *srv, SStream *S)
+{
+    if (S->s) {
+        const int rc = h264r_stream_sync(S->s);  // device errors of its last work
+        if (rc && !S->status) S->status = rc;
+        h264r_stream_close(S->s);
+        S->s = nullptr;
+        srv->st.dpb_bytes_in_use -= S->dpb;
+        srv->st.streams_open--;
+    }
+    for (auto &sl : S->slots) {
+        if (sl.host) cudaFreeHost(sl.host);
+        if (sl.dev) cudaFree(sl.dev);
+        sl = Slot();
+    }
+    S->finished = true;
+    srv->st.streams_done++;
+}
+
+bool admit(h264r_server *srv)
+{
+    bool progress = false;
+    while (!srv->waiting.empty()) {
+        SStream *S = srv->waiting.front();
+        int rc = h264r_stream_open(srv->ctx, &S->cfg, &S->s);
+        if (rc == H264R_ERR_BUDGET) break;  // wait for finished streams to free their DPBs
+        srv->waiting.pop_front();
+        srv->st.streams_waiting--;
+        progress = true;
+        if (rc != H264R_OK) {
+            S->s = nullptr;
+            fail_stream(srv, S, rc);
+            close_stream(srv, S);
+            continue;
+        }
+        S->admitted = true;
+        S->slots.resize(srv->depth);
+        srv->st.streams_open++;
+        srv->st.dpb_bytes_in_use += S->dpb;
+        srv->st.dpb_bytes_peak = std::max(srv->st.dpb_bytes_peak, srv->st.dpb_bytes_in_use);
+    }
+    return progress;
+}
+
+bool retire(h264r_server *srv)
+{
+    bool progress = false;
+    while (!srv->batch_done.empty() && cudaEventQuery(srv->batch_done.front()) == cudaSuccess) {
+        give_event(srv, srv->batch_done.front());
+        srv->batch_done.pop_front();
+    }
+    for (auto &kv : srv->streams) {
+        SStream *S = kv.second;
+        if (!S->admitted || S->finished) continue;
+        while (!S->flight.empty() && !S->status) {
+            Item *it = S->flight.front();
+            cudaError_t e = cudaEventQuery(it->done);
+            if (e == cudaErrorNotReady) break;
+            S->flight.pop_front();
+            const int status = e == cudaSuccess ? H264R_OK : H264R_ERR_CUDA;
+            report(srv, S, it, status);
+            progress = true;
+            if (status != H264R_OK) {
+                fail_stream(srv, S, status);
+                break;
+            }
+        }
+        if (S->ended && S->host_q.empty() && S->dev_q.empty() && S->flight.empty()) {
+            close_stream(srv, S);
+            progress = true;
+        }
+    }
+    return progress;
+}
+
+bool upload(h264r_server *srv)
+{
+    bool progress = false;
+    for (auto &kv : srv->streams) {
+        SStream *S = kv.second;
+        if (!S->admitted || S->finished || S->status) continue;
+        while (!S->host_q.empty()) {
+            int k = -1;
+            for (int i = 0; i < (int)S->slots.size(); i++)
+                if (!S->slots[i].busy) { k = i; break; }
+            if (k < 0) break;
+            Item *it = S->host_q.front();
+            Slot &sl = S->slots[k];
+            const uint64_t need = it->blob.size();
+            if (sl.cap < need) {
+                if (sl.host) cudaFreeHost(sl.host);
+                if (sl.dev) cudaFree(sl.dev);
+                sl = Slot();
+                const uint64_t cap = align_up(need + need / 8, 1 << 16);
+                if (cudaMallocHost(&sl.host, cap) != cudaSuccess || cudaMalloc(&sl.dev, cap) != cudaSuccess) {
+                    if (sl.host) cudaFreeHost(sl.host);
+                    sl = Slot();
+                    fail_stream(srv, S, H264R_ERR_NO_MEMORY);
+                    progress = true;
+                    break;
+                }
+                sl.cap = cap;
+            }
+            memcpy(sl.host, it->blob.data(), need);
+            if (cudaMemcpyAsync(sl.dev, sl.host, need, cudaMemcpyHostToDevice, srv->up) != cudaSuccess) {
+                fail_stream(srv, S, H264R_ERR_CUDA);
+                progress = true;
+                break;
+            }
+            it->uploaded = take_event(srv);
+            cudaEventRecord(it->uploaded, srv->up);
+            sl.busy = true;
+            it->slot = k;
+            uint8_t *d = sl.dev;
+            it->pic.mbs = (const h264r_mb *)(d + it->off[0]);
+            it->pic.slices = (const h264r_slice *)(d + it->off[1]);
+            it->pic.weights = (const h264r_weight *)(d + it->off[2]);
+            it->pic.motion = d + it->off[3];
+            it->pic.coef = d + it->off[4];
+            it->pic.pcm = d + it->off[5];
+            std::vector<uint8_t>().swap(it->blob);
+            S->host_q.pop_front();
+            S->dev_q.push_back(it);
+            progress = true;
+        }
+    }
+    return progress;
+}
+
+bool launch(h264r_server *srv)
+{
+    if ((int)srv->batch_done.size() >= kMaxBatchesInFlight) return false;
+    std::vector<SStream *> order;
+    for (auto &kv : srv->streams)
+        if (kv.second->admitted && !kv.second->finished && !kv.second->status && !kv.second->dev_q.empty()) order.push_back(kv.second);
+    if (order.empty()) return false;
+    // round robin over the streams so that a full batch does not always
+    // leave out the same ones
+    std::rotate(order.begin(), order.begin() + (srv->rr++ % order.size()), order.end());
+    std::vector<h264r_stream *> ss;
+    std::vector<h264r_picture> pics;
+    std::vector<std::pair<SStream *, Item *>> items;
+    for (SStream *S : order) {
+        if (S->groups_in_flight() >= kMaxGroupsInFlight) continue;
+        const int g = S->dev_q.front()->group;
+        size_t take = 0;
+        while (take < S->dev_q.size() && S->dev_q[take]->group == g && (int)pics.size() < srv->max_batch) {
+            Item *it = S->dev_q[take];
+            ss.push_back(S->s);
+            pics.push_back(it->pic);
+            items.emplace_back(S, it);
+            take++;
+        }
+        if ((int)pics.size() >= srv->max_batch) break;
+    }
+    if (pics.empty()) return false;
+    // the records must be on the device before the batch reads them
+    for (auto &pr : items)
+        cudaStreamWaitEvent((cudaStream_t)h264r_stream_cuda_stream(pr.first->s), pr.second->uploaded, 0);
+    const int rc = h264r_submit_batch_device(srv->ctx, (int)pics.size(), ss.data(), pics.data());
+    // move the launched pictures from dev_q to flight (same order)
+    for (auto &pr : items) {
+        SStream *S = pr.first;
+        S->dev_q.pop_front();
+        Item *it = pr.second;
+        if (rc != H264R_OK) {
+            S->flight.push_back(it);
+            continue;
+        }
+        cudaStream_t cs = (cudaStream_t)h264r_stream_cuda_stream(S->s);
+        if (it->out) {
+            const uint64_t W = S->cfg.width_mbs * 16ull, H = S->cfg.height_mbs * 16ull;
+            h264r_output(S->s, it->pic.dst_slot, it->out, it->out + W * H, it->out + W * H + W * H / 4);
+        }
+        it->done = take_event(srv);
+        cudaEventRecord(it->done, cs);
+        S->flight.push_back(it);
+    }
+    if (rc != H264R_OK) {
+        for (auto &pr : items)
+            if (!pr.first->flight.empty()) fail_stream(srv, pr.first, rc);
+        return true;
+    }
+    cudaEvent_t be = take_event(srv);
+    cudaEventRecord(be, (cudaStream_t)h264r_stream_cuda_stream(ss[0]));
+    srv->batch_done.push_back(be);
+    srv->st.batches++;
+    srv->st.batch_pictures += pics.size();
+    return true;
+}
+
+void scheduler(h264r_server *srv)
+{
+    cudaSetDevice(srv->device);
+    std::unique_lock<std::mutex> lk(srv->mu);
+    for (;;) {
+        bool progress = admit(srv);
+        progress = retire(srv) || progress;
+        progress = upload(srv) || progress;
+        progress = launch(srv) || progress;
+        if (srv->stop && srv->waiting.empty()) {
+            bool all = true;
+            for (auto &kv : srv->streams) all = all && kv.second->finished;
+            if (all) break;
+        }
+        if (!progress) srv->wake.wait_for(lk, std::chrono::microseconds(50));
+    }
+}
+
+}  // namespace
+
+extern "C" int h264r_server_create(h264r_ctx *ctx, const h264r_server_cfg *cfg, h264r_server **out)
+{
+    if (!ctx || !out) return H264R_ERR_INVALID_ARG;
+    *out = nullptr;
+    h264r_server *srv = new (std::nothrow) h264r_server();
+    if (!srv) return H264R_ERR_NO_MEMORY;
+    srv->ctx = ctx;
+    srv->device = h264r_ctx_device(ctx);
+    srv->budget = h264r_ctx_dpb_budget(ctx);
+    const int ctx_batch = h264r_ctx_max_batch(ctx);
+    srv->max_batch = (cfg && cfg->max_batch_pictures) ? (int)std::min<uint32_t>(cfg->max_batch_pictures, ctx_batch) : ctx_batch;
+    srv->depth = (cfg && cfg->queue_depth) ? (int)std::min<uint32_t>(cfg->queue_depth, 32) : 4;
+    cudaSetDevice(srv->device);
+    if (cudaStreamCreateWithFlags(&srv->up, cudaStreamNonBlocking) != cudaSuccess) {
+        delete srv;
+        return H264R_ERR_CUDA;
+    }
+    srv->th = std::thread(scheduler, srv);
+    *out = srv;
+    return H264R_OK;
+}
+
+extern "C" int h264r_server_destroy(h264r_server *srv)
+{
+    if (!srv) return H264R_ERR_INVALID_ARG;
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        for (auto &kv : srv->streams) kv.second->ended = true;
+        srv->stop = true;
+    }
+    srv->wake.notify_all();
+    srv->th.join();
+    cudaSetDevice(srv->device);
+    for (auto &kv : srv->streams) delete kv.second;
+    for (auto e : srv->batch_done) cudaEventDestroy(e);
+    for (auto e : srv->ev_pool) cudaEventDestroy(e);
+    cudaStreamDestroy(srv->up);
+    delete srv;
+    return H264R_OK;
+}
+
+extern "C" int h264r_server_open(h264r_server *srv, const h264r_stream_cfg *cfg, int *stream_id)
+{
+    if (!srv || !cfg || !stream_id || !cfg->width_mbs || !cfg->height_mbs || !cfg->dpb_slots || cfg->dpb_slots > 32)
+        return H264R_ERR_INVALID_ARG;
+    const uint64_t dpb = h264r_stream_dpb_bytes(cfg);
+    if (dpb > srv->budget) return H264R_ERR_BUDGET;
+    SStream *S = new (std::nothrow) SStream();
+    if (!S) return H264R_ERR_NO_MEMORY;
+    S->cfg = *cfg;
+    S->dpb = dpb;
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        S->id = srv->next_id++;
+        srv->streams[S->id] = S;
+        srv->waiting.push_back(S);
+        srv->st.streams_waiting++;
+        srv->st.waiting_peak = std::max<uint64_t>(srv->st.waiting_peak, srv->st.streams_waiting);
+    }
+    srv->wake.notify_all();
+    *stream_id = S->id;
+    return H264R_OK;
+}
+
+extern "C" int h264r_server_push(h264r_server *srv, int stream_id, const h264r_picture *pic, int dependency_group, uint64_t tag,
+                                 uint8_t *out_planes)
+{
+    if (!srv || !pic) return H264R_ERR_INVALID_ARG;
+    h264r_stream_cfg cfg;
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        auto f = srv->streams.find(stream_id);
+        if (f == srv->streams.end() || f->second->ended) return H264R_ERR_INVALID_ARG;
+        cfg = f->second->cfg;
+    }
+    if (pic->width_mbs != cfg.width_mbs || pic->height_mbs != cfg.height_mbs) return H264R_ERR_INVALID_ARG;
+    int rc = h264r_validate_picture(pic, cfg.dpb_slots);
+    if (rc) return rc;
+    // pack the records as the device will see them (outside the lock)
+    Item *it = new (std::nothrow) Item();
+    if (!it) return H264R_ERR_NO_MEMORY;
+    const void *src[6] = {pic->mbs, pic->slices, pic->weights, pic->motion, pic->coef, pic->pcm};
+    const uint64_t sz[6] = {sizeof(h264r_mb) * pic->num_mbs, sizeof(h264r_slice) * pic->num_slices,
+                            sizeof(h264r_weight) * pic->num_weights, pic->motion_bytes, pic->coef_bytes, 384ull * pic->num_pcm};
+    uint64_t tot = 0;
+    for (int k = 0; k < 6; k++) {
+        it->off[k] = tot;
+        tot = align_up(tot + sz[k], kAlign);
+    }
+    it->blob.resize(tot);
+    for (int k = 0; k < 6; k++)
+        if (sz[k]) memcpy(it->blob.data() + it->off[k], src[k], sz[k]);
+    it->pic = *pic;
+    it->group = dependency_group;
+    it->tag = tag;
+    it->out = out_planes;
+    it->t_push = now_ms();
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        auto f = srv->streams.find(stream_id);
+        if (f == srv->streams.end() || f->second->ended) {
+            delete it;
+            return H264R_ERR_INVALID_ARG;
+        }
+        SStream *S = f->second;
+        S->pending++;
+        if (S->status) {  // the stream failed earlier: report the picture at once
+            const int st = S->status;
+            report(srv, S, it, st);
+            return st;
+        }
+        S->host_q.push_back(it);
+    }
+    srv->wake.notify_all();
+    return H264R_OK;
+}
+
+extern "C" int h264r_server_end(h264r_server *srv, int stream_id)
+{
+    if (!srv) return H264R_ERR_INVALID_ARG;
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        auto f = srv->streams.find(stream_id);
+        if (f == srv->streams.end()) return H264R_ERR_INVALID_ARG;
+        f->second->ended = true;
+    }
+    srv->wake.notify_all();
+    return H264R_OK;
+}
+
+extern "C" int h264r_server_poll(h264r_server *srv, h264r_server_done *done, int max, int wait_ms)
+{
+    if (!srv || !done || max <= 0) return H264R_ERR_INVALID_ARG;
+    std::unique_lock<std::mutex> lk(srv->mu);
+    if (srv->done_q.empty() && wait_ms > 0)
+        srv->done_cv.wait_for(lk, std::chrono::milliseconds(wait_ms), [srv] { return !srv->done_q.empty(); });
+    int n = 0;
+    while (n < max && !srv->done_q.empty()) {
+        done[n] = srv->done_q.front();
+        srv->done_q.pop_front();
+        auto f = srv->streams.find(done[n].stream);
+        if (f != srv->streams.end()) f->second->pending--;
+        n++;
+    }
+    return n;
+}
+
+extern "C" int h264r_server_pending(h264r_server *srv, int stream_id)
+{
+    if (!srv) return H264R_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(srv->mu);
+    auto f = srv->streams.find(stream_id);
+    if (f == srv->streams.end()) return H264R_ERR_INVALID_ARG;
+    return f->second->pending;
+}
+
+extern "C" int h264r_server_get_stats(h264r_server *srv, h264r_server_stats *out)
+{
+    if (!srv || !out) return H264R_ERR_INVALID_ARG;
+    std::vector<double> l;
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        *out = srv->st;
+        l = srv->lat;
+    }
+    out->p50_ms = out->p99_ms = out->max_ms = 0;
+    if (!l.empty()) {
+        std::sort(l.begin(), l.end());
+        out->p50_ms = l[l.size() / 2];
+        out->p99_ms = l[std::min(l.size() - 1, (size_t)(0.99 * l.size()))];
+        out->max_ms = l.back();
+    }
+    return H264R_OK;
+}

@@ -16,7 +16,7 @@ _LIB = None
 _LIB_LOCK = threading.Lock()
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libh264r.so")
 
-# every symbol include/h264r.h and include/h264r_synth.h declare
+# every symbol include/h264r.h, include/h264r_synth.h and include/h264r_server.h declare
 EXPORTS = [
     "h264r_ctx_create", "h264r_ctx_destroy", "h264r_last_error", "h264r_stream_open",
     "h264r_stream_close", "h264r_stream_dpb_bytes", "h264r_submit_picture",
@@ -27,6 +27,9 @@ EXPORTS = [
     "h264r_synth_create", "h264r_synth_dpb_slots", "h264r_synth_next", "h264r_synth_destroy",
     "h264r_submit_batch", "h264r_picture_bytes", "h264r_ctx_cuda_stream",
     "h264r_deblock_picture_noalloc",
+    "h264r_ctx_device", "h264r_ctx_dpb_budget", "h264r_ctx_max_batch",
+    "h264r_server_create", "h264r_server_destroy", "h264r_server_open", "h264r_server_push",
+    "h264r_server_end", "h264r_server_poll", "h264r_server_pending", "h264r_server_get_stats",
 ]
 
 
@@ -82,6 +85,17 @@ def _load():
         "h264r_synth_dpb_slots": (i32, [vp]),
         "h264r_synth_next": (i32, [vp, P(R.CPicture), P(i32)]),
         "h264r_synth_destroy": (i32, [vp]),
+        "h264r_ctx_device": (i32, [vp]),
+        "h264r_ctx_dpb_budget": (u64, [vp]),
+        "h264r_ctx_max_batch": (i32, [vp]),
+        "h264r_server_create": (i32, [vp, P(R.CServerCfg), P(vp)]),
+        "h264r_server_destroy": (i32, [vp]),
+        "h264r_server_open": (i32, [vp, P(R.CStreamCfg), P(i32)]),
+        "h264r_server_push": (i32, [vp, i32, P(R.CPicture), i32, u64, vp]),
+        "h264r_server_end": (i32, [vp, i32]),
+        "h264r_server_poll": (i32, [vp, P(R.CServerDone), i32, i32]),
+        "h264r_server_pending": (i32, [vp, i32]),
+        "h264r_server_get_stats": (i32, [vp, P(R.CServerStats)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -229,6 +243,70 @@ class Stream:
         if self.h:
             lib().h264r_stream_close(self.h)
             self.h = None
+
+
+class Server:
+    """Continuous-batching server on a context (include/h264r_server.h): streams
+    are admitted by the context's DPB budget, pictures pushed as their records
+    are complete, finished pictures polled with their latency."""
+
+    def __init__(self, ctx, max_batch=0, queue_depth=0):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        cfg = R.CServerCfg(max_batch, queue_depth, 0, 0)
+        ctx.check(lib().h264r_server_create(ctx.h, ctypes.byref(cfg), ctypes.byref(h)), "server_create")
+        self.h = h
+        self._keep = {}
+
+    def open(self, width_mbs, height_mbs, dpb_slots):
+        sid = ctypes.c_int()
+        cfg = R.CStreamCfg(width_mbs, height_mbs, dpb_slots, 0)
+        rc = lib().h264r_server_open(self.h, ctypes.byref(cfg), ctypes.byref(sid))
+        if rc != 0:
+            raise EngineError(rc, "server_open")
+        return sid.value
+
+    def push(self, stream, pic, group, tag, out=None):
+        """Queue a Picture; `out` (numpy uint8, W*H*3/2, ideally pinned) receives the planes."""
+        c = pic.to_c()
+        ptr = out.ctypes.data if out is not None else None
+        if out is not None:
+            self._keep[(stream, tag)] = out
+        return lib().h264r_server_push(self.h, stream, ctypes.byref(c), group, tag, ptr)
+
+    def end(self, stream):
+        return lib().h264r_server_end(self.h, stream)
+
+    def poll(self, max_items=256, wait_ms=10):
+        buf = (R.CServerDone * max_items)()
+        n = lib().h264r_server_poll(self.h, buf, max_items, wait_ms)
+        if n < 0:
+            raise EngineError(n, "server_poll")
+        out = []
+        for i in range(n):
+            d = buf[i]
+            self._keep.pop((d.stream, d.tag), None)
+            out.append((d.stream, d.tag, d.status, d.latency_ms))
+        return out
+
+    def pending(self, stream):
+        return lib().h264r_server_pending(self.h, stream)
+
+    def stats(self):
+        st = R.CServerStats()
+        lib().h264r_server_get_stats(self.h, ctypes.byref(st))
+        return {name: getattr(st, name) for name, _ in R.CServerStats._fields_}
+
+    def close(self):
+        if self.h:
+            lib().h264r_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 class Synth:

@@ -145,3 +145,23 @@ class CSynthCfg(ctypes.Structure):
                 ("edge_mv_percent", ctypes.c_uint8), ("mv_range", ctypes.c_int16),
                 ("filter_offset_max", ctypes.c_int8), ("coef_density", ctypes.c_uint8),
                 ("reserved", ctypes.c_uint8 * 2)]
+
+
+class CServerCfg(ctypes.Structure):
+    """struct h264r_server_cfg (include/h264r_server.h)"""
+    _fields_ = [("max_batch_pictures", ctypes.c_uint32), ("queue_depth", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class CServerDone(ctypes.Structure):
+    """struct h264r_server_done"""
+    _fields_ = [("stream", ctypes.c_int32), ("status", ctypes.c_int32), ("tag", ctypes.c_uint64),
+                ("latency_ms", ctypes.c_double)]
+
+
+class CServerStats(ctypes.Structure):
+    """struct h264r_server_stats"""
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "pictures_done", "streams_open", "streams_waiting", "streams_done", "batches", "batch_pictures",
+        "dpb_bytes_in_use", "dpb_bytes_peak", "waiting_peak")] + [
+        ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double)]

@@ -336,6 +336,11 @@ int  h264r_deblock_picture_noalloc(const h264r_picture *pic, uint8_t *planes, vo
  * Returns 0 or H264R_ERR_BAD_RECORD / H264R_ERR_UNSUPPORTED. */
 int  h264r_validate_picture(const h264r_picture *pic, int dpb_slots);
 
+/* The context's CUDA device, DPB memory budget (bytes) and batch limit. */
+int      h264r_ctx_device(const h264r_ctx *ctx);
+uint64_t h264r_ctx_dpb_budget(const h264r_ctx *ctx);
+int      h264r_ctx_max_batch(const h264r_ctx *ctx);
+
 /* Number of engine kernels launched so far by this context. */
 uint64_t h264r_ctx_kernel_launches(const h264r_ctx *ctx);
 
