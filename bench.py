@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--pictures", type=int, default=30)
     ap.add_argument("--pipelines", type=int, default=2, help="concurrent batch pipelines over disjoint stream sets")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (quick runs)")
+    ap.add_argument("--serve-seconds", type=float, default=4.0,
+                    help="length of the Poisson arrival window of the serving run (0: skip it)")
     return ap.parse_args()
 
 
@@ -222,6 +224,126 @@ def run_reference(args, rank):
         "config": {"workload": WORKLOAD, "streams": cores, "pictures_per_stream": args.pictures, "threads": cores},
         "cpu_baseline": {"value": round(fps, 3), "unit": "frames/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": round(fps, 3), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+SERVE_RES = [("cif", 22, 18, 0.3), ("720p", 80, 45, 0.4), ("1080p", 120, 68, 0.3)]
+
+
+def run_serving(args, device, seed=5000):
+    """Serving: Poisson arrivals of streams at 40 streams/s, resolution drawn
+    from {CIF, 720p, 1080p} with p = {0.3, 0.4, 0.3}, length uniform in
+    [8, 120] pictures, coding structure IP or IBBP, DPBs device-resident and
+    admitted by a 40 GB DPB budget.  Each request replays the records of a
+    pre-generated pool stream of its size and structure (its own DPB, the
+    records shared read-only).  Pictures are pushed as each stream's window
+    of 4 allows and every decoded picture is copied to pinned host memory.
+    Returns aggregate frames/s and the per-picture latency."""
+    import random
+
+    import torch
+
+    import h264_video_decoder_demo_gb300 as h
+
+    rng = random.Random(seed)
+    pools = {}
+    jobs = []
+    for res, wmb, hmb, _ in SERVE_RES:
+        for kind in (0, 1):
+            jobs.append((res, wmb, hmb, kind))
+    errors = []
+
+    def gen(job):
+        res, wmb, hmb, kind = job
+        base = "1080p_high" if kind == 1 else "cif_ippp"
+        over = dict(width_mbs=wmb, height_mbs=hmb, num_pictures=120)
+        if kind == 0:
+            over.update(gop_kind=0, num_refs=1)
+        try:
+            g = h.synth(base, seed=seed + len(res) * 10 + kind, **over)
+            pools[(res, kind)] = (list(g), g.dpb_slots)
+            g.close()
+        except Exception as exc:  # surfaced below
+            errors.append(exc)
+
+    threads = [threading.Thread(target=gen, args=(j,)) for j in jobs]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if errors:
+        raise errors[0]
+    # the request schedule
+    reqs, t = [], 0.0
+    while True:
+        t += rng.expovariate(40.0)
+        if t > args.serve_seconds:
+            break
+        u, acc = rng.random(), 0.0
+        for res, wmb, hmb, p in SERVE_RES:
+            acc += p
+            if u <= acc:
+                break
+        reqs.append((t, res, rng.randint(0, 1), rng.randint(8, 120)))
+    window = 4
+    free_bufs = {}
+
+    def take_buf(nbytes):
+        lst = free_bufs.setdefault(nbytes, [])
+        return lst.pop() if lst else torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+
+    for res, wmb, hmb, _ in SERVE_RES:  # pinned output buffers, allocated before the clock starts
+        nbytes = wmb * hmb * 384
+        free_bufs[nbytes] = [torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy() for _ in range(96)]
+    ctx = h.Context(device, dpb_budget_bytes=40 << 30, max_batch=128)
+    srv = h.Server(ctx, queue_depth=window)
+    state = []  # per request: [stream id, next picture, ended]
+    inflight = {}
+    total = sum(r[3] for r in reqs)
+    done = 0
+    t0 = time.perf_counter()
+    nxt = 0
+    while done < total:
+        now = time.perf_counter() - t0
+        while nxt < len(reqs) and reqs[nxt][0] <= now:
+            _, res, kind, n = reqs[nxt]
+            pics, slots = pools[(res, kind)]
+            state.append([srv.open(pics[0].width_mbs, pics[0].height_mbs, slots), 0, False, pics, n])
+            nxt += 1
+        for stt in state:
+            sid, k, ended, pics, n = stt
+            if ended:
+                continue
+            while k < n and srv.pending(sid) < window:
+                p = pics[k]
+                buf = take_buf(p.plane_bytes)
+                inflight[(sid, k)] = buf
+                rc = srv.push(sid, p, p.group, k, buf)
+                if rc != 0:
+                    raise RuntimeError("server push: %d" % rc)
+                k += 1
+            stt[1] = k
+            if k == n:
+                srv.end(sid)
+                stt[2] = True
+        for sid, tag, status, _ in srv.poll(wait_ms=1):
+            if status != 0:
+                raise RuntimeError("serving: picture failed (%d)" % status)
+            buf = inflight.pop((sid, tag))
+            free_bufs[buf.nbytes].append(buf)
+            done += 1
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    ctx.close()
+    return {
+        "fps": round(total / wall, 1), "pictures": total, "streams": len(reqs), "wall_s": round(wall, 3),
+        "p50_frame_ms": round(st["p50_ms"], 3), "p99_frame_ms": round(st["p99_ms"], 3),
+        "max_frame_ms": round(st["max_ms"], 3), "batches": st["batches"],
+        "pictures_per_batch": round(st["batch_pictures"] / max(1, st["batches"]), 2),
+        "waiting_peak": st["waiting_peak"], "dpb_peak_gb": round(st["dpb_bytes_peak"] / 1e9, 3),
+        "config": "Poisson 40 streams/s for %.1f s, CIF/720p/1080p p=0.3/0.4/0.3, 8..120 pictures, IP or IBBP, "
+                  "40 GB DPB budget, window 4 pictures per stream, outputs to pinned host memory" % args.serve_seconds,
     }
 
 
@@ -405,6 +527,8 @@ def run_engine(args, world, rank, local, dist):
         e2e = {"value": round(frames_per_step * e2e_steps / e2e_dt, 2), "unit": "frames/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": frames_per_step * FRAME_BYTES}
         extra = {"plain_fps": round(plain_fps, 2), "cpu_baseline": cpu, "e2e": e2e, "bit_exact_sample": exact}
+        if args.serve_seconds > 0:
+            extra["serving"] = run_serving(args, local)
 
     for s in streams:
         s.close()
