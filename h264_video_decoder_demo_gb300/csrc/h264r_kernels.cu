@@ -603,6 +603,7 @@ struct IntraSmem {
     int32_t res[384];     // residual: luma raster 16x16, Cb 8x8, Cr 8x8
     int nb[40];           // neighbouring samples (-1: not available)
     int nbf[40];          // filtered (8x8) neighbours
+    int nb4[2][16];       // neighbours of the two 4x4 blocks of a wave
 };
 
 // 4x4 prediction sample (x, y) from nb = {p[-1,-1], p[-1,0..3], p[0..7,-1]}
@@ -1011,15 +1012,36 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     __syncwarp();
     // ---- luma
     if (m.type == H264R_MB_I4x4) {
-        for (int b = 0; b < 16; b++) {
-            const int xO = kBlkX[b] * 4, yO = kBlkY[b] * 4;
-            if (lane < 16) {
-                int nb[13];
-                nb[0] = tile_nb(t, xO - 1, yO - 1, true);
-                for (int i = 0; i < 4; i++) nb[1 + i] = tile_nb(t, xO - 1, yO + i, true);
-                for (int i = 0; i < 8; i++) nb[5 + i] = tile_nb(t, xO + i, yO - 1, !(i > 3 && (b == 3 || b == 11)));
-                if (nb[9] < 0 && nb[10] < 0 && nb[11] < 0 && nb[12] < 0 && nb[8] >= 0) nb[9] = nb[10] = nb[11] = nb[12] = nb[8];
-                const int i = lane >> 2, j = lane & 3;
+        // The 4x4 blocks on one anti-diagonal of the block grid (bx + 2*by
+        // constant) depend on none of each other (left, top, top-left and
+        // top-right all lie on earlier diagonals): 10 waves of at most two
+        // blocks, one per half-warp, in place of 16 steps.
+        const int half = lane >> 4, hl = lane & 15;
+        int *nb = s.nb4[half];
+        for (int wv = 0; wv < 10; wv++) {
+            const int by = min(3, wv >> 1) - half, bx = wv - 2 * by;
+            const bool valid = by >= 0 && bx >= 0 && bx <= 3;
+            const int b = 8 * (by >> 1) + 4 * (bx >> 1) + 2 * (by & 1) + (bx & 1);
+            const int xO = bx * 4, yO = by * 4;
+            if (valid && hl < 13) {
+                // nb = {p[-1,-1], p[-1,0..3], p[0..7,-1]}; an unavailable
+                // top-right quartet takes p[3,-1] (the four are available
+                // together or not at all)
+                int v;
+                if (hl == 0) {
+                    v = tile_nb(t, xO - 1, yO - 1, true);
+                } else if (hl < 5) {
+                    v = tile_nb(t, xO - 1, yO + hl - 1, true);
+                } else {
+                    const int i = hl - 5;
+                    v = tile_nb(t, xO + i, yO - 1, !(i > 3 && (b == 3 || b == 11)));
+                    if (i > 3 && v < 0) v = tile_nb(t, xO + 3, yO - 1, true);
+                }
+                nb[hl] = v;
+            }
+            __syncwarp();
+            if (valid) {
+                const int i = hl >> 2, j = hl & 3;
                 const int mode = (m.ipred[b >> 3] >> (4 * (b & 7))) & 15;
                 int pv = pred4x4_sample(mode, nb, j, i);
                 if (pv < 0) pv = 0;  // prediction not written: the cleared buffer
@@ -1030,42 +1052,46 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     } else if (m.type == H264R_MB_I8x8) {
         for (int b = 0; b < 4; b++) {
             const int xO = (b & 1) * 8, yO = (b >> 1) * 8;
+            // q = {p[-1,-1], p[-1,0..7], p[0..15,-1]}; an unavailable
+            // top-right octet takes p[7,-1]
             if (lane < 25) {
-                int nx = lane < 9 ? -1 : lane - 9, ny = lane < 9 ? lane - 1 : -1;
-                s.nb[lane] = tile_nb(t, xO + nx, yO + ny, true);
+                int v;
+                if (lane == 0) {
+                    v = tile_nb(t, xO - 1, yO - 1, true);
+                } else if (lane < 9) {
+                    v = tile_nb(t, xO - 1, yO + lane - 1, true);
+                } else {
+                    const int i = lane - 9;
+                    v = tile_nb(t, xO + i, yO - 1, true);
+                    if (i > 7 && v < 0) v = tile_nb(t, xO + 7, yO - 1, true);
+                }
+                s.nb[lane] = v;
             }
             __syncwarp();
-            if (lane == 0) {
-                int *q = s.nb;
-                bool all = true;
-                for (int i = 17; i < 25; i++) all = all && q[i] < 0;
-                if (all && q[16] >= 0)
-                    for (int i = 17; i < 25; i++) q[i] = q[16];
-                int *f = s.nbf;
-                for (int i = 0; i < 25; i++) f[i] = -1;
-                bool top16 = true;
-                for (int i = 9; i < 25; i++) top16 = top16 && q[i] >= 0;
-                if (top16) {
-                    f[9] = (q[0] >= 0) ? (q[0] + 2 * q[9] + q[10] + 2) >> 2 : (3 * q[9] + q[10] + 2) >> 2;
-                    for (int i = 10; i < 24; i++) f[i] = (q[i - 1] + 2 * q[i] + q[i + 1] + 2) >> 2;
-                    f[24] = (q[23] + 3 * q[24] + 2) >> 2;
-                }
-                if (q[0] >= 0) {
-                    if (q[9] < 0 || q[1] < 0) {
-                        if (q[9] >= 0) f[0] = (3 * q[0] + q[9] + 2) >> 2;
-                        else if (q[1] >= 0) f[0] = (3 * q[0] + q[1] + 2) >> 2;
-                        else f[0] = q[0];
-                    } else {
-                        f[0] = (q[9] + 2 * q[0] + q[1] + 2) >> 2;
+            // 8.3.2.2.1 reference sample filtering, one sample per lane
+            // (H264PictureBase.cpp:1540-1600)
+            if (lane < 25) {
+                const int *q = s.nb;
+                int f = -1;
+                if (lane == 0) {
+                    if (q[0] >= 0) {
+                        if (q[9] < 0 || q[1] < 0)
+                            f = q[9] >= 0 ? (3 * q[0] + q[9] + 2) >> 2 : q[1] >= 0 ? (3 * q[0] + q[1] + 2) >> 2 : q[0];
+                        else
+                            f = (q[9] + 2 * q[0] + q[1] + 2) >> 2;
                     }
+                } else if (lane < 9) {
+                    if (q[1] >= 0) {  // the left column is available as a whole
+                        if (lane == 1) f = q[0] >= 0 ? (q[0] + 2 * q[1] + q[2] + 2) >> 2 : (3 * q[1] + q[2] + 2) >> 2;
+                        else if (lane < 8) f = (q[lane - 1] + 2 * q[lane] + q[lane + 1] + 2) >> 2;
+                        else f = (q[7] + 3 * q[8] + 2) >> 2;
+                    }
+                } else if (q[9] >= 0 && q[17] >= 0) {  // all 16 top samples
+                    if (lane == 9) f = q[0] >= 0 ? (q[0] + 2 * q[9] + q[10] + 2) >> 2 : (3 * q[9] + q[10] + 2) >> 2;
+                    else if (lane < 24) f = (q[lane - 1] + 2 * q[lane] + q[lane + 1] + 2) >> 2;
+                    else f = (q[23] + 3 * q[24] + 2) >> 2;
                 }
-                bool left8 = true;
-                for (int i = 1; i < 9; i++) left8 = left8 && q[i] >= 0;
-                if (left8) {
-                    f[1] = (q[0] >= 0) ? (q[0] + 2 * q[1] + q[2] + 2) >> 2 : (3 * q[1] + q[2] + 2) >> 2;
-                    for (int i = 2; i < 8; i++) f[i] = (q[i - 1] + 2 * q[i] + q[i + 1] + 2) >> 2;
-                    f[8] = (q[7] + 3 * q[8] + 2) >> 2;
-                }
+                s.nbf[lane] = f;
             }
             __syncwarp();
             const int mode = (m.ipred[0] >> (4 * b)) & 15;
@@ -1115,35 +1141,37 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     const int cmode = m.chroma_mode;
     for (int kk = lane; kk < 128; kk += 32) {
         const int pl = kk >> 6, i = (kk & 63) >> 3, j = kk & 7;
-        int q[17];
-        q[0] = t.c[pl][0][0];
-        for (int u = 0; u < 8; u++) { q[1 + u] = t.c[pl][1 + u][0]; q[9 + u] = t.c[pl][0][1 + u]; }
+        const int(*c)[9] = t.c[pl];  // c[0][0] corner, c[1+u][0] left, c[0][1+u] top
+#define CL(u) c[1 + (u)][0]
+#define CT(u) c[0][1 + (u)]
         int pv = 0;
         if (cmode == 0) {
-            int xO = j & 4, yO = i & 4;
-            bool t4 = q[9 + xO] > 0 && q[10 + xO] > 0 && q[11 + xO] > 0 && q[12 + xO] > 0;
-            bool l4 = q[1 + yO] > 0 && q[2 + yO] > 0 && q[3 + yO] > 0 && q[4 + yO] > 0;
-            int stp = t4 ? q[9 + xO] + q[10 + xO] + q[11 + xO] + q[12 + xO] : 0;
-            int slf = l4 ? q[1 + yO] + q[2 + yO] + q[3 + yO] + q[4 + yO] : 0;
+            const int xO = j & 4, yO = i & 4;
+            const bool t4 = CT(xO) > 0 && CT(xO + 1) > 0 && CT(xO + 2) > 0 && CT(xO + 3) > 0;
+            const bool l4 = CL(yO) > 0 && CL(yO + 1) > 0 && CL(yO + 2) > 0 && CL(yO + 3) > 0;
+            const int stp = t4 ? CT(xO) + CT(xO + 1) + CT(xO + 2) + CT(xO + 3) : 0;
+            const int slf = l4 ? CL(yO) + CL(yO + 1) + CL(yO + 2) + CL(yO + 3) : 0;
             if ((xO == 0 && yO == 0) || (xO > 0 && yO > 0)) pv = (t4 && l4) ? (stp + slf + 4) >> 3 : l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
             else if (xO > 0) pv = t4 ? (stp + 2) >> 2 : l4 ? (slf + 2) >> 2 : 128;
             else pv = l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
         } else if (cmode == 1) {
-            pv = A ? q[1 + i] : 0;
+            pv = A ? CL(i) : 0;
         } else if (cmode == 2) {
-            pv = B ? q[9 + j] : 0;
+            pv = B ? CT(j) : 0;
         } else if (cmode == 3) {
             if (A && B && D) {
                 int H = 0, V = 0;
                 for (int u = 0; u <= 3; u++) {
-                    H += (u + 1) * (q[9 + 4 + u] - (2 - u >= 0 ? q[9 + 2 - u] : q[0]));
-                    V += (u + 1) * (q[1 + 4 + u] - (2 - u >= 0 ? q[1 + 2 - u] : q[0]));
+                    H += (u + 1) * (CT(4 + u) - (2 - u >= 0 ? CT(2 - u) : c[0][0]));
+                    V += (u + 1) * (CL(4 + u) - (2 - u >= 0 ? CL(2 - u) : c[0][0]));
                 }
-                int a = 16 * (q[1 + 7] + q[9 + 7]);
-                int b2 = (34 * H + 32) >> 6, c2 = (34 * V + 32) >> 6;
+                const int a = 16 * (CL(7) + CT(7));
+                const int b2 = (34 * H + 32) >> 6, c2 = (34 * V + 32) >> 6;
                 pv = clip1((a + b2 * (j - 3) + c2 * (i - 3) + 16) >> 5);
             }
         }
+#undef CL
+#undef CT
         s.res[256 + kk] = clip1(pv + s.res[256 + kk]);  // reconstructed chroma, in place
     }
     __syncwarp();
@@ -1158,7 +1186,9 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(32) k_intra(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st)
+// 21 resident row warps per SM (registers capped at 80): a batch of many
+// pictures keeps more rows of its wavefronts in flight
+__global__ void __launch_bounds__(32, 21) k_intra(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st)
 {
     __shared__ IntraSmem s;
     __shared__ IntraTile tile;
@@ -1375,6 +1405,34 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
     EdgeCtl c = edge_ctl(p, cur);
     uint8_t *out = p.bs + (size_t)cur * kBsBytes;
     uint32_t mystop = 0xFFFFFFFFu;
+    if (!p.mbaff) {
+        // Frame picture: a strength depends only on the pair of 4x4 blocks
+        // (no field or mixed edges), so lane (dir, e, b) derives edge e of
+        // direction dir for lines 4b..4b+3, and the 4:2:0 chroma strengths
+        // are the luma ones of the same edge at line 2k (the reference
+        // derives them from the luma positions, 994-1310).
+        const int dir = lane >> 4, e = (lane >> 2) & 3, b = lane & 3;
+        const bool on = e == 0 ? (dir ? c.top : c.left) : (c.internal && (e == 2 || !c.t8));
+        int bs = 0;
+        if (on) bs = dir == 0 ? edge_bs(p, cur, 0, 1, 4 * e, c.mbA, 0, 4 * b) : edge_bs(p, cur, 0, 0, 4 * e, c.mbB, 0, 4 * b);
+        if (bs == 0xFF) mystop = stop_key(cur, dir == 0 ? SEQ_LV0 + e : (e == 0 ? SEQ_LH0 : SEQ_LH4 + e - 1), 4 * b);
+        const int k = lane & 15;
+        uint32_t vrow = 0, hrow = 0;
+#pragma unroll
+        for (int e2 = 0; e2 < 4; e2++) {
+            vrow |= (uint32_t)(__shfl_sync(0xffffffffu, bs, e2 * 4 + (k >> 2)) & 255) << (8 * e2);
+            hrow |= (uint32_t)(__shfl_sync(0xffffffffu, bs, 16 + e2 * 4 + (k >> 2)) & 255) << (8 * e2);
+        }
+        *(uint32_t *)(out + (lane < 16 ? bs_lv(0, k) : bs_lh(0, k))) = lane < 16 ? vrow : hrow;
+        // chroma line ck: edges 0 and 4 are luma edges 0 and 8 at luma line 2*ck
+        const int ck = lane & 7;
+        const uint32_t c0 = (uint32_t)(vrow & 255), c1 = (vrow >> 16) & 255;  // lane k = 2*ck holds line 2*ck
+        const uint32_t h0 = (uint32_t)(hrow & 255), h1 = (hrow >> 16) & 255;
+        const uint32_t cvw = __shfl_sync(0xffffffffu, c0 | (c1 << 8), 2 * ck);
+        const uint32_t chw = __shfl_sync(0xffffffffu, h0 | (h1 << 8), 2 * ck);
+        if (lane < 8) *(uint16_t *)(out + bs_cv(0, ck)) = (uint16_t)cvw;
+        else if (lane < 16) *(uint16_t *)(out + bs_ch(0, ck)) = (uint16_t)chw;
+    } else {
     // luma vertical (4 edges x 16 rows): items 0..63
     for (int it = lane; it < 64; it += 32) {
         int ei = it >> 4, k = it & 15, e = ei * 4;
@@ -1429,6 +1487,7 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
             out[kBsChromaTop2 + k] = (uint8_t)bs;
         }
         if (bs == 0xFF) mystop = min(mystop, stop_key(cur, seqcb, k));
+    }
     }
     // thresholds of each edge class for the frame fast path of k_deblock
     if (!p.mbaff && lane < 9) {
