@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--streams", type=int, default=16)
     ap.add_argument("--pictures", type=int, default=30)
-    ap.add_argument("--pipelines", type=int, default=2, help="concurrent batch pipelines over disjoint stream sets")
+    ap.add_argument("--pipelines", type=int, default=3, help="concurrent batch pipelines over disjoint stream sets")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (quick runs)")
     ap.add_argument("--serve-seconds", type=float, default=4.0,
                     help="length of the Poisson arrival window of the serving run (0: skip it)")

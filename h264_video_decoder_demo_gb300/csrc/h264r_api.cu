@@ -38,6 +38,7 @@ static_assert(sizeof(h264r_slice) == 8, "h264r_slice layout");
 namespace {
 
 constexpr int kRing = 4;                 // in-flight launches per stream
+constexpr int kBatchRing = 8;            // in-flight batched launches per context (all pipelines)
 constexpr uint64_t kAlign = 256;
 constexpr unsigned long long kSpinLimit = 1ull << 25;  // ~ seconds of 64 ns sleeps
 
@@ -146,7 +147,7 @@ struct h264r_ctx {
     std::vector<std::array<cudaEvent_t, 4>> ev_free, ev_pending;
     std::mutex timing_mu;
     cudaStream_t batch_stream = nullptr;
-    LaunchBuf batch_ring[kRing];
+    LaunchBuf batch_ring[kBatchRing];
     int batch_next = 0;
     std::mutex mu;
     char err[256] = {0};
@@ -759,7 +760,7 @@ extern "C" int h264r_submit_batch_device(h264r_ctx *ctx, int n, h264r_stream *co
     cudaSetDevice(ctx->device);
     std::lock_guard<std::mutex> lk(ctx->mu);
     LaunchBuf &b = ctx->batch_ring[ctx->batch_next];
-    ctx->batch_next = (ctx->batch_next + 1) % kRing;
+    ctx->batch_next = (ctx->batch_next + 1) % kBatchRing;
     int rc = wait_slot(ctx, b);
     if (rc) return rc;
     // the batch runs on the CUDA stream of its first member, after any work
@@ -853,7 +854,7 @@ extern "C" int h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *st
     cudaSetDevice(ctx->device);
     std::lock_guard<std::mutex> lk(ctx->mu);
     LaunchBuf &b = ctx->batch_ring[ctx->batch_next];
-    ctx->batch_next = (ctx->batch_next + 1) % kRing;
+    ctx->batch_next = (ctx->batch_next + 1) % kBatchRing;
     int rc = wait_slot(ctx, b);
     if (rc) return rc;
     // layout of the packed records of every picture, then one host -> device copy

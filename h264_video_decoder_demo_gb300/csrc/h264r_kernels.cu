@@ -1207,25 +1207,32 @@ __global__ void __launch_bounds__(32, 21) k_intra(const PicDesc *__restrict__ pi
     // Units without intra MBs were completed by k_inter: progress is only
     // published before this row waits and after each intra unit.
     int posted = 0;
-    for (int u = 0; u < uw; u++) {
-        bool any = false;
-        for (int k = 0; k < per; k++) {
-            int addr = p.mbaff ? 2 * (row * uw + u) + k : row * uw + u;
-            any = any || is_intra_type(p.mbs[addr].type);
+    for (int u0 = 0; u0 < uw; u0 += 32) {
+        // which of the next 32 units hold intra MBs: one record load per lane
+        bool mine = false;
+        if (u0 + lane < uw) {
+            for (int k = 0; k < per; k++) {
+                const int addr = p.mbaff ? 2 * (row * uw + u0 + lane) + k : row * uw + u0 + lane;
+                mine = mine || is_intra_type(p.mbs[addr].type);
+            }
         }
-        if (!any) continue;
-        if (lane == 0 && posted < u) st_release(prog + row, u);
-        posted = u;
-        if (row > 0 && !wait_progress(st, prog + row - 1, min(u + 2, uw))) return;
-        for (int k = 0; k < per; k++) {
-            int addr = p.mbaff ? 2 * (row * uw + u) + k : row * uw + u;
-            if (!is_intra_type(p.mbs[addr].type)) continue;
-            if (p.mbaff) intra_mb(p, addr, s, st);
-            else intra_mb_frame(p, addr, s, tile, st);
+        uint32_t todo = __ballot_sync(0xffffffffu, mine);
+        while (todo) {
+            const int u = u0 + __ffs(todo) - 1;
+            todo &= todo - 1;
+            if (lane == 0 && posted < u) st_release(prog + row, u);
+            posted = u;
+            if (row > 0 && !wait_progress(st, prog + row - 1, min(u + 2, uw))) return;
+            for (int k = 0; k < per; k++) {
+                int addr = p.mbaff ? 2 * (row * uw + u) + k : row * uw + u;
+                if (!is_intra_type(p.mbs[addr].type)) continue;
+                if (p.mbaff) intra_mb(p, addr, s, st);
+                else intra_mb_frame(p, addr, s, tile, st);
+            }
+            __syncwarp();
+            if (lane == 0) st_release(prog + row, u + 1);
+            posted = u + 1;
         }
-        __syncwarp();
-        if (lane == 0) st_release(prog + row, u + 1);
-        posted = u + 1;
     }
     if (lane == 0 && posted < uw) st_release(prog + row, uw);
 }
