@@ -163,12 +163,10 @@ def peak_hbm():
         return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    try:
-        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
-            return json.load(f)
-    except (OSError, ValueError):
-        return {}
+# DRAM bytes (read + write) per MB of each timed kernel, measured with ncu on
+# the 1080p High mix (profiles/dram_traffic_1080p_high_8streams.md); scaled
+# to a launch by the MBs it processes.
+DRAM_BYTES_PER_MB = {"k_inter": 1089, "k_intra": 303, "k_bs+k_deblock": 794}
 
 
 def dist_setup(args):
@@ -452,17 +450,16 @@ def run_engine(args, world, rank, local, dist):
     value = world * frames_per_step * args.steps / (elapsed_ms / 1000.0)
 
     # ---- roofline of the dominant kernel
-    names = ["k_inter", "k_intra", "k_deblock"]
+    names = ["k_inter", "k_intra", "k_bs+k_deblock"]
     dom = int(np.argmax(ktimes))
     per_kernel_bytes = algo[:3] * args.steps
     achieved = per_kernel_bytes[dom] / (ktimes[dom] / 1000.0) / 1e9 if ktimes[dom] > 0 else 0.0
     peak, peak_kind = peak_hbm()
-    tr = ncu_traffic().get(names[dom])
-    traffic = None
-    if tr and "bytes_per_frame" in tr:
-        traffic = int(tr["bytes_per_frame"] * frames_per_step / len(batches))
+    mbs_per_launch = frames_per_step * 120 * 68 / len(batches)
+    traffic = int(DRAM_BYTES_PER_MB[names[dom]] * mbs_per_launch)
     roofline = {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                "traffic_note": "ncu DRAM bytes per MB of this kernel on the same mix, scaled to the MBs of one launch",
                 "algorithmic_bytes_per_launch": int(per_kernel_bytes[dom] / (args.steps * len(batches))),
                 "kernel_ms_per_step": [round(t / args.steps, 3) for t in ktimes]}
 
