@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--streams", type=int, default=16)
+    ap.add_argument("--streams", type=int, default=32)
     ap.add_argument("--pictures", type=int, default=30)
     ap.add_argument("--pipelines", type=int, default=3, help="concurrent batch pipelines over disjoint stream sets")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (quick runs)")

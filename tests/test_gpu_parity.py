@@ -99,3 +99,45 @@ def test_720p_implicit_matches_oracle(gpu_ctx):
 def test_cif_all_intra_and_dense_coefficients(gpu_ctx):
     g = h.synth("cif_ippp", seed=5, intra_percent=100, coef_density=95, qp_min=0, qp_max=51)
     assert run_against_oracle(gpu_ctx, g) == 8
+
+
+def test_mixed_size_batches_match_oracle(gpu_ctx):
+    """Pictures of CIF, 720p and 1080p streams reconstructed together in one
+    launch sequence per dependency group (h264r_submit_batch), as the
+    batched configuration mixes sizes; every picture against the oracle."""
+    specs = [("cif_ippp", 41, 6), ("720p_high", 42, 6), ("1080p_high", 43, 6), ("cif_ippp", 44, 6)]
+    streams, oracles, pics = [], [], []
+    for name, seed, n in specs:
+        g = h.synth(name, seed=seed, num_pictures=n)
+        ps = list(g)
+        pics.append(ps)
+        streams.append(h.Stream(gpu_ctx, ps[0].width_mbs, ps[0].height_mbs, g.dpb_slots))
+        oracles.append(OracleDPB(ps[0].width_mbs, ps[0].height_mbs, g.dpb_slots))
+        g.close()
+    try:
+        cursor = [0] * len(specs)
+        batches = 0
+        while any(c < len(p) for c, p in zip(cursor, pics)):
+            # the next dependency group of every stream, all in one batch
+            ss, pp, who = [], [], []
+            for i, ps in enumerate(pics):
+                if cursor[i] >= len(ps):
+                    continue
+                grp = ps[cursor[i]].group
+                while cursor[i] < len(ps) and ps[cursor[i]].group == grp:
+                    ss.append(streams[i])
+                    pp.append(ps[cursor[i]])
+                    who.append(i)
+                    cursor[i] += 1
+            gpu_ctx.submit_batch(ss, pp)
+            batches += 1
+            for st, p, i in zip(ss, pp, who):
+                rc, _ = oracles[i].reconstruct(p)
+                assert rc == 0
+                out = st.output(p.dst_slot)
+                diff = _first_diff(out, oracles[i].planes(p.dst_slot), p.width_mbs, p.height_mbs)
+                assert diff is None, "%s seed %d: %s" % (specs[i][0], specs[i][1], diff)
+        assert batches < sum(len(p) for p in pics)
+    finally:
+        for s in streams:
+            s.close()
