@@ -13,6 +13,7 @@
 // Cross-row waits spin on per-row progress counters with an iteration
 // limit; on expiry the kernel records H264R_ERR_DEVICE_TIMEOUT and returns.
 #include "h264r_device.cuh"
+#include "h264r_mc.cuh"
 
 namespace h264r {
 
@@ -313,13 +314,11 @@ __device__ bool mb_residual(const PicDesc &p, const h264r_mb &m, int field, int 
 constexpr int kInterWarps = 4;  // 6 blocks (24 warps) per SM: registers capped at 80
 
 struct InterWarpSmem {
-    uint32_t win[32][21];  // per-lane luma reference window, 7 rows x 12 bytes
     int32_t res[384];      // residual: luma raster 16x16, Cb 8x8, Cr 8x8
     int32_t dcs[32];       // Intra16x16 DC work area
     __align__(16) uint8_t out[384];
 };
 
-#define TAP6(a, b, c_, d, e, f) ((a) - 5 * (b) + 20 * (c_) + 20 * (d) - 5 * (e) + (f))
 
 // Reference window of one lane: rows yi-2..yi+4, columns xi-2..xi+6 of a
 // luma plane, clamped at the picture edges like luma_sample (8.4.2.2.1,
@@ -327,7 +326,7 @@ struct InterWarpSmem {
 // row r+2 holds sample (xi+c, yi+r)).  Away from the edges each row is three
 // aligned 32-bit loads and two funnel shifts; the loads may read up to three
 // bytes past the window, which stay inside the picture allocation.
-__device__ __forceinline__ void load_luma_window(const RefView &rv, int ymax, int xi, int yi, uint32_t *win)
+__device__ __forceinline__ void load_luma_window(const RefView &rv, int ymax, int xi, int yi, uint32_t (&win)[21])
 {
     const int x0 = xi - 2, y0 = yi - 2;
     if (x0 >= 0 && xi + 6 <= rv.xmax && y0 >= 0 && yi + 4 <= ymax) {
@@ -388,81 +387,6 @@ __device__ __forceinline__ void chroma_2x2(const uint8_t *pl, int stride, int xm
 #undef CB
 }
 
-// 8.4.2.2.1 for a 2x4 group of samples (rows i0..i0+1, cols 0..3 of the
-// window origin) from the window bytes win[(r+2)*12 + (c+2)], r in -2..4,
-// c in -2..6.  The
-// centre sample j uses horizontal taps first: the taps are exact integers,
-// so the order of the two 6-tap passes does not change j1.
-__device__ __forceinline__ void mc_luma_2x4(const uint8_t *win, int xf, int yf, int out[8])
-{
-#define WV(r, c) ((int)win[((r) + 2) * 12 + (c) + 2])
-    if ((xf | yf) == 0) {
-#pragma unroll
-        for (int i = 0; i < 2; i++)
-#pragma unroll
-            for (int j = 0; j < 4; j++) out[i * 4 + j] = WV(i, j);
-        return;
-    }
-    if (yf == 0) {
-#pragma unroll
-        for (int i = 0; i < 2; i++)
-#pragma unroll 1
-            for (int j = 0; j < 4; j++) {
-                int b = clip1((TAP6(WV(i, j - 2), WV(i, j - 1), WV(i, j), WV(i, j + 1), WV(i, j + 2), WV(i, j + 3)) + 16) >> 5);
-                out[i * 4 + j] = xf == 2 ? b : ((xf == 1 ? WV(i, j) : WV(i, j + 1)) + b + 1) >> 1;
-            }
-        return;
-    }
-    if (xf == 0) {
-#pragma unroll
-        for (int i = 0; i < 2; i++)
-#pragma unroll 1
-            for (int j = 0; j < 4; j++) {
-                int h = clip1((TAP6(WV(i - 2, j), WV(i - 1, j), WV(i, j), WV(i + 1, j), WV(i + 2, j), WV(i + 3, j)) + 16) >> 5);
-                out[i * 4 + j] = yf == 2 ? h : ((yf == 1 ? WV(i, j) : WV(i + 1, j)) + h + 1) >> 1;
-            }
-        return;
-    }
-    if (xf == 2 || yf == 2) {
-        // column by column: the horizontal 6-tap sums of rows -2..4 of one
-        // column give j at rows 0 and 1 of that column
-#pragma unroll 1
-        for (int j = 0; j < 4; j++) {
-            int hb1[7];
-#pragma unroll
-            for (int r = -2; r <= 4; r++)
-                hb1[r + 2] = TAP6(WV(r, j - 2), WV(r, j - 1), WV(r, j), WV(r, j + 1), WV(r, j + 2), WV(r, j + 3));
-#pragma unroll
-            for (int i = 0; i < 2; i++) {
-                int jv = clip1((TAP6(hb1[i], hb1[i + 1], hb1[i + 2], hb1[i + 3], hb1[i + 4], hb1[i + 5]) + 512) >> 10);
-                int o;
-                if (xf == 2 && yf == 2) {
-                    o = jv;
-                } else if (xf == 2) {  // f (row i) / q (row i+1)
-                    int b = clip1(((yf == 3 ? hb1[i + 3] : hb1[i + 2]) + 16) >> 5);
-                    o = (b + jv + 1) >> 1;
-                } else {  // i (col j) / k (col j+1)
-                    int c = j + (xf == 3 ? 1 : 0);
-                    int hh = clip1((TAP6(WV(i - 2, c), WV(i - 1, c), WV(i, c), WV(i + 1, c), WV(i + 2, c), WV(i + 3, c)) + 16) >> 5);
-                    o = (hh + jv + 1) >> 1;
-                }
-                out[i * 4 + j] = o;
-            }
-        }
-        return;
-    }
-    // e, g, p, r
-#pragma unroll
-    for (int i = 0; i < 2; i++)
-#pragma unroll 1
-        for (int j = 0; j < 4; j++) {
-            int r = i + (yf == 3 ? 1 : 0), c = j + (xf == 3 ? 1 : 0);
-            int b = clip1((TAP6(WV(r, j - 2), WV(r, j - 1), WV(r, j), WV(r, j + 1), WV(r, j + 2), WV(r, j + 3)) + 16) >> 5);
-            int h = clip1((TAP6(WV(i - 2, c), WV(i - 1, c), WV(i, c), WV(i + 1, c), WV(i + 2, c), WV(i + 3, c)) + 16) >> 5);
-            out[i * 4 + j] = (b + h + 1) >> 1;
-        }
-#undef WV
-}
 
 __global__ void __launch_bounds__(32 * kInterWarps, 6) k_inter(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st)
 {
@@ -527,7 +451,6 @@ __global__ void __launch_bounds__(32 * kInterWarps, 6) k_inter(const PicDesc *__
             const h264r_weight w = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
             const bool use0 = pp.ref[0] >= 0, use1 = pp.ref[1] >= 0;
             uint32_t va0 = 0, va1 = 0, vb0 = 0, vb1 = 0;  // predictions of list 0 / 1, 8 bytes each
-            uint32_t *win = s.win[lane];
 #pragma unroll 1
             for (int l = 0; l < 2; l++) {
                 if (!(l ? use1 : use0)) continue;
@@ -535,10 +458,10 @@ __global__ void __launch_bounds__(32 * kInterWarps, 6) k_inter(const PicDesc *__
                 const int mvx = l ? pp.mv[1][0] : pp.mv[0][0], mvy = l ? pp.mv[1][1] : pp.mv[0][1];
                 const RefView rv = ref_view(p, ref);
                 const int xi = x + bx * 4 + (mvx >> 2), yi = yAL0 + by * 4 + r0 + (mvy >> 2);
-                load_luma_window(rv, ymax, xi, yi, win);  // the lane's own window: no warp barrier
-                int o[8];
-                mc_luma_2x4((const uint8_t *)win, mvx & 3, mvy & 3, o);
-                const uint32_t w0 = pack4(o[0], o[1], o[2], o[3]), w1 = pack4(o[4], o[5], o[6], o[7]);
+                uint32_t win[21];  // the lane's reference window, in registers
+                load_luma_window(rv, ymax, xi, yi, win);
+                uint32_t w0, w1;
+                mc_luma_2x4_w(win, mvx & 3, mvy & 3, w0, w1);
                 if (l) { vb0 = w0; vb1 = w1; } else { va0 = w0; va1 = w1; }
             }
 #pragma unroll 1
@@ -594,7 +517,6 @@ __global__ void __launch_bounds__(32 * kInterWarps, 6) k_inter(const PicDesc *__
         *(uint2 *)(plane_c(p, pl) + (size_t)(chroma_row0(y) + r * dy) * p.Wc + x / 2) = *(const uint2 *)(s.out + 256 + pl * 64 + r * 8);
     }
 }
-#undef TAP6
 
 // ======================================================================
 // K2: intra macroblocks, wavefront
