@@ -25,6 +25,7 @@ __global__ void k_inter(const PicDesc *__restrict__ pics, int npics, uint32_t to
 __global__ void k_intra(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st);
 __global__ void k_bs(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
 __global__ void k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st);
+__global__ void k_bgr24(const uint8_t *__restrict__ yuv, int W, int H, uint8_t *__restrict__ out, int row_bytes, int flip);
 }  // namespace h264r
 
 using h264r::PicDesc;
@@ -161,6 +162,8 @@ struct h264r_stream {
     cudaStream_t cs = nullptr;
     LaunchBuf ring[kRing];
     int next = 0;
+    uint8_t *bgr = nullptr;  // device staging of h264r_output_bgr24
+    uint64_t bgr_cap = 0;
 };
 
 static void set_err(h264r_ctx *ctx, const char *fmt, ...)
@@ -363,6 +366,7 @@ extern "C" int h264r_stream_close(h264r_stream *s)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(s->cs);
     for (auto &b : s->ring) free_buf(b);
+    if (s->bgr) cudaFree(s->bgr);
     cudaStreamDestroy(s->cs);
     cudaFree(s->dpb);
     {
@@ -794,6 +798,72 @@ extern "C" int h264r_output(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, 
     CUDA_OR(ctx, cudaMemcpyAsync(cb, base + W * H, W * H / 4, cudaMemcpyDeviceToHost, s->cs));
     CUDA_OR(ctx, cudaMemcpyAsync(cr, base + W * H + W * H / 4, W * H / 4, cudaMemcpyDeviceToHost, s->cs));
     return H264R_OK;
+}
+
+extern "C" int h264r_output_bgr24_device(h264r_stream *s, int slot, void *dst, uint32_t row_bytes, int flip)
+{
+    if (!s || slot < 0 || slot >= s->cfg.dpb_slots || !dst || ((uintptr_t)dst & 3)) return H264R_ERR_INVALID_ARG;
+    const int W = s->cfg.width_mbs * 16, H = s->cfg.height_mbs * 16;
+    if ((row_bytes & 3) || row_bytes < 3u * W) return H264R_ERR_INVALID_ARG;
+    h264r_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    const uint8_t *base = s->dpb + (uint64_t)slot * s->slot_bytes;
+    dim3 grid((W / 4 + 255) / 256, H);
+    h264r::k_bgr24<<<grid, 256, 0, s->cs>>>(base, W, H, (uint8_t *)dst, (int)row_bytes, flip ? 1 : 0);
+    CUDA_OR(ctx, cudaGetLastError());
+    ctx->launches++;
+    return H264R_OK;
+}
+
+extern "C" int h264r_output_bgr24(h264r_stream *s, int slot, uint8_t *dst, uint32_t row_bytes, int flip)
+{
+    if (!s || !dst) return H264R_ERR_INVALID_ARG;
+    const uint64_t bytes = (uint64_t)s->cfg.height_mbs * 16 * row_bytes;
+    int rc = ensure(s->ctx, &s->bgr, &s->bgr_cap, bytes, false);
+    if (rc) return rc;
+    rc = h264r_output_bgr24_device(s, slot, s->bgr, row_bytes, flip);
+    if (rc) return rc;
+    CUDA_OR(s->ctx, cudaMemcpyAsync(dst, s->bgr, bytes, cudaMemcpyDeviceToHost, s->cs));
+    return H264R_OK;
+}
+
+static void put_le(uint8_t *p, uint32_t v, int n)
+{
+    for (int i = 0; i < n; i++) p[i] = (uint8_t)(v >> (8 * i));
+}
+
+extern "C" int h264r_write_bmp(const char *path, const uint8_t *bgr, uint32_t width, uint32_t height, uint32_t row_bytes)
+{
+    if (!path || !bgr || !width || !height || row_bytes < 3u * width) return H264R_ERR_INVALID_ARG;
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return H264R_ERR_IO;
+    // 'BM', then the file header (size, reserved, offset) and the 40-byte info header
+    uint8_t hdr[54] = {0};
+    hdr[0] = 'B';
+    hdr[1] = 'M';
+    put_le(hdr + 2, height * row_bytes + 54, 4);
+    put_le(hdr + 10, 54, 4);
+    put_le(hdr + 14, 40, 4);
+    put_le(hdr + 18, width, 4);
+    put_le(hdr + 22, height, 4);
+    put_le(hdr + 26, 1, 2);
+    put_le(hdr + 28, 24, 2);
+    put_le(hdr + 34, height * row_bytes, 4);
+    bool ok = fwrite(hdr, 1, 54, fp) == 54;
+    for (int64_t i = (int64_t)height - 1; ok && i >= 0; i--) ok = fwrite(bgr + (size_t)i * row_bytes, 1, row_bytes, fp) == row_bytes;
+    ok = (fclose(fp) == 0) && ok;
+    return ok ? H264R_OK : H264R_ERR_IO;
+}
+
+extern "C" int h264r_write_yuv(const char *path, const uint8_t *y, const uint8_t *cb, const uint8_t *cr, uint32_t width, uint32_t height)
+{
+    if (!path || !y || !cb || !cr || !width || !height) return H264R_ERR_INVALID_ARG;
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return H264R_ERR_IO;
+    const size_t ny = (size_t)width * height, nc = ny / 4;
+    bool ok = fwrite(y, 1, ny, fp) == ny && fwrite(cb, 1, nc, fp) == nc && fwrite(cr, 1, nc, fp) == nc;
+    ok = (fclose(fp) == 0) && ok;
+    return ok ? H264R_OK : H264R_ERR_IO;
 }
 
 extern "C" int h264r_load_slot(h264r_stream *s, int slot, const uint8_t *y, const uint8_t *cb, const uint8_t *cr)

@@ -1923,4 +1923,42 @@ __global__ void __launch_bounds__(32) k_deblock(const PicDesc *__restrict__ pics
     }
 }
 
+// ======================================================================
+// Output: decoded picture to BGR24 rows
+// ======================================================================
+// CH264PictureBase::convertYuv420pToBgr24 / convertYuv420pToBgr24FlipLines
+// (H264PictureBase.cpp:440-499): BT.601 limited-range integer conversion,
+// C division (truncation toward zero), clipped.  One thread per 4 pixels of
+// a row: one 32-bit luma load, two 16-bit chroma loads, three 32-bit stores.
+__global__ void __launch_bounds__(256) k_bgr24(const uint8_t *__restrict__ yuv, int W, int H, uint8_t *__restrict__ out,
+                                               int row_bytes, int flip)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (q >= W / 4 || y >= H) return;
+    const int x = 4 * q;
+    const uint8_t *cb = yuv + (size_t)W * H, *cr = cb + (size_t)W * H / 4;
+    const uint32_t yw = __ldg((const uint32_t *)(yuv + (size_t)y * W + x));
+    const uint32_t uw = __ldg((const uint16_t *)(cb + (size_t)(y / 2) * (W / 2) + x / 2));
+    const uint32_t vw = __ldg((const uint16_t *)(cr + (size_t)(y / 2) * (W / 2) + x / 2));
+    uint32_t o[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int Y = (yw >> (8 * k)) & 255, U = (uw >> (8 * (k >> 1))) & 255, V = (vw >> (8 * (k >> 1))) & 255;
+        const int b = (1164 * (Y - 16) + 2018 * (U - 128)) / 1000;
+        const int g = (1164 * (Y - 16) - 813 * (V - 128) - 391 * (U - 128)) / 1000;
+        const int r = (1164 * (Y - 16) + 1596 * (V - 128)) / 1000;
+        const int c[3] = {b, g, r};
+#pragma unroll
+        for (int ch = 0; ch < 3; ch++) {
+            const int byte = 3 * k + ch;
+            o[byte >> 2] |= (uint32_t)H264R_CLIP3(0, 255, c[ch]) << (8 * (byte & 3));
+        }
+    }
+    uint32_t *dst = (uint32_t *)(out + (size_t)(flip ? H - 1 - y : y) * row_bytes + 3 * x);
+    dst[0] = o[0];
+    dst[1] = o[1];
+    dst[2] = o[2];
+}
+
 }  // namespace h264r

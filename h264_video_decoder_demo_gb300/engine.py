@@ -28,6 +28,7 @@ EXPORTS = [
     "h264r_submit_batch", "h264r_picture_bytes", "h264r_ctx_cuda_stream",
     "h264r_deblock_picture_noalloc",
     "h264r_ctx_device", "h264r_ctx_dpb_budget", "h264r_ctx_max_batch",
+    "h264r_output_bgr24", "h264r_output_bgr24_device", "h264r_write_bmp", "h264r_write_yuv",
     "h264r_server_create", "h264r_server_destroy", "h264r_server_open", "h264r_server_push",
     "h264r_server_end", "h264r_server_poll", "h264r_server_pending", "h264r_server_get_stats",
 ]
@@ -85,6 +86,10 @@ def _load():
         "h264r_synth_dpb_slots": (i32, [vp]),
         "h264r_synth_next": (i32, [vp, P(R.CPicture), P(i32)]),
         "h264r_synth_destroy": (i32, [vp]),
+        "h264r_output_bgr24": (i32, [vp, i32, vp, ctypes.c_uint32, i32]),
+        "h264r_output_bgr24_device": (i32, [vp, i32, vp, ctypes.c_uint32, i32]),
+        "h264r_write_bmp": (i32, [ctypes.c_char_p, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]),
+        "h264r_write_yuv": (i32, [ctypes.c_char_p, vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32]),
         "h264r_ctx_device": (i32, [vp]),
         "h264r_ctx_dpb_budget": (u64, [vp]),
         "h264r_ctx_max_batch": (i32, [vp]),
@@ -112,6 +117,29 @@ def picture_bytes(pic):
     if rc != 0:
         raise EngineError(rc, "h264r_picture_bytes")
     return list(out)
+
+
+def bgr_row_bytes(width):
+    """Bytes per BGR24 row as the reference's bitmaps pad them (multiple of 4)."""
+    return (3 * width + 3) // 4 * 4
+
+
+def write_bmp(path, bgr, width, height):
+    """24-bit BMP of top-down BGR24 rows (numpy uint8, height x row_bytes)."""
+    bgr = np.ascontiguousarray(bgr, np.uint8)
+    rb = bgr.size // height
+    rc = lib().h264r_write_bmp(os.fsencode(path), bgr.ctypes.data, width, height, rb)
+    if rc != 0:
+        raise EngineError(rc, "write_bmp")
+
+
+def write_yuv(path, planes, width, height):
+    """Planar YUV 4:2:0 file (planes: numpy uint8 of width*height*3/2)."""
+    planes = np.ascontiguousarray(planes, np.uint8)
+    base = planes.ctypes.data
+    rc = lib().h264r_write_yuv(os.fsencode(path), base, base + width * height, base + width * height * 5 // 4, width, height)
+    if rc != 0:
+        raise EngineError(rc, "write_yuv")
 
 
 def validate(pic, dpb_slots):
@@ -221,6 +249,15 @@ class Stream:
         W, H = self.width_mbs * 16, self.height_mbs * 16
         base = out.ctypes.data
         return self.ctx.check(lib().h264r_output(self.h, slot, base, base + W * H, base + W * H + W * H // 4), "output")
+
+    def output_bgr24(self, slot, flip=False):
+        """The picture in a slot as BGR24 rows (height x row_bytes, numpy)."""
+        W, H = self.width_mbs * 16, self.height_mbs * 16
+        rb = bgr_row_bytes(W)
+        out = np.empty((H, rb), np.uint8)
+        self.ctx.check(lib().h264r_output_bgr24(self.h, slot, out.ctypes.data, rb, int(flip)), "output_bgr24")
+        self.sync()
+        return out
 
     def load_slot(self, slot, planes):
         W, H = self.width_mbs * 16, self.height_mbs * 16

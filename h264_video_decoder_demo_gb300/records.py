@@ -31,7 +31,7 @@ NONE32 = 0xFFFFFFFF
 OK = 0
 ERR_INVALID_ARG, ERR_BAD_RECORD, ERR_UNSUPPORTED, ERR_CUDA = -1, -2, -3, -4
 ERR_NO_MEMORY, ERR_BUDGET, ERR_DEVICE_TIMEOUT, ERR_BUSY = -5, -6, -7, -8
-ERR_TOO_LARGE = -9
+ERR_TOO_LARGE, ERR_IO = -9, -10
 
 
 class CPicture(ctypes.Structure):

@@ -49,6 +49,7 @@ extern "C" {
 #define H264R_ERR_DEVICE_TIMEOUT -7  /* a bounded device-side wait expired      */
 #define H264R_ERR_BUSY          -8   /* no free slot / queue full               */
 #define H264R_ERR_TOO_LARGE     -9   /* exceeds a fixed maximum size            */
+#define H264R_ERR_IO           -10   /* a file could not be written             */
 
 /* ---- macroblock record ------------------------------------------------- */
 /* mb type classes (derived from mb_type / MbPartPredMode, 7.4.5)          */
@@ -293,6 +294,25 @@ int  h264r_picture_bytes(const h264r_picture *pic, uint64_t out[4]);
  * reading the planes.
  */
 int  h264r_output(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *cr);
+/*
+ * Decoded picture (DPB slot) as BGR24 rows of row_bytes bytes (at least
+ * 3*width, a multiple of 4, like the reference's bitmap rows), top-down, or
+ * bottom-up when flip != 0: the reference's conversion for its BMP output
+ * and its player (CH264PictureBase::convertYuv420pToBgr24 /
+ * convertYuv420pToBgr24FlipLines, H264PictureBase.cpp:440-499), computed on
+ * the GPU.  dst: host memory (h264r_output_bgr24, enqueued: call
+ * h264r_stream_sync before reading) or 4-byte aligned device memory
+ * (h264r_output_bgr24_device).
+ */
+int  h264r_output_bgr24(h264r_stream *s, int slot, uint8_t *dst, uint32_t row_bytes, int flip);
+int  h264r_output_bgr24_device(h264r_stream *s, int slot, void *dst, uint32_t row_bytes, int flip);
+/* 24-bit BMP file of top-down BGR24 rows, written bottom-up with the
+ * reference's 54-byte header (CH264PictureBase::saveBmp,
+ * H264PictureBase.cpp:554-600).  Host only. */
+int  h264r_write_bmp(const char *path, const uint8_t *bgr, uint32_t width, uint32_t height, uint32_t row_bytes);
+/* Planar YUV 4:2:0 file at coded size (CH264PictureBase::writeYUV,
+ * H264PictureBase.cpp:651-665).  Host only. */
+int  h264r_write_yuv(const char *path, const uint8_t *y, const uint8_t *cb, const uint8_t *cr, uint32_t width, uint32_t height);
 /* Upload host planes into a DPB slot (initial state / tests). */
 int  h264r_load_slot(h264r_stream *s, int slot, const uint8_t *y, const uint8_t *cb, const uint8_t *cr);
 /* Device address of a DPB slot's Y plane (Cb, Cr follow contiguously). */

@@ -1461,3 +1461,25 @@ int h264o_deblock(const h264r_picture *pic, uint8_t *const *dpb, int nslots)
     if (rc) return rc;
     return deblock_picture(&c);
 }
+
+/* ---------------------------------------------------------------- output */
+/* BT.601 limited-range integers with C division (truncation toward zero),
+ * clipped, as H264PictureBase.cpp:457-463. */
+void h264o_bgr24(int width, int height, const uint8_t *yuv, uint8_t *bgr, int row_bytes, int flip)
+{
+    const int W = width, H = height;
+    for (int y = 0; y < H; y++) {
+        uint8_t *row = bgr + (size_t)(flip ? H - 1 - y : y) * row_bytes;
+        for (int x = 0; x < W; x++) {
+            const int Y = yuv[(size_t)y * W + x];
+            const int U = yuv[(size_t)H * W + (size_t)(y / 2) * (W / 2) + x / 2];
+            const int V = yuv[(size_t)H * W + (size_t)H * W / 4 + (size_t)(y / 2) * (W / 2) + x / 2];
+            const int b = (1164 * (Y - 16) + 2018 * (U - 128)) / 1000;
+            const int g = (1164 * (Y - 16) - 813 * (V - 128) - 391 * (U - 128)) / 1000;
+            const int r = (1164 * (Y - 16) + 1596 * (V - 128)) / 1000;
+            row[3 * x + 0] = (uint8_t)(b < 0 ? 0 : b > 255 ? 255 : b);
+            row[3 * x + 1] = (uint8_t)(g < 0 ? 0 : g > 255 ? 255 : g);
+            row[3 * x + 2] = (uint8_t)(r < 0 ? 0 : r > 255 ? 255 : r);
+        }
+    }
+}

@@ -31,6 +31,12 @@ int h264o_reconstruct(const h264r_picture *pic, uint8_t *const *dpb, int nslots,
 /* Only the deblocking pass, in place on dpb[pic->dst_slot]. */
 int h264o_deblock(const h264r_picture *pic, uint8_t *const *dpb, int nslots);
 
+/* YUV 4:2:0 planes (Y, Cb, Cr contiguous, coded size) to BGR24 rows of
+ * row_bytes bytes, bottom-up when flip (CH264PictureBase::
+ * convertYuv420pToBgr24 / convertYuv420pToBgr24FlipLines,
+ * H264PictureBase.cpp:440-499). */
+void h264o_bgr24(int width, int height, const uint8_t *yuv, uint8_t *bgr, int row_bytes, int flip);
+
 #ifdef __cplusplus
 }
 #endif

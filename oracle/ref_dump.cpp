@@ -38,6 +38,7 @@ static FILE *g_out = NULL;
 static int g_pictures = 0;
 static int g_max_pictures = 1 << 30;
 static int g_write_planes = 1;
+static const char *g_bmp_dir = NULL;  // --bmp: the reference's BMP of every dumped picture
 static int g_unsupported = 0;
 static int g_verbose = 1;
 
@@ -402,6 +403,12 @@ extern "C" int __wrap__ZN16CH264PictureBase25Deblocking_filter_processEv(CH264Pi
     int ret = __real__ZN16CH264PictureBase25Deblocking_filter_processEv(self);
     std::vector<uint8_t> post(self->m_pic_buff_luma, self->m_pic_buff_luma + plane_bytes);
     dump_picture(self, pre.data(), post.data(), plane_bytes);
+    if (g_bmp_dir) {
+        // the reference's own output path for this picture (YUV420P -> BGR24 -> BMP)
+        char path[4096];
+        snprintf(path, sizeof(path), "%s/pic_%03d.bmp", g_bmp_dir, g_pictures);
+        self->saveToBmpFile(path);
+    }
     g_pictures++;
     return ret;
 }
@@ -417,11 +424,12 @@ static int on_frame(CH264Picture *out, void *user, int err)
 int main(int argc, char **argv)
 {
     if (argc < 3) {
-        fprintf(stderr, "usage: %s <in.h264> <out.dmp> [max_pictures] [--no-planes]\n", argv[0]);
+        fprintf(stderr, "usage: %s <in.h264> <out.dmp> [max_pictures] [--no-planes] [--bmp <dir>]\n", argv[0]);
         return 2;
     }
     for (int i = 3; i < argc; i++) {
         if (strcmp(argv[i], "--no-planes") == 0) g_write_planes = 0;
+        else if (strcmp(argv[i], "--bmp") == 0 && i + 1 < argc) g_bmp_dir = argv[++i];
         else g_max_pictures = atoi(argv[i]);
     }
     g_out = fopen(argv[2], "wb");

@@ -5,7 +5,9 @@ sources by `make -C oracle ref`) on the reference's bundled streams and keeps
 the first pictures of each stream, in decoding order from the IDR:
 
   <name>.h264r.gz   records of those pictures (dump container, no planes)
-  <name>.json       md5 of the reference's pre- and post-deblocking planes
+  <name>.json       md5 of the reference's pre- and post-deblocking planes,
+                    and of the BMP file the reference writes for each picture
+                    (CH264PictureBase::saveToBmpFile: YUV420P -> BGR24 -> BMP)
 
 Usage: python tests/golden/make_fixtures.py [--ref-data DIR]
 The fixtures are committed; this script needs the reference sources and is
@@ -52,13 +54,17 @@ def main():
     with tempfile.TemporaryDirectory(dir=os.path.join(ROOT, "_work") if os.path.isdir(os.path.join(ROOT, "_work")) else None) as tmp:
         for name, stream, n, tools in FIXTURES:
             dmp = os.path.join(tmp, name + ".dmp")
-            subprocess.run([dumper, os.path.join(args.ref_data, stream), dmp, str(n)],
+            bmp_dir = os.path.join(tmp, name + "_bmp")
+            os.makedirs(bmp_dir)
+            subprocess.run([dumper, os.path.join(args.ref_data, stream), dmp, str(n), "--bmp", bmp_dir],
                            stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, check=True)
             pics = read_dump(dmp)
             meta = {"stream": stream, "coding_tools": tools, "pictures": []}
-            for p in pics:
+            for i, p in enumerate(pics):
+                with open(os.path.join(bmp_dir, "pic_%03d.bmp" % i), "rb") as f:
+                    bmp_md5 = hashlib.md5(f.read()).hexdigest()
                 meta["pictures"].append({"poc": p.poc, "dst_slot": p.dst_slot, "mbaff": p.mbaff,
-                                         "pre_md5": md5(p.pre), "post_md5": md5(p.post)})
+                                         "pre_md5": md5(p.pre), "post_md5": md5(p.post), "bmp_md5": bmp_md5})
             raw = os.path.join(tmp, name + ".raw")
             write_dump(raw, pics, planes=False)
             with open(raw, "rb") as f, gzip.open(os.path.join(HERE, name + ".h264r.gz"), "wb", 9) as g:

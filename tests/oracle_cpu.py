@@ -23,6 +23,8 @@ def lib():
         L.h264o_slot_bytes.argtypes = [ctypes.c_int, ctypes.c_int]
         L.h264o_reconstruct.restype = ctypes.c_int
         L.h264o_reconstruct.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.h264o_bgr24.restype = None
+        L.h264o_bgr24.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         _L = L
     return _L
 
@@ -47,3 +49,12 @@ class OracleDPB:
 
     def planes(self, slot):
         return self.slots[slot][:self.plane_bytes]
+
+
+def bgr24(planes, width, height, flip=False):
+    """The oracle's BGR24 rows of YUV 4:2:0 planes (height x row_bytes)."""
+    rb = (3 * width + 3) // 4 * 4
+    out = np.zeros((height, rb), np.uint8)
+    planes = np.ascontiguousarray(planes, np.uint8)
+    lib().h264o_bgr24(width, height, planes.ctypes.data, out.ctypes.data, rb, int(flip))
+    return out

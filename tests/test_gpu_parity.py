@@ -141,3 +141,22 @@ def test_mixed_size_batches_match_oracle(gpu_ctx):
     finally:
         for s in streams:
             s.close()
+
+
+@pytest.mark.parametrize("name", ["heavyhand_cabac_p_explicit", "gop121_baseline_multislice"])
+def test_engine_bgr24_bmp_matches_reference_bmp(gpu_ctx, name, tmp_path):
+    """Decoded on the GPU, converted to BGR24 on the GPU, written by the
+    library: byte for byte the BMP the reference writes for the picture."""
+    pics, meta = load_fixture(name)
+    W, H = pics[0].width_mbs * 16, pics[0].height_mbs * 16
+    s = h.Stream(gpu_ctx, pics[0].width_mbs, pics[0].height_mbs, 16)
+    try:
+        for i, (p, m) in enumerate(zip(pics, meta["pictures"])):
+            s.submit(p)
+            rows = s.output_bgr24(p.dst_slot)
+            path = tmp_path / ("pic_%d.bmp" % i)
+            h.engine.write_bmp(str(path), rows, W, H)
+            assert hashlib.md5(path.read_bytes()).hexdigest() == m["bmp_md5"], "%s picture %d" % (name, i)
+            assert (s.output_bgr24(p.dst_slot, flip=True) == rows[::-1]).all()
+    finally:
+        s.close()

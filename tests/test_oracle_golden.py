@@ -44,3 +44,24 @@ def test_fixtures_cover_the_hot_path_tools():
                 bipred |= bool(((parts["ref"][:, 0] >= 0) & (parts["ref"][:, 1] >= 0)).any())
     assert {0, 1, 2, 3} <= seen_types
     assert mbaff and t8 and weighted and bipred and none_mbs and slices > 1
+
+
+@pytest.mark.parametrize("name", fixture_names())
+def test_bgr24_and_bmp_writer_match_reference_bmp(name, tmp_path):
+    """The reference's BMP output of each fixture picture
+    (CH264PictureBase::saveToBmpFile: YUV420P -> BGR24 -> BMP) against the
+    oracle's conversion of its planes written by the library's BMP writer
+    (host code, no GPU)."""
+    import h264_video_decoder_demo_gb300 as h
+    from oracle_cpu import bgr24
+    pics, meta = load_fixture(name)
+    W, H = pics[0].width_mbs * 16, pics[0].height_mbs * 16
+    dpb = OracleDPB(pics[0].width_mbs, pics[0].height_mbs)
+    for i, (p, m) in enumerate(zip(pics, meta["pictures"])):
+        assert dpb.reconstruct(p)[0] == 0
+        rows = bgr24(dpb.planes(p.dst_slot), W, H)
+        path = tmp_path / ("pic_%d.bmp" % i)
+        h.engine.write_bmp(str(path), rows, W, H)
+        assert hashlib.md5(path.read_bytes()).hexdigest() == m["bmp_md5"], "picture %d" % i
+        flipped = bgr24(dpb.planes(p.dst_slot), W, H, flip=True)
+        assert (flipped == rows[::-1]).all()
