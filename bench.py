@@ -52,13 +52,15 @@ def parse():
     ap.add_argument("--pictures", type=int, default=30)
     ap.add_argument("--pipelines", type=int, default=3, help="concurrent batch pipelines over disjoint stream sets")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (quick runs)")
+    ap.add_argument("--skip-configs", action="store_true", help="omit the mixed-size and CIF runs")
     ap.add_argument("--serve-seconds", type=float, default=4.0,
                     help="length of the Poisson arrival window of the serving run (0: skip it)")
     return ap.parse_args()
 
 
-def gen_streams(n, pictures, seed0):
-    """Records of n seeded streams (generated in parallel; the generator is C)."""
+def gen_streams(n, pictures, seed0, workloads=None, overrides=None):
+    """Records of n seeded streams (generated in parallel; the generator is C).
+    workloads: per-stream workload names (default: the 1080p High one)."""
     import h264_video_decoder_demo_gb300 as h
     h.lib()
     out = [None] * n
@@ -67,7 +69,11 @@ def gen_streams(n, pictures, seed0):
 
     def work(i):
         try:
-            g = h.synth(WORKLOAD, seed=seed0 + i, num_pictures=pictures)
+            name, over = (workloads[i] if workloads else WORKLOAD), dict(overrides or {})
+            if isinstance(name, tuple):  # (workload, per-stream overrides)
+                name, extra = name
+                over.update(extra)
+            g = h.synth(name, seed=seed0 + i, num_pictures=pictures, **over)
             out[i] = list(g)
             slots[i] = g.dpb_slots
             g.close()
@@ -223,6 +229,107 @@ def run_reference(args, rank):
         "cpu_baseline": {"value": round(fps, 3), "unit": "frames/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": round(fps, 3), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+
+
+def run_mixed(args, device, seed=4000):
+    """Batched configuration: 32 independent streams, 12 CIF, 12 720p and 8
+    1080p, 60 pictures each, I/P anchors with B pictures between them (the
+    generator puts two B between anchors), the CIF configuration's value
+    distributions (MVs +-64 quarter samples, QP 20..36, 10% intra),
+    records resident in HBM; every step reconstructs all 1920 pictures, one
+    fused launch per dependency group across all streams.  Reports frames/s
+    and MB/s."""
+    import numpy as np
+    import torch
+
+    import h264_video_decoder_demo_gb300 as h
+    from h264_video_decoder_demo_gb300 import records as R
+
+    sizes = [(22, 18)] * 12 + [(80, 45)] * 12 + [(120, 68)] * 8
+    kinds = [("cif_ippp", dict(width_mbs=w, height_mbs=hh)) for w, hh in sizes]
+    pics, slots = gen_streams(len(kinds), 60, seed, workloads=kinds, overrides=dict(gop_kind=1, gop_length=15))
+    dev = torch.device("cuda", device)
+    ctx = h.Context(device, max_batch=256)
+    streams = [h.Stream(ctx, p[0].width_mbs, p[0].height_mbs, sl) for p, sl in zip(pics, slots)]
+    keep, cp = [], []
+    for ps in pics:
+        row = []
+        for p in ps:
+            c = p.to_c()
+            for name in R.Picture._ARRAYS:
+                a = np.ascontiguousarray(getattr(p, name)).view(np.uint8).reshape(-1)
+                t = torch.from_numpy(a.copy()).to(dev) if a.size else torch.empty(1, dtype=torch.uint8, device=dev)
+                keep.append(t)
+                setattr(c, name, t.data_ptr())
+            row.append(c)
+        cp.append(row)
+    ngroups = max(p.group for ps in pics for p in ps) + 1
+    batches = []
+    for g in range(ngroups):
+        ss, cc = [], []
+        for i, ps in enumerate(pics):
+            for k, p in enumerate(ps):
+                if p.group == g:
+                    ss.append(streams[i])
+                    cc.append(cp[i][k])
+        if ss:
+            batches.append((ss, cc))
+    cs = torch.cuda.ExternalStream(streams[0].cuda_stream(), device=dev)
+
+    def step():
+        for ss, cc in batches:
+            rc = ctx.submit_batch_device(ss, cc)
+            if rc != 0:
+                raise RuntimeError("mixed batch: %d %s" % (rc, ctx.last_error()))
+
+    for _ in range(2):
+        step()
+    ctx.sync()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nsteps = 3
+    torch.cuda.synchronize()
+    t0.record(cs)
+    for _ in range(nsteps):
+        step()
+    for st in streams:  # every stream's work, seen from the first stream
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.ExternalStream(st.cuda_stream(), device=dev))
+        cs.wait_event(ev)
+    t1.record(cs)
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / nsteps
+    frames = sum(len(p) for p in pics)
+    mbs = sum(p.width_mbs * p.height_mbs for ps in pics for p in ps)
+    for st in streams:
+        st.close()
+    ctx.close()
+    return {"fps": round(frames / (ms / 1000.0), 1), "mb_per_s": round(mbs / (ms / 1000.0), 1),
+            "ms_per_step": round(ms, 3), "batches_per_step": len(batches),
+            "config": "32 streams (12 CIF, 12 720p, 8 1080p) x 60 pictures, IBBP, CIF-configuration distributions, "
+                      "one launch per dependency group across all streams, records in HBM, single pipeline"}
+
+
+def run_plain_cif(device, seed=1000):
+    """CIF 352x288, 8 pictures IPPP, Baseline tools (1 ref, 4x4 transforms),
+    one picture per launch sequence with a host sync after each."""
+    import h264_video_decoder_demo_gb300 as h
+    pics, slots = gen_streams(1, 8, seed, workloads=["cif_ippp"])
+    ctx = h.Context(device)
+    s = h.Stream(ctx, 22, 18, slots[0])
+    for p in pics[0]:
+        s.submit(p)
+        s.sync()
+    t0 = time.perf_counter()
+    n = 0
+    for _ in range(20):
+        for p in pics[0]:
+            s.submit(p)
+            s.sync()
+            n += 1
+    dt = time.perf_counter() - t0
+    s.close()
+    ctx.close()
+    return {"fps": round(n / dt, 1), "config": "CIF IPPP 8 pictures, host records, one picture per launch, host sync"}
 
 
 SERVE_RES = [("cif", 22, 18, 0.3), ("720p", 80, 45, 0.4), ("1080p", 120, 68, 0.3)]
@@ -526,6 +633,9 @@ def run_engine(args, world, rank, local, dist):
         extra = {"plain_fps": round(plain_fps, 2), "cpu_baseline": cpu, "e2e": e2e, "bit_exact_sample": exact}
         if args.serve_seconds > 0:
             extra["serving"] = run_serving(args, local)
+        if not args.skip_configs:
+            extra["batched_mixed"] = run_mixed(args, local)
+            extra["plain_cif"] = run_plain_cif(local)
 
     for s in streams:
         s.close()
