@@ -277,12 +277,20 @@ static void make_picture(h264r_synth *g, const Plan &pl)
         return add_weight(g, w);
     };
 
+    // MBAFF: MBs in pair order (top, bottom); the pair's field decision is
+    // taken at its top MB
+    const bool mbaff = c.mbaff != 0;
+    bool pair_field = false;
     for (int a = 0; a < n; a++) {
-        const int mx = a % W, my = a / W;
+        const int mx = mbaff ? (a / 2) % W : a % W;
+        const int my = mbaff ? 2 * ((a / 2) / W) + (a & 1) : a / W;
         h264r_mb &m = g->mbs[a];
         memset(&m, 0, sizeof(m));
         m.coef = H264R_NONE;
         m.aux = H264R_NONE;
+        if (mbaff && (a & 1) == 0) pair_field = r.pct(c.field_percent);
+        const bool field = mbaff && pair_field;
+        if (field) m.flags |= H264R_MBF_FIELD;
         m.qpy = (uint8_t)r.range(c.qp_min, c.qp_max);
         m.slice = 0;
         bool intra = pl.type == PIC_I || r.pct(c.intra_percent);
@@ -294,7 +302,9 @@ static void make_picture(h264r_synth *g, const Plan &pl)
             else if (roll < 450) m.type = H264R_MB_I4x4;
             else if (roll < 750) m.type = c.transform8x8 ? H264R_MB_I8x8 : H264R_MB_I4x4;
             else m.type = H264R_MB_I16x16;
-            bool A = mx > 0, B = my > 0, D = mx > 0 && my > 0;
+            // MBAFF neighbourhoods depend on the pairs around: DC modes only,
+            // which need no neighbour
+            bool A = !mbaff && mx > 0, B = !mbaff && my > 0, D = !mbaff && mx > 0 && my > 0;
             if (m.type == H264R_MB_IPCM) {
                 m.aux = (uint32_t)(g->pcm.size() / 384);
                 for (int i = 0; i < 384; i++) g->pcm.push_back((uint8_t)r.range(0, 255));
@@ -305,7 +315,8 @@ static void make_picture(h264r_synth *g, const Plan &pl)
                 static const int by[16] = {0, 0, 1, 1, 0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 3, 3};
                 for (int b = 0; b < 16; b++) {
                     bool left = bx[b] > 0 || A, top = by[b] > 0 || B, corner = left && top && (bx[b] > 0 || by[b] > 0 || D);
-                    m.ipred[b >> 3] |= (uint32_t)pick4(r, top, left, corner) << (4 * (b & 7));
+                    const int md = mbaff ? 2 : pick4(r, top, left, corner);
+                    m.ipred[b >> 3] |= (uint32_t)md << (4 * (b & 7));
                     if (make_block(r, cb, b, 0, 16, dens, 1)) m.nz4x4 |= (uint16_t)(1u << b);
                 }
             } else if (m.type == H264R_MB_I8x8) {
@@ -313,7 +324,8 @@ static void make_picture(h264r_synth *g, const Plan &pl)
                 for (int b = 0; b < 4; b++) {
                     int x8 = b & 1, y8 = b >> 1;
                     bool left = x8 > 0 || A, top = y8 > 0 || B, corner = left && top && (x8 > 0 || y8 > 0 || D);
-                    m.ipred[0] |= (uint32_t)pick4(r, top, left, corner) << (4 * b);
+                    const int md = mbaff ? 2 : pick4(r, top, left, corner);
+                    m.ipred[0] |= (uint32_t)md << (4 * b);
                     if (make_block(r, cb, b, 0, 64, dens, 4)) m.nz8x8 |= (uint8_t)(1u << b);
                 }
             } else {
@@ -411,6 +423,10 @@ static void make_picture(h264r_synth *g, const Plan &pl)
                     int slot = l == 0 ? pl.l0[rr[l]] : pl.l1[rr[l]];
                     p.ref[l] = (int8_t)slot;
                     p.dref[l] = (int8_t)slot;
+                    if (field) {  // a field of the reference frame, either parity
+                        p.ref[l] = (int8_t)(slot | H264R_REF_FIELD | (r.pct(50) ? H264R_REF_BOTTOM : 0));
+                        p.dref[l] = (int8_t)(p.ref[l] & 0x7F);
+                    }
                     int mvx, mvy;
                     bool same_as_quadrant = direct16 && (e % 4) != 0;
                     if (same_as_quadrant) {
@@ -430,6 +446,7 @@ static void make_picture(h264r_synth *g, const Plan &pl)
                         if (side == 3) mvy = ((H - my) * 16 + r.range(0, 48)) * 4;
                         mvx = clip3(-2048, 2047, mvx);
                         mvy = clip3(-512, 511, mvy);
+                        if (field) mvy /= 2;  // field rows
                     } else {
                         mvx = r.range(-c.mv_range, c.mv_range);
                         mvy = r.range(-c.mv_range, c.mv_range);
@@ -472,7 +489,7 @@ static void make_picture(h264r_synth *g, const Plan &pl)
 extern "C" int h264r_synth_create(const h264r_synth_cfg *cfg, h264r_synth **out)
 {
     if (!cfg || !out || cfg->width_mbs == 0 || cfg->height_mbs == 0 || cfg->num_pictures == 0 || cfg->qp_min > cfg->qp_max ||
-        cfg->qp_max > 51)
+        cfg->qp_max > 51 || (cfg->mbaff && (cfg->height_mbs & 1)))
         return H264R_ERR_INVALID_ARG;
     h264r_synth *g = new (std::nothrow) h264r_synth();
     if (!g) return H264R_ERR_NO_MEMORY;
@@ -497,7 +514,7 @@ extern "C" int h264r_synth_next(h264r_synth *g, h264r_picture *pic, int *depende
     pic->width_mbs = g->cfg.width_mbs;
     pic->height_mbs = g->cfg.height_mbs;
     pic->structure = H264R_STRUCT_FRAME;
-    pic->mbaff = 0;
+    pic->mbaff = g->cfg.mbaff ? 1 : 0;
     pic->dst_slot = (uint8_t)pl.slot;
     pic->deblock = 1;
     pic->num_slices = (uint16_t)g->slices.size();

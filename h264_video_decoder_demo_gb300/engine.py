@@ -413,6 +413,12 @@ WORKLOADS = {
                        num_refs=4, transform8x8=1, weighted=1, min_partition=3, intra_percent=5,
                        skip_percent=10, qp_min=22, qp_max=40, edge_mv_percent=5, mv_range=256,
                        filter_offset_max=6, coef_density=40),
+    # interlaced 1080i: MBAFF frame/field MB pairs (half the pairs field),
+    # I/P anchors with B between, MVs +-128 qpel, no weighted prediction
+    "1080i_mbaff": dict(width_mbs=120, height_mbs=68, num_pictures=20, gop_length=12, gop_kind=1,
+                        num_refs=2, transform8x8=1, weighted=0, min_partition=3, intra_percent=5,
+                        skip_percent=10, qp_min=22, qp_max=40, edge_mv_percent=5, mv_range=128,
+                        filter_offset_max=6, coef_density=40, mbaff=1, field_percent=50),
     "720p_high": dict(width_mbs=80, height_mbs=45, num_pictures=60, gop_length=15, gop_kind=1,
                       num_refs=4, transform8x8=1, weighted=2, min_partition=3, intra_percent=5,
                       skip_percent=10, qp_min=22, qp_max=40, edge_mv_percent=5, mv_range=256,

@@ -144,7 +144,7 @@ class CSynthCfg(ctypes.Structure):
                 ("qp_min", ctypes.c_uint8), ("qp_max", ctypes.c_uint8),
                 ("edge_mv_percent", ctypes.c_uint8), ("mv_range", ctypes.c_int16),
                 ("filter_offset_max", ctypes.c_int8), ("coef_density", ctypes.c_uint8),
-                ("reserved", ctypes.c_uint8 * 2)]
+                ("mbaff", ctypes.c_uint8), ("field_percent", ctypes.c_uint8)]
 
 
 class CServerCfg(ctypes.Structure):

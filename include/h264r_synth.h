@@ -41,7 +41,8 @@ typedef struct h264r_synth_cfg {
     int16_t  mv_range;          /* MVs uniform in [-mv_range, mv_range] qpel */
     int8_t   filter_offset_max; /* slice alpha/beta offsets in [-max, max]   */
     uint8_t  coef_density;      /* 0..100: share of coded 4x4 blocks        */
-    uint8_t  reserved[2];
+    uint8_t  mbaff;             /* 1: MBAFF frames (frame/field MB pairs)     */
+    uint8_t  field_percent;     /* MBAFF: MB pairs coded as field MBs         */
 } h264r_synth_cfg;
 
 typedef struct h264r_synth h264r_synth;

@@ -160,3 +160,21 @@ def test_engine_bgr24_bmp_matches_reference_bmp(gpu_ctx, name, tmp_path):
             assert (s.output_bgr24(p.dst_slot, flip=True) == rows[::-1]).all()
     finally:
         s.close()
+
+
+def test_mbaff_cif_matches_oracle(gpu_ctx):
+    """MBAFF frames: frame and field MB pairs, field references of either
+    parity, B pictures, 8x8 transforms, MVs past the edges."""
+    g = h.synth("cif_ippp", seed=8, num_pictures=8, mbaff=1, field_percent=50, gop_kind=1, num_refs=2,
+                transform8x8=1, mv_range=128, edge_mv_percent=10)
+    assert run_against_oracle(gpu_ctx, g) == 8
+
+
+def test_mbaff_intra_heavy_matches_oracle(gpu_ctx):
+    g = h.synth("cif_ippp", seed=10, num_pictures=6, mbaff=1, field_percent=50, intra_percent=60, gop_kind=1,
+                transform8x8=1, coef_density=80)
+    assert run_against_oracle(gpu_ctx, g) == 6
+
+
+def test_1080i_mbaff_matches_oracle(gpu_ctx):
+    assert run_against_oracle(gpu_ctx, h.synth("1080i_mbaff", seed=9), npics=6) == 6
