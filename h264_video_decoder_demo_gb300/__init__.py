@@ -5,6 +5,6 @@ include/h264r.h); this package builds it in-tree and binds it for Python
 callers (tests, benchmarks, serving loop).
 """
 from . import records  # noqa: F401
-from .engine import Context, EngineError, Server, Stream, Synth, lib, synth, validate  # noqa: F401
+from .engine import Context, EngineError, Order, Server, Stream, Synth, lib, synth, validate  # noqa: F401
 
 __all__ = ["records", "Context", "Stream", "Synth", "EngineError", "lib", "synth", "validate"]

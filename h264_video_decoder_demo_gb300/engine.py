@@ -16,7 +16,7 @@ _LIB = None
 _LIB_LOCK = threading.Lock()
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libh264r.so")
 
-# every symbol include/h264r.h, include/h264r_synth.h and include/h264r_server.h declare
+# every symbol include/h264r.h, h264r_synth.h, h264r_server.h and h264r_order.h declare
 EXPORTS = [
     "h264r_ctx_create", "h264r_ctx_destroy", "h264r_last_error", "h264r_stream_open",
     "h264r_stream_close", "h264r_stream_dpb_bytes", "h264r_submit_picture",
@@ -29,6 +29,8 @@ EXPORTS = [
     "h264r_deblock_picture_noalloc",
     "h264r_ctx_device", "h264r_ctx_dpb_budget", "h264r_ctx_max_batch",
     "h264r_output_bgr24", "h264r_output_bgr24_device", "h264r_write_bmp", "h264r_write_yuv",
+    "h264r_order_create", "h264r_order_destroy", "h264r_order_push", "h264r_order_flush",
+    "h264r_order_holds", "h264r_order_infer_depth",
     "h264r_server_create", "h264r_server_destroy", "h264r_server_open", "h264r_server_push",
     "h264r_server_end", "h264r_server_poll", "h264r_server_pending", "h264r_server_get_stats",
 ]
@@ -90,6 +92,12 @@ def _load():
         "h264r_output_bgr24_device": (i32, [vp, i32, vp, ctypes.c_uint32, i32]),
         "h264r_write_bmp": (i32, [ctypes.c_char_p, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]),
         "h264r_write_yuv": (i32, [ctypes.c_char_p, vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32]),
+        "h264r_order_create": (i32, [i32, P(vp)]),
+        "h264r_order_destroy": (i32, [vp]),
+        "h264r_order_push": (i32, [vp, u64, ctypes.c_int32, i32, P(u64), i32]),
+        "h264r_order_flush": (i32, [vp, P(u64), i32]),
+        "h264r_order_holds": (i32, [vp, u64]),
+        "h264r_order_infer_depth": (i32, [i32, i32, i32, i32, i32]),
         "h264r_ctx_device": (i32, [vp]),
         "h264r_ctx_dpb_budget": (u64, [vp]),
         "h264r_ctx_max_batch": (i32, [vp]),
@@ -280,6 +288,50 @@ class Stream:
         if self.h:
             lib().h264r_stream_close(self.h)
             self.h = None
+
+
+class Order:
+    """Output order of decoded pictures (include/h264r_order.h): the
+    reference's reorder buffer of max_num_reorder_frames pictures."""
+
+    def __init__(self, max_num_reorder_frames):
+        h = ctypes.c_void_p()
+        rc = lib().h264r_order_create(max_num_reorder_frames, ctypes.byref(h))
+        if rc != 0:
+            raise EngineError(rc, "order_create")
+        self.h = h
+        self._buf = (ctypes.c_uint64 * 32)()
+
+    def push(self, tag, poc, idr=False):
+        """A picture finished decoding; returns the tags to output now."""
+        n = lib().h264r_order_push(self.h, tag, poc, int(bool(idr)), self._buf, 32)
+        if n < 0:
+            raise EngineError(n, "order_push")
+        return [self._buf[i] for i in range(n)]
+
+    def flush(self):
+        n = lib().h264r_order_flush(self.h, self._buf, 32)
+        if n < 0:
+            raise EngineError(n, "order_flush")
+        return [self._buf[i] for i in range(n)]
+
+    def holds(self, tag):
+        return lib().h264r_order_holds(self.h, tag) == 1
+
+    @staticmethod
+    def infer_depth(profile_idc, constraint_set3_flag, level_idc, width_mbs, frame_height_mbs):
+        return lib().h264r_order_infer_depth(profile_idc, constraint_set3_flag, level_idc, width_mbs, frame_height_mbs)
+
+    def close(self):
+        if self.h:
+            lib().h264r_order_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Server:

@@ -39,6 +39,7 @@ static int g_pictures = 0;
 static int g_max_pictures = 1 << 30;
 static int g_write_planes = 1;
 static const char *g_bmp_dir = NULL;  // --bmp: the reference's BMP of every dumped picture
+static FILE *g_order = NULL;         // --order: decoding order (POC, IdrPicFlag, reorder depth) and output order
 static int g_unsupported = 0;
 static int g_verbose = 1;
 
@@ -395,6 +396,10 @@ static void dump_picture(CH264PictureBase *pic, const uint8_t *pre, const uint8_
 
 extern "C" int __wrap__ZN16CH264PictureBase25Deblocking_filter_processEv(CH264PictureBase *self)
 {
+    if (g_order) {  // a completed picture, in decoding order (all but the stream's last)
+        const CH264SliceHeader &sh = self->m_h264_slice_header;
+        fprintf(g_order, "D %d %d %d\n", self->PicOrderCnt, (int)sh.m_nal_unit.IdrPicFlag, (int)sh.m_sps.m_vui.max_num_reorder_frames);
+    }
     if (g_out == NULL || g_pictures >= g_max_pictures || self->m_picture_coded_type != H264_PICTURE_CODED_TYPE_FRAME)
         return __real__ZN16CH264PictureBase25Deblocking_filter_processEv(self);
     size_t plane_bytes = (size_t)self->PicWidthInSamplesL * self->PicHeightInSamplesL +
@@ -418,18 +423,23 @@ static int on_frame(CH264Picture *out, void *user, int err)
     (void)user;
     (void)err;
     if (out == NULL) return -1;
+    if (g_order) fprintf(g_order, "O %d\n", out->m_picture_frame.PicOrderCnt);
     return (g_pictures >= g_max_pictures) ? -1 : 0;
 }
 
 int main(int argc, char **argv)
 {
     if (argc < 3) {
-        fprintf(stderr, "usage: %s <in.h264> <out.dmp> [max_pictures] [--no-planes] [--bmp <dir>]\n", argv[0]);
+        fprintf(stderr, "usage: %s <in.h264> <out.dmp> [max_pictures] [--no-planes] [--bmp <dir>] [--order <file>]\n", argv[0]);
         return 2;
     }
     for (int i = 3; i < argc; i++) {
         if (strcmp(argv[i], "--no-planes") == 0) g_write_planes = 0;
         else if (strcmp(argv[i], "--bmp") == 0 && i + 1 < argc) g_bmp_dir = argv[++i];
+        else if (strcmp(argv[i], "--order") == 0 && i + 1 < argc) {
+            g_order = fopen(argv[++i], "w");
+            if (!g_order) { perror("fopen"); return 1; }
+        }
         else g_max_pictures = atoi(argv[i]);
     }
     g_out = fopen(argv[2], "wb");
@@ -443,6 +453,7 @@ int main(int argc, char **argv)
     dec.set_output_frame_callback_functuin(on_frame, NULL);
     dec.open(argv[1]);
     fclose(g_out);
+    if (g_order) fclose(g_order);
     fprintf(stderr, "ref_dump: %d pictures, unsupported-flags=0x%x\n", g_pictures, g_unsupported);
     return g_unsupported ? 3 : 0;
 }

@@ -9,6 +9,11 @@ the first pictures of each stream, in decoding order from the IDR:
                     and of the BMP file the reference writes for each picture
                     (CH264PictureBase::saveToBmpFile: YUV420P -> BGR24 -> BMP)
 
+  output_order.json for every bundled stream: the pictures in decoding order
+                    as the reference completes them (POC, IdrPicFlag, reorder
+                    depth of the SPS) and the POCs in the order its output
+                    callback receives them
+
 Usage: python tests/golden/make_fixtures.py [--ref-data DIR]
 The fixtures are committed; this script needs the reference sources and is
 only run where they are present.
@@ -44,6 +49,47 @@ def md5(a):
     return hashlib.md5(a.tobytes()).hexdigest()
 
 
+ORDER_STREAMS = ["gop121.naluCnt453.h264", "HeavyHand_1080p.B_frames.cabac.h264",
+                 "HeavyHand_1080p.B_frames_cabac_tff.h264", "HeavyHand_1080p.no_B_frames.cabac.no_tff.h264",
+                 "HeavyHand_1080p.B_frames_4.no_cabac.no_tff.h264"]
+
+
+def make_order_fixture(dumper, ref_data, tmp):
+    """Decoding and output order of whole streams.  The reference completes
+    every picture but the last through its deblocking call (where the dumper
+    records it); the last one is output without deblocking, so its POC is the
+    one output that was never recorded in decoding order."""
+    procs = []
+    for stream in ORDER_STREAMS:
+        path = os.path.join(tmp, stream + ".order")
+        procs.append((stream, path, subprocess.Popen(
+            [dumper, os.path.join(ref_data, stream), os.devnull, "1000000", "--no-planes", "--order", path],
+            stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)))
+    fixture = {}
+    for stream, path, p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("ref_dump failed on " + stream)
+        decoded, output = [], []
+        depth = None
+        with open(path) as f:
+            for line in f:
+                kind, *vals = line.split()
+                if kind == "D":
+                    decoded.append([int(vals[0]), int(vals[1])])
+                    depth = int(vals[2])
+                elif kind == "O":
+                    output.append(int(vals[0]))
+        # POCs restart at every IDR picture: compare as multisets
+        from collections import Counter
+        last = list((Counter(output) - Counter(poc for poc, _ in decoded)).elements())
+        assert len(last) == 1, (stream, last)
+        decoded.append([last[0], 0])
+        fixture[stream] = {"max_num_reorder_frames": depth, "decoded": decoded, "output": output}
+    with open(os.path.join(HERE, "output_order.json"), "w") as f:
+        json.dump(fixture, f)
+    print("output_order.json:", {k: len(v["output"]) for k, v in fixture.items()})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-data", default="/root/reference/data")
@@ -72,6 +118,7 @@ def main():
             with open(os.path.join(HERE, name + ".json"), "w") as f:
                 json.dump(meta, f, indent=1)
             print(name, len(pics), "pictures")
+        make_order_fixture(dumper, args.ref_data, tmp)
 
 
 if __name__ == "__main__":
