@@ -110,8 +110,14 @@ struct LaunchState {
 // Frame (non-MBAFF) pictures also get the filter thresholds of each edge
 // class at kBsParams: [component][left, top, internal] words of
 // alpha | beta << 8 | tC0(bS 1..3) << 16, 21, 26 (8.7.2.2).
+// MBAFF pictures use the same 64 bytes at kBsParams for the MB's edge
+// controls (a word of kDbc* bits) and 5 threshold words per component
+// (indexA | alpha << 8 | beta << 16 of the left edge's even and odd lines,
+// the top edge, the second top edge and the internal edges).
 constexpr int kBsLumaV = 0, kBsLumaH = 64, kBsLumaTop2 = 128, kBsChromaV = 144, kBsChromaH = 160,
               kBsChromaTop2 = 176, kBsParams = 192, kBsBytes = 256;
+constexpr uint32_t kDbcLeft = 1, kDbcTop = 2, kDbcInternal = 4, kDbcT8 = 8, kDbcField = 16, kDbcLeftMixed = 32,
+                   kDbcTopDouble = 64;
 __device__ __forceinline__ constexpr int bs_lv(int e, int k) { return kBsLumaV + 4 * k + e; }
 __device__ __forceinline__ constexpr int bs_lh(int e, int k) { return kBsLumaH + 4 * k + e; }
 __device__ __forceinline__ constexpr int bs_cv(int e, int k) { return kBsChromaV + 2 * k + e; }

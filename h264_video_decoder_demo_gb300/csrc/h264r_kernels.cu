@@ -1430,6 +1430,30 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
                            ((uint32_t)kTc0[1][iA] << 21) | ((uint32_t)kTc0[2][iA] << 26);
         *(uint32_t *)(out + kBsParams + 16 * comp + 4 * kind) = w;
     }
+    // MBAFF pictures: the edge controls of the MB and the thresholds of its
+    // edges, so that the deblocking wavefront reads no records
+    if (p.mbaff && lane < 16) {
+        uint32_t w;
+        if (lane == 15) {
+            w = (c.left ? kDbcLeft : 0u) | (c.top ? kDbcTop : 0u) | (c.internal ? kDbcInternal : 0u) | (c.t8 ? kDbcT8 : 0u) |
+                (c.field ? kDbcField : 0u) | (c.leftMixed ? kDbcLeftMixed : 0u) | (c.topDouble ? kDbcTopDouble : 0u);
+        } else {
+            // 5 words per component: left (even lines), left (odd lines), top,
+            // second top, internal; the p-side MB as deblock_mb's rules
+            const int comp = lane / 5, kind = lane % 5;
+            int mbP = cur;
+            if (kind <= 1 && c.mbA >= 0) mbP = c.leftMixed ? c.mbA + kind : c.mbA;
+            if (kind == 2) {
+                const int mT = (c.topDouble && comp == 0) ? c.mbB - 1 : c.mbB;
+                if (mT >= 0) mbP = mT;
+            }
+            if (kind == 3 && c.topDouble && c.mbB >= 0) mbP = c.mbB;
+            int iA, al, be;
+            edge_params(p, mbP, cur, comp, iA, al, be);
+            w = (uint32_t)iA | ((uint32_t)al << 8) | ((uint32_t)be << 16);
+        }
+        *(uint32_t *)(out + kBsParams + 4 * (lane == 15 ? 0 : 1 + lane)) = w;
+    }
     for (int o = 16; o > 0; o >>= 1) mystop = min(mystop, __shfl_xor_sync(0xffffffffu, mystop, o));
     if (lane == 0 && mystop != 0xFFFFFFFFu) atomicMin(&pp->deblock_stop, mystop);
 }
@@ -1472,127 +1496,163 @@ __device__ __forceinline__ void filter_line(int *pv, int *qv, int bS, bool chrom
     qv[0] = nq0; qv[1] = nq1; qv[2] = nq2;
 }
 
+// Samples of one component around the MB pair being filtered, staged in
+// shared memory: sample (x, y) of the plane is base[(y - y0) * stride + (x - x0)].
+struct DbWin {
+    uint8_t *base;
+    int x0, y0, stride, size;  // size: bytes of the window
+};
+
+// Thresholds of one edge between MBs P and Q (8.7.2.2, 1314-1369).
+struct EdgeQ {
+    int iA, al, be;
+};
+
+__device__ __forceinline__ EdgeQ edge_q(const h264r_mb &P, const h264r_mb &Q, const h264r_slice &sq, int comp)
+{
+    int qPp = P.type == H264R_MB_IPCM ? 0 : P.qpy, qPq = Q.type == H264R_MB_IPCM ? 0 : Q.qpy;
+    if (comp) {
+        const int off = sq.chroma_qp_offset[comp - 1];
+        qPp = chroma_qp(qPp, off);
+        qPq = chroma_qp(qPq, off);
+    }
+    const int qPav = (qPp + qPq + 1) >> 1;
+    EdgeQ q;
+    q.iA = H264R_CLIP3(0, 51, qPav + sq.filter_offset_a);
+    q.al = kAlpha[q.iA];
+    q.be = kBeta[H264R_CLIP3(0, 51, qPav + sq.filter_offset_b)];
+    return q;
+}
+
 // One edge step, one line per active lane (8.7.1, 639-840).  comp: 0 luma,
-// 1 Cb, 2 Cr; k: line index of this lane; bs: its strength.
-__device__ __forceinline__ void edge_line(const PicDesc &p, int cur, int comp, int vertical, int e, int mbN, int leftMbEdge,
-                                          int fieldMode, int k, int bs)
+// 1 Cb, 2 Cr; (xP, yP): the MB's first sample of this component; k: line
+// index of this lane; bs: its strength; q: the edge's thresholds.
+__device__ __forceinline__ void edge_line(int xP, int yP, int comp, int vertical, int e, int fieldMode, int k, int bs,
+                                          const EdgeQ &q, const DbWin &w)
 {
     if (bs == 0) return;
-    const bool chroma = comp != 0;
-    uint8_t *plane = comp == 0 ? plane_y(p) : plane_c(p, comp - 1);
-    const int stride = chroma ? p.Wc : p.W;
     const int ddy = 1 + fieldMode;
-    int xI, yI, dyI;
-    mb_origin(p, cur, xI, yI, dyI);
-    int xP = chroma ? xI / 2 : xI, yP = chroma ? (yI + 1) / 2 : yI;
-    int xE = vertical ? e : k, yE = vertical ? k : e;
-    size_t qi[4], pi[4];
+    const int xE = vertical ? e : k, yE = vertical ? k : e;
+    int qi[4], pi[4];
     for (int i = 0; i < 4; i++) {
+        int qy, qx, py, px;
         if (vertical) {
-            qi[i] = (size_t)(yP + ddy * yE) * stride + (xP + xE + i);
-            pi[i] = (size_t)(yP + ddy * yE) * stride + (xP + xE - i - 1);
+            qy = py = yP + ddy * yE;
+            qx = xP + xE + i;
+            px = xP + xE - i - 1;
         } else {
-            qi[i] = (size_t)(yP + ddy * (yE + i) - (yE % 2)) * stride + (xP + xE);
-            pi[i] = (size_t)(yP + ddy * (yE - i - 1) - (yE % 2)) * stride + (xP + xE);
+            qy = yP + ddy * (yE + i) - (yE % 2);
+            py = yP + ddy * (yE - i - 1) - (yE % 2);
+            qx = px = xP + xE;
         }
+        qi[i] = (qy - w.y0) * w.stride + (qx - w.x0);
+        pi[i] = (py - w.y0) * w.stride + (px - w.x0);
+        // the window covers every sample an MBAFF edge can reach; a line that
+        // would leave it is not filtered (and shows as a parity difference)
+        if ((unsigned)qi[i] >= (unsigned)w.size || (unsigned)pi[i] >= (unsigned)w.size) return;
     }
-    // p-side MB (same rule as edge_bs)
-    int mbP = cur;
-    if (vertical) {
-        if (xE - 1 < 0 && mbN >= 0) mbP = leftMbEdge ? mbN + (yE % 2) : mbN;
-    } else {
-        if ((yE - 1) - (yE % 2) < 0 && mbN >= 0) mbP = mbN;
-    }
-    const h264r_mb P = p.mbs[mbP], Q = p.mbs[cur];
-    const h264r_slice sq = p.slices[min((uint32_t)Q.slice, p.num_slices - 1)];
-    int qPp, qPq;
-    if (!chroma) {
-        qPp = P.type == H264R_MB_IPCM ? 0 : P.qpy;
-        qPq = Q.type == H264R_MB_IPCM ? 0 : Q.qpy;
-    } else {
-        int off = sq.chroma_qp_offset[comp - 1];
-        qPp = chroma_qp(P.type == H264R_MB_IPCM ? 0 : P.qpy, off);
-        qPq = chroma_qp(Q.type == H264R_MB_IPCM ? 0 : Q.qpy, off);
-    }
-    int qPav = (qPp + qPq + 1) >> 1;
-    int indexA = H264R_CLIP3(0, 51, qPav + sq.filter_offset_a);
-    int indexB = H264R_CLIP3(0, 51, qPav + sq.filter_offset_b);
-    int alpha = kAlpha[indexA], beta = kBeta[indexB];
     int pv[4], qv[4];
     for (int i = 0; i < 4; i++) {
-        pv[i] = __ldcg(plane + pi[i]);
-        qv[i] = __ldcg(plane + qi[i]);
+        pv[i] = w.base[pi[i]];
+        qv[i] = w.base[qi[i]];
     }
-    filter_line(pv, qv, bs, chroma, indexA, alpha, beta);
+    filter_line(pv, qv, bs, comp != 0, q.iA, q.al, q.be);
     for (int i = 0; i < 3; i++) {
-        plane[qi[i]] = (uint8_t)qv[i];
-        plane[pi[i]] = (uint8_t)pv[i];
+        w.base[qi[i]] = (uint8_t)qv[i];
+        w.base[pi[i]] = (uint8_t)pv[i];
     }
 }
 
-// Deblock one MB with one warp: lanes 0..15 luma lines, 16..23 Cb, 24..31 Cr.
-__device__ void deblock_mb(const PicDesc &p, int cur)
+// Deblock one MB with one warp: lanes 0..15 luma lines, 16..23 Cb, 24..31 Cr,
+// on the samples staged in wl (luma) and wc[0..1] (Cb, Cr).  The p-side MB of
+// each edge follows the reference's rule (the neighbour when it is
+// available, the MB itself otherwise; alternate lines take the two MBs of a
+// field pair on a mixed left edge); its records and the thresholds are read
+// once per MB.
+__device__ void deblock_mb(const PicDesc &p, int cur, const DbWin &wl, const DbWin *wc)
 {
     const int lane = threadIdx.x & 31;
-    const EdgeCtl c = edge_ctl(p, cur);
     const uint8_t *bs = p.bs + (size_t)cur * kBsBytes;
     const uint32_t stop = p.deblock_stop;
     const bool luma = lane < 16;
     const int k = luma ? lane : (lane & 7);
     const int comp = luma ? 0 : (lane < 24 ? 1 : 2);
+    const DbWin &w = luma ? wl : wc[comp - 1];
+    // edge controls and thresholds precomputed by k_bs; the p-side MB of each
+    // edge follows the reference (for a frame MB under a field pair the first
+    // luma top edge takes the top field MB, mbAddrB - 1, the second and both
+    // chroma ones mbAddrB: H264PictureDeblockingFilterProcess.cpp:246-278,
+    // 400-445)
+    const uint32_t *prm = (const uint32_t *)(bs + kBsParams);
+    const uint32_t ctl = __ldcg(prm);
+    EdgeCtl c;
+    c.left = (ctl & kDbcLeft) != 0;
+    c.top = (ctl & kDbcTop) != 0;
+    c.internal = (ctl & kDbcInternal) != 0;
+    c.t8 = (ctl & kDbcT8) != 0;
+    c.field = (ctl & kDbcField) != 0;
+    c.leftMixed = (ctl & kDbcLeftMixed) != 0;
+    c.topDouble = (ctl & kDbcTopDouble) != 0;
+    auto unq = [](uint32_t v) -> EdgeQ { EdgeQ q; q.iA = v & 255; q.al = (v >> 8) & 255; q.be = (v >> 16) & 255; return q; };
+    const uint32_t *pc = prm + 1 + 5 * comp;
+    const EdgeQ qL = unq(__ldcg(pc + (c.leftMixed ? (k & 1) : 0))), qT = unq(__ldcg(pc + 2)), qT2 = unq(__ldcg(pc + 3)),
+                qI = unq(__ldcg(pc + 4));
+    // MB origin (mb_origin for MBAFF, from the pair index and the field flag)
+    const int pair = cur >> 1, x0 = (pair % p.wmb) * 16, y0 = (pair / p.wmb) * 32;
+    const int xI = x0, yI = c.field ? y0 + (cur & 1) : y0 + 16 * (cur & 1);
+    const int xP = luma ? xI : xI / 2, yP = luma ? yI : (yI + 1) / 2;
     // a step runs only when it comes before the reference's early return
     auto allowed = [&](int seq, int kk) -> bool { return stop_key(cur, seq, kk) < stop; };
     const int cseq = comp == 2 ? 1 : 0;  // Cr steps follow the Cb step of the same edge
     // ---- vertical edges
     if (luma) {
-        if (c.left && allowed(SEQ_LV0, k)) edge_line(p, cur, 0, 1, 0, c.mbA, c.leftMixed, c.field, k, bs[bs_lv(0, k)]);
+        if (c.left && allowed(SEQ_LV0, k)) edge_line(xP, yP, 0, 1, 0, c.field, k, bs[bs_lv(0, k)], qL, w);
         __syncwarp(0x0000FFFFu);
         if (c.internal) {
-            if (!c.t8 && allowed(SEQ_LV4, k)) edge_line(p, cur, 0, 1, 4, c.mbA, 0, c.field, k, bs[bs_lv(1, k)]);
+            if (!c.t8 && allowed(SEQ_LV4, k)) edge_line(xP, yP, 0, 1, 4, c.field, k, bs[bs_lv(1, k)], qI, w);
             __syncwarp(0x0000FFFFu);
-            if (allowed(SEQ_LV8, k)) edge_line(p, cur, 0, 1, 8, c.mbA, 0, c.field, k, bs[bs_lv(2, k)]);
+            if (allowed(SEQ_LV8, k)) edge_line(xP, yP, 0, 1, 8, c.field, k, bs[bs_lv(2, k)], qI, w);
             __syncwarp(0x0000FFFFu);
-            if (!c.t8 && allowed(SEQ_LV12, k)) edge_line(p, cur, 0, 1, 12, c.mbA, 0, c.field, k, bs[bs_lv(3, k)]);
+            if (!c.t8 && allowed(SEQ_LV12, k)) edge_line(xP, yP, 0, 1, 12, c.field, k, bs[bs_lv(3, k)], qI, w);
         }
     } else {
-        if (c.left && allowed(SEQ_CBV0 + cseq, k)) edge_line(p, cur, comp, 1, 0, c.mbA, c.leftMixed, c.field, k, bs[bs_cv(0, k)]);
+        if (c.left && allowed(SEQ_CBV0 + cseq, k)) edge_line(xP, yP, comp, 1, 0, c.field, k, bs[bs_cv(0, k)], qL, w);
         __syncwarp(0xFFFF0000u);
-        if (c.internal && allowed(SEQ_CBV4 + cseq, k)) edge_line(p, cur, comp, 1, 4, c.mbA, 0, c.field, k, bs[bs_cv(1, k)]);
+        if (c.internal && allowed(SEQ_CBV4 + cseq, k)) edge_line(xP, yP, comp, 1, 4, c.field, k, bs[bs_cv(1, k)], qI, w);
     }
     __syncwarp();
     // ---- horizontal edges
     if (luma) {
         if (c.top) {
             if (c.topDouble) {
-                if (allowed(SEQ_LH0, k)) edge_line(p, cur, 0, 0, 0, c.mbB - 1, 0, 1, k, bs[bs_lh(0, k)]);
+                if (allowed(SEQ_LH0, k)) edge_line(xP, yP, 0, 0, 0, 1, k, bs[bs_lh(0, k)], qT, w);
                 __syncwarp(0x0000FFFFu);
-                if (allowed(SEQ_LH0B, k)) edge_line(p, cur, 0, 0, 1, c.mbB, 0, 1, k, bs[kBsLumaTop2 + k]);
+                if (allowed(SEQ_LH0B, k)) edge_line(xP, yP, 0, 0, 1, 1, k, bs[kBsLumaTop2 + k], qT2, w);
             } else if (allowed(SEQ_LH0, k)) {
-                edge_line(p, cur, 0, 0, 0, c.mbB, 0, c.field, k, bs[bs_lh(0, k)]);
+                edge_line(xP, yP, 0, 0, 0, c.field, k, bs[bs_lh(0, k)], qT, w);
             }
         }
         __syncwarp(0x0000FFFFu);
         if (c.internal) {
-            if (!c.t8 && allowed(SEQ_LH4, k)) edge_line(p, cur, 0, 0, 4, c.mbB, 0, c.field, k, bs[bs_lh(1, k)]);
+            if (!c.t8 && allowed(SEQ_LH4, k)) edge_line(xP, yP, 0, 0, 4, c.field, k, bs[bs_lh(1, k)], qI, w);
             __syncwarp(0x0000FFFFu);
-            if (allowed(SEQ_LH8, k)) edge_line(p, cur, 0, 0, 8, c.mbB, 0, c.field, k, bs[bs_lh(2, k)]);
+            if (allowed(SEQ_LH8, k)) edge_line(xP, yP, 0, 0, 8, c.field, k, bs[bs_lh(2, k)], qI, w);
             __syncwarp(0x0000FFFFu);
-            if (!c.t8 && allowed(SEQ_LH12, k)) edge_line(p, cur, 0, 0, 12, c.mbB, 0, c.field, k, bs[bs_lh(3, k)]);
+            if (!c.t8 && allowed(SEQ_LH12, k)) edge_line(xP, yP, 0, 0, 12, c.field, k, bs[bs_lh(3, k)], qI, w);
         }
     } else {
         if (c.top) {
             if (c.topDouble) {
-                if (allowed(SEQ_CBH0 + cseq, k)) edge_line(p, cur, comp, 0, 0, c.mbB, 0, 1, k, bs[bs_ch(0, k)]);
+                if (allowed(SEQ_CBH0 + cseq, k)) edge_line(xP, yP, comp, 0, 0, 1, k, bs[bs_ch(0, k)], qT, w);
                 __syncwarp(0xFFFF0000u);
-                if (allowed(SEQ_CBH0B + cseq, k)) edge_line(p, cur, comp, 0, 1, c.mbB, 0, 1, k, bs[kBsChromaTop2 + k]);
+                if (allowed(SEQ_CBH0B + cseq, k)) edge_line(xP, yP, comp, 0, 1, 1, k, bs[kBsChromaTop2 + k], qT2, w);
             } else if (allowed(SEQ_CBH0 + cseq, k)) {
-                edge_line(p, cur, comp, 0, 0, c.mbB, 0, c.field, k, bs[bs_ch(0, k)]);
+                edge_line(xP, yP, comp, 0, 0, c.field, k, bs[bs_ch(0, k)], qT, w);
             }
         }
         __syncwarp(0xFFFF0000u);
-        if (c.internal && allowed(SEQ_CBH4 + cseq, k)) edge_line(p, cur, comp, 0, 4, c.mbB, 0, c.field, k, bs[bs_ch(1, k)]);
+        if (c.internal && allowed(SEQ_CBH4 + cseq, k)) edge_line(xP, yP, comp, 0, 4, c.field, k, bs[bs_ch(1, k)], qI, w);
     }
-    __threadfence_block();
     __syncwarp();
 }
 
@@ -1885,7 +1945,8 @@ __device__ void deblock_pair_chroma(const PicDesc &p, int pair, DbChromaSmem &s,
     }
 }
 
-__global__ void __launch_bounds__(32) k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st)
+// 28 resident warps per SM (registers capped at 72)
+__global__ void __launch_bounds__(32, 28) k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st)
 {
     __shared__ uint32_t s_row;
     const int lane = threadIdx.x;
@@ -1907,16 +1968,49 @@ __global__ void __launch_bounds__(32) k_deblock(const PicDesc *__restrict__ pics
         else deblock_pair_chroma(p, unit >> 1, pair_smem.c, st);
         return;
     }
+    // MBAFF: one warp per MB-pair row.  Each pair is filtered on a shared-
+    // memory copy of every sample its edges can reach: luma rows y0-8..y0+31
+    // and columns x0-4..x0+15 (field edges reach four field rows, eight frame
+    // rows, up), chroma rows y0/2-8..y0/2+15 and columns x0/2-4..x0/2+7.  Once
+    // the row above is two pairs ahead, all of it is either this warp's or
+    // final, so the whole window is loaded after the wait and written back
+    // before the progress is published.
+    __shared__ __align__(16) uint8_t tl[40 * 20];
+    __shared__ __align__(16) uint8_t tc[2][24 * 12];
     const int row = unit;
     const int uw = (int)p.units_w;
-    const int per = p.mbaff ? 2 : 1;
     int *prog = p.progress + p.units_h;
     const uint32_t stop_mb = p.deblock_stop >> 10;
+    uint8_t *Y = plane_y(p);
     for (int u = 0; u < uw; u++) {
         if (row > 0 && !wait_progress(st, prog + row - 1, min(u + 2, uw))) return;
-        for (int k = 0; k < per; k++) {
-            int addr = p.mbaff ? 2 * (row * uw + u) + k : row * uw + u;
-            if ((uint32_t)addr <= stop_mb) deblock_mb(p, addr);
+        const int x0 = u * 16, y0 = row * 32, xc0 = u * 8, yc0 = row * 16;
+        // 200 luma words (40 rows x 5) then 2 x 72 chroma words (24 rows x 3)
+        for (int i = lane; i < 344; i += 32) {
+            if (i < 200) {
+                const int r = i / 5, q = i % 5, y = y0 - 8 + r, x = x0 - 4 + 4 * q;
+                if (y >= 0 && x >= 0) ((uint32_t *)tl)[i] = __ldcg((const uint32_t *)(Y + (size_t)y * p.W + x));
+            } else {
+                const int j = i - 200, pl = j / 72, r = (j % 72) / 3, q = j % 3, y = yc0 - 8 + r, x = xc0 - 4 + 4 * q;
+                if (y >= 0 && x >= 0) ((uint32_t *)tc[pl])[j % 72] = __ldcg((const uint32_t *)(plane_c(p, pl) + (size_t)y * p.Wc + x));
+            }
+        }
+        __syncwarp();
+        const DbWin wl = {tl, x0 - 4, y0 - 8, 20, 40 * 20};
+        const DbWin wc[2] = {{tc[0], xc0 - 4, yc0 - 8, 12, 24 * 12}, {tc[1], xc0 - 4, yc0 - 8, 12, 24 * 12}};
+        for (int k = 0; k < 2; k++) {
+            const int addr = 2 * (row * uw + u) + k;
+            if ((uint32_t)addr <= stop_mb) deblock_mb(p, addr, wl, wc);
+        }
+        __syncwarp();
+        for (int i = lane; i < 344; i += 32) {
+            if (i < 200) {
+                const int r = i / 5, q = i % 5, y = y0 - 8 + r, x = x0 - 4 + 4 * q;
+                if (y >= 0 && x >= 0) *(uint32_t *)(Y + (size_t)y * p.W + x) = ((const uint32_t *)tl)[i];
+            } else {
+                const int j = i - 200, pl = j / 72, r = (j % 72) / 3, q = j % 3, y = yc0 - 8 + r, x = xc0 - 4 + 4 * q;
+                if (y >= 0 && x >= 0) *(uint32_t *)(plane_c(p, pl) + (size_t)y * p.Wc + x) = ((const uint32_t *)tc[pl])[j % 72];
+            }
         }
         __syncwarp();
         if (lane == 0) st_release(prog + row, u + 1);
