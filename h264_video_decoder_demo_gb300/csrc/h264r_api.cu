@@ -534,7 +534,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
     const uint64_t desc_bytes = align_up(sizeof(PicDesc) * n, kAlign);
     const uint64_t ticket_off = desc_bytes;
     const uint64_t prog_off = ticket_off + kAlign;
-    const uint64_t total = prog_off + align_up(8 * rows + 8, kAlign);
+    const uint64_t total = prog_off + align_up(12 * rows + 8, kAlign);
     int rc = ensure(ctx, &b.host, &b.host_cap, total, true);
     if (rc) return rc;
     rc = ensure(ctx, &b.dev, &b.dev_cap, total, false);
@@ -591,7 +591,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
         p.deblock_stop = 0xFFFFFFFFu;
         mb_base += pic->num_mbs;
         row_base += p.units_h;
-        prog += 2 * p.units_h;
+        prog += 3 * p.units_h;
     }
     CUDA_OR(ctx, cudaMemcpyAsync(b.dev, b.host, total, cudaMemcpyHostToDevice, cs));
     LaunchState st;

@@ -80,7 +80,7 @@ struct PicDesc {
     int flat_scaling;        // every scaling list is flat 16
     uint8_t *bs;             // deblocking strengths, kBsBytes per MB
     int16_t *ires;           // intra MBs' residuals, 384 per MB (null: no intra MB)
-    int *progress;           // per unit row progress counters (2 * units_h)
+    int *progress;           // per unit row progress counters (3 * units_h)
     uint32_t mb_base;        // first global MB index of this picture in the batch
     uint32_t row_base;       // first global unit row of this picture in the batch
     uint32_t units_w, units_h;  // wavefront grid: MBs (or MB pairs) per row, rows
@@ -91,7 +91,7 @@ struct PicDesc {
 // Deblocking tickets of a picture: frame pictures give one ticket to the
 // luma and one to the chroma warp of every pair of MB rows; MBAFF pictures
 // one per MB-pair row.
-__host__ __device__ inline uint32_t deblock_units(int mbaff, uint32_t units_h) { return mbaff ? units_h : 2u * ((units_h + 1u) / 2u); }
+__host__ __device__ inline uint32_t deblock_units(int mbaff, uint32_t units_h) { return mbaff ? 2u * units_h : 2u * ((units_h + 1u) / 2u); }
 
 // Engine-wide device state for one launch.
 struct LaunchState {

@@ -94,6 +94,30 @@ __device__ bool wait_progress(const LaunchState &st, const int *flag, int target
     return ok;
 }
 
+// As wait_progress, with the last value seen cached by the caller: no load
+// when it already satisfies the target.
+__device__ __forceinline__ bool db_wait(const LaunchState &st, const int *flag, int target, int &seen)
+{
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0 && seen < target) {
+        unsigned long long n = 0;
+        while ((seen = ld_acquire(flag)) < target) {
+            if (++n > st.spin_limit) {
+                set_error(st, H264R_ERR_DEVICE_TIMEOUT);
+                ok = 0;
+                break;
+            }
+            if (n > 64) {
+                if (*(volatile int *)st.error != 0) { ok = 0; break; }
+                __nanosleep(32);
+            }
+        }
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __syncwarp();
+    return ok != 0;
+}
+
 // ======================================================================
 // Residual of one macroblock (8.5), whole warp
 // ======================================================================
@@ -1563,97 +1587,266 @@ __device__ __forceinline__ void edge_line(int xP, int yP, int comp, int vertical
     }
 }
 
-// Deblock one MB with one warp: lanes 0..15 luma lines, 16..23 Cb, 24..31 Cr,
-// on the samples staged in wl (luma) and wc[0..1] (Cb, Cr).  The p-side MB of
-// each edge follows the reference's rule (the neighbour when it is
-// available, the MB itself otherwise; alternate lines take the two MBs of a
-// field pair on a mixed left edge); its records and the thresholds are read
-// once per MB.
-__device__ void deblock_mb(const PicDesc &p, int cur, const DbWin &wl, const DbWin *wc)
+// ---------------------------------------------------------------- MBAFF pictures
+// One warp per MB-pair row and plane group: luma (even ticket), or Cb and Cr
+// together (odd ticket); progress of pair row r is published per plane,
+// luma at index 2r + 1, chroma at 2r.  Lanes 0..15 (or 0..7 / 8..15 per
+// chroma plane) take the lines of the pair's top MB, lanes 16..31 those of
+// the bottom MB.  The reference filters a pair as top MB (vertical, then
+// horizontal edges), then bottom MB; the bottom MB's vertical edges touch
+// only its own lines (rows 16..31 of a frame pair, the odd rows of a field
+// pair) and the top MB's horizontal edges never do, so the vertical edges of
+// both MBs run together, before the wait for the row above (they reach no
+// row above the pair).  The horizontal edges of a field pair's two MBs touch
+// opposite parities and run together too; a frame pair's bottom MB follows
+// its top MB on the same lanes.  Within one MB a lane owns a line (vertical
+// edges) or a column (horizontal edges), so the edge steps of a direction
+// need no barrier.  Samples are filtered on a window in shared memory
+// (DbWin): luma columns x0-4..x0+15 and rows y0-8..y0+31, chroma x0/2-4..
+// x0/2+7 and y0/2-8..y0/2+15 per plane.  The window slides right one pair
+// at a time: its first four columns are the previous window's last four
+// (final once the previous pair is done), the pair's own rows are fetched
+// one pair ahead (nothing in this kernel writes them before the pair), and
+// only the eight rows above are loaded after the wait.
+
+// Edge controls, thresholds and strengths of one MB for one lane, from k_bs.
+struct MbaffEdges {
+    uint32_t ctl;                     // kDbc* bits
+    uint32_t qL0, qL1, qT, qT2, qI;   // thresholds of the lane's component (iA | alpha << 8 | beta << 16)
+    uint32_t bv, bh, b2;              // the lane's strengths: vertical edge e (byte e), horizontal edge e, second top edge
+};
+
+__device__ __forceinline__ EdgeQ unq(uint32_t v)
 {
-    const int lane = threadIdx.x & 31;
+    EdgeQ q;
+    q.iA = v & 255;
+    q.al = (v >> 8) & 255;
+    q.be = (v >> 16) & 255;
+    return q;
+}
+
+// comp: 0 luma, 1 Cb, 2 Cr; k: line (or column) of the lane within the MB
+__device__ __forceinline__ void mbaff_fetch(const PicDesc &p, int cur, int comp, int k, MbaffEdges &m)
+{
     const uint8_t *bs = p.bs + (size_t)cur * kBsBytes;
-    const uint32_t stop = p.deblock_stop;
-    const bool luma = lane < 16;
-    const int k = luma ? lane : (lane & 7);
-    const int comp = luma ? 0 : (lane < 24 ? 1 : 2);
-    const DbWin &w = luma ? wl : wc[comp - 1];
-    // edge controls and thresholds precomputed by k_bs; the p-side MB of each
-    // edge follows the reference (for a frame MB under a field pair the first
-    // luma top edge takes the top field MB, mbAddrB - 1, the second and both
-    // chroma ones mbAddrB: H264PictureDeblockingFilterProcess.cpp:246-278,
-    // 400-445)
     const uint32_t *prm = (const uint32_t *)(bs + kBsParams);
-    const uint32_t ctl = __ldcg(prm);
-    EdgeCtl c;
-    c.left = (ctl & kDbcLeft) != 0;
-    c.top = (ctl & kDbcTop) != 0;
-    c.internal = (ctl & kDbcInternal) != 0;
-    c.t8 = (ctl & kDbcT8) != 0;
-    c.field = (ctl & kDbcField) != 0;
-    c.leftMixed = (ctl & kDbcLeftMixed) != 0;
-    c.topDouble = (ctl & kDbcTopDouble) != 0;
-    auto unq = [](uint32_t v) -> EdgeQ { EdgeQ q; q.iA = v & 255; q.al = (v >> 8) & 255; q.be = (v >> 16) & 255; return q; };
     const uint32_t *pc = prm + 1 + 5 * comp;
-    const EdgeQ qL = unq(__ldcg(pc + (c.leftMixed ? (k & 1) : 0))), qT = unq(__ldcg(pc + 2)), qT2 = unq(__ldcg(pc + 3)),
-                qI = unq(__ldcg(pc + 4));
-    // MB origin (mb_origin for MBAFF, from the pair index and the field flag)
-    const int pair = cur >> 1, x0 = (pair % p.wmb) * 16, y0 = (pair / p.wmb) * 32;
-    const int xI = x0, yI = c.field ? y0 + (cur & 1) : y0 + 16 * (cur & 1);
-    const int xP = luma ? xI : xI / 2, yP = luma ? yI : (yI + 1) / 2;
-    // a step runs only when it comes before the reference's early return
-    auto allowed = [&](int seq, int kk) -> bool { return stop_key(cur, seq, kk) < stop; };
-    const int cseq = comp == 2 ? 1 : 0;  // Cr steps follow the Cb step of the same edge
-    // ---- vertical edges
-    if (luma) {
-        if (c.left && allowed(SEQ_LV0, k)) edge_line(xP, yP, 0, 1, 0, c.field, k, bs[bs_lv(0, k)], qL, w);
-        __syncwarp(0x0000FFFFu);
-        if (c.internal) {
-            if (!c.t8 && allowed(SEQ_LV4, k)) edge_line(xP, yP, 0, 1, 4, c.field, k, bs[bs_lv(1, k)], qI, w);
-            __syncwarp(0x0000FFFFu);
-            if (allowed(SEQ_LV8, k)) edge_line(xP, yP, 0, 1, 8, c.field, k, bs[bs_lv(2, k)], qI, w);
-            __syncwarp(0x0000FFFFu);
-            if (!c.t8 && allowed(SEQ_LV12, k)) edge_line(xP, yP, 0, 1, 12, c.field, k, bs[bs_lv(3, k)], qI, w);
-        }
+    m.ctl = __ldcg(prm);
+    m.qL0 = __ldcg(pc);
+    m.qL1 = __ldcg(pc + 1);
+    m.qT = __ldcg(pc + 2);
+    m.qT2 = __ldcg(pc + 3);
+    m.qI = __ldcg(pc + 4);
+    if (comp == 0) {
+        m.bv = __ldcg((const uint32_t *)(bs + bs_lv(0, k)));
+        m.bh = __ldcg((const uint32_t *)(bs + bs_lh(0, k)));
+        m.b2 = __ldcg(bs + kBsLumaTop2 + k);
     } else {
-        if (c.left && allowed(SEQ_CBV0 + cseq, k)) edge_line(xP, yP, comp, 1, 0, c.field, k, bs[bs_cv(0, k)], qL, w);
-        __syncwarp(0xFFFF0000u);
-        if (c.internal && allowed(SEQ_CBV4 + cseq, k)) edge_line(xP, yP, comp, 1, 4, c.field, k, bs[bs_cv(1, k)], qI, w);
+        m.bv = __ldcg((const uint16_t *)(bs + bs_cv(0, k)));
+        m.bh = __ldcg((const uint16_t *)(bs + bs_ch(0, k)));
+        m.b2 = __ldcg(bs + kBsChromaTop2 + k);
     }
-    __syncwarp();
-    // ---- horizontal edges
-    if (luma) {
-        if (c.top) {
-            if (c.topDouble) {
-                if (allowed(SEQ_LH0, k)) edge_line(xP, yP, 0, 0, 0, 1, k, bs[bs_lh(0, k)], qT, w);
-                __syncwarp(0x0000FFFFu);
-                if (allowed(SEQ_LH0B, k)) edge_line(xP, yP, 0, 0, 1, 1, k, bs[kBsLumaTop2 + k], qT2, w);
-            } else if (allowed(SEQ_LH0, k)) {
-                edge_line(xP, yP, 0, 0, 0, c.field, k, bs[bs_lh(0, k)], qT, w);
-            }
+    // a step at or after the reference's early return (a failed bS
+    // derivation) is not filtered
+    const uint32_t stop = p.deblock_stop;
+    if ((uint32_t)cur >= (stop >> 10)) {
+        const int cseq = comp == 2 ? 1 : 0;
+        for (int e = 0; e < 4; e++) {
+            const int sv = comp ? (e == 0 ? SEQ_CBV0 : SEQ_CBV4) + cseq : SEQ_LV0 + e;
+            const int sh = comp ? (e == 0 ? SEQ_CBH0 : SEQ_CBH4) + cseq : (e == 0 ? SEQ_LH0 : SEQ_LH4 + e - 1);
+            if (stop_key(cur, sv, k) >= stop) m.bv &= ~(0xFFu << (8 * e));
+            if (stop_key(cur, sh, k) >= stop) m.bh &= ~(0xFFu << (8 * e));
         }
-        __syncwarp(0x0000FFFFu);
-        if (c.internal) {
-            if (!c.t8 && allowed(SEQ_LH4, k)) edge_line(xP, yP, 0, 0, 4, c.field, k, bs[bs_lh(1, k)], qI, w);
-            __syncwarp(0x0000FFFFu);
-            if (allowed(SEQ_LH8, k)) edge_line(xP, yP, 0, 0, 8, c.field, k, bs[bs_lh(2, k)], qI, w);
-            __syncwarp(0x0000FFFFu);
-            if (!c.t8 && allowed(SEQ_LH12, k)) edge_line(xP, yP, 0, 0, 12, c.field, k, bs[bs_lh(3, k)], qI, w);
-        }
-    } else {
-        if (c.top) {
-            if (c.topDouble) {
-                if (allowed(SEQ_CBH0 + cseq, k)) edge_line(xP, yP, comp, 0, 0, 1, k, bs[bs_ch(0, k)], qT, w);
-                __syncwarp(0xFFFF0000u);
-                if (allowed(SEQ_CBH0B + cseq, k)) edge_line(xP, yP, comp, 0, 1, 1, k, bs[kBsChromaTop2 + k], qT2, w);
-            } else if (allowed(SEQ_CBH0 + cseq, k)) {
-                edge_line(xP, yP, comp, 0, 0, c.field, k, bs[bs_ch(0, k)], qT, w);
-            }
-        }
-        __syncwarp(0xFFFF0000u);
-        if (c.internal && allowed(SEQ_CBH4 + cseq, k)) edge_line(xP, yP, comp, 0, 4, c.field, k, bs[bs_ch(1, k)], qI, w);
+        if (stop_key(cur, comp ? SEQ_CBH0B + cseq : SEQ_LH0B, k) >= stop) m.b2 = 0;
     }
-    __syncwarp();
+}
+
+__device__ __forceinline__ MbaffEdges mbaff_shfl(const MbaffEdges &m, int src)
+{
+    MbaffEdges r;
+    r.ctl = __shfl_sync(0xffffffffu, m.ctl, src);
+    r.qL0 = __shfl_sync(0xffffffffu, m.qL0, src);
+    r.qL1 = __shfl_sync(0xffffffffu, m.qL1, src);
+    r.qT = __shfl_sync(0xffffffffu, m.qT, src);
+    r.qT2 = __shfl_sync(0xffffffffu, m.qT2, src);
+    r.qI = __shfl_sync(0xffffffffu, m.qI, src);
+    r.bv = __shfl_sync(0xffffffffu, m.bv, src);
+    r.bh = __shfl_sync(0xffffffffu, m.bh, src);
+    r.b2 = __shfl_sync(0xffffffffu, m.b2, src);
+    return r;
+}
+
+// Edges of one direction of one MB on the lane's line (vertical) or column
+// (horizontal).  (xP, yP): the MB's first sample of the component.  The
+// p-side MB of each edge is the one k_bs chose: alternate lines of a mixed
+// left edge take the two MBs of the left field pair; a frame MB under a
+// field pair filters its top edge twice, as a top-field and a bottom-field
+// edge (Deblocking_filter_process, H264PictureDeblockingFilterProcess.cpp:
+// 76-160, 246-278).
+template <bool CHROMA>
+__device__ __forceinline__ void mbaff_edges_v(int xP, int yP, int k, const MbaffEdges &m, const DbWin &w)
+{
+    const int comp = CHROMA ? 1 : 0;  // only the filter kind matters to edge_line
+    const int field = (m.ctl & kDbcField) != 0;
+    if (m.ctl & kDbcLeft)
+        edge_line(xP, yP, comp, 1, 0, field, k, m.bv & 255, unq((m.ctl & kDbcLeftMixed) && (k & 1) ? m.qL1 : m.qL0), w);
+    if (m.ctl & kDbcInternal) {
+        const EdgeQ qI = unq(m.qI);
+#pragma unroll 1
+        for (int e = 1; e < (CHROMA ? 2 : 4); e++)
+            if (CHROMA || e == 2 || !(m.ctl & kDbcT8)) edge_line(xP, yP, comp, 1, 4 * e, field, k, (m.bv >> (8 * e)) & 255, qI, w);
+    }
+}
+
+template <bool CHROMA>
+__device__ __forceinline__ void mbaff_edges_h(int xP, int yP, int k, const MbaffEdges &m, const DbWin &w)
+{
+    const int comp = CHROMA ? 1 : 0;
+    const int field = (m.ctl & kDbcField) != 0;
+    if (m.ctl & kDbcTop) {
+        if (m.ctl & kDbcTopDouble) {
+            edge_line(xP, yP, comp, 0, 0, 1, k, m.bh & 255, unq(m.qT), w);
+            edge_line(xP, yP, comp, 0, 1, 1, k, m.b2, unq(m.qT2), w);
+        } else {
+            edge_line(xP, yP, comp, 0, 0, field, k, m.bh & 255, unq(m.qT), w);
+        }
+    }
+    if (m.ctl & kDbcInternal) {
+        const EdgeQ qI = unq(m.qI);
+#pragma unroll 1
+        for (int e = 1; e < (CHROMA ? 2 : 4); e++)
+            if (CHROMA || e == 2 || !(m.ctl & kDbcT8)) edge_line(xP, yP, comp, 0, 4 * e, field, k, (m.bh >> (8 * e)) & 255, qI, w);
+    }
+}
+
+// Luma of MB-pair row `row`; win: 200 words (40 rows of 5).
+__device__ void mbaff_luma_row(const PicDesc &p, int row, uint32_t *win, const LaunchState &st)
+{
+    const int lane = threadIdx.x & 31, h = lane >> 4, k = lane & 15;
+    const int uw = (int)p.units_w, W = p.W, y0 = row * 32;
+    int *prog = p.progress + p.units_h;
+    uint8_t *Y = plane_y(p);
+    const DbWin w0 = {(uint8_t *)win, 0, y0 - 8, 20, 40 * 20};
+    int seen = 0;
+    uint4 nown;  // row y0 + lane of the next pair
+    MbaffEdges nm;
+    auto fetch = [&](int u) {
+        nown = __ldcg((const uint4 *)(Y + (size_t)(y0 + lane) * W + u * 16));
+        mbaff_fetch(p, 2 * (row * uw + u) + h, 0, k, nm);
+    };
+    fetch(0);
+    for (int u = 0; u < uw; u++) {
+        const int x0 = u * 16;
+        const MbaffEdges m = nm;
+        uint32_t *wr = win + (8 + lane) * 5;  // the lane's own row
+        if (u > 0) {
+            wr[0] = wr[4];
+            if (lane < 8) win[lane * 5] = win[lane * 5 + 4];
+        }
+        wr[1] = nown.x;
+        wr[2] = nown.y;
+        wr[3] = nown.z;
+        wr[4] = nown.w;
+        __syncwarp();
+        if (u + 1 < uw) fetch(u + 1);
+        DbWin w = w0;
+        w.x0 = x0 - 4;
+        const int field = (m.ctl & kDbcField) != 0;
+        mbaff_edges_v<false>(x0, field ? y0 + h : y0 + 16 * h, k, m, w);
+        // the row above is final once its warp is two pairs ahead
+        if (row > 0 && !db_wait(st, prog + 2 * row - 1, min(u + 2, uw), seen)) return;
+        if (row > 0 && lane < 8) {
+            const uint4 t = __ldcg((const uint4 *)(Y + (size_t)(y0 - 8 + lane) * W + x0));
+            uint32_t *wt = win + lane * 5;
+            wt[1] = t.x;
+            wt[2] = t.y;
+            wt[3] = t.z;
+            wt[4] = t.w;
+        }
+        const MbaffEdges mb = mbaff_shfl(m, lane | 16);  // the bottom MB's, for a frame pair
+        __syncwarp();
+        if (field) mbaff_edges_h<false>(x0, y0 + h, k, m, w);
+        else if (h == 0) {
+            mbaff_edges_h<false>(x0, y0, k, m, w);
+            mbaff_edges_h<false>(x0, y0 + 16, k, mb, w);
+        }
+        __syncwarp();
+        // rows y0-6..y0+31 (the top edges change at most three field rows up)
+        for (int r = lane + 2; r < 40; r += 32) {
+            const int y = y0 - 8 + r;
+            if (y < 0) continue;
+            const uint32_t *s = win + r * 5;
+            uint8_t *d = Y + (size_t)y * W + x0;
+            *(uint4 *)d = make_uint4(s[1], s[2], s[3], s[4]);
+            if (x0 > 0) *(uint32_t *)(d - 4) = s[0];
+        }
+        __syncwarp();
+        if (lane == 0) st_release(prog + 2 * row + 1, u + 1);
+    }
+}
+
+// Cb and Cr of MB-pair row `row`; win: 2 x 72 words (24 rows of 3 per plane).
+__device__ void mbaff_chroma_row(const PicDesc &p, int row, uint32_t *win, const LaunchState &st)
+{
+    const int lane = threadIdx.x & 31, h = lane >> 4, pl = (lane >> 3) & 1, k = lane & 7;
+    const int uw = (int)p.units_w, Wc = p.Wc, yc0 = row * 16;
+    int *prog = p.progress + p.units_h;
+    // staging lanes: plane sp, row 8 + sr of the window (and sr when sr < 8)
+    const int sp = lane >> 4, sr = lane & 15;
+    uint8_t *Cs = plane_c(p, sp);
+    const DbWin w0 = {(uint8_t *)(win + 72 * pl), 0, yc0 - 8, 12, 24 * 12};
+    int seen = 0;
+    uint2 nown;
+    MbaffEdges nm;
+    auto fetch = [&](int u) {
+        nown = __ldcg((const uint2 *)(Cs + (size_t)(yc0 + sr) * Wc + u * 8));
+        mbaff_fetch(p, 2 * (row * uw + u) + h, 1 + pl, k, nm);
+    };
+    fetch(0);
+    for (int u = 0; u < uw; u++) {
+        const int xc0 = u * 8;
+        const MbaffEdges m = nm;
+        uint32_t *ws = win + 72 * sp;
+        uint32_t *wr = ws + (8 + sr) * 3;
+        if (u > 0) {
+            wr[0] = wr[2];
+            if (sr < 8) ws[sr * 3] = ws[sr * 3 + 2];
+        }
+        wr[1] = nown.x;
+        wr[2] = nown.y;
+        __syncwarp();
+        if (u + 1 < uw) fetch(u + 1);
+        DbWin w = w0;
+        w.x0 = xc0 - 4;
+        const int field = (m.ctl & kDbcField) != 0;
+        // (yI + 1) / 2 of the MB's first luma row yI
+        mbaff_edges_v<true>(xc0, field ? yc0 + h : yc0 + 8 * h, k, m, w);
+        if (row > 0 && !db_wait(st, prog + 2 * row - 2, min(u + 2, uw), seen)) return;
+        if (row > 0 && sr < 8) {
+            const uint2 t = __ldcg((const uint2 *)(Cs + (size_t)(yc0 - 8 + sr) * Wc + xc0));
+            ws[sr * 3 + 1] = t.x;
+            ws[sr * 3 + 2] = t.y;
+        }
+        const MbaffEdges mb = mbaff_shfl(m, lane | 16);
+        __syncwarp();
+        if (field) mbaff_edges_h<true>(xc0, yc0 + h, k, m, w);
+        else if (h == 0) {
+            mbaff_edges_h<true>(xc0, yc0, k, m, w);
+            mbaff_edges_h<true>(xc0, yc0 + 8, k, mb, w);
+        }
+        __syncwarp();
+        // rows yc0-4..yc0+15 of both planes (chroma edges change one row on each side)
+        for (int i = lane; i < 40; i += 32) {
+            const int q = i / 20, r = 4 + i % 20, y = yc0 - 8 + r;
+            if (y < 0) continue;
+            const uint32_t *s = win + 72 * q + r * 3;
+            uint8_t *d = plane_c(p, q) + (size_t)y * Wc + xc0;
+            *(uint2 *)d = make_uint2(s[1], s[2]);
+            if (xc0 > 0) *(uint32_t *)(d - 4) = s[0];
+        }
+        __syncwarp();
+        if (lane == 0) st_release(prog + 2 * row, u + 1);
+    }
 }
 
 // ---------------------------------------------------------------- frame fast path
@@ -1737,29 +1930,6 @@ __device__ __forceinline__ void db_chroma(int (&v)[N], int bS, uint32_t prm)
     const int delta = H264R_CLIP3(-tc, tc, (((q0 - p0) << 2) + (p1 - q1) + 4) >> 3);
     v[Q - 1] = clip1(p0 + delta);
     v[Q] = clip1(q0 - delta);
-}
-
-// Lane 0 polls the row above only when the last value it saw is behind.
-__device__ __forceinline__ bool db_wait(const LaunchState &st, const int *flag, int target, int &seen)
-{
-    int ok = 1;
-    if ((threadIdx.x & 31) == 0 && seen < target) {
-        unsigned long long n = 0;
-        while ((seen = ld_acquire(flag)) < target) {
-            if (++n > st.spin_limit) {
-                set_error(st, H264R_ERR_DEVICE_TIMEOUT);
-                ok = 0;
-                break;
-            }
-            if (n > 64) {
-                if (*(volatile int *)st.error != 0) { ok = 0; break; }
-                __nanosleep(32);
-            }
-        }
-    }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    __syncwarp();
-    return ok != 0;
 }
 
 __device__ void deblock_pair_luma(const PicDesc &p, int pair, DbLumaSmem &s, const LaunchState &st)
@@ -1958,63 +2128,21 @@ __global__ void __launch_bounds__(32, 28) k_deblock(const PicDesc *__restrict__ 
     const PicDesc p = pics[pi];
     if (!p.deblock) return;
     const int unit = (int)(g - p.db_base);
+    __shared__ union {
+        DbLumaSmem l;
+        DbChromaSmem c;
+        uint32_t ml[200];
+        uint32_t mc[144];
+    } db_smem;
     if (!p.mbaff) {
         // even tickets: luma of MB-row pair unit/2; odd: its chroma
-        __shared__ union {
-            DbLumaSmem l;
-            DbChromaSmem c;
-        } pair_smem;
-        if ((unit & 1) == 0) deblock_pair_luma(p, unit >> 1, pair_smem.l, st);
-        else deblock_pair_chroma(p, unit >> 1, pair_smem.c, st);
+        if ((unit & 1) == 0) deblock_pair_luma(p, unit >> 1, db_smem.l, st);
+        else deblock_pair_chroma(p, unit >> 1, db_smem.c, st);
         return;
     }
-    // MBAFF: one warp per MB-pair row.  Each pair is filtered on a shared-
-    // memory copy of every sample its edges can reach: luma rows y0-8..y0+31
-    // and columns x0-4..x0+15 (field edges reach four field rows, eight frame
-    // rows, up), chroma rows y0/2-8..y0/2+15 and columns x0/2-4..x0/2+7.  Once
-    // the row above is two pairs ahead, all of it is either this warp's or
-    // final, so the whole window is loaded after the wait and written back
-    // before the progress is published.
-    __shared__ __align__(16) uint8_t tl[40 * 20];
-    __shared__ __align__(16) uint8_t tc[2][24 * 12];
-    const int row = unit;
-    const int uw = (int)p.units_w;
-    int *prog = p.progress + p.units_h;
-    const uint32_t stop_mb = p.deblock_stop >> 10;
-    uint8_t *Y = plane_y(p);
-    for (int u = 0; u < uw; u++) {
-        if (row > 0 && !wait_progress(st, prog + row - 1, min(u + 2, uw))) return;
-        const int x0 = u * 16, y0 = row * 32, xc0 = u * 8, yc0 = row * 16;
-        // 200 luma words (40 rows x 5) then 2 x 72 chroma words (24 rows x 3)
-        for (int i = lane; i < 344; i += 32) {
-            if (i < 200) {
-                const int r = i / 5, q = i % 5, y = y0 - 8 + r, x = x0 - 4 + 4 * q;
-                if (y >= 0 && x >= 0) ((uint32_t *)tl)[i] = __ldcg((const uint32_t *)(Y + (size_t)y * p.W + x));
-            } else {
-                const int j = i - 200, pl = j / 72, r = (j % 72) / 3, q = j % 3, y = yc0 - 8 + r, x = xc0 - 4 + 4 * q;
-                if (y >= 0 && x >= 0) ((uint32_t *)tc[pl])[j % 72] = __ldcg((const uint32_t *)(plane_c(p, pl) + (size_t)y * p.Wc + x));
-            }
-        }
-        __syncwarp();
-        const DbWin wl = {tl, x0 - 4, y0 - 8, 20, 40 * 20};
-        const DbWin wc[2] = {{tc[0], xc0 - 4, yc0 - 8, 12, 24 * 12}, {tc[1], xc0 - 4, yc0 - 8, 12, 24 * 12}};
-        for (int k = 0; k < 2; k++) {
-            const int addr = 2 * (row * uw + u) + k;
-            if ((uint32_t)addr <= stop_mb) deblock_mb(p, addr, wl, wc);
-        }
-        __syncwarp();
-        for (int i = lane; i < 344; i += 32) {
-            if (i < 200) {
-                const int r = i / 5, q = i % 5, y = y0 - 8 + r, x = x0 - 4 + 4 * q;
-                if (y >= 0 && x >= 0) *(uint32_t *)(Y + (size_t)y * p.W + x) = ((const uint32_t *)tl)[i];
-            } else {
-                const int j = i - 200, pl = j / 72, r = (j % 72) / 3, q = j % 3, y = yc0 - 8 + r, x = xc0 - 4 + 4 * q;
-                if (y >= 0 && x >= 0) *(uint32_t *)(plane_c(p, pl) + (size_t)y * p.Wc + x) = ((const uint32_t *)tc[pl])[j % 72];
-            }
-        }
-        __syncwarp();
-        if (lane == 0) st_release(prog + row, u + 1);
-    }
+    // MBAFF: even tickets luma of pair row unit/2, odd ones its chroma
+    if ((unit & 1) == 0) mbaff_luma_row(p, unit >> 1, db_smem.ml, st);
+    else mbaff_chroma_row(p, unit >> 1, db_smem.mc, st);
 }
 
 // ======================================================================

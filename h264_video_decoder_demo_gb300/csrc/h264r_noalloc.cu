@@ -36,7 +36,7 @@ struct NoAllocScratch {
     PicDesc desc;                             // descriptor the kernels read
     int error;                                // device error word of the call
     unsigned int ticket[2];                   // wavefront row tickets
-    int progress[2 * kNoAllocMaxRows];        // wavefront progress counters
+    int progress[3 * kNoAllocMaxRows];        // wavefront progress counters
     alignas(256) uint8_t bs[kNoAllocMaxMbs * h264r::kBsBytes];  // boundary strengths (read with 16-byte loads)
 };
 static_assert(offsetof(NoAllocScratch, bs) % 256 == 0, "the bS table must start on a 256-byte boundary");
@@ -58,7 +58,7 @@ __global__ void k_noalloc_init(PicDesc d, NoAllocScratch *s)
         s->error = 0;
         s->ticket[0] = s->ticket[1] = 0;
     }
-    for (uint32_t i = threadIdx.x; i < 2 * kNoAllocMaxRows; i += blockDim.x) s->progress[i] = 0;
+    for (uint32_t i = threadIdx.x; i < 3 * kNoAllocMaxRows; i += blockDim.x) s->progress[i] = 0;
 }
 
 }  // namespace
