@@ -701,204 +701,13 @@ __device__ __forceinline__ void load_intra_residual(const PicDesc &p, int addr, 
     }
 }
 
-// Reconstruct one intra MB with one warp (lane = threadIdx.x & 31).
-__device__ void intra_mb(const PicDesc &p, int addr, IntraSmem &s, const LaunchState &st)
-{
-    const int lane = threadIdx.x & 31;
-    const h264r_mb m = p.mbs[addr];
-    int x, y, dy;
-    mb_origin(p, addr, x, y, dy);
-    const int field = field_mb(p, addr);
-    uint8_t *Y = plane_y(p);
-    // ---- residual (computed by k_inter)
-    load_intra_residual(p, addr, s.res);
-    __syncwarp();
-    // ---- luma prediction + reconstruction
-    if (m.type == H264R_MB_I4x4) {
-        for (int b = 0; b < 16; b++) {
-            const int xO = kBlkX[b] * 4, yO = kBlkY[b] * 4;
-            if (lane < 13) {
-                int nx = lane < 5 ? -1 : lane - 5, ny = lane < 5 ? lane - 1 : -1;
-                int v = -1;
-                if (!(nx > 3 && (b == 3 || b == 11))) {
-                    const uint8_t *ptr = intra_nb_ptr(p, addr, 0, 0, xO + nx, yO + ny);
-                    if (ptr) v = ldcg_u8(ptr);
-                }
-                s.nb[lane] = v;
-            }
-            __syncwarp();
-            if (lane == 0 && s.nb[9] < 0 && s.nb[10] < 0 && s.nb[11] < 0 && s.nb[12] < 0 && s.nb[8] >= 0)
-                s.nb[9] = s.nb[10] = s.nb[11] = s.nb[12] = s.nb[8];
-            __syncwarp();
-            if (lane < 16) {
-                int i = lane >> 2, j = lane & 3;
-                int mode = (m.ipred[b >> 3] >> (4 * (b & 7))) & 15;
-                int pv = pred4x4_sample(mode, s.nb, j, i);
-                if (pv < 0) pv = 0;  // prediction not written: the cleared buffer
-                Y[(size_t)(y + (yO + i) * dy) * p.W + x + xO + j] = (uint8_t)clip1(pv + s.res[(yO + i) * 16 + xO + j]);
-            }
-            __threadfence_block();
-            __syncwarp();
-        }
-    } else if (m.type == H264R_MB_I8x8) {
-        for (int b = 0; b < 4; b++) {
-            const int xO = (b & 1) * 8, yO = (b >> 1) * 8;
-            // 25 samples: p[-1,-1], p[-1,0..7], p[0..15,-1]
-            if (lane < 25) {
-                int nx = lane < 9 ? -1 : lane - 9, ny = lane < 9 ? lane - 1 : -1;
-                const uint8_t *ptr = intra_nb_ptr(p, addr, 0, 0, xO + nx, yO + ny);
-                s.nb[lane] = ptr ? ldcg_u8(ptr) : -1;
-            }
-            __syncwarp();
-            if (lane == 0) {
-                int *q = s.nb;  // q[0] corner, q[1..8] left, q[9..24] top
-                bool all = true;
-                for (int i = 17; i < 25; i++) all = all && q[i] < 0;
-                if (all && q[16] >= 0)
-                    for (int i = 17; i < 25; i++) q[i] = q[16];
-                int *f = s.nbf;
-                for (int i = 0; i < 25; i++) f[i] = -1;
-                bool top16 = true;
-                for (int i = 9; i < 25; i++) top16 = top16 && q[i] >= 0;
-                // 8.3.2.2.1 reference sample filtering (H264PictureBase.cpp:1540-1600)
-                if (top16) {
-                    f[9] = (q[0] >= 0) ? (q[0] + 2 * q[9] + q[10] + 2) >> 2 : (3 * q[9] + q[10] + 2) >> 2;
-                    for (int i = 10; i < 24; i++) f[i] = (q[i - 1] + 2 * q[i] + q[i + 1] + 2) >> 2;
-                    f[24] = (q[23] + 3 * q[24] + 2) >> 2;
-                }
-                if (q[0] >= 0) {
-                    if (q[9] < 0 || q[1] < 0) {
-                        if (q[9] >= 0) f[0] = (3 * q[0] + q[9] + 2) >> 2;
-                        else if (q[1] >= 0) f[0] = (3 * q[0] + q[1] + 2) >> 2;
-                        else f[0] = q[0];
-                    } else {
-                        f[0] = (q[9] + 2 * q[0] + q[1] + 2) >> 2;
-                    }
-                }
-                bool left8 = true;
-                for (int i = 1; i < 9; i++) left8 = left8 && q[i] >= 0;
-                if (left8) {
-                    f[1] = (q[0] >= 0) ? (q[0] + 2 * q[1] + q[2] + 2) >> 2 : (3 * q[1] + q[2] + 2) >> 2;
-                    for (int i = 2; i < 8; i++) f[i] = (q[i - 1] + 2 * q[i] + q[i + 1] + 2) >> 2;
-                    f[8] = (q[7] + 3 * q[8] + 2) >> 2;
-                }
-            }
-            __syncwarp();
-            int mode = (m.ipred[0] >> (4 * b)) & 15;
-            for (int k = lane; k < 64; k += 32) {
-                int i = k >> 3, j = k & 7;
-                int pv = pred8x8_sample(mode, s.nbf, j, i);
-                if (pv < 0) pv = 0;
-                Y[(size_t)(y + (yO + i) * dy) * p.W + x + xO + j] = (uint8_t)clip1(pv + s.res[(yO + i) * 16 + xO + j]);
-            }
-            __threadfence_block();
-            __syncwarp();
-        }
-    } else {
-        // Intra_16x16: 33 samples p[-1,-1], p[-1,0..15], p[0..15,-1]
-        for (int k = lane; k < 33; k += 32) {
-            int nx = k < 17 ? -1 : k - 17, ny = k < 17 ? k - 1 : -1;
-            const uint8_t *ptr = intra_nb_ptr(p, addr, 0, 0, nx, ny);
-            s.nb[k] = ptr ? ldcg_u8(ptr) : -1;
-        }
-        __syncwarp();
-        const int *q = s.nb;
-        bool ta = true, la = true;
-        for (int i = 0; i < 16; i++) { ta = ta && q[17 + i] >= 0; la = la && q[1 + i] >= 0; }
-        const int mode = m.i16_mode;
-        int a = 0, bb = 0, cc = 0, dcv = 128;
-        if (mode == 2) {
-            int stp = 0, slf = 0;
-            for (int i = 0; i < 16; i++) { stp += q[17 + i]; slf += q[1 + i]; }
-            if (ta && la) dcv = (stp + slf + 16) >> 5;
-            else if (la) dcv = (slf + 8) >> 4;
-            else if (ta) dcv = (stp + 8) >> 4;
-        } else if (mode == 3) {
-            // quirk: p[-1,-1] is not required; when unavailable -1 enters H, V
-            int H = 0, V = 0;
-            for (int i = 0; i <= 7; i++) {
-                H += (i + 1) * (q[17 + 8 + i] - (6 - i >= 0 ? q[17 + 6 - i] : q[0]));
-                V += (i + 1) * (q[1 + 8 + i] - (6 - i >= 0 ? q[1 + 6 - i] : q[0]));
-            }
-            a = 16 * (q[1 + 15] + q[17 + 15]);
-            bb = (5 * H + 32) >> 6;
-            cc = (5 * V + 32) >> 6;
-        }
-        for (int k = lane; k < 256; k += 32) {
-            int i = k >> 4, j = k & 15, pv;
-            if (mode == 0) pv = ta ? q[17 + j] : 0;
-            else if (mode == 1) pv = la ? q[1 + i] : 0;
-            else if (mode == 2) pv = dcv;
-            else if (mode == 3) pv = (ta && la) ? clip1((a + bb * (j - 7) + cc * (i - 7) + 16) >> 5) : 0;
-            else pv = 0;
-            Y[(size_t)(y + i * dy) * p.W + x + j] = (uint8_t)clip1(pv + s.res[k]);
-        }
-        __threadfence_block();
-        __syncwarp();
-    }
-    // ---- chroma (Intra_chroma_sample_prediction_for_YUV420_or_YUV422,
-    //      H264PictureBase.cpp:2076-2385); quirk: DC treats value 0 as unavailable
-    for (int k = lane; k < 34; k += 32) {
-        int pl = k / 17, i = k % 17;
-        int nx = i < 9 ? -1 : i - 9, ny = i < 9 ? i - 1 : -1;
-        const uint8_t *ptr = intra_nb_ptr(p, addr, 1, pl, nx, ny);
-        s.nb[k] = ptr ? ldcg_u8(ptr) : -1;
-    }
-    __syncwarp();
-    const int cmode = m.chroma_mode;
-    const int xc = x / 2, yc = chroma_row0(y);
-    for (int k = lane; k < 128; k += 32) {
-        const int pl = k >> 6, i = (k & 63) >> 3, j = k & 7;
-        const int *q = s.nb + pl * 17;  // q[0] corner, q[1..8] left, q[9..16] top
-        int pv = 0;
-        if (cmode == 0) {
-            int xO = j & 4, yO = i & 4;
-            bool t4 = q[9 + xO] > 0 && q[10 + xO] > 0 && q[11 + xO] > 0 && q[12 + xO] > 0;
-            bool l4 = q[1 + yO] > 0 && q[2 + yO] > 0 && q[3 + yO] > 0 && q[4 + yO] > 0;
-            int stp = t4 ? q[9 + xO] + q[10 + xO] + q[11 + xO] + q[12 + xO] : 0;
-            int slf = l4 ? q[1 + yO] + q[2 + yO] + q[3 + yO] + q[4 + yO] : 0;
-            if ((xO == 0 && yO == 0) || (xO > 0 && yO > 0)) {
-                pv = (t4 && l4) ? (stp + slf + 4) >> 3 : l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
-            } else if (xO > 0) {
-                pv = t4 ? (stp + 2) >> 2 : l4 ? (slf + 2) >> 2 : 128;
-            } else {
-                pv = l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
-            }
-        } else if (cmode == 1) {
-            bool ok = true;
-            for (int u = 0; u < 8; u++) ok = ok && q[1 + u] >= 0;
-            pv = ok ? q[1 + i] : 0;
-        } else if (cmode == 2) {
-            bool ok = true;
-            for (int u = 0; u < 8; u++) ok = ok && q[9 + u] >= 0;
-            pv = ok ? q[9 + j] : 0;
-        } else if (cmode == 3) {
-            bool ok = q[0] >= 0;
-            for (int u = 0; u < 8; u++) ok = ok && q[9 + u] >= 0 && q[1 + u] >= 0;
-            if (ok) {
-                int H = 0, V = 0;
-                for (int u = 0; u <= 3; u++) {
-                    H += (u + 1) * (q[9 + 4 + u] - (2 - u >= 0 ? q[9 + 2 - u] : q[0]));
-                    V += (u + 1) * (q[1 + 4 + u] - (2 - u >= 0 ? q[1 + 2 - u] : q[0]));
-                }
-                int a = 16 * (q[1 + 7] + q[9 + 7]);
-                int b2 = (34 * H + 32) >> 6, c2 = (34 * V + 32) >> 6;
-                pv = clip1((a + b2 * (j - 3) + c2 * (i - 3) + 16) >> 5);
-            }
-        }
-        uint8_t *C = plane_c(p, pl);
-        C[(size_t)(yc + i * dy) * p.Wc + xc + j] = (uint8_t)clip1(pv + s.res[256 + pl * 64 + i * 8 + j]);
-    }
-    __threadfence_block();
-    __syncwarp();
-}
-
-// ---------------------------------------------------------------- frame fast path
-// Non-MBAFF intra MB with its neighbourhood staged in shared memory: the
-// left column, top row (with the top-right MB's samples) and corner are
-// loaded once; the 4x4 / 8x8 blocks predict from and write into the tile;
-// the MB is stored once.  Neighbour availability follows
-// getMbAddrN_non_MBAFF_frames and the Intra_4x4/8x8 block rules.
+// ---------------------------------------------------------------- tiled intra MB
+// Intra MB with its neighbourhood staged in shared memory: the left column,
+// top row (with the top-right MB's samples) and corner are loaded once; the
+// 4x4 / 8x8 blocks predict from and write into the tile; the MB is stored
+// once.  Neighbour availability follows getMbAddrN_non_MBAFF_frames or
+// getMbAddrN_MBAFF_frames for the MB's border and the Intra_4x4/8x8 block
+// rules inside it.
 struct IntraTile {
     int l[17][25];     // luma rows -1..15 (index +1), cols -1..23 (index +1)
     int c[2][9][9];    // chroma rows -1..7, cols -1..7
@@ -913,48 +722,75 @@ __device__ __forceinline__ int tile_nb(const IntraTile &t, int xN, int yN, bool 
     return t.l[yN + 1][xN + 1];
 }
 
-__device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTile &t, const LaunchState &st)
+__device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTile &t, const LaunchState &st)
 {
     const int lane = threadIdx.x & 31;
     const h264r_mb m = p.mbs[addr];
     const int W = p.W, Wc = p.Wc, wmb = p.wmb;
-    const int mx = addr % wmb, my = addr / wmb;
-    const int x = mx * 16, y = my * 16;
+    int x, y, dy;  // first luma sample and row step (2 for a field MB of an MBAFF picture)
+    bool A = false, B = false, Cc = false, D = false;
+    if (p.mbaff) {
+        mb_origin(p, addr, x, y, dy);
+    } else {
+        // neighbour MBs (6.4.9 / getMbAddrN_non_MBAFF_frames) and CIP
+        const int mx = addr % wmb, my = addr / wmb;
+        x = mx * 16;
+        y = my * 16;
+        dy = 1;
+        auto usable = [&](int n) -> bool {
+            if (n < 0 || n > addr) return false;
+            const h264r_mb &q = p.mbs[n];
+            if (q.slice != m.slice) return false;
+            return !(q.type == H264R_MB_INTER && (q.flags & H264R_MBF_CIP));
+        };
+        A = mx > 0 && usable(addr - 1);
+        B = my > 0 && usable(addr - wmb);
+        Cc = my > 0 && mx + 1 < wmb && usable(addr - wmb + 1);
+        D = mx > 0 && my > 0 && usable(addr - wmb - 1);
+    }
     uint8_t *Y = plane_y(p);
-    // ---- neighbour MBs (6.4.9 / getMbAddrN_non_MBAFF_frames) and CIP
-    auto usable = [&](int n) -> bool {
-        if (n < 0 || n > addr) return false;
-        const h264r_mb &q = p.mbs[n];
-        if (q.slice != m.slice) return false;
-        return !(q.type == H264R_MB_INTER && (q.flags & H264R_MBF_CIP));
-    };
-    const bool A = mx > 0 && usable(addr - 1);
-    const bool B = my > 0 && usable(addr - wmb);
-    const bool Cc = my > 0 && mx + 1 < wmb && usable(addr - wmb + 1);
-    const bool D = mx > 0 && my > 0 && usable(addr - wmb - 1);
     // ---- residual (computed by k_inter)
     load_intra_residual(p, addr, s.res);
-    // ---- stage the neighbourhood (luma: corner, 16 left, 24 top; chroma: corner, 8 left, 8 top)
-    for (int i = lane; i < 41 + 34; i += 32) {
+    // ---- stage the neighbourhood (luma: corner, 16 left, 24 top; chroma:
+    //      corner, 8 left, 8 top), -1 where not available for intra
+    //      prediction.  In an MBAFF picture every sample goes through the
+    //      MBAFF neighbour derivation (6.4.12.2): the left column of a frame
+    //      MB beside a field pair alternates between the pair's MBs, and
+    //      under constrained intra prediction parts of it can be missing.
+    uint32_t avail[3];
+#pragma unroll
+    for (int it = 0; it < 3; it++) {
+        const int i = lane + 32 * it;
+        int v = -1;
         if (i < 41) {
-            int v = -1;
-            if (i == 0) { if (D) v = __ldcg(Y + (size_t)(y - 1) * W + x - 1); t.l[0][0] = v; }
-            else if (i < 17) { if (A) v = __ldcg(Y + (size_t)(y + i - 1) * W + x - 1); t.l[i][0] = v; }
-            else {
-                int xx = i - 17;  // 0..23
-                bool ok = xx < 16 ? B : Cc;
-                if (ok) v = __ldcg(Y + (size_t)(y - 1) * W + x + xx);
-                t.l[0][xx + 1] = v;
+            const int xN = i == 0 ? -1 : (i < 17 ? -1 : i - 17), yN = i == 0 ? -1 : (i < 17 ? i - 1 : -1);
+            if (p.mbaff) {
+                const uint8_t *ptr = intra_nb_ptr(p, addr, 0, 0, xN, yN);
+                if (ptr) v = __ldcg(ptr);
+            } else if (i == 0 ? D : (i < 17 ? A : (i < 33 ? B : Cc))) {
+                v = __ldcg(Y + (size_t)(y + yN) * W + x + xN);
             }
-        } else {
-            int j = i - 41, pl = j / 17, q = j % 17, v = -1;
-            const uint8_t *C = plane_c(p, pl);
-            const int xc = x / 2, yc = y / 2;
-            if (q == 0) { if (D) v = __ldcg(C + (size_t)(yc - 1) * Wc + xc - 1); t.c[pl][0][0] = v; }
-            else if (q < 9) { if (A) v = __ldcg(C + (size_t)(yc + q - 1) * Wc + xc - 1); t.c[pl][q][0] = v; }
-            else { if (B) v = __ldcg(C + (size_t)(yc - 1) * Wc + xc + q - 9); t.c[pl][0][q - 8] = v; }
+            t.l[yN + 1][xN + 1] = v;
+        } else if (i < 75) {
+            const int j = i - 41, pl = j / 17, q = j % 17;
+            const int xN = q < 9 ? -1 : q - 9, yN = q < 9 ? q - 1 : -1;
+            if (p.mbaff) {
+                const uint8_t *ptr = intra_nb_ptr(p, addr, 1, pl, xN, yN);
+                if (ptr) v = __ldcg(ptr);
+            } else if (q == 0 ? D : (q < 9 ? A : B)) {
+                v = __ldcg(plane_c(p, pl) + (size_t)(y / 2 + yN) * Wc + x / 2 + xN);
+            }
+            t.c[pl][yN + 1][xN + 1] = v;
         }
+        avail[it] = __ballot_sync(0xffffffffu, v >= 0);
     }
+    // whole-edge availability from the staged samples (item i is bit i % 32
+    // of avail[i / 32]): luma left 1..16, top 17..32; Cb corner 41, left
+    // 42..49, top 50..57 (Cr is the same)
+    const bool la = ((avail[0] >> 1) & 0xFFFFu) == 0xFFFFu;
+    const bool ta = (avail[0] >> 17) == 0x7FFFu && (avail[1] & 1u);
+    const bool cA = ((avail[1] >> 10) & 0xFFu) == 0xFFu, cB = ((avail[1] >> 18) & 0xFFu) == 0xFFu;
+    const bool cD = (avail[1] >> 9) & 1u;
     __syncwarp();
     // ---- luma
     if (m.type == H264R_MB_I4x4) {
@@ -1000,8 +836,8 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
             const int xO = (b & 1) * 8, yO = (b >> 1) * 8;
             // q = {p[-1,-1], p[-1,0..7], p[0..15,-1]}; an unavailable
             // top-right octet takes p[7,-1]
+            int v = -1;
             if (lane < 25) {
-                int v;
                 if (lane == 0) {
                     v = tile_nb(t, xO - 1, yO - 1, true);
                 } else if (lane < 9) {
@@ -1013,6 +849,11 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
                 }
                 s.nb[lane] = v;
             }
+            // the left column and the 16 top samples are filtered only when
+            // available as a whole (an MBAFF left column can be partly
+            // available under constrained intra prediction)
+            const uint32_t nbm = __ballot_sync(0xffffffffu, v >= 0);
+            const bool left8 = ((nbm >> 1) & 0xFFu) == 0xFFu, top16 = ((nbm >> 9) & 0xFFFFu) == 0xFFFFu;
             __syncwarp();
             // 8.3.2.2.1 reference sample filtering, one sample per lane
             // (H264PictureBase.cpp:1540-1600)
@@ -1027,12 +868,12 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
                             f = (q[9] + 2 * q[0] + q[1] + 2) >> 2;
                     }
                 } else if (lane < 9) {
-                    if (q[1] >= 0) {  // the left column is available as a whole
+                    if (left8) {
                         if (lane == 1) f = q[0] >= 0 ? (q[0] + 2 * q[1] + q[2] + 2) >> 2 : (3 * q[1] + q[2] + 2) >> 2;
                         else if (lane < 8) f = (q[lane - 1] + 2 * q[lane] + q[lane + 1] + 2) >> 2;
                         else f = (q[7] + 3 * q[8] + 2) >> 2;
                     }
-                } else if (q[9] >= 0 && q[17] >= 0) {  // all 16 top samples
+                } else if (top16) {
                     if (lane == 9) f = q[0] >= 0 ? (q[0] + 2 * q[9] + q[10] + 2) >> 2 : (3 * q[9] + q[10] + 2) >> 2;
                     else if (lane < 24) f = (q[lane - 1] + 2 * q[lane] + q[lane + 1] + 2) >> 2;
                     else f = (q[23] + 3 * q[24] + 2) >> 2;
@@ -1052,7 +893,6 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     } else {
         // Intra_16x16 (H264PictureBase.cpp:1847-2059)
         const int *top = &t.l[0][1];
-        bool ta = B, la = A;
         const int mode = m.i16_mode;
         int a = 0, bb = 0, cc = 0, dcv = 128;
         if (mode == 2) {
@@ -1101,11 +941,11 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
             else if (xO > 0) pv = t4 ? (stp + 2) >> 2 : l4 ? (slf + 2) >> 2 : 128;
             else pv = l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
         } else if (cmode == 1) {
-            pv = A ? CL(i) : 0;
+            pv = cA ? CL(i) : 0;
         } else if (cmode == 2) {
-            pv = B ? CT(j) : 0;
+            pv = cB ? CT(j) : 0;
         } else if (cmode == 3) {
-            if (A && B && D) {
+            if (cA && cB && cD) {
                 int H = 0, V = 0;
                 for (int u = 0; u <= 3; u++) {
                     H += (u + 1) * (CT(4 + u) - (2 - u >= 0 ? CT(2 - u) : c[0][0]));
@@ -1123,10 +963,10 @@ __device__ void intra_mb_frame(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     __syncwarp();
     // ---- store the MB: 16 luma rows of 16 bytes, 2 x 8 chroma rows of 8 bytes
     if (lane < 16) {
-        *(uint4 *)(Y + (size_t)(y + lane) * W + x) = pack16(&t.l[1 + lane][1]);
+        *(uint4 *)(Y + (size_t)(y + lane * dy) * W + x) = pack16(&t.l[1 + lane][1]);
     } else {
         const int pl = (lane - 16) >> 3, r = (lane - 16) & 7;
-        *(uint2 *)(plane_c(p, pl) + (size_t)(y / 2 + r) * Wc + x / 2) = pack8(&s.res[256 + pl * 64 + r * 8]);
+        *(uint2 *)(plane_c(p, pl) + (size_t)(chroma_row0(y) + r * dy) * Wc + x / 2) = pack8(&s.res[256 + pl * 64 + r * 8]);
     }
     __threadfence_block();
     __syncwarp();
@@ -1172,8 +1012,7 @@ __global__ void __launch_bounds__(32, 21) k_intra(const PicDesc *__restrict__ pi
             for (int k = 0; k < per; k++) {
                 int addr = p.mbaff ? 2 * (row * uw + u) + k : row * uw + u;
                 if (!is_intra_type(p.mbs[addr].type)) continue;
-                if (p.mbaff) intra_mb(p, addr, s, st);
-                else intra_mb_frame(p, addr, s, tile, st);
+                intra_mb_tiled(p, addr, s, tile, st);
             }
             __syncwarp();
             if (lane == 0) st_release(prog + row, u + 1);
