@@ -1,0 +1,123 @@
+// h264r_bits.h — RBSP bit reading for the host-side syntax parser:
+// emulation-prevention removal (7.4.1), fixed-length, Exp-Golomb (9.1) and
+// more_rbsp_data (7.2).  Reads past the end return zeros and set `err`, so a
+// truncated unit fails its range checks instead of reading out of bounds.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+namespace h264r {
+
+// NAL unit payload (after the one-byte header) with every 0x000003 turned
+// back into 0x0000.
+inline void nal_to_rbsp(const uint8_t *p, size_t n, std::vector<uint8_t> &out)
+{
+    out.clear();
+    out.reserve(n);
+    int zeros = 0;
+    for (size_t i = 0; i < n; i++) {
+        const uint8_t b = p[i];
+        if (zeros >= 2 && b == 3) {
+            zeros = 0;
+            continue;
+        }
+        out.push_back(b);
+        zeros = b == 0 ? zeros + 1 : 0;
+    }
+}
+
+struct BitReader {
+    const uint8_t *p = nullptr;
+    size_t nbits = 0, pos = 0;
+    size_t stop = 0;  // bit position of the rbsp_stop_one_bit
+    bool err = false;
+
+    BitReader() = default;
+    BitReader(const uint8_t *data, size_t nbytes) { reset(data, nbytes); }
+
+    void reset(const uint8_t *data, size_t nbytes)
+    {
+        p = data;
+        nbits = nbytes * 8;
+        pos = 0;
+        err = false;
+        // the last set bit of the unit is the stop bit (trailing zero bytes
+        // of cabac_zero_words or padding are skipped)
+        size_t n = nbytes;
+        while (n > 0 && p[n - 1] == 0) n--;
+        if (n == 0) {
+            stop = 0;
+        } else {
+            int t = 0;
+            while (!((p[n - 1] >> t) & 1)) t++;
+            stop = n * 8 - 1 - t;
+        }
+    }
+
+    // next k (<= 32) bits without consuming them
+    uint32_t peek(int k) const
+    {
+        uint64_t v = 0;
+        for (int i = 0; i < k; i++) {
+            const size_t b = pos + i;
+            const uint32_t bit = b < nbits ? (p[b >> 3] >> (7 - (b & 7))) & 1u : 0u;
+            v = (v << 1) | bit;
+        }
+        return (uint32_t)v;
+    }
+
+    uint32_t u(int k)
+    {
+        if (k == 0) return 0;
+        // byte-wise fast path
+        uint32_t v = 0;
+        int left = k;
+        while (left > 0) {
+            if (pos >= nbits) {
+                err = true;
+                v <<= left;
+                pos += left;
+                return v;
+            }
+            const int bit_in = (int)(pos & 7), avail = 8 - bit_in;
+            const int take = left < avail ? left : avail;
+            const uint32_t byte = p[pos >> 3];
+            v = (v << take) | ((byte >> (avail - take)) & ((1u << take) - 1u));
+            pos += take;
+            left -= take;
+        }
+        return v;
+    }
+
+    bool flag() { return u(1) != 0; }
+    void skip(size_t k) { pos += k; if (pos > nbits) err = true; }
+
+    uint32_t ue()
+    {
+        int lz = 0;
+        while (u(1) == 0) {
+            if (++lz > 31 || err) {
+                err = true;
+                return 0;
+            }
+        }
+        if (lz == 0) return 0;
+        return ((1u << lz) - 1u) + u(lz);
+    }
+
+    int32_t se()
+    {
+        const uint32_t k = ue();
+        return (k & 1) ? (int32_t)((k + 1) >> 1) : -(int32_t)(k >> 1);
+    }
+
+    // te(v) with range >= 1 (7.4.3 ref_idx when more than one reference)
+    uint32_t te(int range) { return range > 1 ? ue() : (u(1) ^ 1u); }
+
+    bool byte_aligned() const { return (pos & 7) == 0; }
+    bool more_rbsp_data() const { return pos < stop; }
+};
+
+}  // namespace h264r

@@ -1,0 +1,1675 @@
+// h264r_parser.cpp — host-side front end (include/h264r_parser.h): NAL units,
+// slice data (CAVLC), the derivations that turn syntax into reconstruction
+// records (intra modes 8.3.1.1 / 8.3.2.1, motion vectors 8.4.1, weights
+// 8.4.2.3), picture order counts (8.2.1), reference lists (8.2.4), marking
+// (8.2.5), DPB slots and output order.  Restated from the standard; the
+// reference's counterparts are named at each step.
+#include "../../include/h264r_parser.h"
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/h264r_order.h"
+#include "h264r_bits.h"
+#include "h264r_syntax.h"
+
+namespace h264r {
+
+int cavlc_residual_block(BitReader &br, int nC, int start, int end, int max_coeff, int *coeff, int &total);
+int cbp_from_code(uint32_t code, bool intra);
+
+namespace {
+
+constexpr int kNoLongTerm = -1;
+
+// luma4x4BlkIdx -> 4x4 block position (in 4-sample units), 6.4.3
+const uint8_t kBlkX[16] = {0, 1, 0, 1, 2, 3, 2, 3, 0, 1, 0, 1, 2, 3, 2, 3};
+const uint8_t kBlkY[16] = {0, 0, 1, 1, 0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 3, 3};
+
+inline int blk_of(int x4, int y4) { return 8 * (y4 >> 1) + 4 * (x4 >> 1) + 2 * (y4 & 1) + (x4 & 1); }
+inline int clip3(int lo, int hi, int v) { return v < lo ? lo : (v > hi ? hi : v); }
+inline int median3(int a, int b, int c) { return std::max(std::min(a, b), std::min(std::max(a, b), c)); }
+
+// ---------------------------------------------------------------- pictures
+// Motion of a decoded picture, kept while it is a reference (co-located
+// data for direct prediction, 8.4.1.2.1).
+struct Motion {
+    std::vector<uint8_t> intra;   // per MB
+    std::vector<int16_t> mv;      // [mb][list][4x4 raster][2]
+    std::vector<int8_t> ref;      // [mb][list][4x4 raster], -1: list unused
+    std::vector<int32_t> refpic;  // [mb][list][4x4 raster]: uid of the reference picture
+};
+
+struct Pic {
+    int uid = -1, slot = -1;
+    int frame_num = 0, frame_num_wrap = 0, long_term_frame_idx = 0;
+    bool short_ref = false, long_ref = false;
+    int poc = 0, top_poc = 0, bottom_poc = 0;
+    bool mmco5 = false;
+    std::shared_ptr<Motion> motion;
+    bool is_ref() const { return short_ref || long_ref; }
+};
+
+// Neighbour state of one MB of the picture being decoded.
+struct MbState {
+    int slice = -1;  // slice number, -1 while not decoded
+    uint8_t cls = 0; // H264R_MB_*
+    bool skip = false;
+    uint8_t tc[16];        // TotalCoeff per luma4x4BlkIdx
+    uint8_t tcc[2][4];     // chroma AC TotalCoeff
+    int8_t ipm4[16];       // Intra4x4PredMode per luma4x4BlkIdx
+    int8_t ipm8[4];        // Intra8x8PredMode
+    int16_t mv[2][16][2];  // per 4x4 block, raster order
+    int8_t ref[2][16];
+    int32_t refpic[2][16];
+    bool intra() const { return cls != H264R_MB_INTER && cls != H264R_MB_NONE; }
+};
+
+struct SliceCtx {
+    SliceHeader sh;
+    const Sps *sps = nullptr;
+    const Pps *pps = nullptr;
+    std::vector<Pic *> list[2];
+    int index = 0;  // slice number within the picture
+};
+
+// one 4x4 block's motion during the MB derivation
+struct Blk {
+    int16_t mv[2][2];
+    int8_t ref[2];
+};
+
+struct PartRec {
+    int mp, sp;         // mbPartIdx, subMbPartIdx
+    int x, y, w, h;     // luma samples within the MB
+};
+
+}  // namespace
+
+}  // namespace h264r
+
+using namespace h264r;
+
+struct h264r_parser {
+    std::string err;
+    // byte stream
+    std::vector<uint8_t> buf;  // unconsumed input
+    bool ended = false, failed = false;
+    // parameter sets
+    Sps sps[32];
+    Pps pps[256];
+    const Sps *active_sps = nullptr;
+    int width_mbs = 0, height_mbs = 0, dpb_slots = 0, reorder_depth = 0;
+    // DPB
+    std::deque<Pic> dpb;       // decoded pictures still referenced or awaiting output
+    int next_uid = 0;
+    uint32_t decoded = 0;
+    h264r_order *order = nullptr;
+    std::vector<int> slot_uid;  // slot -> uid of its picture, -1 free
+    // POC state
+    int prev_poc_msb = 0, prev_poc_lsb = 0, prev_frame_num_offset = 0, prev_frame_num = 0, prev_ref_frame_num = 0;
+    bool prev_ref_mmco5 = false, prev_mmco5 = false;
+    int prev_ref_bottom_field = 0, prev_ref_top_poc = 0;
+    int max_long_term_frame_idx = kNoLongTerm;
+    // current picture
+    bool in_pic = false;
+    SliceHeader first_sh;  // first slice of the current picture
+    Pic cur;
+    int frame_num_offset = 0;
+    int pending_msb = 0, pending_lsb = 0;
+    std::vector<MbState> mbs;
+    std::vector<h264r_mb> rec;
+    std::vector<h264r_slice> rec_slices;
+    std::vector<h264r_weight> rec_weights;
+    std::vector<uint8_t> motion, coef, pcm;
+    std::vector<uint32_t> dref_parts;  // motion offsets of the parts whose dref still holds a refIdx
+    std::vector<Pic *> last_list[2];
+    int num_slices = 0;
+    uint32_t slice_errors = 0;  // slices skipped after a syntax error
+    uint8_t first_slice_type = 0;
+    // completed pictures waiting for h264r_parser_next
+    struct Done {
+        h264r_picture pic;
+        std::vector<h264r_mb> mbs;
+        std::vector<h264r_slice> slices;
+        std::vector<h264r_weight> weights;
+        std::vector<uint8_t> motion, coef, pcm;
+        int32_t poc;
+        uint32_t index;
+        uint8_t idr, reference, slice_type;
+        std::vector<uint8_t> out_slots;
+        std::vector<int32_t> out_poc;
+        std::vector<uint32_t> out_index;
+    };
+    std::deque<Done> done;
+    Done current_out;  // storage behind the last h264r_parser_next result
+    // slot -> (poc, index) of the picture it holds, for output reporting
+    std::vector<int32_t> slot_poc;
+    std::vector<uint32_t> slot_index;
+    std::vector<uint8_t> rbsp;
+
+    ~h264r_parser()
+    {
+        if (order) h264r_order_destroy(order);
+    }
+
+    int fail(int code, const char *fmt, ...)
+    {
+        char m[256];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(m, sizeof(m), fmt, ap);
+        va_end(ap);
+        err = m;
+        failed = true;
+        return code;
+    }
+
+    // ---- NAL units
+    int process_nal(const uint8_t *p, size_t n);
+    int start_picture(const SliceHeader &sh, const Sps &s, const Pps &q);
+    int finish_picture(bool last);
+    int decode_slice(SliceCtx &sc, BitReader &br);
+    int build_lists(SliceCtx &sc);
+    void compute_poc(const SliceHeader &sh, const Sps &s);
+    int mark_references(const SliceHeader &sh, const Sps &s);
+    int alloc_slot();
+};
+
+namespace {
+
+// ---------------------------------------------------------------- MB layer
+// Macroblock-level decoding context: parses one MB, derives its prediction
+// parameters and writes its record.
+struct MbDecoder {
+    h264r_parser &P;
+    SliceCtx &sc;
+    BitReader &br;
+    const Sps &sps;
+    const Pps &pps;
+    int W, addr = 0, qp = 0;
+    MbState *cur = nullptr;
+    bool decoded4x4[16];  // motion of this 4x4 block already derived
+    Blk blk[16];          // motion of the current MB (raster)
+
+    MbDecoder(h264r_parser &p, SliceCtx &s, BitReader &b)
+        : P(p), sc(s), br(b), sps(*s.sps), pps(*s.pps), W(p.width_mbs)
+    {
+        qp = pps.pic_init_qp + s.sh.slice_qp_delta;
+    }
+
+    // ---- neighbours (6.4.12.1): the MB holding luma location (xN, yN)
+    // relative to the current MB, or -1; (xW, yW) inside it
+    int nb_mb(int xN, int yN, int maxW, int maxH, int &xW, int &yW) const
+    {
+        int n;
+        const int x = addr % W;
+        if (xN < 0 && yN < 0) n = x > 0 ? addr - W - 1 : -1;
+        else if (xN < 0 && yN < maxH) n = x > 0 ? addr - 1 : -1;
+        else if (xN < maxW && yN < 0) n = addr - W;
+        else if (xN < maxW && yN < maxH) n = addr;
+        else if (xN >= maxW && yN < 0) n = x + 1 < W ? addr - W + 1 : -1;
+        else return -1;
+        if (n < 0) return -1;
+        if (n != addr && P.mbs[n].slice != sc.index) return -1;  // not yet decoded or another slice
+        xW = (xN + maxW) % maxW;
+        yW = (yN + maxH) % maxH;
+        return n;
+    }
+
+    // ---- intra prediction modes (8.3.1.1 Intra4x4PredMode, 8.3.2.1 Intra8x8PredMode;
+    // CH264PictureBase::getIntra4x4PredMode / getIntra8x8PredMode, H264PictureBase.cpp:773-1058)
+    int pred_mode_nb(int xN, int yN, bool for8x8, bool isA, int &dcflag) const
+    {
+        int xW = 0, yW = 0;
+        const int n = nb_mb(xN, yN, 16, 16, xW, yW);
+        if (n < 0) {
+            dcflag = 1;
+            return 2;
+        }
+        const MbState &m = P.mbs[n];
+        if (!m.intra() && pps.constrained_intra_pred) dcflag = 1;
+        if (m.cls == H264R_MB_I4x4) {
+            const int b = blk_of(xW >> 2, yW >> 2);
+            if (!for8x8) return m.ipm4[b];
+            // 8x8 block of the neighbour, n = 1 for A, 2 for B
+            return m.ipm4[(b >> 2) * 4 + (isA ? 1 : 2)];
+        }
+        if (m.cls == H264R_MB_I8x8) return m.ipm8[blk_of(xW >> 2, yW >> 2) >> 2];
+        return 2;
+    }
+
+    int derive_mode(int x, int y, bool for8x8, int prev_flag, int rem) const
+    {
+        int dc = 0;
+        int a = pred_mode_nb(x - 1, y, for8x8, true, dc);
+        int b = pred_mode_nb(x, y - 1, for8x8, false, dc);
+        if (dc) a = b = 2;
+        const int pred = std::min(a, b);
+        if (prev_flag) return pred;
+        return rem < pred ? rem : rem + 1;
+    }
+
+    // ---- CAVLC nC (9.2.1)
+    int total_of(int n, bool chroma, int comp, int b) const
+    {
+        const MbState &m = P.mbs[n];
+        if (m.skip) return 0;
+        if (m.cls == H264R_MB_IPCM) return 16;
+        return chroma ? m.tcc[comp][b] : m.tc[b];
+    }
+
+    int nc_luma(int b) const
+    {
+        const int x = kBlkX[b] * 4, y = kBlkY[b] * 4;
+        int xW = 0, yW = 0;
+        const int na = nb_mb(x - 1, y, 16, 16, xW, yW);
+        const int nA = na >= 0 ? total_of(na, false, 0, blk_of(xW >> 2, yW >> 2)) : 0;
+        const int nbm = nb_mb(x, y - 1, 16, 16, xW, yW);
+        const int nB = nbm >= 0 ? total_of(nbm, false, 0, blk_of(xW >> 2, yW >> 2)) : 0;
+        if (na >= 0 && nbm >= 0) return (nA + nB + 1) >> 1;
+        return na >= 0 ? nA : (nbm >= 0 ? nB : 0);
+    }
+
+    int nc_chroma(int comp, int b) const
+    {
+        const int x = (b & 1) * 4, y = (b >> 1) * 4;
+        int xW = 0, yW = 0;
+        const int na = nb_mb(x - 1, y, 8, 8, xW, yW);
+        const int nA = na >= 0 ? total_of(na, true, comp, (yW >> 2) * 2 + (xW >> 2)) : 0;
+        const int nbm = nb_mb(x, y - 1, 8, 8, xW, yW);
+        const int nB = nbm >= 0 ? total_of(nbm, true, comp, (yW >> 2) * 2 + (xW >> 2)) : 0;
+        if (na >= 0 && nbm >= 0) return (nA + nB + 1) >> 1;
+        return na >= 0 ? nA : (nbm >= 0 ? nB : 0);
+    }
+
+    // ---- motion neighbours (6.4.11.7, 8.4.1.3.2)
+    struct Nb {
+        bool avail;
+        int ref;
+        int mv[2];
+    };
+
+    Nb nb_motion(int xN, int yN, int list) const
+    {
+        Nb r = {false, -1, {0, 0}};
+        int xW = 0, yW = 0;
+        const int n = nb_mb(xN, yN, 16, 16, xW, yW);
+        if (n < 0) return r;
+        const int bi = (yW >> 2) * 4 + (xW >> 2);
+        if (n == addr) {
+            if (!decoded4x4[bi]) return r;
+            r.avail = true;
+            r.ref = blk[bi].ref[list];
+            if (r.ref >= 0) {
+                r.mv[0] = blk[bi].mv[list][0];
+                r.mv[1] = blk[bi].mv[list][1];
+            }
+            return r;
+        }
+        const MbState &m = P.mbs[n];
+        r.avail = true;
+        if (m.intra()) return r;
+        r.ref = m.ref[list][bi];
+        if (r.ref >= 0) {
+            r.mv[0] = m.mv[list][bi][0];
+            r.mv[1] = m.mv[list][bi][1];
+        }
+        return r;
+    }
+
+    // 8.4.1.3: mvpLX of the partition at (x, y) of width w; shape: 0
+    // 16x16 / other, 1 16x8, 2 8x16 (directional rules), part: mbPartIdx
+    void mvp(int x, int y, int w, int shape, int part, int list, int ref, int out[2]) const
+    {
+        Nb A = nb_motion(x - 1, y, list), B = nb_motion(x, y - 1, list), C = nb_motion(x + w, y - 1, list);
+        if (!C.avail) C = nb_motion(x - 1, y - 1, list);
+        if (shape == 1) {
+            if (part == 0 && B.ref == ref) { out[0] = B.mv[0]; out[1] = B.mv[1]; return; }
+            if (part == 1 && A.ref == ref) { out[0] = A.mv[0]; out[1] = A.mv[1]; return; }
+        } else if (shape == 2) {
+            if (part == 0 && A.ref == ref) { out[0] = A.mv[0]; out[1] = A.mv[1]; return; }
+            if (part == 1 && C.ref == ref) { out[0] = C.mv[0]; out[1] = C.mv[1]; return; }
+        }
+        if (!B.avail && !C.avail && A.avail) B = C = A;
+        const int match = (A.ref == ref) + (B.ref == ref) + (C.ref == ref);
+        if (match == 1) {
+            const Nb &s = A.ref == ref ? A : (B.ref == ref ? B : C);
+            out[0] = s.mv[0];
+            out[1] = s.mv[1];
+            return;
+        }
+        out[0] = median3(A.mv[0], B.mv[0], C.mv[0]);
+        out[1] = median3(A.mv[1], B.mv[1], C.mv[1]);
+    }
+
+    void set_blocks(int x, int y, int w, int h, const Blk &b)
+    {
+        for (int j = y >> 2; j < (y + h) >> 2; j++)
+            for (int i = x >> 2; i < (x + w) >> 2; i++) {
+                blk[j * 4 + i] = b;
+                decoded4x4[j * 4 + i] = true;
+            }
+    }
+
+    // ---- direct prediction (8.4.1.2)
+    struct Col {
+        int mv[2];
+        int ref;      // refIdxCol, -1 for intra
+        int refpic;   // uid of the picture it refers to
+    };
+
+    Col colocated(int bi) const
+    {
+        Col c = {{0, 0}, -1, -1};
+        const Pic *col = sc.list[1].empty() ? nullptr : sc.list[1][0];
+        if (!col || !col->motion) return c;
+        const Motion &m = *col->motion;
+        if (m.intra[addr]) return c;
+        int l = 0;
+        if (m.ref[(addr * 2 + 0) * 16 + bi] < 0) l = 1;
+        const size_t o = (size_t)(addr * 2 + l) * 16 + bi;
+        c.ref = m.ref[o];
+        c.mv[0] = m.mv[o * 2];
+        c.mv[1] = m.mv[o * 2 + 1];
+        c.refpic = m.refpic[o];
+        return c;
+    }
+
+    // spatial direct: MB-level reference indices and predictors (8.4.1.2.2)
+    bool spatial_ready = false;
+    int sp_ref[2];
+    int sp_mv[2][2];
+    bool sp_zero = false;
+
+    void spatial_setup()
+    {
+        if (spatial_ready) return;
+        spatial_ready = true;
+        for (int l = 0; l < 2; l++) {
+            Nb A = nb_motion(-1, 0, l), B = nb_motion(0, -1, l), C = nb_motion(16, -1, l);
+            if (!C.avail) C = nb_motion(-1, -1, l);
+            auto minpos = [](int a, int b) { return (a >= 0 && b >= 0) ? std::min(a, b) : std::max(a, b); };
+            sp_ref[l] = minpos(A.ref, minpos(B.ref, C.ref));
+        }
+        sp_zero = sp_ref[0] < 0 && sp_ref[1] < 0;
+        if (sp_zero) sp_ref[0] = sp_ref[1] = 0;
+        for (int l = 0; l < 2; l++) {
+            sp_mv[l][0] = sp_mv[l][1] = 0;
+            if (sp_ref[l] >= 0 && !sp_zero) mvp(0, 0, 16, 0, 0, l, sp_ref[l], sp_mv[l]);
+        }
+    }
+
+    // direct motion of the 4x4 block (bx, by) (raster units)
+    int direct_block(int bx, int by, Blk &b)
+    {
+        const int q = (by >> 1) * 2 + (bx >> 1);
+        const int cbx = sps.direct_8x8_inference ? ((q & 1) ? 3 : 0) : bx;
+        const int cby = sps.direct_8x8_inference ? ((q & 2) ? 3 : 0) : by;
+        const Col c = colocated(cby * 4 + cbx);
+        if (sc.sh.direct_spatial) {
+            spatial_setup();
+            const Pic *l1 = sc.list[1][0];
+            const bool colzero = l1 && l1->short_ref && c.ref == 0 && c.mv[0] >= -1 && c.mv[0] <= 1 && c.mv[1] >= -1 &&
+                                 c.mv[1] <= 1;
+            for (int l = 0; l < 2; l++) {
+                b.ref[l] = (int8_t)sp_ref[l];
+                if (sp_ref[l] < 0 || sp_zero || (sp_ref[l] == 0 && colzero)) {
+                    b.mv[l][0] = b.mv[l][1] = 0;
+                } else {
+                    b.mv[l][0] = (int16_t)sp_mv[l][0];
+                    b.mv[l][1] = (int16_t)sp_mv[l][1];
+                }
+            }
+            return 0;
+        }
+        // temporal (8.4.1.2.3)
+        int r0 = 0;
+        if (c.ref >= 0) {
+            r0 = -1;
+            for (size_t i = 0; i < sc.list[0].size(); i++)
+                if (sc.list[0][i] && sc.list[0][i]->uid == c.refpic) {
+                    r0 = (int)i;
+                    break;
+                }
+            if (r0 < 0) return P.fail(H264R_ERR_BAD_RECORD, "temporal direct: co-located reference not in RefPicList0 (MB %d)", addr);
+        }
+        const Pic *p0 = sc.list[0][r0], *p1 = sc.list[1][0];
+        b.ref[0] = (int8_t)r0;
+        b.ref[1] = 0;
+        const int td = clip3(-128, 127, p1->poc - p0->poc);
+        if (p0->long_ref || td == 0) {
+            b.mv[0][0] = (int16_t)c.mv[0];
+            b.mv[0][1] = (int16_t)c.mv[1];
+            b.mv[1][0] = b.mv[1][1] = 0;
+        } else {
+            const int tb = clip3(-128, 127, P.cur.poc - p0->poc);
+            const int tx = (16384 + std::abs(td / 2)) / td;
+            const int dsf = clip3(-1024, 1023, (tb * tx + 32) >> 6);
+            for (int k = 0; k < 2; k++) {
+                b.mv[0][k] = (int16_t)((dsf * c.mv[k] + 128) >> 8);
+                b.mv[1][k] = (int16_t)(b.mv[0][k] - c.mv[k]);
+            }
+        }
+        return 0;
+    }
+
+    // ---- prediction weights (8.4.2.3), as the record's weight entry
+    uint16_t weight_index(int ref0, int ref1)
+    {
+        const int st = sc.sh.slice_type;
+        const bool pf0 = ref0 >= 0, pf1 = ref1 >= 0;
+        h264r_weight w;
+        memset(&w, 0, sizeof(w));
+        bool weighted = false;
+        if ((st == kSliceP || st == kSliceSP) && pps.weighted_pred && pf0) {
+            weighted = true;
+            const PredWeights &pw = sc.sh.pw;
+            w.log_wd[0] = (int8_t)pw.luma_log2;
+            w.log_wd[1] = w.log_wd[2] = (int8_t)pw.chroma_log2;
+            w.w0[0] = (int16_t)pw.lw[0][ref0];
+            w.o0[0] = (int16_t)pw.lo[0][ref0];
+            for (int c = 0; c < 2; c++) {
+                w.w0[1 + c] = (int16_t)pw.cw[0][ref0][c];
+                w.o0[1 + c] = (int16_t)pw.co[0][ref0][c];
+            }
+        } else if (st == kSliceB && pps.weighted_bipred_idc == 1 && (pf0 || pf1)) {
+            weighted = true;
+            const PredWeights &pw = sc.sh.pw;
+            w.log_wd[0] = (int8_t)pw.luma_log2;
+            w.log_wd[1] = w.log_wd[2] = (int8_t)pw.chroma_log2;
+            if (pf0) {
+                w.w0[0] = (int16_t)pw.lw[0][ref0];
+                w.o0[0] = (int16_t)pw.lo[0][ref0];
+                for (int c = 0; c < 2; c++) {
+                    w.w0[1 + c] = (int16_t)pw.cw[0][ref0][c];
+                    w.o0[1 + c] = (int16_t)pw.co[0][ref0][c];
+                }
+            }
+            if (pf1) {
+                w.w1[0] = (int16_t)pw.lw[1][ref1];
+                w.o1[0] = (int16_t)pw.lo[1][ref1];
+                for (int c = 0; c < 2; c++) {
+                    w.w1[1 + c] = (int16_t)pw.cw[1][ref1][c];
+                    w.o1[1 + c] = (int16_t)pw.co[1][ref1][c];
+                }
+            }
+        } else if (st == kSliceB && pps.weighted_bipred_idc == 2 && pf0 && pf1) {
+            weighted = true;
+            const Pic *p0 = sc.list[0][ref0], *p1 = sc.list[1][ref1];
+            int w0 = 32, w1 = 32;
+            const int td = clip3(-128, 127, p1->poc - p0->poc);
+            if (td != 0 && !p0->long_ref && !p1->long_ref) {
+                const int tb = clip3(-128, 127, P.cur.poc - p0->poc);
+                const int tx = (16384 + std::abs(td / 2)) / td;
+                const int dsf = clip3(-1024, 1023, (tb * tx + 32) >> 6);
+                if (!((dsf >> 2) < -64 || (dsf >> 2) > 128)) {
+                    w0 = 64 - (dsf >> 2);
+                    w1 = dsf >> 2;
+                }
+            }
+            for (int c = 0; c < 3; c++) {
+                w.log_wd[c] = 5;
+                w.w0[c] = (int16_t)w0;
+                w.w1[c] = (int16_t)w1;
+            }
+        }
+        if (!weighted) return 0;
+        w.weighted = 1;
+        std::vector<h264r_weight> &t = P.rec_weights;
+        for (size_t i = 0; i < t.size(); i++)
+            if (memcmp(&t[i], &w, sizeof(w)) == 0) return (uint16_t)i;
+        t.push_back(w);
+        return (uint16_t)(t.size() - 1);
+    }
+
+    int decode();
+    int residual(int cls, int cbp, bool t8, uint32_t &mask, std::vector<uint16_t> &sig, std::vector<int16_t> &lv, h264r_mb &r);
+    int inter_pred(int mb_type, bool is_b, h264r_mb &r, bool &no_sub_lt8);
+    void emit_motion(int shape, const std::vector<PartRec> &parts, h264r_mb &r);
+    void store_motion();
+};
+
+// P mb_type 0..4 and B mb_type 1..21: partition shape (0 16x16, 1 16x8,
+// 2 8x16) and prediction lists per partition (bit 0 L0, bit 1 L1)
+struct InterType {
+    int shape, pred0, pred1;
+};
+
+InterType b_type(int t)
+{
+    if (t >= 1 && t <= 3) return {0, t, 0};
+    static const int pairs[9][2] = {{1, 1}, {2, 2}, {1, 2}, {2, 1}, {1, 3}, {2, 3}, {3, 1}, {3, 2}, {3, 3}};
+    const int j = (t - 4) / 2;
+    return {(t % 2 == 0) ? 1 : 2, pairs[j][0], pairs[j][1]};
+}
+
+// sub_mb_type: record sub shape (0 8x8, 1 8x4, 2 4x8, 3 4x4), lists
+struct SubType {
+    int shape, pred;
+};
+
+SubType p_sub(int t) { return {t, 1}; }
+SubType b_sub(int t)
+{
+    if (t == 0) return {3, 0};  // direct: 4x4 blocks
+    if (t <= 3) return {0, t};
+    static const SubType s[9] = {{1, 1}, {2, 1}, {1, 2}, {2, 2}, {1, 3}, {2, 3}, {3, 1}, {3, 2}, {3, 3}};
+    return s[t - 4];
+}
+
+void sub_geom(int shape, int sp, int &x, int &y, int &w, int &h)
+{
+    switch (shape) {
+    case 0: x = 0; y = 0; w = 8; h = 8; break;
+    case 1: x = 0; y = 4 * sp; w = 8; h = 4; break;
+    case 2: x = 4 * sp; y = 0; w = 4; h = 8; break;
+    default: x = 4 * (sp & 1); y = 4 * (sp >> 1); w = 4; h = 4; break;
+    }
+}
+
+int MbDecoder::inter_pred(int mb_type, bool is_b, h264r_mb &r, bool &no_sub_lt8)
+{
+    no_sub_lt8 = true;
+    const int nref[2] = {sc.sh.num_ref_idx_active[0], sc.sh.num_ref_idx_active[1]};
+    std::vector<PartRec> parts;
+    int shape = 0;
+    // read the syntax first (mb_pred / sub_mb_pred, 7.3.5.1 / 7.3.5.2)
+    const bool b8x8 = is_b ? mb_type == 22 : (mb_type == 3 || mb_type == 4);
+    for (int i = 0; i < 16; i++) decoded4x4[i] = false;
+    spatial_ready = false;
+    if (!b8x8) {
+        InterType t = is_b ? b_type(mb_type) : InterType{mb_type == 0 ? 0 : mb_type, 1, 1};
+        const int np = t.shape == 0 ? 1 : 2;
+        const int pred[2] = {t.pred0, np == 2 ? t.pred1 : 0};
+        int ref[2][2] = {{-1, -1}, {-1, -1}}, mvd[2][2][2] = {};
+        for (int l = 0; l < 2; l++)
+            for (int p = 0; p < np; p++)
+                if (pred[p] & (1 << l)) {
+                    ref[p][l] = nref[l] > 1 ? (int)br.te(nref[l] - 1) : 0;
+                    if (ref[p][l] >= nref[l] || !sc.list[l][ref[p][l]])
+                        return P.fail(H264R_ERR_BAD_RECORD, "ref_idx names no picture (MB %d)", addr);
+                }
+        for (int l = 0; l < 2; l++)
+            for (int p = 0; p < np; p++)
+                if (pred[p] & (1 << l)) {
+                    mvd[p][l][0] = br.se();
+                    mvd[p][l][1] = br.se();
+                }
+        shape = t.shape;
+        for (int p = 0; p < np; p++) {
+            const int x = t.shape == 2 ? 8 * p : 0, y = t.shape == 1 ? 8 * p : 0;
+            const int w = t.shape == 2 ? 8 : 16, h = t.shape == 1 ? 8 : 16;
+            Blk b;
+            for (int l = 0; l < 2; l++) {
+                b.ref[l] = (int8_t)ref[p][l];
+                b.mv[l][0] = b.mv[l][1] = 0;
+                if (ref[p][l] >= 0) {
+                    int m[2];
+                    mvp(x, y, w, t.shape, p, l, ref[p][l], m);
+                    b.mv[l][0] = (int16_t)(m[0] + mvd[p][l][0]);
+                    b.mv[l][1] = (int16_t)(m[1] + mvd[p][l][1]);
+                }
+            }
+            set_blocks(x, y, w, h, b);
+            parts.push_back({p, 0, x, y, w, h});
+        }
+    } else {
+        int sub[4];
+        SubType st[4];
+        for (int q = 0; q < 4; q++) {
+            sub[q] = (int)br.ue();
+            if (sub[q] > (is_b ? 12 : 3)) return P.fail(H264R_ERR_BAD_RECORD, "sub_mb_type out of range (MB %d)", addr);
+            st[q] = is_b ? b_sub(sub[q]) : p_sub(sub[q]);
+            // noSubMbPartSizeLessThan8x8Flag (7.3.5)
+            if (is_b && sub[q] == 0) {
+                if (!sps.direct_8x8_inference) no_sub_lt8 = false;
+            } else if (st[q].shape != 0) {
+                no_sub_lt8 = false;
+            }
+        }
+        const bool ref0 = !is_b && mb_type == 4;  // P_8x8ref0
+        int ref[4][2], mvd[4][4][2][2] = {};
+        for (int l = 0; l < 2; l++)
+            for (int q = 0; q < 4; q++) {
+                ref[q][l] = -1;
+                if (st[q].pred & (1 << l)) {
+                    ref[q][l] = (!ref0 && nref[l] > 1) ? (int)br.te(nref[l] - 1) : 0;
+                    if (ref[q][l] >= nref[l] || !sc.list[l][ref[q][l]])
+                        return P.fail(H264R_ERR_BAD_RECORD, "ref_idx names no picture (MB %d)", addr);
+                }
+            }
+        for (int l = 0; l < 2; l++)
+            for (int q = 0; q < 4; q++)
+                if (st[q].pred & (1 << l)) {
+                    const int ns = st[q].shape == 0 ? 1 : (st[q].shape == 3 ? 4 : 2);
+                    for (int s = 0; s < ns; s++) {
+                        mvd[q][s][l][0] = br.se();
+                        mvd[q][s][l][1] = br.se();
+                    }
+                }
+        shape = 3;
+        for (int q = 0; q < 4; q++) {
+            shape |= st[q].shape << (2 + 2 * q);
+            const int qx = (q & 1) * 8, qy = (q >> 1) * 8;
+            if (is_b && sub[q] == 0) {  // B_Direct_8x8: four 4x4 blocks
+                for (int s = 0; s < 4; s++) {
+                    const int x = qx + 4 * (s & 1), y = qy + 4 * (s >> 1);
+                    Blk b;
+                    if (direct_block(x >> 2, y >> 2, b)) return -1;
+                    set_blocks(x, y, 4, 4, b);
+                    parts.push_back({q, s, x, y, 4, 4});
+                }
+                continue;
+            }
+            const int ns = st[q].shape == 0 ? 1 : (st[q].shape == 3 ? 4 : 2);
+            for (int s = 0; s < ns; s++) {
+                int sx, sy, w, h;
+                sub_geom(st[q].shape, s, sx, sy, w, h);
+                const int x = qx + sx, y = qy + sy;
+                Blk b;
+                for (int l = 0; l < 2; l++) {
+                    b.ref[l] = (int8_t)ref[q][l];
+                    b.mv[l][0] = b.mv[l][1] = 0;
+                    if (ref[q][l] >= 0) {
+                        int m[2];
+                        mvp(x, y, w, 0, 0, l, ref[q][l], m);
+                        b.mv[l][0] = (int16_t)(m[0] + mvd[q][s][l][0]);
+                        b.mv[l][1] = (int16_t)(m[1] + mvd[q][s][l][1]);
+                    }
+                }
+                set_blocks(x, y, w, h, b);
+                parts.push_back({q, s, x, y, w, h});
+            }
+        }
+    }
+    if (br.err) return P.fail(H264R_ERR_BAD_RECORD, "truncated prediction syntax (MB %d)", addr);
+    emit_motion(shape, parts, r);
+    return 0;
+}
+
+// motion payload of the record: shape, then one h264r_part per partition
+void MbDecoder::emit_motion(int shape, const std::vector<PartRec> &parts, h264r_mb &r)
+{
+    std::vector<uint8_t> &m = P.motion;
+    while (m.size() & 3) m.push_back(0);
+    r.aux = (uint32_t)m.size();
+    const uint16_t hdr[2] = {(uint16_t)shape, (uint16_t)parts.size()};
+    m.insert(m.end(), (const uint8_t *)hdr, (const uint8_t *)hdr + 4);
+    for (const PartRec &pr : parts) {
+        const Blk &b = blk[(pr.y >> 2) * 4 + (pr.x >> 2)];
+        h264r_part p;
+        memset(&p, 0, sizeof(p));
+        for (int l = 0; l < 2; l++) {
+            p.mv[l][0] = b.mv[l][0];
+            p.mv[l][1] = b.mv[l][1];
+            p.ref[l] = -1;
+            p.dref[l] = b.ref[l];  // refIdx for now: the picture-level list resolves it at the end
+            if (b.ref[l] >= 0) {
+                const Pic *rp = sc.list[l][b.ref[l]];
+                p.ref[l] = (int8_t)rp->slot;
+            }
+        }
+        p.wt = weight_index(b.ref[0], b.ref[1]);
+        const size_t off = m.size();
+        m.insert(m.end(), (const uint8_t *)&p, (const uint8_t *)&p + sizeof(p));
+        P.dref_parts.push_back((uint32_t)off);
+    }
+}
+
+// motion of the finished MB into the neighbour state
+void MbDecoder::store_motion()
+{
+    for (int i = 0; i < 16; i++)
+        for (int l = 0; l < 2; l++) {
+            cur->ref[l][i] = blk[i].ref[l];
+            cur->mv[l][i][0] = blk[i].mv[l][0];
+            cur->mv[l][i][1] = blk[i].mv[l][1];
+            cur->refpic[l][i] = blk[i].ref[l] >= 0 ? sc.list[l][blk[i].ref[l]]->uid : -1;
+        }
+}
+
+// residual( 0, 15 ) (7.3.5.3) with CAVLC blocks; fills the coefficient
+// payload parts and the TotalCoeff state
+int MbDecoder::residual(int cls, int cbp, bool t8, uint32_t &mask, std::vector<uint16_t> &sig, std::vector<int16_t> &lv,
+                        h264r_mb &r)
+{
+    const int cbp_luma = cbp & 15, cbp_chroma = cbp >> 4;
+    int c[64];
+    int tc = 0;
+    auto put_block = [&](const int *v, int n, int off, int bit) {
+        uint16_t s = 0;
+        for (int k = 0; k < n; k++)
+            if (v[k]) s |= (uint16_t)(1u << (k + off));
+        if (!s) return;
+        mask |= 1u << bit;
+        sig.push_back(s);
+        for (int k = 0; k < n; k++)
+            if (v[k]) lv.push_back((int16_t)v[k]);
+    };
+    const bool i16 = cls == H264R_MB_I16x16;
+    int dc[16];
+    bool have_dc = false;
+    // r.nz4x4 / nz8x8 follow the blocks as they are parsed, so that a MB
+    // whose residual fails keeps the counts reached, as the reference's does
+    r.nz4x4 = 0;
+    r.nz8x8 = 0;
+    for (int b = 0; b < 16; b++) cur->tc[b] = 0;
+    if (i16) {
+        if (cavlc_residual_block(br, nc_luma(0), 0, 15, 16, dc, tc)) return -1;
+        have_dc = true;
+        // the reference keeps the DC block's TotalCoeff as block 0's count
+        // until an AC block 0 replaces it (H264MacroBlock.cpp residual_luma);
+        // no other MB takes block 0 as a neighbour, so parsing is unaffected
+        cur->tc[0] = (uint8_t)tc;
+        if (tc) r.nz4x4 = 1;
+    }
+    int l8[4][64];
+    memset(l8, 0, sizeof(l8));
+    for (int b8 = 0; b8 < 4; b8++) {
+        for (int b4 = 0; b4 < 4; b4++) {
+            const int b = b8 * 4 + b4;
+            if (!(cbp_luma & (1 << b8))) continue;
+            if (i16) {
+                if (cavlc_residual_block(br, nc_luma(b), 0, 14, 15, c, tc)) return -1;
+                put_block(c, 15, 1, b);
+            } else {
+                if (cavlc_residual_block(br, nc_luma(b), 0, 15, 16, c, tc)) return -1;
+                if (t8) {
+                    for (int k = 0; k < 16; k++) l8[b8][4 * k + b4] = c[k];
+                } else {
+                    put_block(c, 16, 0, b);
+                }
+            }
+            cur->tc[b] = (uint8_t)tc;
+            r.nz4x4 = (uint16_t)((r.nz4x4 & ~(1u << b)) | (tc ? 1u << b : 0u));
+            if (tc) r.nz8x8 |= (uint8_t)(1u << b8);
+        }
+    }
+    if (t8) {
+        for (int b8 = 0; b8 < 4; b8++) {
+            uint16_t s4[4] = {0, 0, 0, 0};
+            std::vector<int16_t> vals;
+            for (int k = 0; k < 64; k++)
+                if (l8[b8][k]) {
+                    s4[k >> 4] |= (uint16_t)(1u << (k & 15));
+                    vals.push_back((int16_t)l8[b8][k]);
+                }
+            if (!vals.empty()) {
+                mask |= 1u << b8;
+                sig.insert(sig.end(), s4, s4 + 4);
+                lv.insert(lv.end(), vals.begin(), vals.end());
+            }
+        }
+    }
+    if (have_dc) put_block(dc, 16, 0, 16);
+    // chroma DC then AC (4:2:0)
+    int cdc[2][4];
+    for (int cc = 0; cc < 2; cc++) {
+        for (int k = 0; k < 4; k++) cdc[cc][k] = 0;
+        if ((cbp_chroma & 3) && cavlc_residual_block(br, -1, 0, 3, 4, cdc[cc], tc)) return -1;
+    }
+    put_block(cdc[0], 4, 0, 17);
+    put_block(cdc[1], 4, 0, 18);
+    for (int cc = 0; cc < 2; cc++)
+        for (int b = 0; b < 4; b++) {
+            cur->tcc[cc][b] = 0;
+            if (!(cbp_chroma & 2)) continue;
+            if (cavlc_residual_block(br, nc_chroma(cc, b), 0, 14, 15, c, tc)) return -1;
+            cur->tcc[cc][b] = (uint8_t)tc;
+            put_block(c, 15, 1, (cc ? H264R_CM_CR_AC0 : H264R_CM_CB_AC0) + b);
+        }
+    return 0;
+}
+
+int MbDecoder::decode()
+{
+    h264r_mb r;
+    memset(&r, 0, sizeof(r));
+    r.coef = H264R_NONE;
+    r.aux = H264R_NONE;
+    r.slice = (uint16_t)sc.index;
+    if (pps.constrained_intra_pred) r.flags |= H264R_MBF_CIP;
+    const int st = sc.sh.slice_type;
+    uint32_t mb_type = br.ue();
+    bool is_intra_type = true;
+    uint32_t itype = mb_type;
+    if (st == kSliceP) {
+        if (mb_type < 5) is_intra_type = false;
+        else itype = mb_type - 5;
+    } else if (st == kSliceB) {
+        if (mb_type < 23) is_intra_type = false;
+        else itype = mb_type - 23;
+    }
+    if (is_intra_type && itype > 25) return P.fail(H264R_ERR_BAD_RECORD, "mb_type %u out of range (MB %d)", mb_type, addr);
+    for (int i = 0; i < 16; i++) {
+        cur->ipm4[i] = 2;
+        cur->tc[i] = 0;
+    }
+    for (int i = 0; i < 4; i++) cur->ipm8[i] = 2;
+    memset(cur->tcc, 0, sizeof(cur->tcc));
+    for (int i = 0; i < 16; i++) {
+        blk[i].ref[0] = blk[i].ref[1] = -1;
+        blk[i].mv[0][0] = blk[i].mv[0][1] = blk[i].mv[1][0] = blk[i].mv[1][1] = 0;
+    }
+    if (is_intra_type && itype == 25) {  // I_PCM
+        while (!br.byte_aligned()) br.u(1);
+        r.type = H264R_MB_IPCM;
+        cur->cls = H264R_MB_IPCM;
+        r.aux = (uint32_t)(P.pcm.size() / 384);
+        for (int i = 0; i < 384; i++) P.pcm.push_back((uint8_t)br.u(8));
+        for (int i = 0; i < 16; i++) cur->tc[i] = 16;
+        r.qpy = (uint8_t)qp;
+        if (br.err) return P.fail(H264R_ERR_BAD_RECORD, "truncated I_PCM (MB %d)", addr);
+        P.rec[addr] = r;
+        return 0;
+    }
+    int cbp = 0;
+    bool t8 = false;
+    int cls;
+    if (is_intra_type) {
+        if (itype == 0) {  // I_NxN
+            if (pps.transform_8x8_mode) t8 = br.flag();
+            cls = t8 ? H264R_MB_I8x8 : H264R_MB_I4x4;
+            cur->cls = (uint8_t)cls;
+            if (!t8) {
+                int flag[16], rem[16];
+                for (int b = 0; b < 16; b++) {
+                    flag[b] = (int)br.u(1);
+                    rem[b] = flag[b] ? 0 : (int)br.u(3);
+                }
+                for (int b = 0; b < 16; b++) {
+                    cur->ipm4[b] = (int8_t)derive_mode(kBlkX[b] * 4, kBlkY[b] * 4, false, flag[b], rem[b]);
+                    r.ipred[b >> 3] |= (uint32_t)(cur->ipm4[b] & 15) << (4 * (b & 7));
+                }
+            } else {
+                int flag[4], rem[4];
+                for (int b = 0; b < 4; b++) {
+                    flag[b] = (int)br.u(1);
+                    rem[b] = flag[b] ? 0 : (int)br.u(3);
+                }
+                for (int b = 0; b < 4; b++) {
+                    cur->ipm8[b] = (int8_t)derive_mode((b & 1) * 8, (b >> 1) * 8, true, flag[b], rem[b]);
+                    r.ipred[0] |= (uint32_t)(cur->ipm8[b] & 15) << (4 * b);
+                    for (int k = 0; k < 4; k++) cur->ipm4[b * 4 + k] = cur->ipm8[b];
+                }
+            }
+            const uint32_t cm = br.ue();
+            if (cm > 3) return P.fail(H264R_ERR_BAD_RECORD, "intra_chroma_pred_mode out of range (MB %d)", addr);
+            r.chroma_mode = (uint8_t)cm;
+            const uint32_t code = br.ue();
+            cbp = cbp_from_code(code, true);
+            if (cbp < 0) return P.fail(H264R_ERR_BAD_RECORD, "coded_block_pattern out of range (MB %d)", addr);
+        } else {  // I_16x16
+            cls = H264R_MB_I16x16;
+            cur->cls = (uint8_t)cls;
+            r.i16_mode = (uint8_t)((itype - 1) % 4);
+            cbp = (((itype - 1) / 4) % 3) << 4 | (itype >= 13 ? 15 : 0);
+            const uint32_t cm = br.ue();
+            if (cm > 3) return P.fail(H264R_ERR_BAD_RECORD, "intra_chroma_pred_mode out of range (MB %d)", addr);
+            r.chroma_mode = (uint8_t)cm;
+        }
+        r.type = (uint8_t)cls;
+        // an intra MB has no motion: list entries stay unused
+    } else {
+        cls = H264R_MB_INTER;
+        cur->cls = H264R_MB_INTER;
+        r.type = H264R_MB_INTER;
+        const bool is_b = st == kSliceB;
+        bool no_sub_lt8 = true;
+        if (is_b && mb_type == 0) {  // B_Direct_16x16
+            for (int i = 0; i < 16; i++) decoded4x4[i] = false;
+            spatial_ready = false;
+            std::vector<PartRec> parts;
+            for (int q = 0; q < 4; q++)
+                for (int s = 0; s < 4; s++) {
+                    const int x = (q & 1) * 8 + 4 * (s & 1), y = (q >> 1) * 8 + 4 * (s >> 1);
+                    Blk b;
+                    if (direct_block(x >> 2, y >> 2, b)) return -1;
+                    set_blocks(x, y, 4, 4, b);
+                    parts.push_back({q, s, x, y, 4, 4});
+                }
+            emit_motion(3 | (3 << 2) | (3 << 4) | (3 << 6) | (3 << 8), parts, r);
+            if (!sps.direct_8x8_inference) no_sub_lt8 = false;
+        } else {
+            if (inter_pred((int)mb_type, is_b, r, no_sub_lt8)) return -1;
+        }
+        const uint32_t code = br.ue();
+        cbp = cbp_from_code(code, false);
+        if (cbp < 0) return P.fail(H264R_ERR_BAD_RECORD, "coded_block_pattern out of range (MB %d)", addr);
+        if ((cbp & 15) && pps.transform_8x8_mode && no_sub_lt8 &&
+            (!(is_b && mb_type == 0) || sps.direct_8x8_inference))
+            t8 = br.flag();
+    }
+    if (t8) r.flags |= H264R_MBF_T8x8;
+    uint32_t mask = 0;
+    std::vector<uint16_t> sig;
+    std::vector<int16_t> lv;
+    if ((cbp & 15) || (cbp >> 4) || cls == H264R_MB_I16x16) {
+        int dq = br.se();
+        dq = clip3(-26, 25, dq);
+        qp = (qp + dq + 52) % 52;
+        if (residual(cls, cbp, t8, mask, sig, lv, r)) {
+            // the reference stops the slice here but has already set up this
+            // MB: it is predicted without residual, with QPY still 0
+            r.qpy = 0;
+            r.coef = H264R_NONE;
+            if (cls == H264R_MB_INTER) store_motion();
+            P.rec[addr] = r;
+            return P.fail(H264R_ERR_BAD_RECORD, "residual syntax error (MB %d)", addr);
+        }
+    }
+    r.qpy = (uint8_t)qp;
+    if (mask) {
+        std::vector<uint8_t> &c = P.coef;
+        while (c.size() & 3) c.push_back(0);
+        r.coef = (uint32_t)c.size();
+        c.insert(c.end(), (const uint8_t *)&mask, (const uint8_t *)&mask + 4);
+        c.insert(c.end(), (const uint8_t *)sig.data(), (const uint8_t *)sig.data() + 2 * sig.size());
+        while (c.size() & 3) c.push_back(0);
+        c.insert(c.end(), (const uint8_t *)lv.data(), (const uint8_t *)lv.data() + 2 * lv.size());
+    }
+    if (br.err) return P.fail(H264R_ERR_BAD_RECORD, "truncated macroblock (MB %d)", addr);
+    if (cls == H264R_MB_INTER) store_motion();
+    P.rec[addr] = r;
+    return 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- slices
+namespace {
+
+// P_Skip / B_Skip (8.4.1.1, 8.4.1.2): motion only, QPY unchanged
+int decode_skip(MbDecoder &d, h264r_mb &r)
+{
+    memset(&r, 0, sizeof(r));
+    r.coef = H264R_NONE;
+    r.aux = H264R_NONE;
+    r.type = H264R_MB_INTER;
+    r.slice = (uint16_t)d.sc.index;
+    if (d.pps.constrained_intra_pred) r.flags |= H264R_MBF_CIP;
+    r.qpy = (uint8_t)d.qp;
+    MbState *cur = d.cur;
+    cur->cls = H264R_MB_INTER;
+    cur->skip = true;
+    for (int i = 0; i < 16; i++) {
+        cur->ipm4[i] = 2;
+        cur->tc[i] = 0;
+        d.decoded4x4[i] = false;
+    }
+    for (int i = 0; i < 4; i++) cur->ipm8[i] = 2;
+    memset(cur->tcc, 0, sizeof(cur->tcc));
+    std::vector<PartRec> parts;
+    if (d.sc.sh.slice_type == kSliceB) {
+        d.spatial_ready = false;
+        for (int q = 0; q < 4; q++)
+            for (int s = 0; s < 4; s++) {
+                const int x = (q & 1) * 8 + 4 * (s & 1), y = (q >> 1) * 8 + 4 * (s >> 1);
+                Blk b;
+                if (d.direct_block(x >> 2, y >> 2, b)) return -1;
+                d.set_blocks(x, y, 4, 4, b);
+                parts.push_back({q, s, x, y, 4, 4});
+            }
+        d.emit_motion(3 | (3 << 2) | (3 << 4) | (3 << 6) | (3 << 8), parts, r);
+    } else {
+        const MbDecoder::Nb A = d.nb_motion(-1, 0, 0), B = d.nb_motion(0, -1, 0);
+        Blk b;
+        b.ref[0] = 0;
+        b.ref[1] = -1;
+        b.mv[0][0] = b.mv[0][1] = b.mv[1][0] = b.mv[1][1] = 0;
+        const bool zero = !A.avail || !B.avail || (A.ref == 0 && A.mv[0] == 0 && A.mv[1] == 0) ||
+                          (B.ref == 0 && B.mv[0] == 0 && B.mv[1] == 0);
+        if (!zero) {
+            int m[2];
+            d.mvp(0, 0, 16, 0, 0, 0, 0, m);
+            b.mv[0][0] = (int16_t)m[0];
+            b.mv[0][1] = (int16_t)m[1];
+        }
+        d.set_blocks(0, 0, 16, 16, b);
+        parts.push_back({0, 0, 0, 0, 16, 16});
+        d.emit_motion(0, parts, r);
+    }
+    d.store_motion();
+    return 0;
+}
+
+}  // namespace
+
+// slice_data( ) (7.3.4), CAVLC
+int h264r_parser::decode_slice(SliceCtx &sc, BitReader &br)
+{
+    const int num_mbs = (int)mbs.size();
+    MbDecoder d(*this, sc, br);
+    int addr = sc.sh.first_mb;
+    if (addr >= num_mbs) return fail(H264R_ERR_BAD_RECORD, "first_mb_in_slice %d out of range", addr);
+    const bool skips = sc.sh.slice_type != kSliceI;
+    bool more = true;
+    while (more) {
+        if (skips) {
+            const uint32_t run = br.ue();
+            if (br.err) return fail(H264R_ERR_BAD_RECORD, "truncated mb_skip_run");
+            for (uint32_t i = 0; i < run; i++) {
+                if (addr >= num_mbs) return fail(H264R_ERR_BAD_RECORD, "mb_skip_run past the picture end");
+                if (mbs[addr].slice >= 0) return fail(H264R_ERR_BAD_RECORD, "MB %d decoded twice", addr);
+                d.addr = addr;
+                d.cur = &mbs[addr];
+                d.cur->slice = sc.index;
+                d.cur->skip = false;
+                if (decode_skip(d, rec[addr])) return failed ? H264R_ERR_BAD_RECORD : fail(H264R_ERR_BAD_RECORD, "skip MB %d", addr);
+                addr++;
+            }
+            if (run > 0) more = br.more_rbsp_data();
+        }
+        if (more) {
+            if (addr >= num_mbs) return fail(H264R_ERR_BAD_RECORD, "slice data past the picture end");
+            if (mbs[addr].slice >= 0) return fail(H264R_ERR_BAD_RECORD, "MB %d decoded twice", addr);
+            d.addr = addr;
+            d.cur = &mbs[addr];
+            d.cur->slice = sc.index;
+            d.cur->skip = false;
+            if (d.decode()) return H264R_ERR_BAD_RECORD;
+            addr++;
+            more = br.more_rbsp_data();
+        }
+    }
+    return H264R_OK;
+}
+
+// ---------------------------------------------------------------- POC (8.2.1)
+void h264r_parser::compute_poc(const SliceHeader &sh, const Sps &s)
+{
+    const int max_frame_num = 1 << s.log2_max_frame_num;
+    if (s.poc_type == 0) {
+        if (sh.idr) {
+            prev_poc_msb = prev_poc_lsb = 0;
+        } else if (prev_ref_mmco5) {
+            prev_poc_msb = 0;
+            prev_poc_lsb = prev_ref_bottom_field ? 0 : prev_ref_top_poc;
+        }
+        const int max_lsb = 1 << s.log2_max_poc_lsb;
+        int msb;
+        if (sh.poc_lsb < prev_poc_lsb && prev_poc_lsb - sh.poc_lsb >= max_lsb / 2) msb = prev_poc_msb + max_lsb;
+        else if (sh.poc_lsb > prev_poc_lsb && sh.poc_lsb - prev_poc_lsb > max_lsb / 2) msb = prev_poc_msb - max_lsb;
+        else msb = prev_poc_msb;
+        cur.top_poc = msb + sh.poc_lsb;
+        cur.bottom_poc = cur.top_poc + sh.delta_poc_bottom;
+        if (sh.nal_ref_idc) {  // becomes prevPicOrderCntMsb / Lsb for the next picture
+            pending_msb = msb;
+            pending_lsb = sh.poc_lsb;
+        }
+    } else {
+        if (sh.idr) frame_num_offset = 0;
+        else {
+            const int prev_off = prev_mmco5 ? 0 : prev_frame_num_offset;
+            frame_num_offset = prev_frame_num > sh.frame_num ? prev_off + max_frame_num : prev_off;
+        }
+        if (s.poc_type == 1) {
+            const int cycle = (int)s.offset_for_ref_frame.size();
+            int abs_frame_num = cycle != 0 ? frame_num_offset + sh.frame_num : 0;
+            if (sh.nal_ref_idc == 0 && abs_frame_num > 0) abs_frame_num--;
+            int expected = 0;
+            if (abs_frame_num > 0) {
+                int delta_cycle = 0;
+                for (int i = 0; i < cycle; i++) delta_cycle += s.offset_for_ref_frame[i];
+                const int cnt = (abs_frame_num - 1) / cycle, in_cycle = (abs_frame_num - 1) % cycle;
+                expected = cnt * delta_cycle;
+                for (int i = 0; i <= in_cycle; i++) expected += s.offset_for_ref_frame[i];
+            }
+            if (sh.nal_ref_idc == 0) expected += s.offset_for_non_ref_pic;
+            cur.top_poc = expected + sh.delta_poc[0];
+            cur.bottom_poc = cur.top_poc + s.offset_for_top_to_bottom_field + sh.delta_poc[1];
+        } else {
+            int t = 0;
+            if (!sh.idr) t = sh.nal_ref_idc == 0 ? 2 * (frame_num_offset + sh.frame_num) - 1 : 2 * (frame_num_offset + sh.frame_num);
+            cur.top_poc = cur.bottom_poc = t;
+        }
+    }
+    cur.poc = std::min(cur.top_poc, cur.bottom_poc);
+}
+
+// ---------------------------------------------------------------- lists (8.2.4)
+int h264r_parser::build_lists(SliceCtx &sc)
+{
+    const SliceHeader &sh = sc.sh;
+    const Sps &s = *sc.sps;
+    const int max_frame_num = 1 << s.log2_max_frame_num;
+    sc.list[0].clear();
+    sc.list[1].clear();
+    if (sh.slice_type == kSliceI) return H264R_OK;
+    std::vector<Pic *> shorts, longs;
+    for (Pic &p : dpb) {
+        if (p.short_ref) {
+            p.frame_num_wrap = p.frame_num > sh.frame_num ? p.frame_num - max_frame_num : p.frame_num;
+            shorts.push_back(&p);
+        } else if (p.long_ref) {
+            longs.push_back(&p);
+        }
+    }
+    std::stable_sort(longs.begin(), longs.end(), [](const Pic *a, const Pic *b) { return a->long_term_frame_idx < b->long_term_frame_idx; });
+    std::vector<Pic *> init[2];
+    if (sh.slice_type == kSliceP) {
+        std::vector<Pic *> st = shorts;
+        std::stable_sort(st.begin(), st.end(), [](const Pic *a, const Pic *b) { return a->frame_num_wrap > b->frame_num_wrap; });
+        init[0] = st;
+        init[0].insert(init[0].end(), longs.begin(), longs.end());
+    } else {
+        // CH264PictureBase::Initialisation_process_for_reference_picture_lists_for_B_slices_in_frames
+        // (H264RefPicList.cpp:830-1015): POC <= current on the L0 side
+        std::vector<Pic *> before, after;
+        for (Pic *p : shorts) (p->poc > cur.poc ? after : before).push_back(p);
+        std::stable_sort(before.begin(), before.end(), [](const Pic *a, const Pic *b) { return a->poc > b->poc; });
+        std::stable_sort(after.begin(), after.end(), [](const Pic *a, const Pic *b) { return a->poc < b->poc; });
+        init[0] = before;
+        init[0].insert(init[0].end(), after.begin(), after.end());
+        init[0].insert(init[0].end(), longs.begin(), longs.end());
+        init[1] = after;
+        init[1].insert(init[1].end(), before.begin(), before.end());
+        init[1].insert(init[1].end(), longs.begin(), longs.end());
+        if (init[1].size() > 1 && init[1] == init[0]) std::swap(init[1][0], init[1][1]);
+        if (init[0].empty()) return fail(H264R_ERR_BAD_RECORD, "B slice without reference pictures");
+    }
+    const int nlists = sh.slice_type == kSliceB ? 2 : 1;
+    for (int l = 0; l < nlists; l++) {
+        const int n = sh.num_ref_idx_active[l];
+        std::vector<Pic *> list = init[l];
+        list.resize(n, nullptr);
+        // modification (8.2.4.3)
+        const int cur_pic_num = sh.frame_num, max_pic_num = max_frame_num;
+        int pred = cur_pic_num, idx = 0;
+        for (const RefMod &m : sh.mods[l]) {
+            if (idx >= n) return fail(H264R_ERR_BAD_RECORD, "too many reference list modifications");
+            Pic *target = nullptr;
+            if (m.idc == 0 || m.idc == 1) {
+                const int d = m.value + 1;
+                int no_wrap;
+                if (m.idc == 0) {
+                    no_wrap = pred - d;
+                    if (no_wrap < 0) no_wrap += max_pic_num;
+                } else {
+                    no_wrap = pred + d;
+                    if (no_wrap >= max_pic_num) no_wrap -= max_pic_num;
+                }
+                pred = no_wrap;
+                const int pic_num = no_wrap > cur_pic_num ? no_wrap - max_pic_num : no_wrap;
+                for (Pic *p : shorts)
+                    if (p->frame_num_wrap == pic_num) target = p;
+                if (!target) return fail(H264R_ERR_BAD_RECORD, "modification names a missing short-term picture");
+            } else if (m.idc == 2) {
+                for (Pic *p : longs)
+                    if (p->long_term_frame_idx == m.value) target = p;
+                if (!target) return fail(H264R_ERR_BAD_RECORD, "modification names a missing long-term picture");
+            } else {
+                return fail(H264R_ERR_UNSUPPORTED, "modification_of_pic_nums_idc %d", m.idc);
+            }
+            // insert target at idx, drop its later duplicate
+            list.insert(list.begin() + idx, target);
+            idx++;
+            int w = idx;
+            for (int k = idx; k < (int)list.size(); k++)
+                if (list[k] != target) list[w++] = list[k];
+            list.resize(std::max(w, n));
+            list.resize(n);
+        }
+        sc.list[l] = list;
+        if (n < 1 || !list[0]) return fail(H264R_ERR_BAD_RECORD, "reference list %d is empty", l);
+    }
+    return H264R_OK;
+}
+
+// ---------------------------------------------------------------- marking (8.2.5)
+int h264r_parser::mark_references(const SliceHeader &sh, const Sps &s)
+{
+    const int max_frame_num = 1 << s.log2_max_frame_num;
+    cur.mmco5 = false;
+    if (sh.idr) {
+        for (Pic &p : dpb) p.short_ref = p.long_ref = false;
+        if (sh.long_term_reference) {
+            cur.long_ref = true;
+            cur.long_term_frame_idx = 0;
+            max_long_term_frame_idx = 0;
+        } else {
+            cur.short_ref = true;
+            max_long_term_frame_idx = kNoLongTerm;
+        }
+        return H264R_OK;
+    }
+    bool cur_long = false;
+    if (sh.adaptive_marking) {
+        for (Pic &p : dpb)
+            if (p.short_ref) p.frame_num_wrap = p.frame_num > sh.frame_num ? p.frame_num - max_frame_num : p.frame_num;
+        for (const Mmco &m : sh.mmcos) {
+            if (m.op == 1 || m.op == 3) {
+                const int pic_num_x = sh.frame_num - (m.diff_pic_nums_minus1 + 1);
+                Pic *t = nullptr;
+                for (Pic &p : dpb)
+                    if (p.short_ref && p.frame_num_wrap == pic_num_x) t = &p;
+                if (!t) continue;
+                if (m.op == 1) {
+                    t->short_ref = false;
+                } else {
+                    for (Pic &p : dpb)
+                        if (p.long_ref && p.long_term_frame_idx == m.long_term_frame_idx) p.long_ref = false;
+                    t->short_ref = false;
+                    t->long_ref = true;
+                    t->long_term_frame_idx = m.long_term_frame_idx;
+                }
+            } else if (m.op == 2) {
+                for (Pic &p : dpb)
+                    if (p.long_ref && p.long_term_frame_idx == m.long_term_pic_num) p.long_ref = false;
+            } else if (m.op == 4) {
+                max_long_term_frame_idx = m.max_long_term_frame_idx_plus1 - 1;
+                for (Pic &p : dpb)
+                    if (p.long_ref && p.long_term_frame_idx > max_long_term_frame_idx) p.long_ref = false;
+            } else if (m.op == 5) {
+                for (Pic &p : dpb) p.short_ref = p.long_ref = false;
+                max_long_term_frame_idx = kNoLongTerm;
+                cur.mmco5 = true;
+            } else if (m.op == 6) {
+                for (Pic &p : dpb)
+                    if (p.long_ref && p.long_term_frame_idx == m.long_term_frame_idx) p.long_ref = false;
+                cur.long_ref = true;
+                cur.long_term_frame_idx = m.long_term_frame_idx;
+                cur_long = true;
+            }
+        }
+    } else {
+        // sliding window (8.2.5.3)
+        int n_short = 0, n_long = 0;
+        for (Pic &p : dpb) {
+            n_short += p.short_ref;
+            n_long += p.long_ref;
+        }
+        if (n_short + n_long >= std::max(s.max_num_ref_frames, 1) && n_short > 0) {
+            Pic *oldest = nullptr;
+            for (Pic &p : dpb)
+                if (p.short_ref) {
+                    p.frame_num_wrap = p.frame_num > sh.frame_num ? p.frame_num - max_frame_num : p.frame_num;
+                    if (!oldest || p.frame_num_wrap < oldest->frame_num_wrap) oldest = &p;
+                }
+            oldest->short_ref = false;
+        }
+    }
+    if (!cur_long) cur.short_ref = true;
+    if (cur.mmco5) {  // the picture counts as frame_num 0 with its POC rebased (8.2.1)
+        const int t = cur.poc;
+        cur.top_poc -= t;
+        cur.bottom_poc -= t;
+        cur.poc = 0;
+        cur.frame_num = 0;
+    }
+    return H264R_OK;
+}
+
+int h264r_parser::alloc_slot()
+{
+    for (int i = 0; i < (int)slot_uid.size(); i++)
+        if (slot_uid[i] < 0) return i;
+    return -1;
+}
+
+// first slice of a new picture
+int h264r_parser::start_picture(const SliceHeader &sh, const Sps &s, const Pps &q)
+{
+    (void)q;
+    if (!active_sps) {
+        active_sps = &s;
+        width_mbs = s.width_mbs;
+        height_mbs = s.frame_height_mbs();
+        reorder_depth = s.has_reorder ? s.max_num_reorder_frames
+                                      : h264r_order_infer_depth(s.profile_idc, s.constraint_set3, s.level_idc, width_mbs, height_mbs);
+        if (reorder_depth < 0) reorder_depth = 0;
+        if (reorder_depth > 16) reorder_depth = 16;
+        dpb_slots = std::min(32, std::max(s.max_num_ref_frames, 1) + reorder_depth + 1);
+        slot_uid.assign(dpb_slots, -1);
+        slot_poc.assign(dpb_slots, 0);
+        slot_index.assign(dpb_slots, 0);
+        if (h264r_order_create(reorder_depth, &order)) return fail(H264R_ERR_INVALID_ARG, "reorder depth");
+    } else if (s.width_mbs != width_mbs || s.frame_height_mbs() != height_mbs) {
+        return fail(H264R_ERR_UNSUPPORTED, "picture size change within the stream");
+    }
+    if (!s.frame_mbs_only && s.mbaff) return fail(H264R_ERR_UNSUPPORTED, "MBAFF frames");
+    cur = Pic();
+    cur.uid = next_uid++;
+    cur.frame_num = sh.frame_num;
+    compute_poc(sh, s);
+    const int slot = alloc_slot();
+    if (slot < 0) return fail(H264R_ERR_BUSY, "no free DPB slot");
+    cur.slot = slot;
+    slot_uid[slot] = cur.uid;
+    slot_poc[slot] = cur.poc;
+    slot_index[slot] = decoded;
+    const int n = width_mbs * height_mbs;
+    mbs.assign(n, MbState());
+    h264r_mb none;
+    memset(&none, 0, sizeof(none));
+    none.type = H264R_MB_NONE;
+    none.coef = H264R_NONE;
+    none.aux = H264R_NONE;
+    rec.assign(n, none);
+    rec_slices.clear();
+    rec_weights.assign(1, h264r_weight());
+    memset(&rec_weights[0], 0, sizeof(h264r_weight));
+    motion.clear();
+    coef.clear();
+    pcm.clear();
+    dref_parts.clear();
+    num_slices = 0;
+    first_sh = sh;
+    first_slice_type = (uint8_t)sh.slice_type;
+    in_pic = true;
+    return H264R_OK;
+}
+
+// the current picture is complete: records out, marking, DPB, output order
+int h264r_parser::finish_picture(bool last)
+{
+    if (!in_pic) return H264R_OK;
+    in_pic = false;
+    const SliceHeader &sh = first_sh;
+    const Sps &s = *active_sps;
+    // deblocking identity of every part: the last slice's lists
+    for (uint32_t off : dref_parts) {
+        h264r_part p;
+        memcpy(&p, &motion[off], sizeof(p));
+        for (int l = 0; l < 2; l++) {
+            const int ri = p.dref[l];
+            p.dref[l] = -1;
+            if (ri >= 0 && ri < (int)last_list[l].size() && last_list[l][ri]) p.dref[l] = (int8_t)last_list[l][ri]->slot;
+        }
+        memcpy(&motion[off], &p, sizeof(p));
+    }
+    // co-located motion for later direct prediction
+    const int n = (int)mbs.size();
+    auto mo = std::make_shared<Motion>();
+    mo->intra.resize(n);
+    mo->mv.resize((size_t)n * 2 * 16 * 2);
+    mo->ref.resize((size_t)n * 2 * 16);
+    mo->refpic.resize((size_t)n * 2 * 16);
+    for (int a = 0; a < n; a++) {
+        const MbState &m = mbs[a];
+        const bool inter = m.slice >= 0 && m.cls == H264R_MB_INTER;
+        mo->intra[a] = inter ? 0 : 1;
+        for (int l = 0; l < 2; l++)
+            for (int i = 0; i < 16; i++) {
+                const size_t o = (size_t)(a * 2 + l) * 16 + i;
+                mo->ref[o] = inter ? m.ref[l][i] : -1;
+                mo->mv[o * 2] = inter ? m.mv[l][i][0] : 0;
+                mo->mv[o * 2 + 1] = inter ? m.mv[l][i][1] : 0;
+                mo->refpic[o] = inter ? m.refpic[l][i] : -1;
+            }
+    }
+    cur.motion = mo;
+    // marking, then POC state for the next picture
+    if (sh.nal_ref_idc) {
+        const int rc = mark_references(sh, s);
+        if (rc) return rc;
+        prev_ref_mmco5 = cur.mmco5;
+        prev_ref_bottom_field = 0;
+        prev_ref_top_poc = cur.top_poc;
+        if (s.poc_type == 0) {
+            prev_poc_msb = cur.mmco5 ? 0 : pending_msb;
+            prev_poc_lsb = cur.mmco5 ? cur.top_poc : pending_lsb;
+        }
+    }
+    prev_mmco5 = cur.mmco5;
+    prev_frame_num_offset = frame_num_offset;
+    prev_frame_num = cur.mmco5 ? 0 : sh.frame_num;
+    // records out
+    Done d;
+    d.mbs.swap(rec);
+    d.slices.swap(rec_slices);
+    d.weights.swap(rec_weights);
+    d.motion.swap(motion);
+    d.coef.swap(coef);
+    d.pcm.swap(pcm);
+    memset(&d.pic, 0, sizeof(d.pic));
+    d.pic.width_mbs = (uint16_t)width_mbs;
+    d.pic.height_mbs = (uint16_t)height_mbs;
+    d.pic.structure = H264R_STRUCT_FRAME;
+    d.pic.mbaff = 0;
+    d.pic.dst_slot = (uint8_t)cur.slot;
+    d.pic.deblock = last ? 0 : 1;
+    const Pps &q = pps[sh.pps_id];
+    for (int i = 0; i < 6; i++) memcpy(d.pic.scaling4x4[i], q.sl4[i], 16);
+    for (int i = 0; i < 6; i++) memcpy(d.pic.scaling8x8[i], q.sl8[i], 64);
+    d.poc = cur.poc;
+    d.index = decoded++;
+    d.idr = (uint8_t)sh.idr;
+    d.reference = sh.nal_ref_idc != 0;
+    d.slice_type = first_slice_type;
+    // output order (CH264VideoDecoder::do_callback through the reorder buffer)
+    uint64_t outs[40];
+    int k = h264r_order_push(order, (uint64_t)cur.slot, cur.poc, sh.idr, outs, 40);
+    if (k < 0) return fail(k, "output order");
+    if (last) {
+        const int k2 = h264r_order_flush(order, outs + k, 40 - k);
+        if (k2 < 0) return fail(k2, "output order flush");
+        k += k2;
+    }
+    for (int i = 0; i < k; i++) {
+        const int sl = (int)outs[i];
+        d.out_slots.push_back((uint8_t)sl);
+        d.out_poc.push_back(slot_poc[sl]);
+        d.out_index.push_back(slot_index[sl]);
+    }
+    // the picture joins the DPB; free what is neither referenced nor held
+    dpb.push_back(cur);
+    for (auto it = dpb.begin(); it != dpb.end();) {
+        if (!it->is_ref() && !h264r_order_holds(order, (uint64_t)it->slot)) {
+            slot_uid[it->slot] = -1;
+            it = dpb.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    done.push_back(std::move(d));
+    return H264R_OK;
+}
+
+// ---------------------------------------------------------------- NAL units
+int h264r_parser::process_nal(const uint8_t *p, size_t n)
+{
+    if (n < 1) return H264R_OK;
+    const int nal_ref_idc = (p[0] >> 5) & 3, type = p[0] & 31;
+    nal_to_rbsp(p + 1, n - 1, rbsp);
+    BitReader br(rbsp.data(), rbsp.size());
+    const char *why = nullptr;
+    if (type == 7) {
+        Sps s;
+        const int rc = parse_sps(br, s, &why);
+        if (rc) return fail(rc, "SPS: %s", why ? why : "error");
+        if (active_sps && s.id == active_sps->id && (s.width_mbs != width_mbs || s.frame_height_mbs() != height_mbs))
+            return fail(H264R_ERR_UNSUPPORTED, "picture size change within the stream");
+        sps[s.id] = s;
+        return H264R_OK;
+    }
+    if (type == 8) {
+        Pps q;
+        const int rc = parse_pps(br, sps, q, &why);
+        if (rc) return fail(rc, "PPS: %s", why ? why : "error");
+        pps[q.id] = q;
+        return H264R_OK;
+    }
+    if (type == 2 || type == 3 || type == 4) return fail(H264R_ERR_UNSUPPORTED, "data partitioning");
+    if (type != 1 && type != 5) return H264R_OK;  // SEI, AUD, filler and others carry no picture data here
+    SliceCtx sc;
+    const int rc = parse_slice_header(br, type, nal_ref_idc, sps, pps, sc.sh, &why);
+    if (rc) return fail(rc, "slice header: %s", why ? why : "error");
+    sc.pps = &pps[sc.sh.pps_id];
+    sc.sps = &sps[sc.pps->sps_id];
+    if (sc.sh.redundant_pic_cnt > 0) return H264R_OK;  // redundant slices are not decoded
+    // first VCL NAL unit of a new primary picture (7.4.1.2.4)
+    bool first = !in_pic;
+    if (in_pic) {
+        const SliceHeader &a = first_sh;
+        const SliceHeader &b = sc.sh;
+        first = a.frame_num != b.frame_num || a.pps_id != b.pps_id || (a.nal_ref_idc == 0) != (b.nal_ref_idc == 0) ||
+                a.poc_lsb != b.poc_lsb || a.delta_poc_bottom != b.delta_poc_bottom || a.delta_poc[0] != b.delta_poc[0] ||
+                a.delta_poc[1] != b.delta_poc[1] || a.idr != b.idr || (a.idr && b.idr && a.idr_pic_id != b.idr_pic_id);
+    }
+    if (first) {
+        int r2 = finish_picture(false);
+        if (r2) return r2;
+        r2 = start_picture(sc.sh, *sc.sps, *sc.pps);
+        if (r2) return r2;
+    }
+    sc.index = num_slices++;
+    h264r_slice rs;
+    memset(&rs, 0, sizeof(rs));
+    rs.chroma_qp_offset[0] = (int8_t)sc.pps->chroma_qp_offset[0];
+    rs.chroma_qp_offset[1] = (int8_t)sc.pps->chroma_qp_offset[1];
+    rs.filter_offset_a = (int8_t)(sc.sh.alpha_offset_div2 * 2);
+    rs.filter_offset_b = (int8_t)(sc.sh.beta_offset_div2 * 2);
+    rs.disable_deblocking_filter_idc = (uint8_t)sc.sh.disable_deblocking_filter_idc;
+    rs.slice_type = (uint8_t)sc.sh.slice_type;
+    rec_slices.push_back(rs);
+    int r3 = build_lists(sc);
+    if (r3) return r3;
+    last_list[0] = sc.list[0];
+    last_list[1] = sc.list[1];
+    r3 = decode_slice(sc, br);
+    if (r3 == H264R_ERR_BAD_RECORD) {
+        // the reference skips the rest of a slice that fails to decode and
+        // goes on with the next one (H264VideoDecoder.cpp:136): its MBs
+        // from the failing one on stay undecoded
+        slice_errors++;
+        failed = false;
+        for (MbState &m : mbs)
+            if (m.slice == sc.index && rec[&m - mbs.data()].type == H264R_MB_NONE) m.slice = -1;
+        return H264R_OK;
+    }
+    return r3;
+}
+
+// ---------------------------------------------------------------- C API
+namespace {
+
+// start code positions in buf: returns the offset of the next 00 00 01 at or after `from`, or npos
+size_t find_start(const std::vector<uint8_t> &b, size_t from)
+{
+    for (size_t i = from; i + 2 < b.size(); i++)
+        if (b[i] == 0 && b[i + 1] == 0 && b[i + 2] == 1) return i;
+    return std::string::npos;
+}
+
+int drain(h264r_parser *p, bool at_end)
+{
+    size_t s = find_start(p->buf, 0);
+    if (s == std::string::npos) {
+        if (at_end) p->buf.clear();
+        return H264R_OK;
+    }
+    size_t consumed = s;
+    while (true) {
+        const size_t begin = s + 3;
+        size_t next = find_start(p->buf, begin);
+        size_t end;
+        if (next == std::string::npos) {
+            if (!at_end) break;
+            end = p->buf.size();
+        } else {
+            end = next;
+        }
+        // trailing zero bytes belong to the next start code (zero_byte) or are trailing_zero_8bits
+        size_t e = end;
+        while (e > begin && p->buf[e - 1] == 0) e--;
+        if (e > begin) {
+            const int rc = p->process_nal(p->buf.data() + begin, e - begin);
+            if (rc) return rc;
+        }
+        consumed = end;
+        if (next == std::string::npos) break;
+        s = next;
+    }
+    p->buf.erase(p->buf.begin(), p->buf.begin() + (ptrdiff_t)consumed);
+    return H264R_OK;
+}
+
+}  // namespace
+
+extern "C" int h264r_parser_create(h264r_parser **out)
+{
+    if (!out) return H264R_ERR_INVALID_ARG;
+    h264r_parser *p = new (std::nothrow) h264r_parser();
+    if (!p) return H264R_ERR_NO_MEMORY;
+    *out = p;
+    return H264R_OK;
+}
+
+extern "C" int h264r_parser_destroy(h264r_parser *p)
+{
+    if (!p) return H264R_ERR_INVALID_ARG;
+    delete p;
+    return H264R_OK;
+}
+
+extern "C" const char *h264r_parser_last_error(const h264r_parser *p) { return p ? p->err.c_str() : "null parser"; }
+
+extern "C" int h264r_parser_feed(h264r_parser *p, const uint8_t *data, size_t size)
+{
+    if (!p || (!data && size)) return H264R_ERR_INVALID_ARG;
+    if (p->failed) return H264R_ERR_BAD_RECORD;
+    if (p->ended) return p->fail(H264R_ERR_INVALID_ARG, "feed after end of stream");
+    p->buf.insert(p->buf.end(), data, data + size);
+    return drain(p, false);
+}
+
+extern "C" int h264r_parser_end(h264r_parser *p)
+{
+    if (!p) return H264R_ERR_INVALID_ARG;
+    if (p->failed) return H264R_ERR_BAD_RECORD;
+    if (p->ended) return H264R_OK;
+    int rc = drain(p, true);
+    if (rc) return rc;
+    p->ended = true;
+    return p->finish_picture(true);
+}
+
+extern "C" int h264r_parser_next(h264r_parser *p, h264r_parsed *out)
+{
+    if (!p || !out) return H264R_ERR_INVALID_ARG;
+    if (p->done.empty()) return p->failed ? H264R_ERR_BAD_RECORD : 0;
+    p->current_out = std::move(p->done.front());
+    p->done.pop_front();
+    h264r_parser::Done &d = p->current_out;
+    memset(out, 0, sizeof(*out));
+    out->pic = d.pic;
+    out->pic.num_slices = (uint16_t)d.slices.size();
+    out->pic.num_weights = (uint16_t)d.weights.size();
+    out->pic.num_mbs = (uint32_t)d.mbs.size();
+    out->pic.motion_bytes = (uint32_t)d.motion.size();
+    out->pic.coef_bytes = (uint32_t)d.coef.size();
+    out->pic.num_pcm = (uint32_t)(d.pcm.size() / 384);
+    out->pic.mbs = d.mbs.data();
+    out->pic.slices = d.slices.data();
+    out->pic.weights = d.weights.data();
+    out->pic.motion = d.motion.data();
+    out->pic.coef = d.coef.data();
+    out->pic.pcm = d.pcm.data();
+    out->poc = d.poc;
+    out->index = d.index;
+    out->idr = d.idr;
+    out->reference = d.reference;
+    out->slice_type = d.slice_type;
+    out->num_output = (uint32_t)d.out_slots.size();
+    out->output_slots = d.out_slots.data();
+    out->output_poc = d.out_poc.data();
+    out->output_index = d.out_index.data();
+    return 1;
+}
+
+extern "C" int h264r_parser_geometry(const h264r_parser *p, int *width_mbs, int *height_mbs, int *dpb_slots)
+{
+    if (!p) return H264R_ERR_INVALID_ARG;
+    if (width_mbs) *width_mbs = p->width_mbs;
+    if (height_mbs) *height_mbs = p->height_mbs;
+    if (dpb_slots) *dpb_slots = p->dpb_slots;
+    return H264R_OK;
+}

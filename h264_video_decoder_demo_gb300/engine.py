@@ -16,7 +16,7 @@ _LIB = None
 _LIB_LOCK = threading.Lock()
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libh264r.so")
 
-# every symbol include/h264r.h, h264r_synth.h, h264r_server.h and h264r_order.h declare
+# every symbol include/h264r.h, h264r_synth.h, h264r_server.h, h264r_order.h and h264r_parser.h declare
 EXPORTS = [
     "h264r_ctx_create", "h264r_ctx_destroy", "h264r_last_error", "h264r_stream_open",
     "h264r_stream_close", "h264r_stream_dpb_bytes", "h264r_submit_picture",
@@ -33,6 +33,9 @@ EXPORTS = [
     "h264r_order_holds", "h264r_order_infer_depth",
     "h264r_server_create", "h264r_server_destroy", "h264r_server_open", "h264r_server_push",
     "h264r_server_end", "h264r_server_poll", "h264r_server_pending", "h264r_server_get_stats",
+    "h264r_parser_create", "h264r_parser_destroy", "h264r_parser_last_error", "h264r_parser_feed",
+    "h264r_parser_end", "h264r_parser_next", "h264r_parser_geometry",
+    "h264r_probe_coeff_token", "h264r_probe_total_zeros", "h264r_probe_run_before", "h264r_probe_cbp",
 ]
 
 
@@ -109,6 +112,17 @@ def _load():
         "h264r_server_poll": (i32, [vp, P(R.CServerDone), i32, i32]),
         "h264r_server_pending": (i32, [vp, i32]),
         "h264r_server_get_stats": (i32, [vp, P(R.CServerStats)]),
+        "h264r_parser_create": (i32, [P(vp)]),
+        "h264r_parser_destroy": (i32, [vp]),
+        "h264r_parser_last_error": (ctypes.c_char_p, [vp]),
+        "h264r_parser_feed": (i32, [vp, vp, ctypes.c_size_t]),
+        "h264r_parser_end": (i32, [vp]),
+        "h264r_parser_next": (i32, [vp, P(R.CParsed)]),
+        "h264r_parser_geometry": (i32, [vp, P(i32), P(i32), P(i32)]),
+        "h264r_probe_coeff_token": (i32, [i32, ctypes.c_uint32, P(i32)]),
+        "h264r_probe_total_zeros": (i32, [i32, i32, ctypes.c_uint32, P(i32)]),
+        "h264r_probe_run_before": (i32, [i32, ctypes.c_uint32, P(i32)]),
+        "h264r_probe_cbp": (i32, [ctypes.c_uint32, i32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -325,6 +339,96 @@ class Order:
     def close(self):
         if self.h:
             lib().h264r_order_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Parser:
+    """Host-side front end (include/h264r_parser.h): Annex B bytes in,
+    completed pictures (records plus DPB slot and output list) out."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        rc = lib().h264r_parser_create(ctypes.byref(h))
+        if rc != 0:
+            raise EngineError(rc, "parser_create")
+        self.h = h
+        self._out = R.CParsed()
+
+    def _check(self, rc, what):
+        if rc < 0:
+            raise EngineError(rc, "%s: %s" % (what, lib().h264r_parser_last_error(self.h).decode()))
+        return rc
+
+    def feed(self, data):
+        buf = (ctypes.c_uint8 * len(data)).from_buffer_copy(data)
+        self._check(lib().h264r_parser_feed(self.h, buf, len(data)), "parser_feed")
+
+    def end(self):
+        self._check(lib().h264r_parser_end(self.h), "parser_end")
+
+    def geometry(self):
+        w, hh, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        lib().h264r_parser_geometry(self.h, ctypes.byref(w), ctypes.byref(hh), ctypes.byref(s))
+        return w.value, hh.value, s.value
+
+    def next(self):
+        """The next completed picture as (records.Picture, info dict), or None."""
+        rc = self._check(lib().h264r_parser_next(self.h, ctypes.byref(self._out)), "parser_next")
+        if rc == 0:
+            return None
+        o = self._out
+        c = o.pic
+        p = R.Picture()
+        p.width_mbs, p.height_mbs, p.structure, p.mbaff = c.width_mbs, c.height_mbs, c.structure, c.mbaff
+        p.dst_slot, p.deblock = c.dst_slot, c.deblock
+        p.scaling4x4 = np.frombuffer(bytes(c.scaling4x4), np.uint8).reshape(6, 16).copy()
+        p.scaling8x8 = np.frombuffer(bytes(c.scaling8x8), np.uint8).reshape(6, 64).copy()
+
+        def arr(ptr, n, dtype):
+            if n == 0 or not ptr:
+                return np.zeros(0, dtype)
+            nbytes = n * np.dtype(dtype).itemsize
+            return np.frombuffer(ctypes.string_at(ptr, nbytes), dtype).copy()
+
+        p.mbs = arr(c.mbs, c.num_mbs, R.MB_DTYPE)
+        p.slices = arr(c.slices, c.num_slices, R.SLICE_DTYPE)
+        p.weights = arr(c.weights, c.num_weights, R.WEIGHT_DTYPE)
+        p.motion = arr(c.motion, c.motion_bytes, np.uint8)
+        p.coef = arr(c.coef, c.coef_bytes, np.uint8)
+        p.pcm = arr(c.pcm, c.num_pcm * 384, np.uint8)
+        n = o.num_output
+        info = {"poc": o.poc, "index": o.index, "idr": bool(o.idr), "reference": bool(o.reference),
+                "slice_type": o.slice_type,
+                "output_slots": list(arr(o.output_slots, n, np.uint8)),
+                "output_poc": list(arr(o.output_poc, n, np.int32)),
+                "output_index": list(arr(o.output_index, n, np.uint32))}
+        return p, info
+
+    def pictures(self, data, chunk=1 << 20):
+        """Parse a whole byte stream; yields (Picture, info) in decoding order."""
+        for i in range(0, len(data), chunk):
+            self.feed(data[i:i + chunk])
+            while True:
+                r = self.next()
+                if r is None:
+                    break
+                yield r
+        self.end()
+        while True:
+            r = self.next()
+            if r is None:
+                break
+            yield r
+
+    def close(self):
+        if self.h:
+            lib().h264r_parser_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -48,6 +48,16 @@ class CPicture(ctypes.Structure):
                 ("coef", ctypes.c_void_p), ("pcm", ctypes.c_void_p)]
 
 
+
+class CParsed(ctypes.Structure):
+    """struct h264r_parsed (include/h264r_parser.h)"""
+    _fields_ = [("pic", CPicture), ("poc", ctypes.c_int32), ("index", ctypes.c_uint32),
+                ("idr", ctypes.c_uint8), ("reference", ctypes.c_uint8), ("slice_type", ctypes.c_uint8),
+                ("reserved", ctypes.c_uint8), ("num_output", ctypes.c_uint32),
+                ("output_slots", ctypes.c_void_p), ("output_poc", ctypes.c_void_p),
+                ("output_index", ctypes.c_void_p)]
+
+
 class Picture:
     """One picture's records in host memory (numpy arrays)."""
 
