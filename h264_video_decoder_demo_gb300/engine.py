@@ -16,7 +16,8 @@ _LIB = None
 _LIB_LOCK = threading.Lock()
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libh264r.so")
 
-# every symbol include/h264r.h, h264r_synth.h, h264r_server.h, h264r_order.h and h264r_parser.h declare
+# every symbol include/h264r.h, h264r_synth.h, h264r_server.h, h264r_order.h, h264r_parser.h and
+# h264r_decoder.h declare
 EXPORTS = [
     "h264r_ctx_create", "h264r_ctx_destroy", "h264r_last_error", "h264r_stream_open",
     "h264r_stream_close", "h264r_stream_dpb_bytes", "h264r_submit_picture",
@@ -36,6 +37,9 @@ EXPORTS = [
     "h264r_parser_create", "h264r_parser_destroy", "h264r_parser_last_error", "h264r_parser_feed",
     "h264r_parser_end", "h264r_parser_next", "h264r_parser_geometry",
     "h264r_probe_coeff_token", "h264r_probe_total_zeros", "h264r_probe_run_before", "h264r_probe_cbp",
+    "h264r_decoder_create", "h264r_decoder_destroy", "h264r_decoder_last_error", "h264r_decoder_set_callback",
+    "h264r_decoder_push", "h264r_decoder_flush", "h264r_decoder_open", "h264r_decoder_decoded",
+    "h264r_decoder_output",
 ]
 
 
@@ -123,6 +127,15 @@ def _load():
         "h264r_probe_total_zeros": (i32, [i32, i32, ctypes.c_uint32, P(i32)]),
         "h264r_probe_run_before": (i32, [i32, ctypes.c_uint32, P(i32)]),
         "h264r_probe_cbp": (i32, [ctypes.c_uint32, i32]),
+        "h264r_decoder_create": (i32, [vp, P(vp)]),
+        "h264r_decoder_destroy": (i32, [vp]),
+        "h264r_decoder_last_error": (ctypes.c_char_p, [vp]),
+        "h264r_decoder_set_callback": (i32, [vp, R.FRAME_CALLBACK, vp]),
+        "h264r_decoder_push": (i32, [vp, vp, ctypes.c_size_t]),
+        "h264r_decoder_flush": (i32, [vp]),
+        "h264r_decoder_open": (i32, [vp, ctypes.c_char_p]),
+        "h264r_decoder_decoded": (ctypes.c_uint32, [vp]),
+        "h264r_decoder_output": (ctypes.c_uint32, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -429,6 +442,70 @@ class Parser:
     def close(self):
         if self.h:
             lib().h264r_parser_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Decoder:
+    """Whole-stream decoding on the context's GPU (include/h264r_decoder.h):
+    on_frame(frame, error_code) is called per output picture in output order
+    (frame: dict with poc, decode_index, slice_type, width, height, planes =
+    one uint8 array Y|Cb|Cr copied out of the callback), then once with
+    frame None and H264R_DECODE_FILE_END.  A true return value stops the
+    decode, as the reference's callback convention has it."""
+
+    FILE_END, OPEN_FILE_FAILED = 1, 2
+
+    def __init__(self, ctx, on_frame):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        rc = lib().h264r_decoder_create(ctx.h, ctypes.byref(h))
+        if rc != 0:
+            raise EngineError(rc, "decoder_create")
+        self.h = h
+        self._user = on_frame
+
+        def trampoline(fp, user, code):
+            if not fp:
+                return int(bool(self._user(None, code)))
+            f = fp.contents
+            n = f.width * f.height * 3 // 2
+            planes = np.frombuffer(ctypes.string_at(f.y, n), np.uint8).copy()
+            info = {"poc": f.poc, "decode_index": f.decode_index, "slice_type": f.slice_type,
+                    "output_count": f.output_count, "width": f.width, "height": f.height, "planes": planes,
+                    "slot": f.slot}
+            return int(bool(self._user(info, code)))
+
+        self._cb = R.FRAME_CALLBACK(trampoline)
+        lib().h264r_decoder_set_callback(self.h, self._cb, None)
+
+    def _check(self, rc, what):
+        if rc < 0:
+            raise EngineError(rc, "%s: %s" % (what, lib().h264r_decoder_last_error(self.h).decode()))
+        return rc
+
+    def push(self, data):
+        buf = (ctypes.c_uint8 * len(data)).from_buffer_copy(data)
+        return self._check(lib().h264r_decoder_push(self.h, buf, len(data)), "decoder_push")
+
+    def flush(self):
+        return self._check(lib().h264r_decoder_flush(self.h), "decoder_flush")
+
+    def open(self, path):
+        return lib().h264r_decoder_open(self.h, path.encode())
+
+    @property
+    def decoded(self):
+        return lib().h264r_decoder_decoded(self.h)
+
+    def close(self):
+        if self.h:
+            lib().h264r_decoder_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -58,6 +58,19 @@ class CParsed(ctypes.Structure):
                 ("output_index", ctypes.c_void_p)]
 
 
+
+class CFrame(ctypes.Structure):
+    """struct h264r_frame (include/h264r_decoder.h)"""
+    _fields_ = [("y", ctypes.c_void_p), ("cb", ctypes.c_void_p), ("cr", ctypes.c_void_p),
+                ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("poc", ctypes.c_int32),
+                ("output_count", ctypes.c_int32), ("decode_index", ctypes.c_uint32),
+                ("slice_type", ctypes.c_uint8), ("reserved", ctypes.c_uint8 * 3),
+                ("slot", ctypes.c_int32), ("stream", ctypes.c_void_p)]
+
+
+FRAME_CALLBACK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(CFrame), ctypes.c_void_p, ctypes.c_int)
+
+
 class Picture:
     """One picture's records in host memory (numpy arrays)."""
 

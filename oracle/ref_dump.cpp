@@ -16,7 +16,8 @@
  * The records are what the GPU engine consumes; the planes are the golden
  * outputs its oracle and kernels must reproduce byte for byte.
  *
- * Usage: ref_dump <in.h264> <out.dmp> [max_pictures] [--no-planes]
+ * Usage: ref_dump <in.h264> <out.dmp> [max_pictures] [--no-planes] [--bmp <dir>]
+ *                 [--order <file>] [--yuv <file>] (--yuv: every output picture's planes)
  * Test infrastructure only; never part of the engine.
  */
 #include <cstdio>
@@ -40,6 +41,7 @@ static int g_max_pictures = 1 << 30;
 static int g_write_planes = 1;
 static const char *g_bmp_dir = NULL;  // --bmp: the reference's BMP of every dumped picture
 static FILE *g_order = NULL;         // --order: decoding order (POC, IdrPicFlag, reorder depth) and output order
+static FILE *g_yuv = NULL;           // --yuv: every output picture's planes, in output order
 static int g_unsupported = 0;
 static int g_verbose = 1;
 
@@ -424,13 +426,19 @@ static int on_frame(CH264Picture *out, void *user, int err)
     (void)err;
     if (out == NULL) return -1;
     if (g_order) fprintf(g_order, "O %d\n", out->m_picture_frame.PicOrderCnt);
+    if (g_yuv) {
+        const CH264PictureBase &f = out->m_picture_frame;
+        fwrite(f.m_pic_buff_luma, 1, (size_t)f.PicWidthInSamplesL * f.PicHeightInSamplesL, g_yuv);
+        fwrite(f.m_pic_buff_cb, 1, (size_t)f.PicWidthInSamplesC * f.PicHeightInSamplesC, g_yuv);
+        fwrite(f.m_pic_buff_cr, 1, (size_t)f.PicWidthInSamplesC * f.PicHeightInSamplesC, g_yuv);
+    }
     return (g_pictures >= g_max_pictures) ? -1 : 0;
 }
 
 int main(int argc, char **argv)
 {
     if (argc < 3) {
-        fprintf(stderr, "usage: %s <in.h264> <out.dmp> [max_pictures] [--no-planes] [--bmp <dir>] [--order <file>]\n", argv[0]);
+        fprintf(stderr, "usage: %s <in.h264> <out.dmp> [max_pictures] [--no-planes] [--bmp <dir>] [--order <file>] [--yuv <file>]\n", argv[0]);
         return 2;
     }
     for (int i = 3; i < argc; i++) {
@@ -439,6 +447,10 @@ int main(int argc, char **argv)
         else if (strcmp(argv[i], "--order") == 0 && i + 1 < argc) {
             g_order = fopen(argv[++i], "w");
             if (!g_order) { perror("fopen"); return 1; }
+        }
+        else if (strcmp(argv[i], "--yuv") == 0 && i + 1 < argc) {
+            g_yuv = fopen(argv[++i], "wb");
+            if (!g_yuv) { perror("fopen"); return 1; }
         }
         else g_max_pictures = atoi(argv[i]);
     }
@@ -454,6 +466,7 @@ int main(int argc, char **argv)
     dec.open(argv[1]);
     fclose(g_out);
     if (g_order) fclose(g_order);
+    if (g_yuv) fclose(g_yuv);
     fprintf(stderr, "ref_dump: %d pictures, unsupported-flags=0x%x\n", g_pictures, g_unsupported);
     return g_unsupported ? 3 : 0;
 }

@@ -14,7 +14,14 @@ the first pictures of each stream, in decoding order from the IDR:
                     depth of the SPS) and the POCs in the order its output
                     callback receives them
 
-Usage: python tests/golden/make_fixtures.py [--ref-data DIR]
+  <name>.h264       for the two CAVLC streams: the stream cut before the first
+                    slice of picture N (parameter sets included), with
+  <name>.frames.json  every picture the reference outputs for that cut stream,
+                    in output order: POC, md5 of its planes (ref_dump --yuv) and
+                    md5 of the BMP the reference's own main.cpp writes for it
+                    (oracle/_ref/h264dec)
+
+Usage: python tests/golden/make_fixtures.py [--ref-data DIR] [--bitstreams-only]
 The fixtures are committed; this script needs the reference sources and is
 only run where they are present.
 """
@@ -90,15 +97,72 @@ def make_order_fixture(dumper, ref_data, tmp):
     print("output_order.json:", {k: len(v["output"]) for k, v in fixture.items()})
 
 
+# (fixture name, stream file, pictures kept)
+BITSTREAMS = [
+    ("gop121_cavlc_4pics", "gop121.naluCnt453.h264", 4),
+    ("heavyhand_cavlc_b4_6pics", "HeavyHand_1080p.B_frames_4.no_cabac.no_tff.h264", 6),
+]
+
+
+def cut_stream(data, pictures):
+    """The bytes before the start code of the first slice of picture `pictures`."""
+    i, n = 0, 0
+    while True:
+        j = data.find(b"\x00\x00\x01", i)
+        if j < 0:
+            return data
+        t = data[j + 3] & 31
+        if t in (1, 5) and (data[j + 4] & 0x80):  # first_mb_in_slice == 0
+            if n == pictures:
+                while j > 0 and data[j - 1] == 0:  # the start code's zero_byte
+                    j -= 1
+                return data[:j]
+            n += 1
+        i = j + 3
+
+
+def make_bitstream_fixtures(ref_data, tmp):
+    dumper = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
+    h264dec = os.path.join(ROOT, "oracle", "_ref", "h264dec")
+    for name, stream, n in BITSTREAMS:
+        with open(os.path.join(ref_data, stream), "rb") as f:
+            cut = cut_stream(f.read(), n)
+        path = os.path.join(HERE, name + ".h264")
+        with open(path, "wb") as f:
+            f.write(cut)
+        yuv = os.path.join(tmp, name + ".yuv")
+        order = os.path.join(tmp, name + ".order")
+        subprocess.run([dumper, path, os.path.join(tmp, name + ".dmp"), "100000", "--no-planes", "--yuv", yuv,
+                        "--order", order], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, check=True)
+        bmp_dir = os.path.join(tmp, name + "_bmp")
+        os.makedirs(bmp_dir)
+        subprocess.run([h264dec, path, bmp_dir], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        pocs = [int(l.split()[1]) for l in open(order) if l.startswith("O ")]
+        with open(yuv, "rb") as f:
+            raw = f.read()
+        frame = 1920 * 1088 * 3 // 2
+        assert len(raw) == frame * len(pocs), (len(raw), len(pocs))
+        frames = []
+        for k, poc in enumerate(pocs):
+            with open(os.path.join(bmp_dir, "out_1920x1088.%d.bmp" % k), "rb") as f:
+                bmp = hashlib.md5(f.read()).hexdigest()
+            frames.append({"poc": poc, "yuv_md5": hashlib.md5(raw[k * frame:(k + 1) * frame]).hexdigest(),
+                           "bmp_md5": bmp})
+        with open(os.path.join(HERE, name + ".frames.json"), "w") as f:
+            json.dump({"stream": stream, "pictures": n, "width": 1920, "height": 1088, "frames": frames}, f, indent=1)
+        print(name, len(cut), "bytes", len(frames), "frames")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-data", default="/root/reference/data")
+    ap.add_argument("--bitstreams-only", action="store_true", help="only the cut streams and their frame md5s")
     args = ap.parse_args()
     dumper = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
     if not os.path.exists(dumper):
         subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"])
     with tempfile.TemporaryDirectory(dir=os.path.join(ROOT, "_work") if os.path.isdir(os.path.join(ROOT, "_work")) else None) as tmp:
-        for name, stream, n, tools in FIXTURES:
+        for name, stream, n, tools in ([] if args.bitstreams_only else FIXTURES):
             dmp = os.path.join(tmp, name + ".dmp")
             bmp_dir = os.path.join(tmp, name + "_bmp")
             os.makedirs(bmp_dir)
@@ -118,7 +182,9 @@ def main():
             with open(os.path.join(HERE, name + ".json"), "w") as f:
                 json.dump(meta, f, indent=1)
             print(name, len(pics), "pictures")
-        make_order_fixture(dumper, args.ref_data, tmp)
+        if not args.bitstreams_only:
+            make_order_fixture(dumper, args.ref_data, tmp)
+        make_bitstream_fixtures(args.ref_data, tmp)
 
 
 if __name__ == "__main__":

@@ -185,3 +185,72 @@ def test_unsupported_tools_are_reported(lib):
         p.feed(nal(0x68, pps))  # a unit is parsed once the next start code or the end arrives
         p.end()
     assert ei.value.code == -3 and "CABAC" in str(ei.value)
+
+
+# ---- committed cut streams (tests/golden/*.h264): no reference needed
+
+BITSTREAMS = ["gop121_cavlc_4pics", "heavyhand_cavlc_b4_6pics"]
+
+
+def _golden_stream(name):
+    with open(os.path.join(HERE, "golden", name + ".h264"), "rb") as f:
+        data = f.read()
+    with open(os.path.join(HERE, "golden", name + ".frames.json")) as f:
+        return data, json.load(f)
+
+
+@pytest.mark.parametrize("name", BITSTREAMS)
+def test_cut_streams_reconstruct_to_reference_frames(lib, name):
+    """Parser records reconstructed by the CPU oracle give the reference's
+    output pictures (planes md5, output order), the last one undeblocked."""
+    import hashlib
+    from h264_video_decoder_demo_gb300.engine import Parser
+    from oracle_cpu import OracleDPB
+    data, meta = _golden_stream(name)
+    dpb, got = None, []
+    for pic, info in Parser().pictures(data):
+        if dpb is None:
+            dpb = OracleDPB(pic.width_mbs, pic.height_mbs)
+        rc, _ = dpb.reconstruct(pic)
+        assert rc == 0
+        for s, poc in zip(info["output_slots"], info["output_poc"]):
+            got.append((int(poc), hashlib.md5(dpb.planes(int(s)).tobytes()).hexdigest()))
+    assert got == [(f["poc"], f["yuv_md5"]) for f in meta["frames"]]
+
+
+@pytest.mark.parametrize("name", BITSTREAMS)
+def test_parsing_does_not_depend_on_chunking(lib, name):
+    from h264_video_decoder_demo_gb300.engine import Parser
+    data, _ = _golden_stream(name)
+    whole = [(p.mbs.tobytes(), p.motion.tobytes(), p.coef.tobytes(), i["output_slots"]) for p, i in Parser().pictures(data)]
+    for chunk in (1, 7, 4093):
+        got = [(p.mbs.tobytes(), p.motion.tobytes(), p.coef.tobytes(), i["output_slots"])
+               for p, i in Parser().pictures(data, chunk=chunk)]
+        assert got == whole
+
+
+def _compat_build(src, out):
+    from h264_video_decoder_demo_gb300 import build
+    lib_dir = os.path.dirname(build.LIB)
+    cmd = ["g++", "-std=c++11", "-O1", "-I", os.path.join(ROOT, "include", "compat"), src, "-o", out,
+           "-L" + lib_dir, "-lh264r", "-Wl,-rpath," + lib_dir]
+    return subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+
+
+def test_compat_program_builds(lib, tmp_path):
+    r = _compat_build(os.path.join(HERE, "compat", "compat_main.cpp"), str(tmp_path / "compat_main"))
+    assert r.returncode == 0, r.stdout
+
+
+def test_reference_main_builds_against_compat_headers(lib, tmp_path):
+    """The reference's own main.cpp compiles unchanged against
+    include/compat and links with libh264r.so (drop-in interface)."""
+    if not os.path.exists(os.path.join(REF_SRC, "main.cpp")):
+        pytest.skip("reference sources not present")
+    # a copy away from the reference's own headers (#include "..." looks in
+    # the including file's directory first), as a user's program would be
+    import shutil
+    src = str(tmp_path / "main.cpp")
+    shutil.copy(os.path.join(REF_SRC, "main.cpp"), src)
+    r = _compat_build(src, str(tmp_path / "ref_main"))
+    assert r.returncode == 0, r.stdout
