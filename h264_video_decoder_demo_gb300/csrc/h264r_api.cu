@@ -25,6 +25,7 @@ __global__ void k_inter(const PicDesc *__restrict__ pics, int npics, uint32_t to
 __global__ void k_intra(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st);
 __global__ void k_bs(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
 __global__ void k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st);
+__global__ void k_deblock_frame(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st);
 __global__ void k_bgr24(const uint8_t *__restrict__ yuv, int W, int H, uint8_t *__restrict__ out, int row_bytes, int flip);
 }  // namespace h264r
 
@@ -547,7 +548,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
     }
     memset(b.host, 0, total);
     PicDesc *d = (PicDesc *)b.host;
-    uint64_t mb_base = 0, row_base = 0, prog = 0, db_base = 0;
+    uint64_t mb_base = 0, row_base = 0, prog = 0, db_base = 0, dbf_base = 0;
     for (int i = 0; i < n; i++) {
         const h264r_picture *pic = items[i].pic;
         h264r_stream *s = items[i].s;
@@ -588,6 +589,9 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
         p.db_units = h264r::deblock_units(p.mbaff, p.units_h);
         p.db_base = (uint32_t)db_base;
         db_base += p.db_units;
+        p.dbf_units = h264r::deblock_frame_units(p.mbaff, p.units_h);
+        p.dbf_base = (uint32_t)dbf_base;
+        dbf_base += p.dbf_units;
         p.deblock_stop = 0xFFFFFFFFu;
         mb_base += pic->num_mbs;
         row_base += p.units_h;
@@ -614,8 +618,15 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
     if (ctx->timing) cudaEventRecord(ev[2], cs);
     if (any_deblock) {
         h264r::k_bs<<<(unsigned)((mbs + 3) / 4), 128, 0, cs>>>(dd, n, (uint32_t)mbs, st);
-        h264r::k_deblock<<<(unsigned)db_base, 32, 0, cs>>>(dd, n, (uint32_t)db_base, st);
-        ctx->launches += 2;
+        ctx->launches++;
+        if (dbf_base) {
+            h264r::k_deblock_frame<<<(unsigned)dbf_base, 32 * h264r::kDbWarps, 0, cs>>>(dd, n, (uint32_t)dbf_base, st);
+            ctx->launches++;
+        }
+        if (db_base) {
+            h264r::k_deblock<<<(unsigned)db_base, 32, 0, cs>>>(dd, n, (uint32_t)db_base, st);
+            ctx->launches++;
+        }
     }
     if (ctx->timing) cudaEventRecord(ev[3], cs);
     cudaError_t e = cudaGetLastError();

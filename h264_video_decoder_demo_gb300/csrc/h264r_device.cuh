@@ -84,19 +84,28 @@ struct PicDesc {
     uint32_t mb_base;        // first global MB index of this picture in the batch
     uint32_t row_base;       // first global unit row of this picture in the batch
     uint32_t units_w, units_h;  // wavefront grid: MBs (or MB pairs) per row, rows
-    uint32_t db_base, db_units; // first deblocking ticket of this picture in the batch, ticket count
+    uint32_t db_base, db_units; // MBAFF deblocking: first ticket of this picture in the batch, ticket count
+    uint32_t dbf_base, dbf_units; // frame deblocking: first block ticket, block count
     uint32_t deblock_stop;   // first failing bS derivation key (0xFFFFFFFF: none)
 };
 
-// Deblocking tickets of a picture: frame pictures give one ticket to the
-// luma and one to the chroma warp of every pair of MB rows; MBAFF pictures
-// one per MB-pair row.
-__host__ __device__ inline uint32_t deblock_units(int mbaff, uint32_t units_h) { return mbaff ? 2u * units_h : 2u * ((units_h + 1u) / 2u); }
+// Deblocking tickets of a picture.  Frame pictures (k_deblock_frame): one
+// block ticket for the luma and one for the chroma of every kDbWarps pairs
+// of MB rows, a warp per pair.  MBAFF pictures (k_deblock): one warp ticket
+// for the luma and one for the chroma of every MB-pair row.
+constexpr int kDbWarps = 4;   // MB-row pairs (warps) per frame deblocking block
+constexpr int kDbXRing = 16;  // MBs of a warp's bottom lines kept for the warp below
+__host__ __device__ inline uint32_t deblock_units(int mbaff, uint32_t units_h) { return mbaff ? 2u * units_h : 0u; }
+__host__ __device__ inline uint32_t deblock_frame_units(int mbaff, uint32_t units_h)
+{
+    const uint32_t pairs = (units_h + 1u) / 2u;
+    return mbaff ? 0u : 2u * ((pairs + kDbWarps - 1u) / kDbWarps);
+}
 
 // Engine-wide device state for one launch.
 struct LaunchState {
     int *error;              // first error code (0 ok)
-    unsigned int *ticket;    // wavefront row tickets [2]
+    unsigned int *ticket;    // wavefront tickets: [0] k_intra, [1] k_deblock, [2] k_deblock_frame
     unsigned long long spin_limit;
 };
 

@@ -51,6 +51,19 @@ __device__ __forceinline__ int find_pic_by_db(const PicDesc *pics, int npics, ui
     return lo;
 }
 
+// last picture whose first frame-deblocking block is <= g (pictures without
+// frame blocks share the next picture's base and are skipped by "last")
+__device__ __forceinline__ int find_pic_by_dbf(const PicDesc *pics, int npics, uint32_t g)
+{
+    int lo = 0, hi = npics - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pics[mid].dbf_base <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 __device__ __forceinline__ void set_error(const LaunchState &st, int code) { atomicCAS(st.error, 0, code); }
 
 __device__ __forceinline__ uint32_t pack4(int a, int b, int c, int d)
@@ -1712,6 +1725,51 @@ struct DbChromaSmem {
     uint2 ring[3][2][4];                   // first row: rows 4..7, per plane
 };
 
+// A frame deblocking block: kDbWarps warps on consecutive MB-row pairs of one
+// plane.  A warp's first row takes the rows above from the warp before it
+// through shared memory (x: that warp's second row's bottom lines, kDbXRing
+// MBs deep) and waits on its shared-memory progress (done); only the block's
+// first warp waits on, and reads, global memory, and only its last warp
+// publishes global progress.  used is the consumer's progress, which keeps a
+// producer from overwriting lines not yet taken.
+struct DbFrameShared {
+    union {
+        DbLumaSmem l[kDbWarps];
+        DbChromaSmem c[kDbWarps];
+    } w;
+    union {
+        uint4 l[kDbWarps - 1][kDbXRing][4];     // luma rows 12..15
+        uint2 c[kDbWarps - 1][kDbXRing][2][4];  // chroma rows 4..7 per plane
+    } x;
+    int done[kDbWarps];  // second row: MBs completed
+    int used[kDbWarps];  // first row: MBs whose rows above were taken
+};
+
+// Wait (whole warp) until the shared-memory counter *flag >= target, with
+// the last value seen cached; bounded like the global waits.
+__device__ __forceinline__ bool cta_wait(const LaunchState &st, const int *flag, int target, int &seen)
+{
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0 && seen < target) {
+        unsigned long long n = 0;
+        while ((seen = *(const volatile int *)flag) < target) {
+            if (++n > st.spin_limit) {
+                set_error(st, H264R_ERR_DEVICE_TIMEOUT);
+                ok = 0;
+                break;
+            }
+            if ((n & 255) == 0 && *(volatile int *)st.error != 0) {
+                ok = 0;
+                break;
+            }
+        }
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __syncwarp();
+    __threadfence_block();
+    return ok != 0;
+}
+
 __device__ __forceinline__ int db_tc0(uint32_t prm, int bS) { return (prm >> (11 + 5 * bS)) & 31; }
 
 // 8.7.2.3 / 8.7.2.4 on the luma line v with q0 at index Q
@@ -1771,7 +1829,8 @@ __device__ __forceinline__ void db_chroma(int (&v)[N], int bS, uint32_t prm)
     v[Q] = clip1(q0 - delta);
 }
 
-__device__ void deblock_pair_luma(const PicDesc &p, int pair, DbLumaSmem &s, const LaunchState &st)
+__device__ void deblock_pair_luma(const PicDesc &p, int pair, int wi, int nw, DbLumaSmem &s, DbFrameShared &S,
+                                  const LaunchState &st)
 {
     const int lane = threadIdx.x & 31;
     const int h = lane >> 4, k = lane & 15;
@@ -1780,12 +1839,14 @@ __device__ void deblock_pair_luma(const PicDesc &p, int pair, DbLumaSmem &s, con
     const bool row_ok = row < rows;
     const bool has_second = 2 * pair + 1 < rows;
     const int steps = has_second ? uw + 2 : uw;
+    const bool from_cta = wi > 0;                  // rows above from the warp before, in shared memory
+    const bool to_cta = wi + 1 < nw && has_second;  // bottom lines to the warp after
     int *prog = p.progress + p.units_h;
     uint8_t *Y = plane_y(p);
     uint8_t(*t)[16] = s.t[h];
     const uint32_t stop = p.deblock_stop;
     int left[4] = {0, 0, 0, 0};
-    int seen = 0;
+    int seen = 0, seen_used = 0;
     // prefetched per MB: the lane's line, its strengths (byte e: edge e), the thresholds
     uint4 nl = make_uint4(0, 0, 0, 0), npl = nl;
     uint32_t nlv = 0, nlh = 0;
@@ -1804,6 +1865,8 @@ __device__ void deblock_pair_luma(const PicDesc &p, int pair, DbLumaSmem &s, con
         const uint4 line = nl, prm = npl;
         uint32_t lv = nlv, lh = nlh;
         if (row_ok && u + 1 >= 0 && u + 1 < uw) fetch(u + 1);
+        // the warp after must have taken the lines this step overwrites
+        if (to_cta && step >= 2 && !cta_wait(st, &S.used[wi + 1], min(step - 1 - kDbXRing, uw), seen_used)) return;
         const int x0 = u * 16, y0 = row * 16;
         if (act) {
             const int cur = row * uw + u;
@@ -1830,13 +1893,20 @@ __device__ void deblock_pair_luma(const PicDesc &p, int pair, DbLumaSmem &s, con
                 const uint32_t lw = pack4(v[0], v[1], v[2], v[3]);
                 *(uint32_t *)(Y + (size_t)(y0 + k) * W + x0 - 4) = lw;
                 if (h == 0 && k >= 12) s.ring[(u - 1) % 3][k - 12].w = lw;
+                if (h == 1 && to_cta && k >= 12) S.x.l[wi][(u - 1) % kDbXRing][k - 12].w = lw;
             }
             *(uint4 *)&t[k + 4][0] = pack16(&v[4]);
         }
         // ---- the row above: final once its warp is two MBs ahead
-        if (2 * pair > 0 && step < uw && !db_wait(st, prog + 2 * pair - 1, min(step + 2, uw), seen)) return;
+        if (2 * pair > 0 && step < uw) {
+            const bool ok = from_cta ? cta_wait(st, &S.done[wi - 1], min(step + 2, uw), seen)
+                                     : db_wait(st, prog + 2 * pair - 1, min(step + 2, uw), seen);
+            if (!ok) return;
+        }
         if (act && row > 0 && k < 4)
-            *(uint4 *)&t[k][0] = h == 0 ? __ldcg((const uint4 *)(Y + (size_t)(y0 - 4 + k) * W + x0)) : s.ring[u % 3][k];
+            *(uint4 *)&t[k][0] = h == 1 ? s.ring[u % 3][k]
+                                        : (from_cta ? S.x.l[wi - 1][u % kDbXRing][k]
+                                                    : __ldcg((const uint4 *)(Y + (size_t)(y0 - 4 + k) * W + x0)));
         __syncwarp();
         // ---- horizontal edges: the lane owns a column
         if (act) {
@@ -1858,14 +1928,27 @@ __device__ void deblock_pair_luma(const PicDesc &p, int pair, DbLumaSmem &s, con
 #pragma unroll
             for (int i = 0; i < 4; i++) left[i] = (lr.w >> (8 * i)) & 255;
             if (h == 0 && k >= 12) s.ring[u % 3][k - 12] = lr;
+            if (h == 1 && to_cta && k >= 12) S.x.l[wi][u % kDbXRing][k - 12] = lr;
             if (row > 0 && k < 3) *(uint4 *)(Y + (size_t)(y0 - 3 + k) * W + x0) = *(const uint4 *)&t[1 + k][0];
         }
         __syncwarp();
-        if (lane == 0 && has_second && step >= 2) st_release(prog + 2 * pair + 1, step - 1);
+        if (has_second && step >= 2) {
+            if (to_cta) {
+                __threadfence_block();
+                if (lane == 0) *(volatile int *)&S.done[wi] = step - 1;
+            } else if (lane == 0) {
+                st_release(prog + 2 * pair + 1, step - 1);
+            }
+        }
+        if (from_cta && step < uw) {
+            __threadfence_block();
+            if (lane == 0) *(volatile int *)&S.used[wi] = step + 1;
+        }
     }
 }
 
-__device__ void deblock_pair_chroma(const PicDesc &p, int pair, DbChromaSmem &s, const LaunchState &st)
+__device__ void deblock_pair_chroma(const PicDesc &p, int pair, int wi, int nw, DbChromaSmem &s, DbFrameShared &S,
+                                    const LaunchState &st)
 {
     const int lane = threadIdx.x & 31;
     const int h = lane >> 4, k = lane & 15, comp = k >> 3, ck = k & 7;
@@ -1874,12 +1957,14 @@ __device__ void deblock_pair_chroma(const PicDesc &p, int pair, DbChromaSmem &s,
     const bool row_ok = row < rows;
     const bool has_second = 2 * pair + 1 < rows;
     const int steps = has_second ? uw + 2 : uw;
+    const bool from_cta = wi > 0;
+    const bool to_cta = wi + 1 < nw && has_second;
     int *prog = p.progress + p.units_h;
     uint8_t *C = plane_c(p, comp);
     uint8_t(*t)[8] = s.t[h][comp];
     const uint32_t stop = p.deblock_stop;
     int left[4] = {0, 0, 0, 0};
-    int seen = 0;
+    int seen = 0, seen_used = 0;
     uint2 nl = make_uint2(0, 0);
     uint4 npc = make_uint4(0, 0, 0, 0);
     uint32_t ncv = 0, nch = 0;
@@ -1899,6 +1984,7 @@ __device__ void deblock_pair_chroma(const PicDesc &p, int pair, DbChromaSmem &s,
         const uint4 prm = npc;
         uint32_t cv = ncv, ch = nch;
         if (row_ok && u + 1 >= 0 && u + 1 < uw) fetch(u + 1);
+        if (to_cta && step >= 2 && !cta_wait(st, &S.used[wi + 1], min(step - 1 - kDbXRing, uw), seen_used)) return;
         const int x0 = u * 8, y0 = row * 8;
         if (act) {
             const int cur = row * uw + u;
@@ -1922,12 +2008,19 @@ __device__ void deblock_pair_chroma(const PicDesc &p, int pair, DbChromaSmem &s,
                 const uint32_t cw = pack4(w[0], w[1], w[2], w[3]);
                 *(uint32_t *)(C + (size_t)(y0 + ck) * Wc + x0 - 4) = cw;
                 if (h == 0 && ck >= 4) s.ring[(u - 1) % 3][comp][ck - 4].y = cw;
+                if (h == 1 && to_cta && ck >= 4) S.x.c[wi][(u - 1) % kDbXRing][comp][ck - 4].y = cw;
             }
             *(uint2 *)&t[ck + 4][0] = pack8(&w[4]);
         }
-        if (2 * pair > 0 && step < uw && !db_wait(st, prog + 2 * pair - 2, min(step + 2, uw), seen)) return;
+        if (2 * pair > 0 && step < uw) {
+            const bool ok = from_cta ? cta_wait(st, &S.done[wi - 1], min(step + 2, uw), seen)
+                                     : db_wait(st, prog + 2 * pair - 2, min(step + 2, uw), seen);
+            if (!ok) return;
+        }
         if (act && row > 0 && ck < 4)
-            *(uint2 *)&t[ck][0] = h == 0 ? __ldcg((const uint2 *)(C + (size_t)(y0 - 4 + ck) * Wc + x0)) : s.ring[u % 3][comp][ck];
+            *(uint2 *)&t[ck][0] = h == 1 ? s.ring[u % 3][comp][ck]
+                                         : (from_cta ? S.x.c[wi - 1][u % kDbXRing][comp][ck]
+                                                     : __ldcg((const uint2 *)(C + (size_t)(y0 - 4 + ck) * Wc + x0)));
         __syncwarp();
         if (act) {
             int w[12];
@@ -1947,10 +2040,22 @@ __device__ void deblock_pair_chroma(const PicDesc &p, int pair, DbChromaSmem &s,
 #pragma unroll
             for (int i = 0; i < 4; i++) left[i] = (cr.y >> (8 * i)) & 255;
             if (h == 0 && ck >= 4) s.ring[u % 3][comp][ck - 4] = cr;
+            if (h == 1 && to_cta && ck >= 4) S.x.c[wi][u % kDbXRing][comp][ck - 4] = cr;
             if (row > 0 && ck < 3) *(uint2 *)(C + (size_t)(y0 - 3 + ck) * Wc + x0) = *(const uint2 *)&t[1 + ck][0];
         }
         __syncwarp();
-        if (lane == 0 && has_second && step >= 2) st_release(prog + 2 * pair, step - 1);
+        if (has_second && step >= 2) {
+            if (to_cta) {
+                __threadfence_block();
+                if (lane == 0) *(volatile int *)&S.done[wi] = step - 1;
+            } else if (lane == 0) {
+                st_release(prog + 2 * pair, step - 1);
+            }
+        }
+        if (from_cta && step < uw) {
+            __threadfence_block();
+            if (lane == 0) *(volatile int *)&S.used[wi] = step + 1;
+        }
     }
 }
 
@@ -1968,20 +2073,40 @@ __global__ void __launch_bounds__(32, 28) k_deblock(const PicDesc *__restrict__ 
     if (!p.deblock) return;
     const int unit = (int)(g - p.db_base);
     __shared__ union {
-        DbLumaSmem l;
-        DbChromaSmem c;
         uint32_t ml[200];
         uint32_t mc[144];
     } db_smem;
-    if (!p.mbaff) {
-        // even tickets: luma of MB-row pair unit/2; odd: its chroma
-        if ((unit & 1) == 0) deblock_pair_luma(p, unit >> 1, db_smem.l, st);
-        else deblock_pair_chroma(p, unit >> 1, db_smem.c, st);
-        return;
-    }
+    if (!p.mbaff) return;  // frame pictures have no k_deblock tickets (k_deblock_frame)
     // MBAFF: even tickets luma of pair row unit/2, odd ones its chroma
     if ((unit & 1) == 0) mbaff_luma_row(p, unit >> 1, db_smem.ml, st);
     else mbaff_chroma_row(p, unit >> 1, db_smem.mc, st);
+}
+
+// Frame pictures: a block of kDbWarps warps per kDbWarps MB-row pairs of one
+// plane (even block tickets luma, odd ones chroma); see DbFrameShared.
+__global__ void __launch_bounds__(32 * kDbWarps, 28 / kDbWarps) k_deblock_frame(const PicDesc *__restrict__ pics, int npics,
+                                                                              uint32_t total_units, LaunchState st)
+{
+    __shared__ DbFrameShared S;
+    __shared__ uint32_t s_unit;
+    if (threadIdx.x == 0) s_unit = atomicAdd(&st.ticket[2], 1u);
+    if (threadIdx.x < kDbWarps) {
+        S.done[threadIdx.x] = 0;
+        S.used[threadIdx.x] = 0;
+    }
+    __syncthreads();
+    const uint32_t g = s_unit;
+    if (g >= total_units) return;
+    const int pi = find_pic_by_dbf(pics, npics, g);
+    const PicDesc p = pics[pi];
+    if (!p.deblock || p.mbaff) return;
+    const int unit = (int)(g - p.dbf_base);
+    const int wi = threadIdx.x >> 5;
+    const int first = (unit >> 1) * kDbWarps, pairs = ((int)p.units_h + 1) / 2;
+    const int nw = min(kDbWarps, pairs - first);
+    if (wi >= nw) return;
+    if ((unit & 1) == 0) deblock_pair_luma(p, first + wi, wi, nw, S.w.l[wi], S, st);
+    else deblock_pair_chroma(p, first + wi, wi, nw, S.w.c[wi], S, st);
 }
 
 // ======================================================================

@@ -21,6 +21,7 @@
 namespace h264r {
 __global__ void k_bs(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
 __global__ void k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st);
+__global__ void k_deblock_frame(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st);
 }  // namespace h264r
 
 using h264r::PicDesc;
@@ -35,7 +36,7 @@ constexpr unsigned long long kNoAllocSpinLimit = 1ull << 25;
 struct NoAllocScratch {
     PicDesc desc;                             // descriptor the kernels read
     int error;                                // device error word of the call
-    unsigned int ticket[2];                   // wavefront row tickets
+    unsigned int ticket[3];                   // wavefront tickets
     int progress[3 * kNoAllocMaxRows];        // wavefront progress counters
     alignas(256) uint8_t bs[kNoAllocMaxMbs * h264r::kBsBytes];  // boundary strengths (read with 16-byte loads)
 };
@@ -56,7 +57,7 @@ __global__ void k_noalloc_init(PicDesc d, NoAllocScratch *s)
     if (threadIdx.x == 0) {
         s->desc = d;
         s->error = 0;
-        s->ticket[0] = s->ticket[1] = 0;
+        s->ticket[0] = s->ticket[1] = s->ticket[2] = 0;
     }
     for (uint32_t i = threadIdx.x; i < 3 * kNoAllocMaxRows; i += blockDim.x) s->progress[i] = 0;
 }
@@ -118,6 +119,8 @@ extern "C" int h264r_deblock_picture_noalloc(const h264r_picture *pic, uint8_t *
     d.units_h = rows;
     d.db_base = 0;
     d.db_units = h264r::deblock_units(d.mbaff, rows);
+    d.dbf_base = 0;
+    d.dbf_units = h264r::deblock_frame_units(d.mbaff, rows);
     d.deblock_stop = 0xFFFFFFFFu;
 
     cudaStream_t cs = (cudaStream_t)cuda_stream;
@@ -127,7 +130,8 @@ extern "C" int h264r_deblock_picture_noalloc(const h264r_picture *pic, uint8_t *
     st.spin_limit = kNoAllocSpinLimit;
     k_noalloc_init<<<1, 256, 0, cs>>>(d, s);
     h264r::k_bs<<<(pic->num_mbs + 3) / 4, 128, 0, cs>>>(&s->desc, 1, pic->num_mbs, st);
-    h264r::k_deblock<<<d.db_units, 32, 0, cs>>>(&s->desc, 1, d.db_units, st);
+    if (d.dbf_units) h264r::k_deblock_frame<<<d.dbf_units, 32 * h264r::kDbWarps, 0, cs>>>(&s->desc, 1, d.dbf_units, st);
+    if (d.db_units) h264r::k_deblock<<<d.db_units, 32, 0, cs>>>(&s->desc, 1, d.db_units, st);
     if (cudaGetLastError() != cudaSuccess) return H264R_ERR_CUDA;
     int herr = 0;
     if (cudaMemcpyAsync(&herr, &s->error, sizeof(int), cudaMemcpyDeviceToHost, cs) != cudaSuccess) return H264R_ERR_CUDA;
