@@ -350,6 +350,74 @@ def run_plain_cif(device, seed=1000):
     return {"fps": round(n / dt, 1), "config": "CIF IPPP 8 pictures, host records, one picture per launch, host sync"}
 
 
+def run_bitstream(device, streams=12, repeats=24):
+    """The drop-in path on real bitstreams: the two CAVLC cut streams of
+    tests/golden (1080p, 4 and 6 pictures, each repeated `repeats` times as
+    one stream) decoded by `streams` decoders at once (one host thread each:
+    the front end parses, the engine reconstructs on the GPU, every output
+    picture is copied back to pinned host memory and handed to the
+    callback).  Also the front end alone on one core.  Frames/s."""
+    import ctypes
+    import threading
+
+    import h264_video_decoder_demo_gb300 as h
+    from h264_video_decoder_demo_gb300 import records as R
+    from h264_video_decoder_demo_gb300.engine import lib
+
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden")
+    sources = []
+    for name in ("gop121_cavlc_4pics", "heavyhand_cavlc_b4_6pics"):
+        with open(os.path.join(here, name + ".h264"), "rb") as f:
+            sources.append(f.read() * repeats)
+    # the front end alone, one core
+    data = sources[1]
+    p = h.Parser()
+    buf = (ctypes.c_uint8 * len(data)).from_buffer_copy(data)
+    out = R.CParsed()
+    t0 = time.perf_counter()
+    lib().h264r_parser_feed(p.h, buf, len(data))
+    lib().h264r_parser_end(p.h)
+    n_parse = 0
+    while lib().h264r_parser_next(p.h, ctypes.byref(out)) == 1:
+        n_parse += 1
+    parse_fps = n_parse / (time.perf_counter() - t0)
+    p.close()
+    # decoders in parallel
+    ctx = h.Context(device)
+    counts = [0] * streams
+    errors = []
+
+    def work(i):
+        def on_frame(f, code):
+            if f is not None:
+                counts[i] += 1
+            return 0
+        d = h.Decoder(ctx, on_frame, copy_planes=False)
+        try:
+            d.push(sources[i % 2])
+            d.flush()
+        except Exception as e:  # reported in the result line
+            errors.append(str(e))
+        d.close()
+
+    work(0)  # warm-up: buffers, first launches
+    counts[0] = 0
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(streams)]
+    t0 = time.perf_counter()
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    dt = time.perf_counter() - t0
+    ctx.close()
+    frames = sum(counts)
+    return {"fps": round(frames / dt, 1), "frames": frames, "streams": streams, "wall_s": round(dt, 3),
+            "front_end_fps_one_core": round(parse_fps, 1), "errors": errors[:2],
+            "config": "1080p CAVLC bitstreams (the bundled gop121 and HeavyHand B_frames_4 streams cut after 4 and 6 "
+                      "pictures, each repeated %d times), %d decoders on their own host threads and engine streams, "
+                      "parse + GPU reconstruction + every frame to pinned host memory" % (repeats, streams)}
+
+
 SERVE_RES = [("cif", 22, 18, 0.3), ("720p", 80, 45, 0.4), ("1080p", 120, 68, 0.3)]
 
 
@@ -655,6 +723,7 @@ def run_engine(args, world, rank, local, dist):
             extra["batched_mixed"] = run_mixed(args, local)
             extra["interlaced_mbaff"] = run_interlaced(args, local)
             extra["plain_cif"] = run_plain_cif(local)
+            extra["bitstream_decode"] = run_bitstream(local)
 
     for s in streams:
         s.close()

@@ -56,38 +56,29 @@ struct BitReader {
         }
     }
 
-    // next k (<= 32) bits without consuming them
-    uint32_t peek(int k) const
+    // the 64 bits from the byte holding `pos`, big-endian (zeros past the end)
+    uint64_t window() const
     {
+        const size_t byte = pos >> 3, nbytes = nbits >> 3;
         uint64_t v = 0;
-        for (int i = 0; i < k; i++) {
-            const size_t b = pos + i;
-            const uint32_t bit = b < nbits ? (p[b >> 3] >> (7 - (b & 7))) & 1u : 0u;
-            v = (v << 1) | bit;
+        if (byte + 8 <= nbytes) {
+            for (int i = 0; i < 8; i++) v = (v << 8) | p[byte + i];
+        } else {
+            for (int i = 0; i < 8; i++) v = (v << 8) | (byte + i < nbytes ? p[byte + i] : 0u);
         }
-        return (uint32_t)v;
+        return v;
     }
 
+    // next k (1..32) bits without consuming them
+    uint32_t peek(int k) const { return (uint32_t)((window() << (pos & 7)) >> (64 - k)); }
+
+    // k (0..32) bits
     uint32_t u(int k)
     {
         if (k == 0) return 0;
-        // byte-wise fast path
-        uint32_t v = 0;
-        int left = k;
-        while (left > 0) {
-            if (pos >= nbits) {
-                err = true;
-                v <<= left;
-                pos += left;
-                return v;
-            }
-            const int bit_in = (int)(pos & 7), avail = 8 - bit_in;
-            const int take = left < avail ? left : avail;
-            const uint32_t byte = p[pos >> 3];
-            v = (v << take) | ((byte >> (avail - take)) & ((1u << take) - 1u));
-            pos += take;
-            left -= take;
-        }
+        const uint32_t v = peek(k);
+        pos += (size_t)k;
+        if (pos > nbits) err = true;
         return v;
     }
 
@@ -96,15 +87,18 @@ struct BitReader {
 
     uint32_t ue()
     {
-        int lz = 0;
-        while (u(1) == 0) {
-            if (++lz > 31 || err) {
-                err = true;
-                return 0;
-            }
+        const uint32_t w = peek(32);
+        if (w == 0) {  // more than 31 leading zeros: not a code of this decoder's range
+            err = true;
+            pos += 32;
+            return 0;
         }
-        if (lz == 0) return 0;
-        return ((1u << lz) - 1u) + u(lz);
+        const int lz = __builtin_clz(w);
+        pos += (size_t)lz + 1;
+        if (lz == 0) return pos > nbits ? (err = true, 0u) : 0u;
+        const uint32_t v = ((1u << lz) - 1u) + u(lz);
+        if (pos > nbits) err = true;
+        return v;
     }
 
     int32_t se()

@@ -197,6 +197,10 @@ struct MbDecoder {
     MbState *cur = nullptr;
     bool decoded4x4[16];  // motion of this 4x4 block already derived
     Blk blk[16];          // motion of the current MB (raster)
+    // per-MB scratch, reused across the slice's MBs
+    std::vector<PartRec> parts;
+    std::vector<uint16_t> sig;
+    std::vector<int16_t> lv;
 
     MbDecoder(h264r_parser &p, SliceCtx &s, BitReader &b)
         : P(p), sc(s), br(b), sps(*s.sps), pps(*s.pps), W(p.width_mbs)
@@ -578,7 +582,7 @@ int MbDecoder::inter_pred(int mb_type, bool is_b, h264r_mb &r, bool &no_sub_lt8)
 {
     no_sub_lt8 = true;
     const int nref[2] = {sc.sh.num_ref_idx_active[0], sc.sh.num_ref_idx_active[1]};
-    std::vector<PartRec> parts;
+    parts.clear();
     int shape = 0;
     // read the syntax first (mb_pred / sub_mb_pred, 7.3.5.1 / 7.3.5.2)
     const bool b8x8 = is_b ? mb_type == 22 : (mb_type == 3 || mb_type == 4);
@@ -926,7 +930,7 @@ int MbDecoder::decode()
         if (is_b && mb_type == 0) {  // B_Direct_16x16
             for (int i = 0; i < 16; i++) decoded4x4[i] = false;
             spatial_ready = false;
-            std::vector<PartRec> parts;
+            parts.clear();
             for (int q = 0; q < 4; q++)
                 for (int s = 0; s < 4; s++) {
                     const int x = (q & 1) * 8 + 4 * (s & 1), y = (q >> 1) * 8 + 4 * (s >> 1);
@@ -949,8 +953,8 @@ int MbDecoder::decode()
     }
     if (t8) r.flags |= H264R_MBF_T8x8;
     uint32_t mask = 0;
-    std::vector<uint16_t> sig;
-    std::vector<int16_t> lv;
+    sig.clear();
+    lv.clear();
     if ((cbp & 15) || (cbp >> 4) || cls == H264R_MB_I16x16) {
         int dq = br.se();
         dq = clip3(-26, 25, dq);
@@ -1006,7 +1010,8 @@ int decode_skip(MbDecoder &d, h264r_mb &r)
     }
     for (int i = 0; i < 4; i++) cur->ipm8[i] = 2;
     memset(cur->tcc, 0, sizeof(cur->tcc));
-    std::vector<PartRec> parts;
+    std::vector<PartRec> &parts = d.parts;
+    parts.clear();
     if (d.sc.sh.slice_type == kSliceB) {
         d.spatial_ready = false;
         for (int q = 0; q < 4; q++)

@@ -461,7 +461,7 @@ class Decoder:
 
     FILE_END, OPEN_FILE_FAILED = 1, 2
 
-    def __init__(self, ctx, on_frame):
+    def __init__(self, ctx, on_frame, copy_planes=True):
         self.ctx = ctx
         h = ctypes.c_void_p()
         rc = lib().h264r_decoder_create(ctx.h, ctypes.byref(h))
@@ -475,7 +475,7 @@ class Decoder:
                 return int(bool(self._user(None, code)))
             f = fp.contents
             n = f.width * f.height * 3 // 2
-            planes = np.frombuffer(ctypes.string_at(f.y, n), np.uint8).copy()
+            planes = np.frombuffer(ctypes.string_at(f.y, n), np.uint8).copy() if copy_planes else None
             info = {"poc": f.poc, "decode_index": f.decode_index, "slice_type": f.slice_type,
                     "output_count": f.output_count, "width": f.width, "height": f.height, "planes": planes,
                     "slot": f.slot}
