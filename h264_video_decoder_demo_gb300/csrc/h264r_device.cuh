@@ -93,7 +93,7 @@ struct PicDesc {
 // block ticket for the luma and one for the chroma of every kDbWarps pairs
 // of MB rows, a warp per pair.  MBAFF pictures (k_deblock): one warp ticket
 // for the luma and one for the chroma of every MB-pair row.
-constexpr int kDbWarps = 4;   // MB-row pairs (warps) per frame deblocking block
+constexpr int kDbWarps = 8;   // MB-row pairs (warps) per frame deblocking block
 constexpr int kDbXRing = 16;  // MBs of a warp's bottom lines kept for the warp below
 __host__ __device__ inline uint32_t deblock_units(int mbaff, uint32_t units_h) { return mbaff ? 2u * units_h : 0u; }
 __host__ __device__ inline uint32_t deblock_frame_units(int mbaff, uint32_t units_h)

@@ -1705,8 +1705,9 @@ __device__ void mbaff_chroma_row(const PicDesc &p, int row, uint32_t *win, const
 // Non-MBAFF pictures.  Luma and chroma are filtered by separate warps (the
 // planes never interact), each warp taking a pair of MB rows: lanes 0..15
 // work on the first row, 16..31 on the second, which trails the first by
-// two MBs (in the reference's raster order a MB's top edge comes after the
-// left edge of the MB above-right).  A luma lane owns one line of the MB;
+// one MB: in the reference's raster order a MB's top edge comes after the
+// left edge of the MB above-right, and every step runs both rows' vertical
+// edges before either row's horizontal edges.  A luma lane owns one line of the MB;
 // a chroma lane one line of Cb (lanes 0..7 of the half) or Cr (8..15).  A
 // line is filtered in registers across all edges of one direction, and the
 // MB passes through a byte tile in shared memory once, between its vertical
@@ -1741,7 +1742,7 @@ struct DbFrameShared {
         uint4 l[kDbWarps - 1][kDbXRing][4];     // luma rows 12..15
         uint2 c[kDbWarps - 1][kDbXRing][2][4];  // chroma rows 4..7 per plane
     } x;
-    int done[kDbWarps];  // second row: MBs completed
+    int done[kDbWarps];  // second row: MBs up to done-2 completed and the vertical edges of MB done-1 (uw+1: all)
     int used[kDbWarps];  // first row: MBs whose rows above were taken
 };
 
@@ -1838,7 +1839,7 @@ __device__ void deblock_pair_luma(const PicDesc &p, int pair, int wi, int nw, Db
     const int row = 2 * pair + h;
     const bool row_ok = row < rows;
     const bool has_second = 2 * pair + 1 < rows;
-    const int steps = has_second ? uw + 2 : uw;
+    const int steps = has_second ? uw + 1 : uw;
     const bool from_cta = wi > 0;                  // rows above from the warp before, in shared memory
     const bool to_cta = wi + 1 < nw && has_second;  // bottom lines to the warp after
     int *prog = p.progress + p.units_h;
@@ -1860,13 +1861,13 @@ __device__ void deblock_pair_luma(const PicDesc &p, int pair, int wi, int nw, Db
     };
     if (row_ok && h == 0) fetch(0);
     for (int step = 0; step < steps; step++) {
-        const int u = step - 2 * h;
+        const int u = step - h;
         const bool act = row_ok && u >= 0 && u < uw;
         const uint4 line = nl, prm = npl;
         uint32_t lv = nlv, lh = nlh;
         if (row_ok && u + 1 >= 0 && u + 1 < uw) fetch(u + 1);
         // the warp after must have taken the lines this step overwrites
-        if (to_cta && step >= 2 && !cta_wait(st, &S.used[wi + 1], min(step - 1 - kDbXRing, uw), seen_used)) return;
+        if (to_cta && step >= 1 && !cta_wait(st, &S.used[wi + 1], min(step - kDbXRing, uw), seen_used)) return;
         const int x0 = u * 16, y0 = row * 16;
         if (act) {
             const int cur = row * uw + u;
@@ -1897,12 +1898,23 @@ __device__ void deblock_pair_luma(const PicDesc &p, int pair, int wi, int nw, Db
             }
             *(uint4 *)&t[k + 4][0] = pack16(&v[4]);
         }
+        // the warp below needs MB u of this warp's second row and the vertical
+        // edges of MB u+1: both are done once this step's vertical edges are
+        if (to_cta && step >= 1) {
+            __syncwarp();
+            __threadfence_block();
+            if (lane == 0) *(volatile int *)&S.done[wi] = step;
+        }
         // ---- the row above: final once its warp is two MBs ahead
         if (2 * pair > 0 && step < uw) {
-            const bool ok = from_cta ? cta_wait(st, &S.done[wi - 1], min(step + 2, uw), seen)
+            // in the block: MB step and the vertical edges of MB step+1 of the
+            // row above (its last MB: the end of that warp's last step, uw+1);
+            // across blocks: MBs 0..step+1 completed
+            const bool ok = from_cta ? cta_wait(st, &S.done[wi - 1], step + 2, seen)
                                      : db_wait(st, prog + 2 * pair - 1, min(step + 2, uw), seen);
             if (!ok) return;
         }
+        __syncwarp();  // the first row's vertical edges of this step updated the ring
         if (act && row > 0 && k < 4)
             *(uint4 *)&t[k][0] = h == 1 ? s.ring[u % 3][k]
                                         : (from_cta ? S.x.l[wi - 1][u % kDbXRing][k]
@@ -1932,13 +1944,12 @@ __device__ void deblock_pair_luma(const PicDesc &p, int pair, int wi, int nw, Db
             if (row > 0 && k < 3) *(uint4 *)(Y + (size_t)(y0 - 3 + k) * W + x0) = *(const uint4 *)&t[1 + k][0];
         }
         __syncwarp();
-        if (has_second && step >= 2) {
-            if (to_cta) {
-                __threadfence_block();
-                if (lane == 0) *(volatile int *)&S.done[wi] = step - 1;
-            } else if (lane == 0) {
-                st_release(prog + 2 * pair + 1, step - 1);
-            }
+        if (has_second && step >= 1 && !to_cta && lane == 0)  // the second row has MBs 0..step-1 done
+            st_release(prog + 2 * pair + 1, step);
+        if (to_cta && step == uw) {  // the second row's last MB is complete
+            __syncwarp();
+            __threadfence_block();
+            if (lane == 0) *(volatile int *)&S.done[wi] = uw + 1;
         }
         if (from_cta && step < uw) {
             __threadfence_block();
@@ -1956,7 +1967,7 @@ __device__ void deblock_pair_chroma(const PicDesc &p, int pair, int wi, int nw, 
     const int row = 2 * pair + h;
     const bool row_ok = row < rows;
     const bool has_second = 2 * pair + 1 < rows;
-    const int steps = has_second ? uw + 2 : uw;
+    const int steps = has_second ? uw + 1 : uw;
     const bool from_cta = wi > 0;
     const bool to_cta = wi + 1 < nw && has_second;
     int *prog = p.progress + p.units_h;
@@ -1978,13 +1989,13 @@ __device__ void deblock_pair_chroma(const PicDesc &p, int pair, int wi, int nw, 
     };
     if (row_ok && h == 0) fetch(0);
     for (int step = 0; step < steps; step++) {
-        const int u = step - 2 * h;
+        const int u = step - h;
         const bool act = row_ok && u >= 0 && u < uw;
         const uint2 line = nl;
         const uint4 prm = npc;
         uint32_t cv = ncv, ch = nch;
         if (row_ok && u + 1 >= 0 && u + 1 < uw) fetch(u + 1);
-        if (to_cta && step >= 2 && !cta_wait(st, &S.used[wi + 1], min(step - 1 - kDbXRing, uw), seen_used)) return;
+        if (to_cta && step >= 1 && !cta_wait(st, &S.used[wi + 1], min(step - kDbXRing, uw), seen_used)) return;
         const int x0 = u * 8, y0 = row * 8;
         if (act) {
             const int cur = row * uw + u;
@@ -2012,11 +2023,17 @@ __device__ void deblock_pair_chroma(const PicDesc &p, int pair, int wi, int nw, 
             }
             *(uint2 *)&t[ck + 4][0] = pack8(&w[4]);
         }
+        if (to_cta && step >= 1) {
+            __syncwarp();
+            __threadfence_block();
+            if (lane == 0) *(volatile int *)&S.done[wi] = step;
+        }
         if (2 * pair > 0 && step < uw) {
-            const bool ok = from_cta ? cta_wait(st, &S.done[wi - 1], min(step + 2, uw), seen)
+            const bool ok = from_cta ? cta_wait(st, &S.done[wi - 1], step + 2, seen)
                                      : db_wait(st, prog + 2 * pair - 2, min(step + 2, uw), seen);
             if (!ok) return;
         }
+        __syncwarp();  // the first row's vertical edges of this step updated the ring
         if (act && row > 0 && ck < 4)
             *(uint2 *)&t[ck][0] = h == 1 ? s.ring[u % 3][comp][ck]
                                          : (from_cta ? S.x.c[wi - 1][u % kDbXRing][comp][ck]
@@ -2044,13 +2061,11 @@ __device__ void deblock_pair_chroma(const PicDesc &p, int pair, int wi, int nw, 
             if (row > 0 && ck < 3) *(uint2 *)(C + (size_t)(y0 - 3 + ck) * Wc + x0) = *(const uint2 *)&t[1 + ck][0];
         }
         __syncwarp();
-        if (has_second && step >= 2) {
-            if (to_cta) {
-                __threadfence_block();
-                if (lane == 0) *(volatile int *)&S.done[wi] = step - 1;
-            } else if (lane == 0) {
-                st_release(prog + 2 * pair, step - 1);
-            }
+        if (has_second && step >= 1 && !to_cta && lane == 0) st_release(prog + 2 * pair, step);
+        if (to_cta && step == uw) {
+            __syncwarp();
+            __threadfence_block();
+            if (lane == 0) *(volatile int *)&S.done[wi] = uw + 1;
         }
         if (from_cta && step < uw) {
             __threadfence_block();
