@@ -83,32 +83,9 @@ __device__ __forceinline__ void st_release(int *p, int v)
     asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Wait (whole warp) until *flag >= target.  Returns false on timeout or when
-// another block reported an error.
-__device__ bool wait_progress(const LaunchState &st, const int *flag, int target)
-{
-    bool ok = true;
-    if ((threadIdx.x & 31) == 0) {
-        unsigned long long n = 0;
-        while (ld_acquire(flag) < target) {
-            if (++n > st.spin_limit) {
-                set_error(st, H264R_ERR_DEVICE_TIMEOUT);
-                ok = false;
-                break;
-            }
-            if (n > 64) {
-                if (*(volatile int *)st.error != 0) { ok = false; break; }
-                __nanosleep(32);
-            }
-        }
-    }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    __syncwarp();
-    return ok;
-}
-
-// As wait_progress, with the last value seen cached by the caller: no load
-// when it already satisfies the target.
+// Wait (whole warp) until the global counter *flag >= target, with the last
+// value seen cached by the caller (no load when it already satisfies the
+// target).  Returns false on timeout or when another block reported an error.
 __device__ __forceinline__ bool db_wait(const LaunchState &st, const int *flag, int target, int &seen)
 {
     int ok = 1;
@@ -563,7 +540,35 @@ struct IntraSmem {
     int nb[40];           // neighbouring samples (-1: not available)
     int nbf[40];          // filtered (8x8) neighbours
     int nb4[2][16];       // neighbours of the two 4x4 blocks of a wave
+    // record and residual (int16 pairs, as k_inter stored them) of an intra
+    // MB, copied in ahead of its turn; two buffers so that the next MB's copy
+    // overlaps the current MB's work
+    __align__(16) uint32_t raw[2][192];
+    __align__(16) h264r_mb rec[2];
 };
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+// start copying MB addr's record and residual into buffer buf (one commit group)
+__device__ __forceinline__ void intra_prefetch(const PicDesc &p, int addr, IntraSmem &s, int buf)
+{
+    const int lane = threadIdx.x & 31;
+    const uint8_t *src = (const uint8_t *)(p.ires + (size_t)addr * 384);
+    for (int i = lane; i < 48; i += 32) cp_async16(&s.raw[buf][4 * i], src + 16 * i);
+    // the residual buffer is the engine's (768 bytes per MB); the record array
+    // may be a caller's with 4-byte alignment only: plain copy then
+    const uint8_t *rec = (const uint8_t *)(p.mbs + addr);
+    if (((uintptr_t)rec & 15u) == 0) {
+        if (lane < 2) cp_async16((uint8_t *)&s.rec[buf] + 16 * lane, rec + 16 * lane);
+    } else if (lane < 8) {
+        ((uint32_t *)&s.rec[buf])[lane] = ((const uint32_t *)rec)[lane];
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
 
 // 4x4 prediction sample (x, y) from nb = {p[-1,-1], p[-1,0..3], p[0..7,-1]}
 // (Intra_4x4_sample_prediction, H264PictureBase.cpp:1062-1419); returns -1
@@ -735,10 +740,11 @@ __device__ __forceinline__ int tile_nb(const IntraTile &t, int xN, int yN, bool 
     return t.l[yN + 1][xN + 1];
 }
 
-__device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTile &t, const LaunchState &st)
+// buf: the IntraSmem buffer holding the MB's record and residual
+__device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTile &t, int buf, const LaunchState &st)
 {
     const int lane = threadIdx.x & 31;
-    const h264r_mb m = p.mbs[addr];
+    const h264r_mb m = s.rec[buf];
     const int W = p.W, Wc = p.Wc, wmb = p.wmb;
     int x, y, dy;  // first luma sample and row step (2 for a field MB of an MBAFF picture)
     bool A = false, B = false, Cc = false, D = false;
@@ -762,8 +768,14 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
         D = mx > 0 && my > 0 && usable(addr - wmb - 1);
     }
     uint8_t *Y = plane_y(p);
-    // ---- residual (computed by k_inter)
-    load_intra_residual(p, addr, s.res);
+    // ---- residual (computed by k_inter), from the prefetch buffer
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const int i = lane + 32 * k;
+        const uint32_t w = s.raw[buf][i];
+        s.res[2 * i] = (int16_t)(w & 0xFFFFu);
+        s.res[2 * i + 1] = (int16_t)(w >> 16);
+    }
     // ---- stage the neighbourhood (luma: corner, 16 left, 24 top; chroma:
     //      corner, 8 left, 8 top), -1 where not available for intra
     //      prediction.  In an MBAFF picture every sample goes through the
@@ -1005,7 +1017,8 @@ __global__ void __launch_bounds__(32, 21) k_intra(const PicDesc *__restrict__ pi
     int *prog = p.progress;
     // Units without intra MBs were completed by k_inter: progress is only
     // published before this row waits and after each intra unit.
-    int posted = 0;
+    int posted = 0, seen = 0;
+    int buf = 0, ahead = -1;  // ahead: MB whose copy into buffer buf is in flight
     for (int u0 = 0; u0 < uw; u0 += 32) {
         // which of the next 32 units hold intra MBs: one record load per lane
         bool mine = false;
@@ -1021,11 +1034,32 @@ __global__ void __launch_bounds__(32, 21) k_intra(const PicDesc *__restrict__ pi
             todo &= todo - 1;
             if (lane == 0 && posted < u) st_release(prog + row, u);
             posted = u;
-            if (row > 0 && !wait_progress(st, prog + row - 1, min(u + 2, uw))) return;
-            for (int k = 0; k < per; k++) {
-                int addr = p.mbaff ? 2 * (row * uw + u) + k : row * uw + u;
-                if (!is_intra_type(p.mbs[addr].type)) continue;
-                intra_mb_tiled(p, addr, s, tile, st);
+            if (row > 0 && !db_wait(st, prog + row - 1, min(u + 2, uw), seen)) return;
+            if (p.mbaff) {
+                for (int k = 0; k < per; k++) {
+                    const int addr = 2 * (row * uw + u) + k;
+                    if (!is_intra_type(p.mbs[addr].type)) continue;
+                    intra_prefetch(p, addr, s, buf);
+                    asm volatile("cp.async.wait_group 0;" ::: "memory");
+                    __syncwarp();
+                    intra_mb_tiled(p, addr, s, tile, buf, st);
+                }
+            } else {
+                // the next intra MB of this group of 32 is copied in while this one runs
+                const int addr = row * uw + u;
+                if (ahead != addr) intra_prefetch(p, addr, s, buf);
+                const bool more = todo != 0;
+                if (more) {
+                    ahead = row * uw + u0 + __ffs(todo) - 1;
+                    intra_prefetch(p, ahead, s, buf ^ 1);
+                    asm volatile("cp.async.wait_group 1;" ::: "memory");
+                } else {
+                    ahead = -1;
+                    asm volatile("cp.async.wait_group 0;" ::: "memory");
+                }
+                __syncwarp();
+                intra_mb_tiled(p, addr, s, tile, buf, st);
+                buf ^= 1;
             }
             __syncwarp();
             if (lane == 0) st_release(prog + row, u + 1);
