@@ -1272,61 +1272,80 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
         if (lane < 8) *(uint16_t *)(out + bs_cv(0, ck)) = (uint16_t)cvw;
         else if (lane < 16) *(uint16_t *)(out + bs_ch(0, ck)) = (uint16_t)chw;
     } else {
-    // luma vertical (4 edges x 16 rows): items 0..63
-    for (int it = lane; it < 64; it += 32) {
-        int ei = it >> 4, k = it & 15, e = ei * 4;
-        bool on = (ei == 0) ? c.left : (c.internal && (ei == 2 || !c.t8));
-        int bs = on ? edge_bs(p, cur, 0, 1, e, c.mbA, ei == 0 ? c.leftMixed : 0, k) : 0;
-        if (bs == 0xFF) mystop = min(mystop, stop_key(cur, SEQ_LV0 + ei, k));
-        out[bs_lv(ei, k)] = (uint8_t)bs;
-    }
-    // luma horizontal: items 0..63 (+16 for the MBAFF second top edge)
-    for (int it = lane; it < 80; it += 32) {
-        int bs = 0, seq, k;
-        if (it < 64) {
-            int ei = it >> 4, e = ei * 4;
-            k = it & 15;
-            bool on = (ei == 0) ? c.top : (c.internal && (ei == 2 || !c.t8));
-            if (on) {
-                if (ei == 0 && c.topDouble) bs = edge_bs(p, cur, 0, 0, 0, c.mbB - 1, 0, k);
-                else bs = edge_bs(p, cur, 0, 0, e, c.mbB, 0, k);
+        // MBAFF.  Internal edges join two 4x4 blocks of the same MB (never a
+        // mixed edge), so their strength is uniform over the 4 lines of a
+        // block pair as in frame pictures: lanes 0..23 derive them
+        // (dir, edge 1..3, block), and 4:2:0 chroma takes the luma value of
+        // edge 8 at luma line 2k.  The MB edges (left, top, second top of a
+        // frame MB under a field pair) are derived per line.
+        uint32_t ivrow = 0, ihrow = 0;  // lane k < 16: internal strengths of line / column k, byte e
+        {
+            int bs = 0, dir = 0, ei = 1, b = 0;
+            if (lane < 24) {
+                dir = lane / 12;
+                ei = 1 + (lane % 12) / 4;
+                b = lane & 3;
+                if (c.internal && (ei == 2 || !c.t8))
+                    bs = dir == 0 ? edge_bs(p, cur, 0, 1, 4 * ei, c.mbA, 0, 4 * b) : edge_bs(p, cur, 0, 0, 4 * ei, c.mbB, 0, 4 * b);
+                if (bs == 0xFF) mystop = min(mystop, stop_key(cur, dir == 0 ? SEQ_LV0 + ei : SEQ_LH4 + ei - 1, 4 * b));
             }
-            seq = ei == 0 ? SEQ_LH0 : SEQ_LH4 + ei - 1;
-            out[bs_lh(ei, k)] = (uint8_t)bs;
-        } else {
-            k = it - 64;
-            if (c.top && c.topDouble) bs = edge_bs(p, cur, 0, 0, 1, c.mbB, 0, k);
-            seq = SEQ_LH0B;
-            out[kBsLumaTop2 + k] = (uint8_t)bs;
+            const int k = lane & 15;
+#pragma unroll
+            for (int e2 = 1; e2 < 4; e2++) {
+                ivrow |= (uint32_t)(__shfl_sync(0xffffffffu, bs, (e2 - 1) * 4 + (k >> 2)) & 255) << (8 * e2);
+                ihrow |= (uint32_t)(__shfl_sync(0xffffffffu, bs, 12 + (e2 - 1) * 4 + (k >> 2)) & 255) << (8 * e2);
+            }
         }
-        if (bs == 0xFF) mystop = min(mystop, stop_key(cur, seq, k));
-    }
-    // chroma: vertical 2 edges x 8 rows, horizontal 2 x 8, extra top 8;
-    // Cb and Cr share the strengths but are separate steps of the order
-    for (int it = lane; it < 40; it += 32) {
-        int bs = 0, seqcb, k;
-        if (it < 16) {
-            int ei = it >> 3;
-            k = it & 7;
-            bool on = ei == 0 ? c.left : c.internal;
-            if (on) bs = edge_bs(p, cur, 1, 1, ei * 4, c.mbA, ei == 0 ? c.leftMixed : 0, k);
-            seqcb = ei == 0 ? SEQ_CBV0 : SEQ_CBV4;
-            out[bs_cv(ei, k)] = (uint8_t)bs;
-        } else if (it < 32) {
-            int ei = (it - 16) >> 3;
-            k = it & 7;
-            bool on = ei == 0 ? c.top : c.internal;
-            if (on) bs = edge_bs(p, cur, 1, 0, ei == 0 ? 0 : 4, c.mbB, 0, k);
-            seqcb = ei == 0 ? SEQ_CBH0 : SEQ_CBH4;
-            out[bs_ch(ei, k)] = (uint8_t)bs;
-        } else {
-            k = it - 32;
-            if (c.top && c.topDouble) bs = edge_bs(p, cur, 1, 0, 1, c.mbB, 0, k);
-            seqcb = SEQ_CBH0B;
-            out[kBsChromaTop2 + k] = (uint8_t)bs;
+        // MB edges per line: left (0..15), top (16..31), second top (32..47) luma;
+        // chroma left (48..55), top (56..63), second top (64..71)
+        uint32_t lv0 = 0, lh0 = 0;  // lane k < 16: luma left / top strength of line / column k
+        for (int it = lane; it < 72; it += 32) {
+            int bs = 0, seq = 0, k = 0;
+            if (it < 16) {
+                k = it;
+                if (c.left) bs = edge_bs(p, cur, 0, 1, 0, c.mbA, c.leftMixed, k);
+                seq = SEQ_LV0;
+                lv0 = (uint32_t)bs;
+            } else if (it < 32) {
+                k = it - 16;
+                if (c.top) bs = c.topDouble ? edge_bs(p, cur, 0, 0, 0, c.mbB - 1, 0, k) : edge_bs(p, cur, 0, 0, 0, c.mbB, 0, k);
+                seq = SEQ_LH0;
+            } else if (it < 48) {
+                k = it - 32;
+                if (c.top && c.topDouble) bs = edge_bs(p, cur, 0, 0, 1, c.mbB, 0, k);
+                seq = SEQ_LH0B;
+                out[kBsLumaTop2 + k] = (uint8_t)bs;
+            } else if (it < 56) {
+                k = it - 48;
+                if (c.left) bs = edge_bs(p, cur, 1, 1, 0, c.mbA, c.leftMixed, k);
+                seq = SEQ_CBV0;
+                out[bs_cv(0, k)] = (uint8_t)bs;
+            } else if (it < 64) {
+                k = it - 56;
+                if (c.top) bs = edge_bs(p, cur, 1, 0, 0, c.mbB, 0, k);
+                seq = SEQ_CBH0;
+                out[bs_ch(0, k)] = (uint8_t)bs;
+            } else {
+                k = it - 64;
+                if (c.top && c.topDouble) bs = edge_bs(p, cur, 1, 0, 1, c.mbB, 0, k);
+                seq = SEQ_CBH0B;
+                out[kBsChromaTop2 + k] = (uint8_t)bs;
+            }
+            if (it >= 16 && it < 32) lh0 = (uint32_t)bs;
+            if (bs == 0xFF) mystop = min(mystop, stop_key(cur, seq, k));
         }
-        if (bs == 0xFF) mystop = min(mystop, stop_key(cur, seqcb, k));
-    }
+        // lanes 16..31 derived the top edge of column lane-16 in their first item
+        lh0 = __shfl_sync(0xffffffffu, lh0, (lane & 15) + 16);
+        if (lane < 16) {
+            *(uint32_t *)(out + bs_lv(0, lane)) = ivrow | (lv0 & 255);
+            *(uint32_t *)(out + bs_lh(0, lane)) = ihrow | (lh0 & 255);
+        }
+        // chroma internal edge (4): luma edge 8 at luma line / column 2k
+        const int ck = lane & 7;
+        const uint32_t civ = __shfl_sync(0xffffffffu, (ivrow >> 16) & 255, 2 * ck);
+        const uint32_t cih = __shfl_sync(0xffffffffu, (ihrow >> 16) & 255, 2 * ck);
+        if (lane < 8) out[bs_cv(1, ck)] = (uint8_t)civ;
+        else if (lane < 16) out[bs_ch(1, ck)] = (uint8_t)cih;
     }
     // thresholds of each edge class for the frame fast path of k_deblock
     if (!p.mbaff && lane < 9) {
