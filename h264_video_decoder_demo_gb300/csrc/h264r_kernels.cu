@@ -1036,13 +1036,30 @@ __global__ void __launch_bounds__(32, 21) k_intra(const PicDesc *__restrict__ pi
             posted = u;
             if (row > 0 && !db_wait(st, prog + row - 1, min(u + 2, uw), seen)) return;
             if (p.mbaff) {
-                for (int k = 0; k < per; k++) {
-                    const int addr = 2 * (row * uw + u) + k;
-                    if (!is_intra_type(p.mbs[addr].type)) continue;
-                    intra_prefetch(p, addr, s, buf);
-                    asm volatile("cp.async.wait_group 0;" ::: "memory");
+                // the pair's intra MBs; the copy of the next intra MB (the
+                // pair's second, else the next pair's first of this group)
+                // overlaps the current one
+                const int pa = 2 * (row * uw + u);
+                const bool in0 = is_intra_type(p.mbs[pa].type), in1 = is_intra_type(p.mbs[pa + 1].type);
+                int nxt = -1;  // first intra MB of the next pair with intra MBs in this group
+                if (todo) {
+                    const int pn = 2 * (row * uw + u0 + __ffs(todo) - 1);
+                    nxt = is_intra_type(p.mbs[pn].type) ? pn : pn + 1;
+                }
+                for (int k = 0; k < 2; k++) {
+                    if (!(k ? in1 : in0)) continue;
+                    const int addr = pa + k;
+                    if (ahead != addr) intra_prefetch(p, addr, s, buf);
+                    ahead = (k == 0 && in1) ? pa + 1 : nxt;
+                    if (ahead >= 0) {
+                        intra_prefetch(p, ahead, s, buf ^ 1);
+                        asm volatile("cp.async.wait_group 1;" ::: "memory");
+                    } else {
+                        asm volatile("cp.async.wait_group 0;" ::: "memory");
+                    }
                     __syncwarp();
                     intra_mb_tiled(p, addr, s, tile, buf, st);
+                    buf ^= 1;
                 }
             } else {
                 // the next intra MB of this group of 32 is copied in while this one runs
