@@ -624,7 +624,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
             ctx->launches++;
         }
         if (db_base) {
-            h264r::k_deblock<<<(unsigned)db_base, 32, 0, cs>>>(dd, n, (uint32_t)db_base, st);
+            h264r::k_deblock<<<(unsigned)db_base, 32 * h264r::kMbWarps, 0, cs>>>(dd, n, (uint32_t)db_base, st);
             ctx->launches++;
         }
     }

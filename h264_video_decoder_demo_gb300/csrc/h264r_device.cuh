@@ -91,11 +91,17 @@ struct PicDesc {
 
 // Deblocking tickets of a picture.  Frame pictures (k_deblock_frame): one
 // block ticket for the luma and one for the chroma of every kDbWarps pairs
-// of MB rows, a warp per pair.  MBAFF pictures (k_deblock): one warp ticket
-// for the luma and one for the chroma of every MB-pair row.
+// of MB rows, a warp per pair.  MBAFF pictures (k_deblock): one block ticket
+// for the luma and one for the chroma of every kMbWarps MB-pair rows, a
+// warp per pair row.
 constexpr int kDbWarps = 8;   // MB-row pairs (warps) per frame deblocking block
 constexpr int kDbXRing = 16;  // MBs of a warp's bottom lines kept for the warp below
-__host__ __device__ inline uint32_t deblock_units(int mbaff, uint32_t units_h) { return mbaff ? 2u * units_h : 0u; }
+constexpr int kMbWarps = 8;   // MB-pair rows (warps) per MBAFF deblocking block
+constexpr int kMbXRing = 8;   // MB pairs of a warp's bottom rows kept for the warp below
+__host__ __device__ inline uint32_t deblock_units(int mbaff, uint32_t units_h)
+{
+    return mbaff ? 2u * ((units_h + kMbWarps - 1u) / kMbWarps) : 0u;
+}
 __host__ __device__ inline uint32_t deblock_frame_units(int mbaff, uint32_t units_h)
 {
     const uint32_t pairs = (units_h + 1u) / 2u;

@@ -108,6 +108,31 @@ __device__ __forceinline__ bool db_wait(const LaunchState &st, const int *flag, 
     return ok != 0;
 }
 
+// Wait (whole warp) until the shared-memory counter *flag >= target, with
+// the last value seen cached; bounded like the global waits.
+__device__ __forceinline__ bool cta_wait(const LaunchState &st, const int *flag, int target, int &seen)
+{
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0 && seen < target) {
+        unsigned long long n = 0;
+        while ((seen = *(const volatile int *)flag) < target) {
+            if (++n > st.spin_limit) {
+                set_error(st, H264R_ERR_DEVICE_TIMEOUT);
+                ok = 0;
+                break;
+            }
+            if ((n & 255) == 0 && *(volatile int *)st.error != 0) {
+                ok = 0;
+                break;
+            }
+        }
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __syncwarp();
+    __threadfence_block();
+    return ok != 0;
+}
+
 // ======================================================================
 // Residual of one macroblock (8.5), whole warp
 // ======================================================================
@@ -1641,9 +1666,31 @@ __device__ __forceinline__ void mbaff_edges_h(int xP, int yP, int k, const Mbaff
     }
 }
 
-// Luma of MB-pair row `row`; win: 200 words (40 rows of 5).
-__device__ void mbaff_luma_row(const PicDesc &p, int row, uint32_t *win, const LaunchState &st)
+// An MBAFF deblocking block: kMbWarps warps on consecutive MB-pair rows of
+// one plane.  As in frame pictures, a warp takes the rows above from the
+// warp before it through shared memory (x: that warp's bottom eight rows of
+// each pair, own columns; the last word is filled in once the next pair's
+// left edge is done) and waits on its shared-memory progress; the block's
+// first warp reads and waits on global memory, its last warp publishes.
+struct DbMbaffShared {
+    union {
+        uint32_t l[kMbWarps][200];  // luma windows: 40 rows of 5 words
+        uint32_t c[kMbWarps][144];  // chroma windows: 2 planes x 24 rows of 3 words
+    } win;
+    union {
+        uint32_t l[kMbWarps - 1][kMbXRing][8][4];     // luma rows 24..31 of the pair
+        uint32_t c[kMbWarps - 1][kMbXRing][2][8][2];  // chroma rows 8..15 per plane
+    } x;
+    int done[kMbWarps];  // pairs completed
+    int used[kMbWarps];  // pairs whose rows above were taken
+};
+
+// Luma of MB-pair row `row`, warp wi of nw in its block.
+__device__ void mbaff_luma_row(const PicDesc &p, int row, int wi, int nw, DbMbaffShared &S, const LaunchState &st)
 {
+    uint32_t *win = S.win.l[wi];
+    const bool from_cta = wi > 0, to_cta = wi + 1 < nw;
+    int seen_used = 0;
     const int lane = threadIdx.x & 31, h = lane >> 4, k = lane & 15;
     const int uw = (int)p.units_w, W = p.W, y0 = row * 32;
     int *prog = p.progress + p.units_h;
@@ -1658,6 +1705,8 @@ __device__ void mbaff_luma_row(const PicDesc &p, int row, uint32_t *win, const L
     };
     fetch(0);
     for (int u = 0; u < uw; u++) {
+        // the warp below must have taken the rows this pair's end overwrites
+        if (to_cta && !cta_wait(st, &S.used[wi + 1], u + 1 - kMbXRing, seen_used)) return;
         const int x0 = u * 16;
         const MbaffEdges m = nm;
         uint32_t *wr = win + (8 + lane) * 5;  // the lane's own row
@@ -1676,14 +1725,26 @@ __device__ void mbaff_luma_row(const PicDesc &p, int row, uint32_t *win, const L
         const int field = (m.ctl & kDbcField) != 0;
         mbaff_edges_v<false>(x0, field ? y0 + h : y0 + 16 * h, k, m, w);
         // the row above is final once its warp is two pairs ahead
-        if (row > 0 && !db_wait(st, prog + 2 * row - 1, min(u + 2, uw), seen)) return;
+        if (row > 0) {
+            const bool ok = from_cta ? cta_wait(st, &S.done[wi - 1], min(u + 2, uw), seen)
+                                     : db_wait(st, prog + 2 * row - 1, min(u + 2, uw), seen);
+            if (!ok) return;
+        }
         if (row > 0 && lane < 8) {
-            const uint4 t = __ldcg((const uint4 *)(Y + (size_t)(y0 - 8 + lane) * W + x0));
             uint32_t *wt = win + lane * 5;
-            wt[1] = t.x;
-            wt[2] = t.y;
-            wt[3] = t.z;
-            wt[4] = t.w;
+            if (from_cta) {
+                const uint32_t *e = S.x.l[wi - 1][u % kMbXRing][lane];
+                wt[1] = e[0];
+                wt[2] = e[1];
+                wt[3] = e[2];
+                wt[4] = e[3];
+            } else {
+                const uint4 t = __ldcg((const uint4 *)(Y + (size_t)(y0 - 8 + lane) * W + x0));
+                wt[1] = t.x;
+                wt[2] = t.y;
+                wt[3] = t.z;
+                wt[4] = t.w;
+            }
         }
         const MbaffEdges mb = mbaff_shfl(m, lane | 16);  // the bottom MB's, for a frame pair
         __syncwarp();
@@ -1702,14 +1763,37 @@ __device__ void mbaff_luma_row(const PicDesc &p, int row, uint32_t *win, const L
             *(uint4 *)d = make_uint4(s[1], s[2], s[3], s[4]);
             if (x0 > 0) *(uint32_t *)(d - 4) = s[0];
         }
+        // the bottom rows for the warp below; this pair's left edge finished
+        // the previous pair's last columns
+        if (to_cta && lane < 8) {
+            const uint32_t *s = win + (32 + lane) * 5;
+            uint32_t *e = S.x.l[wi][u % kMbXRing][lane];
+            e[0] = s[1];
+            e[1] = s[2];
+            e[2] = s[3];
+            e[3] = s[4];
+            if (u > 0) S.x.l[wi][(u - 1) % kMbXRing][lane][3] = s[0];
+        }
         __syncwarp();
-        if (lane == 0) st_release(prog + 2 * row + 1, u + 1);
+        if (to_cta) {
+            __threadfence_block();
+            if (lane == 0) *(volatile int *)&S.done[wi] = u + 1;
+        } else if (lane == 0) {
+            st_release(prog + 2 * row + 1, u + 1);
+        }
+        if (from_cta && row > 0) {
+            __threadfence_block();
+            if (lane == 0) *(volatile int *)&S.used[wi] = u + 1;
+        }
     }
 }
 
-// Cb and Cr of MB-pair row `row`; win: 2 x 72 words (24 rows of 3 per plane).
-__device__ void mbaff_chroma_row(const PicDesc &p, int row, uint32_t *win, const LaunchState &st)
+// Cb and Cr of MB-pair row `row`, warp wi of nw in its block.
+__device__ void mbaff_chroma_row(const PicDesc &p, int row, int wi, int nw, DbMbaffShared &S, const LaunchState &st)
 {
+    uint32_t *win = S.win.c[wi];
+    const bool from_cta = wi > 0, to_cta = wi + 1 < nw;
+    int seen_used = 0;
     const int lane = threadIdx.x & 31, h = lane >> 4, pl = (lane >> 3) & 1, k = lane & 7;
     const int uw = (int)p.units_w, Wc = p.Wc, yc0 = row * 16;
     int *prog = p.progress + p.units_h;
@@ -1726,6 +1810,7 @@ __device__ void mbaff_chroma_row(const PicDesc &p, int row, uint32_t *win, const
     };
     fetch(0);
     for (int u = 0; u < uw; u++) {
+        if (to_cta && !cta_wait(st, &S.used[wi + 1], u + 1 - kMbXRing, seen_used)) return;
         const int xc0 = u * 8;
         const MbaffEdges m = nm;
         uint32_t *ws = win + 72 * sp;
@@ -1743,11 +1828,21 @@ __device__ void mbaff_chroma_row(const PicDesc &p, int row, uint32_t *win, const
         const int field = (m.ctl & kDbcField) != 0;
         // (yI + 1) / 2 of the MB's first luma row yI
         mbaff_edges_v<true>(xc0, field ? yc0 + h : yc0 + 8 * h, k, m, w);
-        if (row > 0 && !db_wait(st, prog + 2 * row - 2, min(u + 2, uw), seen)) return;
+        if (row > 0) {
+            const bool ok = from_cta ? cta_wait(st, &S.done[wi - 1], min(u + 2, uw), seen)
+                                     : db_wait(st, prog + 2 * row - 2, min(u + 2, uw), seen);
+            if (!ok) return;
+        }
         if (row > 0 && sr < 8) {
-            const uint2 t = __ldcg((const uint2 *)(Cs + (size_t)(yc0 - 8 + sr) * Wc + xc0));
-            ws[sr * 3 + 1] = t.x;
-            ws[sr * 3 + 2] = t.y;
+            if (from_cta) {
+                const uint32_t *e = S.x.c[wi - 1][u % kMbXRing][sp][sr];
+                ws[sr * 3 + 1] = e[0];
+                ws[sr * 3 + 2] = e[1];
+            } else {
+                const uint2 t = __ldcg((const uint2 *)(Cs + (size_t)(yc0 - 8 + sr) * Wc + xc0));
+                ws[sr * 3 + 1] = t.x;
+                ws[sr * 3 + 2] = t.y;
+            }
         }
         const MbaffEdges mb = mbaff_shfl(m, lane | 16);
         __syncwarp();
@@ -1766,8 +1861,24 @@ __device__ void mbaff_chroma_row(const PicDesc &p, int row, uint32_t *win, const
             *(uint2 *)d = make_uint2(s[1], s[2]);
             if (xc0 > 0) *(uint32_t *)(d - 4) = s[0];
         }
+        if (to_cta && sr < 8) {
+            const uint32_t *s = ws + (16 + sr) * 3;
+            uint32_t *e = S.x.c[wi][u % kMbXRing][sp][sr];
+            e[0] = s[1];
+            e[1] = s[2];
+            if (u > 0) S.x.c[wi][(u - 1) % kMbXRing][sp][sr][1] = s[0];
+        }
         __syncwarp();
-        if (lane == 0) st_release(prog + 2 * row, u + 1);
+        if (to_cta) {
+            __threadfence_block();
+            if (lane == 0) *(volatile int *)&S.done[wi] = u + 1;
+        } else if (lane == 0) {
+            st_release(prog + 2 * row, u + 1);
+        }
+        if (from_cta && row > 0) {
+            __threadfence_block();
+            if (lane == 0) *(volatile int *)&S.used[wi] = u + 1;
+        }
     }
 }
 
@@ -1816,30 +1927,6 @@ struct DbFrameShared {
     int used[kDbWarps];  // first row: MBs whose rows above were taken
 };
 
-// Wait (whole warp) until the shared-memory counter *flag >= target, with
-// the last value seen cached; bounded like the global waits.
-__device__ __forceinline__ bool cta_wait(const LaunchState &st, const int *flag, int target, int &seen)
-{
-    int ok = 1;
-    if ((threadIdx.x & 31) == 0 && seen < target) {
-        unsigned long long n = 0;
-        while ((seen = *(const volatile int *)flag) < target) {
-            if (++n > st.spin_limit) {
-                set_error(st, H264R_ERR_DEVICE_TIMEOUT);
-                ok = 0;
-                break;
-            }
-            if ((n & 255) == 0 && *(volatile int *)st.error != 0) {
-                ok = 0;
-                break;
-            }
-        }
-    }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    __syncwarp();
-    __threadfence_block();
-    return ok != 0;
-}
 
 __device__ __forceinline__ int db_tc0(uint32_t prm, int bS) { return (prm >> (11 + 5 * bS)) & 31; }
 
@@ -2144,27 +2231,31 @@ __device__ void deblock_pair_chroma(const PicDesc &p, int pair, int wi, int nw, 
     }
 }
 
-// 28 resident warps per SM (registers capped at 72)
-__global__ void __launch_bounds__(32, 28) k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st)
+// MBAFF pictures: a block of kMbWarps warps per kMbWarps MB-pair rows of one
+// plane (even block tickets luma, odd ones chroma); see DbMbaffShared.
+__global__ void __launch_bounds__(32 * kMbWarps, 24 / kMbWarps) k_deblock(const PicDesc *__restrict__ pics, int npics,
+                                                                        uint32_t total_units, LaunchState st)
 {
-    __shared__ uint32_t s_row;
-    const int lane = threadIdx.x;
-    if (lane == 0) s_row = atomicAdd(&st.ticket[1], 1u);
-    __syncwarp();
-    const uint32_t g = s_row;
+    __shared__ DbMbaffShared S;
+    __shared__ uint32_t s_unit;
+    if (threadIdx.x == 0) s_unit = atomicAdd(&st.ticket[1], 1u);
+    if (threadIdx.x < kMbWarps) {
+        S.done[threadIdx.x] = 0;
+        S.used[threadIdx.x] = 0;
+    }
+    __syncthreads();
+    const uint32_t g = s_unit;
     if (g >= total_units) return;
     const int pi = find_pic_by_db(pics, npics, g);
     const PicDesc p = pics[pi];
-    if (!p.deblock) return;
+    if (!p.deblock || !p.mbaff) return;
     const int unit = (int)(g - p.db_base);
-    __shared__ union {
-        uint32_t ml[200];
-        uint32_t mc[144];
-    } db_smem;
-    if (!p.mbaff) return;  // frame pictures have no k_deblock tickets (k_deblock_frame)
-    // MBAFF: even tickets luma of pair row unit/2, odd ones its chroma
-    if ((unit & 1) == 0) mbaff_luma_row(p, unit >> 1, db_smem.ml, st);
-    else mbaff_chroma_row(p, unit >> 1, db_smem.mc, st);
+    const int wi = threadIdx.x >> 5;
+    const int first = (unit >> 1) * kMbWarps;
+    const int nw = min(kMbWarps, (int)p.units_h - first);
+    if (wi >= nw) return;
+    if ((unit & 1) == 0) mbaff_luma_row(p, first + wi, wi, nw, S, st);
+    else mbaff_chroma_row(p, first + wi, wi, nw, S, st);
 }
 
 // Frame pictures: a block of kDbWarps warps per kDbWarps MB-row pairs of one
