@@ -560,6 +560,42 @@ __global__ void __launch_bounds__(32 * kInterWarps, 6) k_inter(const PicDesc *__
 // ======================================================================
 // K2: intra macroblocks, wavefront
 // ======================================================================
+// Intra_4x4 prediction (8.3.1.2.1 - 8.3.1.2.9, H264PictureBase.cpp:1062-1419)
+// as one formula: every sample of every mode but DC is
+// (w0*E[i0] + w1*E[i1] + w2*E[i2] + 2) >> 2 over E = {p[-1,-1], p[-1,0..3],
+// p[0..7,-1]} (a single sample is w = 4,0,0; a two-tap average 2,2,0; the
+// three-tap filter 1,2,1; the two corner cases 1,3,0).  Entry [mode][4y+x]:
+// i0 | i1 << 4 | i2 << 8 | w0 << 12 | w1 << 15 | w2 << 18, derived from the
+// mode formulas and checked against them sample by sample.
+__constant__ uint32_t kPred4[9][16] = {
+    {0x04005, 0x04006, 0x04007, 0x04008, 0x04005, 0x04006, 0x04007, 0x04008, 0x04005, 0x04006, 0x04007, 0x04008, 0x04005, 0x04006, 0x04007, 0x04008},
+    {0x04001, 0x04001, 0x04001, 0x04001, 0x04002, 0x04002, 0x04002, 0x04002, 0x04003, 0x04003, 0x04003, 0x04003, 0x04004, 0x04004, 0x04004, 0x04004},
+    {0x00000, 0x00000, 0x00000, 0x00000, 0x00000, 0x00000, 0x00000, 0x00000, 0x00000, 0x00000, 0x00000, 0x00000, 0x00000, 0x00000, 0x00000, 0x00000},
+    {0x51765, 0x51876, 0x51987, 0x51a98, 0x51876, 0x51987, 0x51a98, 0x51ba9, 0x51987, 0x51a98, 0x51ba9, 0x51cba, 0x51a98, 0x51ba9, 0x51cba, 0x190cb},
+    {0x51105, 0x51650, 0x51765, 0x51876, 0x51210, 0x51105, 0x51650, 0x51765, 0x51321, 0x51210, 0x51105, 0x51650, 0x51432, 0x51321, 0x51210, 0x51105},
+    {0x12050, 0x12065, 0x12076, 0x12087, 0x51501, 0x51650, 0x51765, 0x51876, 0x51012, 0x12050, 0x12065, 0x12076, 0x51123, 0x51501, 0x51650, 0x51765},
+    {0x12010, 0x51501, 0x51056, 0x51567, 0x12021, 0x51210, 0x12010, 0x51501, 0x12032, 0x51321, 0x12021, 0x51210, 0x12043, 0x51432, 0x12032, 0x51321},
+    {0x12065, 0x12076, 0x12087, 0x12098, 0x51765, 0x51876, 0x51987, 0x51a98, 0x12076, 0x12087, 0x12098, 0x120a9, 0x51876, 0x51987, 0x51a98, 0x51ba9},
+    {0x12021, 0x51321, 0x12032, 0x51432, 0x12032, 0x51432, 0x12043, 0x19043, 0x12043, 0x19043, 0x04004, 0x04004, 0x04004, 0x04004, 0x04004, 0x04004},
+};
+
+// Intra_8x8 prediction (8.3.2.2.2 - 8.3.2.2.10, H264PictureBase.cpp:1600-1846)
+// in the same form over the filtered E = {p'[-1,-1], p'[-1,0..7],
+// p'[0..15,-1]}: entry [mode][8y+x] = i0 | i1 << 5 | i2 << 10 | w0 << 15 |
+// w1 << 18 | w2 << 21.  Global memory: the 32 lanes of a warp read 32
+// consecutive entries.
+__device__ const uint32_t kPred8[9][64] = {
+    {0x020009, 0x02000a, 0x02000b, 0x02000c, 0x02000d, 0x02000e, 0x02000f, 0x020010, 0x020009, 0x02000a, 0x02000b, 0x02000c, 0x02000d, 0x02000e, 0x02000f, 0x020010, 0x020009, 0x02000a, 0x02000b, 0x02000c, 0x02000d, 0x02000e, 0x02000f, 0x020010, 0x020009, 0x02000a, 0x02000b, 0x02000c, 0x02000d, 0x02000e, 0x02000f, 0x020010, 0x020009, 0x02000a, 0x02000b, 0x02000c, 0x02000d, 0x02000e, 0x02000f, 0x020010, 0x020009, 0x02000a, 0x02000b, 0x02000c, 0x02000d, 0x02000e, 0x02000f, 0x020010, 0x020009, 0x02000a, 0x02000b, 0x02000c, 0x02000d, 0x02000e, 0x02000f, 0x020010, 0x020009, 0x02000a, 0x02000b, 0x02000c, 0x02000d, 0x02000e, 0x02000f, 0x020010},
+    {0x020001, 0x020001, 0x020001, 0x020001, 0x020001, 0x020001, 0x020001, 0x020001, 0x020002, 0x020002, 0x020002, 0x020002, 0x020002, 0x020002, 0x020002, 0x020002, 0x020003, 0x020003, 0x020003, 0x020003, 0x020003, 0x020003, 0x020003, 0x020003, 0x020004, 0x020004, 0x020004, 0x020004, 0x020004, 0x020004, 0x020004, 0x020004, 0x020005, 0x020005, 0x020005, 0x020005, 0x020005, 0x020005, 0x020005, 0x020005, 0x020006, 0x020006, 0x020006, 0x020006, 0x020006, 0x020006, 0x020006, 0x020006, 0x020007, 0x020007, 0x020007, 0x020007, 0x020007, 0x020007, 0x020007, 0x020007, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008},
+    {0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000, 0x000000},
+    {0x28ad49, 0x28b16a, 0x28b58b, 0x28b9ac, 0x28bdcd, 0x28c1ee, 0x28c60f, 0x28ca30, 0x28b16a, 0x28b58b, 0x28b9ac, 0x28bdcd, 0x28c1ee, 0x28c60f, 0x28ca30, 0x28ce51, 0x28b58b, 0x28b9ac, 0x28bdcd, 0x28c1ee, 0x28c60f, 0x28ca30, 0x28ce51, 0x28d272, 0x28b9ac, 0x28bdcd, 0x28c1ee, 0x28c60f, 0x28ca30, 0x28ce51, 0x28d272, 0x28d693, 0x28bdcd, 0x28c1ee, 0x28c60f, 0x28ca30, 0x28ce51, 0x28d272, 0x28d693, 0x28dab4, 0x28c1ee, 0x28c60f, 0x28ca30, 0x28ce51, 0x28d272, 0x28d693, 0x28dab4, 0x28ded5, 0x28c60f, 0x28ca30, 0x28ce51, 0x28d272, 0x28d693, 0x28dab4, 0x28ded5, 0x28e2f6, 0x28ca30, 0x28ce51, 0x28d272, 0x28d693, 0x28dab4, 0x28ded5, 0x28e2f6, 0x0c8317},
+    {0x288409, 0x28a920, 0x28ad49, 0x28b16a, 0x28b58b, 0x28b9ac, 0x28bdcd, 0x28c1ee, 0x288820, 0x288409, 0x28a920, 0x28ad49, 0x28b16a, 0x28b58b, 0x28b9ac, 0x28bdcd, 0x288c41, 0x288820, 0x288409, 0x28a920, 0x28ad49, 0x28b16a, 0x28b58b, 0x28b9ac, 0x289062, 0x288c41, 0x288820, 0x288409, 0x28a920, 0x28ad49, 0x28b16a, 0x28b58b, 0x289483, 0x289062, 0x288c41, 0x288820, 0x288409, 0x28a920, 0x28ad49, 0x28b16a, 0x2898a4, 0x289483, 0x289062, 0x288c41, 0x288820, 0x288409, 0x28a920, 0x28ad49, 0x289cc5, 0x2898a4, 0x289483, 0x289062, 0x288c41, 0x288820, 0x288409, 0x28a920, 0x28a0e6, 0x289cc5, 0x2898a4, 0x289483, 0x289062, 0x288c41, 0x288820, 0x288409},
+    {0x090120, 0x090149, 0x09016a, 0x09018b, 0x0901ac, 0x0901cd, 0x0901ee, 0x09020f, 0x28a401, 0x28a920, 0x28ad49, 0x28b16a, 0x28b58b, 0x28b9ac, 0x28bdcd, 0x28c1ee, 0x288022, 0x090120, 0x090149, 0x09016a, 0x09018b, 0x0901ac, 0x0901cd, 0x0901ee, 0x288443, 0x28a401, 0x28a920, 0x28ad49, 0x28b16a, 0x28b58b, 0x28b9ac, 0x28bdcd, 0x288864, 0x288022, 0x090120, 0x090149, 0x09016a, 0x09018b, 0x0901ac, 0x0901cd, 0x288c85, 0x288443, 0x28a401, 0x28a920, 0x28ad49, 0x28b16a, 0x28b58b, 0x28b9ac, 0x2890a6, 0x288864, 0x288022, 0x090120, 0x090149, 0x09016a, 0x09018b, 0x0901ac, 0x2894c7, 0x288c85, 0x288443, 0x28a401, 0x28a920, 0x28ad49, 0x28b16a, 0x28b58b},
+    {0x090020, 0x28a401, 0x28812a, 0x28a54b, 0x28a96c, 0x28ad8d, 0x28b1ae, 0x28b5cf, 0x090041, 0x288820, 0x090020, 0x28a401, 0x28812a, 0x28a54b, 0x28a96c, 0x28ad8d, 0x090062, 0x288c41, 0x090041, 0x288820, 0x090020, 0x28a401, 0x28812a, 0x28a54b, 0x090083, 0x289062, 0x090062, 0x288c41, 0x090041, 0x288820, 0x090020, 0x28a401, 0x0900a4, 0x289483, 0x090083, 0x289062, 0x090062, 0x288c41, 0x090041, 0x288820, 0x0900c5, 0x2898a4, 0x0900a4, 0x289483, 0x090083, 0x289062, 0x090062, 0x288c41, 0x0900e6, 0x289cc5, 0x0900c5, 0x2898a4, 0x0900a4, 0x289483, 0x090083, 0x289062, 0x090107, 0x28a0e6, 0x0900e6, 0x289cc5, 0x0900c5, 0x2898a4, 0x0900a4, 0x289483},
+    {0x090149, 0x09016a, 0x09018b, 0x0901ac, 0x0901cd, 0x0901ee, 0x09020f, 0x090230, 0x28ad49, 0x28b16a, 0x28b58b, 0x28b9ac, 0x28bdcd, 0x28c1ee, 0x28c60f, 0x28ca30, 0x09016a, 0x09018b, 0x0901ac, 0x0901cd, 0x0901ee, 0x09020f, 0x090230, 0x090251, 0x28b16a, 0x28b58b, 0x28b9ac, 0x28bdcd, 0x28c1ee, 0x28c60f, 0x28ca30, 0x28ce51, 0x09018b, 0x0901ac, 0x0901cd, 0x0901ee, 0x09020f, 0x090230, 0x090251, 0x090272, 0x28b58b, 0x28b9ac, 0x28bdcd, 0x28c1ee, 0x28c60f, 0x28ca30, 0x28ce51, 0x28d272, 0x0901ac, 0x0901cd, 0x0901ee, 0x09020f, 0x090230, 0x090251, 0x090272, 0x090293, 0x28b9ac, 0x28bdcd, 0x28c1ee, 0x28c60f, 0x28ca30, 0x28ce51, 0x28d272, 0x28d693},
+    {0x090041, 0x288c41, 0x090062, 0x289062, 0x090083, 0x289483, 0x0900a4, 0x2898a4, 0x090062, 0x289062, 0x090083, 0x289483, 0x0900a4, 0x2898a4, 0x0900c5, 0x289cc5, 0x090083, 0x289483, 0x0900a4, 0x2898a4, 0x0900c5, 0x289cc5, 0x0900e6, 0x28a0e6, 0x0900a4, 0x2898a4, 0x0900c5, 0x289cc5, 0x0900e6, 0x28a0e6, 0x090107, 0x0c8107, 0x0900c5, 0x289cc5, 0x0900e6, 0x28a0e6, 0x090107, 0x0c8107, 0x020008, 0x020008, 0x0900e6, 0x28a0e6, 0x090107, 0x0c8107, 0x020008, 0x020008, 0x020008, 0x020008, 0x090107, 0x0c8107, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008, 0x020008},
+};
+
 struct IntraSmem {
     int32_t res[384];     // residual: luma raster 16x16, Cb 8x8, Cr 8x8
     int nb[40];           // neighbouring samples (-1: not available)
@@ -570,6 +606,7 @@ struct IntraSmem {
     // overlaps the current MB's work
     __align__(16) uint32_t raw[2][192];
     __align__(16) h264r_mb rec[2];
+    uint32_t pred4[9][16];  // kPred4, for lane-varying reads
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -593,155 +630,6 @@ __device__ __forceinline__ void intra_prefetch(const PicDesc &p, int addr, Intra
         ((uint32_t *)&s.rec[buf])[lane] = ((const uint32_t *)rec)[lane];
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
-}
-
-// 4x4 prediction sample (x, y) from nb = {p[-1,-1], p[-1,0..3], p[0..7,-1]}
-// (Intra_4x4_sample_prediction, H264PictureBase.cpp:1062-1419); returns -1
-// when the mode's samples are not available (prediction not written).
-__device__ int pred4x4_sample(int mode, const int *nb, int x, int y)
-{
-#define L(i) nb[1 + (i)]
-#define T(i) nb[5 + (i)]
-#define C nb[0]
-    bool top = T(0) >= 0 && T(1) >= 0 && T(2) >= 0 && T(3) >= 0;
-    bool top8 = top && T(4) >= 0 && T(5) >= 0 && T(6) >= 0 && T(7) >= 0;
-    bool left = L(0) >= 0 && L(1) >= 0 && L(2) >= 0 && L(3) >= 0;
-    bool corner = C >= 0;
-    auto pt = [&](int xx, int yy) -> int { return yy < 0 ? (xx < 0 ? C : T(xx)) : L(yy); };
-    switch (mode) {
-    case 0: return top ? T(x) : -1;
-    case 1: return left ? L(y) : -1;
-    case 2:
-        if (top && left) return (T(0) + T(1) + T(2) + T(3) + L(0) + L(1) + L(2) + L(3) + 4) >> 3;
-        if (left) return (L(0) + L(1) + L(2) + L(3) + 2) >> 2;
-        if (top) return (T(0) + T(1) + T(2) + T(3) + 2) >> 2;
-        return 128;
-    case 3:
-        if (!top8) return -1;
-        if (x == 3 && y == 3) return (T(6) + 3 * T(7) + 2) >> 2;
-        return (T(x + y) + 2 * T(x + y + 1) + T(x + y + 2) + 2) >> 2;
-    case 4:
-        if (!(top && left && corner)) return -1;
-        if (x > y) return (pt(x - y - 2, -1) + 2 * pt(x - y - 1, -1) + pt(x - y, -1) + 2) >> 2;
-        if (x < y) return (pt(-1, y - x - 2) + 2 * pt(-1, y - x - 1) + pt(-1, y - x) + 2) >> 2;
-        return (T(0) + 2 * C + L(0) + 2) >> 2;
-    case 5: {
-        if (!(top && left && corner)) return -1;
-        int z = 2 * x - y;
-        if (z >= 0 && (z & 1) == 0) return (pt(x - (y >> 1) - 1, -1) + pt(x - (y >> 1), -1) + 1) >> 1;
-        if (z >= 0) return (pt(x - (y >> 1) - 2, -1) + 2 * pt(x - (y >> 1) - 1, -1) + pt(x - (y >> 1), -1) + 2) >> 2;
-        if (z == -1) return (L(0) + 2 * C + T(0) + 2) >> 2;
-        return (pt(-1, y - 1) + 2 * pt(-1, y - 2) + pt(-1, y - 3) + 2) >> 2;
-    }
-    case 6: {
-        if (!(top && left && corner)) return -1;
-        int z = 2 * y - x;
-        if (z >= 0 && (z & 1) == 0) return (pt(-1, y - (x >> 1) - 1) + pt(-1, y - (x >> 1)) + 1) >> 1;
-        if (z >= 0) return (pt(-1, y - (x >> 1) - 2) + 2 * pt(-1, y - (x >> 1) - 1) + pt(-1, y - (x >> 1)) + 2) >> 2;
-        if (z == -1) return (L(0) + 2 * C + T(0) + 2) >> 2;
-        return (pt(x - 1, -1) + 2 * pt(x - 2, -1) + pt(x - 3, -1) + 2) >> 2;
-    }
-    case 7:
-        if (!top8) return -1;
-        if ((y & 1) == 0) return (T(x + (y >> 1)) + T(x + (y >> 1) + 1) + 1) >> 1;
-        return (T(x + (y >> 1)) + 2 * T(x + (y >> 1) + 1) + T(x + (y >> 1) + 2) + 2) >> 2;
-    case 8: {
-        if (!left) return -1;
-        int z = x + 2 * y;
-        if (z <= 4 && (z & 1) == 0) return (L(y + (x >> 1)) + L(y + (x >> 1) + 1) + 1) >> 1;
-        if (z < 5) return (L(y + (x >> 1)) + 2 * L(y + (x >> 1) + 1) + L(y + (x >> 1) + 2) + 2) >> 2;
-        if (z == 5) return (L(2) + 3 * L(3) + 2) >> 2;
-        return L(3);
-    }
-    }
-    return -1;
-#undef L
-#undef T
-#undef C
-}
-
-// 8x8 prediction sample from filtered nb = {p'[-1,-1], p'[-1,0..7], p'[0..15,-1]}
-// (Intra_8x8_sample_prediction, H264PictureBase.cpp:1600-1846)
-__device__ int pred8x8_sample(int mode, const int *nb, int x, int y)
-{
-#define L(i) nb[1 + (i)]
-#define T(i) nb[9 + (i)]
-#define C nb[0]
-    bool top = true, topr = true, left = true;
-    for (int i = 0; i < 8; i++) { top = top && T(i) >= 0; left = left && L(i) >= 0; }
-    topr = top;
-    for (int i = 8; i < 16; i++) topr = topr && T(i) >= 0;
-    bool corner = C >= 0;
-    auto pt = [&](int xx, int yy) -> int { return yy < 0 ? (xx < 0 ? C : T(xx)) : L(yy); };
-    switch (mode) {
-    case 0: return top ? T(x) : -1;
-    case 1: return left ? L(y) : -1;
-    case 2: {
-        int st = 0, sl = 0;
-        for (int i = 0; i < 8; i++) { st += top ? T(i) : 0; sl += left ? L(i) : 0; }
-        if (top && left) return (st + sl + 8) >> 4;
-        if (left) return (sl + 4) >> 3;
-        if (top) return (st + 4) >> 3;
-        return 128;
-    }
-    case 3:
-        if (!topr) return -1;
-        if (x == 7 && y == 7) return (T(14) + 3 * T(15) + 2) >> 2;
-        return (T(x + y) + 2 * T(x + y + 1) + T(x + y + 2) + 2) >> 2;
-    case 4:
-        if (!(top && left && corner)) return -1;
-        if (x > y) return (pt(x - y - 2, -1) + 2 * pt(x - y - 1, -1) + pt(x - y, -1) + 2) >> 2;
-        if (x < y) return (pt(-1, y - x - 2) + 2 * pt(-1, y - x - 1) + pt(-1, y - x) + 2) >> 2;
-        return (T(0) + 2 * C + L(0) + 2) >> 2;
-    case 5: {
-        if (!(top && left && corner)) return -1;
-        int z = 2 * x - y;
-        if (z >= 0 && (z & 1) == 0) return (pt(x - (y >> 1) - 1, -1) + pt(x - (y >> 1), -1) + 1) >> 1;
-        if (z >= 0) return (pt(x - (y >> 1) - 2, -1) + 2 * pt(x - (y >> 1) - 1, -1) + pt(x - (y >> 1), -1) + 2) >> 2;
-        if (z == -1) return (L(0) + 2 * C + T(0) + 2) >> 2;
-        return (pt(-1, y - 2 * x - 1) + 2 * pt(-1, y - 2 * x - 2) + pt(-1, y - 2 * x - 3) + 2) >> 2;
-    }
-    case 6: {
-        if (!(top && left && corner)) return -1;
-        int z = 2 * y - x;
-        if (z >= 0 && (z & 1) == 0) return (pt(-1, y - (x >> 1) - 1) + pt(-1, y - (x >> 1)) + 1) >> 1;
-        if (z >= 0) return (pt(-1, y - (x >> 1) - 2) + 2 * pt(-1, y - (x >> 1) - 1) + pt(-1, y - (x >> 1)) + 2) >> 2;
-        if (z == -1) return (L(0) + 2 * C + T(0) + 2) >> 2;
-        return (pt(x - 2 * y - 1, -1) + 2 * pt(x - 2 * y - 2, -1) + pt(x - 2 * y - 3, -1) + 2) >> 2;
-    }
-    case 7:
-        if (!topr) return -1;
-        if ((y & 1) == 0) return (T(x + (y >> 1)) + T(x + (y >> 1) + 1) + 1) >> 1;
-        return (T(x + (y >> 1)) + 2 * T(x + (y >> 1) + 1) + T(x + (y >> 1) + 2) + 2) >> 2;
-    case 8: {
-        if (!left) return -1;
-        int z = x + 2 * y;
-        if (z <= 12 && (z & 1) == 0) return (L(y + (x >> 1)) + L(y + (x >> 1) + 1) + 1) >> 1;
-        if (z < 13) return (L(y + (x >> 1)) + 2 * L(y + (x >> 1) + 1) + L(y + (x >> 1) + 2) + 2) >> 2;
-        if (z == 13) return (L(6) + 3 * L(7) + 2) >> 2;
-        return L(7);
-    }
-    }
-    return -1;
-#undef L
-#undef T
-#undef C
-}
-
-__device__ __forceinline__ int ldcg_u8(const uint8_t *ptr) { return (int)__ldcg(ptr); }
-
-// The MB's residual, computed by k_inter, into res (int32 per sample).
-__device__ __forceinline__ void load_intra_residual(const PicDesc &p, int addr, int32_t *res)
-{
-    const int lane = threadIdx.x & 31;
-    const uint32_t *src = (const uint32_t *)(p.ires + (size_t)addr * 384);
-#pragma unroll
-    for (int t = 0; t < 6; t++) {
-        const int i = lane + 32 * t;
-        const uint32_t w = __ldcg(src + i);
-        res[2 * i] = (int16_t)(w & 0xFFFFu);
-        res[2 * i + 1] = (int16_t)(w >> 16);
-    }
 }
 
 // ---------------------------------------------------------------- tiled intra MB
@@ -855,11 +743,11 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
             const bool valid = by >= 0 && bx >= 0 && bx <= 3;
             const int b = 8 * (by >> 1) + 4 * (bx >> 1) + 2 * (by & 1) + (bx & 1);
             const int xO = bx * 4, yO = by * 4;
+            int v = -1;
             if (valid && hl < 13) {
                 // nb = {p[-1,-1], p[-1,0..3], p[0..7,-1]}; an unavailable
                 // top-right quartet takes p[3,-1] (the four are available
                 // together or not at all)
-                int v;
                 if (hl == 0) {
                     v = tile_nb(t, xO - 1, yO - 1, true);
                 } else if (hl < 5) {
@@ -871,12 +759,27 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
                 }
                 nb[hl] = v;
             }
+            // availability of the half's 13 samples (bit k: nb[k] available)
+            const uint32_t am = (__ballot_sync(0xffffffffu, v >= 0) >> (16 * half)) & 0x1FFFu;
             __syncwarp();
             if (valid) {
                 const int i = hl >> 2, j = hl & 3;
                 const int mode = (m.ipred[b >> 3] >> (4 * (b & 7))) & 15;
-                int pv = pred4x4_sample(mode, nb, j, i);
-                if (pv < 0) pv = 0;  // prediction not written: the cleared buffer
+                const bool corner = am & 1u, left = ((am >> 1) & 15u) == 15u, top = ((am >> 5) & 15u) == 15u;
+                const bool top8 = ((am >> 5) & 0xFFu) == 0xFFu;
+                int pv = 0;  // a mode without its samples writes no prediction: the cleared buffer
+                if (mode == 2) {
+                    const int st4 = top ? nb[5] + nb[6] + nb[7] + nb[8] : 0, sl4 = left ? nb[1] + nb[2] + nb[3] + nb[4] : 0;
+                    pv = (top && left) ? (st4 + sl4 + 4) >> 3 : left ? (sl4 + 2) >> 2 : top ? (st4 + 2) >> 2 : 128;
+                } else if (mode <= 8) {
+                    const bool ok = mode == 0 ? top : (mode == 1 || mode == 8) ? left : (mode == 3 || mode == 7) ? top8
+                                                                                                      : (top && left && corner);
+                    if (ok) {
+                        const uint32_t e = s.pred4[mode][hl];
+                        pv = ((int)((e >> 12) & 7u) * nb[e & 15u] + (int)((e >> 15) & 7u) * nb[(e >> 4) & 15u] +
+                              (int)((e >> 18) & 7u) * nb[(e >> 8) & 15u] + 2) >> 2;
+                    }
+                }
                 t.l[yO + i + 1][xO + j + 1] = clip1(pv + s.res[(yO + i) * 16 + xO + j]);
             }
             __syncwarp();
@@ -907,6 +810,7 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
             __syncwarp();
             // 8.3.2.2.1 reference sample filtering, one sample per lane
             // (H264PictureBase.cpp:1540-1600)
+            int fsample = -1;
             if (lane < 25) {
                 const int *q = s.nb;
                 int f = -1;
@@ -929,13 +833,36 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
                     else f = (q[23] + 3 * q[24] + 2) >> 2;
                 }
                 s.nbf[lane] = f;
+                fsample = f;
             }
+            // availability of the 25 filtered samples (bit k: s.nbf[k])
+            const uint32_t fm = __ballot_sync(0xffffffffu, lane < 25 && fsample >= 0);
             __syncwarp();
             const int mode = (m.ipred[0] >> (4 * b)) & 15;
+            const bool corner = fm & 1u, left = ((fm >> 1) & 0xFFu) == 0xFFu, top = ((fm >> 9) & 0xFFu) == 0xFFu;
+            const bool topr = ((fm >> 9) & 0xFFFFu) == 0xFFFFu;
+            const bool ok = mode == 0 ? top : (mode == 1 || mode == 8) ? left : (mode == 3 || mode == 7) ? topr
+                                                                                              : (top && left && corner);
+            int dcv = 128;
+            if (mode == 2) {
+                int st8 = 0, sl8 = 0;
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    st8 += top ? s.nbf[9 + q] : 0;
+                    sl8 += left ? s.nbf[1 + q] : 0;
+                }
+                dcv = (top && left) ? (st8 + sl8 + 8) >> 4 : left ? (sl8 + 4) >> 3 : top ? (st8 + 4) >> 3 : 128;
+            }
             for (int kk = lane; kk < 64; kk += 32) {
-                int i = kk >> 3, j = kk & 7;
-                int pv = pred8x8_sample(mode, s.nbf, j, i);
-                if (pv < 0) pv = 0;
+                const int i = kk >> 3, j = kk & 7;
+                int pv = 0;  // a mode without its samples writes no prediction: the cleared buffer
+                if (mode == 2) {
+                    pv = dcv;
+                } else if (mode <= 8 && ok) {
+                    const uint32_t e = __ldg(&kPred8[mode][kk]);
+                    pv = ((int)((e >> 15) & 7u) * s.nbf[e & 31u] + (int)((e >> 18) & 7u) * s.nbf[(e >> 5) & 31u] +
+                          (int)((e >> 21) & 7u) * s.nbf[(e >> 10) & 31u] + 2) >> 2;
+                }
                 t.l[yO + i + 1][xO + j + 1] = clip1(pv + s.res[(yO + i) * 16 + xO + j]);
             }
             __syncwarp();
@@ -1031,6 +958,7 @@ __global__ void __launch_bounds__(32, 21) k_intra(const PicDesc *__restrict__ pi
     __shared__ uint32_t s_row;
     const int lane = threadIdx.x;
     if (lane == 0) s_row = atomicAdd(&st.ticket[0], 1u);
+    for (int i = lane; i < 9 * 16; i += 32) (&s.pred4[0][0])[i] = (&kPred4[0][0])[i];
     __syncwarp();
     const uint32_t g = s_row;
     if (g >= total_rows) return;
