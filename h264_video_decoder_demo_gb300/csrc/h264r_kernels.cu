@@ -607,6 +607,7 @@ struct IntraSmem {
     __align__(16) uint32_t raw[2][192];
     __align__(16) h264r_mb rec[2];
     uint32_t pred4[9][16];  // kPred4, for lane-varying reads
+    int cpar[8];            // chroma: DC per plane and quadrant, or plane a, b, c per plane
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -900,41 +901,44 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
         }
         __syncwarp();
     }
-    // ---- chroma; quirk: DC treats a neighbouring value 0 as unavailable
+    // ---- chroma (Intra_chroma_sample_prediction, H264PictureBase.cpp:2076-2385):
+    //      the per-MB values first (DC of each 4x4 quadrant, or the plane
+    //      parameters), one per lane; quirk: DC treats a neighbouring value
+    //      0 as unavailable
     const int cmode = m.chroma_mode;
+    if (cmode == 0 && lane < 8) {
+        const int pl = lane >> 2, xO = (lane & 1) * 4, yO = (lane & 2) * 2;
+        const int(*c)[9] = t.c[pl];  // c[0][0] corner, c[1+u][0] left, c[0][1+u] top
+        const bool t4 = c[0][1 + xO] > 0 && c[0][2 + xO] > 0 && c[0][3 + xO] > 0 && c[0][4 + xO] > 0;
+        const bool l4 = c[1 + yO][0] > 0 && c[2 + yO][0] > 0 && c[3 + yO][0] > 0 && c[4 + yO][0] > 0;
+        const int stp = t4 ? c[0][1 + xO] + c[0][2 + xO] + c[0][3 + xO] + c[0][4 + xO] : 0;
+        const int slf = l4 ? c[1 + yO][0] + c[2 + yO][0] + c[3 + yO][0] + c[4 + yO][0] : 0;
+        int pv;
+        if ((xO == 0 && yO == 0) || (xO > 0 && yO > 0)) pv = (t4 && l4) ? (stp + slf + 4) >> 3 : l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
+        else if (xO > 0) pv = t4 ? (stp + 2) >> 2 : l4 ? (slf + 2) >> 2 : 128;
+        else pv = l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
+        s.cpar[lane] = pv;
+    } else if (cmode == 3 && lane < 2 && cA && cB && cD) {
+        const int(*c)[9] = t.c[lane];
+        int H = 0, V = 0;
+        for (int u = 0; u <= 3; u++) {
+            H += (u + 1) * (c[0][5 + u] - (2 - u >= 0 ? c[0][3 - u] : c[0][0]));
+            V += (u + 1) * (c[5 + u][0] - (2 - u >= 0 ? c[3 - u][0] : c[0][0]));
+        }
+        s.cpar[3 * lane] = 16 * (c[8][0] + c[0][8]);
+        s.cpar[3 * lane + 1] = (34 * H + 32) >> 6;
+        s.cpar[3 * lane + 2] = (34 * V + 32) >> 6;
+    }
+    __syncwarp();
     for (int kk = lane; kk < 128; kk += 32) {
         const int pl = kk >> 6, i = (kk & 63) >> 3, j = kk & 7;
-        const int(*c)[9] = t.c[pl];  // c[0][0] corner, c[1+u][0] left, c[0][1+u] top
-#define CL(u) c[1 + (u)][0]
-#define CT(u) c[0][1 + (u)]
+        const int(*c)[9] = t.c[pl];
         int pv = 0;
-        if (cmode == 0) {
-            const int xO = j & 4, yO = i & 4;
-            const bool t4 = CT(xO) > 0 && CT(xO + 1) > 0 && CT(xO + 2) > 0 && CT(xO + 3) > 0;
-            const bool l4 = CL(yO) > 0 && CL(yO + 1) > 0 && CL(yO + 2) > 0 && CL(yO + 3) > 0;
-            const int stp = t4 ? CT(xO) + CT(xO + 1) + CT(xO + 2) + CT(xO + 3) : 0;
-            const int slf = l4 ? CL(yO) + CL(yO + 1) + CL(yO + 2) + CL(yO + 3) : 0;
-            if ((xO == 0 && yO == 0) || (xO > 0 && yO > 0)) pv = (t4 && l4) ? (stp + slf + 4) >> 3 : l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
-            else if (xO > 0) pv = t4 ? (stp + 2) >> 2 : l4 ? (slf + 2) >> 2 : 128;
-            else pv = l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
-        } else if (cmode == 1) {
-            pv = cA ? CL(i) : 0;
-        } else if (cmode == 2) {
-            pv = cB ? CT(j) : 0;
-        } else if (cmode == 3) {
-            if (cA && cB && cD) {
-                int H = 0, V = 0;
-                for (int u = 0; u <= 3; u++) {
-                    H += (u + 1) * (CT(4 + u) - (2 - u >= 0 ? CT(2 - u) : c[0][0]));
-                    V += (u + 1) * (CL(4 + u) - (2 - u >= 0 ? CL(2 - u) : c[0][0]));
-                }
-                const int a = 16 * (CL(7) + CT(7));
-                const int b2 = (34 * H + 32) >> 6, c2 = (34 * V + 32) >> 6;
-                pv = clip1((a + b2 * (j - 3) + c2 * (i - 3) + 16) >> 5);
-            }
-        }
-#undef CL
-#undef CT
+        if (cmode == 0) pv = s.cpar[4 * pl + (i >> 2) * 2 + (j >> 2)];
+        else if (cmode == 1) pv = cA ? c[1 + i][0] : 0;
+        else if (cmode == 2) pv = cB ? c[0][1 + j] : 0;
+        else if (cmode == 3 && cA && cB && cD)
+            pv = clip1((s.cpar[3 * pl] + s.cpar[3 * pl + 1] * (j - 3) + s.cpar[3 * pl + 2] * (i - 3) + 16) >> 5);
         s.res[256 + kk] = clip1(pv + s.res[256 + kk]);  // reconstructed chroma, in place
     }
     __syncwarp();
