@@ -428,80 +428,6 @@ __device__ __forceinline__ RefView ref_view(const PicDesc &p, int ref)
     return r;
 }
 
-// 8.4.2.2.1 Luma_sample_interpolation_process (H264InterPrediction.cpp:2344-2480)
-__device__ __forceinline__ int luma_sample(const RefView &r, int ymax, int xi, int yi, int xf, int yf)
-{
-#define S(dx, dy) ((int)__ldg(r.y + (size_t)H264R_CLIP3(0, ymax, yi + (dy)) * r.ystride + H264R_CLIP3(0, r.xmax, xi + (dx))))
-#define TAP(a, b, c_, d, e, f) ((a) - 5 * (b) + 20 * (c_) + 20 * (d) - 5 * (e) + (f))
-    int G = S(0, 0);
-    if ((xf | yf) == 0) return G;
-    if (yf == 0) {  // a, b, c
-        int b = clip1((TAP(S(-2, 0), S(-1, 0), G, S(1, 0), S(2, 0), S(3, 0)) + 16) >> 5);
-        if (xf == 2) return b;
-        return xf == 1 ? (G + b + 1) >> 1 : (S(1, 0) + b + 1) >> 1;
-    }
-    if (xf == 0) {  // d, h, n
-        int h = clip1((TAP(S(0, -2), S(0, -1), G, S(0, 1), S(0, 2), S(0, 3)) + 16) >> 5);
-        if (yf == 2) return h;
-        return yf == 1 ? (G + h + 1) >> 1 : (S(0, 1) + h + 1) >> 1;
-    }
-    if (xf == 2 || yf == 2) {  // f, i, j, k, q
-        int cc = TAP(S(-2, -2), S(-2, -1), S(-2, 0), S(-2, 1), S(-2, 2), S(-2, 3));
-        int dd = TAP(S(-1, -2), S(-1, -1), S(-1, 0), S(-1, 1), S(-1, 2), S(-1, 3));
-        int h1 = TAP(S(0, -2), S(0, -1), G, S(0, 1), S(0, 2), S(0, 3));
-        int m1 = TAP(S(1, -2), S(1, -1), S(1, 0), S(1, 1), S(1, 2), S(1, 3));
-        int ee = TAP(S(2, -2), S(2, -1), S(2, 0), S(2, 1), S(2, 2), S(2, 3));
-        int ff = TAP(S(3, -2), S(3, -1), S(3, 0), S(3, 1), S(3, 2), S(3, 3));
-        int j = clip1((TAP(cc, dd, h1, m1, ee, ff) + 512) >> 10);
-        if (xf == 2 && yf == 2) return j;
-        if (xf == 2) {  // f (yf 1) / q (yf 3)
-            int row = yf == 1 ? 0 : 1;
-            int b = clip1((TAP(S(-2, row), S(-1, row), S(0, row), S(1, row), S(2, row), S(3, row)) + 16) >> 5);
-            return (b + j + 1) >> 1;
-        }
-        // i (xf 1) / k (xf 3)
-        int hh = clip1(((xf == 1 ? h1 : m1) + 16) >> 5);
-        return (hh + j + 1) >> 1;
-    }
-    // e, g, p, r: average of a horizontal and a vertical half sample
-    int row = yf == 1 ? 0 : 1, col = xf == 1 ? 0 : 1;
-    int b = clip1((TAP(S(-2, row), S(-1, row), S(0, row), S(1, row), S(2, row), S(3, row)) + 16) >> 5);
-    int h = clip1((TAP(S(col, -2), S(col, -1), S(col, 0), S(col, 1), S(col, 2), S(col, 3)) + 16) >> 5);
-    return (b + h + 1) >> 1;
-#undef S
-#undef TAP
-}
-
-// 8.4.2.2.2 (H264InterPrediction.cpp:2485-2522)
-__device__ __forceinline__ int chroma_sample(const uint8_t *pl, int stride, int xmax, int ymax, int xi, int yi, int xf, int yf)
-{
-    int xa = H264R_CLIP3(0, xmax, xi), xb = H264R_CLIP3(0, xmax, xi + 1);
-    int ya = H264R_CLIP3(0, ymax, yi), yb = H264R_CLIP3(0, ymax, yi + 1);
-    int A = __ldg(pl + (size_t)ya * stride + xa), B = __ldg(pl + (size_t)ya * stride + xb);
-    int C = __ldg(pl + (size_t)yb * stride + xa), D = __ldg(pl + (size_t)yb * stride + xb);
-    return ((8 - xf) * (8 - yf) * A + xf * (8 - yf) * B + (8 - xf) * yf * C + xf * yf * D + 32) >> 6;
-}
-
-// 8.4.2.3 (H264InterPrediction.cpp:2526-2829); quirk: explicit weights with
-// only list 1 in use apply w0/o0 to luma
-__device__ __forceinline__ int weigh(const h264r_weight &w, int comp, bool use0, bool use1, int p0, int p1)
-{
-    if (!use0 && !use1) return 0;
-    if (!w.weighted) {
-        if (use0 && use1) return (p0 + p1 + 1) >> 1;
-        return use0 ? p0 : p1;
-    }
-    int lw = w.log_wd[comp];
-    if (use0 && use1)
-        return clip1(((p0 * w.w0[comp] + p1 * w.w1[comp] + (1 << lw)) >> (lw + 1)) + ((w.o0[comp] + w.o1[comp] + 1) >> 1));
-    int pv = use0 ? p0 : p1;
-    int ww, oo;
-    if (use0 || comp == 0) { ww = w.w0[comp]; oo = w.o0[comp]; }
-    else { ww = w.w1[comp]; oo = w.o1[comp]; }
-    if (lw >= 1) return clip1(((pv * ww + (1 << (lw - 1))) >> lw) + oo);
-    return clip1(pv * ww + oo);
-}
-
 // ---------------------------------------------------------------- neighbours
 __device__ __forceinline__ bool avail_mb(const PicDesc &p, int cur, int n)
 {

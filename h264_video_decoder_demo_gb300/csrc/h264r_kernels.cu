@@ -346,10 +346,12 @@ __device__ bool mb_residual(const PicDesc &p, const h264r_mb &m, int field, int 
 // ======================================================================
 // K1: inter macroblocks, I_PCM, undecoded macroblocks
 // ======================================================================
-// One warp per MB, 4 MBs per block.  Lane l predicts rows 2*(l&1), +1 of
-// 4x4 block l>>1 (raster order within the MB) from a 7x9 window of the
-// reference staged in shared memory, and the 2x2 chroma samples of block
-// l&15 for plane l>>4; residuals come from lanes owning whole blocks.
+// One warp per MB, 4 MBs per block.  Lane l predicts the 4x2 luma samples
+// in columns 2*(l&1), +1 of 4x4 block l>>1 (raster order within the MB)
+// from a 9x8 window of the reference held in registers, and the 2x2 chroma
+// samples of the same block in plane l&1, so that the partition, its
+// references and its weights are looked up once per lane; residuals come
+// from lanes owning whole blocks.
 constexpr int kInterWarps = 4;  // 6 blocks (24 warps) per SM: registers capped at 80
 
 struct InterWarpSmem {
@@ -359,43 +361,47 @@ struct InterWarpSmem {
 };
 
 
-// Reference window of one lane: rows yi-2..yi+4, columns xi-2..xi+6 of a
-// luma plane, clamped at the picture edges like luma_sample (8.4.2.2.1,
-// H264InterPrediction.cpp:2344-2363), as 7 rows of 12 bytes (byte c+2 of
-// row r+2 holds sample (xi+c, yi+r)).  Away from the edges each row is three
-// aligned 32-bit loads and two funnel shifts; the loads may read up to three
-// bytes past the window, which stay inside the picture allocation.
-__device__ __forceinline__ void load_luma_window(const RefView &rv, int ymax, int xi, int yi, uint32_t (&win)[21])
+// Reference window of one lane: rows yi-2..yi+6, columns xi-2..xi+5 of a
+// luma plane, clamped at the picture edges like 8.4.2.2.1
+// (H264InterPrediction.cpp:2344-2363), as 9 rows of 8 bytes (byte c of row
+// r holds sample (xi-2+c, yi-2+r); byte 7 is not used).  Away from the edges
+// each row is three aligned 32-bit loads and two funnel shifts; the loads
+// may read up to five bytes past the window, which stay inside the picture
+// slot (the chroma planes and the slot padding follow every luma row).
+__device__ __forceinline__ void load_luma_window(const RefView &rv, int ymax, int xi, int yi, uint32_t (&win)[18])
 {
     const int x0 = xi - 2, y0 = yi - 2;
-    if (x0 >= 0 && xi + 6 <= rv.xmax && y0 >= 0 && yi + 4 <= ymax) {
+    if (x0 >= 0 && xi + 4 <= rv.xmax && y0 >= 0 && yi + 6 <= ymax) {
         const int sh = (x0 & 3) * 8;
         const uint8_t *row = rv.y + (size_t)y0 * rv.ystride + (x0 & ~3);
 #pragma unroll
-        for (int r = 0; r < 7; r++) {
+        for (int r = 0; r < 9; r++) {
             const uint32_t *q = (const uint32_t *)(row + (size_t)r * rv.ystride);
             const uint32_t a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
-            win[3 * r] = __funnelshift_r(a, b, sh);
-            win[3 * r + 1] = __funnelshift_r(b, c, sh);
-            win[3 * r + 2] = c >> sh;
+            win[2 * r] = __funnelshift_r(a, b, sh);
+            win[2 * r + 1] = __funnelshift_r(b, c, sh);
         }
         return;
     }
-    for (int r = 0; r < 7; r++) {
-        const uint8_t *row = rv.y + (size_t)H264R_CLIP3(0, ymax, y0 + r) * rv.ystride;
-        uint32_t w[3] = {0, 0, 0};
 #pragma unroll
-        for (int c = 0; c < 9; c++) w[c >> 2] |= (uint32_t)__ldg(row + H264R_CLIP3(0, rv.xmax, x0 + c)) << (8 * (c & 3));
-        win[3 * r] = w[0];
-        win[3 * r + 1] = w[1];
-        win[3 * r + 2] = w[2];
+    for (int r = 0; r < 9; r++) {
+        const uint8_t *row = rv.y + (size_t)H264R_CLIP3(0, ymax, y0 + r) * rv.ystride;
+        uint32_t w0 = 0, w1 = 0;
+#pragma unroll
+        for (int c = 0; c < 7; c++) {
+            const uint32_t v = __ldg(row + H264R_CLIP3(0, rv.xmax, x0 + c));
+            if (c < 4) w0 |= v << (8 * c);
+            else w1 |= v << (8 * (c - 4));
+        }
+        win[2 * r] = w0;
+        win[2 * r + 1] = w1;
     }
 }
 
 // 8.4.2.2.2 for the 2x2 chroma samples at (xi, yi) .. (xi+1, yi+1)
 // (Chroma_sample_interpolation_process, H264InterPrediction.cpp:2485-2522):
 // the 3x3 neighbourhood is held in three registers.
-__device__ __forceinline__ void chroma_2x2(const uint8_t *pl, int stride, int xmax, int ymax, int xi, int yi, int xf, int yf, int out[4])
+__device__ __forceinline__ uint32_t chroma_2x2(const uint8_t *pl, int stride, int xmax, int ymax, int xi, int yi, int xf, int yf)
 {
     uint32_t rw[3];
     if (xi >= 0 && xi + 2 <= xmax && yi >= 0 && yi + 2 <= ymax) {
@@ -416,14 +422,7 @@ __device__ __forceinline__ void chroma_2x2(const uint8_t *pl, int stride, int xm
             rw[r] = w;
         }
     }
-    const int w00 = (8 - xf) * (8 - yf), w01 = xf * (8 - yf), w10 = (8 - xf) * yf, w11 = xf * yf;
-#define CB(r, c) ((int)((rw[r] >> (8 * (c))) & 255))
-#pragma unroll
-    for (int i = 0; i < 2; i++)
-#pragma unroll
-        for (int j = 0; j < 2; j++)
-            out[i * 2 + j] = (w00 * CB(i, j) + w01 * CB(i, j + 1) + w10 * CB(i + 1, j) + w11 * CB(i + 1, j + 1) + 32) >> 6;
-#undef CB
+    return mc_chroma_2x2(rw[0], rw[1], rw[2], xf, yf);
 }
 
 
@@ -481,69 +480,56 @@ __global__ void __launch_bounds__(32 * kInterWarps, 6) k_inter(const PicDesc *__
         const int yAL0 = field ? (y - (y & 1)) / 2 : y;
         const int ymax = field ? p.H / 2 - 1 : p.H - 1;
         const int ymaxc = field ? p.Hc / 2 - 1 : p.Hc - 1;
-        // ---- luma prediction: 4x4 block lane>>1 (raster), rows 2*(lane&1), +1
-        {
-            const int blk = lane >> 1, bx = blk & 3, by = blk >> 2, r0 = 2 * (lane & 1);
-            int e = part_of_block(shape, bx, by);
-            if (e >= (int)count) e = 0;
-            const h264r_part pp = parts[e];
-            const h264r_weight w = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
-            const bool use0 = pp.ref[0] >= 0, use1 = pp.ref[1] >= 0;
-            uint32_t va0 = 0, va1 = 0, vb0 = 0, vb1 = 0;  // predictions of list 0 / 1, 8 bytes each
+        const int blk = lane >> 1, half = lane & 1, bx = blk & 3, by = blk >> 2;
+        int e = part_of_block(shape, bx, by);
+        if (e >= (int)count) e = 0;
+        const h264r_part pp = parts[e];
+        const bool use0 = pp.ref[0] >= 0, use1 = pp.ref[1] >= 0;
+        // predictions of list 0 / 1: luma rows 0-1 and 2-3 (byte 2i + k),
+        // chroma 2x2 of plane `half` (byte 2i + j)
+        uint32_t ya0 = 0, ya1 = 0, yb0 = 0, yb1 = 0, ca = 0, cb = 0;
 #pragma unroll 1
-            for (int l = 0; l < 2; l++) {
-                if (!(l ? use1 : use0)) continue;
-                const int ref = l ? pp.ref[1] : pp.ref[0];
-                const int mvx = l ? pp.mv[1][0] : pp.mv[0][0], mvy = l ? pp.mv[1][1] : pp.mv[0][1];
-                const RefView rv = ref_view(p, ref);
-                const int xi = x + bx * 4 + (mvx >> 2), yi = yAL0 + by * 4 + r0 + (mvy >> 2);
-                uint32_t win[21];  // the lane's reference window, in registers
-                load_luma_window(rv, ymax, xi, yi, win);
-                uint32_t w0, w1;
-                mc_luma_2x4_w(win, mvx & 3, mvy & 3, w0, w1);
-                if (l) { vb0 = w0; vb1 = w1; } else { va0 = w0; va1 = w1; }
+        for (int l = 0; l < 2; l++) {
+            if (!(l ? use1 : use0)) continue;
+            const int ref = l ? pp.ref[1] : pp.ref[0];
+            const int mvx = l ? pp.mv[1][0] : pp.mv[0][0], mvy = l ? pp.mv[1][1] : pp.mv[0][1];
+            const RefView rv = ref_view(p, ref);
+            uint32_t win[18];
+            load_luma_window(rv, ymax, x + bx * 4 + 2 * half + (mvx >> 2), yAL0 + by * 4 + (mvy >> 2), win);
+            uint32_t o0, o1;
+            mc_luma_4x2(win, mvx & 3, mvy & 3, o0, o1);
+            int cmvy = mvy;
+            if (field) {  // Table 8-10 (H264InterPrediction.cpp:2006-2047)
+                const int refbot = (ref & H264R_REF_BOTTOM) ? 1 : 0;
+                if (!refbot && bottom_mb) cmvy += 2;
+                else if (refbot && !bottom_mb) cmvy -= 2;
             }
-#pragma unroll 1
-            for (int t = 0; t < 8; t++) {
-                const int i = t >> 2, j = t & 3;
-                const int oy = by * 4 + r0 + i, ox = bx * 4 + j;
-                const int a = ((i ? va1 : va0) >> (8 * j)) & 255, b = ((i ? vb1 : vb0) >> (8 * j)) & 255;
-                s.out[oy * 16 + ox] = (uint8_t)clip1(weigh(w, 0, use0, use1, a, b) + s.res[oy * 16 + ox]);
+            const uint32_t c = chroma_2x2(half ? rv.cr : rv.cb, rv.cstride, rv.xmaxc, ymaxc, x / 2 + bx * 2 + (mvx >> 3),
+                                          yAL0 / 2 + by * 2 + (cmvy >> 3), mvx & 7, cmvy & 7);
+            if (l) { yb0 = o0; yb1 = o1; cb = c; } else { ya0 = o0; ya1 = o1; ca = c; }
+        }
+        // ---- weighting (8.4.2.3) and residual, two samples per row
+        const h264r_weight wt = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
+        {
+            const McWeight mw = mc_weight(wt, 0, use0, use1);
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const uint32_t a = (i < 2 ? ya0 : ya1) >> (16 * (i & 1)), b = (i < 2 ? yb0 : yb1) >> (16 * (i & 1));
+                const int o = (by * 4 + i) * 16 + bx * 4 + 2 * half;
+                const int2 r = *(const int2 *)&s.res[o];
+                const int v0 = clip1(mc_weigh(mw, a & 255, b & 255) + r.x), v1 = clip1(mc_weigh(mw, (a >> 8) & 255, (b >> 8) & 255) + r.y);
+                *(uint16_t *)&s.out[o] = (uint16_t)(v0 | (v1 << 8));
             }
         }
-        // ---- chroma prediction: plane lane>>4, 2x2 samples of 4x4 block lane&15 (raster)
         {
-            const int pl = lane >> 4, blk = lane & 15, bx = blk & 3, by = blk >> 2;
-            int e = part_of_block(shape, bx, by);
-            if (e >= (int)count) e = 0;
-            const h264r_part pp = parts[e];
-            const h264r_weight w = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
-            const bool use0 = pp.ref[0] >= 0, use1 = pp.ref[1] >= 0;
-            uint32_t ca = 0, cb = 0;  // 2x2 predictions of list 0 / 1
-#pragma unroll 1
-            for (int l = 0; l < 2; l++) {
-                if (!(l ? use1 : use0)) continue;
-                const int ref = l ? pp.ref[1] : pp.ref[0];
-                const RefView rv = ref_view(p, ref);
-                int mvx = l ? pp.mv[1][0] : pp.mv[0][0], mvy = l ? pp.mv[1][1] : pp.mv[0][1];
-                if (field) {  // Table 8-10 (H264InterPrediction.cpp:2006-2047)
-                    int refbot = (ref & H264R_REF_BOTTOM) ? 1 : 0;
-                    if (!refbot && bottom_mb) mvy += 2;
-                    else if (refbot && !bottom_mb) mvy -= 2;
-                }
-                const uint8_t *plane = pl ? rv.cr : rv.cb;
-                const int xi = x / 2 + bx * 2 + (mvx >> 3), yi = yAL0 / 2 + by * 2 + (mvy >> 3);
-                int o[4];
-                chroma_2x2(plane, rv.cstride, rv.xmaxc, ymaxc, xi, yi, mvx & 7, mvy & 7, o);
-                const uint32_t wv = pack4(o[0], o[1], o[2], o[3]);
-                if (l) cb = wv; else ca = wv;
-            }
-#pragma unroll 1
-            for (int t = 0; t < 4; t++) {
-                const int i = t >> 1, j = t & 1;
-                const int oy = by * 2 + i, ox = bx * 2 + j, o = 256 + pl * 64 + oy * 8 + ox;
-                const int a = (ca >> (8 * t)) & 255, b = (cb >> (8 * t)) & 255;
-                s.out[o] = (uint8_t)clip1(weigh(w, 1 + pl, use0, use1, a, b) + s.res[o]);
+            const McWeight mw = mc_weight(wt, 1 + half, use0, use1);
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const uint32_t a = ca >> (16 * i), b = cb >> (16 * i);
+                const int o = 256 + half * 64 + (by * 2 + i) * 8 + bx * 2;
+                const int2 r = *(const int2 *)&s.res[o];
+                const int v0 = clip1(mc_weigh(mw, a & 255, b & 255) + r.x), v1 = clip1(mc_weigh(mw, (a >> 8) & 255, (b >> 8) & 255) + r.y);
+                *(uint16_t *)&s.out[o] = (uint16_t)(v0 | (v1 << 8));
             }
         }
     }

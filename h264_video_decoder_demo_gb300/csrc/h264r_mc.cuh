@@ -1,21 +1,32 @@
-// h264r_mc.cuh — 8.4.2.2.1 luma sample interpolation for a 2x4 group of
-// samples from a reference window held in registers
-// (Luma_sample_interpolation_process, H264InterPrediction.cpp:2344-2480).
+// h264r_mc.cuh — motion-compensated prediction of one lane's samples:
+// 8.4.2.2.1 luma interpolation of a 4-row x 2-column group
+// (Luma_sample_interpolation_process, H264InterPrediction.cpp:2344-2480),
+// 8.4.2.2.2 chroma interpolation of a 2x2 group (2485-2522) and the
+// 8.4.2.3 weighting of a sample pair (2526-2829).  Host and device code, so
+// that the same functions are checked on the CPU against a scalar
+// restatement of the standard's formulas.
 //
-// The window of a lane is 7 rows of 12 bytes, three 32-bit words per row:
-// byte c of row r is the reference sample (xi - 2 + c, yi - 2 + r), so the
-// 2x4 outputs (xi..xi+3, yi..yi+1) sit at bytes 2..5 of rows 2 and 3.  A
-// horizontal 6-tap sum over bytes j..j+5 of a row is two funnel shifts of
-// the row's words (bytes j..j+3 and j+4..j+7) and two four-way byte dot
-// products with the taps (1, -5, 20, 20) and (-5, 1, 0, 0); the same shifted
-// word gives the full-sample values of columns j and j+1 for the vertical
-// taps.  Column loops stay rolled (only shift amounts depend on the column),
-// and the outputs are packed by shifts, so no array is indexed at run time.
-// The arithmetic is the reference's, in integers, so the result is
-// bit-exact whichever order the taps are summed in.
+// Luma window of a lane: 9 rows of 8 bytes, two 32-bit words per row; byte
+// c of row r is the reference sample (xi - 2 + c, yi - 2 + r), so the
+// outputs (xi..xi+1, yi..yi+3) sit at bytes 2..3 of rows 2..5.  Four rows
+// per lane instead of two need 9 window rows for 4 output rows, and the
+// fractional position only selects which of four components are formed:
+//   G  full samples (byte 2, or byte 3 for xFrac 3; row r, or r+1 for yFrac 3)
+//   B  horizontal half samples b / s      (row r or r+1)
+//   V  vertical half samples h / m        (column x or x+1)
+//   J  the centre half sample j
+// and the output is the rounded byte average of two of them (a component
+// averaged with itself when Table 8-12 names one).  Horizontal 6-tap sums
+// are two dp4a of the row's words with the taps shifted to the output
+// column; vertical sums are dp4a over column words gathered by byte
+// permutes (four rows per word) with the taps shifted to the output row.
+// All arithmetic is the reference's, in integers, so the result is bit-exact
+// whichever order the taps are summed in.
 #pragma once
 
 #include <cstdint>
+
+#include "../../include/h264r.h"
 
 namespace h264r {
 
@@ -42,115 +53,194 @@ __host__ __device__ __forceinline__ int mc_dp4a(uint32_t a, uint32_t b, int c)
 #endif
 }
 
-__host__ __device__ __forceinline__ int mc_clip1(int v) { return v < 0 ? 0 : (v > 255 ? 255 : v); }
-
-constexpr uint32_t kTapLo = 0x1414FB01u;  // taps 1, -5, 20, 20 as signed bytes
-constexpr uint32_t kTapHi = 0x000001FBu;  // taps -5, 1, 0, 0
-
-// 6-tap sum over bytes j..j+5 of a row given its words shifted by 8*j
-__host__ __device__ __forceinline__ int mc_htap(uint32_t a, uint32_t b) { return mc_dp4a(a, kTapLo, mc_dp4a(b, kTapHi, 0)); }
-
-__host__ __device__ __forceinline__ int mc_vtap(int a, int b, int c, int d, int e, int f)
+// byte n of the result = byte ((s >> 4n) & 7) of the 8 bytes {b, a}
+__host__ __device__ __forceinline__ uint32_t mc_prmt(uint32_t a, uint32_t b, uint32_t s)
 {
-    return a - 5 * b + 20 * c + 20 * d - 5 * e + f;
+#ifdef __CUDA_ARCH__
+    return __byte_perm(a, b, s);
+#else
+    const uint64_t v = ((uint64_t)b << 32) | a;
+    uint32_t r = 0;
+    for (int n = 0; n < 4; n++) r |= (uint32_t)((v >> (8 * ((s >> (4 * n)) & 7))) & 255u) << (8 * n);
+    return r;
+#endif
 }
 
-// w: the window (21 words), xf / yf: quarter-sample fractions.  Returns the
-// predicted samples of rows yi and yi+1 as two words (byte j = column xi+j).
-__host__ __device__ __forceinline__ void mc_luma_2x4_w(const uint32_t (&w)[21], int xf, int yf, uint32_t &o0, uint32_t &o1)
+__host__ __device__ __forceinline__ int mc_clip1(int v) { return v < 0 ? 0 : (v > 255 ? 255 : v); }
+
+// per byte (a + b + 1) >> 1
+__host__ __device__ __forceinline__ uint32_t mc_avg4(uint32_t a, uint32_t b) { return (a | b) - (((a ^ b) >> 1) & 0x7F7F7F7Fu); }
+
+__host__ __device__ __forceinline__ uint32_t mc_pack4(int a, int b, int c, int d)
 {
-    o0 = o1 = 0;
-    if ((xf | yf) == 0) {  // G
-        o0 = mc_fshr(w[6], w[7], 16);
-        o1 = mc_fshr(w[9], w[10], 16);
-        return;
+    return (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)c << 16) | ((uint32_t)d << 24);
+}
+
+// 6-tap (1, -5, 20, 20, -5, 1) as signed bytes, shifted to start at byte
+// 0 / 1 of the first word (horizontal: output column 0 / 1) and to start at
+// byte 0..3 of a column word (vertical: output row 0..3)
+constexpr uint32_t kTap0Lo = 0x1414FB01u, kTap0Hi = 0x000001FBu;  // (1,-5,20,20) (-5,1,0,0)
+constexpr uint32_t kTap1Lo = 0x14FB0100u, kTap1Hi = 0x0001FB14u;  // (0,1,-5,20) (20,-5,1,0)
+constexpr uint32_t kTap2Lo = 0xFB010000u, kTap2Hi = 0x01FB1414u;  // (0,0,1,-5) (20,20,-5,1)
+constexpr uint32_t kTap3Lo = 0x01000000u, kTap3Hi = 0xFB1414FBu;  // (0,0,0,1) (-5,20,20,-5), then 1
+
+// horizontal 6-tap sum of output column k (0, 1) of window row (lo, hi), plus c
+__host__ __device__ __forceinline__ int mc_hsum(uint32_t lo, uint32_t hi, int k, int c)
+{
+    return k ? mc_dp4a(lo, kTap1Lo, mc_dp4a(hi, kTap1Hi, c)) : mc_dp4a(lo, kTap0Lo, mc_dp4a(hi, kTap0Hi, c));
+}
+
+// V: the vertical half samples of the 4x2 outputs at window byte 2 + dx of
+// every row, packed as two words (rows 0-1, rows 2-3; byte 2i + k).
+__host__ __device__ __forceinline__ void mc_vhalf(const uint32_t (&w)[18], int dx, uint32_t &v0, uint32_t &v1)
+{
+    const uint32_t sel = dx ? 0x43u : 0x32u;  // bytes (2, 3) or (3, 4) of the row's 8 bytes
+    uint32_t e[9];
+#pragma unroll
+    for (int r = 0; r < 9; r++) e[r] = mc_prmt(w[2 * r], w[2 * r + 1], sel);
+    // column words: byte j = row 4q + j of output column k
+    const uint32_t t01 = mc_prmt(e[0], e[1], 0x5140u), t23 = mc_prmt(e[2], e[3], 0x5140u);
+    const uint32_t t45 = mc_prmt(e[4], e[5], 0x5140u), t67 = mc_prmt(e[6], e[7], 0x5140u);
+    int h[2][4];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const uint32_t c0 = mc_prmt(t01, t23, k ? 0x7632u : 0x5410u), c1 = mc_prmt(t45, t67, k ? 0x7632u : 0x5410u);
+        h[k][0] = mc_dp4a(c0, kTap0Lo, mc_dp4a(c1, kTap0Hi, 16));
+        h[k][1] = mc_dp4a(c0, kTap1Lo, mc_dp4a(c1, kTap1Hi, 16));
+        h[k][2] = mc_dp4a(c0, kTap2Lo, mc_dp4a(c1, kTap2Hi, 16));
+        h[k][3] = mc_dp4a(c0, kTap3Lo, mc_dp4a(c1, kTap3Hi, mc_dp4a(e[8], k ? 0x100u : 0x1u, 16)));
     }
-    if (yf == 0) {  // a, b, c: rows 0 and 1
-#pragma unroll 1
-        for (int j = 0; j < 4; j++) {
-            const int sh = 8 * j;
+#define MC_H(i, k) mc_clip1(h[k][i] >> 5)
+    v0 = mc_pack4(MC_H(0, 0), MC_H(0, 1), MC_H(1, 0), MC_H(1, 1));
+    v1 = mc_pack4(MC_H(2, 0), MC_H(2, 1), MC_H(3, 0), MC_H(3, 1));
+#undef MC_H
+}
+
+// B: the horizontal half samples of window rows 2 + dy .. 5 + dy
+__host__ __device__ __forceinline__ void mc_bhalf(const uint32_t (&w)[18], int dy, uint32_t &b0, uint32_t &b1)
+{
+    int b[4][2];
 #pragma unroll
-            for (int i = 0; i < 2; i++) {
-                const int R = 3 * (i + 2);
-                const uint32_t A = mc_fshr(w[R], w[R + 1], sh), B = mc_fshr(w[R + 1], w[R + 2], sh);
-                const int b = mc_clip1((mc_htap(A, B) + 16) >> 5);
-                const int g = (int)((A >> (xf == 3 ? 24 : 16)) & 255u);
-                const int v = xf == 2 ? b : (g + b + 1) >> 1;
-                (i ? o1 : o0) |= (uint32_t)v << sh;
-            }
-        }
-        return;
+    for (int i = 0; i < 4; i++) {
+        const uint32_t lo = dy ? w[2 * (i + 3)] : w[2 * (i + 2)], hi = dy ? w[2 * (i + 3) + 1] : w[2 * (i + 2) + 1];
+        b[i][0] = mc_clip1(mc_hsum(lo, hi, 0, 16) >> 5);
+        b[i][1] = mc_clip1(mc_hsum(lo, hi, 1, 16) >> 5);
     }
-    if (xf == 0) {  // d, h, n: column j over rows -2..4
-#pragma unroll 1
-        for (int j = 0; j < 4; j++) {
-            const int sh = 8 * j;
-            int G[7];
+    b0 = mc_pack4(b[0][0], b[0][1], b[1][0], b[1][1]);
+    b1 = mc_pack4(b[2][0], b[2][1], b[3][0], b[3][1]);
+}
+
+// J: the centre half samples (vertical 6-tap of the unrounded horizontal sums)
+__host__ __device__ __forceinline__ void mc_jhalf(const uint32_t (&w)[18], uint32_t &j0, uint32_t &j1)
+{
+    int jv[4][2];
 #pragma unroll
-            for (int r = 0; r < 7; r++) G[r] = (int)((mc_fshr(w[3 * r], w[3 * r + 1], sh) >> 16) & 255u);
+    for (int k = 0; k < 2; k++) {
+        int H[9];
 #pragma unroll
-            for (int i = 0; i < 2; i++) {
-                const int h = mc_clip1((mc_vtap(G[i], G[i + 1], G[i + 2], G[i + 3], G[i + 4], G[i + 5]) + 16) >> 5);
-                const int v = yf == 2 ? h : ((yf == 1 ? G[i + 2] : G[i + 3]) + h + 1) >> 1;
-                (i ? o1 : o0) |= (uint32_t)v << sh;
-            }
-        }
-        return;
+        for (int r = 0; r < 9; r++) H[r] = mc_hsum(w[2 * r], w[2 * r + 1], k, 0);
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+            jv[i][k] = mc_clip1((H[i] + H[i + 5] - 5 * (H[i + 1] + H[i + 4]) + 20 * (H[i + 2] + H[i + 3]) + 512) >> 10);
     }
-    if (xf == 2 || yf == 2) {  // j, f, q, i, k
-#pragma unroll 1
-        for (int j = 0; j < 4; j++) {
-            const int sh = 8 * j;
-            int hb[7], gc[7];  // horizontal sums (b1) and full samples of column j (+1 for k)
+    j0 = mc_pack4(jv[0][0], jv[0][1], jv[1][0], jv[1][1]);
+    j1 = mc_pack4(jv[2][0], jv[2][1], jv[3][0], jv[3][1]);
+}
+
+// G: full samples at window byte 2 + dx of rows 2 + dy .. 5 + dy
+__host__ __device__ __forceinline__ void mc_full(const uint32_t (&w)[18], int dx, int dy, uint32_t &g0, uint32_t &g1)
+{
+    const uint32_t sel = dx ? 0x43u : 0x32u;
+    uint32_t e[4];
 #pragma unroll
-            for (int r = 0; r < 7; r++) {
-                const uint32_t A = mc_fshr(w[3 * r], w[3 * r + 1], sh), B = mc_fshr(w[3 * r + 1], w[3 * r + 2], sh);
-                hb[r] = mc_htap(A, B);
-                gc[r] = (int)((A >> (xf == 3 ? 24 : 16)) & 255u);
-            }
-#pragma unroll
-            for (int i = 0; i < 2; i++) {
-                const int jv = mc_clip1((mc_vtap(hb[i], hb[i + 1], hb[i + 2], hb[i + 3], hb[i + 4], hb[i + 5]) + 512) >> 10);
-                int v;
-                if (xf == 2 && yf == 2) {
-                    v = jv;
-                } else if (xf == 2) {  // f (row i) / q (row i+1)
-                    const int b = mc_clip1(((yf == 3 ? hb[i + 3] : hb[i + 2]) + 16) >> 5);
-                    v = (b + jv + 1) >> 1;
-                } else {  // i (column j) / k (column j+1)
-                    const int h = mc_clip1((mc_vtap(gc[i], gc[i + 1], gc[i + 2], gc[i + 3], gc[i + 4], gc[i + 5]) + 16) >> 5);
-                    v = (h + jv + 1) >> 1;
-                }
-                (i ? o1 : o0) |= (uint32_t)v << sh;
-            }
-        }
-        return;
+    for (int i = 0; i < 4; i++) {
+        const uint32_t lo = dy ? w[2 * (i + 3)] : w[2 * (i + 2)], hi = dy ? w[2 * (i + 3) + 1] : w[2 * (i + 2) + 1];
+        e[i] = mc_prmt(lo, hi, sel);
     }
-    // e, g, p, r: b at row i (+1) and h at column j (+1)
-#pragma unroll 1
-    for (int j = 0; j < 4; j++) {
-        const int sh = 8 * j;
-        int gc[7];
-        uint32_t A2 = 0, A3 = 0, A4 = 0;
-#pragma unroll
-        for (int r = 0; r < 7; r++) {
-            const uint32_t A = mc_fshr(w[3 * r], w[3 * r + 1], sh);
-            gc[r] = (int)((A >> (xf == 3 ? 24 : 16)) & 255u);
-            if (r == 2) A2 = A;
-            if (r == 3) A3 = A;
-            if (r == 4) A4 = A;
+    g0 = mc_prmt(e[0], e[1], 0x5410u);
+    g1 = mc_prmt(e[2], e[3], 0x5410u);
+}
+
+// The 4x2 prediction for quarter-sample fractions (xf, yf) (Table 8-12):
+// o0 = rows 0-1, o1 = rows 2-3, byte 2i + k = (column k, row i).
+//   (0,0) G      (1|3,0) G B    (2,0) B      (0,1|3) G V    (0,2) V
+//   (2,2) J      (2,1|3) B J    (1|3,2) V J  (1|3,1|3) B V
+__host__ __device__ __forceinline__ void mc_luma_4x2(const uint32_t (&w)[18], int xf, int yf, uint32_t &o0, uint32_t &o1)
+{
+    const int dx = xf == 3, dy = yf == 3;
+    const bool gc = (xf == 0 || yf == 0) && xf != 2 && yf != 2;
+    const bool bc = xf != 0 && yf != 2;
+    const bool vc = yf != 0 && xf != 2;
+    const bool jc = xf != 0 && yf != 0 && (xf == 2 || yf == 2);
+    uint32_t g0 = 0, g1 = 0, b0 = 0, b1 = 0, v0 = 0, v1 = 0, j0 = 0, j1 = 0;
+    if (gc) mc_full(w, dx, dy, g0, g1);
+    if (bc) mc_bhalf(w, dy, b0, b1);
+    if (vc) mc_vhalf(w, dx, v0, v1);
+    if (jc) mc_jhalf(w, j0, j1);
+    const uint32_t p0 = gc ? g0 : (bc ? b0 : (vc ? v0 : j0)), p1 = gc ? g1 : (bc ? b1 : (vc ? v1 : j1));
+    const uint32_t q0 = jc ? j0 : (vc ? v0 : (bc ? b0 : g0)), q1 = jc ? j1 : (vc ? v1 : (bc ? b1 : g1));
+    o0 = mc_avg4(p0, q0);
+    o1 = mc_avg4(p1, q1);
+}
+
+// Chroma 2x2 prediction from three window words (row r: bytes 0..2 = the
+// samples (xi..xi+2, yi+r)); eighth-sample fractions xf, yf.  Result byte
+// 2i + j = (xi + j, yi + i).
+__host__ __device__ __forceinline__ uint32_t mc_chroma_2x2(uint32_t r0, uint32_t r1, uint32_t r2, int xf, int yf)
+{
+    const uint32_t t = (uint32_t)((8 - xf) * (8 - yf)) | ((uint32_t)(xf * (8 - yf)) << 8);  // taps of row i
+    const uint32_t u = (uint32_t)((8 - xf) * yf) | ((uint32_t)(xf * yf) << 8);              // taps of row i + 1
+    const int a = mc_dp4a(r0, t, mc_dp4a(r1, u, 32)) >> 6, b = mc_dp4a(r0, t << 8, mc_dp4a(r1, u << 8, 32)) >> 6;
+    const int c = mc_dp4a(r1, t, mc_dp4a(r2, u, 32)) >> 6, d = mc_dp4a(r1, t << 8, mc_dp4a(r2, u << 8, 32)) >> 6;
+    return mc_pack4(a, b, c, d);
+}
+
+// 8.4.2.3 as one formula per partition and component:
+// Clip1(((p0 * w0 + p1 * w1 + round) >> shift) + offset), covering default
+// prediction (H264InterPrediction.cpp:2526-2560), explicit / implicit
+// weighting (2560-2829) and the unused-list cases.  Quirk kept: explicit
+// weights with only list 1 in use apply w0 / o0 to luma.
+struct McWeight {
+    int w0, w1, round, shift, offset;
+};
+
+__host__ __device__ __forceinline__ McWeight mc_weight(const h264r_weight &w, int comp, bool use0, bool use1)
+{
+    McWeight m = {0, 0, 0, 0, 0};
+    if (!use0 && !use1) return m;
+    if (!w.weighted) {
+        if (use0 && use1) {
+            m.w0 = m.w1 = 1;
+            m.round = 1;
+            m.shift = 1;
+        } else {
+            (use0 ? m.w0 : m.w1) = 1;
         }
-#pragma unroll
-        for (int i = 0; i < 2; i++) {
-            // b at window row i+2, or i+3 when yf == 3 (selects, not indexing)
-            const bool down = yf == 3;
-            const uint32_t A = i == 0 ? (down ? A3 : A2) : (down ? A4 : A3);
-            const uint32_t B = mc_fshr(down ? w[3 * (i + 3) + 1] : w[3 * (i + 2) + 1], down ? w[3 * (i + 3) + 2] : w[3 * (i + 2) + 2], sh);
-            const int b = mc_clip1((mc_htap(A, B) + 16) >> 5);
-            const int h = mc_clip1((mc_vtap(gc[i], gc[i + 1], gc[i + 2], gc[i + 3], gc[i + 4], gc[i + 5]) + 16) >> 5);
-            (i ? o1 : o0) |= (uint32_t)((b + h + 1) >> 1) << sh;
-        }
+        return m;
     }
+    const int lw = w.log_wd[comp];
+    if (use0 && use1) {
+        m.w0 = w.w0[comp];
+        m.w1 = w.w1[comp];
+        m.round = 1 << lw;
+        m.shift = lw + 1;
+        m.offset = (w.o0[comp] + w.o1[comp] + 1) >> 1;
+        return m;
+    }
+    const bool first = use0 || comp == 0;
+    const int ww = first ? w.w0[comp] : w.w1[comp];
+    (use0 ? m.w0 : m.w1) = ww;
+    m.offset = first ? w.o0[comp] : w.o1[comp];
+    if (lw >= 1) {
+        m.round = 1 << (lw - 1);
+        m.shift = lw;
+    }
+    return m;
+}
+
+__host__ __device__ __forceinline__ int mc_weigh(const McWeight &m, int p0, int p1)
+{
+    return mc_clip1(((p0 * m.w0 + p1 * m.w1 + m.round) >> m.shift) + m.offset);
 }
 
 }  // namespace h264r
