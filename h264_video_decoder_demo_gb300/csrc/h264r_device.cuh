@@ -19,23 +19,56 @@ __device__ __forceinline__ int clip1(int v) { return min(max(v, 0), 255); }
 
 // ---------------------------------------------------------------- tables
 // scan index -> raster index (row*4+col / row*8+col), Table 8-12/8-13
-// (H264PictureBase.cpp:4542, 4597)
-__device__ const uint8_t kZigzag4x4[16] = {0, 1, 4, 8, 5, 2, 3, 6, 9, 12, 13, 10, 7, 11, 14, 15};
-__device__ const uint8_t kField4x4[16] = {0, 4, 1, 8, 12, 5, 9, 13, 2, 6, 10, 14, 3, 7, 11, 15};
-__device__ const uint8_t kZigzag8x8[64] = {
+// (H264PictureBase.cpp:4542, 4597).  Compile-time tables; the kernels use
+// them packed into words (no table loads in the coefficient loops).
+constexpr uint8_t kZigzag4x4[16] = {0, 1, 4, 8, 5, 2, 3, 6, 9, 12, 13, 10, 7, 11, 14, 15};
+constexpr uint8_t kField4x4[16] = {0, 4, 1, 8, 12, 5, 9, 13, 2, 6, 10, 14, 3, 7, 11, 15};
+constexpr uint8_t kZigzag8x8[64] = {
     0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5,
     12, 19, 26, 33, 40, 48, 41, 34, 27, 20, 13, 6, 7, 14, 21, 28,
     35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51,
     58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63};
-__device__ const uint8_t kField8x8[64] = {
+constexpr uint8_t kField8x8[64] = {
     0, 8, 16, 1, 9, 24, 32, 17, 2, 25, 40, 48, 56, 33, 10, 3,
     18, 41, 49, 57, 26, 11, 4, 19, 34, 42, 50, 58, 27, 12, 5, 20,
     35, 43, 51, 59, 28, 13, 6, 21, 36, 44, 52, 60, 29, 14, 22, 37,
     45, 53, 61, 30, 7, 15, 38, 46, 54, 62, 23, 31, 39, 47, 55, 63};
-// normAdjust (scaling_functions, H264PictureBase.cpp:4900-4951)
-__device__ const uint8_t kV4[6][3] = {{10, 16, 13}, {11, 18, 14}, {13, 20, 16}, {14, 23, 18}, {16, 25, 20}, {18, 29, 23}};
-__device__ const uint8_t kV8[6][6] = {{20, 18, 32, 19, 25, 24}, {22, 19, 35, 21, 28, 26}, {26, 23, 42, 24, 33, 31},
-                                      {28, 25, 45, 26, 35, 33}, {32, 28, 51, 30, 40, 38}, {36, 32, 58, 34, 46, 43}};
+// 4x4: raster of scan index k in bits 4k..4k+3
+constexpr uint64_t pack_scan4(const uint8_t (&t)[16])
+{
+    uint64_t v = 0;
+    for (int k = 0; k < 16; k++) v |= (uint64_t)t[k] << (4 * k);
+    return v;
+}
+// 8x8: raster of scan index 8r + i in bits 6i..6i+5 of word r
+constexpr uint64_t pack_scan8(const uint8_t (&t)[64], int r)
+{
+    uint64_t v = 0;
+    for (int i = 0; i < 8; i++) v |= (uint64_t)t[8 * r + i] << (6 * i);
+    return v;
+}
+constexpr uint64_t kZigzag4P = pack_scan4(kZigzag4x4), kField4P = pack_scan4(kField4x4);
+__constant__ uint64_t kScan8P[2][8] = {
+    {pack_scan8(kZigzag8x8, 0), pack_scan8(kZigzag8x8, 1), pack_scan8(kZigzag8x8, 2), pack_scan8(kZigzag8x8, 3),
+     pack_scan8(kZigzag8x8, 4), pack_scan8(kZigzag8x8, 5), pack_scan8(kZigzag8x8, 6), pack_scan8(kZigzag8x8, 7)},
+    {pack_scan8(kField8x8, 0), pack_scan8(kField8x8, 1), pack_scan8(kField8x8, 2), pack_scan8(kField8x8, 3),
+     pack_scan8(kField8x8, 4), pack_scan8(kField8x8, 5), pack_scan8(kField8x8, 6), pack_scan8(kField8x8, 7)}};
+// normAdjust (scaling_functions, H264PictureBase.cpp:4900-4951) per qP % 6
+// and position class; the kernels read one packed word per qP % 6 (byte c =
+// the value of class c)
+constexpr uint8_t kV4[6][3] = {{10, 16, 13}, {11, 18, 14}, {13, 20, 16}, {14, 23, 18}, {16, 25, 20}, {18, 29, 23}};
+constexpr uint8_t kV8[6][6] = {{20, 18, 32, 19, 25, 24}, {22, 19, 35, 21, 28, 26}, {26, 23, 42, 24, 33, 31},
+                               {28, 25, 45, 26, 35, 33}, {32, 28, 51, 30, 40, 38}, {36, 32, 58, 34, 46, 43}};
+template <int N> constexpr uint64_t pack_bytes(const uint8_t (&t)[N])
+{
+    uint64_t v = 0;
+    for (int i = 0; i < N; i++) v |= (uint64_t)t[i] << (8 * i);
+    return v;
+}
+__constant__ uint32_t kV4P[6] = {(uint32_t)pack_bytes(kV4[0]), (uint32_t)pack_bytes(kV4[1]), (uint32_t)pack_bytes(kV4[2]),
+                                 (uint32_t)pack_bytes(kV4[3]), (uint32_t)pack_bytes(kV4[4]), (uint32_t)pack_bytes(kV4[5])};
+__constant__ uint64_t kV8P[6] = {pack_bytes(kV8[0]), pack_bytes(kV8[1]), pack_bytes(kV8[2]),
+                                 pack_bytes(kV8[3]), pack_bytes(kV8[4]), pack_bytes(kV8[5])};
 // Table 8-15 (H264PictureBase.cpp:4773-4778)
 __device__ const uint8_t kQpc[52] = {
     0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25,
@@ -54,9 +87,6 @@ __device__ const uint8_t kTc0[3][52] = {
      1, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 4, 4, 5, 5, 6, 7, 8, 8, 10, 11, 12, 13, 15, 17},
     {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 1,
      1, 2, 2, 2, 2, 3, 3, 3, 4, 4, 4, 5, 6, 6, 7, 8, 9, 10, 11, 13, 14, 16, 18, 20, 23, 25}};
-// luma4x4BlkIdx -> 4x4-block column / row (6.4.3)
-__device__ const uint8_t kBlkX[16] = {0, 1, 0, 1, 2, 3, 2, 3, 0, 1, 0, 1, 2, 3, 2, 3};
-__device__ const uint8_t kBlkY[16] = {0, 0, 1, 1, 0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 3, 3};
 
 // ---------------------------------------------------------------- picture
 // Device view of one picture of a batch (built by the host for every launch).
@@ -177,76 +207,15 @@ __device__ __forceinline__ int chroma_qp(int qpy, int offset) { return kQpc[H264
 __device__ __forceinline__ bool is_intra_type(int t) { return t == H264R_MB_I4x4 || t == H264R_MB_I8x8 || t == H264R_MB_I16x16; }
 
 // ---------------------------------------------------------------- scaling
-__device__ __forceinline__ int scan_pos_of(const uint8_t *scan, int n, int raster)
+// LevelScale4x4(m, 0, 0) of scaling list `list` (8.5.9): the DC position is
+// scan index 0 in both scans
+__device__ __forceinline__ int level_scale_dc(const PicDesc &p, int list, int m)
 {
-    for (int k = 0; k < n; k++)
-        if (scan[k] == raster) return k;
-    return 0;
-}
-
-// LevelScale4x4(m, i, j) of scaling list `list` (8.5.9)
-__device__ __forceinline__ int level_scale4(const PicDesc &p, int list, int field, int m, int i, int j)
-{
-    int ws = 16;
-    if (!p.flat_scaling) ws = p.scaling[list * 16 + scan_pos_of(field ? kField4x4 : kZigzag4x4, 16, i * 4 + j)];
-    int v = ((i & 1) == 0 && (j & 1) == 0) ? kV4[m][0] : (((i & 1) && (j & 1)) ? kV4[m][1] : kV4[m][2]);
-    return ws * v;
-}
-
-__device__ __forceinline__ int level_scale8(const PicDesc &p, int list, int field, int m, int i, int j)
-{
-    int ws = 16;
-    if (!p.flat_scaling) ws = p.scaling[96 + list * 64 + scan_pos_of(field ? kField8x8 : kZigzag8x8, 64, i * 8 + j)];
-    int v;
-    if (i % 4 == 0 && j % 4 == 0) v = kV8[m][0];
-    else if (i % 2 == 1 && j % 2 == 1) v = kV8[m][1];
-    else if (i % 4 == 2 && j % 4 == 2) v = kV8[m][2];
-    else if ((i % 4 == 0 && j % 2 == 1) || (i % 2 == 1 && j % 4 == 0)) v = kV8[m][3];
-    else if ((i % 4 == 0 && j % 4 == 2) || (i % 4 == 2 && j % 4 == 0)) v = kV8[m][4];
-    else v = kV8[m][5];
-    return ws * v;
+    const int ws = p.flat_scaling ? 16 : p.scaling[list * 16];
+    return ws * (int)(kV4P[m] & 255u);
 }
 
 // ---------------------------------------------------------------- transforms
-// 8.5.12 on a 4x4 array already in raster order (Scaling_and_transformation_
-// process_for_residual_4x4_blocks, H264PictureBase.cpp:4106-4266)
-__device__ __forceinline__ void idct4x4(const PicDesc &p, int32_t c[16], int field, int qp, int ls_list, bool dc_pass,
-                                        int32_t r[16])
-{
-    int32_t d[16];
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            int32_t v = c[i * 4 + j];
-            if (i == 0 && j == 0 && dc_pass) {
-                d[0] = v;
-            } else if (v == 0) {
-                d[i * 4 + j] = 0;
-            } else {
-                int ls = level_scale4(p, ls_list, field, qp % 6, i, j);
-                if (qp >= 24) d[i * 4 + j] = (v * ls) << (qp / 6 - 4);
-                else d[i * 4 + j] = (v * ls + (1 << (3 - qp / 6))) >> (4 - qp / 6);
-            }
-        }
-    int32_t f[16];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        int e0 = d[i * 4 + 0] + d[i * 4 + 2], e1 = d[i * 4 + 0] - d[i * 4 + 2];
-        int e2 = (d[i * 4 + 1] >> 1) - d[i * 4 + 3], e3 = d[i * 4 + 1] + (d[i * 4 + 3] >> 1);
-        f[i * 4 + 0] = e0 + e3; f[i * 4 + 1] = e1 + e2; f[i * 4 + 2] = e1 - e2; f[i * 4 + 3] = e0 - e3;
-    }
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-        int g0 = f[0 * 4 + j] + f[2 * 4 + j], g1 = f[0 * 4 + j] - f[2 * 4 + j];
-        int g2 = (f[1 * 4 + j] >> 1) - f[3 * 4 + j], g3 = f[1 * 4 + j] + (f[3 * 4 + j] >> 1);
-        r[0 * 4 + j] = (g0 + g3 + 32) >> 6;
-        r[1 * 4 + j] = (g1 + g2 + 32) >> 6;
-        r[2 * 4 + j] = (g1 - g2 + 32) >> 6;
-        r[3 * 4 + j] = (g0 - g3 + 32) >> 6;
-    }
-}
-
 // one 8-point pass of 8.5.13.2
 __device__ __forceinline__ void idct8_1d(int x0, int x1, int x2, int x3, int x4, int x5, int x6, int x7, int o[8])
 {
@@ -264,29 +233,6 @@ __device__ __forceinline__ void idct8_1d(int x0, int x1, int x2, int x3, int x4,
     o[4] = f6 - f1; o[5] = f4 - f3; o[6] = f2 - f5; o[7] = f0 - f7;
 }
 
-// 8.5.13 (H264PictureBase.cpp:4270-4403); c and r in raster order; in place allowed
-__device__ __forceinline__ void idct8x8(const PicDesc &p, int32_t *c, int field, int qp, int ls_list, int32_t *r)
-{
-    int32_t d[64];
-    for (int i = 0; i < 8; i++)
-        for (int j = 0; j < 8; j++) {
-            int32_t v = c[i * 8 + j];
-            if (v == 0) { d[i * 8 + j] = 0; continue; }
-            int ls = level_scale8(p, ls_list, field, qp % 6, i, j);
-            if (qp >= 36) d[i * 8 + j] = (v * ls) << (qp / 6 - 6);
-            else d[i * 8 + j] = (v * ls + (1 << (5 - qp / 6))) >> (6 - qp / 6);
-        }
-    int o[8];
-    for (int i = 0; i < 8; i++) {
-        idct8_1d(d[i * 8 + 0], d[i * 8 + 1], d[i * 8 + 2], d[i * 8 + 3], d[i * 8 + 4], d[i * 8 + 5], d[i * 8 + 6], d[i * 8 + 7], o);
-        for (int j = 0; j < 8; j++) d[i * 8 + j] = o[j];
-    }
-    for (int j = 0; j < 8; j++) {
-        idct8_1d(d[0 * 8 + j], d[1 * 8 + j], d[2 * 8 + j], d[3 * 8 + j], d[4 * 8 + j], d[5 * 8 + j], d[6 * 8 + j], d[7 * 8 + j], o);
-        for (int i = 0; i < 8; i++) r[i * 8 + j] = (o[i] + 32) >> 6;
-    }
-}
-
 // 8.5.10 Intra16x16 DC (H264PictureBase.cpp:4993-5088): c raster -> dcY raster
 __device__ __forceinline__ void luma_dc(const PicDesc &p, const int32_t c[16], int field, int qp, int32_t dcY[16])
 {
@@ -297,7 +243,7 @@ __device__ __forceinline__ void luma_dc(const PicDesc &p, const int32_t c[16], i
         g[2 * 4 + j] = c[0 * 4 + j] - c[1 * 4 + j] - c[2 * 4 + j] + c[3 * 4 + j];
         g[3 * 4 + j] = c[0 * 4 + j] - c[1 * 4 + j] + c[2 * 4 + j] - c[3 * 4 + j];
     }
-    int ls = level_scale4(p, 0, field, qp % 6, 0, 0);
+    int ls = level_scale_dc(p, 0, qp % 6);
     for (int i = 0; i < 4; i++) {
         int f0 = g[i * 4 + 0] + g[i * 4 + 1] + g[i * 4 + 2] + g[i * 4 + 3];
         int f1 = g[i * 4 + 0] + g[i * 4 + 1] - g[i * 4 + 2] - g[i * 4 + 3];
@@ -317,7 +263,7 @@ __device__ __forceinline__ void chroma_dc(const PicDesc &p, const int32_t lv[4],
 {
     int e00 = lv[0] + lv[2], e01 = lv[1] + lv[3], e10 = lv[0] - lv[2], e11 = lv[1] - lv[3];
     int f[4] = {e00 + e01, e00 - e01, e10 + e11, e10 - e11};
-    int ls = level_scale4(p, ls_list, field, qpc % 6, 0, 0);
+    int ls = level_scale_dc(p, ls_list, qpc % 6);
     for (int i = 0; i < 4; i++) dcC[i] = ((f[i] * ls) << (qpc / 6)) >> 5;
 }
 
@@ -348,32 +294,6 @@ __device__ __forceinline__ bool coef_view(const PicDesc &p, const h264r_mb &m, C
     v.lv = (const int16_t *)(p.coef + voff);
     v.max_levels = (int)((p.coef_bytes - voff) / 2);
     return true;
-}
-
-// word index and level index of block bit b (all blocks before it)
-__device__ __forceinline__ void coef_block(const CoefView &v, int b, int &word, int &level)
-{
-    uint32_t before = v.mask & ((1u << b) - 1u);
-    word = __popc(before) + (v.t8 ? 3 * __popc(before & 15u) : 0);
-    level = 0;
-    for (int w = 0; w < word; w++) level += __popc((uint32_t)v.sig[w]);
-}
-
-// scan list of a 16-position block bit b into raster array c (zeroed first)
-__device__ __forceinline__ void coef_list16(const CoefView &v, int b, int field, int32_t c[16])
-{
-#pragma unroll
-    for (int i = 0; i < 16; i++) c[i] = 0;
-    if (!(v.mask & (1u << b))) return;
-    int w, l;
-    coef_block(v, b, w, l);
-    uint32_t s = v.sig[w];
-    const uint8_t *scan = field ? kField4x4 : kZigzag4x4;
-    while (s && l < v.max_levels) {
-        int k = __ffs(s) - 1;
-        s &= s - 1;
-        c[scan[k]] = v.lv[l++];
-    }
 }
 
 // ---------------------------------------------------------------- motion

@@ -164,47 +164,91 @@ __device__ __forceinline__ void itrans4_tile(int32_t *b, int st)
     }
 }
 
-__device__ __forceinline__ int norm4_class(int i, int j) { return ((i & 1) == 0 && (j & 1) == 0) ? 0 : (((i & 1) && (j & 1)) ? 1 : 2); }
+// Dequantisation of the levels of one block list (8.5.12.1 / 8.5.13.1),
+// prepared once per lane: the normAdjust values of qP % 6 by position class
+// and the shifts of qP / 6, so that a level costs a multiply and two shifts.
+struct Dequant {
+    uint64_t v;  // byte c: normAdjust of position class c
+    int lsh, rnd, rsh;
+};
 
-__device__ __forceinline__ int norm8_class(int i, int j)
+// 4x4: qP >= 24 shifts left by qP/6 - 4, else rounds and shifts right by 4 - qP/6
+__device__ __forceinline__ Dequant dequant4(int qp)
 {
-    if (i % 4 == 0 && j % 4 == 0) return 0;
-    if (i % 2 == 1 && j % 2 == 1) return 1;
-    if (i % 4 == 2 && j % 4 == 2) return 2;
-    if ((i % 4 == 0 && j % 2 == 1) || (i % 2 == 1 && j % 4 == 0)) return 3;
-    if ((i % 4 == 0 && j % 4 == 2) || (i % 4 == 2 && j % 4 == 0)) return 4;
-    return 5;
+    const int q6 = qp / 6;
+    Dequant d;
+    d.v = kV4P[qp % 6];
+    d.lsh = q6 >= 4 ? q6 - 4 : 0;
+    d.rnd = q6 >= 4 ? 0 : 1 << (3 - q6);
+    d.rsh = q6 >= 4 ? 0 : 4 - q6;
+    return d;
 }
 
-// scaled coefficient of a 4x4 block (LevelScale4x4 from scan position k)
-__device__ __forceinline__ int scale4(const PicDesc &p, int list, int k, int raster, int qp, int v)
+// 8x8: qP >= 36 shifts left by qP/6 - 6, else rounds and shifts right by 6 - qP/6
+__device__ __forceinline__ Dequant dequant8(int qp)
 {
-    const int ws = p.flat_scaling ? 16 : p.scaling[list * 16 + k];
-    const int ls = ws * kV4[qp % 6][norm4_class(raster >> 2, raster & 3)];
-    return qp >= 24 ? (v * ls) << (qp / 6 - 4) : (v * ls + (1 << (3 - qp / 6))) >> (4 - qp / 6);
+    const int q6 = qp / 6;
+    Dequant d;
+    d.v = kV8P[qp % 6];
+    d.lsh = q6 >= 6 ? q6 - 6 : 0;
+    d.rnd = q6 >= 6 ? 0 : 1 << (5 - q6);
+    d.rsh = q6 >= 6 ? 0 : 6 - q6;
+    return d;
 }
 
-__device__ __forceinline__ int scale8(const PicDesc &p, int list, int k, int raster, int qp, int v)
+__device__ __forceinline__ int dequant(const Dequant &d, int cls, int ws, int level)
 {
-    const int ws = p.flat_scaling ? 16 : p.scaling[96 + list * 64 + k];
-    const int ls = ws * kV8[qp % 6][norm8_class(raster >> 3, raster & 7)];
-    return qp >= 36 ? (v * ls) << (qp / 6 - 6) : (v * ls + (1 << (5 - qp / 6))) >> (6 - qp / 6);
+    const int ls = ws * (int)((d.v >> (8 * cls)) & 255u);
+    return (((level * ls) << d.lsh) + d.rnd) >> d.rsh;
 }
+
+// position class of raster index rp of a 4x4 block: 0 even row and column,
+// 1 odd row and column, 2 otherwise
+__device__ __forceinline__ int class4(int rp)
+{
+    const int t = rp & 5;
+    return t == 0 ? 0 : (t == 5 ? 1 : 2);
+}
+
+// position class of (i, j) in an 8x8 block (the six normAdjust8x8 cases)
+constexpr int norm8_class_of(int i, int j)
+{
+    return (i % 4 == 0 && j % 4 == 0) ? 0
+         : (i % 2 == 1 && j % 2 == 1) ? 1
+         : (i % 4 == 2 && j % 4 == 2) ? 2
+         : ((i % 4 == 0 && j % 2 == 1) || (i % 2 == 1 && j % 4 == 0)) ? 3
+         : ((i % 4 == 0 && j % 4 == 2) || (i % 4 == 2 && j % 4 == 0)) ? 4 : 5;
+}
+// the class depends on (i & 3, j & 3) only: 3 bits at 3 * (4 (i & 3) + (j & 3))
+constexpr uint64_t pack_class8()
+{
+    uint64_t v = 0;
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) v |= (uint64_t)norm8_class_of(i, j) << (3 * (4 * i + j));
+    return v;
+}
+constexpr uint64_t kClass8 = pack_class8();
+
+__device__ __forceinline__ int class8(int rp) { return (int)((kClass8 >> (3 * (((rp >> 1) & 12) | (rp & 3)))) & 7u); }
 
 // res: 384 ints (luma 16x16 raster, Cb 8x8, Cr 8x8); dcs: 32 ints of
-// scratch.  ls4 / ls8: LevelScale lists of the luma blocks (intra 0 / 0,
-// inter 3 / 1); the chroma blocks use ls4 as well (quirk: the reference
-// scales chroma with the LevelScale4x4 it computed last, the luma one,
-// H264PictureBase.cpp:3752-3940).  Returns false for a malformed payload
-// (the residual is then zero).
-__device__ bool mb_residual(const PicDesc &p, const h264r_mb &m, int field, int ls4, int ls8, int32_t *res, int32_t *dcs)
+// scratch; lev: 512 int16 of scratch (the MB's levels, copied in once).
+// ls4 / ls8: LevelScale lists of the luma blocks (intra 0 / 0, inter 3 /
+// 1); the chroma blocks use ls4 as well (quirk: the reference scales chroma
+// with the LevelScale4x4 it computed last, the luma one,
+// H264PictureBase.cpp:3752-3940).  Luma 4x4 blocks (lanes 0-15) and chroma
+// AC blocks (lanes 16-23) are scattered and transformed in one pass.
+// Returns false for a malformed payload (the residual is then zero).
+__device__ bool mb_residual(const PicDesc &p, const h264r_mb &m, int field, int ls4, int ls8, int32_t *res, int32_t *dcs,
+                            int16_t *lev)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    int4 *res4 = reinterpret_cast<int4 *>(res);
 #pragma unroll
-    for (int i = 0; i < 12; i++) res[lane + 32 * i] = 0;
+    for (int i = 0; i < 3; i++) res4[lane + 32 * i] = make_int4(0, 0, 0, 0);
     CoefView cv;
-    bool ok = coef_view(p, m, cv);
+    const bool ok = coef_view(p, m, cv);
     const uint32_t mask = ok ? cv.mask : 0u;
     if (mask == 0) {
         __syncwarp();
@@ -221,18 +265,20 @@ __device__ bool mb_residual(const PicDesc &p, const h264r_mb &m, int field, int 
         if (lane >= o) inc += t;
     }
     const int off = inc - cnt;
-    if (__shfl_sync(FULL, inc, 31) > cv.max_levels) {
+    const int total = __shfl_sync(FULL, inc, 31);  // at most 32 words of 16 bits
+    if (total > cv.max_levels) {
         __syncwarp();
         return false;
     }
+    for (int i = lane; i < total; i += 32) lev[i] = cv.lv[i];
+    __syncwarp();
     auto word_of = [&](int bit) -> int {
         const uint32_t before = mask & ((1u << bit) - 1u);
         return __popc(before) + (t8 ? 3 * __popc(before & 15u) : 0);
     };
     const int qp = m.qpy;
     const bool i16 = m.type == H264R_MB_I16x16;
-    const uint8_t *scan4 = field ? kField4x4 : kZigzag4x4;
-    const int16_t *lv = cv.lv;
+    const uint64_t scan4 = field ? kField4P : kZigzag4P;
     // ---- Intra16x16 DC (8.5.10)
     if (i16) {
         const int w = word_of(16) & 31;
@@ -240,13 +286,13 @@ __device__ bool mb_residual(const PicDesc &p, const h264r_mb &m, int field, int 
         const int o = __shfl_sync(FULL, off, w);
         if (lane < 16) {
             const int k = lane;
-            dcs[scan4[k]] = ((sg >> k) & 1) ? lv[o + __popc(sg & ((1u << k) - 1u))] : 0;
+            dcs[(scan4 >> (4 * k)) & 15u] = ((sg >> k) & 1) ? lev[o + __popc(sg & ((1u << k) - 1u))] : 0;
         }
         __syncwarp();
         if (lane == 0) luma_dc(p, dcs, field, qp, dcs + 16);
         __syncwarp();
     }
-    // ---- luma levels
+    // ---- luma 8x8 levels: lane (b, r) owns scan indices 8r..8r+7 of block b
     if (t8) {
         const int b = lane >> 3, r = lane & 7;
         const int w = (word_of(b) + (r >> 1)) & 31;
@@ -256,89 +302,79 @@ __device__ bool mb_residual(const PicDesc &p, const h264r_mb &m, int field, int 
             const int half = (r & 1) * 8;
             int l = o + __popc(sg & ((1u << half) - 1u));
             uint32_t bits = (sg >> half) & 255u;
-            const uint8_t *scan8 = field ? kField8x8 : kZigzag8x8;
-            const int bx = (b & 1) * 8, by = (b >> 1) * 8;
+            const uint64_t sc = kScan8P[field][r];
+            const Dequant dq = dequant8(qp);
+            int32_t *blk = res + (b >> 1) * 128 + (b & 1) * 8;
             while (bits) {
                 const int t = __ffs(bits) - 1;
                 bits &= bits - 1;
-                const int k = 16 * (r >> 1) + half + t, rp = scan8[k];
-                res[(by + (rp >> 3)) * 16 + bx + (rp & 7)] = scale8(p, ls8, k, rp, qp, lv[l++]);
+                const int rp = (int)((sc >> (6 * t)) & 63u);
+                const int ws = p.flat_scaling ? 16 : p.scaling[96 + ls8 * 64 + 8 * r + t];
+                blk[(rp >> 3) * 16 + (rp & 7)] = dequant(dq, class8(rp), ws, lev[l++]);
             }
-        }
-    } else {
-        const int b = lane & 15;
-        const int w = word_of(b) & 31;
-        const uint32_t sg = __shfl_sync(FULL, sw, w);
-        const int o = __shfl_sync(FULL, off, w);
-        if (lane < 16) {
-            const int bx = kBlkX[b] * 4, by = kBlkY[b] * 4;
-            if (mask & (1u << b)) {
-                int l = o;
-                uint32_t bits = sg & 0xFFFFu;
-                while (bits) {
-                    const int k = __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    const int rp = scan4[k];
-                    res[(by + (rp >> 2)) * 16 + bx + (rp & 3)] = scale4(p, ls4, k, rp, qp, lv[l++]);
-                }
-            }
-            if (i16) res[by * 16 + bx] = dcs[16 + kBlkY[b] * 4 + kBlkX[b]];
         }
     }
-    // ---- chroma levels (lanes 16..23: plane (lane-16)>>2, block (lane-16)&3)
+    // ---- 4x4 levels: lanes 0-15 luma block `lane` (unless 8x8), lanes
+    // 16-23 chroma AC block (plane (lane-16)>>2, block (lane-16)&3)
     const int pl = ((lane - 16) >> 2) & 1, cb = (lane - 16) & 3;
     const bool chroma_lane = lane >= 16 && lane < 24;
-    const int wdc = word_of(17 + pl) & 31, wac = word_of(H264R_CM_CB_AC0 + 4 * pl + cb) & 31;
-    const uint32_t sdc = __shfl_sync(FULL, sw, wdc), sac = __shfl_sync(FULL, sw, wac);
-    const int odc = __shfl_sync(FULL, off, wdc), oac = __shfl_sync(FULL, off, wac);
     const bool any_chroma = (mask >> 17) != 0;
+    const int bx = (((lane >> 2) & 1) << 1) | (lane & 1), by = (((lane >> 3) & 1) << 1) | ((lane >> 1) & 1);
+    const int my_bit = lane < 16 ? lane : (H264R_CM_CB_AC0 + 4 * pl + cb);
+    const int wq = word_of(my_bit) & 31, wdc = word_of(17 + pl) & 31;
+    const uint32_t sq = __shfl_sync(FULL, sw, wq), sdc = __shfl_sync(FULL, sw, wdc);
+    const int oq = __shfl_sync(FULL, off, wq), odc = __shfl_sync(FULL, off, wdc);
+    int qpc = qp;
+    if (chroma_lane) qpc = chroma_qp(qp, p.slices[min((uint32_t)m.slice, p.num_slices - 1)].chroma_qp_offset[pl]);
+    int32_t *blk = lane < 16 ? res + by * 64 + bx * 4 : res + 256 + pl * 64 + (cb >> 1) * 32 + (cb & 1) * 4;
+    const int stride = lane < 16 ? 16 : 8;
+    {
+        uint32_t bits = 0;
+        if (lane < 16 ? (!t8 && ((mask >> lane) & 1)) : (chroma_lane && ((mask >> my_bit) & 1))) bits = sq & 0xFFFFu;
+        const Dequant dq = dequant4(lane < 16 ? qp : qpc);
+        int l = oq;
+        // chroma: AC list (a level at position 0 is replaced by the DC below)
+        while (bits) {
+            const int k = __ffs(bits) - 1;
+            bits &= bits - 1;
+            const int rp = (int)((scan4 >> (4 * k)) & 15u);
+            const int ws = p.flat_scaling ? 16 : p.scaling[ls4 * 16 + k];
+            blk[(rp >> 2) * stride + (rp & 3)] = dequant(dq, class4(rp), ws, lev[l++]);
+        }
+    }
+    if (lane < 16 && i16 && !t8) blk[0] = dcs[16 + by * 4 + bx];
     if (chroma_lane && any_chroma) {
-        const int qpc = chroma_qp(qp, p.slices[min((uint32_t)m.slice, p.num_slices - 1)].chroma_qp_offset[pl]);
         int32_t dc4[4] = {0, 0, 0, 0}, dcC[4];
         if (mask & (1u << (17 + pl))) {
 #pragma unroll
-            for (int k = 0; k < 4; k++) dc4[k] = ((sdc >> k) & 1) ? lv[odc + __popc(sdc & ((1u << k) - 1u))] : 0;
+            for (int k = 0; k < 4; k++) dc4[k] = ((sdc >> k) & 1) ? lev[odc + __popc(sdc & ((1u << k) - 1u))] : 0;
         }
         chroma_dc(p, dc4, field, qpc, ls4, dcC);
-        int32_t *blk = res + 256 + pl * 64 + (cb >> 1) * 32 + (cb & 1) * 4;
-        if (mask & (1u << (H264R_CM_CB_AC0 + 4 * pl + cb))) {
-            int l = oac;
-            uint32_t bits = sac & 0xFFFFu;  // AC list: positions 1..15 (a level at 0 is replaced by DC below)
-            while (bits) {
-                const int k = __ffs(bits) - 1;
-                bits &= bits - 1;
-                const int rp = scan4[k];
-                blk[(rp >> 2) * 8 + (rp & 3)] = scale4(p, ls4, k, rp, qpc, lv[l++]);
-            }
-        }
         blk[0] = cb == 0 ? dcC[0] : cb == 1 ? dcC[1] : cb == 2 ? dcC[2] : dcC[3];
     }
     __syncwarp();
     // ---- inverse transforms in place
     if (t8) {
         const int b = lane >> 3, r = lane & 7;
-        const int bx = (b & 1) * 8, by = (b >> 1) * 8;
+        const int x8 = (b & 1) * 8, y8 = (b >> 1) * 8;
         const bool on = (mask >> b) & 1;
         int o8[8];
         if (on) {
-            int32_t *row = res + (by + r) * 16 + bx;
+            int32_t *row = res + (y8 + r) * 16 + x8;
             idct8_1d(row[0], row[1], row[2], row[3], row[4], row[5], row[6], row[7], o8);
 #pragma unroll
             for (int j = 0; j < 8; j++) row[j] = o8[j];
         }
         __syncwarp();
         if (on) {
-            int32_t *col = res + by * 16 + bx + r;
+            int32_t *col = res + y8 * 16 + x8 + r;
             idct8_1d(col[0], col[16], col[32], col[48], col[64], col[80], col[96], col[112], o8);
 #pragma unroll
             for (int i = 0; i < 8; i++) col[i * 16] = (o8[i] + 32) >> 6;
         }
-    } else if (lane < 16) {
-        const int b = lane;
-        const int bx = kBlkX[b] * 4, by = kBlkY[b] * 4;
-        if (((mask >> b) & 1) || (i16 && dcs[16 + kBlkY[b] * 4 + kBlkX[b]] != 0)) itrans4_tile(res + by * 16 + bx, 16);
     }
-    if (chroma_lane && any_chroma) itrans4_tile(res + 256 + pl * 64 + (cb >> 1) * 32 + (cb & 1) * 4, 8);
+    const bool on4 = lane < 16 ? (!t8 && (((mask >> lane) & 1) || (i16 && dcs[16 + by * 4 + bx] != 0))) : (chroma_lane && any_chroma);
+    if (on4) itrans4_tile(blk, stride);
     __syncwarp();
     return ok;
 }
@@ -358,6 +394,7 @@ struct InterWarpSmem {
     int32_t res[384];      // residual: luma raster 16x16, Cb 8x8, Cr 8x8
     int32_t dcs[32];       // Intra16x16 DC work area
     __align__(16) uint8_t out[384];
+    int16_t lev[512];      // the MB's coefficient levels
 };
 
 
@@ -443,7 +480,7 @@ __global__ void __launch_bounds__(32 * kInterWarps, 6) k_inter(const PicDesc *__
     // (the code of this kernel is kept compact: instruction fetch, not
     // arithmetic or memory, is what its warps wait on)
     if (intra || m.type == H264R_MB_INTER) {
-        if (!mb_residual(p, m, field, intra ? 0 : 3, intra ? 0 : 1, s.res, s.dcs) && lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
+        if (!mb_residual(p, m, field, intra ? 0 : 3, intra ? 0 : 1, s.res, s.dcs, s.lev) && lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
     }
     if (intra) {
         // intra MB: only its residual, for the intra wavefront (k_intra).
