@@ -684,26 +684,6 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     const h264r_mb m = s.rec[buf];
     const int W = p.W, Wc = p.Wc, wmb = p.wmb;
     int x, y, dy;  // first luma sample and row step (2 for a field MB of an MBAFF picture)
-    bool A = false, B = false, Cc = false, D = false;
-    if (p.mbaff) {
-        mb_origin(p, addr, x, y, dy);
-    } else {
-        // neighbour MBs (6.4.9 / getMbAddrN_non_MBAFF_frames) and CIP
-        const int mx = addr % wmb, my = addr / wmb;
-        x = mx * 16;
-        y = my * 16;
-        dy = 1;
-        auto usable = [&](int n) -> bool {
-            if (n < 0 || n > addr) return false;
-            const h264r_mb &q = p.mbs[n];
-            if (q.slice != m.slice) return false;
-            return !(q.type == H264R_MB_INTER && (q.flags & H264R_MBF_CIP));
-        };
-        A = mx > 0 && usable(addr - 1);
-        B = my > 0 && usable(addr - wmb);
-        Cc = my > 0 && mx + 1 < wmb && usable(addr - wmb + 1);
-        D = mx > 0 && my > 0 && usable(addr - wmb - 1);
-    }
     uint8_t *Y = plane_y(p);
     // ---- residual (computed by k_inter), from the prefetch buffer
 #pragma unroll
@@ -715,36 +695,91 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     }
     // ---- stage the neighbourhood (luma: corner, 16 left, 24 top; chroma:
     //      corner, 8 left, 8 top), -1 where not available for intra
-    //      prediction.  In an MBAFF picture every sample goes through the
-    //      MBAFF neighbour derivation (6.4.12.2): the left column of a frame
-    //      MB beside a field pair alternates between the pair's MBs, and
-    //      under constrained intra prediction parts of it can be missing.
+    //      prediction.  Item i (lane + 32 * it): 0 luma corner, 1..16 left,
+    //      17..40 top; 41..74 chroma (17 per plane: corner, 8 left, 8 top).
     uint32_t avail[3];
+    if (p.mbaff) {
+        // every sample through the MBAFF neighbour derivation (6.4.12.2):
+        // the left column of a frame MB beside a field pair alternates
+        // between the pair's MBs, and under constrained intra prediction
+        // parts of it can be missing
+        mb_origin(p, addr, x, y, dy);
 #pragma unroll
-    for (int it = 0; it < 3; it++) {
-        const int i = lane + 32 * it;
-        int v = -1;
-        if (i < 41) {
-            const int xN = i == 0 ? -1 : (i < 17 ? -1 : i - 17), yN = i == 0 ? -1 : (i < 17 ? i - 1 : -1);
-            if (p.mbaff) {
+        for (int it = 0; it < 3; it++) {
+            const int i = lane + 32 * it;
+            int v = -1;
+            if (i < 41) {
+                const int xN = i == 0 ? -1 : (i < 17 ? -1 : i - 17), yN = i == 0 ? -1 : (i < 17 ? i - 1 : -1);
                 const uint8_t *ptr = intra_nb_ptr(p, addr, 0, 0, xN, yN);
                 if (ptr) v = __ldcg(ptr);
-            } else if (i == 0 ? D : (i < 17 ? A : (i < 33 ? B : Cc))) {
-                v = __ldcg(Y + (size_t)(y + yN) * W + x + xN);
-            }
-            t.l[yN + 1][xN + 1] = v;
-        } else if (i < 75) {
-            const int j = i - 41, pl = j / 17, q = j % 17;
-            const int xN = q < 9 ? -1 : q - 9, yN = q < 9 ? q - 1 : -1;
-            if (p.mbaff) {
+                t.l[yN + 1][xN + 1] = v;
+            } else if (i < 75) {
+                const int j = i - 41, pl = j / 17, q = j % 17;
+                const int xN = q < 9 ? -1 : q - 9, yN = q < 9 ? q - 1 : -1;
                 const uint8_t *ptr = intra_nb_ptr(p, addr, 1, pl, xN, yN);
                 if (ptr) v = __ldcg(ptr);
-            } else if (q == 0 ? D : (q < 9 ? A : B)) {
-                v = __ldcg(plane_c(p, pl) + (size_t)(y / 2 + yN) * Wc + x / 2 + xN);
+                t.c[pl][yN + 1][xN + 1] = v;
             }
-            t.c[pl][yN + 1][xN + 1] = v;
+            avail[it] = __ballot_sync(0xffffffffu, v >= 0);
         }
-        avail[it] = __ballot_sync(0xffffffffu, v >= 0);
+    } else {
+        // Neighbour MBs A (left), B (above), C (above right), D (above left)
+        // (6.4.9, getMbAddrN_non_MBAFF_frames) and every neighbouring sample
+        // are loaded together; availability for intra prediction (same slice,
+        // constrained intra prediction) is applied to the samples afterwards.
+        const int mx = addr % wmb, my = addr / wmb;
+        x = mx * 16;
+        y = my * 16;
+        dy = 1;
+        const bool inA = mx > 0, inB = my > 0, inC = my > 0 && mx + 1 < wmb, inD = mx > 0 && my > 0;
+        uint32_t r0 = 0, r2 = 0;  // record words 0 (type, flags) and 2 (slice) of neighbour `lane`
+        const bool nb_in = lane < 4 && (lane == 0 ? inA : lane == 1 ? inB : lane == 2 ? inC : inD);
+        if (nb_in) {
+            const int n = lane == 0 ? addr - 1 : lane == 1 ? addr - wmb : lane == 2 ? addr - wmb + 1 : addr - wmb - 1;
+            const uint32_t *q = (const uint32_t *)(p.mbs + n);
+            r0 = __ldg(q);
+            r2 = __ldg(q + 2);
+        }
+        int v[3], owner[3];  // owner: the neighbour MB (0 A, 1 B, 2 C, 3 D) of the item, -1 none
+#pragma unroll
+        for (int it = 0; it < 3; it++) {
+            const int i = lane + 32 * it;
+            v[it] = -1;
+            owner[it] = -1;
+            if (i < 41) {
+                const int xN = i == 0 ? -1 : (i < 17 ? -1 : i - 17), yN = i == 0 ? -1 : (i < 17 ? i - 1 : -1);
+                const int o = i == 0 ? 3 : (i < 17 ? 0 : (xN < 16 ? 1 : 2));
+                if (o == 0 ? inA : o == 1 ? inB : o == 2 ? inC : inD) {
+                    owner[it] = o;
+                    v[it] = __ldcg(Y + (size_t)(y + yN) * W + x + xN);
+                }
+            } else if (i < 75) {
+                const int j = i - 41, pl = j / 17, q = j % 17;
+                const int xN = q < 9 ? -1 : q - 9, yN = q < 9 ? q - 1 : -1;
+                const int o = q == 0 ? 3 : (q < 9 ? 0 : 1);
+                if (o == 0 ? inA : o == 1 ? inB : inD) {
+                    owner[it] = o;
+                    v[it] = __ldcg(plane_c(p, pl) + (size_t)(y / 2 + yN) * Wc + x / 2 + xN);
+                }
+            }
+        }
+        // same slice, and not an inter MB under constrained intra prediction
+        const bool usable = nb_in && (r2 & 0xFFFFu) == m.slice && !((r0 & 255u) == H264R_MB_INTER && ((r0 >> 8) & H264R_MBF_CIP));
+        const uint32_t um = __ballot_sync(0xffffffffu, usable);
+#pragma unroll
+        for (int it = 0; it < 3; it++) {
+            const int i = lane + 32 * it;
+            const int val = (owner[it] >= 0 && ((um >> owner[it]) & 1u)) ? v[it] : -1;
+            if (i < 41) {
+                const int xN = i == 0 ? -1 : (i < 17 ? -1 : i - 17), yN = i == 0 ? -1 : (i < 17 ? i - 1 : -1);
+                t.l[yN + 1][xN + 1] = val;
+            } else if (i < 75) {
+                const int j = i - 41, pl = j / 17, q = j % 17;
+                const int xN = q < 9 ? -1 : q - 9, yN = q < 9 ? q - 1 : -1;
+                t.c[pl][yN + 1][xN + 1] = val;
+            }
+            avail[it] = __ballot_sync(0xffffffffu, val >= 0);
+        }
     }
     // whole-edge availability from the staged samples (item i is bit i % 32
     // of avail[i / 32]): luma left 1..16, top 17..32; Cb corner 41, left
@@ -759,49 +794,43 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
         // The 4x4 blocks on one anti-diagonal of the block grid (bx + 2*by
         // constant) depend on none of each other (left, top, top-left and
         // top-right all lie on earlier diagonals): 10 waves of at most two
-        // blocks, one per half-warp, in place of 16 steps.
-        const int half = lane >> 4, hl = lane & 15;
-        int *nb = s.nb4[half];
+        // blocks, one per half-warp, in place of 16 steps.  A lane reads the
+        // three neighbours its table entry names straight from the tile;
+        // availability comes from the MB-edge bitmaps and the block position
+        // (inside the MB every earlier block is reconstructed; the top-right
+        // block is not yet for blocks 3, 7, 11, 13 and 15, 8.3.1.2).
+        const int half = lane >> 4, hl = lane & 15, i = hl >> 2, j = hl & 3;
+        const uint32_t leftm = (avail[0] >> 1) & 0xFFFFu;                     // p[-1, 0..15]
+        const uint32_t topm = (avail[0] >> 17) | ((avail[1] & 0x1FFu) << 15);  // p[0..23, -1]
+        const bool cornerm = avail[0] & 1u;
         for (int wv = 0; wv < 10; wv++) {
             const int by = min(3, wv >> 1) - half, bx = wv - 2 * by;
-            const bool valid = by >= 0 && bx >= 0 && bx <= 3;
-            const int b = 8 * (by >> 1) + 4 * (bx >> 1) + 2 * (by & 1) + (bx & 1);
-            const int xO = bx * 4, yO = by * 4;
-            int v = -1;
-            if (valid && hl < 13) {
-                // nb = {p[-1,-1], p[-1,0..3], p[0..7,-1]}; an unavailable
-                // top-right quartet takes p[3,-1] (the four are available
-                // together or not at all)
-                if (hl == 0) {
-                    v = tile_nb(t, xO - 1, yO - 1, true);
-                } else if (hl < 5) {
-                    v = tile_nb(t, xO - 1, yO + hl - 1, true);
-                } else {
-                    const int i = hl - 5;
-                    v = tile_nb(t, xO + i, yO - 1, !(i > 3 && (b == 3 || b == 11)));
-                    if (i > 3 && v < 0) v = tile_nb(t, xO + 3, yO - 1, true);
-                }
-                nb[hl] = v;
-            }
-            // availability of the half's 13 samples (bit k: nb[k] available)
-            const uint32_t am = (__ballot_sync(0xffffffffu, v >= 0) >> (16 * half)) & 0x1FFFu;
-            __syncwarp();
-            if (valid) {
-                const int i = hl >> 2, j = hl & 3;
+            if (by >= 0 && bx >= 0 && bx <= 3) {
+                const int b = 8 * (by >> 1) + 4 * (bx >> 1) + 2 * (by & 1) + (bx & 1);
+                const int xO = bx * 4, yO = by * 4;
+                const bool left = bx > 0 || ((leftm >> yO) & 15u) == 15u;
+                const bool top = by > 0 || ((topm >> xO) & 15u) == 15u;
+                const bool corner = bx > 0 ? (by > 0 || ((topm >> (xO - 1)) & 1u)) : (by > 0 ? ((leftm >> (yO - 1)) & 1u) : cornerm);
+                // p[4..7, -1] of the block: bit k available (else p[3, -1] stands in)
+                const uint32_t trm = by > 0 ? ((bx < 3 && b != 3 && b != 11) ? 15u : 0u) : ((topm >> (xO + 4)) & 15u);
                 const int mode = (m.ipred[b >> 3] >> (4 * (b & 7))) & 15;
-                const bool corner = am & 1u, left = ((am >> 1) & 15u) == 15u, top = ((am >> 5) & 15u) == 15u;
-                const bool top8 = ((am >> 5) & 0xFFu) == 0xFFu;
+                // T[r * 25 + c] = p[xO + c - 1, yO + r - 1]
+                const int *T = &t.l[yO][xO];
+                // tile offset of neighbour index k of {p[-1,-1], p[-1,0..3], p[0..7,-1]}
+                auto at = [&](uint32_t k) -> int {
+                    return k == 0 ? 0 : (k <= 4 ? 25 * (int)k : ((k >= 9 && !((trm >> (k - 9)) & 1u)) ? 4 : (int)k - 4));
+                };
                 int pv = 0;  // a mode without its samples writes no prediction: the cleared buffer
                 if (mode == 2) {
-                    const int st4 = top ? nb[5] + nb[6] + nb[7] + nb[8] : 0, sl4 = left ? nb[1] + nb[2] + nb[3] + nb[4] : 0;
+                    const int st4 = top ? T[1] + T[2] + T[3] + T[4] : 0, sl4 = left ? T[25] + T[50] + T[75] + T[100] : 0;
                     pv = (top && left) ? (st4 + sl4 + 4) >> 3 : left ? (sl4 + 2) >> 2 : top ? (st4 + 2) >> 2 : 128;
                 } else if (mode <= 8) {
-                    const bool ok = mode == 0 ? top : (mode == 1 || mode == 8) ? left : (mode == 3 || mode == 7) ? top8
+                    const bool ok = mode == 0 ? top : (mode == 1 || mode == 8) ? left : (mode == 3 || mode == 7) ? top
                                                                                                       : (top && left && corner);
                     if (ok) {
                         const uint32_t e = s.pred4[mode][hl];
-                        pv = ((int)((e >> 12) & 7u) * nb[e & 15u] + (int)((e >> 15) & 7u) * nb[(e >> 4) & 15u] +
-                              (int)((e >> 18) & 7u) * nb[(e >> 8) & 15u] + 2) >> 2;
+                        pv = ((int)((e >> 12) & 7u) * T[at(e & 15u)] + (int)((e >> 15) & 7u) * T[at((e >> 4) & 15u)] +
+                              (int)((e >> 18) & 7u) * T[at((e >> 8) & 15u)] + 2) >> 2;
                     }
                 }
                 t.l[yO + i + 1][xO + j + 1] = clip1(pv + s.res[(yO + i) * 16 + xO + j]);
