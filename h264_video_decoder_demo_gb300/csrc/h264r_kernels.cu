@@ -620,16 +620,16 @@ __device__ const uint32_t kPred8[9][64] = {
 };
 
 struct IntraSmem {
-    int32_t res[384];     // residual: luma raster 16x16, Cb 8x8, Cr 8x8
     int nb[40];           // neighbouring samples (-1: not available)
     int nbf[40];          // filtered (8x8) neighbours
-    int nb4[2][16];       // neighbours of the two 4x4 blocks of a wave
+    uint32_t d4[10][32];  // Intra_4x4: what each lane computes in each wave
     // record and residual (int16 pairs, as k_inter stored them) of an intra
     // MB, copied in ahead of its turn; two buffers so that the next MB's copy
     // overlaps the current MB's work
     __align__(16) uint32_t raw[2][192];
     __align__(16) h264r_mb rec[2];
     uint32_t pred4[9][16];  // kPred4, for lane-varying reads
+    uint32_t pred8[9][64];  // kPred8
     int cpar[8];            // chroma: DC per plane and quadrant, or plane a, b, c per plane
 };
 
@@ -664,8 +664,8 @@ __device__ __forceinline__ void intra_prefetch(const PicDesc &p, int addr, Intra
 // getMbAddrN_MBAFF_frames for the MB's border and the Intra_4x4/8x8 block
 // rules inside it.
 struct IntraTile {
-    int l[17][25];     // luma rows -1..15 (index +1), cols -1..23 (index +1)
-    int c[2][9][9];    // chroma rows -1..7, cols -1..7
+    int16_t l[17][25];     // luma rows -1..15 (index +1), cols -1..23 (index +1)
+    int16_t c[2][9][9];    // chroma rows -1..7, cols -1..7
 };
 
 // luma neighbour p[xN, yN] (relative to the MB) of a block, -1 when not
@@ -685,14 +685,9 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     const int W = p.W, Wc = p.Wc, wmb = p.wmb;
     int x, y, dy;  // first luma sample and row step (2 for a field MB of an MBAFF picture)
     uint8_t *Y = plane_y(p);
-    // ---- residual (computed by k_inter), from the prefetch buffer
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-        const int i = lane + 32 * k;
-        const uint32_t w = s.raw[buf][i];
-        s.res[2 * i] = (int16_t)(w & 0xFFFFu);
-        s.res[2 * i + 1] = (int16_t)(w >> 16);
-    }
+    // residual (computed by k_inter, luma raster 16x16, Cb 8x8, Cr 8x8) in
+    // the prefetch buffer; the reconstructed chroma replaces it in place
+    int16_t *res = reinterpret_cast<int16_t *>(s.raw[buf]);
     // ---- stage the neighbourhood (luma: corner, 16 left, 24 top; chroma:
     //      corner, 8 left, 8 top), -1 where not available for intra
     //      prediction.  Item i (lane + 32 * it): 0 luma corner, 1..16 left,
@@ -790,83 +785,113 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     const bool cD = (avail[1] >> 9) & 1u;
     __syncwarp();
     // ---- luma
+    // MB-edge availability of the luma neighbours (item bitmaps above)
+    const uint32_t leftm = (avail[0] >> 1) & 0xFFFFu;                     // p[-1, 0..15]
+    const uint32_t topm = (avail[0] >> 17) | ((avail[1] & 0x1FFu) << 15);  // p[0..23, -1]
+    const bool cornerm = avail[0] & 1u;
     if (m.type == H264R_MB_I4x4) {
         // The 4x4 blocks on one anti-diagonal of the block grid (bx + 2*by
         // constant) depend on none of each other (left, top, top-left and
         // top-right all lie on earlier diagonals): 10 waves of at most two
-        // blocks, one per half-warp, in place of 16 steps.  A lane reads the
-        // three neighbours its table entry names straight from the tile;
-        // availability comes from the MB-edge bitmaps and the block position
-        // (inside the MB every earlier block is reconstructed; the top-right
-        // block is not yet for blocks 3, 7, 11, 13 and 15, 8.3.1.2).
+        // blocks, one per half-warp, in place of 16 steps.  What a lane
+        // computes in each wave depends only on the modes and on
+        // availability, so it is worked out for all waves first (independent
+        // iterations) and the waves themselves only read three samples (or
+        // the DC sums) from the tile.  Availability comes from the MB-edge
+        // bitmaps and the block position: inside the MB every earlier block
+        // is reconstructed, and the top-right block is not yet for blocks
+        // 3, 7, 11, 13 and 15 (8.3.1.2).  Wave word: bits 0-1 kind (0 none,
+        // 1 three taps, 2 DC), 2-3 bx, 4-5 by; three taps: 6-17 the three
+        // neighbour indices of {p[-1,-1], p[-1,0..3], p[0..7,-1]} after the
+        // p[3,-1] substitution, 18-26 the weights; DC: bit 6 top, 7 left.
         const int half = lane >> 4, hl = lane & 15, i = hl >> 2, j = hl & 3;
-        const uint32_t leftm = (avail[0] >> 1) & 0xFFFFu;                     // p[-1, 0..15]
-        const uint32_t topm = (avail[0] >> 17) | ((avail[1] & 0x1FFu) << 15);  // p[0..23, -1]
-        const bool cornerm = avail[0] & 1u;
+#pragma unroll 2
         for (int wv = 0; wv < 10; wv++) {
             const int by = min(3, wv >> 1) - half, bx = wv - 2 * by;
+            uint32_t d = 0;
             if (by >= 0 && bx >= 0 && bx <= 3) {
                 const int b = 8 * (by >> 1) + 4 * (bx >> 1) + 2 * (by & 1) + (bx & 1);
                 const int xO = bx * 4, yO = by * 4;
                 const bool left = bx > 0 || ((leftm >> yO) & 15u) == 15u;
                 const bool top = by > 0 || ((topm >> xO) & 15u) == 15u;
                 const bool corner = bx > 0 ? (by > 0 || ((topm >> (xO - 1)) & 1u)) : (by > 0 ? ((leftm >> (yO - 1)) & 1u) : cornerm);
-                // p[4..7, -1] of the block: bit k available (else p[3, -1] stands in)
+                // p[4..7, -1]: bit k available (else p[3, -1] stands in)
                 const uint32_t trm = by > 0 ? ((bx < 3 && b != 3 && b != 11) ? 15u : 0u) : ((topm >> (xO + 4)) & 15u);
                 const int mode = (m.ipred[b >> 3] >> (4 * (b & 7))) & 15;
-                // T[r * 25 + c] = p[xO + c - 1, yO + r - 1]
-                const int *T = &t.l[yO][xO];
-                // tile offset of neighbour index k of {p[-1,-1], p[-1,0..3], p[0..7,-1]}
-                auto at = [&](uint32_t k) -> int {
-                    return k == 0 ? 0 : (k <= 4 ? 25 * (int)k : ((k >= 9 && !((trm >> (k - 9)) & 1u)) ? 4 : (int)k - 4));
-                };
-                int pv = 0;  // a mode without its samples writes no prediction: the cleared buffer
+                const uint32_t pos = ((uint32_t)bx << 2) | ((uint32_t)by << 4);
                 if (mode == 2) {
-                    const int st4 = top ? T[1] + T[2] + T[3] + T[4] : 0, sl4 = left ? T[25] + T[50] + T[75] + T[100] : 0;
-                    pv = (top && left) ? (st4 + sl4 + 4) >> 3 : left ? (sl4 + 2) >> 2 : top ? (st4 + 2) >> 2 : 128;
-                } else if (mode <= 8) {
+                    d = 2u | pos | ((uint32_t)top << 6) | ((uint32_t)left << 7);
+                } else {
                     const bool ok = mode == 0 ? top : (mode == 1 || mode == 8) ? left : (mode == 3 || mode == 7) ? top
                                                                                                       : (top && left && corner);
-                    if (ok) {
-                        const uint32_t e = s.pred4[mode][hl];
-                        pv = ((int)((e >> 12) & 7u) * T[at(e & 15u)] + (int)((e >> 15) & 7u) * T[at((e >> 4) & 15u)] +
-                              (int)((e >> 18) & 7u) * T[at((e >> 8) & 15u)] + 2) >> 2;
+                    // a mode without its samples predicts 0 (the cleared buffer): all weights 0
+                    const uint32_t e = (ok && mode <= 8) ? s.pred4[mode][hl] : 0u;
+                    uint32_t k3 = 0;
+#pragma unroll
+                    for (int q = 0; q < 3; q++) {
+                        uint32_t k = (e >> (4 * q)) & 15u;
+                        if (k >= 9 && !((trm >> (k - 9)) & 1u)) k = 8;
+                        k3 |= k << (4 * q);
                     }
+                    d = 1u | pos | (k3 << 6) | (((e >> 12) & 0x1FFu) << 18);
                 }
-                t.l[yO + i + 1][xO + j + 1] = clip1(pv + s.res[(yO + i) * 16 + xO + j]);
+            }
+            s.d4[wv][lane] = d;
+        }
+        // tile offset of neighbour index k relative to p[-1,-1] of the block
+        auto at = [](uint32_t k) -> int { return k == 0 ? 0 : (k <= 4 ? 25 * (int)k : (int)k - 4); };
+        for (int wv = 0; wv < 10; wv++) {
+            const uint32_t d = s.d4[wv][lane];
+            if (d & 3u) {
+                const int xO = ((d >> 2) & 3u) * 4, yO = ((d >> 4) & 3u) * 4;
+                const int16_t *T = &t.l[yO][xO];  // T[r * 25 + c] = p[xO + c - 1, yO + r - 1]
+                int pv;
+                if (d & 2u) {
+                    const bool top = (d >> 6) & 1u, left = (d >> 7) & 1u;
+                    const int st4 = top ? T[1] + T[2] + T[3] + T[4] : 0, sl4 = left ? T[25] + T[50] + T[75] + T[100] : 0;
+                    pv = (top && left) ? (st4 + sl4 + 4) >> 3 : left ? (sl4 + 2) >> 2 : top ? (st4 + 2) >> 2 : 128;
+                } else {
+                    pv = ((int)((d >> 18) & 7u) * T[at((d >> 6) & 15u)] + (int)((d >> 21) & 7u) * T[at((d >> 10) & 15u)] +
+                          (int)((d >> 24) & 7u) * T[at((d >> 14) & 15u)] + 2) >> 2;
+                }
+                t.l[yO + i + 1][xO + j + 1] = clip1(pv + res[(yO + i) * 16 + xO + j]);
             }
             __syncwarp();
         }
     } else if (m.type == H264R_MB_I8x8) {
+        // availability of q = {p[-1,-1], p[-1,0..7], p[0..15,-1]} per 8x8
+        // block from the MB-edge bitmaps: inside the MB every earlier block is
+        // reconstructed; the top-right octet of block 3 is right of the MB
         for (int b = 0; b < 4; b++) {
             const int xO = (b & 1) * 8, yO = (b >> 1) * 8;
-            // q = {p[-1,-1], p[-1,0..7], p[0..15,-1]}; an unavailable
-            // top-right octet takes p[7,-1]
-            int v = -1;
+            const bool cor = b == 3 || (b == 0 ? cornerm : (b == 1 ? ((topm >> 7) & 1u) : ((leftm >> 7) & 1u)));
+            const bool left8 = (b & 1) || ((leftm >> yO) & 0xFFu) == 0xFFu;
+            const bool top8 = (b & 2) || ((topm >> xO) & 0xFFu) == 0xFFu;
+            // p[8..15, -1] of the block: bit k available (else p[7, -1] stands in)
+            const uint32_t trm = b == 0 ? ((topm >> 8) & 0xFFu) : (b == 1 ? ((topm >> 16) & 0xFFu) : (b == 2 ? 0xFFu : 0u));
+            // an unavailable top-right octet takes p[7,-1], so the 16 top
+            // samples are available exactly when the first 8 are
+            const bool top16 = top8;
+            // the staged samples themselves (-1 where not available: the
+            // filter looks at single samples of a partly available edge)
             if (lane < 25) {
+                int v;
                 if (lane == 0) {
-                    v = tile_nb(t, xO - 1, yO - 1, true);
+                    v = t.l[yO][xO];
                 } else if (lane < 9) {
-                    v = tile_nb(t, xO - 1, yO + lane - 1, true);
+                    v = t.l[yO + lane][xO];
                 } else {
                     const int i = lane - 9;
-                    v = tile_nb(t, xO + i, yO - 1, true);
-                    if (i > 7 && v < 0) v = tile_nb(t, xO + 7, yO - 1, true);
+                    v = t.l[yO][xO + 1 + ((i > 7 && !((trm >> (i - 8)) & 1u)) ? 7 : i)];
                 }
                 s.nb[lane] = v;
             }
-            // the left column and the 16 top samples are filtered only when
-            // available as a whole (an MBAFF left column can be partly
-            // available under constrained intra prediction)
-            const uint32_t nbm = __ballot_sync(0xffffffffu, v >= 0);
-            const bool left8 = ((nbm >> 1) & 0xFFu) == 0xFFu, top16 = ((nbm >> 9) & 0xFFFFu) == 0xFFFFu;
             __syncwarp();
             // 8.3.2.2.1 reference sample filtering, one sample per lane
             // (H264PictureBase.cpp:1540-1600)
-            int fsample = -1;
+            int f = -1;
             if (lane < 25) {
                 const int *q = s.nb;
-                int f = -1;
                 if (lane == 0) {
                     if (q[0] >= 0) {
                         if (q[9] < 0 || q[1] < 0)
@@ -886,43 +911,36 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
                     else f = (q[23] + 3 * q[24] + 2) >> 2;
                 }
                 s.nbf[lane] = f;
-                fsample = f;
             }
-            // availability of the 25 filtered samples (bit k: s.nbf[k])
-            const uint32_t fm = __ballot_sync(0xffffffffu, lane < 25 && fsample >= 0);
-            __syncwarp();
             const int mode = (m.ipred[0] >> (4 * b)) & 15;
-            const bool corner = fm & 1u, left = ((fm >> 1) & 0xFFu) == 0xFFu, top = ((fm >> 9) & 0xFFu) == 0xFFu;
-            const bool topr = ((fm >> 9) & 0xFFFFu) == 0xFFFFu;
+            // availability of the filtered samples: corner, left 8, top 8, top 16
+            const bool corner = cor, left = left8, top = top16, topr = top16;
             const bool ok = mode == 0 ? top : (mode == 1 || mode == 8) ? left : (mode == 3 || mode == 7) ? topr
                                                                                               : (top && left && corner);
             int dcv = 128;
             if (mode == 2) {
-                int st8 = 0, sl8 = 0;
-#pragma unroll
-                for (int q = 0; q < 8; q++) {
-                    st8 += top ? s.nbf[9 + q] : 0;
-                    sl8 += left ? s.nbf[1 + q] : 0;
-                }
+                const int st8 = __reduce_add_sync(0xffffffffu, (top && lane >= 9 && lane < 17) ? f : 0);
+                const int sl8 = __reduce_add_sync(0xffffffffu, (left && lane >= 1 && lane < 9) ? f : 0);
                 dcv = (top && left) ? (st8 + sl8 + 8) >> 4 : left ? (sl8 + 4) >> 3 : top ? (st8 + 4) >> 3 : 128;
             }
+            __syncwarp();
             for (int kk = lane; kk < 64; kk += 32) {
                 const int i = kk >> 3, j = kk & 7;
                 int pv = 0;  // a mode without its samples writes no prediction: the cleared buffer
                 if (mode == 2) {
                     pv = dcv;
                 } else if (mode <= 8 && ok) {
-                    const uint32_t e = __ldg(&kPred8[mode][kk]);
+                    const uint32_t e = s.pred8[mode][kk];
                     pv = ((int)((e >> 15) & 7u) * s.nbf[e & 31u] + (int)((e >> 18) & 7u) * s.nbf[(e >> 5) & 31u] +
                           (int)((e >> 21) & 7u) * s.nbf[(e >> 10) & 31u] + 2) >> 2;
                 }
-                t.l[yO + i + 1][xO + j + 1] = clip1(pv + s.res[(yO + i) * 16 + xO + j]);
+                t.l[yO + i + 1][xO + j + 1] = clip1(pv + res[(yO + i) * 16 + xO + j]);
             }
             __syncwarp();
         }
     } else {
         // Intra_16x16 (H264PictureBase.cpp:1847-2059)
-        const int *top = &t.l[0][1];
+        const int16_t *top = &t.l[0][1];
         const int mode = m.i16_mode;
         int a = 0, bb = 0, cc = 0, dcv = 128;
         if (mode == 2) {
@@ -949,7 +967,7 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
             else if (mode == 2) pv = dcv;
             else if (mode == 3) pv = (ta && la) ? clip1((a + bb * (j - 7) + cc * (i - 7) + 16) >> 5) : 0;
             else pv = 0;
-            t.l[1 + i][1 + j] = clip1(pv + s.res[kk]);
+            t.l[1 + i][1 + j] = clip1(pv + res[kk]);
         }
         __syncwarp();
     }
@@ -960,7 +978,7 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     const int cmode = m.chroma_mode;
     if (cmode == 0 && lane < 8) {
         const int pl = lane >> 2, xO = (lane & 1) * 4, yO = (lane & 2) * 2;
-        const int(*c)[9] = t.c[pl];  // c[0][0] corner, c[1+u][0] left, c[0][1+u] top
+        const int16_t(*c)[9] = t.c[pl];  // c[0][0] corner, c[1+u][0] left, c[0][1+u] top
         const bool t4 = c[0][1 + xO] > 0 && c[0][2 + xO] > 0 && c[0][3 + xO] > 0 && c[0][4 + xO] > 0;
         const bool l4 = c[1 + yO][0] > 0 && c[2 + yO][0] > 0 && c[3 + yO][0] > 0 && c[4 + yO][0] > 0;
         const int stp = t4 ? c[0][1 + xO] + c[0][2 + xO] + c[0][3 + xO] + c[0][4 + xO] : 0;
@@ -971,7 +989,7 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
         else pv = l4 ? (slf + 2) >> 2 : t4 ? (stp + 2) >> 2 : 128;
         s.cpar[lane] = pv;
     } else if (cmode == 3 && lane < 2 && cA && cB && cD) {
-        const int(*c)[9] = t.c[lane];
+        const int16_t(*c)[9] = t.c[lane];
         int H = 0, V = 0;
         for (int u = 0; u <= 3; u++) {
             H += (u + 1) * (c[0][5 + u] - (2 - u >= 0 ? c[0][3 - u] : c[0][0]));
@@ -984,22 +1002,28 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
     __syncwarp();
     for (int kk = lane; kk < 128; kk += 32) {
         const int pl = kk >> 6, i = (kk & 63) >> 3, j = kk & 7;
-        const int(*c)[9] = t.c[pl];
+        const int16_t(*c)[9] = t.c[pl];
         int pv = 0;
         if (cmode == 0) pv = s.cpar[4 * pl + (i >> 2) * 2 + (j >> 2)];
         else if (cmode == 1) pv = cA ? c[1 + i][0] : 0;
         else if (cmode == 2) pv = cB ? c[0][1 + j] : 0;
         else if (cmode == 3 && cA && cB && cD)
             pv = clip1((s.cpar[3 * pl] + s.cpar[3 * pl + 1] * (j - 3) + s.cpar[3 * pl + 2] * (i - 3) + 16) >> 5);
-        s.res[256 + kk] = clip1(pv + s.res[256 + kk]);  // reconstructed chroma, in place
+        res[256 + kk] = (int16_t)clip1(pv + res[256 + kk]);  // reconstructed chroma, in place
     }
     __syncwarp();
     // ---- store the MB: 16 luma rows of 16 bytes, 2 x 8 chroma rows of 8 bytes
     if (lane < 16) {
-        *(uint4 *)(Y + (size_t)(y + lane * dy) * W + x) = pack16(&t.l[1 + lane][1]);
+        const int16_t *q = &t.l[1 + lane][1];
+        uint32_t w[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < 16; k++) w[k >> 2] |= (uint32_t)(q[k] & 255) << (8 * (k & 3));
+        *(uint4 *)(Y + (size_t)(y + lane * dy) * W + x) = make_uint4(w[0], w[1], w[2], w[3]);
     } else {
         const int pl = (lane - 16) >> 3, r = (lane - 16) & 7;
-        *(uint2 *)(plane_c(p, pl) + (size_t)(chroma_row0(y) + r * dy) * Wc + x / 2) = pack8(&s.res[256 + pl * 64 + r * 8]);
+        const uint4 q = *reinterpret_cast<const uint4 *>(res + 256 + pl * 64 + r * 8);  // 8 samples as int16
+        *(uint2 *)(plane_c(p, pl) + (size_t)(chroma_row0(y) + r * dy) * Wc + x / 2) =
+            make_uint2(__byte_perm(q.x, q.y, 0x6420), __byte_perm(q.z, q.w, 0x6420));
     }
     __threadfence_block();
     __syncwarp();
@@ -1015,6 +1039,7 @@ __global__ void __launch_bounds__(32, 21) k_intra(const PicDesc *__restrict__ pi
     const int lane = threadIdx.x;
     if (lane == 0) s_row = atomicAdd(&st.ticket[0], 1u);
     for (int i = lane; i < 9 * 16; i += 32) (&s.pred4[0][0])[i] = (&kPred4[0][0])[i];
+    for (int i = lane; i < 9 * 64; i += 32) (&s.pred8[0][0])[i] = __ldg(&kPred8[0][0] + i);
     __syncwarp();
     const uint32_t g = s_row;
     if (g >= total_rows) return;
