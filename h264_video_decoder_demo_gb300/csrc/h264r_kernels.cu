@@ -817,7 +817,7 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
                 const bool corner = bx > 0 ? (by > 0 || ((topm >> (xO - 1)) & 1u)) : (by > 0 ? ((leftm >> (yO - 1)) & 1u) : cornerm);
                 // p[4..7, -1]: bit k available (else p[3, -1] stands in)
                 const uint32_t trm = by > 0 ? ((bx < 3 && b != 3 && b != 11) ? 15u : 0u) : ((topm >> (xO + 4)) & 15u);
-                const int mode = (m.ipred[b >> 3] >> (4 * (b & 7))) & 15;
+                const int mode = (((b >> 3) ? m.ipred[1] : m.ipred[0]) >> (4 * (b & 7))) & 15;
                 const uint32_t pos = ((uint32_t)bx << 2) | ((uint32_t)by << 4);
                 if (mode == 2) {
                     d = 2u | pos | ((uint32_t)top << 6) | ((uint32_t)left << 7);
