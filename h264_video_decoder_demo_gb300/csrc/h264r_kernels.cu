@@ -1129,23 +1129,49 @@ struct BlkMotion {
     int id[2];
 };
 
-__device__ __forceinline__ void get_motion(const PicDesc &p, int addr, int xq, int yq, BlkMotion &o)
+// motion of 4x4 block (bx, by) of a macroblock of type `type` whose motion
+// payload is at `aux`
+__device__ __forceinline__ void block_motion(const PicDesc &p, int type, uint32_t aux, int bx, int by, BlkMotion &o)
 {
-    const h264r_mb &m = p.mbs[addr];
     o.mv[0][0] = o.mv[0][1] = o.mv[1][0] = o.mv[1][1] = 0;
     o.pf[0] = o.pf[1] = 0;
     o.id[0] = o.id[1] = -1;
-    if (m.type != H264R_MB_INTER || m.aux == H264R_NONE || (m.aux & 3) || (uint64_t)m.aux + 4 > p.motion_bytes) return;
-    uint32_t hdr = *(const uint32_t *)(p.motion + m.aux);
-    int e = part_of_block(hdr & 0xFFFF, xq >> 2, yq >> 2);
-    if (e >= (int)(hdr >> 16) || (uint64_t)m.aux + 4 + 16ull * (e + 1) > p.motion_bytes) return;
-    const h264r_part pp = ((const h264r_part *)(p.motion + m.aux + 4))[e];
+    if (type != H264R_MB_INTER || aux == H264R_NONE || (aux & 3) || (uint64_t)aux + 4 > p.motion_bytes) return;
+    uint32_t hdr = *(const uint32_t *)(p.motion + aux);
+    int e = part_of_block(hdr & 0xFFFF, bx, by);
+    if (e >= (int)(hdr >> 16) || (uint64_t)aux + 4 + 16ull * (e + 1) > p.motion_bytes) return;
+    const h264r_part pp = ((const h264r_part *)(p.motion + aux + 4))[e];
     for (int l = 0; l < 2; l++) {
         o.mv[l][0] = pp.mv[l][0];
         o.mv[l][1] = pp.mv[l][1];
         o.pf[l] = pp.ref[l] >= 0;
         o.id[l] = pp.dref[l];
     }
+}
+
+// The motion rules of 8.7.2.1 for two blocks of inter MBs: 1 when the
+// references or the motion vectors differ (vertical limit lim), else 0
+// (H264PictureDeblockingFilterProcess.cpp:1230-1310)
+__device__ __forceinline__ int bs_motion(const BlkMotion &a, const BlkMotion &b, int lim)
+{
+#define DIFF(u, v) (abs((u)[0] - (v)[0]) >= 4 || abs((u)[1] - (v)[1]) >= lim)
+    int r0p = a.id[0], r1p = a.id[1], r0q = b.id[0], r1q = b.id[1];
+    int np = a.pf[0] + a.pf[1], nq = b.pf[0] + b.pf[1];
+    if (!(((r0p == r0q && r1p == r1q) || (r0p == r1q && r1p == r0q)) && np == nq)) return 1;
+    if (a.pf[0] && !a.pf[1] && b.pf[0] && !b.pf[1] && DIFF(a.mv[0], b.mv[0])) return 1;
+    if (a.pf[0] && !a.pf[1] && !b.pf[0] && b.pf[1] && DIFF(a.mv[0], b.mv[1])) return 1;
+    if (!a.pf[0] && a.pf[1] && b.pf[0] && !b.pf[1] && DIFF(a.mv[1], b.mv[0])) return 1;
+    if (!a.pf[0] && a.pf[1] && !b.pf[0] && b.pf[1] && DIFF(a.mv[1], b.mv[1])) return 1;
+    if (a.pf[0] && a.pf[1] && r0p != r1p && b.pf[0] && b.pf[1] && ((r0q == r0p && r1q == r1p) || (r0q == r1p && r1q == r0p))) {
+        if (r0q == r0p && (DIFF(a.mv[0], b.mv[0]) || DIFF(a.mv[1], b.mv[1]))) return 1;
+        else if (r0q == r1p && (DIFF(a.mv[1], b.mv[0]) || DIFF(a.mv[0], b.mv[1]))) return 1;
+    }
+    // quirk: parsed as (A || B) && C || D (1289-1298)
+    if (a.pf[0] && a.pf[1] && r0p == r1p && b.pf[0] && b.pf[1] && r0q == r1q && r0q == r0p) {
+        if (((DIFF(a.mv[0], b.mv[0]) || DIFF(a.mv[1], b.mv[1])) && DIFF(a.mv[0], b.mv[1])) || DIFF(a.mv[1], b.mv[0])) return 1;
+    }
+#undef DIFF
+    return 0;
 }
 
 // 8.7.2.1 (Derivation_process_for_the_luma_content_dependent_boundary_
@@ -1180,26 +1206,9 @@ __device__ int derive_bs(const PicDesc &p, int mbP, int mbQ, int xp, int yp, int
     if (mixed) return 1;
     const int lim = fQ ? 2 : 4;
     BlkMotion a, b;
-    get_motion(p, mbP, xp, yp, a);
-    get_motion(p, mbQ, xq, yq, b);
-#define DIFF(u, v) (abs((u)[0] - (v)[0]) >= 4 || abs((u)[1] - (v)[1]) >= lim)
-    int r0p = a.id[0], r1p = a.id[1], r0q = b.id[0], r1q = b.id[1];
-    int np = a.pf[0] + a.pf[1], nq = b.pf[0] + b.pf[1];
-    if (!(((r0p == r0q && r1p == r1q) || (r0p == r1q && r1p == r0q)) && np == nq)) return 1;
-    if (a.pf[0] && !a.pf[1] && b.pf[0] && !b.pf[1] && DIFF(a.mv[0], b.mv[0])) return 1;
-    if (a.pf[0] && !a.pf[1] && !b.pf[0] && b.pf[1] && DIFF(a.mv[0], b.mv[1])) return 1;
-    if (!a.pf[0] && a.pf[1] && b.pf[0] && !b.pf[1] && DIFF(a.mv[1], b.mv[0])) return 1;
-    if (!a.pf[0] && a.pf[1] && !b.pf[0] && b.pf[1] && DIFF(a.mv[1], b.mv[1])) return 1;
-    if (a.pf[0] && a.pf[1] && r0p != r1p && b.pf[0] && b.pf[1] && ((r0q == r0p && r1q == r1p) || (r0q == r1p && r1q == r0p))) {
-        if (r0q == r0p && (DIFF(a.mv[0], b.mv[0]) || DIFF(a.mv[1], b.mv[1]))) return 1;
-        else if (r0q == r1p && (DIFF(a.mv[1], b.mv[0]) || DIFF(a.mv[0], b.mv[1]))) return 1;
-    }
-    // quirk: parsed as (A || B) && C || D (1289-1298)
-    if (a.pf[0] && a.pf[1] && r0p == r1p && b.pf[0] && b.pf[1] && r0q == r1q && r0q == r0p) {
-        if (((DIFF(a.mv[0], b.mv[0]) || DIFF(a.mv[1], b.mv[1])) && DIFF(a.mv[0], b.mv[1])) || DIFF(a.mv[1], b.mv[0])) return 1;
-    }
-#undef DIFF
-    return 0;
+    block_motion(p, P.type, P.aux, xp >> 2, yp >> 2, a);
+    block_motion(p, Q.type, Q.aux, xq >> 2, yq >> 2, b);
+    return bs_motion(a, b, lim);
 }
 
 // Per-MB filter controls of Deblocking_filter_process (76-160)
@@ -1301,10 +1310,66 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
         // direction dir for lines 4b..4b+3, and the 4:2:0 chroma strengths
         // are the luma ones of the same edge at line 2k (the reference
         // derives them from the luma positions, 994-1310).
+        // The records of the MB and of its left and top neighbours are read
+        // once, and the motion of every block an edge touches once, by one
+        // lane each (0-15 the MB's blocks in raster order, 16-19 column 3
+        // of the left MB, 20-23 row 3 of the MB above); an edge lane takes
+        // its two blocks by shuffles.  The rules are derive_bs's for a frame
+        // picture (no field MBs).
         const int dir = lane >> 4, e = (lane >> 2) & 3, b = lane & 3;
         const bool on = e == 0 ? (dir ? c.top : c.left) : (c.internal && (e == 2 || !c.t8));
+        const h264r_mb Q = p.mbs[cur];
+        const h264r_mb A = c.mbA >= 0 ? p.mbs[c.mbA] : Q, B = c.mbB >= 0 ? p.mbs[c.mbB] : Q;
+        uint32_t mv0, mv1, rf;  // this lane's block: list 0 / 1 vectors (x | y << 16), refs and flags
+        {
+            const int src = lane < 16 ? 0 : (lane < 20 ? 1 : 2);
+            const int bx = lane < 16 ? (lane & 3) : (lane < 20 ? 3 : (lane < 24 ? lane - 20 : 0));
+            const int by = lane < 16 ? (lane >> 2) : (lane < 20 ? lane - 16 : 3);
+            BlkMotion bm;
+            block_motion(p, src == 0 ? Q.type : (src == 1 ? A.type : B.type), src == 0 ? Q.aux : (src == 1 ? A.aux : B.aux), bx, by, bm);
+            mv0 = ((uint32_t)bm.mv[0][0] & 0xFFFFu) | ((uint32_t)bm.mv[0][1] << 16);
+            mv1 = ((uint32_t)bm.mv[1][0] & 0xFFFFu) | ((uint32_t)bm.mv[1][1] << 16);
+            rf = ((uint32_t)bm.id[0] & 0xFFu) | (((uint32_t)bm.id[1] & 0xFFu) << 8) | ((uint32_t)bm.pf[0] << 16) | ((uint32_t)bm.pf[1] << 17);
+        }
+        const int qsrc = dir == 0 ? b * 4 + e : e * 4 + b;
+        const int psrc = e > 0 ? (dir == 0 ? b * 4 + e - 1 : (e - 1) * 4 + b) : (dir == 0 ? 16 + b : 20 + b);
+        auto unpack = [](uint32_t v0, uint32_t v1, uint32_t r, BlkMotion &o) {
+            o.mv[0][0] = (int16_t)(v0 & 0xFFFFu);
+            o.mv[0][1] = (int16_t)(v0 >> 16);
+            o.mv[1][0] = (int16_t)(v1 & 0xFFFFu);
+            o.mv[1][1] = (int16_t)(v1 >> 16);
+            o.id[0] = (int8_t)(r & 0xFFu);
+            o.id[1] = (int8_t)((r >> 8) & 0xFFu);
+            o.pf[0] = (r >> 16) & 1u;
+            o.pf[1] = (r >> 17) & 1u;
+        };
+        BlkMotion mp, mq;
+        unpack(__shfl_sync(0xffffffffu, mv0, psrc), __shfl_sync(0xffffffffu, mv1, psrc), __shfl_sync(0xffffffffu, rf, psrc), mp);
+        unpack(__shfl_sync(0xffffffffu, mv0, qsrc), __shfl_sync(0xffffffffu, mv1, qsrc), __shfl_sync(0xffffffffu, rf, qsrc), mq);
+        auto sp_of = [&](const h264r_mb &m) -> bool {
+            const int t = p.slices[min((uint32_t)m.slice, p.num_slices - 1)].slice_type;
+            return t == 3 || t == 4;
+        };
         int bs = 0;
-        if (on) bs = dir == 0 ? edge_bs(p, cur, 0, 1, 4 * e, c.mbA, 0, 4 * b) : edge_bs(p, cur, 0, 0, 4 * e, c.mbB, 0, 4 * b);
+        if (on) {
+            const bool mbedge = e == 0;
+            const int ptype = mbedge ? (dir == 0 ? A.type : B.type) : Q.type;
+            const bool spP = mbedge ? (dir == 0 ? sp_of(A) : sp_of(B)) : sp_of(Q), spQ = sp_of(Q);
+            if (is_intra_type(ptype) || is_intra_type(Q.type) || spP || spQ) {
+                bs = mbedge ? 4 : 3;
+            } else {
+                const int qx = dir == 0 ? e : b, qy = dir == 0 ? b : e;
+                const int px = dir == 0 ? (e > 0 ? e - 1 : 3) : b, py = dir == 0 ? b : (e > 0 ? e - 1 : 3);
+                const int pflags = mbedge ? (dir == 0 ? A.flags : B.flags) : Q.flags;
+                const int pnz4 = mbedge ? (dir == 0 ? A.nz4x4 : B.nz4x4) : Q.nz4x4, pnz8 = mbedge ? (dir == 0 ? A.nz8x8 : B.nz8x8) : Q.nz8x8;
+                auto blk4 = [](int x4, int y4) { return 8 * (y4 >> 1) + 4 * (x4 >> 1) + 2 * (y4 & 1) + (x4 & 1); };
+                const int nzP = (pflags & H264R_MBF_T8x8) ? ((pnz8 >> (2 * (py >> 1) + (px >> 1))) & 1) : ((pnz4 >> blk4(px, py)) & 1);
+                const int nzQ = (Q.flags & H264R_MBF_T8x8) ? ((Q.nz8x8 >> (2 * (qy >> 1) + (qx >> 1))) & 1) : ((Q.nz4x4 >> blk4(qx, qy)) & 1);
+                if (nzP || nzQ) bs = 2;
+                else if (ptype == H264R_MB_NONE || Q.type == H264R_MB_NONE) bs = 0xFF;
+                else bs = bs_motion(mp, mq, 4);
+            }
+        }
         if (bs == 0xFF) mystop = stop_key(cur, dir == 0 ? SEQ_LV0 + e : (e == 0 ? SEQ_LH0 : SEQ_LH4 + e - 1), 4 * b);
         const int k = lane & 15;
         uint32_t vrow = 0, hrow = 0;
