@@ -1352,7 +1352,10 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
         };
         int bs = 0;
         if (on) {
-            const bool mbedge = e == 0;
+            // an MB edge whose neighbour is not available (another slice
+            // under disable_deblocking_filter_idc 0) takes the MB itself as
+            // its p side, as derive_bs does: no bS 4 there
+            const bool mbedge = e == 0 && (dir == 0 ? c.mbA >= 0 : c.mbB >= 0);
             const int ptype = mbedge ? (dir == 0 ? A.type : B.type) : Q.type;
             const bool spP = mbedge ? (dir == 0 ? sp_of(A) : sp_of(B)) : sp_of(Q), spQ = sp_of(Q);
             if (is_intra_type(ptype) || is_intra_type(Q.type) || spP || spQ) {

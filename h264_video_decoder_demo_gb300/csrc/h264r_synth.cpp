@@ -229,6 +229,27 @@ static void make_picture(h264r_synth *g, const Plan &pl)
     s.disable_deblocking_filter_idc = 0;
     s.slice_type = pl.type == PIC_I ? 2 : (pl.type == PIC_P ? 0 : 1);
     g->slices.push_back(s);
+    // further slices every slice_rows MB rows (MB-pair rows for MBAFF), and
+    // constrained intra prediction; the extra draws happen only when asked
+    // for, so streams without them are unchanged
+    const int unit_rows = c.mbaff ? H / 2 : H;
+    if (c.slice_rows > 0) {
+        const int nslices = (unit_rows + c.slice_rows - 1) / c.slice_rows;
+        for (int k = 0; k < nslices; k++) {
+            h264r_slice t = s;
+            if (k > 0) {
+                t.chroma_qp_offset[0] = (int8_t)r.range(-2, 2);
+                t.chroma_qp_offset[1] = (int8_t)r.range(-2, 2);
+                t.filter_offset_a = (int8_t)(2 * r.range(-c.filter_offset_max, c.filter_offset_max));
+                t.filter_offset_b = (int8_t)(2 * r.range(-c.filter_offset_max, c.filter_offset_max));
+            }
+            const int roll = r.range(0, 99);
+            t.disable_deblocking_filter_idc = (uint8_t)(roll < 50 ? 0 : (roll < 85 ? 2 : 1));
+            if (k == 0) g->slices[0] = t;
+            else g->slices.push_back(t);
+        }
+    }
+    const bool cip = c.cip_percent > 0 && pl.type != PIC_I && r.pct(c.cip_percent);
 
     const bool explicit_p = c.weighted != H264R_SYNTH_WP_NONE && pl.type == PIC_P;
     const bool explicit_b = c.weighted == H264R_SYNTH_WP_EXPLICIT && pl.type == PIC_B;
@@ -292,7 +313,8 @@ static void make_picture(h264r_synth *g, const Plan &pl)
         const bool field = mbaff && pair_field;
         if (field) m.flags |= H264R_MBF_FIELD;
         m.qpy = (uint8_t)r.range(c.qp_min, c.qp_max);
-        m.slice = 0;
+        m.slice = (uint16_t)(c.slice_rows > 0 ? (mbaff ? (a / 2) / W : a / W) / c.slice_rows : 0);
+        if (cip) m.flags |= H264R_MBF_CIP;
         bool intra = pl.type == PIC_I || r.pct(c.intra_percent);
         CoefBuilder cb;
         const int dens = c.coef_density;
@@ -304,7 +326,14 @@ static void make_picture(h264r_synth *g, const Plan &pl)
             else m.type = H264R_MB_I16x16;
             // MBAFF neighbourhoods depend on the pairs around: DC modes only,
             // which need no neighbour
-            bool A = !mbaff && mx > 0, B = !mbaff && my > 0, D = !mbaff && mx > 0 && my > 0;
+            // neighbours usable for intra prediction: same slice, and not an
+            // inter MB under constrained intra prediction
+            auto usable = [&](int nb) {
+                const h264r_mb &q = g->mbs[nb];
+                return q.slice == m.slice && !(cip && q.type == H264R_MB_INTER);
+            };
+            bool A = !mbaff && mx > 0 && usable(a - 1), B = !mbaff && my > 0 && usable(a - W);
+            bool D = !mbaff && mx > 0 && my > 0 && usable(a - W - 1);
             if (m.type == H264R_MB_IPCM) {
                 m.aux = (uint32_t)(g->pcm.size() / 384);
                 for (int i = 0; i < 384; i++) g->pcm.push_back((uint8_t)r.range(0, 255));

@@ -43,6 +43,12 @@ typedef struct h264r_synth_cfg {
     uint8_t  coef_density;      /* 0..100: share of coded 4x4 blocks        */
     uint8_t  mbaff;             /* 1: MBAFF frames (frame/field MB pairs)     */
     uint8_t  field_percent;     /* MBAFF: MB pairs coded as field MBs         */
+    uint8_t  slice_rows;        /* 0: one slice per picture; N: a new slice
+                                   every N MB rows (MB-pair rows for MBAFF),
+                                   each with its own QP offsets, filter
+                                   offsets and deblocking mode (0, 1 or 2)    */
+    uint8_t  cip_percent;       /* P/B pictures coded with
+                                   constrained_intra_pred_flag               */
 } h264r_synth_cfg;
 
 typedef struct h264r_synth h264r_synth;

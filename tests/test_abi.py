@@ -118,3 +118,17 @@ def test_synth_records_validate(engine_lib, name):
     if name == "1080p_high":
         assert any((p.weights["weighted"] != 0).any() for p in pics)
         assert any((p.mbs["flags"] & 1).any() for p in pics)
+
+
+def test_synth_slice_and_cip_options_leave_default_streams_unchanged():
+    """The generator draws for slices and constrained intra prediction only
+    when asked, so existing seeds keep their streams."""
+    import numpy as np
+    import h264_video_decoder_demo_gb300 as h
+    a = list(h.synth("1080p_high", seed=5, width_mbs=20, height_mbs=12, num_pictures=4))
+    b = list(h.synth("1080p_high", seed=5, width_mbs=20, height_mbs=12, num_pictures=4, slice_rows=0, cip_percent=0))
+    assert all(np.array_equal(x.mbs, y.mbs) and np.array_equal(x.coef, y.coef) and np.array_equal(x.motion, y.motion)
+               for x, y in zip(a, b))
+    c = list(h.synth("1080p_high", seed=5, width_mbs=20, height_mbs=12, num_pictures=4, slice_rows=3, cip_percent=100))
+    assert all(len(p.slices) == 4 for p in c)
+    assert all(set(np.unique(p.mbs["slice"]).tolist()) == {0, 1, 2, 3} for p in c)

@@ -86,3 +86,22 @@ def test_batch_argument_checks(gpu_ctx):
     # a stream wider than the engine's limit is refused at open
     with pytest.raises(h.EngineError):
         h.Stream(gpu_ctx, 513, 4, 4)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("slice_rows,cip", [(1, 0), (3, 0), (2, 100), (0, 100)])
+def test_slices_and_constrained_intra_match_oracle(gpu_ctx, slice_rows, cip):
+    """Several slices per picture (their own QP and filter offsets, deblocking
+    modes 0, 1 and 2) and constrained intra prediction: intra neighbour
+    availability and the deblocking edges at slice boundaries."""
+    g = h.synth("1080p_high", seed=800 + 7 * slice_rows + cip, width_mbs=20, height_mbs=12, num_pictures=8,
+                gop_length=8, gop_kind=1, num_refs=2, intra_percent=40, filter_offset_max=6,
+                slice_rows=slice_rows, cip_percent=cip)
+    assert run_against_oracle(gpu_ctx, g) == 8
+
+
+@pytest.mark.gpu
+def test_mbaff_slices_and_constrained_intra_match_oracle(gpu_ctx):
+    g = h.synth("1080i_mbaff", seed=900, width_mbs=12, height_mbs=8, num_pictures=5, gop_length=5, num_refs=2,
+                field_percent=50, intra_percent=30, slice_rows=2, cip_percent=100)
+    assert run_against_oracle(gpu_ctx, g) == 5
