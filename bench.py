@@ -174,7 +174,7 @@ def peak_hbm():
 # to a launch by the MBs it processes.  The boundary strengths (k_bs) run on
 # a side stream beside k_inter and k_intra, so the deblocking stage timed
 # after k_intra is the deblocking kernel alone.
-DRAM_BYTES_PER_MB = {"k_inter": 1089, "k_intra": 303, "k_deblock_frame": 678}
+DRAM_BYTES_PER_MB = {"k_inter": 494, "k_intra": 418, "k_deblock_frame": 669}
 
 
 def dist_setup(args):
