@@ -1063,12 +1063,23 @@ __global__ void __launch_bounds__(32, 21) k_intra(const PicDesc *__restrict__ pi
             }
         }
         uint32_t todo = __ballot_sync(0xffffffffu, mine);
+        // Frame pictures: an intra MB whose neighbours above (top-left, top,
+        // top-right) are all inter MBs, final since k_inter, need not wait for
+        // the row above; only intra neighbours are still being written.  Bit
+        // c - (u0 - 1) of `up`: MB (row - 1, c) is intra.
+        uint64_t up = ~0ull;
+        if (!p.mbaff && row > 0 && todo) {
+            const int c0 = u0 - 1 + lane, c1 = u0 + 31 + lane;
+            const bool a0 = c0 >= 0 && c0 < uw && is_intra_type(p.mbs[(row - 1) * uw + c0].type);
+            const bool a1 = lane < 2 && c1 < uw && is_intra_type(p.mbs[(row - 1) * uw + c1].type);
+            up = (uint64_t)__ballot_sync(0xffffffffu, a0) | ((uint64_t)(__ballot_sync(0xffffffffu, a1) & 3u) << 32);
+        }
         while (todo) {
             const int u = u0 + __ffs(todo) - 1;
             todo &= todo - 1;
             if (lane == 0 && posted < u) st_release(prog + row, u);
             posted = u;
-            if (row > 0 && !db_wait(st, prog + row - 1, min(u + 2, uw), seen)) return;
+            if (row > 0 && ((up >> (u - u0)) & 7u) && !db_wait(st, prog + row - 1, min(u + 2, uw), seen)) return;
             if (p.mbaff) {
                 // the pair's intra MBs; the copy of the next intra MB (the
                 // pair's second, else the next pair's first of this group)
