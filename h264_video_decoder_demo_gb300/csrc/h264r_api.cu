@@ -163,6 +163,12 @@ struct h264r_stream {
     uint8_t *dpb = nullptr;
     cudaStream_t cs = nullptr;
     cudaStream_t side = nullptr;  // boundary strengths of launches on cs, beside inter and intra
+    // h264r_output_async: copies to the host on their own stream; a launch
+    // that writes a slot waits for the slot's pending copy
+    cudaStream_t out = nullptr;
+    cudaEvent_t out_ready = nullptr;
+    std::vector<cudaEvent_t> slot_ev;
+    std::unique_ptr<std::atomic<uint8_t>[]> slot_pending;
     LaunchBuf ring[kRing];
     int next = 0;
     uint8_t *bgr = nullptr;  // device staging of h264r_output_bgr24
@@ -365,6 +371,12 @@ extern "C" int h264r_stream_open(h264r_ctx *ctx, const h264r_stream_cfg *cfg, h2
     cudaMemset(s->dpb, 0, bytes);
     cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking);
     cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
+    cudaStreamCreateWithFlags(&s->out, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&s->out_ready, cudaEventDisableTiming);
+    s->slot_ev.resize(cfg->dpb_slots);
+    for (auto &e : s->slot_ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    s->slot_pending.reset(new std::atomic<uint8_t>[cfg->dpb_slots]);
+    for (int i = 0; i < cfg->dpb_slots; i++) s->slot_pending[i] = 0;
     for (auto &b : s->ring) create_events(b);
     cudaDeviceSynchronize();
     ctx->used += bytes;
@@ -381,8 +393,12 @@ extern "C" int h264r_stream_close(h264r_stream *s)
     for (auto &b : s->ring) free_buf(b);
     if (s->bgr) cudaFree(s->bgr);
     cudaStreamSynchronize(s->side);
+    cudaStreamSynchronize(s->out);
+    for (auto e : s->slot_ev) cudaEventDestroy(e);
+    cudaEventDestroy(s->out_ready);
     cudaStreamDestroy(s->cs);
     cudaStreamDestroy(s->side);
+    cudaStreamDestroy(s->out);
     cudaFree(s->dpb);
     {
         std::lock_guard<std::mutex> lk(ctx->mu);
@@ -537,6 +553,13 @@ struct BatchItem {
 };
 
 // Build the PicDesc array + counters in b.host, upload, run the kernels.
+// a slot about to be written: wait (on cs) for its pending copy to the host
+static void wait_slot_copy(h264r_stream *s, int slot, cudaStream_t cs)
+{
+    if (slot >= 0 && slot < s->cfg.dpb_slots && s->slot_pending[slot].exchange(0))
+        cudaStreamWaitEvent(cs, s->slot_ev[slot], 0);
+}
+
 static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vector<BatchItem> &items, bool any_intra)
 {
     const int n = (int)items.size();
@@ -561,6 +584,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
         if (rc) return rc;
     }
     memset(b.host, 0, total);
+    for (auto &it : items) wait_slot_copy(it.s, it.pic->dst_slot, cs);
     PicDesc *d = (PicDesc *)b.host;
     uint64_t mb_base = 0, row_base = 0, prog = 0, db_base = 0, dbf_base = 0;
     for (int i = 0; i < n; i++) {
@@ -843,6 +867,24 @@ extern "C" int h264r_output(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, 
     return H264R_OK;
 }
 
+extern "C" int h264r_output_async(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *cr)
+{
+    if (!s || slot < 0 || slot >= s->cfg.dpb_slots || !y || !cb || !cr) return H264R_ERR_INVALID_ARG;
+    h264r_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    const uint64_t W = s->cfg.width_mbs * 16ull, H = s->cfg.height_mbs * 16ull;
+    const uint8_t *base = s->dpb + (uint64_t)slot * s->slot_bytes;
+    // after everything enqueued on the stream so far (the picture's batch)
+    CUDA_OR(ctx, cudaEventRecord(s->out_ready, s->cs));
+    CUDA_OR(ctx, cudaStreamWaitEvent(s->out, s->out_ready, 0));
+    CUDA_OR(ctx, cudaMemcpyAsync(y, base, W * H, cudaMemcpyDeviceToHost, s->out));
+    CUDA_OR(ctx, cudaMemcpyAsync(cb, base + W * H, W * H / 4, cudaMemcpyDeviceToHost, s->out));
+    CUDA_OR(ctx, cudaMemcpyAsync(cr, base + W * H + W * H / 4, W * H / 4, cudaMemcpyDeviceToHost, s->out));
+    CUDA_OR(ctx, cudaEventRecord(s->slot_ev[slot], s->out));
+    s->slot_pending[slot] = 1;
+    return H264R_OK;
+}
+
 extern "C" int h264r_output_bgr24_device(h264r_stream *s, int slot, void *dst, uint32_t row_bytes, int flip)
 {
     if (!s || slot < 0 || slot >= s->cfg.dpb_slots || !dst || ((uintptr_t)dst & 3)) return H264R_ERR_INVALID_ARG;
@@ -916,6 +958,7 @@ extern "C" int h264r_load_slot(h264r_stream *s, int slot, const uint8_t *y, cons
     cudaSetDevice(ctx->device);
     const uint64_t W = s->cfg.width_mbs * 16ull, H = s->cfg.height_mbs * 16ull;
     uint8_t *base = s->dpb + (uint64_t)slot * s->slot_bytes;
+    wait_slot_copy(s, slot, s->cs);
     CUDA_OR(ctx, cudaMemcpyAsync(base, y, W * H, cudaMemcpyHostToDevice, s->cs));
     CUDA_OR(ctx, cudaMemcpyAsync(base + W * H, cb, W * H / 4, cudaMemcpyHostToDevice, s->cs));
     CUDA_OR(ctx, cudaMemcpyAsync(base + W * H + W * H / 4, cr, W * H / 4, cudaMemcpyHostToDevice, s->cs));
@@ -943,6 +986,7 @@ extern "C" int h264r_stream_sync(h264r_stream *s)
     if (!s) return H264R_ERR_INVALID_ARG;
     cudaSetDevice(s->ctx->device);
     CUDA_OR(s->ctx, cudaStreamSynchronize(s->cs));
+    CUDA_OR(s->ctx, cudaStreamSynchronize(s->out));
     return check_device_error(s->ctx, s->cs);
 }
 

@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libh264r.so
 EXPORTS = [
     "h264r_ctx_create", "h264r_ctx_destroy", "h264r_last_error", "h264r_stream_open",
     "h264r_stream_close", "h264r_stream_dpb_bytes", "h264r_submit_picture",
-    "h264r_submit_picture_device", "h264r_submit_batch_device", "h264r_output",
+    "h264r_submit_picture_device", "h264r_submit_batch_device", "h264r_output", "h264r_output_async",
     "h264r_load_slot", "h264r_slot_device_ptr", "h264r_stream_sync", "h264r_ctx_sync",
     "h264r_stream_cuda_stream", "h264r_validate_picture", "h264r_ctx_kernel_launches",
     "h264r_ctx_set_timing", "h264r_ctx_last_timing",
@@ -78,6 +78,7 @@ def _load():
         "h264r_submit_picture_device": (i32, [vp, P(R.CPicture)]),
         "h264r_submit_batch_device": (i32, [vp, i32, P(vp), P(R.CPicture)]),
         "h264r_output": (i32, [vp, i32, vp, vp, vp]),
+        "h264r_output_async": (i32, [vp, i32, vp, vp, vp]),
         "h264r_load_slot": (i32, [vp, i32, vp, vp, vp]),
         "h264r_slot_device_ptr": (i32, [vp, i32, P(vp)]),
         "h264r_stream_sync": (i32, [vp]),
@@ -281,9 +282,12 @@ class Stream:
         return out
 
     def output_async(self, slot, out):
+        """Copy a slot into `out` (numpy uint8, pinned for overlap) on the
+        stream's copy stream (h264r_output_async); sync before reading."""
         W, H = self.width_mbs * 16, self.height_mbs * 16
         base = out.ctypes.data
-        return self.ctx.check(lib().h264r_output(self.h, slot, base, base + W * H, base + W * H + W * H // 4), "output")
+        return self.ctx.check(lib().h264r_output_async(self.h, slot, base, base + W * H, base + W * H + W * H // 4),
+                              "output_async")
 
     def output_bgr24(self, slot, flip=False):
         """The picture in a slot as BGR24 rows (height x row_bytes, numpy)."""

@@ -295,6 +295,14 @@ int  h264r_picture_bytes(const h264r_picture *pic, uint64_t out[4]);
  */
 int  h264r_output(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *cr);
 /*
+ * As h264r_output, on the stream's own copy stream: the copy starts when the
+ * work enqueued on the stream so far is done and overlaps the stream's later
+ * launches; a later launch (or h264r_load_slot) that writes the same slot
+ * waits for the copy.  Host planes should be pinned for the copy to be
+ * asynchronous; call h264r_stream_sync before reading them.
+ */
+int  h264r_output_async(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *cr);
+/*
  * Decoded picture (DPB slot) as BGR24 rows of row_bytes bytes (at least
  * 3*width, a multiple of 4, like the reference's bitmap rows), top-down, or
  * bottom-up when flip != 0: the reference's conversion for its BMP output

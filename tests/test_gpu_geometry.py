@@ -105,3 +105,36 @@ def test_mbaff_slices_and_constrained_intra_match_oracle(gpu_ctx):
     g = h.synth("1080i_mbaff", seed=900, width_mbs=12, height_mbs=8, num_pictures=5, gop_length=5, num_refs=2,
                 field_percent=50, intra_percent=30, slice_rows=2, cip_percent=100)
     assert run_against_oracle(gpu_ctx, g) == 5
+
+
+@pytest.mark.gpu
+def test_output_async_copies_survive_slot_reuse(gpu_ctx):
+    """h264r_output_async copies on the stream's copy stream while the stream
+    goes on reconstructing; a later picture that reuses a slot waits for the
+    slot's copy.  Twelve pictures submitted back to back, each copied out
+    right after its submission, one sync at the end: every copy equals the
+    oracle's picture."""
+    import torch
+    from oracle_cpu import OracleDPB
+    w, hh = 20, 12
+    g = h.synth("1080p_high", seed=950, width_mbs=w, height_mbs=hh, num_pictures=12, gop_length=12, gop_kind=1,
+                num_refs=2, intra_percent=20)
+    pics = list(g)
+    slots = g.dpb_slots
+    s = h.Stream(gpu_ctx, w, hh, slots)
+    d = OracleDPB(w, hh, slots)
+    n = w * 16 * hh * 16 * 3 // 2
+    outs = [torch.empty(n, dtype=torch.uint8, pin_memory=True).numpy() for _ in pics]
+    expected = []
+    try:
+        for k, p in enumerate(pics):
+            s.submit(p)
+            s.output_async(p.dst_slot, outs[k])
+            rc, _ = d.reconstruct(p)
+            assert rc == 0
+            expected.append(d.planes(p.dst_slot).copy())
+        s.sync()
+        for k in range(len(pics)):
+            assert np.array_equal(outs[k], expected[k]), k
+    finally:
+        s.close()
