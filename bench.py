@@ -169,9 +169,10 @@ def peak_hbm():
         return 6800.0, "fallback"
 
 
-# DRAM bytes (read + write) per MB of each timed kernel, measured with ncu on
-# the 1080p High mix (profiles/dram_traffic_1080p_high_8streams.md); scaled
-# to a launch by the MBs it processes.  The boundary strengths (k_bs) run on
+# DRAM bytes (read + write) per MB of each timed kernel, measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) over 40 launches of 8 streams
+# of the 1080p High mix, 6 pictures each; scaled to a launch by the MBs it
+# processes.  The boundary strengths (k_bs) run on
 # a side stream beside k_inter and k_intra, so the deblocking stage timed
 # after k_intra is the deblocking kernel alone.
 DRAM_BYTES_PER_MB = {"k_inter": 494, "k_intra": 418, "k_deblock_frame": 669}

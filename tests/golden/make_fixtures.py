@@ -161,7 +161,7 @@ def main():
     dumper = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
     if not os.path.exists(dumper):
         subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"])
-    with tempfile.TemporaryDirectory(dir=os.path.join(ROOT, "_work") if os.path.isdir(os.path.join(ROOT, "_work")) else None) as tmp:
+    with tempfile.TemporaryDirectory() as tmp:
         for name, stream, n, tools in ([] if args.bitstreams_only else FIXTURES):
             dmp = os.path.join(tmp, name + ".dmp")
             bmp_dir = os.path.join(tmp, name + "_bmp")
