@@ -409,6 +409,7 @@ extern "C" int h264r_stream_close(h264r_stream *s)
 }
 
 extern "C" void *h264r_stream_cuda_stream(h264r_stream *s) { return s ? (void *)s->cs : nullptr; }
+extern "C" void *h264r_stream_output_cuda_stream(h264r_stream *s) { return s ? (void *)s->out : nullptr; }
 
 extern "C" void *h264r_ctx_cuda_stream(h264r_ctx *ctx) { return ctx ? (void *)ctx->batch_stream : nullptr; }
 

@@ -330,8 +330,10 @@ bool launch(h264r_server *srv)
         }
         cudaStream_t cs = (cudaStream_t)h264r_stream_cuda_stream(S->s);
         if (it->out) {
+            // the copy runs on the stream's copy stream, beside its next batches
             const uint64_t W = S->cfg.width_mbs * 16ull, H = S->cfg.height_mbs * 16ull;
-            h264r_output(S->s, it->pic.dst_slot, it->out, it->out + W * H, it->out + W * H + W * H / 4);
+            h264r_output_async(S->s, it->pic.dst_slot, it->out, it->out + W * H, it->out + W * H + W * H / 4);
+            cs = (cudaStream_t)h264r_stream_output_cuda_stream(S->s);
         }
         it->done = take_event(srv);
         cudaEventRecord(it->done, cs);

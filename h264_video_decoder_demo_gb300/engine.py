@@ -23,7 +23,7 @@ EXPORTS = [
     "h264r_stream_close", "h264r_stream_dpb_bytes", "h264r_submit_picture",
     "h264r_submit_picture_device", "h264r_submit_batch_device", "h264r_output", "h264r_output_async",
     "h264r_load_slot", "h264r_slot_device_ptr", "h264r_stream_sync", "h264r_ctx_sync",
-    "h264r_stream_cuda_stream", "h264r_validate_picture", "h264r_ctx_kernel_launches",
+    "h264r_stream_cuda_stream", "h264r_stream_output_cuda_stream", "h264r_validate_picture", "h264r_ctx_kernel_launches",
     "h264r_ctx_set_timing", "h264r_ctx_last_timing",
     "h264r_synth_create", "h264r_synth_dpb_slots", "h264r_synth_next", "h264r_synth_destroy",
     "h264r_submit_batch", "h264r_picture_bytes", "h264r_ctx_cuda_stream",
@@ -79,6 +79,7 @@ def _load():
         "h264r_submit_batch_device": (i32, [vp, i32, P(vp), P(R.CPicture)]),
         "h264r_output": (i32, [vp, i32, vp, vp, vp]),
         "h264r_output_async": (i32, [vp, i32, vp, vp, vp]),
+        "h264r_stream_output_cuda_stream": (vp, [vp]),
         "h264r_load_slot": (i32, [vp, i32, vp, vp, vp]),
         "h264r_slot_device_ptr": (i32, [vp, i32, P(vp)]),
         "h264r_stream_sync": (i32, [vp]),

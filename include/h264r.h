@@ -329,6 +329,10 @@ int  h264r_stream_sync(h264r_stream *s);
 int  h264r_ctx_sync(h264r_ctx *ctx);
 /* The CUDA stream the engine enqueues this stream's work on (cudaStream_t). */
 void *h264r_stream_cuda_stream(h264r_stream *s);
+/* The stream's copy stream, which h264r_output_async enqueues on
+ * (cudaStream_t): an event recorded on it after h264r_output_async marks the
+ * copy as done. */
+void *h264r_stream_output_cuda_stream(h264r_stream *s);
 /* The context's own CUDA stream (used by h264r_ctx_sync), cudaStream_t. */
 void *h264r_ctx_cuda_stream(h264r_ctx *ctx);
 
