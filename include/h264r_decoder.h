@@ -57,7 +57,10 @@ const char *h264r_decoder_last_error(const h264r_decoder *d);
 int  h264r_decoder_set_callback(h264r_decoder *d, h264r_frame_callback cb, void *user);
 
 /* Bytes of an Annex B stream, any chunking: pictures are reconstructed on
- * the GPU as they complete and handed out as they become due. */
+ * the GPU as they complete; a due picture is copied to host memory beside the
+ * stream's later pictures and handed out once the copy is done (at the
+ * latest by h264r_decoder_flush), so parsing is not held up by the GPU.  The
+ * picture's slot is not overwritten before its callback has returned. */
 int  h264r_decoder_push(h264r_decoder *d, const uint8_t *data, size_t size);
 /* End of the stream: the remaining pictures, then the final callback.
  * Returns that callback's return value (or a negative error). */
