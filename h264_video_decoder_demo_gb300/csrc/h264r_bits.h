@@ -6,6 +6,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
 namespace h264r {
@@ -26,6 +27,15 @@ inline void nal_to_rbsp(const uint8_t *p, size_t n, std::vector<uint8_t> &out)
         out.push_back(b);
         zeros = b == 0 ? zeros + 1 : 0;
     }
+}
+
+// the 8 bytes of v in big-endian order, as a number
+inline uint64_t be64(uint64_t v)
+{
+    const uint16_t probe = 1;
+    uint8_t first;
+    memcpy(&first, &probe, 1);
+    return first ? __builtin_bswap64(v) : v;  // little-endian hosts swap
 }
 
 struct BitReader {
@@ -62,7 +72,8 @@ struct BitReader {
         const size_t byte = pos >> 3, nbytes = nbits >> 3;
         uint64_t v = 0;
         if (byte + 8 <= nbytes) {
-            for (int i = 0; i < 8; i++) v = (v << 8) | p[byte + i];
+            memcpy(&v, p + byte, 8);
+            v = be64(v);
         } else {
             for (int i = 0; i < 8; i++) v = (v << 8) | (byte + i < nbytes ? p[byte + i] : 0u);
         }

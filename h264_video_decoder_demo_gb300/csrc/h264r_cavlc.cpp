@@ -156,11 +156,10 @@ struct Tables {
     Vlc total_zeros[15], total_zeros_dc[3], run_before[7];
 };
 
-const Tables &tables()
+Tables build_tables()
 {
-    static Tables t;
-    static std::once_flag once;
-    std::call_once(once, [] {
+    Tables t;
+    {
         for (int c = 0; c < 3; c++) {
             t.coeff_token[c].init(16);
             for (int tc = 0; tc <= 16; tc++)
@@ -196,9 +195,13 @@ const Tables &tables()
             for (int r = 0; r < 15; r++)
                 if (kRunBefore[i][r]) t.run_before[i].add(kRunBefore[i][r], r);
         }
-    });
+    }
     return t;
 }
+
+// built once when the library is loaded; read without a guard per code word
+const Tables g_tables = build_tables();
+inline const Tables &tables() { return g_tables; }
 
 int nc_class(int nC) { return nC == -1 ? 4 : nC < 2 ? 0 : nC < 4 ? 1 : nC < 8 ? 2 : 3; }
 
@@ -243,10 +246,12 @@ int cavlc_residual_block(BitReader &br, int nC, int start, int end, int max_coef
             level[i] = br.u(1) ? -1 : 1;
             continue;
         }
-        int prefix = 0;
-        while (br.u(1) == 0) {
-            if (++prefix > 32 || br.err) return -1;
-        }
+        // level_prefix: leading zero bits, then a one
+        const uint32_t lead = br.peek(32);
+        if (lead == 0) return -1;
+        const int prefix = __builtin_clz(lead);
+        br.skip((size_t)prefix + 1);
+        if (br.err) return -1;
         int code = (prefix < 15 ? prefix : 15) << suffix_len;
         const int suffix_size = (prefix == 14 && suffix_len == 0) ? 4 : (prefix >= 15 ? prefix - 3 : suffix_len);
         if (suffix_size > 0) code += (int)br.u(suffix_size);

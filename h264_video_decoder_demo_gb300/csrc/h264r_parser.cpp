@@ -775,7 +775,7 @@ int MbDecoder::residual(int cls, int cbp, bool t8, uint32_t &mask, std::vector<u
         if (tc) r.nz4x4 = 1;
     }
     int l8[4][64];
-    memset(l8, 0, sizeof(l8));
+    if (t8) memset(l8, 0, sizeof(l8));
     for (int b8 = 0; b8 < 4; b8++) {
         for (int b4 = 0; b4 < 4; b4++) {
             const int b = b8 * 4 + b4;
@@ -799,16 +799,17 @@ int MbDecoder::residual(int cls, int cbp, bool t8, uint32_t &mask, std::vector<u
     if (t8) {
         for (int b8 = 0; b8 < 4; b8++) {
             uint16_t s4[4] = {0, 0, 0, 0};
-            std::vector<int16_t> vals;
+            int16_t vals[64];
+            int nv = 0;
             for (int k = 0; k < 64; k++)
                 if (l8[b8][k]) {
                     s4[k >> 4] |= (uint16_t)(1u << (k & 15));
-                    vals.push_back((int16_t)l8[b8][k]);
+                    vals[nv++] = (int16_t)l8[b8][k];
                 }
-            if (!vals.empty()) {
+            if (nv) {
                 mask |= 1u << b8;
                 sig.insert(sig.end(), s4, s4 + 4);
-                lv.insert(lv.end(), vals.begin(), vals.end());
+                lv.insert(lv.end(), vals, vals + nv);
             }
         }
     }
@@ -1390,8 +1391,12 @@ int h264r_parser::finish_picture(bool last)
         }
         memcpy(&motion[off], &p, sizeof(p));
     }
-    // co-located motion for later direct prediction
+    // co-located motion for later direct prediction; the co-located picture
+    // is a reference picture (RefPicList1[0]), so non-reference pictures keep
+    // none (a missing one reads as intra, as before any motion exists)
     const int n = (int)mbs.size();
+    cur.motion.reset();
+    if (sh.nal_ref_idc) {
     auto mo = std::make_shared<Motion>();
     mo->intra.resize(n);
     mo->mv.resize((size_t)n * 2 * 16 * 2);
@@ -1411,6 +1416,7 @@ int h264r_parser::finish_picture(bool last)
             }
     }
     cur.motion = mo;
+    }
     // marking, then POC state for the next picture
     if (sh.nal_ref_idc) {
         const int rc = mark_references(sh, s);
