@@ -129,6 +129,7 @@ struct h264r_parser {
     std::vector<h264r_weight> rec_weights;
     std::vector<uint8_t> motion, coef, pcm;
     std::vector<uint32_t> dref_parts;  // motion offsets of the parts whose dref still holds a refIdx
+    std::vector<std::shared_ptr<Motion>> motion_pool;  // co-located motion buffers, reused
     std::vector<Pic *> last_list[2];
     int num_slices = 0;
     uint32_t slice_errors = 0;  // slices skipped after a syntax error
@@ -1352,7 +1353,11 @@ int h264r_parser::start_picture(const SliceHeader &sh, const Sps &s, const Pps &
     slot_poc[slot] = cur.poc;
     slot_index[slot] = decoded;
     const int n = width_mbs * height_mbs;
-    mbs.assign(n, MbState());
+    // every reader of a neighbour's state checks that it was decoded in the
+    // same slice (slice >= 0) first, so only that mark is reset per picture
+    if ((int)mbs.size() != n) mbs.assign(n, MbState());
+    else
+        for (MbState &m : mbs) m.slice = -1;
     h264r_mb none;
     memset(&none, 0, sizeof(none));
     none.type = H264R_MB_NONE;
@@ -1397,7 +1402,17 @@ int h264r_parser::finish_picture(bool last)
     const int n = (int)mbs.size();
     cur.motion.reset();
     if (sh.nal_ref_idc) {
-    auto mo = std::make_shared<Motion>();
+    // a buffer no picture holds any more is reused (every entry is rewritten)
+    std::shared_ptr<Motion> mo;
+    for (auto &m : motion_pool)
+        if (m.use_count() == 1) {
+            mo = m;
+            break;
+        }
+    if (!mo) {
+        mo = std::make_shared<Motion>();
+        motion_pool.push_back(mo);
+    }
     mo->intra.resize(n);
     mo->mv.resize((size_t)n * 2 * 16 * 2);
     mo->ref.resize((size_t)n * 2 * 16);
