@@ -230,16 +230,16 @@ int cavlc_run_before(BitReader &br, int zeros_left) { return tables().run_before
 // residual_block_cavlc( coeffLevel, startIdx, endIdx, maxNumCoeff ) (7.3.5.3.2,
 // 9.2.2 - 9.2.4).  coeff[startIdx..endIdx] receive the levels (the rest of
 // coeff[0..maxNumCoeff-1] zero); returns 0 or -1 on a syntax error.
-int cavlc_residual_block(BitReader &br, int nC, int start, int end, int max_coeff, int *coeff, int &total)
+// residual_block_cavlc (7.3.5.3.2) up to the levels and runs: level[i]
+// and run[i] for i < total, highest frequency first (9.2.2 - 9.2.4)
+static int cavlc_levels_runs(BitReader &br, int nC, int start, int end, int max_coeff, int *level, int *run, int &total)
 {
-    for (int i = 0; i < max_coeff; i++) coeff[i] = 0;
     int t1 = 0;
     total = 0;
     if (cavlc_coeff_token(br, nC, total, t1)) return -1;
     if (total == 0) return 0;
     const int n = end - start + 1;
     if (total > n || t1 > total) return -1;
-    int level[16], run[16];
     int suffix_len = (total > 10 && t1 < 3) ? 1 : 0;
     for (int i = 0; i < total; i++) {
         if (i < t1) {
@@ -279,12 +279,35 @@ int cavlc_residual_block(BitReader &br, int nC, int start, int end, int max_coef
         zeros_left -= run[i];
     }
     run[total - 1] = zeros_left;
+    return br.err ? -1 : 0;
+}
+
+int cavlc_residual_block(BitReader &br, int nC, int start, int end, int max_coeff, int *coeff, int &total)
+{
+    for (int i = 0; i < max_coeff; i++) coeff[i] = 0;
+    int level[16], run[16];
+    if (cavlc_levels_runs(br, nC, start, end, max_coeff, level, run, total)) return -1;
     int pos = -1;
     for (int i = total - 1; i >= 0; i--) {
         pos += run[i] + 1;
         coeff[start + pos] = level[i];
     }
-    return br.err ? -1 : 0;
+    return 0;
+}
+
+int cavlc_residual_sparse(BitReader &br, int nC, int start, int end, int max_coeff, int off, uint16_t &sig, int16_t *lev,
+                          int &total)
+{
+    sig = 0;
+    int level[16], run[16];
+    if (cavlc_levels_runs(br, nC, start, end, max_coeff, level, run, total)) return -1;
+    int pos = -1;
+    for (int i = total - 1; i >= 0; i--) {
+        pos += run[i] + 1;
+        sig |= (uint16_t)(1u << (start + pos + off));
+        lev[total - 1 - i] = (int16_t)level[i];
+    }
+    return 0;
 }
 
 }  // namespace h264r

@@ -22,6 +22,8 @@
 namespace h264r {
 
 int cavlc_residual_block(BitReader &br, int nC, int start, int end, int max_coeff, int *coeff, int &total);
+int cavlc_residual_sparse(BitReader &br, int nC, int start, int end, int max_coeff, int off, uint16_t &sig, int16_t *lev,
+                          int &total);
 int cbp_from_code(uint32_t code, bool intra);
 
 namespace {
@@ -748,26 +750,29 @@ int MbDecoder::residual(int cls, int cbp, bool t8, uint32_t &mask, std::vector<u
     const int cbp_luma = cbp & 15, cbp_chroma = cbp >> 4;
     int c[64];
     int tc = 0;
-    auto put_block = [&](const int *v, int n, int off, int bit) {
-        uint16_t s = 0;
-        for (int k = 0; k < n; k++)
-            if (v[k]) s |= (uint16_t)(1u << (k + off));
+    // a block's significance word and its levels in scan order, as the
+    // block decoder returns them
+    auto put_sparse = [&](uint16_t s, const int16_t *v, int n, int bit) {
         if (!s) return;
         mask |= 1u << bit;
         sig.push_back(s);
-        for (int k = 0; k < n; k++)
-            if (v[k]) lv.push_back((int16_t)v[k]);
+        lv.insert(lv.end(), v, v + n);
     };
     const bool i16 = cls == H264R_MB_I16x16;
-    int dc[16];
+    uint16_t dc_sig = 0;
+    int16_t dc_lev[16];
+    int dc_n = 0;
     bool have_dc = false;
+    int16_t lev[16];
+    uint16_t bsig = 0;
     // r.nz4x4 / nz8x8 follow the blocks as they are parsed, so that a MB
     // whose residual fails keeps the counts reached, as the reference's does
     r.nz4x4 = 0;
     r.nz8x8 = 0;
     for (int b = 0; b < 16; b++) cur->tc[b] = 0;
     if (i16) {
-        if (cavlc_residual_block(br, nc_luma(0), 0, 15, 16, dc, tc)) return -1;
+        if (cavlc_residual_sparse(br, nc_luma(0), 0, 15, 16, 0, dc_sig, dc_lev, tc)) return -1;
+        dc_n = tc;
         have_dc = true;
         // the reference keeps the DC block's TotalCoeff as block 0's count
         // until an AC block 0 replaces it (H264MacroBlock.cpp residual_luma);
@@ -782,15 +787,14 @@ int MbDecoder::residual(int cls, int cbp, bool t8, uint32_t &mask, std::vector<u
             const int b = b8 * 4 + b4;
             if (!(cbp_luma & (1 << b8))) continue;
             if (i16) {
-                if (cavlc_residual_block(br, nc_luma(b), 0, 14, 15, c, tc)) return -1;
-                put_block(c, 15, 1, b);
-            } else {
+                if (cavlc_residual_sparse(br, nc_luma(b), 0, 14, 15, 1, bsig, lev, tc)) return -1;
+                put_sparse(bsig, lev, tc, b);
+            } else if (t8) {
                 if (cavlc_residual_block(br, nc_luma(b), 0, 15, 16, c, tc)) return -1;
-                if (t8) {
-                    for (int k = 0; k < 16; k++) l8[b8][4 * k + b4] = c[k];
-                } else {
-                    put_block(c, 16, 0, b);
-                }
+                for (int k = 0; k < 16; k++) l8[b8][4 * k + b4] = c[k];
+            } else {
+                if (cavlc_residual_sparse(br, nc_luma(b), 0, 15, 16, 0, bsig, lev, tc)) return -1;
+                put_sparse(bsig, lev, tc, b);
             }
             cur->tc[b] = (uint8_t)tc;
             r.nz4x4 = (uint16_t)((r.nz4x4 & ~(1u << b)) | (tc ? 1u << b : 0u));
@@ -814,22 +818,24 @@ int MbDecoder::residual(int cls, int cbp, bool t8, uint32_t &mask, std::vector<u
             }
         }
     }
-    if (have_dc) put_block(dc, 16, 0, 16);
+    if (have_dc) put_sparse(dc_sig, dc_lev, dc_n, 16);
     // chroma DC then AC (4:2:0)
-    int cdc[2][4];
+    uint16_t cdc_sig[2] = {0, 0};
+    int16_t cdc_lev[2][4];
+    int cdc_n[2] = {0, 0};
     for (int cc = 0; cc < 2; cc++) {
-        for (int k = 0; k < 4; k++) cdc[cc][k] = 0;
-        if ((cbp_chroma & 3) && cavlc_residual_block(br, -1, 0, 3, 4, cdc[cc], tc)) return -1;
+        if ((cbp_chroma & 3) && cavlc_residual_sparse(br, -1, 0, 3, 4, 0, cdc_sig[cc], cdc_lev[cc], tc)) return -1;
+        if (cbp_chroma & 3) cdc_n[cc] = tc;
     }
-    put_block(cdc[0], 4, 0, 17);
-    put_block(cdc[1], 4, 0, 18);
+    put_sparse(cdc_sig[0], cdc_lev[0], cdc_n[0], 17);
+    put_sparse(cdc_sig[1], cdc_lev[1], cdc_n[1], 18);
     for (int cc = 0; cc < 2; cc++)
         for (int b = 0; b < 4; b++) {
             cur->tcc[cc][b] = 0;
             if (!(cbp_chroma & 2)) continue;
-            if (cavlc_residual_block(br, nc_chroma(cc, b), 0, 14, 15, c, tc)) return -1;
+            if (cavlc_residual_sparse(br, nc_chroma(cc, b), 0, 14, 15, 1, bsig, lev, tc)) return -1;
             cur->tcc[cc][b] = (uint8_t)tc;
-            put_block(c, 15, 1, (cc ? H264R_CM_CR_AC0 : H264R_CM_CB_AC0) + b);
+            put_sparse(bsig, lev, tc, (cc ? H264R_CM_CR_AC0 : H264R_CM_CB_AC0) + b);
         }
     return 0;
 }
