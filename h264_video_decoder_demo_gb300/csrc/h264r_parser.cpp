@@ -748,7 +748,6 @@ int MbDecoder::residual(int cls, int cbp, bool t8, uint32_t &mask, std::vector<u
                         h264r_mb &r)
 {
     const int cbp_luma = cbp & 15, cbp_chroma = cbp >> 4;
-    int c[64];
     int tc = 0;
     // a block's significance word and its levels in scan order, as the
     // block decoder returns them
@@ -780,8 +779,10 @@ int MbDecoder::residual(int cls, int cbp, bool t8, uint32_t &mask, std::vector<u
         cur->tc[0] = (uint8_t)tc;
         if (tc) r.nz4x4 = 1;
     }
-    int l8[4][64];
-    if (t8) memset(l8, 0, sizeof(l8));
+    // 8x8 transform: coefficient k of 4x4 block b4 is 8x8 scan index
+    // 4k + b4; the set indices per 8x8 block, and the levels at them
+    uint64_t m64[4] = {0, 0, 0, 0};
+    int16_t v64[4][64];
     for (int b8 = 0; b8 < 4; b8++) {
         for (int b4 = 0; b4 < 4; b4++) {
             const int b = b8 * 4 + b4;
@@ -790,8 +791,15 @@ int MbDecoder::residual(int cls, int cbp, bool t8, uint32_t &mask, std::vector<u
                 if (cavlc_residual_sparse(br, nc_luma(b), 0, 14, 15, 1, bsig, lev, tc)) return -1;
                 put_sparse(bsig, lev, tc, b);
             } else if (t8) {
-                if (cavlc_residual_block(br, nc_luma(b), 0, 15, 16, c, tc)) return -1;
-                for (int k = 0; k < 16; k++) l8[b8][4 * k + b4] = c[k];
+                if (cavlc_residual_sparse(br, nc_luma(b), 0, 15, 16, 0, bsig, lev, tc)) return -1;
+                uint32_t bits = bsig;
+                for (int j = 0; bits; j++) {
+                    const int k = __builtin_ctz(bits);
+                    bits &= bits - 1;
+                    const int idx = 4 * k + b4;
+                    m64[b8] |= 1ull << idx;
+                    v64[b8][idx] = lev[j];
+                }
             } else {
                 if (cavlc_residual_sparse(br, nc_luma(b), 0, 15, 16, 0, bsig, lev, tc)) return -1;
                 put_sparse(bsig, lev, tc, b);
@@ -803,19 +811,10 @@ int MbDecoder::residual(int cls, int cbp, bool t8, uint32_t &mask, std::vector<u
     }
     if (t8) {
         for (int b8 = 0; b8 < 4; b8++) {
-            uint16_t s4[4] = {0, 0, 0, 0};
-            int16_t vals[64];
-            int nv = 0;
-            for (int k = 0; k < 64; k++)
-                if (l8[b8][k]) {
-                    s4[k >> 4] |= (uint16_t)(1u << (k & 15));
-                    vals[nv++] = (int16_t)l8[b8][k];
-                }
-            if (nv) {
-                mask |= 1u << b8;
-                sig.insert(sig.end(), s4, s4 + 4);
-                lv.insert(lv.end(), vals, vals + nv);
-            }
+            if (!m64[b8]) continue;
+            mask |= 1u << b8;
+            for (int w = 0; w < 4; w++) sig.push_back((uint16_t)(m64[b8] >> (16 * w)));
+            for (uint64_t bits = m64[b8]; bits; bits &= bits - 1) lv.push_back(v64[b8][__builtin_ctzll(bits)]);
         }
     }
     if (have_dc) put_sparse(dc_sig, dc_lev, dc_n, 16);
