@@ -15,18 +15,29 @@ namespace h264r {
 // back into 0x0000.
 inline void nal_to_rbsp(const uint8_t *p, size_t n, std::vector<uint8_t> &out)
 {
-    out.clear();
-    out.reserve(n);
+    out.resize(n);
+    uint8_t *o = out.data();
+    size_t w = 0, i = 0;
     int zeros = 0;
-    for (size_t i = 0; i < n; i++) {
-        const uint8_t b = p[i];
+    while (i < n) {
+        if (zeros == 0) {
+            // copy up to the next zero byte in one go
+            const void *z = memchr(p + i, 0, n - i);
+            const size_t end = z ? (size_t)((const uint8_t *)z - p) : n;
+            memcpy(o + w, p + i, end - i);
+            w += end - i;
+            i = end;
+            if (i == n) break;
+        }
+        const uint8_t b = p[i++];
         if (zeros >= 2 && b == 3) {
             zeros = 0;
             continue;
         }
-        out.push_back(b);
+        o[w++] = b;
         zeros = b == 0 ? zeros + 1 : 0;
     }
+    out.resize(w);
 }
 
 // the 8 bytes of v in big-endian order, as a number
