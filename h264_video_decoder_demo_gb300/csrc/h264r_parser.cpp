@@ -197,6 +197,7 @@ struct MbDecoder {
     const Sps &sps;
     const Pps &pps;
     int W, addr = 0, qp = 0;
+    int mbx = 0;  // addr % W, set with addr
     MbState *cur = nullptr;
     bool decoded4x4[16];  // motion of this 4x4 block already derived
     Blk blk[16];          // motion of the current MB (raster)
@@ -216,7 +217,7 @@ struct MbDecoder {
     int nb_mb(int xN, int yN, int maxW, int maxH, int &xW, int &yW) const
     {
         int n;
-        const int x = addr % W;
+        const int x = mbx;
         if (xN < 0 && yN < 0) n = x > 0 ? addr - W - 1 : -1;
         else if (xN < 0 && yN < maxH) n = x > 0 ? addr - 1 : -1;
         else if (xN < maxW && yN < 0) n = addr - W;
@@ -225,8 +226,8 @@ struct MbDecoder {
         else return -1;
         if (n < 0) return -1;
         if (n != addr && P.mbs[n].slice != sc.index) return -1;  // not yet decoded or another slice
-        xW = (xN + maxW) % maxW;
-        yW = (yN + maxH) % maxH;
+        xW = (xN + maxW) & (maxW - 1);  // maxW, maxH: 16 or 8
+        yW = (yN + maxH) & (maxH - 1);
         return n;
     }
 
@@ -1071,6 +1072,7 @@ int h264r_parser::decode_slice(SliceCtx &sc, BitReader &br)
                 if (addr >= num_mbs) return fail(H264R_ERR_BAD_RECORD, "mb_skip_run past the picture end");
                 if (mbs[addr].slice >= 0) return fail(H264R_ERR_BAD_RECORD, "MB %d decoded twice", addr);
                 d.addr = addr;
+                d.mbx = addr % width_mbs;
                 d.cur = &mbs[addr];
                 d.cur->slice = sc.index;
                 d.cur->skip = false;
@@ -1083,6 +1085,7 @@ int h264r_parser::decode_slice(SliceCtx &sc, BitReader &br)
             if (addr >= num_mbs) return fail(H264R_ERR_BAD_RECORD, "slice data past the picture end");
             if (mbs[addr].slice >= 0) return fail(H264R_ERR_BAD_RECORD, "MB %d decoded twice", addr);
             d.addr = addr;
+            d.mbx = addr % width_mbs;
             d.cur = &mbs[addr];
             d.cur->slice = sc.index;
             d.cur->skip = false;
