@@ -17,6 +17,10 @@ wavefront), batches in decoding order.
   e2e       host records through h264r_submit_batch (pinned staging + H2D)
             and every decoded frame copied back to pinned host memory
   plain_fps one picture per launch sequence with a host sync after each
+  tuning    launch shapes and graph replay chosen by the engine's autotuner
+            (h264r_autotune_batch_device) per batch geometry mix, before
+            the warm-up; kernel times for the roofline come from a separate
+            pass with per-kernel CUDA events (graph replay off in it)
   cpu_baseline  the CPU oracle (a restatement of the reference's
             reconstruction) on a bounded sample, one host core
   --impl reference  that CPU implementation with every host core
@@ -53,6 +57,8 @@ def parse():
     ap.add_argument("--pipelines", type=int, default=3, help="concurrent batch pipelines over disjoint stream sets")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (quick runs)")
     ap.add_argument("--skip-configs", action="store_true", help="omit the mixed-size and CIF runs")
+    ap.add_argument("--tune", default="auto", choices=["auto", "off"],
+                    help="auto: autotune launch shapes and graph replay per batch mix; off: default shapes, no graphs")
     ap.add_argument("--serve-seconds", type=float, default=4.0,
                     help="length of the Poisson arrival window of the serving run (0: skip it)")
     return ap.parse_args()
@@ -596,6 +602,20 @@ def run_engine(args, world, rank, local, dist):
     pipes = [torch.cuda.ExternalStream(streams[idxs[0]].cuda_stream(), device=dev) for idxs in sets]
     cs = pipes[0]
 
+    # ---- autotuner: one batch per geometry mix (here: per pictures per
+    # batch, all 1080p), and the one-picture mix of the plain path; run
+    # before the warm-up, which re-decodes every picture in order
+    tuning = {}
+    if args.tune == "auto":
+        for j, ss, cc, hp in batches:
+            key = "batch_%d_pictures" % len(ss)
+            if key not in tuning and hp[0].group > 0:
+                best, ms = ctx.autotune_batch_device(ss, cc, reps=5)
+                tuning[key] = dict(best, ms_per_batch=round(ms, 3))
+        kp = next(k for k, p in enumerate(streams_pics[0]) if p.group > 0)
+        best, ms = ctx.autotune_batch_device([streams[0]], [cpics[0][kp]], reps=10)
+        tuning["plain_1_picture"] = dict(best, ms_per_batch=round(ms, 3))
+
     def step(evs=None):
         for bi, (j, ss, cc, _) in enumerate(batches):
             if evs is not None:
@@ -612,10 +632,10 @@ def run_engine(args, world, rank, local, dist):
 
     # ---- timed region
     launches0 = ctx.kernel_launches()
+    replays0 = ctx.graph_counts()[0]
     batch_evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in batches]
                  for _ in range(args.steps)]
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ctx.set_timing(True)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -636,6 +656,14 @@ def run_engine(args, world, rank, local, dist):
         dist.barrier()
     elapsed_ms = start.elapsed_time(end)
     launches = ctx.kernel_launches() - launches0
+    graph_replays = ctx.graph_counts()[0] - replays0
+    # kernel times: a separate pass of the same steps with CUDA events around
+    # each kernel on the stream it runs on (launched directly, same shapes)
+    kt_steps = 2
+    ctx.set_timing(True)
+    for _ in range(kt_steps):
+        step()
+    ctx.sync()
     ktimes, nlaunch = ctx.last_timing()
     ctx.set_timing(False)
     if dist:
@@ -648,7 +676,7 @@ def run_engine(args, world, rank, local, dist):
     # ---- roofline of the dominant kernel
     names = ["k_inter", "k_intra", "k_deblock_frame"]
     dom = int(np.argmax(ktimes))
-    per_kernel_bytes = algo[:3] * args.steps
+    per_kernel_bytes = algo[:3] * kt_steps
     achieved = per_kernel_bytes[dom] / (ktimes[dom] / 1000.0) / 1e9 if ktimes[dom] > 0 else 0.0
     peak, peak_kind = peak_hbm()
     mbs_per_launch = frames_per_step * 120 * 68 / len(batches)
@@ -656,8 +684,9 @@ def run_engine(args, world, rank, local, dist):
     roofline = {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                 "traffic_note": "ncu DRAM bytes per MB of this kernel on the same mix, scaled to the MBs of one launch",
-                "algorithmic_bytes_per_launch": int(per_kernel_bytes[dom] / (args.steps * len(batches))),
-                "kernel_ms_per_step": [round(t / args.steps, 3) for t in ktimes]}
+                "algorithmic_bytes_per_launch": int(per_kernel_bytes[dom] / (kt_steps * len(batches))),
+                "kernel_ms_per_step": [round(t / kt_steps, 3) for t in ktimes],
+                "kernel_timing": "%d steps after the timed region, CUDA events per kernel" % kt_steps}
 
     extra = {}
     if rank == 0:
@@ -751,6 +780,8 @@ def run_engine(args, world, rank, local, dist):
         "frame_latency_note": "device time of the batched launch sequence that reconstructs the frame",
         "roofline": roofline,
         "gpu_launches": int(launches),
+        "graph_replays": int(graph_replays),
+        "tuning": tuning if tuning else "default shapes (4 MBs per k_inter block, 8 row pairs per deblocking block), no graphs",
         "clocks": clk.summary(),
     }
     out.update(extra)

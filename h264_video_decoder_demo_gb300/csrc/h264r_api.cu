@@ -13,19 +13,24 @@
 #include <cstring>
 #include <functional>
 #include <memory>
+#include <chrono>
 #include <mutex>
 #include <new>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "h264r_device.cuh"
 
 namespace h264r {
 __global__ void k_inter(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
+__global__ void k_inter2(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
+__global__ void k_inter8(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
 __global__ void k_intra(const PicDesc *__restrict__ pics, int npics, uint32_t total_rows, LaunchState st);
 __global__ void k_bs(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st);
 __global__ void k_deblock(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st);
 __global__ void k_deblock_frame(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st);
+__global__ void k_deblock_frame4(const PicDesc *__restrict__ pics, int npics, uint32_t total_units, LaunchState st);
 __global__ void k_bgr24(const uint8_t *__restrict__ yuv, int W, int H, uint8_t *__restrict__ out, int row_bytes, int flip);
 }  // namespace h264r
 
@@ -46,6 +51,23 @@ constexpr unsigned long long kSpinLimit = 1ull << 25;  // ~ seconds of 64 ns sle
 
 inline uint64_t align_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
 
+// What a captured launch sequence depends on: the buffers and streams it
+// names and the sizes of its launches.  Compared bytewise (zeroed first).
+struct GraphKey {
+    const void *host, *dev, *bs, *ires;
+    cudaStream_t cs, side;
+    uint64_t total, mbs, rows;
+    uint32_t n, dbf_units, db_units, flags, inter_w, dbf_w;
+};
+
+struct GraphEntry {
+    GraphKey key;
+    cudaGraphExec_t exec = nullptr;  // instantiated at the second sighting of key
+    uint32_t kernels = 0;
+    uint64_t used = 0;               // last use (LRU clock)
+};
+constexpr int kGraphCache = 16;  // shapes remembered per launch buffer
+
 // Per-launch scratch: PicDesc array, wavefront tickets, progress counters,
 // bS tables.  Host mirror in pinned memory, device copy uploaded per launch.
 struct LaunchBuf {
@@ -64,6 +86,9 @@ struct LaunchBuf {
     cudaEvent_t done = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;  // k_bs on the owner's side stream
     bool pending = false;
+    GraphEntry graphs[kGraphCache];
+    int ngraphs = 0;
+    uint64_t graph_clock = 0;
 };
 
 }  // namespace
@@ -150,6 +175,11 @@ struct h264r_ctx {
     std::vector<std::array<cudaEvent_t, 4>> ev_free, ev_pending;
     std::mutex timing_mu;
     cudaStream_t batch_stream = nullptr;
+    // launch shapes: the default and the autotuner's choice per geometry mix
+    std::mutex tune_mu;
+    h264r_tuning tuning{4, 8, 0, 0};
+    std::unordered_map<uint64_t, h264r_tuning> tuned;
+    std::atomic<uint64_t> graph_replays{0}, graphs_captured{0};
     LaunchBuf batch_ring[kBatchRing];
     int batch_next = 0;
     std::mutex mu;
@@ -259,6 +289,8 @@ static void free_buf(LaunchBuf &b)
     if (b.done) cudaEventDestroy(b.done);
     if (b.fork) cudaEventDestroy(b.fork);
     if (b.join) cudaEventDestroy(b.join);
+    for (int i = 0; i < b.ngraphs; i++)
+        if (b.graphs[i].exec) cudaGraphExecDestroy(b.graphs[i].exec);
     b = LaunchBuf();
 }
 
@@ -561,9 +593,135 @@ static void wait_slot_copy(h264r_stream *s, int slot, cudaStream_t cs)
         cudaStreamWaitEvent(cs, s->slot_ev[slot], 0);
 }
 
+// Geometry mix of a batch: an order-independent hash of the width, height
+// and MBAFF flag of its pictures (the key of the autotuner's choices).
+static uint64_t mix_key(int n, const h264r_picture *const *pics)
+{
+    uint64_t k = 0;
+    for (int i = 0; i < n; i++) {
+        uint64_t z = (uint64_t)pics[i]->width_mbs | (uint64_t)pics[i]->height_mbs << 16 | (uint64_t)(pics[i]->mbaff ? 1 : 0) << 32;
+        z += 0x9e3779b97f4a7c15ull;  // splitmix64 finaliser
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        k += z ^ (z >> 31);
+    }
+    return k;
+}
+
+static bool valid_tuning(const h264r_tuning &t)
+{
+    return (t.inter_mbs_per_cta == 2 || t.inter_mbs_per_cta == 4 || t.inter_mbs_per_cta == 8) &&
+           (t.deblock_pairs_per_cta == 4 || t.deblock_pairs_per_cta == 8);
+}
+
+static h264r_tuning tuning_for(h264r_ctx *ctx, uint64_t key)
+{
+    std::lock_guard<std::mutex> lk(ctx->tune_mu);
+    auto it = ctx->tuned.find(key);
+    return it != ctx->tuned.end() ? it->second : ctx->tuning;
+}
+
+// The sizes of one launch sequence (see launch()).
+struct Seq {
+    const PicDesc *dd;
+    LaunchState st;
+    int n;
+    uint64_t total, mbs, rows;
+    uint32_t dbf_units, db_units;
+    bool any_intra, any_deblock, bs_aside;
+    int inter_w, dbf_w;
+};
+
+// Enqueue the descriptor upload and the kernels of one launch sequence on cs
+// (directly, or into a stream capture); *kernels receives how many kernels.
+static int enqueue_sequence(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const Seq &q, cudaStream_t side,
+                            const std::array<cudaEvent_t, 4> *ev, uint32_t *kernels)
+{
+    uint32_t nk = 0;
+    CUDA_OR(ctx, cudaMemcpyAsync(b.dev, b.host, q.total, cudaMemcpyHostToDevice, cs));
+    const unsigned bs_grid = (unsigned)((q.mbs + 3) / 4);
+    // The strengths depend on the records alone, so for frame pictures k_bs
+    // runs on the side stream of the batch's first stream while k_inter and
+    // k_intra fill the device; the deblocking kernels wait for it.  MBAFF
+    // strengths cost more and slow the intra wavefront they would share the
+    // SMs with (measured: 6 % fewer 1080i frames/s), so they stay in line.
+    if (q.bs_aside) {
+        CUDA_OR(ctx, cudaEventRecord(b.fork, cs));
+        CUDA_OR(ctx, cudaStreamWaitEvent(side, b.fork, 0));
+        h264r::k_bs<<<bs_grid, 128, 0, side>>>(q.dd, q.n, (uint32_t)q.mbs, q.st);
+        nk++;
+        CUDA_OR(ctx, cudaEventRecord(b.join, side));
+    }
+    if (ev) cudaEventRecord((*ev)[0], cs);
+    const unsigned inter_grid = (unsigned)((q.mbs + q.inter_w - 1) / q.inter_w);
+    if (q.inter_w == 2)
+        h264r::k_inter2<<<inter_grid, 64, 0, cs>>>(q.dd, q.n, (uint32_t)q.mbs, q.st);
+    else if (q.inter_w == 8)
+        h264r::k_inter8<<<inter_grid, 256, 0, cs>>>(q.dd, q.n, (uint32_t)q.mbs, q.st);
+    else
+        h264r::k_inter<<<inter_grid, 128, 0, cs>>>(q.dd, q.n, (uint32_t)q.mbs, q.st);
+    nk++;
+    if (ev) cudaEventRecord((*ev)[1], cs);
+    if (q.any_intra) {
+        h264r::k_intra<<<(unsigned)q.rows, 32, 0, cs>>>(q.dd, q.n, (uint32_t)q.rows, q.st);
+        nk++;
+    }
+    if (ev) cudaEventRecord((*ev)[2], cs);
+    if (q.any_deblock) {
+        if (q.bs_aside) {
+            CUDA_OR(ctx, cudaStreamWaitEvent(cs, b.join, 0));
+        } else {
+            h264r::k_bs<<<bs_grid, 128, 0, cs>>>(q.dd, q.n, (uint32_t)q.mbs, q.st);
+            nk++;
+        }
+        if (q.dbf_units) {
+            if (q.dbf_w == 4)
+                h264r::k_deblock_frame4<<<q.dbf_units, 128, 0, cs>>>(q.dd, q.n, q.dbf_units, q.st);
+            else
+                h264r::k_deblock_frame<<<q.dbf_units, 32 * h264r::kDbWarps, 0, cs>>>(q.dd, q.n, q.dbf_units, q.st);
+            nk++;
+        }
+        if (q.db_units) {
+            h264r::k_deblock<<<q.db_units, 32 * h264r::kMbWarps, 0, cs>>>(q.dd, q.n, q.db_units, q.st);
+            nk++;
+        }
+    }
+    if (ev) cudaEventRecord((*ev)[3], cs);
+    *kernels = nk;
+    return H264R_OK;
+}
+
+// The graph cache entry of this launch shape in b, noting a first sighting
+// (returns nullptr then: the sequence is launched directly).
+static GraphEntry *graph_entry(LaunchBuf &b, const GraphKey &key)
+{
+    b.graph_clock++;
+    for (int i = 0; i < b.ngraphs; i++)
+        if (memcmp(&b.graphs[i].key, &key, sizeof(key)) == 0) {
+            b.graphs[i].used = b.graph_clock;
+            return &b.graphs[i];
+        }
+    int v = b.ngraphs;
+    if (v == kGraphCache) {
+        v = 0;
+        for (int i = 1; i < kGraphCache; i++)
+            if (b.graphs[i].used < b.graphs[v].used) v = i;
+        if (b.graphs[v].exec) cudaGraphExecDestroy(b.graphs[v].exec);
+    } else {
+        b.ngraphs++;
+    }
+    b.graphs[v] = GraphEntry();
+    b.graphs[v].key = key;
+    b.graphs[v].used = b.graph_clock;
+    return nullptr;
+}
+
 static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vector<BatchItem> &items, bool any_intra)
 {
     const int n = (int)items.size();
+    std::vector<const h264r_picture *> pl(n);
+    for (int i = 0; i < n; i++) pl[i] = items[i].pic;
+    const h264r_tuning tune = tuning_for(ctx, mix_key(n, pl.data()));
     uint64_t rows = 0, mbs = 0;
     for (auto &it : items) {
         uint32_t uh = it.pic->mbaff ? it.pic->height_mbs / 2 : it.pic->height_mbs;
@@ -628,7 +786,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
         p.db_units = h264r::deblock_units(p.mbaff, p.units_h);
         p.db_base = (uint32_t)db_base;
         db_base += p.db_units;
-        p.dbf_units = h264r::deblock_frame_units(p.mbaff, p.units_h);
+        p.dbf_units = h264r::deblock_frame_units(p.mbaff, p.units_h, (uint32_t)tune.deblock_pairs_per_cta);
         p.dbf_base = (uint32_t)dbf_base;
         dbf_base += p.dbf_units;
         p.deblock_stop = 0xFFFFFFFFu;
@@ -636,56 +794,76 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
         row_base += p.units_h;
         prog += 3 * p.units_h;
     }
-    CUDA_OR(ctx, cudaMemcpyAsync(b.dev, b.host, total, cudaMemcpyHostToDevice, cs));
-    LaunchState st;
-    st.error = ctx->d_error;
-    st.ticket = (unsigned int *)(b.dev + ticket_off);
-    st.spin_limit = kSpinLimit;
-    const PicDesc *dd = (const PicDesc *)b.dev;
-    bool any_deblock = false;
-    for (auto &it : items) any_deblock = any_deblock || it.pic->deblock;
-    std::array<cudaEvent_t, 4> ev{};
-    if (ctx->timing) ev = *take_events(ctx);
-    // The strengths depend on the records alone, so for frame pictures k_bs
-    // runs on the side stream of the batch's first stream while k_inter and
-    // k_intra fill the device; the deblocking kernels wait for it.  MBAFF
-    // strengths cost more and slow the intra wavefront they would share the
-    // SMs with (measured: 6 % fewer 1080i frames/s), so they stay in line.
+    Seq q;
+    q.dd = (const PicDesc *)b.dev;
+    q.st.error = ctx->d_error;
+    q.st.ticket = (unsigned int *)(b.dev + ticket_off);
+    q.st.spin_limit = kSpinLimit;
+    q.n = n;
+    q.total = total;
+    q.mbs = mbs;
+    q.rows = rows;
+    q.dbf_units = (uint32_t)dbf_base;
+    q.db_units = (uint32_t)db_base;
+    q.any_intra = any_intra;
+    q.any_deblock = false;
+    for (auto &it : items) q.any_deblock = q.any_deblock || it.pic->deblock;
+    q.bs_aside = q.any_deblock && db_base == 0;
+    q.inter_w = tune.inter_mbs_per_cta;
+    q.dbf_w = tune.deblock_pairs_per_cta;
     cudaStream_t side = items[0].s->side;
-    const bool bs_aside = any_deblock && db_base == 0;
-    if (bs_aside) {
-        CUDA_OR(ctx, cudaEventRecord(b.fork, cs));
-        CUDA_OR(ctx, cudaStreamWaitEvent(side, b.fork, 0));
-        h264r::k_bs<<<(unsigned)((mbs + 3) / 4), 128, 0, side>>>(dd, n, (uint32_t)mbs, st);
-        ctx->launches++;
-        CUDA_OR(ctx, cudaEventRecord(b.join, side));
+    uint32_t nk = 0;
+    GraphEntry *g = nullptr;
+    // no graph of our own inside a capture the caller is making of cs
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (tune.graphs && !ctx->timing && cudaStreamIsCapturing(cs, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
+        GraphKey key;
+        memset(&key, 0, sizeof(key));
+        key.host = b.host;
+        key.dev = b.dev;
+        key.bs = b.bs;
+        key.ires = any_intra ? b.ires : nullptr;
+        key.cs = cs;
+        key.side = side;
+        key.total = total;
+        key.mbs = mbs;
+        key.rows = rows;
+        key.n = (uint32_t)n;
+        key.dbf_units = q.dbf_units;
+        key.db_units = q.db_units;
+        key.flags = (q.any_intra ? 1u : 0u) | (q.any_deblock ? 2u : 0u) | (q.bs_aside ? 4u : 0u);
+        key.inter_w = (uint32_t)q.inter_w;
+        key.dbf_w = (uint32_t)q.dbf_w;
+        g = graph_entry(b, key);
     }
-    if (ctx->timing) cudaEventRecord(ev[0], cs);
-    h264r::k_inter<<<(unsigned)((mbs + 3) / 4), 128, 0, cs>>>(dd, n, (uint32_t)mbs, st);
-    ctx->launches++;
-    if (ctx->timing) cudaEventRecord(ev[1], cs);
-    if (any_intra) {
-        h264r::k_intra<<<(unsigned)rows, 32, 0, cs>>>(dd, n, (uint32_t)rows, st);
-        ctx->launches++;
+    if (g && !g->exec) {
+        // second sighting of this shape: capture the sequence once
+        CUDA_OR(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue_sequence(ctx, cs, b, q, side, nullptr, &nk);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(cs, &graph);
+        if (rc == H264R_OK && e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (rc) return rc;
+        if (e != cudaSuccess) {
+            g->exec = nullptr;
+            set_err(ctx, "launch graph capture: %s", cudaGetErrorString(e));
+            return H264R_ERR_CUDA;
+        }
+        g->kernels = nk;
+        ctx->graphs_captured++;
     }
-    if (ctx->timing) cudaEventRecord(ev[2], cs);
-    if (any_deblock) {
-        if (bs_aside) {
-            CUDA_OR(ctx, cudaStreamWaitEvent(cs, b.join, 0));
-        } else {
-            h264r::k_bs<<<(unsigned)((mbs + 3) / 4), 128, 0, cs>>>(dd, n, (uint32_t)mbs, st);
-            ctx->launches++;
-        }
-        if (dbf_base) {
-            h264r::k_deblock_frame<<<(unsigned)dbf_base, 32 * h264r::kDbWarps, 0, cs>>>(dd, n, (uint32_t)dbf_base, st);
-            ctx->launches++;
-        }
-        if (db_base) {
-            h264r::k_deblock<<<(unsigned)db_base, 32 * h264r::kMbWarps, 0, cs>>>(dd, n, (uint32_t)db_base, st);
-            ctx->launches++;
-        }
+    if (g) {
+        CUDA_OR(ctx, cudaGraphLaunch(g->exec, cs));
+        ctx->launches += g->kernels;
+        ctx->graph_replays++;
+    } else {
+        std::array<cudaEvent_t, 4> ev{};
+        if (ctx->timing) ev = *take_events(ctx);
+        rc = enqueue_sequence(ctx, cs, b, q, side, ctx->timing ? &ev : nullptr, &nk);
+        if (rc) return rc;
+        ctx->launches += nk;
     }
-    if (ctx->timing) cudaEventRecord(ev[3], cs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_err(ctx, "kernel launch: %s", cudaGetErrorString(e));
@@ -854,6 +1032,91 @@ extern "C" int h264r_submit_batch_device(h264r_ctx *ctx, int n, h264r_stream *co
     cudaEventDestroy(ev);
     return rc;
 }
+
+extern "C" int h264r_ctx_set_tuning(h264r_ctx *ctx, const h264r_tuning *t)
+{
+    if (!ctx || !t) return H264R_ERR_INVALID_ARG;
+    h264r_tuning v = *t;
+    if (!v.inter_mbs_per_cta) v.inter_mbs_per_cta = 4;
+    if (!v.deblock_pairs_per_cta) v.deblock_pairs_per_cta = 8;
+    v.graphs = v.graphs ? 1 : 0;
+    v.reserved = 0;
+    if (!valid_tuning(v)) {
+        set_err(ctx, "h264r_ctx_set_tuning: %d MBs or %d row pairs per block is not a launch shape", t->inter_mbs_per_cta,
+                t->deblock_pairs_per_cta);
+        return H264R_ERR_INVALID_ARG;
+    }
+    std::lock_guard<std::mutex> lk(ctx->tune_mu);
+    ctx->tuning = v;
+    return H264R_OK;
+}
+
+extern "C" int h264r_ctx_get_tuning(h264r_ctx *ctx, int n, const h264r_picture *pics, h264r_tuning *out)
+{
+    if (!ctx || !out || n < 0 || (n > 0 && !pics)) return H264R_ERR_INVALID_ARG;
+    std::vector<const h264r_picture *> pl(n);
+    for (int i = 0; i < n; i++) pl[i] = &pics[i];
+    if (n == 0) {
+        std::lock_guard<std::mutex> lk(ctx->tune_mu);
+        *out = ctx->tuning;
+    } else {
+        *out = tuning_for(ctx, mix_key(n, pl.data()));
+    }
+    return H264R_OK;
+}
+
+extern "C" int h264r_autotune_batch_device(h264r_ctx *ctx, int n, h264r_stream *const *streams, const h264r_picture *pics,
+                                           int reps, h264r_tuning *best, float *best_ms)
+{
+    if (!ctx || n <= 0 || !streams || !pics || !streams[0]) return H264R_ERR_INVALID_ARG;
+    if (reps < 1) reps = 1;
+    std::vector<const h264r_picture *> pl(n);
+    for (int i = 0; i < n; i++) pl[i] = &pics[i];
+    const uint64_t key = mix_key(n, pl.data());
+    static const int kInter[3] = {2, 4, 8}, kPairs[2] = {4, 8};
+    h264r_tuning top{};
+    double top_ms = 1e30;
+    for (int graphs = 0; graphs < 2; graphs++)
+        for (int iw : kInter)
+            for (int dw : kPairs) {
+                const h264r_tuning t{iw, dw, graphs, 0};
+                {
+                    std::lock_guard<std::mutex> lk(ctx->tune_mu);
+                    ctx->tuned[key] = t;
+                }
+                // warm-up: with graphs, every launch buffer of the ring sees
+                // the shape twice (first sighting, capture) before timing
+                const int warm = graphs ? 2 * kBatchRing : 1;
+                int rc = H264R_OK;
+                for (int r = 0; r < warm && rc == H264R_OK; r++) rc = h264r_submit_batch_device(ctx, n, streams, pics);
+                if (rc == H264R_OK) rc = h264r_stream_sync(streams[0]);
+                const auto t0 = std::chrono::steady_clock::now();
+                for (int r = 0; r < reps && rc == H264R_OK; r++) rc = h264r_submit_batch_device(ctx, n, streams, pics);
+                if (rc == H264R_OK) rc = h264r_stream_sync(streams[0]);
+                const auto t1 = std::chrono::steady_clock::now();
+                if (rc) {
+                    std::lock_guard<std::mutex> lk(ctx->tune_mu);
+                    ctx->tuned.erase(key);
+                    return rc;
+                }
+                const double ms = std::chrono::duration<double, std::milli>(t1 - t0).count() / reps;
+                if (ms < top_ms) {
+                    top_ms = ms;
+                    top = t;
+                }
+            }
+    {
+        std::lock_guard<std::mutex> lk(ctx->tune_mu);
+        ctx->tuned[key] = top;
+    }
+    if (best) *best = top;
+    if (best_ms) *best_ms = (float)top_ms;
+    return H264R_OK;
+}
+
+extern "C" uint64_t h264r_ctx_graph_replays(const h264r_ctx *ctx) { return ctx ? ctx->graph_replays.load() : 0; }
+
+extern "C" uint64_t h264r_ctx_graphs_captured(const h264r_ctx *ctx) { return ctx ? ctx->graphs_captured.load() : 0; }
 
 extern "C" int h264r_output(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *cr)
 {

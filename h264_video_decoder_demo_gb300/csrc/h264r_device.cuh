@@ -132,10 +132,12 @@ __host__ __device__ inline uint32_t deblock_units(int mbaff, uint32_t units_h)
 {
     return mbaff ? 2u * ((units_h + kMbWarps - 1u) / kMbWarps) : 0u;
 }
-__host__ __device__ inline uint32_t deblock_frame_units(int mbaff, uint32_t units_h)
+// warps: MB-row pairs per block of the launch's kernel (k_deblock_frame:
+// kDbWarps, k_deblock_frame4: 4)
+__host__ __device__ inline uint32_t deblock_frame_units(int mbaff, uint32_t units_h, uint32_t warps = kDbWarps)
 {
     const uint32_t pairs = (units_h + 1u) / 2u;
-    return mbaff ? 0u : 2u * ((pairs + kDbWarps - 1u) / kDbWarps);
+    return mbaff ? 0u : 2u * ((pairs + warps - 1u) / warps);
 }
 
 // Engine-wide device state for one launch.

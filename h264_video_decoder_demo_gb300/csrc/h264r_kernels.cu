@@ -463,11 +463,16 @@ __device__ __forceinline__ uint32_t chroma_2x2(const uint8_t *pl, int stride, in
 }
 
 
-__global__ void __launch_bounds__(32 * kInterWarps, 6) k_inter(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st)
+// The MB work of k_inter for blocks of W MBs (one warp each).  The launch
+// shape is a tuning choice: k_inter (4 MBs per block) is the default, and
+// k_inter2 / k_inter8 are the shapes the autotuner also tries.  Every shape
+// keeps 24 warps per SM (registers capped at 80).
+template <int W>
+__device__ __forceinline__ void inter_body(InterWarpSmem (&smem)[W], const PicDesc *__restrict__ pics, int npics,
+                                           uint32_t total_mbs, const LaunchState &st)
 {
-    __shared__ InterWarpSmem smem[kInterWarps];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const uint32_t g = blockIdx.x * kInterWarps + wid;
+    const uint32_t g = blockIdx.x * W + wid;
     if (g >= total_mbs) return;
     InterWarpSmem &s = smem[wid];
     const PicDesc p = pics[find_pic_by_mb(pics, npics, g)];
@@ -578,6 +583,25 @@ __global__ void __launch_bounds__(32 * kInterWarps, 6) k_inter(const PicDesc *__
         const int pl = (lane - 16) >> 3, r = (lane - 16) & 7;
         *(uint2 *)(plane_c(p, pl) + (size_t)(chroma_row0(y) + r * dy) * p.Wc + x / 2) = *(const uint2 *)(s.out + 256 + pl * 64 + r * 8);
     }
+}
+
+__global__ void __launch_bounds__(32 * kInterWarps, 24 / kInterWarps) k_inter(const PicDesc *__restrict__ pics, int npics,
+                                                                             uint32_t total_mbs, LaunchState st)
+{
+    __shared__ InterWarpSmem smem[kInterWarps];
+    inter_body<kInterWarps>(smem, pics, npics, total_mbs, st);
+}
+
+__global__ void __launch_bounds__(64, 12) k_inter2(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st)
+{
+    __shared__ InterWarpSmem smem[2];
+    inter_body<2>(smem, pics, npics, total_mbs, st);
+}
+
+__global__ void __launch_bounds__(256, 3) k_inter8(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st)
+{
+    __shared__ InterWarpSmem smem[8];
+    inter_body<8>(smem, pics, npics, total_mbs, st);
 }
 
 // ======================================================================
@@ -2002,17 +2026,20 @@ struct DbChromaSmem {
 // first warp waits on, and reads, global memory, and only its last warp
 // publishes global progress.  used is the consumer's progress, which keeps a
 // producer from overwriting lines not yet taken.
+// W row-pair warps per block: k_deblock_frame uses kDbWarps, k_deblock_frame4
+// four (the other shape the autotuner tries).
+template <int W>
 struct DbFrameShared {
     union {
-        DbLumaSmem l[kDbWarps];
-        DbChromaSmem c[kDbWarps];
+        DbLumaSmem l[W];
+        DbChromaSmem c[W];
     } w;
     union {
-        uint4 l[kDbWarps - 1][kDbXRing][4];     // luma rows 12..15
-        uint2 c[kDbWarps - 1][kDbXRing][2][4];  // chroma rows 4..7 per plane
+        uint4 l[W - 1][kDbXRing][4];     // luma rows 12..15
+        uint2 c[W - 1][kDbXRing][2][4];  // chroma rows 4..7 per plane
     } x;
-    int done[kDbWarps];  // second row: MBs up to done-2 completed and the vertical edges of MB done-1 (uw+1: all)
-    int used[kDbWarps];  // first row: MBs whose rows above were taken
+    int done[W];  // second row: MBs up to done-2 completed and the vertical edges of MB done-1 (uw+1: all)
+    int used[W];  // first row: MBs whose rows above were taken
 };
 
 
@@ -2075,7 +2102,8 @@ __device__ __forceinline__ void db_chroma(int (&v)[N], int bS, uint32_t prm)
     v[Q] = clip1(q0 - delta);
 }
 
-__device__ void deblock_pair_luma(const PicDesc &p, int pair, int wi, int nw, DbLumaSmem &s, DbFrameShared &S,
+template <int NW>
+__device__ void deblock_pair_luma(const PicDesc &p, int pair, int wi, int nw, DbLumaSmem &s, DbFrameShared<NW> &S,
                                   const LaunchState &st)
 {
     const int lane = threadIdx.x & 31;
@@ -2203,7 +2231,8 @@ __device__ void deblock_pair_luma(const PicDesc &p, int pair, int wi, int nw, Db
     }
 }
 
-__device__ void deblock_pair_chroma(const PicDesc &p, int pair, int wi, int nw, DbChromaSmem &s, DbFrameShared &S,
+template <int NW>
+__device__ void deblock_pair_chroma(const PicDesc &p, int pair, int wi, int nw, DbChromaSmem &s, DbFrameShared<NW> &S,
                                     const LaunchState &st)
 {
     const int lane = threadIdx.x & 31;
@@ -2348,13 +2377,12 @@ __global__ void __launch_bounds__(32 * kMbWarps, 24 / kMbWarps) k_deblock(const 
 
 // Frame pictures: a block of kDbWarps warps per kDbWarps MB-row pairs of one
 // plane (even block tickets luma, odd ones chroma); see DbFrameShared.
-__global__ void __launch_bounds__(32 * kDbWarps, 28 / kDbWarps) k_deblock_frame(const PicDesc *__restrict__ pics, int npics,
-                                                                              uint32_t total_units, LaunchState st)
+template <int W>
+__device__ __forceinline__ void deblock_frame_body(DbFrameShared<W> &S, uint32_t &s_unit, const PicDesc *__restrict__ pics,
+                                                   int npics, uint32_t total_units, const LaunchState &st)
 {
-    __shared__ DbFrameShared S;
-    __shared__ uint32_t s_unit;
     if (threadIdx.x == 0) s_unit = atomicAdd(&st.ticket[2], 1u);
-    if (threadIdx.x < kDbWarps) {
+    if (threadIdx.x < W) {
         S.done[threadIdx.x] = 0;
         S.used[threadIdx.x] = 0;
     }
@@ -2366,11 +2394,29 @@ __global__ void __launch_bounds__(32 * kDbWarps, 28 / kDbWarps) k_deblock_frame(
     if (!p.deblock || p.mbaff) return;
     const int unit = (int)(g - p.dbf_base);
     const int wi = threadIdx.x >> 5;
-    const int first = (unit >> 1) * kDbWarps, pairs = ((int)p.units_h + 1) / 2;
-    const int nw = min(kDbWarps, pairs - first);
+    const int first = (unit >> 1) * W, pairs = ((int)p.units_h + 1) / 2;
+    const int nw = min(W, pairs - first);
     if (wi >= nw) return;
-    if ((unit & 1) == 0) deblock_pair_luma(p, first + wi, wi, nw, S.w.l[wi], S, st);
-    else deblock_pair_chroma(p, first + wi, wi, nw, S.w.c[wi], S, st);
+    if ((unit & 1) == 0) deblock_pair_luma<W>(p, first + wi, wi, nw, S.w.l[wi], S, st);
+    else deblock_pair_chroma<W>(p, first + wi, wi, nw, S.w.c[wi], S, st);
+}
+
+__global__ void __launch_bounds__(32 * kDbWarps, 28 / kDbWarps) k_deblock_frame(const PicDesc *__restrict__ pics, int npics,
+                                                                              uint32_t total_units, LaunchState st)
+{
+    __shared__ DbFrameShared<kDbWarps> S;
+    __shared__ uint32_t s_unit;
+    deblock_frame_body<kDbWarps>(S, s_unit, pics, npics, total_units, st);
+}
+
+// The same with blocks of four MB-row pairs; the picture descriptors of its
+// launch count units with deblock_frame_units(mbaff, units_h, 4).
+__global__ void __launch_bounds__(128, 7) k_deblock_frame4(const PicDesc *__restrict__ pics, int npics, uint32_t total_units,
+                                                           LaunchState st)
+{
+    __shared__ DbFrameShared<4> S;
+    __shared__ uint32_t s_unit;
+    deblock_frame_body<4>(S, s_unit, pics, npics, total_units, st);
 }
 
 // ======================================================================

@@ -29,6 +29,8 @@ EXPORTS = [
     "h264r_submit_batch", "h264r_picture_bytes", "h264r_ctx_cuda_stream",
     "h264r_deblock_picture_noalloc",
     "h264r_ctx_device", "h264r_ctx_dpb_budget", "h264r_ctx_max_batch",
+    "h264r_ctx_set_tuning", "h264r_ctx_get_tuning", "h264r_autotune_batch_device",
+    "h264r_ctx_graph_replays", "h264r_ctx_graphs_captured",
     "h264r_output_bgr24", "h264r_output_bgr24_device", "h264r_write_bmp", "h264r_write_yuv",
     "h264r_order_create", "h264r_order_destroy", "h264r_order_push", "h264r_order_flush",
     "h264r_order_holds", "h264r_order_infer_depth",
@@ -110,6 +112,12 @@ def _load():
         "h264r_ctx_device": (i32, [vp]),
         "h264r_ctx_dpb_budget": (u64, [vp]),
         "h264r_ctx_max_batch": (i32, [vp]),
+        "h264r_ctx_set_tuning": (i32, [vp, P(R.CTuning)]),
+        "h264r_ctx_get_tuning": (i32, [vp, i32, P(R.CPicture), P(R.CTuning)]),
+        "h264r_autotune_batch_device": (i32, [vp, i32, P(vp), P(R.CPicture), i32, P(R.CTuning),
+                                              P(ctypes.c_float)]),
+        "h264r_ctx_graph_replays": (u64, [vp]),
+        "h264r_ctx_graphs_captured": (u64, [vp]),
         "h264r_server_create": (i32, [vp, P(R.CServerCfg), P(vp)]),
         "h264r_server_destroy": (i32, [vp]),
         "h264r_server_open": (i32, [vp, P(R.CStreamCfg), P(i32)]),
@@ -235,6 +243,35 @@ class Context:
         arr = (ctypes.c_void_p * n)(*[s.h.value for s in streams])
         pics = (R.CPicture * n)(*cpics)
         return lib().h264r_submit_batch_device(self.h, n, arr, pics)
+
+    def set_tuning(self, inter_mbs_per_cta=4, deblock_pairs_per_cta=8, graphs=False):
+        """Default launch shapes and graph replay of every batch (h264r_ctx_set_tuning)."""
+        t = R.CTuning(inter_mbs_per_cta, deblock_pairs_per_cta, 1 if graphs else 0, 0)
+        return self.check(lib().h264r_ctx_set_tuning(self.h, ctypes.byref(t)), "set_tuning")
+
+    def tuning(self, cpics=()):
+        """The tuning a batch of these pictures (CPicture) launches with, as a dict."""
+        n = len(cpics)
+        pics = (R.CPicture * max(n, 1))(*cpics)
+        t = R.CTuning()
+        self.check(lib().h264r_ctx_get_tuning(self.h, n, pics, ctypes.byref(t)), "get_tuning")
+        return t.as_dict()
+
+    def autotune_batch_device(self, streams, cpics, reps=5):
+        """Time every launch shape on this batch and keep the fastest for its
+        geometry mix (h264r_autotune_batch_device); returns (tuning dict, ms per batch)."""
+        n = len(streams)
+        arr = (ctypes.c_void_p * n)(*[s.h.value for s in streams])
+        pics = (R.CPicture * n)(*cpics)
+        t = R.CTuning()
+        ms = ctypes.c_float()
+        self.check(lib().h264r_autotune_batch_device(self.h, n, arr, pics, reps, ctypes.byref(t), ctypes.byref(ms)),
+                   "autotune_batch_device")
+        return t.as_dict(), ms.value
+
+    def graph_counts(self):
+        """(launch sequences replayed from captured graphs, graphs captured)."""
+        return int(lib().h264r_ctx_graph_replays(self.h)), int(lib().h264r_ctx_graphs_captured(self.h))
 
     def close(self):
         if self.h:

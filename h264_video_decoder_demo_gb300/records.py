@@ -156,6 +156,16 @@ class CCfg(ctypes.Structure):
                 ("max_batch_pictures", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
 
 
+class CTuning(ctypes.Structure):
+    """struct h264r_tuning (include/h264r.h): launch shapes and graph replay"""
+    _fields_ = [("inter_mbs_per_cta", ctypes.c_int32), ("deblock_pairs_per_cta", ctypes.c_int32),
+                ("graphs", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {"inter_mbs_per_cta": self.inter_mbs_per_cta,
+                "deblock_pairs_per_cta": self.deblock_pairs_per_cta, "graphs": self.graphs}
+
+
 class CSynthCfg(ctypes.Structure):
     """struct h264r_synth_cfg (include/h264r_synth.h)"""
     _fields_ = [("seed", ctypes.c_uint32), ("width_mbs", ctypes.c_uint16),

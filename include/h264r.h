@@ -385,6 +385,54 @@ uint64_t h264r_ctx_kernel_launches(const h264r_ctx *ctx);
 int  h264r_ctx_set_timing(h264r_ctx *ctx, int enable);
 int  h264r_ctx_last_timing(h264r_ctx *ctx, float t[3], int *launches);
 
+/* ---- launch shapes, captured launch graphs, autotuner ------------------ */
+/*
+ * No counterpart in the reference, which reconstructs one macroblock at a
+ * time on one CPU thread.  The tuning of a launch sequence:
+ *   inter_mbs_per_cta      k_inter: MBs (one warp each) per thread block,
+ *                          2, 4 or 8 (0: 4)
+ *   deblock_pairs_per_cta  frame-picture deblocking: MB-row pairs (one warp
+ *                          each) per thread block, 4 or 8 (0: 8)
+ *   graphs                 non-zero: a launch sequence (descriptor upload,
+ *                          k_bs beside k_inter / k_intra, deblocking) whose
+ *                          shape a launch buffer has seen before is captured
+ *                          once as a CUDA graph and replayed from then on;
+ *                          not while kernel timing is on
+ * Decoded samples do not depend on the tuning.  A context starts with the
+ * defaults {4, 8, 0}; h264r_ctx_set_tuning changes them for every batch
+ * without an autotuned entry.  Entries are keyed by the batch's picture
+ * geometry mix (the multiset of width x height x MBAFF of its pictures).
+ * Returns H264R_ERR_INVALID_ARG for a shape outside the lists above.
+ */
+typedef struct h264r_tuning {
+    int32_t inter_mbs_per_cta;
+    int32_t deblock_pairs_per_cta;
+    int32_t graphs;
+    int32_t reserved;
+} h264r_tuning;
+
+int  h264r_ctx_set_tuning(h264r_ctx *ctx, const h264r_tuning *t);
+/* The tuning a batch of these n pictures would launch with (n = 0: the
+ * context's default). */
+int  h264r_ctx_get_tuning(h264r_ctx *ctx, int n, const h264r_picture *pics, h264r_tuning *out);
+/*
+ * Autotuner: runs the batch (as h264r_submit_batch_device) under every
+ * launch shape and graph setting, reps times each after warm-up runs,
+ * times each setting on the host clock from the first submission to the
+ * end of the last (a synchronised throughput measurement on streams[0]'s
+ * CUDA stream), and keeps the fastest for the batch's geometry mix.  The
+ * batch must be one that can run again with the same result: its pictures
+ * reference none of its own destination slots, which holds for every
+ * dependency group.  *best / *best_ms (either may be NULL) receive the
+ * choice and its milliseconds per batch.
+ */
+int  h264r_autotune_batch_device(h264r_ctx *ctx, int n, h264r_stream *const *streams, const h264r_picture *pics,
+                                 int reps, h264r_tuning *best, float *best_ms);
+/* Launch sequences replayed from captured graphs, and graphs instantiated,
+ * so far by this context. */
+uint64_t h264r_ctx_graph_replays(const h264r_ctx *ctx);
+uint64_t h264r_ctx_graphs_captured(const h264r_ctx *ctx);
+
 #ifdef __cplusplus
 }
 #endif
