@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--skip-configs", action="store_true", help="omit the mixed-size and CIF runs")
     ap.add_argument("--tune", default="auto", choices=["auto", "off"],
                     help="auto: autotune launch shapes and graph replay per batch mix; off: default shapes, no graphs")
+    ap.add_argument("--tune-from", default="",
+                    help="JSON file with the 'tuning' object of an earlier bench line: use those choices, no autotuning")
     ap.add_argument("--serve-seconds", type=float, default=4.0,
                     help="length of the Poisson arrival window of the serving run (0: skip it)")
     return ap.parse_args()
@@ -606,13 +608,27 @@ def run_engine(args, world, rank, local, dist):
     # batch, all 1080p), and the one-picture mix of the plain path; run
     # before the warm-up, which re-decodes every picture in order
     tuning = {}
-    if args.tune == "auto":
+    kp = next(k for k, p in enumerate(streams_pics[0]) if p.group > 0)
+    if args.tune_from:
+        with open(args.tune_from) as f:
+            kept = json.load(f)
+        kept = kept.get("tuning", kept)
+        for j, ss, cc, hp in batches:
+            key = "batch_%d_pictures" % len(ss)
+            if key in kept and key not in tuning:
+                t = kept[key]
+                ctx.set_mix_tuning(cc, t["inter_mbs_per_cta"], t["deblock_pairs_per_cta"], bool(t["graphs"]))
+                tuning[key] = dict(t, source=args.tune_from)
+        if "plain_1_picture" in kept:
+            t = kept["plain_1_picture"]
+            ctx.set_mix_tuning([cpics[0][kp]], t["inter_mbs_per_cta"], t["deblock_pairs_per_cta"], bool(t["graphs"]))
+            tuning["plain_1_picture"] = dict(t, source=args.tune_from)
+    elif args.tune == "auto":
         for j, ss, cc, hp in batches:
             key = "batch_%d_pictures" % len(ss)
             if key not in tuning and hp[0].group > 0:
                 best, ms = ctx.autotune_batch_device(ss, cc, reps=5)
                 tuning[key] = dict(best, ms_per_batch=round(ms, 3))
-        kp = next(k for k, p in enumerate(streams_pics[0]) if p.group > 0)
         best, ms = ctx.autotune_batch_device([streams[0]], [cpics[0][kp]], reps=10)
         tuning["plain_1_picture"] = dict(best, ms_per_batch=round(ms, 3))
 

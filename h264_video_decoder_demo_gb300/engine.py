@@ -29,7 +29,7 @@ EXPORTS = [
     "h264r_submit_batch", "h264r_picture_bytes", "h264r_ctx_cuda_stream",
     "h264r_deblock_picture_noalloc",
     "h264r_ctx_device", "h264r_ctx_dpb_budget", "h264r_ctx_max_batch",
-    "h264r_ctx_set_tuning", "h264r_ctx_get_tuning", "h264r_autotune_batch_device",
+    "h264r_ctx_set_tuning", "h264r_ctx_get_tuning", "h264r_ctx_set_mix_tuning", "h264r_autotune_batch_device",
     "h264r_ctx_graph_replays", "h264r_ctx_graphs_captured",
     "h264r_output_bgr24", "h264r_output_bgr24_device", "h264r_write_bmp", "h264r_write_yuv",
     "h264r_order_create", "h264r_order_destroy", "h264r_order_push", "h264r_order_flush",
@@ -114,6 +114,7 @@ def _load():
         "h264r_ctx_max_batch": (i32, [vp]),
         "h264r_ctx_set_tuning": (i32, [vp, P(R.CTuning)]),
         "h264r_ctx_get_tuning": (i32, [vp, i32, P(R.CPicture), P(R.CTuning)]),
+        "h264r_ctx_set_mix_tuning": (i32, [vp, i32, P(R.CPicture), P(R.CTuning)]),
         "h264r_autotune_batch_device": (i32, [vp, i32, P(vp), P(R.CPicture), i32, P(R.CTuning),
                                               P(ctypes.c_float)]),
         "h264r_ctx_graph_replays": (u64, [vp]),
@@ -256,6 +257,13 @@ class Context:
         t = R.CTuning()
         self.check(lib().h264r_ctx_get_tuning(self.h, n, pics, ctypes.byref(t)), "get_tuning")
         return t.as_dict()
+
+    def set_mix_tuning(self, cpics, inter_mbs_per_cta=4, deblock_pairs_per_cta=8, graphs=False):
+        """Tuning of the geometry mix of these pictures (CPicture), e.g. a kept autotuner result."""
+        n = len(cpics)
+        pics = (R.CPicture * n)(*cpics)
+        t = R.CTuning(inter_mbs_per_cta, deblock_pairs_per_cta, 1 if graphs else 0, 0)
+        return self.check(lib().h264r_ctx_set_mix_tuning(self.h, n, pics, ctypes.byref(t)), "set_mix_tuning")
 
     def autotune_batch_device(self, streams, cpics, reps=5):
         """Time every launch shape on this batch and keep the fastest for its

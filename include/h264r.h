@@ -415,12 +415,19 @@ int  h264r_ctx_set_tuning(h264r_ctx *ctx, const h264r_tuning *t);
 /* The tuning a batch of these n pictures would launch with (n = 0: the
  * context's default). */
 int  h264r_ctx_get_tuning(h264r_ctx *ctx, int n, const h264r_picture *pics, h264r_tuning *out);
+/* Set the tuning of the geometry mix of these n pictures, e.g. one that an
+ * earlier autotuner run found and the caller kept (only the pictures'
+ * width_mbs, height_mbs and mbaff are read). */
+int  h264r_ctx_set_mix_tuning(h264r_ctx *ctx, int n, const h264r_picture *pics, const h264r_tuning *t);
 /*
  * Autotuner: runs the batch (as h264r_submit_batch_device) under every
  * launch shape and graph setting, reps times each after warm-up runs,
  * times each setting on the host clock from the first submission to the
  * end of the last (a synchronised throughput measurement on streams[0]'s
- * CUDA stream), and keeps the fastest for the batch's geometry mix.  The
+ * CUDA stream), in three rounds over all settings in turn, each setting
+ * keeping its best round.  It keeps the fastest for the batch's geometry
+ * mix, unless that is less than 3 % faster than the mix's current tuning
+ * (which then stays).  The
  * batch must be one that can run again with the same result: its pictures
  * reference none of its own destination slots, which holds for every
  * dependency group.  *best / *best_ms (either may be NULL) receive the

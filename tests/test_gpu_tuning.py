@@ -167,5 +167,15 @@ def test_tuning_rejects_unknown_shapes(engine_lib):
         assert ctx.tuning() == {"inter_mbs_per_cta": 4, "deblock_pairs_per_cta": 8, "graphs": 0}
         ctx.set_tuning(0, 0, graphs=True)  # 0 selects the default shapes
         assert ctx.tuning() == {"inter_mbs_per_cta": 4, "deblock_pairs_per_cta": 8, "graphs": 1}
+        # a kept choice for one geometry mix (one CIF picture) leaves other mixes alone
+        g = h.synth("cif_ippp", seed=66, num_pictures=1)
+        p = next(iter(g))
+        c = p.to_c()
+        ctx.set_mix_tuning([c], 2, 4, graphs=False)
+        assert ctx.tuning([c]) == {"inter_mbs_per_cta": 2, "deblock_pairs_per_cta": 4, "graphs": 0}
+        assert ctx.tuning([c, c]) == ctx.tuning()
+        with pytest.raises(h.EngineError):
+            ctx.set_mix_tuning([c], 5, 8)
+        g.close()
     finally:
         ctx.close()
