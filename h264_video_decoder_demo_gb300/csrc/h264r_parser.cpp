@@ -1425,18 +1425,27 @@ int h264r_parser::finish_picture(bool last)
     mo->mv.resize((size_t)n * 2 * 16 * 2);
     mo->ref.resize((size_t)n * 2 * 16);
     mo->refpic.resize((size_t)n * 2 * 16);
+    // per MB the [list][4x4 block] arrays have the MB state's layout: one
+    // copy each (intra and undecoded MBs: no motion, references -1)
+    static_assert(sizeof(MbState::mv) == 2 * 16 * 2 * sizeof(int16_t) && sizeof(MbState::ref) == 32 &&
+                      sizeof(MbState::refpic) == 32 * sizeof(int32_t),
+                  "co-located motion layout");
     for (int a = 0; a < n; a++) {
         const MbState &m = mbs[a];
         const bool inter = m.slice >= 0 && m.cls == H264R_MB_INTER;
         mo->intra[a] = inter ? 0 : 1;
-        for (int l = 0; l < 2; l++)
-            for (int i = 0; i < 16; i++) {
-                const size_t o = (size_t)(a * 2 + l) * 16 + i;
-                mo->ref[o] = inter ? m.ref[l][i] : -1;
-                mo->mv[o * 2] = inter ? m.mv[l][i][0] : 0;
-                mo->mv[o * 2 + 1] = inter ? m.mv[l][i][1] : 0;
-                mo->refpic[o] = inter ? m.refpic[l][i] : -1;
-            }
+        int16_t *mv = &mo->mv[(size_t)a * 64];
+        int8_t *ref = &mo->ref[(size_t)a * 32];
+        int32_t *rp = &mo->refpic[(size_t)a * 32];
+        if (inter) {
+            memcpy(mv, m.mv, sizeof(m.mv));
+            memcpy(ref, m.ref, sizeof(m.ref));
+            memcpy(rp, m.refpic, sizeof(m.refpic));
+        } else {
+            memset(mv, 0, sizeof(m.mv));
+            memset(ref, 0xFF, sizeof(m.ref));
+            memset(rp, 0xFF, sizeof(m.refpic));  // -1 in every int32
+        }
     }
     cur.motion = mo;
     }
