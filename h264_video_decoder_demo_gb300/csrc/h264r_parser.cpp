@@ -205,11 +205,17 @@ struct MbDecoder {
     std::vector<PartRec> parts;
     std::vector<uint16_t> sig;
     std::vector<int16_t> lv;
+    // uid of the slice's list entry refIdx at [list][refIdx + 1] (-1 for
+    // refIdx -1 and for missing entries)
+    int32_t uid[2][33];
 
     MbDecoder(h264r_parser &p, SliceCtx &s, BitReader &b)
         : P(p), sc(s), br(b), sps(*s.sps), pps(*s.pps), W(p.width_mbs)
     {
         qp = pps.pic_init_qp + s.sh.slice_qp_delta;
+        for (int l = 0; l < 2; l++)
+            for (int i = 0; i < 33; i++)
+                uid[l][i] = (i > 0 && i - 1 < (int)s.list[l].size() && s.list[l][i - 1]) ? s.list[l][i - 1]->uid : -1;
     }
 
     // ---- neighbours (6.4.12.1): the MB holding luma location (xN, yN)
@@ -734,12 +740,13 @@ void MbDecoder::emit_motion(int shape, const std::vector<PartRec> &parts, h264r_
 // motion of the finished MB into the neighbour state
 void MbDecoder::store_motion()
 {
-    for (int i = 0; i < 16; i++)
-        for (int l = 0; l < 2; l++) {
-            cur->ref[l][i] = blk[i].ref[l];
+    for (int l = 0; l < 2; l++)
+        for (int i = 0; i < 16; i++) {
+            const int r = blk[i].ref[l];  // -1 .. 31 (the entry was checked when parsed)
+            cur->ref[l][i] = (int8_t)r;
             cur->mv[l][i][0] = blk[i].mv[l][0];
             cur->mv[l][i][1] = blk[i].mv[l][1];
-            cur->refpic[l][i] = blk[i].ref[l] >= 0 ? sc.list[l][blk[i].ref[l]]->uid : -1;
+            cur->refpic[l][i] = uid[l][r + 1];
         }
 }
 
