@@ -81,11 +81,22 @@ def test_every_launch_shape_matches_oracle(engine_lib, mixed_workload, iw, dw, g
         ctx.close()
 
 
-def test_graph_replay_per_picture_matches_oracle(engine_lib):
+def _synth_cif(seed):
+    return h.synth("cif_ippp", seed=seed)
+
+
+def _synth_cif_mbaff(seed):
+    # MBAFF frames: k_bs in line and the MBAFF deblocking kernel in the graph
+    return h.synth("cif_ippp", seed=seed, num_pictures=8, mbaff=1, field_percent=50, gop_kind=1, num_refs=2,
+                   transform8x8=1, mv_range=128, edge_mv_percent=10)
+
+
+@pytest.mark.parametrize("make", [_synth_cif, _synth_cif_mbaff], ids=["frame", "mbaff"])
+def test_graph_replay_per_picture_matches_oracle(engine_lib, make):
     """One CIF stream, one picture per launch, decoded three times over: the
     per-stream launch buffers see each shape again and replay graphs; every
     picture equals the oracle's."""
-    g = h.synth("cif_ippp", seed=64)
+    g = make(64)
     ps = list(g)
     slots = g.dpb_slots
     g.close()
@@ -106,7 +117,7 @@ def test_graph_replay_per_picture_matches_oracle(engine_lib):
         replays, captured = ctx.graph_counts()
         assert captured >= 1 and replays >= captured
         # replayed sequences count their kernels like direct launches
-        assert ctx.kernel_launches() - launches0 >= 3 * 3 * len(ps)
+        assert ctx.kernel_launches() - launches0 >= 3 * 2 * len(ps)
     finally:
         s.close()
         ctx.close()
