@@ -239,6 +239,22 @@ class Context:
         cpics = (R.CPicture * n)(*[p.to_c() for p in pics])
         return self.check(lib().h264r_submit_batch(self.h, n, arr, cpics), "submit_batch")
 
+    def prepare_batch(self, streams, pics):
+        """The C arguments of a host-record batch (streams and h264r_picture
+        descriptors pointing into the Pictures' arrays), built once for
+        submit_prepared, as a C caller keeps the descriptors its parser
+        emitted.  The Pictures must stay alive and unchanged."""
+        n = len(streams)
+        arr = (ctypes.c_void_p * n)(*[s.h.value for s in streams])
+        cpics = (R.CPicture * n)(*[p.to_c() for p in pics])
+        return n, arr, cpics, list(pics)
+
+    def submit_prepared(self, prep):
+        """h264r_submit_batch of a prepare_batch result: validation, packing
+        and the host-to-device copy of the records happen on every call."""
+        n, arr, cpics, _ = prep
+        return self.check(lib().h264r_submit_batch(self.h, n, arr, cpics), "submit_batch")
+
     def submit_batch_device(self, streams, cpics):
         n = len(streams)
         arr = (ctypes.c_void_p * n)(*[s.h.value for s in streams])
