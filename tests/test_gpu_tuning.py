@@ -190,3 +190,26 @@ def test_tuning_rejects_unknown_shapes(engine_lib):
         g.close()
     finally:
         ctx.close()
+
+
+def test_prepared_batches_match_oracle(engine_lib, mixed_workload):
+    """Batch arguments built once (Context.prepare_batch) and submitted on
+    every pass, as the end-to-end benchmark does: each pass re-validates,
+    packs and uploads the records; every picture of both passes equals the
+    oracle's."""
+    pics, slots, expect, batches = mixed_workload
+    ctx = h.Context(0)
+    streams = [h.Stream(ctx, ps[0].width_mbs, ps[0].height_mbs, sl) for ps, sl in zip(pics, slots)]
+    try:
+        prepared = [(ctx.prepare_batch([streams[i] for i, _ in grp], [pics[i][k] for i, k in grp]), grp)
+                    for grp in batches]
+        for rep in range(2):
+            for prep, grp in prepared:
+                ctx.submit_prepared(prep)
+                for i, k in grp:
+                    out = streams[i].output(pics[i][k].dst_slot)
+                    assert np.array_equal(out, expect[i][k]), "pass %d stream %d picture %d" % (rep, i, k)
+    finally:
+        for s in streams:
+            s.close()
+        ctx.close()
