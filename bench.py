@@ -61,8 +61,10 @@ def parse():
                     help="auto: autotune launch shapes and graph replay per batch mix; off: default shapes, no graphs")
     ap.add_argument("--tune-from", default="",
                     help="JSON file with the 'tuning' object of an earlier bench line: use those choices, no autotuning")
-    ap.add_argument("--serve-seconds", type=float, default=4.0,
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="length of the Poisson arrival window of the serving run (0: skip it)")
+    ap.add_argument("--sweep-seconds", type=float, default=4.0,
+                    help="arrival window of each point of the serving saturation sweep (0: skip it)")
     return ap.parse_args()
 
 
@@ -184,6 +186,9 @@ def peak_hbm():
 # a side stream beside k_inter and k_intra, so the deblocking stage timed
 # after k_intra is the deblocking kernel alone.
 DRAM_BYTES_PER_MB = {"k_inter": 494, "k_intra": 418, "k_deblock_frame": 669}
+# Warp instructions per MB of k_inter on this mix (ncu smsp__inst_executed per
+# launch / MBs of the launch), for the issue-rate line of the roofline.
+K_INTER_WARP_INST_PER_MB = 1876
 
 
 def dist_setup(args):
@@ -430,37 +435,27 @@ def run_bitstream(device, streams=12, repeats=24):
 
 
 SERVE_RES = [("cif", 22, 18, 0.3), ("720p", 80, 45, 0.4), ("1080p", 120, 68, 0.3)]
+# coding modes of the serving configuration: CAVLC IP (CIF-configuration
+# tools), CABAC IBP (1080p-configuration tools), MBAFF CAVLC (frame/field MB
+# pairs, half of them field pairs; 720p is coded 46 MB rows high so that it
+# has whole MB pairs)
+SERVE_MODES = ("cavlc_ip", "cabac_ibp", "mbaff_cavlc")
 
 
-def run_serving(args, device, seed=5000):
-    """Serving: Poisson arrivals of streams at 40 streams/s, resolution drawn
-    from {CIF, 720p, 1080p} with p = {0.3, 0.4, 0.3}, length uniform in
-    [8, 120] pictures, coding structure IP or IBBP, DPBs device-resident and
-    admitted by a 40 GB DPB budget.  Each request replays the records of a
-    pre-generated pool stream of its size and structure (its own DPB, the
-    records shared read-only).  Pictures are pushed as each stream's window
-    of 4 allows and every decoded picture is copied to pinned host memory.
-    Returns aggregate frames/s and the per-picture latency."""
-    import random
-
-    import torch
-
+def serving_pools(seed=5000):
+    """Records of one 120-picture pool stream per resolution and coding mode."""
     import h264_video_decoder_demo_gb300 as h
-
-    rng = random.Random(seed)
     pools = {}
-    jobs = []
-    for res, wmb, hmb, _ in SERVE_RES:
-        for kind in (0, 1):
-            jobs.append((res, wmb, hmb, kind))
     errors = []
 
     def gen(job):
         res, wmb, hmb, kind = job
-        base = "1080p_high" if kind == 1 else "cif_ippp"
+        base = ("cif_ippp", "1080p_high", "1080i_mbaff")[kind]
         over = dict(width_mbs=wmb, height_mbs=hmb, num_pictures=120)
         if kind == 0:
             over.update(gop_kind=0, num_refs=1)
+        if kind == 2:
+            over.update(height_mbs=hmb + (hmb & 1))
         try:
             g = h.synth(base, seed=seed + len(res) * 10 + kind, **over)
             pools[(res, kind)] = (list(g), g.dpb_slots)
@@ -468,25 +463,46 @@ def run_serving(args, device, seed=5000):
         except Exception as exc:  # surfaced below
             errors.append(exc)
 
-    threads = [threading.Thread(target=gen, args=(j,)) for j in jobs]
+    threads = [threading.Thread(target=gen, args=((res, wmb, hmb, kind),))
+               for res, wmb, hmb, _ in SERVE_RES for kind in range(len(SERVE_MODES))]
     for t in threads:
         t.start()
     for t in threads:
         t.join()
     if errors:
         raise errors[0]
+    return pools
+
+
+def run_serving(args, device, pools, rate=40.0, seconds=60.0, seed=5000):
+    """Serving: Poisson arrivals of streams at `rate` streams/s for `seconds`,
+    resolution drawn from {CIF, 720p, 1080p} with p = {0.3, 0.4, 0.3}, length
+    uniform in [8, 120] pictures, coding mode drawn from {CAVLC IP, CABAC IBP,
+    MBAFF CAVLC}, DPBs device-resident and admitted by a 40 GB DPB budget.
+    Each request replays the records of the pool stream of its size and mode
+    (its own DPB, the records shared read-only).  Pictures are pushed as each
+    stream's window of 4 allows and every decoded picture is copied to pinned
+    host memory.  Returns aggregate frames/s and the per-picture latency from
+    push to planes ready on the host."""
+    import random
+
+    import torch
+
+    import h264_video_decoder_demo_gb300 as h
+
+    rng = random.Random(seed)
     # the request schedule
     reqs, t = [], 0.0
     while True:
-        t += rng.expovariate(40.0)
-        if t > args.serve_seconds:
+        t += rng.expovariate(rate)
+        if t > seconds:
             break
         u, acc = rng.random(), 0.0
         for res, wmb, hmb, p in SERVE_RES:
             acc += p
             if u <= acc:
                 break
-        reqs.append((t, res, rng.randint(0, 1), rng.randint(8, 120)))
+        reqs.append((t, res, rng.randint(0, len(SERVE_MODES) - 1), rng.randint(8, 120)))
     window = 4
     free_bufs = {}
 
@@ -494,9 +510,10 @@ def run_serving(args, device, seed=5000):
         lst = free_bufs.setdefault(nbytes, [])
         return lst.pop() if lst else torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
 
-    for res, wmb, hmb, _ in SERVE_RES:  # pinned output buffers, allocated before the clock starts
-        nbytes = wmb * hmb * 384
-        free_bufs[nbytes] = [torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy() for _ in range(96)]
+    for (res, kind), (pics, _) in pools.items():  # pinned output buffers, allocated before the clock starts
+        nbytes = pics[0].plane_bytes
+        if nbytes not in free_bufs:
+            free_bufs[nbytes] = [torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy() for _ in range(96)]
     ctx = h.Context(device, dpb_budget_bytes=40 << 30, max_batch=128)
     srv = h.Server(ctx, queue_depth=window)
     state = []  # per request: [stream id, next picture, ended]
@@ -538,15 +555,38 @@ def run_serving(args, device, seed=5000):
     st = srv.stats()
     srv.close()
     ctx.close()
+    mbs = 0
+    for _, res, kind, n in reqs:
+        pics, _ = pools[(res, kind)]
+        mbs += n * pics[0].width_mbs * pics[0].height_mbs
     return {
-        "fps": round(total / wall, 1), "pictures": total, "streams": len(reqs), "wall_s": round(wall, 3),
+        "fps": round(total / wall, 1), "fps_1080p_equivalent": round(mbs / 8160.0 / wall, 1),
+        "arrival_streams_per_s": rate, "pictures": total, "streams": len(reqs), "wall_s": round(wall, 3),
         "p50_frame_ms": round(st["p50_ms"], 3), "p99_frame_ms": round(st["p99_ms"], 3),
         "max_frame_ms": round(st["max_ms"], 3), "batches": st["batches"],
         "pictures_per_batch": round(st["batch_pictures"] / max(1, st["batches"]), 2),
         "waiting_peak": st["waiting_peak"], "dpb_peak_gb": round(st["dpb_bytes_peak"] / 1e9, 3),
-        "config": "Poisson 40 streams/s for %.1f s, CIF/720p/1080p p=0.3/0.4/0.3, 8..120 pictures, IP or IBBP, "
-                  "40 GB DPB budget, window 4 pictures per stream, outputs to pinned host memory" % args.serve_seconds,
+        "config": "Poisson %g streams/s for %.1f s, CIF/720p/1080p p=0.3/0.4/0.3, 8..120 pictures, modes CAVLC IP / "
+                  "CABAC IBP / MBAFF CAVLC (records of the modes' tools), 40 GB DPB budget, window 4 pictures per "
+                  "stream, outputs to pinned host memory" % (rate, seconds),
     }
+
+
+def run_serving_sweep(args, device, pools, plain_fps):
+    """Serving at rising arrival rates (short windows): the highest served
+    throughput whose push-to-ready p99 stays under 33 ms."""
+    points = []
+    for rate in (80.0, 160.0, 320.0, 480.0):
+        r = run_serving(args, device, pools, rate=rate, seconds=args.sweep_seconds, seed=6000 + int(rate))
+        points.append({k: r[k] for k in ("arrival_streams_per_s", "fps", "fps_1080p_equivalent", "p50_frame_ms",
+                                         "p99_frame_ms", "pictures", "wall_s")})
+    ok = [p for p in points if p["p99_frame_ms"] < 33.0]
+    best = max(ok, key=lambda p: p["fps_1080p_equivalent"]) if ok else None
+    out = {"points": points, "window_s": args.sweep_seconds,
+           "best_under_33ms": best}
+    if best and plain_fps:
+        out["best_1080p_equivalent_over_plain"] = round(best["fps_1080p_equivalent"] / plain_fps, 2)
+    return out
 
 
 def run_engine(args, world, rank, local, dist):
@@ -673,14 +713,20 @@ def run_engine(args, world, rank, local, dist):
     elapsed_ms = start.elapsed_time(end)
     launches = ctx.kernel_launches() - launches0
     graph_replays = ctx.graph_counts()[0] - replays0
-    # kernel times: a separate pass of the same steps with CUDA events around
-    # each kernel on the stream it runs on (launched directly, same shapes)
+    # kernel times: a separate pass of the same steps, one launch sequence in
+    # flight at a time (the device is synchronised after every batch, so no
+    # other pipeline's kernels overlap), k_bs in line, CUDA events around each
+    # kernel on the stream it runs on (launched directly, same shapes)
     kt_steps = 2
     ctx.set_timing(True)
     for _ in range(kt_steps):
-        step()
+        for j, ss, cc, _ in batches:
+            rc = ctx.submit_batch_device(ss, cc)
+            if rc != 0:
+                raise RuntimeError("submit_batch_device: %d %s" % (rc, ctx.last_error()))
+            torch.cuda.synchronize()
     ctx.sync()
-    ktimes, nlaunch = ctx.last_timing()
+    ktimes, nlaunch = ctx.kernel_timing()
     ctx.set_timing(False)
     if dist:
         t = torch.tensor([elapsed_ms], device=dev)
@@ -689,20 +735,41 @@ def run_engine(args, world, rank, local, dist):
     lat = sorted(b[0].elapsed_time(b[1]) for stepev in batch_evs for b in stepev)
     value = world * frames_per_step * args.steps / (elapsed_ms / 1000.0)
 
-    # ---- roofline of the dominant kernel
-    names = ["k_inter", "k_intra", "k_deblock_frame"]
-    dom = int(np.argmax(ktimes))
-    per_kernel_bytes = algo[:3] * kt_steps
-    achieved = per_kernel_bytes[dom] / (ktimes[dom] / 1000.0) / 1e9 if ktimes[dom] > 0 else 0.0
+    # ---- roofline of every kernel; the dominant one is the line's figure.
+    # Algorithmic bytes per step (h264r_picture_bytes): k_inter reads records
+    # + reference samples and writes 384 B per inter MB; k_intra 384 B per
+    # intra MB + records; k_bs reads the MB records (32 B) and motion and
+    # writes its 256-byte strength table per MB; the filter reads and writes
+    # 768 B per deblocked MB and reads its 32-byte record and 256 B of
+    # strengths.
+    names = ["k_inter", "k_intra", "k_bs", "k_deblock_frame"]
+    mbs_step = frames_per_step * 120 * 68
+    motion_step = sum(len(p.motion) for ps in streams_pics for p in ps)
+    bs_bytes = mbs_step * (32 + 256) + motion_step
+    flt_bytes = algo[2] + mbs_step * 256
+    kbytes = [float(algo[0]), float(algo[1]), float(bs_bytes), float(flt_bytes)]
     peak, peak_kind = peak_hbm()
-    mbs_per_launch = frames_per_step * 120 * 68 / len(batches)
-    traffic = int(DRAM_BYTES_PER_MB[names[dom]] * mbs_per_launch)
-    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
+    per_kernel = {}
+    for k, nm in enumerate(names):
+        ms = ktimes[k] / kt_steps
+        gbs = kbytes[k] / (ms / 1000.0) / 1e9 if ms > 0 else 0.0
+        per_kernel[nm] = {"ms_per_step": round(ms, 3), "bytes_per_step": int(kbytes[k]),
+                          "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    dom = int(np.argmax(ktimes))
+    achieved = per_kernel[names[dom]]["achieved_gbs"]
+    mbs_per_launch = mbs_step / len(batches)
+    traffic = int(DRAM_BYTES_PER_MB[names[dom]] * mbs_per_launch) if names[dom] in DRAM_BYTES_PER_MB else None
+    inter_mb_per_s = mbs_step / (ktimes[0] / kt_steps / 1000.0) if ktimes[0] > 0 else 0.0
+    issue_peak = 152 * 4 * 2.07e9  # warp instructions/s: 152 SMs x 4 schedulers x 2.07 GHz
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                 "traffic_note": "ncu DRAM bytes per MB of this kernel on the same mix, scaled to the MBs of one launch",
-                "algorithmic_bytes_per_launch": int(per_kernel_bytes[dom] / (kt_steps * len(batches))),
-                "kernel_ms_per_step": [round(t / kt_steps, 3) for t in ktimes],
-                "kernel_timing": "%d steps after the timed region, CUDA events per kernel" % kt_steps}
+                "algorithmic_bytes_per_launch": int(kbytes[dom] / len(batches)),
+                "per_kernel": per_kernel,
+                "k_inter_issue": {"warp_inst_per_mb": K_INTER_WARP_INST_PER_MB, "mb_per_s": round(inter_mb_per_s, 1),
+                                  "frac_of_issue_peak": round(K_INTER_WARP_INST_PER_MB * inter_mb_per_s / issue_peak, 4)},
+                "kernel_timing": "%d steps after the timed region, one launch sequence in flight at a time, "
+                                 "k_bs in line, CUDA events per kernel" % kt_steps}
 
     extra = {}
     if rank == 0:
@@ -785,7 +852,10 @@ def run_engine(args, world, rank, local, dist):
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": frames_per_step * FRAME_BYTES}
         extra = {"plain_fps": round(plain_fps, 2), "cpu_baseline": cpu, "e2e": e2e, "bit_exact_sample": exact}
         if args.serve_seconds > 0:
-            extra["serving"] = run_serving(args, local)
+            pools = serving_pools()
+            extra["serving"] = run_serving(args, local, pools, rate=40.0, seconds=args.serve_seconds)
+            if args.sweep_seconds > 0:
+                extra["serving_sweep"] = run_serving_sweep(args, local, pools, plain_fps)
         if not args.skip_configs:
             extra["batched_mixed"] = run_mixed(args, local)
             extra["interlaced_mbaff"] = run_interlaced(args, local)
@@ -811,8 +881,8 @@ def run_engine(args, world, rank, local, dist):
                    "pipelines": npipe,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "mb_per_s": round(value * mbs, 1),
-        "p50_frame_ms": round(statistics.median(lat), 3), "p99_frame_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
-        "frame_latency_note": "device time of the batched launch sequence that reconstructs the frame",
+        "p50_batch_ms": round(statistics.median(lat), 3), "p99_batch_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
+        "batch_latency_note": "device time of the batched launch sequence that reconstructs the frame",
         "roofline": roofline,
         "gpu_launches": int(launches),
         "graph_replays": int(graph_replays),
@@ -820,6 +890,11 @@ def run_engine(args, world, rank, local, dist):
         "clocks": clk.summary(),
     }
     out.update(extra)
+    if isinstance(out.get("serving"), dict):
+        out["p50_frame_ms"] = out["serving"]["p50_frame_ms"]
+        out["p99_frame_ms"] = out["serving"]["p99_frame_ms"]
+        out["frame_latency_note"] = ("serving run: per picture, from h264r_server_push to its planes ready in pinned "
+                                     "host memory")
     if out.get("plain_fps"):
         out["batched_over_plain"] = round(value / world / out["plain_fps"], 2)
     return out

@@ -76,8 +76,9 @@ def build_oracle(force=False):
     if force:
         cmd.insert(3, "-B")
     _run(cmd)
-    if os.path.isdir("/root/reference/h264_video_decoder_demo"):
-        _run(["make", "-C", odir, "-s", "-j8", "ref"])
+    # the reference decoder from its own sources, where they are present
+    # (H264R_REFERENCE_DIR, or the recipe's default location)
+    _run(["make", "-C", odir, "-s", "-j8", "ref-if-present"])
     return os.path.join(odir, "liboracle.so")
 
 

@@ -171,9 +171,9 @@ struct h264r_ctx {
     int *h_error = nullptr;  // pinned
     std::atomic<uint64_t> launches{0};
     bool timing = false;
-    double total_ms[3] = {0, 0, 0};
+    double total_ms[4] = {0, 0, 0, 0};  // inter, intra, bS, deblocking filter
     int timed_launches = 0;
-    std::vector<std::array<cudaEvent_t, 4>> ev_free, ev_pending;
+    std::vector<std::array<cudaEvent_t, 5>> ev_free, ev_pending;
     std::mutex timing_mu;
     cudaStream_t batch_stream = nullptr;
     // launch shapes: the default and the autotuner's choice per geometry mix
@@ -181,6 +181,10 @@ struct h264r_ctx {
     h264r_tuning tuning{4, 8, 0, 0};
     std::unordered_map<uint64_t, h264r_tuning> tuned;
     std::atomic<uint64_t> graph_replays{0}, graphs_captured{0};
+    // failure-path tests (h264r_ctx_set_wait_test): spin limit of the
+    // device waits, and whether launches withhold their first rows
+    std::atomic<unsigned long long> spin_limit{kSpinLimit};
+    std::atomic<int> withhold{0};
     LaunchBuf batch_ring[kBatchRing];
     int batch_next = 0;
     std::mutex mu;
@@ -325,9 +329,9 @@ static int drain_timing(h264r_ctx *ctx)
 {
     std::lock_guard<std::mutex> lk(ctx->timing_mu);
     for (auto &q : ctx->ev_pending) {
-        CUDA_OR(ctx, cudaEventSynchronize(q[3]));
+        CUDA_OR(ctx, cudaEventSynchronize(q[4]));
         float ms;
-        for (int k = 0; k < 3; k++) {
+        for (int k = 0; k < 4; k++) {
             cudaEventElapsedTime(&ms, q[k], q[k + 1]);
             ctx->total_ms[k] += ms;
         }
@@ -338,6 +342,14 @@ static int drain_timing(h264r_ctx *ctx)
     return H264R_OK;
 }
 
+extern "C" int h264r_ctx_set_wait_test(h264r_ctx *ctx, uint64_t spin_limit, int withhold_first_rows)
+{
+    if (!ctx) return H264R_ERR_INVALID_ARG;
+    ctx->spin_limit.store(spin_limit ? (unsigned long long)spin_limit : kSpinLimit);
+    ctx->withhold.store(withhold_first_rows ? 1 : 0);
+    return H264R_OK;
+}
+
 extern "C" int h264r_ctx_set_timing(h264r_ctx *ctx, int enable)
 {
     if (!ctx) return H264R_ERR_INVALID_ARG;
@@ -345,7 +357,7 @@ extern "C" int h264r_ctx_set_timing(h264r_ctx *ctx, int enable)
     if (rc) return rc;
     std::lock_guard<std::mutex> lk(ctx->timing_mu);
     ctx->timing = enable != 0;
-    ctx->total_ms[0] = ctx->total_ms[1] = ctx->total_ms[2] = 0;
+    ctx->total_ms[0] = ctx->total_ms[1] = ctx->total_ms[2] = ctx->total_ms[3] = 0;
     ctx->timed_launches = 0;
     return H264R_OK;
 }
@@ -355,16 +367,28 @@ extern "C" int h264r_ctx_last_timing(h264r_ctx *ctx, float t[3], int *launches)
     if (!ctx || !t) return H264R_ERR_INVALID_ARG;
     int rc = drain_timing(ctx);
     if (rc) return rc;
-    for (int k = 0; k < 3; k++) t[k] = (float)ctx->total_ms[k];
+    t[0] = (float)ctx->total_ms[0];
+    t[1] = (float)ctx->total_ms[1];
+    t[2] = (float)(ctx->total_ms[2] + ctx->total_ms[3]);
     if (launches) *launches = ctx->timed_launches;
     return H264R_OK;
 }
 
-static std::array<cudaEvent_t, 4> *take_events(h264r_ctx *ctx)
+extern "C" int h264r_ctx_kernel_timing(h264r_ctx *ctx, float t[4], int *launches)
+{
+    if (!ctx || !t) return H264R_ERR_INVALID_ARG;
+    int rc = drain_timing(ctx);
+    if (rc) return rc;
+    for (int k = 0; k < 4; k++) t[k] = (float)ctx->total_ms[k];
+    if (launches) *launches = ctx->timed_launches;
+    return H264R_OK;
+}
+
+static std::array<cudaEvent_t, 5> *take_events(h264r_ctx *ctx)
 {
     std::lock_guard<std::mutex> lk(ctx->timing_mu);
     if (ctx->ev_free.empty()) {
-        std::array<cudaEvent_t, 4> q;
+        std::array<cudaEvent_t, 5> q;
         for (auto &e : q) cudaEventCreate(&e);
         ctx->ev_free.push_back(q);
     }
@@ -636,7 +660,7 @@ struct Seq {
 // Enqueue the descriptor upload and the kernels of one launch sequence on cs
 // (directly, or into a stream capture); *kernels receives how many kernels.
 static int enqueue_sequence(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const Seq &q, cudaStream_t side,
-                            const std::array<cudaEvent_t, 4> *ev, uint32_t *kernels)
+                            const std::array<cudaEvent_t, 5> *ev, uint32_t *kernels)
 {
     uint32_t nk = 0;
     CUDA_OR(ctx, cudaMemcpyAsync(b.dev, b.host, q.total, cudaMemcpyHostToDevice, cs));
@@ -675,6 +699,9 @@ static int enqueue_sequence(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const
             h264r::k_bs<<<bs_grid, 128, 0, cs>>>(q.dd, q.n, (uint32_t)q.mbs, q.st);
             nk++;
         }
+    }
+    if (ev) cudaEventRecord((*ev)[3], cs);
+    if (q.any_deblock) {
         if (q.dbf_units) {
             if (q.dbf_w == 4)
                 h264r::k_deblock_frame4<<<q.dbf_units, 128, 0, cs>>>(q.dd, q.n, q.dbf_units, q.st);
@@ -687,7 +714,7 @@ static int enqueue_sequence(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const
             nk++;
         }
     }
-    if (ev) cudaEventRecord((*ev)[3], cs);
+    if (ev) cudaEventRecord((*ev)[4], cs);
     *kernels = nk;
     return H264R_OK;
 }
@@ -795,11 +822,21 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
         row_base += p.units_h;
         prog += 3 * p.units_h;
     }
+    const bool withhold = ctx->withhold.load() != 0;
+    if (withhold) {
+        // the wavefronts' first tickets are never handed out: the first
+        // picture's first intra row and first deblocking blocks do not run,
+        // so the rows below them wait on progress that is never published
+        unsigned int *t = (unsigned int *)(b.host + ticket_off);
+        t[0] = 1;
+        t[1] = 2;
+        t[2] = 2;
+    }
     Seq q;
     q.dd = (const PicDesc *)b.dev;
     q.st.error = ctx->d_error;
     q.st.ticket = (unsigned int *)(b.dev + ticket_off);
-    q.st.spin_limit = kSpinLimit;
+    q.st.spin_limit = ctx->spin_limit.load();
     q.n = n;
     q.total = total;
     q.mbs = mbs;
@@ -809,7 +846,8 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
     q.any_intra = any_intra;
     q.any_deblock = false;
     for (auto &it : items) q.any_deblock = q.any_deblock || it.pic->deblock;
-    q.bs_aside = q.any_deblock && db_base == 0;
+    // kernel timing keeps k_bs in line, so that each kernel is timed alone
+    q.bs_aside = q.any_deblock && db_base == 0 && !ctx->timing;
     q.inter_w = tune.inter_mbs_per_cta;
     q.dbf_w = tune.deblock_pairs_per_cta;
     cudaStream_t side = items[0].s->side;
@@ -817,7 +855,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
     GraphEntry *g = nullptr;
     // no graph of our own inside a capture the caller is making of cs
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    if (tune.graphs && !ctx->timing && cudaStreamIsCapturing(cs, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
+    if (tune.graphs && !ctx->timing && !withhold && cudaStreamIsCapturing(cs, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
         GraphKey key;
         memset(&key, 0, sizeof(key));
         key.host = b.host;
@@ -859,7 +897,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
         ctx->launches += g->kernels;
         ctx->graph_replays++;
     } else {
-        std::array<cudaEvent_t, 4> ev{};
+        std::array<cudaEvent_t, 5> ev{};
         if (ctx->timing) ev = *take_events(ctx);
         rc = enqueue_sequence(ctx, cs, b, q, side, ctx->timing ? &ev : nullptr, &nk);
         if (rc) return rc;

@@ -128,11 +128,22 @@ extern "C" int h264r_deblock_picture_noalloc(const h264r_picture *pic, uint8_t *
     st.error = &s->error;
     st.ticket = s->ticket;
     st.spin_limit = kNoAllocSpinLimit;
+    // An error left by the caller's earlier work is reported without being
+    // cleared (it is not this call's); once none is pending, an error seen
+    // right after a launch belongs to that launch.
+    if (cudaPeekAtLastError() != cudaSuccess) return H264R_ERR_CUDA;
     k_noalloc_init<<<1, 256, 0, cs>>>(d, s);
-    h264r::k_bs<<<(pic->num_mbs + 3) / 4, 128, 0, cs>>>(&s->desc, 1, pic->num_mbs, st);
-    if (d.dbf_units) h264r::k_deblock_frame<<<d.dbf_units, 32 * h264r::kDbWarps, 0, cs>>>(&s->desc, 1, d.dbf_units, st);
-    if (d.db_units) h264r::k_deblock<<<d.db_units, 32 * h264r::kMbWarps, 0, cs>>>(&s->desc, 1, d.db_units, st);
     if (cudaGetLastError() != cudaSuccess) return H264R_ERR_CUDA;
+    h264r::k_bs<<<(pic->num_mbs + 3) / 4, 128, 0, cs>>>(&s->desc, 1, pic->num_mbs, st);
+    if (cudaGetLastError() != cudaSuccess) return H264R_ERR_CUDA;
+    if (d.dbf_units) {
+        h264r::k_deblock_frame<<<d.dbf_units, 32 * h264r::kDbWarps, 0, cs>>>(&s->desc, 1, d.dbf_units, st);
+        if (cudaGetLastError() != cudaSuccess) return H264R_ERR_CUDA;
+    }
+    if (d.db_units) {
+        h264r::k_deblock<<<d.db_units, 32 * h264r::kMbWarps, 0, cs>>>(&s->desc, 1, d.db_units, st);
+        if (cudaGetLastError() != cudaSuccess) return H264R_ERR_CUDA;
+    }
     int herr = 0;
     if (cudaMemcpyAsync(&herr, &s->error, sizeof(int), cudaMemcpyDeviceToHost, cs) != cudaSuccess) return H264R_ERR_CUDA;
     if (cudaStreamSynchronize(cs) != cudaSuccess) return H264R_ERR_CUDA;

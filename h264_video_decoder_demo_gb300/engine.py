@@ -24,7 +24,7 @@ EXPORTS = [
     "h264r_submit_picture_device", "h264r_submit_batch_device", "h264r_output", "h264r_output_async",
     "h264r_load_slot", "h264r_slot_device_ptr", "h264r_stream_sync", "h264r_ctx_sync",
     "h264r_stream_cuda_stream", "h264r_stream_output_cuda_stream", "h264r_validate_picture", "h264r_ctx_kernel_launches",
-    "h264r_ctx_set_timing", "h264r_ctx_last_timing",
+    "h264r_ctx_set_timing", "h264r_ctx_last_timing", "h264r_ctx_kernel_timing", "h264r_ctx_set_wait_test",
     "h264r_synth_create", "h264r_synth_dpb_slots", "h264r_synth_next", "h264r_synth_destroy",
     "h264r_submit_batch", "h264r_picture_bytes", "h264r_ctx_cuda_stream",
     "h264r_deblock_picture_noalloc",
@@ -92,6 +92,8 @@ def _load():
         "h264r_validate_picture": (i32, [P(R.CPicture), i32]),
         "h264r_ctx_kernel_launches": (u64, [vp]),
         "h264r_ctx_set_timing": (i32, [vp, i32]),
+        "h264r_ctx_set_wait_test": (i32, [vp, u64, i32]),
+        "h264r_ctx_kernel_timing": (i32, [vp, P(ctypes.c_float), P(i32)]),
         "h264r_ctx_last_timing": (i32, [vp, P(ctypes.c_float), P(i32)]),
         "h264r_submit_batch": (i32, [vp, i32, P(vp), P(R.CPicture)]),
         "h264r_picture_bytes": (i32, [P(R.CPicture), P(ctypes.c_uint64)]),
@@ -218,11 +220,26 @@ class Context:
     def set_timing(self, on):
         self.check(lib().h264r_ctx_set_timing(self.h, 1 if on else 0), "set_timing")
 
+    def set_wait_test(self, spin_limit=0, withhold_first_rows=False):
+        """Failure-path tests: a small device spin limit and/or launches that
+        withhold their wavefronts' first rows (h264r_ctx_set_wait_test);
+        set_wait_test() restores normal operation."""
+        self.check(lib().h264r_ctx_set_wait_test(self.h, int(spin_limit), 1 if withhold_first_rows else 0),
+                   "set_wait_test")
+
     def last_timing(self):
         """(summed ms of [inter, intra, deblock], launch sequences) since set_timing(True)."""
         t = (ctypes.c_float * 3)()
         n = ctypes.c_int()
         self.check(lib().h264r_ctx_last_timing(self.h, t, ctypes.byref(n)), "last_timing")
+        return list(t), n.value
+
+    def kernel_timing(self):
+        """(summed ms of [k_inter, k_intra, k_bs, deblocking filter], launch
+        sequences) since set_timing(True); k_bs runs in line while timing."""
+        t = (ctypes.c_float * 4)()
+        n = ctypes.c_int()
+        self.check(lib().h264r_ctx_kernel_timing(self.h, t, ctypes.byref(n)), "kernel_timing")
         return list(t), n.value
 
     def sync(self):

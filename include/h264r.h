@@ -384,6 +384,32 @@ uint64_t h264r_ctx_kernel_launches(const h264r_ctx *ctx);
  * of launch sequences summed. */
 int  h264r_ctx_set_timing(h264r_ctx *ctx, int enable);
 int  h264r_ctx_last_timing(h264r_ctx *ctx, float t[3], int *launches);
+/* The same totals per kernel: t[0] k_inter, t[1] k_intra, t[2] k_bs,
+ * t[3] the deblocking filter kernels.  While timing is on, k_bs runs in line
+ * on the batch's stream (not beside k_inter / k_intra), so that with one
+ * launch sequence in flight at a time each kernel is timed alone. */
+int  h264r_ctx_kernel_timing(h264r_ctx *ctx, float t[4], int *launches);
+
+/*
+ * Failure-path tests.  The reference's error convention is to print and
+ * return a negative code (RETURN_IF_FAILED, CommonFunction.h:40-47); the
+ * engine's device-side equivalent is a bounded wait that records
+ * H264R_ERR_DEVICE_TIMEOUT and returns.  This makes such a wait run out on
+ * purpose, without a fault or a hang:
+ *   spin_limit           iterations a device wait may spin before it gives
+ *                        up (0: the default, ~seconds)
+ *   withhold_first_rows  non-zero: later launches do not hand out the first
+ *                        tickets of the intra and deblocking wavefronts, so
+ *                        the first picture's first row (block of rows) never
+ *                        runs and the rows below it wait on progress that is
+ *                        never published; with a small spin_limit the
+ *                        launch ends with every kernel returned, and
+ *                        h264r_stream_sync / h264r_ctx_sync report
+ *                        H264R_ERR_DEVICE_TIMEOUT once
+ * h264r_ctx_set_wait_test(ctx, 0, 0) restores normal operation; the context
+ * stays usable.  Not for production use.
+ */
+int  h264r_ctx_set_wait_test(h264r_ctx *ctx, uint64_t spin_limit, int withhold_first_rows);
 
 /* ---- launch shapes, captured launch graphs, autotuner ------------------ */
 /*

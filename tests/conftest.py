@@ -15,6 +15,21 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs on the GB300 box)")
 
 
+def reference_dir():
+    """The reference checkout: $H264R_REFERENCE_DIR, else where the oracle
+    recipe (oracle/Makefile, print-ref) expects it."""
+    env = os.environ.get("H264R_REFERENCE_DIR")
+    if env:
+        return env
+    import subprocess
+    try:
+        out = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "print-ref"], stdout=subprocess.PIPE,
+                             stderr=subprocess.DEVNULL, text=True, check=True).stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return ""
+    return out.splitlines()[-1] if out else ""
+
+
 def fixture_names():
     return sorted(os.path.basename(p)[:-len(".h264r.gz")] for p in glob.glob(os.path.join(HERE, "golden", "*.h264r.gz")))
 

@@ -37,6 +37,7 @@ import tempfile
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.dirname(HERE))
+from conftest import reference_dir  # noqa: E402
 from h264r_dump import read_dump, write_dump  # noqa: E402
 
 # (fixture name, stream file, pictures kept, coding tools covered)
@@ -155,7 +156,7 @@ def make_bitstream_fixtures(ref_data, tmp):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-data", default="/root/reference/data")
+    ap.add_argument("--ref-data", default=os.path.join(reference_dir(), "data"))
     ap.add_argument("--bitstreams-only", action="store_true", help="only the cut streams and their frame md5s")
     args = ap.parse_args()
     dumper = os.path.join(ROOT, "oracle", "_ref", "ref_dump")

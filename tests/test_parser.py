@@ -23,8 +23,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 sys.path.insert(0, ROOT)
 
-REF_DATA = "/root/reference/data"
-REF_SRC = "/root/reference/h264_video_decoder_demo"
+from conftest import reference_dir
+
+REF_DATA = os.path.join(reference_dir(), "data")
+REF_SRC = os.path.join(reference_dir(), "h264_video_decoder_demo")
 ORACLE = os.path.join(ROOT, "oracle")
 PROBE = os.path.join(ORACLE, "_ref", "libref_probe.so")
 DUMPER = os.path.join(ORACLE, "_ref", "ref_dump")

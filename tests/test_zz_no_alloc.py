@@ -32,11 +32,17 @@ def device_picture(pic, keep):
     return c
 
 
-def test_noalloc_deblock_matches_engine_two_calls(gpu_ctx):
+@pytest.mark.parametrize("workload,seed", [("1080p_high", 77), ("1080i_mbaff", 78)])
+def test_noalloc_deblock_matches_engine_two_calls(gpu_ctx, workload, seed):
+    """Frame pictures go through the frame deblocking kernel; MBAFF pictures
+    (half the MB pairs field pairs) through the MB-pair-row kernel, whose
+    progress counters span three per pair row."""
     import torch
     lib = h.lib()
-    gen = h.synth("1080p_high", seed=77, num_pictures=4)
+    gen = h.synth(workload, seed=seed, num_pictures=4)
     pics = list(gen)
+    if workload == "1080i_mbaff":
+        assert all(p.mbaff for p in pics)
     s = h.Stream(gpu_ctx, pics[0].width_mbs, pics[0].height_mbs, gen.dpb_slots)
     keep = []
     try:
