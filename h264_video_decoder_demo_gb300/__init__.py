@@ -6,7 +6,8 @@ whole-stream decoder of include/h264r_decoder.h); this package builds it
 in-tree and binds it for Python callers (tests, benchmarks, serving loop).
 """
 from . import records  # noqa: F401
-from .engine import Context, Decoder, EngineError, Order, Parser, Server, Stream, Synth, lib, synth, validate  # noqa: F401
+from .engine import (Context, Decoder, EngineError, Order, Parser, Server, Stream, Synth, lib, synth,  # noqa: F401
+                     validate, write_stream)
 
 __all__ = ["records", "Context", "Decoder", "Parser", "Order", "Server", "Stream", "Synth", "EngineError", "lib",
-           "synth", "validate"]
+           "synth", "validate", "write_stream"]

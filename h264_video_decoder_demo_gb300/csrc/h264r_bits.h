@@ -136,4 +136,70 @@ struct BitReader {
     bool more_rbsp_data() const { return pos < stop; }
 };
 
+// RBSP bit writing for the seeded bitstream writer: fixed-length,
+// Exp-Golomb (9.1) and trailing bits.  `buf` always holds every bit written
+// so far, the last byte zero-padded, so a BitReader can read it back in place.
+struct BitWriter {
+    std::vector<uint8_t> buf;
+    size_t nbits = 0;
+
+    // k (0..32) bits of v, most significant first
+    void u(int k, uint32_t v)
+    {
+        for (int i = k - 1; i >= 0; i--) {
+            if ((nbits & 7) == 0) buf.push_back(0);
+            if ((v >> i) & 1u) buf.back() |= (uint8_t)(0x80u >> (nbits & 7));
+            nbits++;
+        }
+    }
+    void flag(bool b) { u(1, b ? 1u : 0u); }
+    void ue(uint32_t v)
+    {
+        const uint64_t k = (uint64_t)v + 1;
+        int len = 0;
+        while ((k >> len) > 1) len++;
+        u(len, 0);
+        // the code is len zeros, then k in len + 1 bits
+        if (len >= 32) {
+            u(1, 1);
+            u(len, (uint32_t)(k & 0xFFFFFFFFu));
+        } else {
+            u(len + 1, (uint32_t)k);
+        }
+    }
+    void se(int32_t v) { ue(v > 0 ? (uint32_t)(2 * (int64_t)v - 1) : (uint32_t)(-2 * (int64_t)v)); }
+    // te(v) (7.4.3 ref_idx): one inverted bit when the range is 1
+    void te(int range, uint32_t v)
+    {
+        if (range > 1) ue(v);
+        else u(1, v ^ 1u);
+    }
+    bool byte_aligned() const { return (nbits & 7) == 0; }
+    // rbsp_trailing_bits( ): the stop bit, then zeros to a byte boundary
+    void trailing()
+    {
+        u(1, 1);
+        while (!byte_aligned()) u(1, 0);
+    }
+};
+
+// NAL unit in Annex B form: start code, header byte, payload with an
+// emulation_prevention_three_byte after every two zero bytes that precede a
+// byte <= 3 (7.4.1)
+inline void put_nal(std::vector<uint8_t> &out, int nal_ref_idc, int nal_unit_type, const uint8_t *rbsp, size_t n)
+{
+    static const uint8_t start[4] = {0, 0, 0, 1};
+    out.insert(out.end(), start, start + 4);
+    out.push_back((uint8_t)(((nal_ref_idc & 3) << 5) | (nal_unit_type & 31)));
+    int zeros = 0;
+    for (size_t i = 0; i < n; i++) {
+        if (zeros >= 2 && rbsp[i] <= 3) {
+            out.push_back(3);
+            zeros = 0;
+        }
+        out.push_back(rbsp[i]);
+        zeros = rbsp[i] == 0 ? zeros + 1 : 0;
+    }
+}
+
 }  // namespace h264r

@@ -310,6 +310,93 @@ int cavlc_residual_sparse(BitReader &br, int nC, int start, int end, int max_coe
     return 0;
 }
 
+// ---------------------------------------------------------------- writing
+// The inverse of the decoding above, for the seeded bitstream writer: the
+// same code tables, read as bit strings.
+
+static void put_code(BitWriter &bw, const char *code)
+{
+    for (const char *c = code; *c; c++) bw.u(1, *c == '1' ? 1u : 0u);
+}
+
+int cbp_to_code(int cbp, bool intra)
+{
+    for (int code = 0; code < 48; code++)
+        if (kCbpMap[code][intra ? 0 : 1] == cbp) return code;
+    return -1;
+}
+
+// residual_block_cavlc( ) of the levels coeff[start..end] (scan positions;
+// max_coeff as in the syntax: 4 for 4:2:0 chroma DC, 15 for AC lists, 16
+// otherwise).  Returns TotalCoeff, or -1 for a level outside the range the
+// escape codes of a non-High profile carry.
+int cavlc_write_block(BitWriter &bw, int nC, int start, int end, int max_coeff, const int *coeff)
+{
+    int level[16], run[16], total = 0;
+    // highest frequency first; run[i] = zeros between level i and level i + 1
+    int last = -1, hi = -1;
+    for (int k = end; k >= start; k--) {
+        if (!coeff[k]) continue;
+        if (hi < 0) hi = k;
+        level[total] = coeff[k];
+        if (total > 0) run[total - 1] = last - k - 1;
+        last = k;
+        total++;
+    }
+    int t1 = 0;
+    while (t1 < total && t1 < 3 && (level[t1] == 1 || level[t1] == -1)) t1++;
+    // coeff_token
+    if (nC == -1) {
+        put_code(bw, kCoeffToken[3][total][t1]);
+    } else if (nC >= 8) {
+        if (total == 0) put_code(bw, "000011");
+        else bw.u(6, (uint32_t)(((total - 1) << 2) | t1));
+    } else {
+        put_code(bw, kCoeffToken[nC < 2 ? 0 : (nC < 4 ? 1 : 2)][total][t1]);
+    }
+    if (total == 0) return 0;
+    int suffix_len = (total > 10 && t1 < 3) ? 1 : 0;
+    for (int i = 0; i < total; i++) {
+        const int v = level[i];
+        if (i < t1) {
+            bw.u(1, v < 0 ? 1u : 0u);
+            continue;
+        }
+        int code = v > 0 ? 2 * v - 2 : -2 * v - 1;
+        if (i == t1 && t1 < 3) code -= 2;
+        int prefix, ssize, suffix;
+        if (suffix_len == 0) {
+            if (code < 14) {
+                prefix = code, ssize = 0, suffix = 0;
+            } else if (code < 30) {
+                prefix = 14, ssize = 4, suffix = code - 14;
+            } else {
+                prefix = 15, ssize = 12, suffix = code - 30;
+            }
+        } else if (code < (15 << suffix_len)) {
+            prefix = code >> suffix_len, ssize = suffix_len, suffix = code & ((1 << suffix_len) - 1);
+        } else {
+            prefix = 15, ssize = 12, suffix = code - (15 << suffix_len);
+        }
+        if (suffix >= 4096) return -1;
+        bw.u(prefix, 0);
+        bw.u(1, 1);
+        if (ssize) bw.u(ssize, (uint32_t)suffix);
+        if (suffix_len == 0) suffix_len = 1;
+        const int a = v < 0 ? -v : v;
+        if (a > (3 << (suffix_len - 1)) && suffix_len < 6) suffix_len++;
+    }
+    // total_zeros: the zeros below the highest non-zero level
+    int zeros = hi - start + 1 - total;
+    if (total < end - start + 1)
+        put_code(bw, max_coeff == 4 ? kTotalZerosDc[total - 1][zeros] : kTotalZeros[total - 1][zeros]);
+    for (int i = 0; i < total - 1 && zeros > 0; i++) {
+        put_code(bw, kRunBefore[(zeros < 7 ? zeros : 7) - 1][run[i]]);
+        zeros -= run[i];
+    }
+    return total;
+}
+
 }  // namespace h264r
 
 // ---- table probes (tests compare them with the reference's decoders)

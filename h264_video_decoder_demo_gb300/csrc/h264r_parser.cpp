@@ -342,7 +342,7 @@ int MbDecoder::decode()
         cur->cls = H264R_MB_IPCM;
         r.aux = (uint32_t)(P.pcm.size() / 384);
         for (int i = 0; i < 384; i++) P.pcm.push_back((uint8_t)br.u(8));
-        for (int i = 0; i < 16; i++) cur->tc[i] = 16;
+        // non-zero counts stay 0 (see total_of: the reference's nN of an I_PCM MB)
         r.qpy = (uint8_t)qp;
         if (br.err) return P.fail(H264R_ERR_BAD_RECORD, "truncated I_PCM (MB %d)", addr);
         P.rec[addr] = r;

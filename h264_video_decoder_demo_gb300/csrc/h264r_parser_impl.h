@@ -280,7 +280,11 @@ struct MbDecoder {
     {
         const MbState &m = P.mbs[n];
         if (m.skip) return 0;
-        if (m.cls == H264R_MB_IPCM) return 16;
+        // 9.2.1 gives an I_PCM neighbour nN = 16; the reference compares the
+        // MB's type number (25) with its enum value of I_PCM (26,
+        // H264ResidualBlockCavlc.cpp:497 / 532, H264CommonFunc.h:183-210), so
+        // the test never holds and it reads the PCM MB's non-zero counts,
+        // which it leaves at zero: an I_PCM neighbour counts as 0 here too
         return chroma ? m.tcc[comp][b] : m.tc[b];
     }
 
@@ -323,8 +327,19 @@ struct MbDecoder {
         if (n < 0) return r;
         const int bi = (yW >> 2) * 4 + (xW >> 2);
         if (n == addr) {
-            if (!decoded4x4[bi]) return r;
+            // 6.4.11.7 marks a partition of the current MB that is not yet
+            // decoded as not available (C is then replaced by D); the
+            // reference leaves that rule out (commented out at
+            // H264InterPrediction.cpp:3158-3165) and reads the partition's
+            // motion as stored so far: the MB record is cleared per picture
+            // and a partition's prediction flags and vectors are written only
+            // once it is derived (H264InterPrediction.cpp:592-603), so such a
+            // C neighbour is available with no prediction from this list.  It
+            // happens for sub-macroblock partitions whose top-right
+            // neighbour lies in the next 8x8 quadrant (8x4 / 4x4 partitions
+            // in the lower half of quadrants 0 and 2).
             r.avail = true;
+            if (!decoded4x4[bi]) return r;
             r.ref = blk[bi].ref[list];
             if (r.ref >= 0) {
                 r.mv[0] = blk[bi].mv[list][0];

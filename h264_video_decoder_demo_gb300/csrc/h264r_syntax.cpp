@@ -235,8 +235,13 @@ int parse_pps(BitReader &br, const Sps *sps_table, Pps &pps, const char **why)
             q.scaling_present = true;
             read_lists(br, 6 + (sps.chroma_format_idc != 3 ? 2 : 6) * q.transform_8x8_mode, q.sl4, q.sl8, sps.sl4, sps.sl8,
                        q.sl_present);
+            // second_chroma_qp_index_offset follows the scaling lists for
+            // every PPS in 7.3.2.2; the reference reads it only inside the
+            // pic_scaling_matrix_present_flag branch (H264PPS.cpp:206-227)
+            // and otherwise keeps chroma_qp_index_offset, which is followed
+            // here so that Cr is reconstructed as the reference does
+            q.chroma_qp_offset[1] = br.se();
         }
-        q.chroma_qp_offset[1] = br.se();
     }
     if (br.err) FAIL("truncated picture parameter set");
     if (q.num_ref_idx_default[0] > 32 || q.num_ref_idx_default[1] > 32 || q.weighted_bipred_idc > 2 ||

@@ -41,7 +41,7 @@ EXPORTS = [
     "h264r_probe_coeff_token", "h264r_probe_total_zeros", "h264r_probe_run_before", "h264r_probe_cbp",
     "h264r_decoder_create", "h264r_decoder_destroy", "h264r_decoder_last_error", "h264r_decoder_set_callback",
     "h264r_decoder_push", "h264r_decoder_flush", "h264r_decoder_open", "h264r_decoder_decoded",
-    "h264r_decoder_output",
+    "h264r_decoder_output", "h264r_write_stream", "h264r_writer_free", "h264r_writer_last_error",
 ]
 
 
@@ -94,6 +94,9 @@ def _load():
         "h264r_ctx_set_timing": (i32, [vp, i32]),
         "h264r_ctx_set_wait_test": (i32, [vp, u64, i32]),
         "h264r_ctx_kernel_timing": (i32, [vp, P(ctypes.c_float), P(i32)]),
+        "h264r_write_stream": (i32, [P(R.CWriterCfg), P(P(ctypes.c_uint8)), P(ctypes.c_size_t)]),
+        "h264r_writer_free": (None, [P(ctypes.c_uint8)]),
+        "h264r_writer_last_error": (ctypes.c_char_p, []),
         "h264r_ctx_last_timing": (i32, [vp, P(ctypes.c_float), P(i32)]),
         "h264r_submit_batch": (i32, [vp, i32, P(vp), P(R.CPicture)]),
         "h264r_picture_bytes": (i32, [P(R.CPicture), P(ctypes.c_uint64)]),
@@ -746,3 +749,44 @@ def synth(name, seed=1, **over):
     kw = dict(WORKLOADS[name])
     kw.update(over)
     return Synth(seed=seed, **kw)
+
+
+# named bitstream configurations of the seeded writer (include/h264r_writer.h):
+# the reference's benchmark configurations as CAVLC Annex B streams
+STREAMS = {
+    # CIF 352x288, 8 pictures IPPP, Baseline CAVLC, one slice, 1 reference,
+    # partitions 16x16 / 16x8 / 8x16 / 8x8, MVs +-64 qpel, QP 20..36, 10% intra
+    "cif_ippp": dict(width_mbs=22, height_mbs=18, num_pictures=8, profile_idc=66, gop_length=0, b_pictures=0,
+                     num_refs=1, transform8x8=0, weighted=0, direct_spatial=1, min_partition=2, intra_percent=10,
+                     skip_percent=5, edge_mv_percent=0, qp_min=20, qp_max=36, filter_offset_max=0,
+                     coef_density=40, slices=1, pcm_permille=0, chroma_qp_offset_max=0, mv_range=64),
+    # 1080p High (coded 1920x1088), 30 pictures, GOP 15 IBBP, 8x8 transforms,
+    # partitions down to 4x4, up to 4 references, explicit weighted prediction
+    # (weights -64..127, every bi-predictive sum <= 128, offsets +-32), spatial
+    # direct, MVs +-256 qpel with 5% past the edges, QP 22..40, alpha / beta
+    # offsets +-6; CAVLC (the writer has no CABAC)
+    "1080p_high": dict(width_mbs=120, height_mbs=68, num_pictures=30, profile_idc=100, gop_length=15, b_pictures=2,
+                       num_refs=4, transform8x8=1, weighted=1, direct_spatial=1, min_partition=3, intra_percent=5,
+                       skip_percent=10, edge_mv_percent=5, qp_min=22, qp_max=40, filter_offset_max=6,
+                       coef_density=40, slices=1, pcm_permille=2, chroma_qp_offset_max=3, mv_range=256),
+}
+
+
+def write_stream(name=None, seed=1, **over):
+    """Annex B bytes of a seeded stream (h264r_write_stream): a named
+    configuration of STREAMS with fields overridden, or fields alone."""
+    kw = dict(STREAMS[name]) if name else {}
+    kw.update(over)
+    cfg = R.CWriterCfg()
+    cfg.seed = seed
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    data = ctypes.POINTER(ctypes.c_uint8)()
+    size = ctypes.c_size_t()
+    rc = lib().h264r_write_stream(ctypes.byref(cfg), ctypes.byref(data), ctypes.byref(size))
+    if rc != 0:
+        raise EngineError(rc, "h264r_write_stream: %s" % lib().h264r_writer_last_error().decode())
+    try:
+        return ctypes.string_at(data, size.value)
+    finally:
+        lib().h264r_writer_free(data)

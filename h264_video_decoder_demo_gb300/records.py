@@ -181,6 +181,20 @@ class CSynthCfg(ctypes.Structure):
                 ("slice_rows", ctypes.c_uint8), ("cip_percent", ctypes.c_uint8)]
 
 
+class CWriterCfg(ctypes.Structure):
+    """struct h264r_writer_cfg (include/h264r_writer.h)"""
+    _fields_ = [("seed", ctypes.c_uint32), ("width_mbs", ctypes.c_uint16), ("height_mbs", ctypes.c_uint16),
+                ("num_pictures", ctypes.c_uint16), ("profile_idc", ctypes.c_uint8), ("level_idc", ctypes.c_uint8),
+                ("gop_length", ctypes.c_uint8), ("b_pictures", ctypes.c_uint8), ("num_refs", ctypes.c_uint8),
+                ("transform8x8", ctypes.c_uint8), ("weighted", ctypes.c_uint8), ("direct_spatial", ctypes.c_uint8),
+                ("min_partition", ctypes.c_uint8), ("intra_percent", ctypes.c_uint8),
+                ("skip_percent", ctypes.c_uint8), ("edge_mv_percent", ctypes.c_uint8), ("qp_min", ctypes.c_uint8),
+                ("qp_max", ctypes.c_uint8), ("filter_offset_max", ctypes.c_uint8), ("coef_density", ctypes.c_uint8),
+                ("slices", ctypes.c_uint8), ("pcm_permille", ctypes.c_uint8),
+                ("chroma_qp_offset_max", ctypes.c_uint8), ("reserved", ctypes.c_uint8 * 3),
+                ("mv_range", ctypes.c_uint16), ("reserved2", ctypes.c_uint16)]
+
+
 class CServerCfg(ctypes.Structure):
     """struct h264r_server_cfg (include/h264r_server.h)"""
     _fields_ = [("max_batch_pictures", ctypes.c_uint32), ("queue_depth", ctypes.c_uint32),

@@ -15,7 +15,8 @@ from conftest import ROOT, load_fixture
 
 def declared_symbols():
     names = set()
-    for hdr in ("h264r.h", "h264r_synth.h", "h264r_server.h", "h264r_order.h", "h264r_parser.h", "h264r_decoder.h"):
+    for hdr in ("h264r.h", "h264r_synth.h", "h264r_server.h", "h264r_order.h", "h264r_parser.h", "h264r_decoder.h",
+                "h264r_writer.h"):
         with open(os.path.join(ROOT, "include", hdr)) as f:
             src = f.read()
         names |= set(re.findall(r"\b(h264r_[a-z0-9_]+)\s*\(", src))
