@@ -770,12 +770,15 @@ int h264r_parser::mark_references(const SliceHeader &sh, const Sps &s)
             n_long += p.long_ref;
         }
         if (n_short + n_long >= std::max(s.max_num_ref_frames, 1) && n_short > 0) {
+            // the smallest FrameNumWrap as last derived: the reference derives
+            // it only while building the lists of a P or B slice
+            // (H264RefPicList.cpp:339-349) and compares those stored values
+            // (H264RefPicList.cpp:1660-1676), so a picture decoded after the
+            // last list construction still has its initial 0 (build_lists
+            // keeps frame_num_wrap the same way)
             Pic *oldest = nullptr;
             for (Pic &p : dpb)
-                if (p.short_ref) {
-                    p.frame_num_wrap = p.frame_num > sh.frame_num ? p.frame_num - max_frame_num : p.frame_num;
-                    if (!oldest || p.frame_num_wrap < oldest->frame_num_wrap) oldest = &p;
-                }
+                if (p.short_ref && (!oldest || p.frame_num_wrap < oldest->frame_num_wrap)) oldest = &p;
             oldest->short_ref = false;
         }
     }
@@ -820,7 +823,13 @@ int h264r_parser::start_picture(const SliceHeader &sh, const Sps &s, const Pps &
     if (!s.frame_mbs_only && s.mbaff) return fail(H264R_ERR_UNSUPPORTED, "MBAFF frames");
     cur = Pic();
     cur.uid = next_uid++;
-    cur.frame_num = sh.frame_num;
+    // FrameNum of the picture as a reference: the reference decoder assigns
+    // it (from frame_num) only while it builds reference lists, i.e. in P and
+    // B slices (H264RefPicList.cpp:334, reached from H264RefPicList.cpp:284
+    // for P / B slices only); a picture of I slices keeps FrameNum 0, so a
+    // non-IDR I picture sorts last in P lists and is the first one the
+    // sliding window drops.  begin_slice sets it for P / B slices.
+    cur.frame_num = 0;
     compute_poc(sh, s);
     const int slot = alloc_slot();
     if (slot < 0) return fail(H264R_ERR_BUSY, "no free DPB slot");
@@ -901,7 +910,7 @@ int h264r_parser::finish_picture(bool last)
     for (int a = 0; a < n; a++) {
         const MbState &m = mbs[a];
         const bool inter = m.slice >= 0 && m.cls == H264R_MB_INTER;
-        mo->intra[a] = inter ? 0 : 1;
+        mo->intra[a] = inter ? 0 : (m.slice >= 0 && m.cls == H264R_MB_IPCM ? 2 : 1);
         int16_t *mv = &mo->mv[(size_t)a * 64];
         int8_t *ref = &mo->ref[(size_t)a * 32];
         int32_t *rp = &mo->refpic[(size_t)a * 32];
@@ -1059,6 +1068,7 @@ int h264r_parser::begin_slice(const uint8_t *p, size_t n, SliceCtx &sc, BitReade
         if (r2) return r2;
     }
     sc.index = num_slices++;
+    if (sc.sh.slice_type != kSliceI && sc.sh.slice_type != kSliceSI) cur.frame_num = sc.sh.frame_num;
     h264r_slice rs;
     memset(&rs, 0, sizeof(rs));
     rs.chroma_qp_offset[0] = (int8_t)sc.pps->chroma_qp_offset[0];

@@ -41,7 +41,7 @@ inline int median3(int a, int b, int c) { return std::max(std::min(a, b), std::m
 // Motion of a decoded picture, kept while it is a reference (co-located
 // data for direct prediction, 8.4.1.2.1).
 struct Motion {
-    std::vector<uint8_t> intra;   // per MB
+    std::vector<uint8_t> intra;   // per MB: 1 intra or undecoded, 2 I_PCM
     std::vector<int16_t> mv;      // [mb][list][4x4 raster][2]
     std::vector<int8_t> ref;      // [mb][list][4x4 raster], -1: list unused
     std::vector<int32_t> refpic;  // [mb][list][4x4 raster]: uid of the reference picture
@@ -405,6 +405,14 @@ struct MbDecoder {
         const Pic *col = sc.list[1].empty() ? nullptr : sc.list[1][0];
         if (!col || !col->motion) return c;
         const Motion &m = *col->motion;
+        if (m.intra[addr] == 2 && sc.sh.direct_spatial) {
+            // an I_PCM co-located MB: the reference's intra test does not
+            // cover I_PCM (prediction mode Intra_NA), so it reads the MB's
+            // cleared motion as list 1, refIdxCol 0 and mvCol (0, 0)
+            // (H264InterPrediction.cpp:1230-1253), which sets colZeroFlag
+            c.ref = 0;
+            return c;
+        }
         if (m.intra[addr]) return c;
         int l = 0;
         if (m.ref[(addr * 2 + 0) * 16 + bi] < 0) l = 1;

@@ -533,21 +533,46 @@ struct Writer {
         }
     }
 
-    // all direct blocks of the MB use list 0 (explicit weighting never meets
-    // a list-1-only partition, whose weights the reference reads out of range)
+    // implicit weighting of a bi-predicted block whose two references are
+    // the same picture: the reference decoder divides by their POC distance
+    // before it tests it for zero (H264InterPrediction.cpp:2955-2960)
+    bool same_picture(const MbDecoder &d, int ref0, int ref1) const
+    {
+        return ref0 >= 0 && ref1 >= 0 && d.sc.list[0][ref0] && d.sc.list[1][ref1] &&
+               d.sc.list[0][ref0]->poc == d.sc.list[1][ref1]->poc;
+    }
+
+    // direct blocks the reference decodes as the standard does: explicit
+    // weighting never meets a list-1-only block (the reference reads its
+    // weights out of range, H264InterPrediction.cpp:2756-2771), implicit
+    // weighting never a bi-predicted block from one picture twice
     bool direct_ok(MbDecoder &d, int quadrant_mask)
     {
-        if (cfg.weighted != 1 || !cfg.direct_spatial) return true;
+        if (cfg.weighted == 0 || (cfg.weighted == 1 && !cfg.direct_spatial)) return true;
         for (int q = 0; q < 4; q++) {
             if (!(quadrant_mask & (1 << q))) continue;
             for (int s = 0; s < 4; s++) {
                 Blk b;
                 const int x = (q & 1) * 8 + 4 * (s & 1), y = (q >> 1) * 8 + 4 * (s >> 1);
                 if (d.direct_block(x >> 2, y >> 2, b)) die("direct prediction failed: %s", P.err.c_str());
-                if (b.ref[0] < 0) return false;
+                if (cfg.weighted == 1 && b.ref[0] < 0) return false;
+                if (cfg.weighted == 2 && same_picture(d, b.ref[0], b.ref[1])) return false;
             }
         }
         return true;
+    }
+
+    // reference indices of a partition predicted from lists `pred`
+    void draw_refs(const MbDecoder &d, int pred, const int nref[2], int ref[2])
+    {
+        for (int tries = 0;; tries++) {
+            for (int l = 0; l < 2; l++) ref[l] = (pred & (1 << l)) ? rng.range(0, nref[l] - 1) : -1;
+            if (cfg.weighted != 2 || pred != 3 || !same_picture(d, ref[0], ref[1])) return;
+            if (tries > 16) {  // every pair names one picture: predict from list 0 only
+                ref[1] = -1;
+                return;
+            }
+        }
     }
 
     void reset_mb_motion(MbDecoder &d)
@@ -595,6 +620,12 @@ struct Writer {
         } else if (shape < 3) {
             const int np = shape == 0 ? 1 : 2;
             int pred[2] = {lists_of(!explicit_b), lists_of(!explicit_b)};
+            int refs[2][2];
+            for (int p = 0; p < np; p++) {
+                draw_refs(d, pred[p], nref, refs[p]);
+                pred[p] = (refs[p][0] >= 0 ? 1 : 0) | (refs[p][1] >= 0 ? 2 : 0);
+            }
+            if (np == 1) pred[1] = pred[0];
             if (!is_b) {
                 mb_type = shape;
             } else if (shape == 0) {
@@ -609,11 +640,10 @@ struct Writer {
             for (int p = 0; p < np; p++) {
                 Part q{shape == 2 ? 8 * p : 0, shape == 1 ? 8 * p : 0, shape == 2 ? 8 : 16, shape == 1 ? 8 : 16,
                        pred[p], {-1, -1}, {{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}};
+                q.ref[0] = refs[p][0];
+                q.ref[1] = refs[p][1];
                 for (int l = 0; l < 2; l++)
-                    if (pred[p] & (1 << l)) {
-                        q.ref[l] = rng.range(0, nref[l] - 1);
-                        draw_mv(px + q.x, py + q.y, q.w, q.h, q.mv[l]);
-                    }
+                    if (q.ref[l] >= 0) draw_mv(px + q.x, py + q.y, q.w, q.h, q.mv[l]);
                 parts.push_back(q);
             }
         } else {
@@ -632,6 +662,8 @@ struct Writer {
                         pred = 0;
                     } else {
                         pred = lists_of(!explicit_b);
+                        draw_refs(d, pred, nref, ref[q]);
+                        pred = (ref[q][0] >= 0 ? 1 : 0) | (ref[q][1] >= 0 ? 2 : 0);
                         // sub_mb_type of (shape, lists): 8x8 L0 1, L1 2, Bi 3; 8x4 L0 4, L1 6, Bi 8;
                         // 4x8 L0 5, L1 7, Bi 9; 4x4 L0 10, L1 11, Bi 12
                         static const int tab[4][4] = {{0, 1, 2, 3}, {0, 4, 6, 8}, {0, 5, 7, 9}, {0, 10, 11, 12}};
@@ -646,7 +678,8 @@ struct Writer {
                     no_sub_lt8 = false;
                 }
                 shape |= subshape << (2 + 2 * q);
-                for (int l = 0; l < 2; l++) ref[q][l] = (pred & (1 << l)) ? rng.range(0, nref[l] - 1) : -1;
+                if (!is_b) draw_refs(d, pred, nref, ref[q]);
+                if (pred == 0) ref[q][0] = ref[q][1] = -1;
                 const int qx = (q & 1) * 8, qy = (q >> 1) * 8;
                 const int nsub = pred == 0 ? 4 : (subshape == 0 ? 1 : subshape == 3 ? 4 : 2);
                 for (int s = 0; s < nsub; s++) {

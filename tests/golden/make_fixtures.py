@@ -15,7 +15,8 @@ the first pictures of each stream, in decoding order from the IDR:
                     callback receives them
 
   <name>.h264       for the two CAVLC streams: the stream cut before the first
-                    slice of picture N (parameter sets included), with
+                    slice of picture N (parameter sets included), and each
+                    stream whole, with
   <name>.frames.json  every picture the reference outputs for that cut stream,
                     in output order: POC, md5 of its planes (ref_dump --yuv) and
                     md5 of the BMP the reference's own main.cpp writes for it
@@ -102,6 +103,9 @@ def make_order_fixture(dumper, ref_data, tmp):
 BITSTREAMS = [
     ("gop121_cavlc_4pics", "gop121.naluCnt453.h264", 4),
     ("heavyhand_cavlc_b4_6pics", "HeavyHand_1080p.B_frames_4.no_cabac.no_tff.h264", 6),
+    # the two CAVLC streams whole (50 and 76 pictures)
+    ("gop121_cavlc_whole", "gop121.naluCnt453.h264", 1 << 20),
+    ("heavyhand_cavlc_b4_whole", "HeavyHand_1080p.B_frames_4.no_cabac.no_tff.h264", 1 << 20),
 ]
 
 
@@ -149,8 +153,12 @@ def make_bitstream_fixtures(ref_data, tmp):
                 bmp = hashlib.md5(f.read()).hexdigest()
             frames.append({"poc": poc, "yuv_md5": hashlib.md5(raw[k * frame:(k + 1) * frame]).hexdigest(),
                            "bmp_md5": bmp})
+        decoded = sum(1 for l in open(order) if l.startswith("D "))
         with open(os.path.join(HERE, name + ".frames.json"), "w") as f:
-            json.dump({"stream": stream, "pictures": n, "width": 1920, "height": 1088, "frames": frames}, f, indent=1)
+            # pictures: decoded pictures (the last one is output without
+            # deblocking and not in the decoding-order lines)
+            json.dump({"stream": stream, "pictures": min(n, decoded + 1), "width": 1920, "height": 1088,
+                       "frames": frames}, f, indent=1)
         print(name, len(cut), "bytes", len(frames), "frames")
 
 
