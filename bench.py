@@ -1,11 +1,15 @@
 #!/usr/bin/env python3
 """Benchmark: 1080p decoded frames/s of the GB300 reconstruction engine.
 
-Workload (the reference's 1080p High configuration as seeded synthetic
-record streams): S independent streams of 1920x1088, 30 pictures each, GOP
-15 IBBP, 8x8 transforms, partitions down to 4x4, 4 reference pictures,
-explicit weighted prediction, MVs +-256 quarter samples with 5% past the
-picture edges, QP 22..40, alpha/beta offsets +-6.  Seeds 1000 + stream.
+Workload (the reference's 1080p High configuration as seeded bitstreams):
+S independent CAVLC streams of 1920x1088, 30 pictures each, GOP 15 IBBP,
+8x8 transforms, P partitions down to 4x4, 4 reference pictures, explicit
+weighted bi-prediction, MVs +-256 quarter samples with 5% past the picture
+edges, QP 22..40, alpha/beta offsets +-6, written by the library's seeded
+writer (include/h264r_writer.h; seeds 1000 + stream) and parsed by its front
+end before the timed region.  Stream 0 is a case of
+tests/golden/writer_streams.json, so its pictures are compared with the
+reference decoder's own output of the same stream.
 
 One step reconstructs every picture of every stream (30 * S frames): the
 pictures of all streams that do not reference each other go into one
@@ -98,6 +102,54 @@ def gen_streams(n, pictures, seed0, workloads=None, overrides=None):
     if errors:
         raise errors[0]
     return out, slots
+
+
+def gen_written(n, seed0, name="1080p_high", pictures=None):
+    """Records of n seeded bitstreams: each stream is written by the library's
+    bitstream writer (the named configuration, seed seed0 + i) and parsed by
+    its front end, in parallel threads (both are C; ctypes releases the
+    GIL).  Returns (pictures per stream in decoding order with their
+    dependency groups, DPB slots per stream)."""
+    import h264_video_decoder_demo_gb300 as h
+    from h264_video_decoder_demo_gb300.engine import parse_stream
+    h.lib()
+    out = [None] * n
+    slots = [0] * n
+    errors = []
+    over = {} if pictures is None else {"num_pictures": pictures}
+
+    def work(i):
+        try:
+            data = h.write_stream(name, seed=seed0 + i, **over)
+            out[i], slots[i] = parse_stream(data)
+        except Exception as exc:  # surfaced below
+            errors.append(exc)
+
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(n)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if errors:
+        raise errors[0]
+    return out, slots
+
+
+def reference_pictures(name, seed, pictures):
+    """The reference decoder's md5 of every picture of a written stream, in
+    decoding order (planes after deblocking; the last picture, which it
+    outputs without deblocking, from its output frames), when the stream is
+    a case of tests/golden/writer_streams.json; else None."""
+    from h264_video_decoder_demo_gb300.engine import STREAMS
+    with open(os.path.join(ROOT, "tests", "golden", "writer_streams.json")) as f:
+        cases = json.load(f)["cases"]
+    want = dict(STREAMS[name], seed=seed, num_pictures=pictures)
+    for c in cases.values():
+        if c["writer"] == want:
+            md5s = [p["post_md5"] for p in c["pictures"]]
+            last = {f["poc"]: f["yuv_md5"] for f in c["frames"]}
+            return md5s, last
+    return None
 
 
 def oracle_sample(pics, slots, seconds, check=None):
@@ -208,7 +260,7 @@ def run_reference(args, rank):
     if rank != 0:
         return None
     cores = os.cpu_count() or 1
-    pics, slots = gen_streams(cores, args.pictures, SEED_BASE)
+    pics, slots = gen_written(cores, SEED_BASE, pictures=args.pictures)
     from oracle_cpu import OracleDPB
     dpbs = [OracleDPB(p[0].width_mbs, p[0].height_mbs, s) for p, s in zip(pics, slots)]
     cursor = [0] * cores
@@ -240,7 +292,8 @@ def run_reference(args, rank):
         "impl": "reference", "metric": METRIC, "value": round(fps, 3), "unit": "frames/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * dt / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-        "data": "synthetic (seeded 1080p High records; CPU restatement of the reference's reconstruction)",
+        "data": "synthetic (seeded 1080p High CAVLC bitstreams written by the library's writer, parsed by its "
+                "front end; CPU restatement of the reference's reconstruction)",
         "config": {"workload": WORKLOAD, "streams": cores, "pictures_per_stream": args.pictures, "threads": cores},
         "cpu_baseline": {"value": round(fps, 3), "unit": "frames/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": round(fps, 3), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -343,11 +396,12 @@ def run_batched(device, kinds, pictures, seed, overrides):
             "ms_per_step": round(ms, 3), "batches_per_step": len(batches)}
 
 
-def run_plain_cif(device, seed=1000):
-    """CIF 352x288, 8 pictures IPPP, Baseline tools (1 ref, 4x4 transforms),
-    one picture per launch sequence with a host sync after each."""
+def run_plain_cif(device):
+    """CIF 352x288, 8 pictures IPPP, Baseline CAVLC (the writer's cif_ippp
+    stream, seed 1, whose output the reference's fixture pins), one picture
+    per launch sequence with a host sync after each."""
     import h264_video_decoder_demo_gb300 as h
-    pics, slots = gen_streams(1, 8, seed, workloads=["cif_ippp"])
+    pics, slots = gen_written(1, 1, name="cif_ippp")
     ctx = h.Context(device)
     s = h.Stream(ctx, 22, 18, slots[0])
     for p in pics[0]:
@@ -601,8 +655,8 @@ def run_engine(args, world, rank, local, dist):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     S = args.streams
-    streams_pics, slots = gen_streams(S, args.pictures, SEED_BASE + 100 * rank)
-    ngroups = max(p.group for p in streams_pics[0]) + 1
+    streams_pics, slots = gen_written(S, SEED_BASE + 100 * rank, pictures=args.pictures)
+    ngroups = max(p.group for ps in streams_pics for p in ps) + 1
     ctx = h.Context(local, max_batch=4 * S)
     streams = [h.Stream(ctx, 120, 68, slots[i]) for i in range(S)]
 
@@ -794,6 +848,14 @@ def run_engine(args, world, rank, local, dist):
             s1.submit(p)
             gpu_frames.append(s1.output(p.dst_slot).copy())
         s1.close()
+        ref = reference_pictures("1080p_high", SEED_BASE, args.pictures) if rank == 0 else None
+        ref_exact = None
+        if ref is not None:
+            import hashlib
+            md5s, last = ref
+            got = [hashlib.md5(f.tobytes()).hexdigest() for f in gpu_frames]
+            ref_exact = {"pictures": len(got), "equal": got[:len(md5s)] == md5s and len(got) == len(md5s) + 1,
+                         "source": "the reference decoder's own planes for stream 0 (tests/golden/writer_streams.json)"}
         if args.skip_cpu:
             cpu = None
             exact = None
@@ -850,7 +912,8 @@ def run_engine(args, world, rank, local, dist):
         e2e_dt = time.perf_counter() - t0
         e2e = {"value": round(frames_per_step * e2e_steps / e2e_dt, 2), "unit": "frames/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": frames_per_step * FRAME_BYTES}
-        extra = {"plain_fps": round(plain_fps, 2), "cpu_baseline": cpu, "e2e": e2e, "bit_exact_sample": exact}
+        extra = {"plain_fps": round(plain_fps, 2), "cpu_baseline": cpu, "e2e": e2e, "bit_exact_sample": exact,
+                 "bit_exact_vs_reference": ref_exact}
         if args.serve_seconds > 0:
             pools = serving_pools()
             extra["serving"] = run_serving(args, local, pools, rate=40.0, seconds=args.serve_seconds)
@@ -872,7 +935,8 @@ def run_engine(args, world, rank, local, dist):
         "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(elapsed_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-        "data": "synthetic (seeded 1080p High record streams, shapes and distributions of the reference's 1080p config)",
+        "data": "synthetic (seeded 1080p High CAVLC bitstreams with the 1080p configuration's tools and "
+                "distributions, written by the library's writer and parsed by its front end before the timed region)",
         "config": {"workload": WORKLOAD, "streams_per_gpu": S, "pictures_per_stream": args.pictures,
                    "batches_per_step": len(batches), "frames_per_step": frames_per_step,
                    "coded_size": "1920x1088", "gop": "15, IBBP", "refs": 4, "weighted_prediction": "explicit",

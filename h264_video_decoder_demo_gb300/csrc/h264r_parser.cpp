@@ -795,9 +795,13 @@ int h264r_parser::mark_references(const SliceHeader &sh, const Sps &s)
 
 int h264r_parser::alloc_slot()
 {
+    // the free slot that has been free longest: consecutive pictures land in
+    // different slots, so pictures that do not reference each other (B
+    // pictures between two anchors) can be reconstructed in one batch
+    int best = -1;
     for (int i = 0; i < (int)slot_uid.size(); i++)
-        if (slot_uid[i] < 0) return i;
-    return -1;
+        if (slot_uid[i] < 0 && (best < 0 || slot_freed[i] < slot_freed[best])) best = i;
+    return best;
 }
 
 // first slice of a new picture
@@ -812,8 +816,13 @@ int h264r_parser::start_picture(const SliceHeader &sh, const Sps &s, const Pps &
                                       : h264r_order_infer_depth(s.profile_idc, s.constraint_set3, s.level_idc, width_mbs, height_mbs);
         if (reorder_depth < 0) reorder_depth = 0;
         if (reorder_depth > 16) reorder_depth = 16;
-        dpb_slots = std::min(32, std::max(s.max_num_ref_frames, 1) + reorder_depth + 1);
+        // references + pictures held for output + the picture being decoded,
+        // and one spare slot: with it the B pictures between two anchors and
+        // the next anchor land in slots no picture they depend on uses, so
+        // the batched entry points can reconstruct them together
+        dpb_slots = std::min(32, std::max(s.max_num_ref_frames, 1) + reorder_depth + 2);
         slot_uid.assign(dpb_slots, -1);
+        slot_freed.assign(dpb_slots, -1);
         slot_poc.assign(dpb_slots, 0);
         slot_index.assign(dpb_slots, 0);
         if (h264r_order_create(reorder_depth, &order)) return fail(H264R_ERR_INVALID_ARG, "reorder depth");
@@ -984,6 +993,7 @@ int h264r_parser::finish_picture(bool last)
     for (auto it = dpb.begin(); it != dpb.end();) {
         if (!it->is_ref() && !h264r_order_holds(order, (uint64_t)it->slot)) {
             slot_uid[it->slot] = -1;
+            slot_freed[it->slot] = (int64_t)decoded;
             it = dpb.erase(it);
         } else {
             ++it;

@@ -114,6 +114,7 @@ struct h264r_parser {
     uint32_t decoded = 0;
     h264r_order *order = nullptr;
     std::vector<int> slot_uid;  // slot -> uid of its picture, -1 free
+    std::vector<int64_t> slot_freed;  // slot -> pictures decoded when it was freed (-1: never used)
     // POC state
     int prev_poc_msb = 0, prev_poc_lsb = 0, prev_frame_num_offset = 0, prev_frame_num = 0, prev_ref_frame_num = 0;
     bool prev_ref_mmco5 = false, prev_mmco5 = false;

@@ -772,6 +772,47 @@ STREAMS = {
 }
 
 
+def assign_groups(pics):
+    """Dependency groups of pictures in decoding order, as the batched entry
+    points need them: a picture comes after the pictures it reads (its
+    references), after every reader of the picture its DPB slot held before
+    and after that picture's writer.  Sets pic.group; returns the count."""
+    writer, readers = {}, {}
+    ngroups = 0
+    for p in pics:
+        refs = p.ref_slots()
+        g = 0
+        for sl in refs:
+            g = max(g, writer.get(sl, -1) + 1)
+        g = max(g, readers.get(p.dst_slot, -1) + 1, writer.get(p.dst_slot, -1) + 1)
+        p.group = g
+        for sl in refs:
+            readers[sl] = max(readers.get(sl, -1), g)
+        writer[p.dst_slot] = g
+        readers[p.dst_slot] = -1
+        ngroups = max(ngroups, g + 1)
+    return ngroups
+
+
+def parse_stream(data):
+    """Records of every picture of an Annex B stream (front end), with their
+    dependency groups: (list of Picture, DPB slots the stream needs)."""
+    p = Parser()
+    try:
+        pics = [pic for pic, _ in p.pictures(data)]
+        p.end()
+        while True:
+            r = p.next()
+            if r is None:
+                break
+            pics.append(r[0])
+        slots = p.geometry()[2]
+    finally:
+        p.close()
+    assign_groups(pics)
+    return pics, slots
+
+
 def write_stream(name=None, seed=1, **over):
     """Annex B bytes of a seeded stream (h264r_write_stream): a named
     configuration of STREAMS with fields overridden, or fields alone."""

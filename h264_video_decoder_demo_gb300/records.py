@@ -115,6 +115,19 @@ class Picture:
             setattr(c, name, a.ctypes.data if a.size else None)
         return c
 
+    def ref_slots(self):
+        """DPB slots the picture's inter partitions read (motion payload)."""
+        inter = np.nonzero(self.mbs["type"] == MB_INTER)[0]
+        if len(inter) == 0:
+            return set()
+        raw = np.ascontiguousarray(self.motion).view(np.uint8)
+        aux = self.mbs["aux"][inter].astype(np.int64)
+        cnt = raw[aux[:, None] + np.array([2, 3])].astype(np.int64)
+        cnt = cnt[:, 0] | (cnt[:, 1] << 8)
+        first = np.repeat(aux + 4, cnt) + 16 * (np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt))
+        refs = raw[first[:, None] + np.array([8, 9])].view(np.int8).reshape(-1)
+        return set(int(r) & 31 for r in np.unique(refs[refs >= 0]))
+
     @classmethod
     def from_c(cls, c):
         """Copy an h264r_picture with host pointers into numpy arrays."""

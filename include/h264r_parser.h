@@ -69,7 +69,9 @@ int  h264r_parser_next(h264r_parser *p, h264r_parsed *out);
 
 /* Geometry of the active sequence once the first picture started (0 before):
  * MB width / frame height, and the DPB slots the parser uses (its references
- * plus the output reorder depth plus the picture being decoded). */
+ * plus the output reorder depth plus the picture being decoded, plus one
+ * spare).  A new picture takes the slot that has been free longest, so that
+ * pictures that do not depend on each other use different slots. */
 int  h264r_parser_geometry(const h264r_parser *p, int *width_mbs, int *height_mbs, int *dpb_slots);
 
 /* CAVLC table probes: decode a 16-bit window (first code bit = bit 15)
