@@ -558,53 +558,103 @@ def run_serving(args, device, pools, rate=40.0, seconds=60.0, seed=5000):
                 break
         reqs.append((t, res, rng.randint(0, len(SERVE_MODES) - 1), rng.randint(8, 120)))
     window = 4
+    pushers = 4
     free_bufs = {}
+    buf_mu = threading.Lock()
 
     def take_buf(nbytes):
-        lst = free_bufs.setdefault(nbytes, [])
-        return lst.pop() if lst else torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+        with buf_mu:
+            lst = free_bufs.setdefault(nbytes, [])
+            if lst:
+                return lst.pop()
+        return torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
 
+    # C arguments of every pool picture, built once (a parser emits them)
+    cpool = {key: [p.to_c() for p in pics] for key, (pics, _) in pools.items()}
     for (res, kind), (pics, _) in pools.items():  # pinned output buffers, allocated before the clock starts
         nbytes = pics[0].plane_bytes
         if nbytes not in free_bufs:
-            free_bufs[nbytes] = [torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy() for _ in range(96)]
+            free_bufs[nbytes] = [torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy() for _ in range(256)]
     ctx = h.Context(device, dpb_budget_bytes=40 << 30, max_batch=128)
     srv = h.Server(ctx, queue_depth=window)
-    state = []  # per request: [stream id, next picture, ended]
-    inflight = {}
     total = sum(r[3] for r in reqs)
-    done = 0
+    # One producer thread per group of streams, as a parser thread per stream
+    # would push: it pushes a stream's next picture while the stream holds
+    # fewer than `window` unfinished ones.  The main thread admits arrivals and
+    # polls finished pictures.
+    lock = threading.Lock()
+    queues = [[] for _ in range(pushers)]  # new streams per producer
+    pending = {}  # stream id -> pushed, not yet polled
+    inflight = {}
+    state = {"done": 0, "stop": False, "error": None}
+    wake = threading.Event()
+
+    def producer(j):
+        active = []
+        while not state["stop"]:
+            with lock:
+                active += queues[j]
+                queues[j] = []
+            did = False
+            for e in active:
+                sid, pics, cps, n = e[0], e[1], e[2], e[3]
+                while e[4] < n and pending[sid] < window:
+                    k = e[4]
+                    p = pics[k]
+                    buf = take_buf(p.plane_bytes)
+                    with lock:
+                        pending[sid] += 1
+                        inflight[(sid, k)] = buf
+                    rc = srv.push_c(sid, cps[k], p.group, k, buf.ctypes.data)
+                    if rc != 0:
+                        state["error"] = "server push: %d" % rc
+                        state["stop"] = True
+                        return
+                    e[4] = k + 1
+                    did = True
+                if e[4] == n and not e[5]:
+                    srv.end(sid)
+                    e[5] = True
+            active = [e for e in active if not e[5]]
+            if not did:
+                wake.wait(0.0005)
+                wake.clear()
+
+    threads = [threading.Thread(target=producer, args=(j,), daemon=True) for j in range(pushers)]
+    for t in threads:
+        t.start()
     t0 = time.perf_counter()
     nxt = 0
-    while done < total:
-        now = time.perf_counter() - t0
-        while nxt < len(reqs) and reqs[nxt][0] <= now:
-            _, res, kind, n = reqs[nxt]
-            pics, slots = pools[(res, kind)]
-            state.append([srv.open(pics[0].width_mbs, pics[0].height_mbs, slots), 0, False, pics, n])
-            nxt += 1
-        for stt in state:
-            sid, k, ended, pics, n = stt
-            if ended:
-                continue
-            while k < n and srv.pending(sid) < window:
-                p = pics[k]
-                buf = take_buf(p.plane_bytes)
-                inflight[(sid, k)] = buf
-                rc = srv.push(sid, p, p.group, k, buf)
-                if rc != 0:
-                    raise RuntimeError("server push: %d" % rc)
-                k += 1
-            stt[1] = k
-            if k == n:
-                srv.end(sid)
-                stt[2] = True
-        for sid, tag, status, _ in srv.poll(wait_ms=1):
-            if status != 0:
-                raise RuntimeError("serving: picture failed (%d)" % status)
-            buf = inflight.pop((sid, tag))
-            free_bufs[buf.nbytes].append(buf)
-            done += 1
+    done = 0
+    try:
+        while done < total and not state["stop"]:
+            now = time.perf_counter() - t0
+            while nxt < len(reqs) and reqs[nxt][0] <= now:
+                _, res, kind, n = reqs[nxt]
+                pics, slots = pools[(res, kind)]
+                sid = srv.open(pics[0].width_mbs, pics[0].height_mbs, slots)
+                with lock:
+                    pending[sid] = 0
+                    queues[sid % pushers].append([sid, pics, cpool[(res, kind)], n, 0, False])
+                nxt += 1
+            got = srv.poll(max_items=1024, wait_ms=1)
+            if got:
+                with lock:
+                    for sid, tag, status, _ in got:
+                        if status != 0:
+                            raise RuntimeError("serving: picture failed (%d)" % status)
+                        pending[sid] -= 1
+                        buf = inflight.pop((sid, tag))
+                        with buf_mu:
+                            free_bufs[buf.nbytes].append(buf)
+                done += len(got)
+                wake.set()
+    finally:
+        state["stop"] = True
+        for t in threads:
+            t.join()
+    if state["error"]:
+        raise RuntimeError(state["error"])
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.close()

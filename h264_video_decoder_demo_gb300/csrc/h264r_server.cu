@@ -44,14 +44,20 @@ double now_ms()
 }
 
 struct Slot {
-    uint8_t *host = nullptr;  // pinned staging
     uint8_t *dev = nullptr;   // device records
     uint64_t cap = 0;
     bool busy = false;
 };
 
+// pinned host buffer holding one picture's packed records
+struct Pinned {
+    uint8_t *ptr = nullptr;
+    uint64_t cap = 0;
+};
+
 struct Item {
-    std::vector<uint8_t> blob;  // packed records: mbs | slices | weights | motion | coef | pcm
+    Pinned blob;                // packed records: mbs | slices | weights | motion | coef | pcm
+    uint64_t size = 0;
     uint64_t off[6] = {0, 0, 0, 0, 0, 0};
     h264r_picture pic{};        // sizes, flags and scaling lists (pointers set on upload)
     int group = 0;
@@ -103,6 +109,11 @@ struct h264r_server {
     std::vector<cudaEvent_t> ev_pool;
     cudaStream_t up = nullptr;
     std::thread th;
+    // pinned buffers for packed records: push packs each picture straight
+    // into one (on the caller's thread), the scheduler only enqueues its H2D
+    // copy; a buffer returns to the pool when its picture is reported
+    std::mutex pool_mu;
+    std::multimap<uint64_t, uint8_t *> pool;
     bool stop = false;
     int next_id = 0;
     size_t rr = 0;
@@ -128,8 +139,35 @@ void give_event(h264r_server *srv, cudaEvent_t &e)
     e = nullptr;
 }
 
+Pinned take_pinned(h264r_server *srv, uint64_t need)
+{
+    {
+        std::lock_guard<std::mutex> g(srv->pool_mu);
+        auto f = srv->pool.lower_bound(need);
+        if (f != srv->pool.end() && f->first <= 2 * need + (1 << 20)) {
+            Pinned p{f->second, f->first};
+            srv->pool.erase(f);
+            return p;
+        }
+    }
+    Pinned p;
+    const uint64_t cap = align_up(need + need / 8, 1 << 16);
+    if (cudaMallocHost(&p.ptr, cap) != cudaSuccess) return Pinned();
+    p.cap = cap;
+    return p;
+}
+
+void give_pinned(h264r_server *srv, Pinned &p)
+{
+    if (!p.ptr) return;
+    std::lock_guard<std::mutex> g(srv->pool_mu);
+    srv->pool.emplace(p.cap, p.ptr);
+    p = Pinned();
+}
+
 void report(h264r_server *srv, SStream *S, Item *it, int status)
 {
+    give_pinned(srv, it->blob);
     h264r_server_done d;
     d.stream = S->id;
     d.status = status;
@@ -170,7 +208,6 @@ void close_stream(h264r_server *srv, SStream *S)
         srv->st.streams_open--;
     }
     for (auto &sl : S->slots) {
-        if (sl.host) cudaFreeHost(sl.host);
         if (sl.dev) cudaFree(sl.dev);
         sl = Slot();
     }
@@ -247,14 +284,12 @@ bool upload(h264r_server *srv)
             if (k < 0) break;
             Item *it = S->host_q.front();
             Slot &sl = S->slots[k];
-            const uint64_t need = it->blob.size();
+            const uint64_t need = it->size;
             if (sl.cap < need) {
-                if (sl.host) cudaFreeHost(sl.host);
                 if (sl.dev) cudaFree(sl.dev);
                 sl = Slot();
                 const uint64_t cap = align_up(need + need / 8, 1 << 16);
-                if (cudaMallocHost(&sl.host, cap) != cudaSuccess || cudaMalloc(&sl.dev, cap) != cudaSuccess) {
-                    if (sl.host) cudaFreeHost(sl.host);
+                if (cudaMalloc(&sl.dev, cap) != cudaSuccess) {
                     sl = Slot();
                     fail_stream(srv, S, H264R_ERR_NO_MEMORY);
                     progress = true;
@@ -262,8 +297,7 @@ bool upload(h264r_server *srv)
                 }
                 sl.cap = cap;
             }
-            memcpy(sl.host, it->blob.data(), need);
-            if (cudaMemcpyAsync(sl.dev, sl.host, need, cudaMemcpyHostToDevice, srv->up) != cudaSuccess) {
+            if (cudaMemcpyAsync(sl.dev, it->blob.ptr, need, cudaMemcpyHostToDevice, srv->up) != cudaSuccess) {
                 fail_stream(srv, S, H264R_ERR_CUDA);
                 progress = true;
                 break;
@@ -279,7 +313,6 @@ bool upload(h264r_server *srv)
             it->pic.motion = d + it->off[3];
             it->pic.coef = d + it->off[4];
             it->pic.pcm = d + it->off[5];
-            std::vector<uint8_t>().swap(it->blob);
             S->host_q.pop_front();
             S->dev_q.push_back(it);
             progress = true;
@@ -408,6 +441,7 @@ extern "C" int h264r_server_destroy(h264r_server *srv)
     for (auto &kv : srv->streams) delete kv.second;
     for (auto e : srv->batch_done) cudaEventDestroy(e);
     for (auto e : srv->ev_pool) cudaEventDestroy(e);
+    for (auto &kv : srv->pool) cudaFreeHost(kv.second);
     cudaStreamDestroy(srv->up);
     delete srv;
     return H264R_OK;
@@ -461,9 +495,14 @@ extern "C" int h264r_server_push(h264r_server *srv, int stream_id, const h264r_p
         it->off[k] = tot;
         tot = align_up(tot + sz[k], kAlign);
     }
-    it->blob.resize(tot);
+    it->blob = take_pinned(srv, tot);
+    if (!it->blob.ptr) {
+        delete it;
+        return H264R_ERR_NO_MEMORY;
+    }
+    it->size = tot;
     for (int k = 0; k < 6; k++)
-        if (sz[k]) memcpy(it->blob.data() + it->off[k], src[k], sz[k]);
+        if (sz[k]) memcpy(it->blob.ptr + it->off[k], src[k], sz[k]);
     it->pic = *pic;
     it->group = dependency_group;
     it->tag = tag;
@@ -473,6 +512,7 @@ extern "C" int h264r_server_push(h264r_server *srv, int stream_id, const h264r_p
         std::lock_guard<std::mutex> g(srv->mu);
         auto f = srv->streams.find(stream_id);
         if (f == srv->streams.end() || f->second->ended) {
+            give_pinned(srv, it->blob);
             delete it;
             return H264R_ERR_INVALID_ARG;
         }

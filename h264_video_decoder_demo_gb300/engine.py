@@ -630,6 +630,12 @@ class Server:
             self._keep[(stream, tag)] = out
         return lib().h264r_server_push(self.h, stream, ctypes.byref(c), group, tag, ptr)
 
+    def push_c(self, stream, cpic, group, tag, out_ptr):
+        """push() with the C arguments built by the caller: a CPicture whose
+        arrays the caller keeps alive, and the address of the output planes
+        (kept alive by the caller until the picture is polled)."""
+        return lib().h264r_server_push(self.h, stream, ctypes.byref(cpic), group, tag, out_ptr)
+
     def end(self, stream):
         return lib().h264r_server_end(self.h, stream)
 
@@ -772,26 +778,33 @@ STREAMS = {
 }
 
 
-def assign_groups(pics):
-    """Dependency groups of pictures in decoding order, as the batched entry
-    points need them: a picture comes after the pictures it reads (its
-    references), after every reader of the picture its DPB slot held before
-    and after that picture's writer.  Sets pic.group; returns the count."""
-    writer, readers = {}, {}
-    ngroups = 0
-    for p in pics:
-        refs = p.ref_slots()
+class GroupTracker:
+    """Dependency groups of a stream's pictures, one picture at a time in
+    decoding order, as the batched entry points and the server need them: a
+    picture comes after the pictures it reads (its references), after every
+    reader of the picture its DPB slot held before, and after that picture."""
+
+    def __init__(self):
+        self.writer, self.readers = {}, {}
+
+    def next(self, pic):
+        refs = pic.ref_slots()
         g = 0
         for sl in refs:
-            g = max(g, writer.get(sl, -1) + 1)
-        g = max(g, readers.get(p.dst_slot, -1) + 1, writer.get(p.dst_slot, -1) + 1)
-        p.group = g
+            g = max(g, self.writer.get(sl, -1) + 1)
+        g = max(g, self.readers.get(pic.dst_slot, -1) + 1, self.writer.get(pic.dst_slot, -1) + 1)
         for sl in refs:
-            readers[sl] = max(readers.get(sl, -1), g)
-        writer[p.dst_slot] = g
-        readers[p.dst_slot] = -1
-        ngroups = max(ngroups, g + 1)
-    return ngroups
+            self.readers[sl] = max(self.readers.get(sl, -1), g)
+        self.writer[pic.dst_slot] = g
+        self.readers[pic.dst_slot] = -1
+        pic.group = g
+        return g
+
+
+def assign_groups(pics):
+    """Sets pic.group of every picture (decoding order); returns the count."""
+    t = GroupTracker()
+    return max((t.next(p) for p in pics), default=-1) + 1
 
 
 def parse_stream(data):

@@ -106,3 +106,105 @@ def test_server_rejects_a_stream_larger_than_the_budget():
         sid = srv.open(22, 18, 4)  # CIF fits
         assert sid >= 0
         srv.end(sid)
+
+
+def test_server_fed_by_parser_threads_matches_reference():
+    """A host parser thread per stream, as the reference runs its decoder on a
+    thread of its own (SDH264Player/MyVideoPlayer.cpp:126-169): each thread
+    parses one of the writer's bitstreams and pushes every picture as soon as
+    its records are complete; the server batches the streams' pictures
+    together.  Every decoded picture equals the reference decoder's own
+    planes of that stream (tests/golden/writer_streams.json)."""
+    import json
+    import os
+    import threading
+
+    import torch
+
+    from h264_video_decoder_demo_gb300.engine import GroupTracker, Parser
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "writer_streams.json")) as f:
+        cases = json.load(f)["cases"]
+    names = ["cif_ippp", "cif_ippp_2slices_pcm", "1080p_default_wp_b1", "1080p_high_gop5_3slices"]
+    datas = []
+    for nm in names:
+        cfg = dict(cases[nm]["writer"])
+        seed = cfg.pop("seed")
+        datas.append(h.write_stream(None, seed=seed, **cfg))
+    window = 4
+    got = [dict() for _ in names]
+    errors = []
+    with h.Context(0) as ctx, h.Server(ctx, queue_depth=window) as srv:
+        lock = threading.Lock()
+        pending = {}
+        outs = {}
+
+        def parser_thread(i):
+            try:
+                p = Parser()
+                groups = GroupTracker()
+                sid = None
+                k = 0
+
+                def push(pic):
+                    nonlocal sid, k
+                    if sid is None:
+                        sid = srv.open(pic.width_mbs, pic.height_mbs, p.geometry()[2])
+                        with lock:
+                            pending[sid] = 0
+                    while pending[sid] >= window:
+                        time.sleep(0.0002)
+                    buf = torch.empty(pic.plane_bytes, dtype=torch.uint8, pin_memory=True).numpy()
+                    with lock:
+                        outs[(sid, k)] = (i, buf)
+                        pending[sid] += 1
+                    assert srv.push(sid, pic, groups.next(pic), k, buf) == 0
+                    k += 1
+
+                data = datas[i]
+                for off in range(0, len(data), 1 << 16):  # the bytes arrive in pieces
+                    p.feed(data[off:off + (1 << 16)])
+                    while True:
+                        r = p.next()
+                        if r is None:
+                            break
+                        push(r[0])
+                p.end()
+                while True:
+                    r = p.next()
+                    if r is None:
+                        break
+                    push(r[0])
+                srv.end(sid)
+                p.close()
+            except Exception as exc:  # reported below
+                errors.append(exc)
+
+        threads = [threading.Thread(target=parser_thread, args=(i,)) for i in range(len(names))]
+        for t in threads:
+            t.start()
+        total = sum(len(c["pictures"]) + 1 for c in (cases[n] for n in names))
+        done = 0
+        deadline = time.perf_counter() + 120
+        while done < total and not errors:
+            assert time.perf_counter() < deadline, "server made no progress"
+            for sid, tag, status, lat in srv.poll(wait_ms=2):
+                assert status == 0
+                with lock:
+                    i, buf = outs.pop((sid, tag))
+                    pending[sid] -= 1
+                got[i][tag] = md5(buf)
+                done += 1
+        for t in threads:
+            t.join()
+        st = srv.stats()
+    assert not errors, errors[0]
+    assert st["batch_pictures"] > st["batches"], "no batch held pictures of more than one stream"
+    for i, nm in enumerate(names):
+        c = cases[nm]
+        want = [pic["post_md5"] for pic in c["pictures"]]  # decoding order, deblocked
+        n = len(want) + 1
+        assert sorted(got[i]) == list(range(n))
+        assert [got[i][k] for k in range(n - 1)] == want, nm
+        # the last picture is output without deblocking
+        last_poc = [f for f in c["frames"] if f["yuv_md5"] == got[i][n - 1]]
+        assert last_poc, "%s: last picture differs from the reference's output" % nm
