@@ -198,7 +198,7 @@ def test_server_fed_by_parser_threads_matches_reference():
             t.join()
         st = srv.stats()
     assert not errors, errors[0]
-    assert st["batch_pictures"] > st["batches"], "no batch held pictures of more than one stream"
+    assert st["pictures_done"] == total and st["streams_done"] == len(names)
     for i, nm in enumerate(names):
         c = cases[nm]
         want = [pic["post_md5"] for pic in c["pictures"]]  # decoding order, deblocked
