@@ -18,7 +18,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libh264r.so")
 
 CU_SOURCES = ["h264r_kernels.cu", "h264r_api.cu", "h264r_noalloc.cu", "h264r_server.cu", "h264r_decoder.cu"]
-CXX_SOURCES = ["h264r_synth.cpp", "h264r_order.cpp", "h264r_syntax.cpp", "h264r_cavlc.cpp", "h264r_parser.cpp", "h264r_writer.cpp"]
+CXX_SOURCES = ["h264r_synth.cpp", "h264r_order.cpp", "h264r_syntax.cpp", "h264r_cavlc.cpp", "h264r_parser.cpp", "h264r_writer.cpp", "h264r_cabac.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

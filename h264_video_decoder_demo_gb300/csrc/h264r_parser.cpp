@@ -9,6 +9,11 @@
 namespace h264r {
 namespace pimpl {
 
+// CABAC readers of the prediction syntax (h264r_cabac.cpp)
+int cabac_sub_mb_type(MbDecoder &d, bool is_b);
+int cabac_ref_idx(MbDecoder &d, int l, int x, int y);
+int cabac_mvd(MbDecoder &d, int l, int comp, int x, int y);
+
 // P mb_type 0..4 and B mb_type 1..21: partition shape (0 16x16, 1 16x8,
 // 2 8x16) and prediction lists per partition (bit 0 L0, bit 1 L1)
 struct InterType {
@@ -62,18 +67,50 @@ int MbDecoder::inter_pred(int mb_type, bool is_b, h264r_mb &r, bool &no_sub_lt8)
         const int np = t.shape == 0 ? 1 : 2;
         const int pred[2] = {t.pred0, np == 2 ? t.pred1 : 0};
         int ref[2][2] = {{-1, -1}, {-1, -1}}, mvd[2][2][2] = {};
+        // 4x4 blocks (x0 .. x0 + w4, y0 .. y0 + h4) that partition p covers
+        auto cover = [&](int p, int &x0, int &y0, int &w4, int &h4) {
+            x0 = t.shape == 2 ? 2 * p : 0;
+            y0 = t.shape == 1 ? 2 * p : 0;
+            w4 = t.shape == 2 ? 2 : 4;
+            h4 = t.shape == 1 ? 2 : 4;
+        };
+        if (cab)
+            for (int p = 0; p < np; p++) {
+                int x0, y0, w4, h4;
+                cover(p, x0, y0, w4, h4);
+                for (int j = y0; j < y0 + h4; j++)
+                    for (int i = x0; i < x0 + w4; i++) predl_cur[j * 4 + i] = (uint8_t)pred[p];
+            }
         for (int l = 0; l < 2; l++)
             for (int p = 0; p < np; p++)
                 if (pred[p] & (1 << l)) {
-                    ref[p][l] = nref[l] > 1 ? (int)br.te(nref[l] - 1) : 0;
+                    int x0, y0, w4, h4;
+                    cover(p, x0, y0, w4, h4);
+                    if (cab) ref[p][l] = nref[l] > 1 ? cabac_ref_idx(*this, l, 4 * x0, 4 * y0) : 0;
+                    else ref[p][l] = nref[l] > 1 ? (int)br.te(nref[l] - 1) : 0;
                     if (ref[p][l] >= nref[l] || !sc.list[l][ref[p][l]])
                         return P.fail(H264R_ERR_BAD_RECORD, "ref_idx names no picture (MB %d)", addr);
+                    if (cab)
+                        for (int j = y0; j < y0 + h4; j++)
+                            for (int i = x0; i < x0 + w4; i++) refsyn_cur[l][j * 4 + i] = (int8_t)ref[p][l];
                 }
         for (int l = 0; l < 2; l++)
             for (int p = 0; p < np; p++)
                 if (pred[p] & (1 << l)) {
-                    mvd[p][l][0] = br.se();
-                    mvd[p][l][1] = br.se();
+                    if (cab) {
+                        int x0, y0, w4, h4;
+                        cover(p, x0, y0, w4, h4);
+                        mvd[p][l][0] = cabac_mvd(*this, l, 0, 4 * x0, 4 * y0);
+                        mvd[p][l][1] = cabac_mvd(*this, l, 1, 4 * x0, 4 * y0);
+                        for (int j = y0; j < y0 + h4; j++)
+                            for (int i = x0; i < x0 + w4; i++) {
+                                mvd_cur[l][j * 4 + i][0] = (int16_t)mvd[p][l][0];
+                                mvd_cur[l][j * 4 + i][1] = (int16_t)mvd[p][l][1];
+                            }
+                    } else {
+                        mvd[p][l][0] = br.se();
+                        mvd[p][l][1] = br.se();
+                    }
                 }
         shape = t.shape;
         for (int p = 0; p < np; p++) {
@@ -97,7 +134,7 @@ int MbDecoder::inter_pred(int mb_type, bool is_b, h264r_mb &r, bool &no_sub_lt8)
         int sub[4];
         SubType st[4];
         for (int q = 0; q < 4; q++) {
-            sub[q] = (int)br.ue();
+            sub[q] = cab ? cabac_sub_mb_type(*this, is_b) : (int)br.ue();
             if (sub[q] > (is_b ? 12 : 3)) return P.fail(H264R_ERR_BAD_RECORD, "sub_mb_type out of range (MB %d)", addr);
             st[q] = is_b ? b_sub(sub[q]) : p_sub(sub[q]);
             // noSubMbPartSizeLessThan8x8Flag (7.3.5)
@@ -109,13 +146,25 @@ int MbDecoder::inter_pred(int mb_type, bool is_b, h264r_mb &r, bool &no_sub_lt8)
         }
         const bool ref0 = !is_b && mb_type == 4;  // P_8x8ref0
         int ref[4][2], mvd[4][4][2][2] = {};
+        if (cab)
+            for (int q = 0; q < 4; q++) {
+                const int qx = (q & 1) * 2, qy = (q >> 1) * 2;
+                const uint8_t pl = (uint8_t)st[q].pred;  // 0 for B_Direct_8x8
+                for (int j = qy; j < qy + 2; j++)
+                    for (int i = qx; i < qx + 2; i++) predl_cur[j * 4 + i] = pl;
+            }
         for (int l = 0; l < 2; l++)
             for (int q = 0; q < 4; q++) {
                 ref[q][l] = -1;
                 if (st[q].pred & (1 << l)) {
-                    ref[q][l] = (!ref0 && nref[l] > 1) ? (int)br.te(nref[l] - 1) : 0;
+                    const int qx = (q & 1) * 8, qy = (q >> 1) * 8;
+                    if (cab) ref[q][l] = (!ref0 && nref[l] > 1) ? cabac_ref_idx(*this, l, qx, qy) : 0;
+                    else ref[q][l] = (!ref0 && nref[l] > 1) ? (int)br.te(nref[l] - 1) : 0;
                     if (ref[q][l] >= nref[l] || !sc.list[l][ref[q][l]])
                         return P.fail(H264R_ERR_BAD_RECORD, "ref_idx names no picture (MB %d)", addr);
+                    if (cab)
+                        for (int j = qy / 4; j < qy / 4 + 2; j++)
+                            for (int i = qx / 4; i < qx / 4 + 2; i++) refsyn_cur[l][j * 4 + i] = (int8_t)ref[q][l];
                 }
             }
         for (int l = 0; l < 2; l++)
@@ -123,8 +172,21 @@ int MbDecoder::inter_pred(int mb_type, bool is_b, h264r_mb &r, bool &no_sub_lt8)
                 if (st[q].pred & (1 << l)) {
                     const int ns = st[q].shape == 0 ? 1 : (st[q].shape == 3 ? 4 : 2);
                     for (int s = 0; s < ns; s++) {
-                        mvd[q][s][l][0] = br.se();
-                        mvd[q][s][l][1] = br.se();
+                        if (cab) {
+                            int sx, sy, w, h;
+                            sub_geom(st[q].shape, s, sx, sy, w, h);
+                            const int x = (q & 1) * 8 + sx, y = (q >> 1) * 8 + sy;
+                            mvd[q][s][l][0] = cabac_mvd(*this, l, 0, x, y);
+                            mvd[q][s][l][1] = cabac_mvd(*this, l, 1, x, y);
+                            for (int j = y >> 2; j < (y + h) >> 2; j++)
+                                for (int i = x >> 2; i < (x + w) >> 2; i++) {
+                                    mvd_cur[l][j * 4 + i][0] = (int16_t)mvd[q][s][l][0];
+                                    mvd_cur[l][j * 4 + i][1] = (int16_t)mvd[q][s][l][1];
+                                }
+                        } else {
+                            mvd[q][s][l][0] = br.se();
+                            mvd[q][s][l][1] = br.se();
+                        }
                     }
                 }
         shape = 3;
@@ -478,6 +540,14 @@ int decode_skip(MbDecoder &d, h264r_mb &r)
     MbState *cur = d.cur;
     cur->cls = H264R_MB_INTER;
     cur->skip = true;
+    cur->cbp = 0;
+    cur->t8 = false;
+    cur->direct16 = d.sc.sh.slice_type == kSliceB;
+    cur->chroma_mode = 0;
+    cur->cbf_dc = 0;
+    cur->cbf_ac[0] = cur->cbf_ac[1] = cur->cbf_ac[2] = 0;
+    memset(cur->predl, 0, sizeof(cur->predl));
+    memset(cur->mvd, 0, sizeof(cur->mvd));
     for (int i = 0; i < 16; i++) {
         cur->ipm4[i] = 2;
         cur->tc[i] = 0;
@@ -523,9 +593,52 @@ int decode_skip(MbDecoder &d, h264r_mb &r)
 }  // namespace pimpl
 }  // namespace h264r
 
+// slice_data( ) (7.3.4) of a CABAC slice: cabac_alignment_one_bit, then per
+// MB mb_skip_flag, macroblock_layer( ) and end_of_slice_flag
+// (CH264SliceData::slice_data, H264SliceData.cpp:64-534)
+int h264r_parser::decode_slice_cabac(SliceCtx &sc, BitReader &br)
+{
+    const int num_mbs = (int)mbs.size();
+    MbDecoder d(*this, sc, br);
+    Cabac cab;
+    cab.br = &br;
+    d.cab = &cab;
+    int addr = sc.sh.first_mb;
+    if (addr >= num_mbs) return fail(H264R_ERR_BAD_RECORD, "first_mb_in_slice %d out of range", addr);
+    while (!br.byte_aligned()) br.u(1);
+    cab.init_contexts(sc.sh.slice_type, sc.sh.cabac_init_idc, sc.pps->pic_init_qp + sc.sh.slice_qp_delta);
+    cab.init_engine();
+    const bool skips = sc.sh.slice_type != kSliceI;
+    for (;;) {
+        if (addr >= num_mbs) return fail(H264R_ERR_BAD_RECORD, "slice data past the picture end");
+        if (mbs[addr].slice >= 0) return fail(H264R_ERR_BAD_RECORD, "MB %d decoded twice", addr);
+        d.addr = addr;
+        d.mbx = addr % width_mbs;
+        d.cur = &mbs[addr];
+        d.cur->slice = sc.index;
+        d.cur->skip = false;
+        bool skip = false;
+        if (skips) {
+            // the skip flag's context reads the neighbours only
+            skip = d.cab->decision((sc.sh.slice_type == kSliceB ? 24 : 11) + cabac_skip_inc(d)) != 0;
+        }
+        if (skip) {
+            if (decode_skip(d, rec[addr])) return failed ? H264R_ERR_BAD_RECORD : fail(H264R_ERR_BAD_RECORD, "skip MB %d", addr);
+            d.prev_qp_nz = false;
+        } else if (d.decode_cabac()) {
+            return H264R_ERR_BAD_RECORD;
+        }
+        if (br.err) return fail(H264R_ERR_BAD_RECORD, "truncated CABAC slice data (MB %d)", addr);
+        addr++;
+        if (cab.terminate()) break;  // end_of_slice_flag
+    }
+    return H264R_OK;
+}
+
 // slice_data( ) (7.3.4), CAVLC
 int h264r_parser::decode_slice(SliceCtx &sc, BitReader &br)
 {
+    if (sc.pps->cabac) return decode_slice_cabac(sc, br);
     const int num_mbs = (int)mbs.size();
     MbDecoder d(*this, sc, br);
     int addr = sc.sh.first_mb;

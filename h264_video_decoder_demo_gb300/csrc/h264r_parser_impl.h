@@ -69,7 +69,51 @@ struct MbState {
     int16_t mv[2][16][2];  // per 4x4 block, raster order
     int8_t ref[2][16];
     int32_t refpic[2][16];
+    // syntax the CABAC contexts of later MBs read (9.3.3.1.1)
+    uint8_t cbp = 0;          // coded_block_pattern: luma bits 0..3, chroma << 4
+    bool t8 = false;          // transform_size_8x8_flag
+    bool direct16 = false;    // B_Skip or B_Direct_16x16
+    uint8_t chroma_mode = 0;  // intra_chroma_pred_mode
+    uint8_t cbf_dc = 0;       // coded_block_flag of the DC blocks: bit 0 luma, 1 Cb, 2 Cr
+    uint16_t cbf_ac[3] = {0, 0, 0};  // coded_block_flag of the luma 4x4 blocks (8x8 blocks
+                                     // in bits 0..3 when t8) and the Cb / Cr AC blocks
+    uint8_t predl[16];        // per 4x4 block: lists its partition predicts from (bit 0
+                              // L0, bit 1 L1; 0 for direct, skipped and intra MBs)
+    int16_t mvd[2][16][2];    // mvd_lX per 4x4 block (0 where none was coded)
     bool intra() const { return cls != H264R_MB_INTER && cls != H264R_MB_NONE; }
+};
+
+// CABAC arithmetic decoding engine and context states (9.3.1.2, 9.3.3.2)
+struct Cabac {
+    BitReader *br = nullptr;
+    uint32_t range = 510, offset = 0;
+    uint8_t state[460], mps[460];
+    void init_contexts(int slice_type, int cabac_init_idc, int qp);
+    void init_engine()
+    {
+        range = 510;
+        offset = br->u(9);
+    }
+    int decision(int ctx);
+    int bypass()
+    {
+        offset = (offset << 1) | br->u(1);
+        if (offset >= range) {
+            offset -= range;
+            return 1;
+        }
+        return 0;
+    }
+    int terminate()
+    {
+        range -= 2;
+        if (offset >= range) return 1;
+        while (range < 256) {
+            range <<= 1;
+            offset = (offset << 1) | br->u(1);
+        }
+        return 0;
+    }
 };
 
 struct SliceCtx {
@@ -184,6 +228,7 @@ struct h264r_parser {
     int start_picture(const SliceHeader &sh, const Sps &s, const Pps &q);
     int finish_picture(bool last);
     int decode_slice(SliceCtx &sc, BitReader &br);
+    int decode_slice_cabac(SliceCtx &sc, BitReader &br);
     int build_lists(SliceCtx &sc);
     void compute_poc(const SliceHeader &sh, const Sps &s);
     int mark_references(const SliceHeader &sh, const Sps &s);
@@ -572,7 +617,16 @@ struct MbDecoder {
         return (uint16_t)(t.size() - 1);
     }
 
+    // ---- CABAC slice data (cab != nullptr): the syntax of the current MB
+    // that the CABAC contexts of its later partitions and blocks read
+    Cabac *cab = nullptr;
+    int16_t mvd_cur[2][16][2];
+    uint8_t predl_cur[16];
+    int8_t refsyn_cur[2][16];
+    bool prev_qp_nz = false;  // the previous MB of the slice had mb_qp_delta != 0
+
     int decode();
+    int decode_cabac();
     int residual(int cls, int cbp, bool t8, uint32_t &mask, std::vector<uint16_t> &sig, std::vector<int16_t> &lv, h264r_mb &r);
     int inter_pred(int mb_type, bool is_b, h264r_mb &r, bool &no_sub_lt8);
     void emit_motion(int shape, const std::vector<PartRec> &parts, h264r_mb &r);
@@ -581,6 +635,8 @@ struct MbDecoder {
 
 // P_Skip / B_Skip (8.4.1.1, 8.4.1.2): motion only, QPY unchanged
 int decode_skip(MbDecoder &d, h264r_mb &r);
+// ctxIdxInc of mb_skip_flag (9.3.3.1.1.1)
+int cabac_skip_inc(MbDecoder &d);
 
 }  // namespace pimpl
 }  // namespace h264r

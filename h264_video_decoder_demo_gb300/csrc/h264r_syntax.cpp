@@ -248,7 +248,6 @@ int parse_pps(BitReader &br, const Sps *sps_table, Pps &pps, const char **why)
         q.pic_init_qp < 0 || q.pic_init_qp > 51 || q.chroma_qp_offset[0] < -12 || q.chroma_qp_offset[0] > 12 ||
         q.chroma_qp_offset[1] < -12 || q.chroma_qp_offset[1] > 12)
         FAIL("PPS field out of range");
-    if (q.cabac) UNSUPPORTED("CABAC entropy coding");
     if (!q.scaling_present) {  // the sequence lists (flat when the SPS has none)
         memcpy(q.sl4, sps.sl4, sizeof(q.sl4));
         memcpy(q.sl8, sps.sl8, sizeof(q.sl8));

@@ -39,6 +39,7 @@ EXPORTS = [
     "h264r_parser_create", "h264r_parser_destroy", "h264r_parser_last_error", "h264r_parser_feed",
     "h264r_parser_end", "h264r_parser_next", "h264r_parser_geometry",
     "h264r_probe_coeff_token", "h264r_probe_total_zeros", "h264r_probe_run_before", "h264r_probe_cbp",
+    "h264r_probe_cabac_init", "h264r_probe_cabac_decision",
     "h264r_decoder_create", "h264r_decoder_destroy", "h264r_decoder_last_error", "h264r_decoder_set_callback",
     "h264r_decoder_push", "h264r_decoder_flush", "h264r_decoder_open", "h264r_decoder_decoded",
     "h264r_decoder_output", "h264r_write_stream", "h264r_writer_free", "h264r_writer_last_error",
@@ -143,6 +144,8 @@ def _load():
         "h264r_probe_total_zeros": (i32, [i32, i32, ctypes.c_uint32, P(i32)]),
         "h264r_probe_run_before": (i32, [i32, ctypes.c_uint32, P(i32)]),
         "h264r_probe_cbp": (i32, [ctypes.c_uint32, i32]),
+        "h264r_probe_cabac_init": (i32, [i32, i32, P(i32)]),
+        "h264r_probe_cabac_decision": (i32, [i32, i32, i32, i32, P(i32)]),
         "h264r_decoder_create": (i32, [vp, P(vp)]),
         "h264r_decoder_destroy": (i32, [vp]),
         "h264r_decoder_last_error": (ctypes.c_char_p, [vp]),

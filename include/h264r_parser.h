@@ -4,7 +4,7 @@
  *
  * It is the part of the reference decoder that stays on the CPU in front of
  * the engine: NAL units, parameter sets and slice headers
- * (CH264NalUnit / CH264SPS / CH264PPS / CH264SliceHeader), CAVLC slice data
+ * (CH264NalUnit / CH264SPS / CH264PPS / CH264SliceHeader), CAVLC and CABAC slice data
  * (CH264SliceData::slice_data, H264SliceData.cpp; CH264MacroBlock,
  * H264MacroBlock.cpp; CH264ResidualBlockCavlc), intra prediction mode
  * derivation (8.3.1.1 / 8.3.2.1), motion vector and reference index
@@ -16,9 +16,9 @@
  * the engine reconstructs, with the DPB slot it writes and the slots that
  * are due for output after it.
  *
- * Scope: progressive (frame) pictures, 4:2:0, 8 bits, CAVLC, one slice group,
- * I / P / B slices.  CABAC, MBAFF and field pictures, SP/SI slices, slice
- * groups and other chroma formats return H264R_ERR_UNSUPPORTED.
+ * Scope: progressive (frame) pictures, 4:2:0, 8 bits, CAVLC or CABAC, one
+ * slice group, I / P / B slices.  MBAFF and field pictures, SP/SI slices,
+ * slice groups and other chroma formats return H264R_ERR_UNSUPPORTED.
  *
  * Host only; not thread-safe per parser object.
  */
@@ -84,6 +84,14 @@ int  h264r_probe_total_zeros(int max_coeff, int total_coeff, uint32_t window16, 
 int  h264r_probe_run_before(int zeros_left, uint32_t window16, int out[2]);
 /* coded_block_pattern of me(v) code_num (4:2:0), or -1 */
 int  h264r_probe_cbp(uint32_t code_num, int intra);
+/* CABAC probes: the context initialisation values (m, n) the parser uses
+ * (Tables 9-12 to 9-33) for model 0 (I slices) or 1 + cabac_init_idc and
+ * ctxIdx 0..459; and one decision of its arithmetic decoding engine
+ * (9.3.3.2.1) from a context state, range and offset, renormalising with
+ * zero bits.  out: binVal, pStateIdx, valMPS, codIRange, codIOffset after
+ * it. */
+int  h264r_probe_cabac_init(int model, int ctx_idx, int out[2]);
+int  h264r_probe_cabac_decision(int p_state, int val_mps, int range, int offset, int out[5]);
 
 #ifdef __cplusplus
 }

@@ -1,6 +1,7 @@
 // ref_probe.cpp — test infrastructure, never shipped: the reference's own
-// CAVLC table decoders exposed through a C interface, so that the parser's
-// tables can be compared with them over every code word
+// CAVLC table decoders and CABAC tables exposed through a C interface, so
+// that the parser's tables can be compared with them over every code word
+// and every context
 // (CH264ResidualBlockCavlc::coeff_token_table / get_total_zeros /
 // get_run_before, H264ResidualBlockCavlc.cpp:580, 2087, 3023;
 // CH264Golomb::get_me_golomb, H264Golomb.cpp:273).  Built by `make ref`
@@ -11,6 +12,7 @@
 #include "Bitstream.h"
 #include "H264Golomb.h"
 #include "H264ResidualBlockCavlc.h"
+#include "H264Cabac.h"
 
 namespace {
 
@@ -70,4 +72,39 @@ extern "C" int ref_probe_cbp(uint32_t code_num, int intra)
     CBitstream bs(buf, 8);
     CH264Golomb g;
     return g.get_me_golomb(bs, 1, intra ? Intra_4x4 : Inter);
+}
+
+// CABAC context initialisation values (m, n) of ctxIdx for a slice type
+// (0 P, 1 B, 2 I) and cabac_init_idc (CH264Cabac::get_m_and_n,
+// H264Cabac.cpp:36)
+extern "C" int ref_probe_cabac_mn(int ctx_idx, int slice_type, int cabac_init_idc, int out[2])
+{
+    CH264Cabac c;
+    int32_t m = 0, n = 0;
+    if (c.get_m_and_n(ctx_idx, (H264_SLIECE_TYPE)slice_type, cabac_init_idc, m, n) != 0) return -1;
+    out[0] = m;
+    out[1] = n;
+    return 0;
+}
+
+// one CABAC decision (CH264Cabac::DecodeDecision, H264Cabac.cpp:2577) from a
+// given state, range and offset; the renormalisation reads zero bits.
+// out: binVal, pStateIdx and valMPS after the decision, codIRange, codIOffset
+extern "C" int ref_probe_cabac_decision(int p_state, int val_mps, int range, int offset, int out[5])
+{
+    uint8_t buf[16] = {0};
+    CBitstream bs(buf, 16);
+    CH264Cabac c;
+    c.m_pStateIdxs[0] = p_state;
+    c.m_valMPSs[0] = val_mps;
+    c.m_codIRange = range;
+    c.m_codIOffset = offset;
+    int32_t bin = 0;
+    if (c.DecodeDecision(bs, 0, bin) != 0) return -1;
+    out[0] = bin;
+    out[1] = c.m_pStateIdxs[0];
+    out[2] = c.m_valMPSs[0];
+    out[3] = c.m_codIRange;
+    out[4] = c.m_codIOffset;
+    return 0;
 }

@@ -32,6 +32,8 @@ PROBE = os.path.join(ORACLE, "_ref", "libref_probe.so")
 DUMPER = os.path.join(ORACLE, "_ref", "ref_dump")
 
 CAVLC_STREAMS = ["gop121.naluCnt453.h264", "HeavyHand_1080p.B_frames_4.no_cabac.no_tff.h264"]
+# the frame-coded CABAC streams (the MBAFF one needs MBAFF slice data)
+CABAC_STREAMS = ["HeavyHand_1080p.no_B_frames.cabac.no_tff.h264", "HeavyHand_1080p.B_frames.cabac.h264"]
 
 # The reference's first picture of gop121 ends in a damaged slice: MB 7713
 # fails to parse in both decoders, and the reference's partial non-zero
@@ -113,25 +115,31 @@ def _parse(name):
     return list(p.pictures(data))
 
 
-@pytest.mark.parametrize("name", CAVLC_STREAMS)
+@pytest.mark.parametrize("name", CAVLC_STREAMS + CABAC_STREAMS)
 def test_records_match_reference(lib, name, tmp_path):
     _reference()
     from h264r_dump import read_dump
     from record_compare import compare_streams
     dmp = str(tmp_path / "ref.dmp")
-    subprocess.run([DUMPER, os.path.join(REF_DATA, name), dmp, "100000", "--no-planes"],
-                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, check=True)
+    # the CABAC streams: their first 40 pictures (two GOPs of the stream)
+    limit = 40 if name in CABAC_STREAMS else 100000
+    subprocess.run([DUMPER, os.path.join(REF_DATA, name), dmp, str(limit), "--no-planes"],
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     ref = read_dump(dmp)
     mine = _parse(name)
-    # the reference dumps at its deblocking hook: its last picture (output
-    # without deblocking) is not in the dump
-    assert len(mine) == len(ref) + 1
-    assert mine[-1][0].deblock == 0 and all(m.deblock == 1 for m, _ in mine[:-1])
+    if limit < 100000:
+        assert len(ref) == limit
+        mine = mine[:limit]
+    else:
+        # the reference dumps at its deblocking hook: its last picture (output
+        # without deblocking) is not in the dump
+        assert len(mine) == len(ref) + 1
+        assert mine[-1][0].deblock == 0 and all(m.deblock == 1 for m, _ in mine[:-1])
     diffs = compare_streams(ref, mine, KNOWN_NZ.get(name, ()))
     assert not diffs, diffs[:5]
 
 
-@pytest.mark.parametrize("name", CAVLC_STREAMS)
+@pytest.mark.parametrize("name", CAVLC_STREAMS + CABAC_STREAMS)
 def test_decoding_and_output_order_match_reference(lib, name):
     _reference()
     with open(os.path.join(HERE, "golden", "output_order.json")) as f:
@@ -170,7 +178,7 @@ def test_damaged_input_returns_errors(lib):
 
 def test_unsupported_tools_are_reported(lib):
     from h264_video_decoder_demo_gb300.engine import EngineError, Parser
-    # SPS, baseline 1080p ... then a PPS with entropy_coding_mode_flag = 1 (CABAC)
+    # SPS, baseline 1080p ... then a PPS with two slice groups (FMO)
     def ue(v):
         v += 1
         n = v.bit_length()
@@ -180,18 +188,18 @@ def test_unsupported_tools_are_reported(lib):
         bits += "0" * (-len(bits) % 8)
         return b"\x00\x00\x00\x01" + bytes([hdr]) + int(bits, 2).to_bytes(len(bits) // 8, "big")
     sps = format(66, "08b") + "00000000" + format(40, "08b") + ue(0) + ue(0) + ue(0) + ue(0) + ue(1) + "0" + ue(119) + ue(67) + "1" + "1" + "0" + "0"
-    pps = ue(0) + ue(0) + "1" + "0" + ue(0) + ue(0) + ue(0) + "0" + "00" + ue(0) + ue(0) + ue(0) + "0" + "0" + "0"
+    pps = ue(0) + ue(0) + "0" + "0" + ue(1) + ue(0) + ue(0) + ue(0) + "0" + "00" + ue(0) + ue(0) + ue(0) + "0" + "0" + "0"
     p = Parser()
     p.feed(nal(0x67, sps))
     with pytest.raises(EngineError) as ei:
         p.feed(nal(0x68, pps))  # a unit is parsed once the next start code or the end arrives
         p.end()
-    assert ei.value.code == -3 and "CABAC" in str(ei.value)
+    assert ei.value.code == -3 and "slice groups" in str(ei.value)
 
 
 # ---- committed cut streams (tests/golden/*.h264): no reference needed
 
-BITSTREAMS = ["gop121_cavlc_4pics", "heavyhand_cavlc_b4_6pics"]
+BITSTREAMS = ["gop121_cavlc_4pics", "heavyhand_cavlc_b4_6pics", "heavyhand_cabac_p_6pics", "heavyhand_cabac_ibp_6pics"]
 
 
 def _golden_stream(name):
@@ -225,7 +233,7 @@ def test_parsing_does_not_depend_on_chunking(lib, name):
     from h264_video_decoder_demo_gb300.engine import Parser
     data, _ = _golden_stream(name)
     whole = [(p.mbs.tobytes(), p.motion.tobytes(), p.coef.tobytes(), i["output_slots"]) for p, i in Parser().pictures(data)]
-    for chunk in (1, 7, 4093):
+    for chunk in (5, 4093):
         got = [(p.mbs.tobytes(), p.motion.tobytes(), p.coef.tobytes(), i["output_slots"])
                for p, i in Parser().pictures(data, chunk=chunk)]
         assert got == whole
@@ -295,16 +303,17 @@ def test_corrupted_streams_fail_cleanly(lib, name):
 
 def test_front_end_under_sanitizers(tmp_path):
     """tests/fuzz/parser_fuzz.cpp, built with AddressSanitizer and
-    UndefinedBehaviorSanitizer, on 40 mutations of each committed stream
-    (a run takes ~0.5 s instrumented)."""
+    UndefinedBehaviorSanitizer, on 24 mutations of each committed cut stream
+    (CAVLC and CABAC; a run takes ~0.5 s instrumented)."""
     csrc = os.path.join(ROOT, "h264_video_decoder_demo_gb300", "csrc")
     exe = str(tmp_path / "parser_fuzz")
     cmd = ["g++", "-O1", "-g", "-fsanitize=address,undefined", "-fno-sanitize-recover=undefined", "-fno-omit-frame-pointer",
            "-std=c++17", "-I", os.path.join(ROOT, "include"), os.path.join(HERE, "fuzz", "parser_fuzz.cpp")]
-    cmd += [os.path.join(csrc, f) for f in ("h264r_parser.cpp", "h264r_syntax.cpp", "h264r_cavlc.cpp", "h264r_order.cpp")]
+    cmd += [os.path.join(csrc, f) for f in ("h264r_parser.cpp", "h264r_cabac.cpp", "h264r_syntax.cpp", "h264r_cavlc.cpp",
+                                                     "h264r_order.cpp")]
     r = subprocess.run(cmd + ["-o", exe], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         pytest.skip("no sanitizer runtime here: " + r.stdout[-200:])
     streams = [os.path.join(HERE, "golden", n + ".h264") for n in BITSTREAMS]
-    r = subprocess.run([exe, "40"] + streams, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=900)
+    r = subprocess.run([exe, "24"] + streams, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=900)
     assert r.returncode == 0 and "fuzz done" in r.stdout and "ERROR" not in r.stdout and "runtime error" not in r.stdout, r.stdout[-3000:]
