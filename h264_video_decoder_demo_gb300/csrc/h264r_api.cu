@@ -491,12 +491,20 @@ static int parts_count(uint32_t shape)
     return n;
 }
 
+// MBs of a picture: a field picture (PAFF) holds half the frame's MB rows
+static uint32_t picture_mbs(const h264r_picture *pic)
+{
+    const uint32_t rows = pic->structure == H264R_STRUCT_FRAME ? pic->height_mbs : pic->height_mbs / 2u;
+    return (uint32_t)pic->width_mbs * rows;
+}
+
 extern "C" int h264r_validate_picture(const h264r_picture *pic, int dpb_slots)
 {
     if (!pic || !pic->mbs || !pic->slices || !pic->weights) return H264R_ERR_INVALID_ARG;
-    if (pic->structure != H264R_STRUCT_FRAME) return H264R_ERR_UNSUPPORTED;
-    if (pic->width_mbs == 0 || pic->height_mbs == 0 || pic->num_mbs != (uint32_t)pic->width_mbs * pic->height_mbs)
-        return H264R_ERR_BAD_RECORD;
+    if (pic->structure > H264R_STRUCT_BOTTOM) return H264R_ERR_BAD_RECORD;
+    const bool fpic = pic->structure != H264R_STRUCT_FRAME;
+    if (fpic && (pic->mbaff || (pic->height_mbs & 1))) return H264R_ERR_BAD_RECORD;
+    if (pic->width_mbs == 0 || pic->height_mbs == 0 || pic->num_mbs != picture_mbs(pic)) return H264R_ERR_BAD_RECORD;
     if (pic->mbaff && (pic->height_mbs & 1)) return H264R_ERR_BAD_RECORD;
     if (pic->dst_slot >= dpb_slots || pic->num_slices == 0 || pic->num_weights == 0) return H264R_ERR_BAD_RECORD;
     if ((pic->motion_bytes && !pic->motion) || (pic->coef_bytes && !pic->coef) || (pic->num_pcm && !pic->pcm))
@@ -550,10 +558,19 @@ extern "C" int h264r_validate_picture(const h264r_picture *pic, int dpb_slots)
                 memcpy(&p, pic->motion + m.aux + 4 + 16 * e, 16);
                 if (p.wt >= pic->num_weights) return H264R_ERR_BAD_RECORD;
                 for (int l = 0; l < 2; l++) {
-                    if (p.ref[l] >= 0 && (H264R_REF_SLOT(p.ref[l]) >= dpb_slots || H264R_REF_SLOT(p.ref[l]) == pic->dst_slot))
-                        return H264R_ERR_BAD_RECORD;
-                    if (p.ref[l] >= 0 && (p.ref[l] & H264R_REF_FIELD) && !((m.flags & H264R_MBF_FIELD) && pic->mbaff))
-                        return H264R_ERR_BAD_RECORD;
+                    if (p.ref[l] < 0) continue;
+                    const int slot = H264R_REF_SLOT(p.ref[l]);
+                    const bool fref = (p.ref[l] & H264R_REF_FIELD) != 0, bref = (p.ref[l] & H264R_REF_BOTTOM) != 0;
+                    if (slot >= dpb_slots) return H264R_ERR_BAD_RECORD;
+                    if (fpic) {
+                        // fields only; its own slot only for the opposite
+                        // parity (the first field of the frame)
+                        if (!fref) return H264R_ERR_BAD_RECORD;
+                        if (slot == pic->dst_slot && bref == (pic->structure == H264R_STRUCT_BOTTOM)) return H264R_ERR_BAD_RECORD;
+                    } else {
+                        if (slot == pic->dst_slot) return H264R_ERR_BAD_RECORD;
+                        if (fref && !((m.flags & H264R_MBF_FIELD) && pic->mbaff)) return H264R_ERR_BAD_RECORD;
+                    }
                 }
             }
         } else if (m.type == H264R_MB_IPCM) {
@@ -624,7 +641,8 @@ static uint64_t mix_key(int n, const h264r_picture *const *pics)
 {
     uint64_t k = 0;
     for (int i = 0; i < n; i++) {
-        uint64_t z = (uint64_t)pics[i]->width_mbs | (uint64_t)pics[i]->height_mbs << 16 | (uint64_t)(pics[i]->mbaff ? 1 : 0) << 32;
+        uint64_t z = (uint64_t)pics[i]->width_mbs | (uint64_t)pics[i]->height_mbs << 16 | (uint64_t)(pics[i]->mbaff ? 1 : 0) << 32 |
+                     (uint64_t)pics[i]->structure << 33;
         z += 0x9e3779b97f4a7c15ull;  // splitmix64 finaliser
         z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
         z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
@@ -752,7 +770,7 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
     const h264r_tuning tune = tuning_for(ctx, mix_key(n, pl.data()));
     uint64_t rows = 0, mbs = 0;
     for (auto &it : items) {
-        uint32_t uh = it.pic->mbaff ? it.pic->height_mbs / 2 : it.pic->height_mbs;
+        uint32_t uh = (it.pic->mbaff || it.pic->structure != H264R_STRUCT_FRAME) ? it.pic->height_mbs / 2 : it.pic->height_mbs;
         rows += uh;
         mbs += it.pic->num_mbs;
     }
@@ -778,12 +796,19 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
         const h264r_picture *pic = items[i].pic;
         h264r_stream *s = items[i].s;
         PicDesc &p = d[i];
+        // a field picture runs as a picture of its field's size whose planes
+        // step two frame lines from the field's first line
+        const int bot = pic->structure == H264R_STRUCT_BOTTOM;
+        p.fpic = pic->structure;
         p.wmb = pic->width_mbs;
-        p.hmb = pic->height_mbs;
+        p.hmb = p.fpic ? pic->height_mbs / 2 : pic->height_mbs;
         p.W = p.wmb * 16;
         p.H = p.hmb * 16;
         p.Wc = p.W / 2;
         p.Hc = p.H / 2;
+        p.fH = pic->height_mbs * 16;
+        p.ys = p.fpic ? 2 * p.W : p.W;
+        p.cs = p.ys / 2;
         p.mbaff = pic->mbaff;
         p.deblock = pic->deblock;
         p.num_mbs = pic->num_mbs;
@@ -803,11 +828,14 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
         p.dpb = s->dpb;
         p.slot_bytes = s->slot_bytes;
         p.nslots = s->cfg.dpb_slots;
-        p.dst = s->dpb + (uint64_t)pic->dst_slot * s->slot_bytes;
+        uint8_t *slot = s->dpb + (uint64_t)pic->dst_slot * s->slot_bytes;
+        p.dst = slot + (size_t)bot * p.W;
+        p.coff = p.W * p.fH + bot * p.Wc - bot * p.W;
+        p.cplane = p.Wc * (p.fH / 2);
         p.bs = b.bs + mb_base * h264r::kBsBytes;
         p.ires = any_intra ? (int16_t *)b.ires + mb_base * 384 : nullptr;
         p.units_w = pic->width_mbs;
-        p.units_h = pic->mbaff ? pic->height_mbs / 2 : pic->height_mbs;
+        p.units_h = pic->mbaff ? pic->height_mbs / 2 : p.hmb;
         p.progress = (int *)(b.dev + prog_off) + prog;
         p.mb_base = (uint32_t)mb_base;
         p.row_base = (uint32_t)row_base;
@@ -1006,10 +1034,10 @@ static int check_device_pic(h264r_stream *s, const h264r_picture *pic)
 {
     if (!s || !pic || !pic->mbs || !pic->slices || !pic->weights) return H264R_ERR_INVALID_ARG;
     if (pic->num_slices == 0 || pic->num_weights == 0) return H264R_ERR_BAD_RECORD;
-    if (pic->structure != H264R_STRUCT_FRAME) return H264R_ERR_UNSUPPORTED;
-    if (pic->width_mbs != s->cfg.width_mbs || pic->height_mbs != s->cfg.height_mbs ||
-        pic->num_mbs != (uint32_t)pic->width_mbs * pic->height_mbs || pic->dst_slot >= s->cfg.dpb_slots ||
-        (pic->mbaff && (pic->height_mbs & 1)))
+    if (pic->structure > H264R_STRUCT_BOTTOM) return H264R_ERR_INVALID_ARG;
+    if (pic->width_mbs != s->cfg.width_mbs || pic->height_mbs != s->cfg.height_mbs || pic->num_mbs != picture_mbs(pic) ||
+        pic->dst_slot >= s->cfg.dpb_slots || ((pic->mbaff || pic->structure != H264R_STRUCT_FRAME) && (pic->height_mbs & 1)) ||
+        (pic->mbaff && pic->structure != H264R_STRUCT_FRAME))
         return H264R_ERR_INVALID_ARG;
     return H264R_OK;
 }

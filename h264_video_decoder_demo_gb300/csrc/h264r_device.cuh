@@ -90,9 +90,16 @@ __device__ const uint8_t kTc0[3][52] = {
 
 // ---------------------------------------------------------------- picture
 // Device view of one picture of a batch (built by the host for every launch).
+// A field picture (PAFF) runs as a picture of its field's size: W x H and
+// the MB grid are the field's, the destination planes start on the field's
+// first line and step two frame lines (ys, cs); its MBs are field MBs for
+// scans, reference views, chroma vectors and strengths (fpic).
 struct PicDesc {
-    int wmb, hmb;            // frame size in MBs
-    int W, H, Wc, Hc;        // frame size in samples
+    int wmb, hmb;            // picture size in MBs (a field picture: its field)
+    int W, H, Wc, Hc;        // picture size in samples
+    int ys, cs;              // row pitch of the destination luma / chroma planes
+    int fH;                  // frame height in luma samples (DPB slot layout)
+    int fpic;                // 0 frame, 1 top field, 2 bottom field
     int mbaff, deblock;
     uint32_t num_mbs, num_slices, num_weights, num_pcm;
     uint32_t motion_bytes, coef_bytes;
@@ -103,7 +110,8 @@ struct PicDesc {
     const uint8_t *coef;
     const uint8_t *pcm;
     const uint8_t *scaling;  // 96 bytes ScalingList4x4 then 384 bytes ScalingList8x8
-    uint8_t *dst;            // destination slot: Y, then Cb, then Cr
+    uint8_t *dst;            // destination luma origin (slot: Y, then Cb, then Cr)
+    int coff, cplane;        // Cb origin - dst, Cr origin - Cb origin (bytes)
     const uint8_t *dpb;      // slot 0 of the stream's DPB
     uint64_t slot_bytes;
     int nslots;
@@ -171,10 +179,8 @@ __device__ __forceinline__ constexpr int bs_cv(int e, int k) { return kBsChromaV
 __device__ __forceinline__ constexpr int bs_ch(int e, int k) { return kBsChromaH + 2 * k + e; }
 
 __device__ __forceinline__ uint8_t *plane_y(const PicDesc &p) { return p.dst; }
-__device__ __forceinline__ uint8_t *plane_c(const PicDesc &p, int pl)
-{
-    return p.dst + (size_t)p.W * p.H + (size_t)pl * p.Wc * p.Hc;
-}
+// from dst and two offsets (no second pointer kept live in the kernels)
+__device__ __forceinline__ uint8_t *plane_c(const PicDesc &p, int pl) { return p.dst + p.coff + (size_t)pl * p.cplane; }
 
 // Inverse_macroblock_scanning_process (H264PictureBase.cpp:2503)
 __device__ __forceinline__ void mb_origin(const PicDesc &p, int addr, int &x, int &y, int &dy)
@@ -201,6 +207,9 @@ __device__ __forceinline__ int field_mb(const PicDesc &p, int addr)
 {
     return p.mbaff && (p.mbs[addr].flags & H264R_MBF_FIELD);
 }
+
+// field scans and field rules: MBAFF field MBs and every MB of a field picture
+__device__ __forceinline__ int field_coded(const PicDesc &p, int addr) { return field_mb(p, addr) | (p.fpic != 0); }
 
 __device__ __forceinline__ int chroma_row0(int y) { return (y >> 4) * 8 + (y & 1); }
 
@@ -325,14 +334,16 @@ struct RefView {
 };
 
 // frame reference, or field of a frame for MBAFF field MBs; quirk: x is
-// clamped to the doubled field-view width (H264InterPrediction.cpp:2363)
+// clamped to the doubled field-view width (H264InterPrediction.cpp:2363).
+// Field pictures clamp x to the picture width, as 8.4.2.2 has it (the
+// reference decodes no field picture to follow).
 __device__ __forceinline__ RefView ref_view(const PicDesc &p, int ref)
 {
     RefView r;
     int slot = ref & 31;
     if (slot >= p.nslots) slot = 0;  // out-of-range slots are rejected on the host; stay in bounds regardless
     const uint8_t *base = p.dpb + (uint64_t)slot * p.slot_bytes;
-    const uint8_t *cb = base + (size_t)p.W * p.H, *cr = cb + (size_t)p.Wc * p.Hc;
+    const uint8_t *cb = base + (size_t)p.W * p.fH, *cr = cb + (size_t)p.Wc * (p.fH / 2);
     if (ref & H264R_REF_FIELD) {
         int bot = (ref & H264R_REF_BOTTOM) ? 1 : 0;
         r.y = base + bot * p.W;
@@ -340,8 +351,8 @@ __device__ __forceinline__ RefView ref_view(const PicDesc &p, int ref)
         r.cr = cr + bot * p.Wc;
         r.ystride = 2 * p.W;
         r.cstride = 2 * p.Wc;
-        r.xmax = 2 * p.W - 1;
-        r.xmaxc = 2 * p.Wc - 1;
+        r.xmax = p.fpic ? p.W - 1 : 2 * p.W - 1;
+        r.xmaxc = p.fpic ? p.Wc - 1 : 2 * p.Wc - 1;
     } else {
         r.y = base; r.cb = cb; r.cr = cr;
         r.ystride = p.W; r.cstride = p.Wc;
@@ -462,8 +473,8 @@ __device__ __forceinline__ const uint8_t *intra_nb_ptr(const PicDesc &p, int cur
     if (n != cur && mn.type == H264R_MB_INTER && (mn.flags & H264R_MBF_CIP)) return nullptr;
     int x, y, dy;
     mb_origin(p, n, x, y, dy);
-    if (!isChroma) return plane_y(p) + (size_t)(y + dy * yW) * p.W + x + xW;
-    return plane_c(p, pl) + (size_t)(chroma_row0(y) + dy * yW) * p.Wc + x / 2 + xW;
+    if (!isChroma) return plane_y(p) + (size_t)(y + dy * yW) * p.ys + x + xW;
+    return plane_c(p, pl) + (size_t)(chroma_row0(y) + dy * yW) * p.cs + x / 2 + xW;
 }
 
 // ---------------------------------------------------------------- byte packing

@@ -435,12 +435,13 @@ __device__ __forceinline__ void load_luma_window(const RefView &rv, int ymax, in
     }
 }
 
-// 8.4.2.2.2 for the 2x2 chroma samples at (xi, yi) .. (xi+1, yi+1)
-// (Chroma_sample_interpolation_process, H264InterPrediction.cpp:2485-2522):
-// the 3x3 neighbourhood is held in three registers.
-__device__ __forceinline__ uint32_t chroma_2x2(const uint8_t *pl, int stride, int xmax, int ymax, int xi, int yi, int xf, int yf)
+// The 3x3 chroma neighbourhood of the 2x2 samples at (xi, yi) .. (xi+1,
+// yi+1) for 8.4.2.2.2 (Chroma_sample_interpolation_process,
+// H264InterPrediction.cpp:2485-2522), clamped at the picture edges, in three
+// registers (row r: bytes 0..2).
+__device__ __forceinline__ void load_chroma_window(const uint8_t *pl, int stride, int xmax, int ymax, int xi, int yi,
+                                                   uint32_t (&rw)[3])
 {
-    uint32_t rw[3];
     if (xi >= 0 && xi + 2 <= xmax && yi >= 0 && yi + 2 <= ymax) {
         const int sh = (xi & 3) * 8;
         const uint8_t *row = pl + (size_t)yi * stride + (xi & ~3);
@@ -459,7 +460,6 @@ __device__ __forceinline__ uint32_t chroma_2x2(const uint8_t *pl, int stride, in
             rw[r] = w;
         }
     }
-    return mc_chroma_2x2(rw[0], rw[1], rw[2], xf, yf);
 }
 
 
@@ -475,17 +475,17 @@ __device__ __forceinline__ void inter_body(InterWarpSmem (&smem)[W], const PicDe
     const uint32_t g = blockIdx.x * W + wid;
     if (g >= total_mbs) return;
     InterWarpSmem &s = smem[wid];
-    const PicDesc p = pics[find_pic_by_mb(pics, npics, g)];
+    const PicDesc &p = pics[find_pic_by_mb(pics, npics, g)];
     const int addr = (int)(g - p.mb_base);
     const h264r_mb m = p.mbs[addr];
-    const int field = field_mb(p, addr);
+    const int field = field_mb(p, addr);  // geometry: a field MB of an MBAFF frame
     const bool intra = is_intra_type(m.type);
     if (intra && !p.ires) return;
     // ---- residual (8.5) into s.res: one call site for intra and inter MBs
     // (the code of this kernel is kept compact: instruction fetch, not
     // arithmetic or memory, is what its warps wait on)
     if (intra || m.type == H264R_MB_INTER) {
-        if (!mb_residual(p, m, field, intra ? 0 : 3, intra ? 0 : 1, s.res, s.dcs, s.lev) && lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
+        if (!mb_residual(p, m, field | (p.fpic != 0), intra ? 0 : 3, intra ? 0 : 1, s.res, s.dcs, s.lev) && lane == 0) set_error(st, H264R_ERR_BAD_RECORD);
     }
     if (intra) {
         // intra MB: only its residual, for the intra wavefront (k_intra).
@@ -518,7 +518,11 @@ __device__ __forceinline__ void inter_body(InterWarpSmem (&smem)[W], const PicDe
             return;
         }
         const h264r_part *parts = (const h264r_part *)(p.motion + m.aux + 4);
-        const int bottom_mb = p.mbaff ? (addr & 1) : 0;
+        // Table 8-10 (H264InterPrediction.cpp:2006-2047): a field MB (MBAFF
+        // field MB or field picture) moves the chroma vector of a reference
+        // field of the other parity by +2 (bottom MB, top field) or -2 (top
+        // MB, bottom field)
+        const int cadj = (field || p.fpic) ? ((p.mbaff ? (addr & 1) : (p.fpic == 2)) ? 2 : -2) : 0;
         const int yAL0 = field ? (y - (y & 1)) / 2 : y;
         const int ymax = field ? p.H / 2 - 1 : p.H - 1;
         const int ymaxc = field ? p.Hc / 2 - 1 : p.Hc - 1;
@@ -538,16 +542,16 @@ __device__ __forceinline__ void inter_body(InterWarpSmem (&smem)[W], const PicDe
             const RefView rv = ref_view(p, ref);
             uint32_t win[18];
             load_luma_window(rv, ymax, x + bx * 4 + 2 * half + (mvx >> 2), yAL0 + by * 4 + (mvy >> 2), win);
+            int cmvy = mvy;
+            if ((cadj > 0) != ((ref & H264R_REF_BOTTOM) != 0) && cadj != 0) cmvy += cadj;
+            // the chroma loads are issued before the luma arithmetic, which
+            // hides their latency
+            uint32_t cw[3];
+            load_chroma_window(half ? rv.cr : rv.cb, rv.cstride, rv.xmaxc, ymaxc, x / 2 + bx * 2 + (mvx >> 3),
+                               yAL0 / 2 + by * 2 + (cmvy >> 3), cw);
             uint32_t o0, o1;
             mc_luma_4x2(win, mvx & 3, mvy & 3, o0, o1);
-            int cmvy = mvy;
-            if (field) {  // Table 8-10 (H264InterPrediction.cpp:2006-2047)
-                const int refbot = (ref & H264R_REF_BOTTOM) ? 1 : 0;
-                if (!refbot && bottom_mb) cmvy += 2;
-                else if (refbot && !bottom_mb) cmvy -= 2;
-            }
-            const uint32_t c = chroma_2x2(half ? rv.cr : rv.cb, rv.cstride, rv.xmaxc, ymaxc, x / 2 + bx * 2 + (mvx >> 3),
-                                          yAL0 / 2 + by * 2 + (cmvy >> 3), mvx & 7, cmvy & 7);
+            const uint32_t c = mc_chroma_2x2(cw[0], cw[1], cw[2], mvx & 7, cmvy & 7);
             if (l) { yb0 = o0; yb1 = o1; cb = c; } else { ya0 = o0; ya1 = o1; ca = c; }
         }
         // ---- weighting (8.4.2.3) and residual, two samples per row
@@ -578,10 +582,10 @@ __device__ __forceinline__ void inter_body(InterWarpSmem (&smem)[W], const PicDe
     __syncwarp();
     // ---- store: 16 luma rows of 16 bytes, 2 x 8 chroma rows of 8 bytes
     if (lane < 16) {
-        *(uint4 *)(plane_y(p) + (size_t)(y + lane * dy) * p.W + x) = *(const uint4 *)(s.out + lane * 16);
+        *(uint4 *)(plane_y(p) + (size_t)(y + lane * dy) * p.ys + x) = *(const uint4 *)(s.out + lane * 16);
     } else {
         const int pl = (lane - 16) >> 3, r = (lane - 16) & 7;
-        *(uint2 *)(plane_c(p, pl) + (size_t)(chroma_row0(y) + r * dy) * p.Wc + x / 2) = *(const uint2 *)(s.out + 256 + pl * 64 + r * 8);
+        *(uint2 *)(plane_c(p, pl) + (size_t)(chroma_row0(y) + r * dy) * p.cs + x / 2) = *(const uint2 *)(s.out + 256 + pl * 64 + r * 8);
     }
 }
 
@@ -706,7 +710,7 @@ __device__ void intra_mb_tiled(const PicDesc &p, int addr, IntraSmem &s, IntraTi
 {
     const int lane = threadIdx.x & 31;
     const h264r_mb m = s.rec[buf];
-    const int W = p.W, Wc = p.Wc, wmb = p.wmb;
+    const int W = p.ys, Wc = p.cs, wmb = p.wmb;  // row pitches
     int x, y, dy;  // first luma sample and row step (2 for a field MB of an MBAFF picture)
     uint8_t *Y = plane_y(p);
     // residual (computed by k_inter, luma raster 16x16, Cb 8x8, Cr 8x8) in
@@ -1216,16 +1220,17 @@ __device__ __forceinline__ int bs_motion(const BlkMotion &a, const BlkMotion &b,
 __device__ int derive_bs(const PicDesc &p, int mbP, int mbQ, int xp, int yp, int xq, int yq, int vertical)
 {
     const h264r_mb P = p.mbs[mbP], Q = p.mbs[mbQ];
-    const int mbaff = p.mbaff;
-    int fP = (P.flags & H264R_MBF_FIELD) && mbaff, fQ = (Q.flags & H264R_MBF_FIELD) && mbaff;
+    const int mbaff = p.mbaff, fpic = p.fpic != 0;
+    // every MB of a field picture is a field MB
+    int fP = ((P.flags & H264R_MBF_FIELD) && mbaff) || fpic, fQ = ((Q.flags & H264R_MBF_FIELD) && mbaff) || fpic;
     int mixed = mbaff && mbP != mbQ && fP != fQ;
     bool intraP = is_intra_type(P.type), intraQ = is_intra_type(Q.type);
     int stP = p.slices[min((uint32_t)P.slice, p.num_slices - 1)].slice_type;
     int stQ = p.slices[min((uint32_t)Q.slice, p.num_slices - 1)].slice_type;
     bool spP = stP == 3 || stP == 4, spQ = stQ == 3 || stQ == 4;
     if (mbP != mbQ) {
-        if ((!fP && !fQ && (intraP || intraQ)) || (!fP && !fQ && (spP || spQ)) || (mbaff && vertical && (intraP || intraQ)) ||
-            (mbaff && vertical && (spP || spQ)))
+        if ((!fP && !fQ && (intraP || intraQ)) || (!fP && !fQ && (spP || spQ)) || ((mbaff || fpic) && vertical && (intraP || intraQ)) ||
+            ((mbaff || fpic) && vertical && (spP || spQ)))
             return 4;
     }
     if ((!mixed && (intraP || intraQ)) || (!mixed && (spP || spQ)) || (mixed && !vertical && (intraP || intraQ)) ||
@@ -1350,7 +1355,8 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
         // lane each (0-15 the MB's blocks in raster order, 16-19 column 3
         // of the left MB, 20-23 row 3 of the MB above); an edge lane takes
         // its two blocks by shuffles.  The rules are derive_bs's for a frame
-        // picture (no field MBs).
+        // picture (no field MBs) or a field picture (all field MBs: bS 3 on
+        // horizontal MB edges of intra MBs, vertical MV limit 2).
         const int dir = lane >> 4, e = (lane >> 2) & 3, b = lane & 3;
         const bool on = e == 0 ? (dir ? c.top : c.left) : (c.internal && (e == 2 || !c.t8));
         const h264r_mb Q = p.mbs[cur];
@@ -1394,7 +1400,7 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
             const int ptype = mbedge ? (dir == 0 ? A.type : B.type) : Q.type;
             const bool spP = mbedge ? (dir == 0 ? sp_of(A) : sp_of(B)) : sp_of(Q), spQ = sp_of(Q);
             if (is_intra_type(ptype) || is_intra_type(Q.type) || spP || spQ) {
-                bs = mbedge ? 4 : 3;
+                bs = mbedge && (dir == 0 || !p.fpic) ? 4 : 3;
             } else {
                 const int qx = dir == 0 ? e : b, qy = dir == 0 ? b : e;
                 const int px = dir == 0 ? (e > 0 ? e - 1 : 3) : b, py = dir == 0 ? b : (e > 0 ? e - 1 : 3);
@@ -1405,7 +1411,7 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
                 const int nzQ = (Q.flags & H264R_MBF_T8x8) ? ((Q.nz8x8 >> (2 * (qy >> 1) + (qx >> 1))) & 1) : ((Q.nz4x4 >> blk4(qx, qy)) & 1);
                 if (nzP || nzQ) bs = 2;
                 else if (ptype == H264R_MB_NONE || Q.type == H264R_MB_NONE) bs = 0xFF;
-                else bs = bs_motion(mp, mq, 4);
+                else bs = bs_motion(mp, mq, p.fpic ? 2 : 4);
             }
         }
         if (bs == 0xFF) mystop = stop_key(cur, dir == 0 ? SEQ_LV0 + e : (e == 0 ? SEQ_LH0 : SEQ_LH4 + e - 1), 4 * b);
@@ -1804,7 +1810,7 @@ __device__ void mbaff_luma_row(const PicDesc &p, int row, int wi, int nw, DbMbaf
     const bool from_cta = wi > 0, to_cta = wi + 1 < nw;
     int seen_used = 0;
     const int lane = threadIdx.x & 31, h = lane >> 4, k = lane & 15;
-    const int uw = (int)p.units_w, W = p.W, y0 = row * 32;
+    const int uw = (int)p.units_w, W = p.ys, y0 = row * 32;
     int *prog = p.progress + p.units_h;
     uint8_t *Y = plane_y(p);
     const DbWin w0 = {(uint8_t *)win, 0, y0 - 8, 20, 40 * 20};
@@ -1907,7 +1913,7 @@ __device__ void mbaff_chroma_row(const PicDesc &p, int row, int wi, int nw, DbMb
     const bool from_cta = wi > 0, to_cta = wi + 1 < nw;
     int seen_used = 0;
     const int lane = threadIdx.x & 31, h = lane >> 4, pl = (lane >> 3) & 1, k = lane & 7;
-    const int uw = (int)p.units_w, Wc = p.Wc, yc0 = row * 16;
+    const int uw = (int)p.units_w, Wc = p.cs, yc0 = row * 16;
     int *prog = p.progress + p.units_h;
     // staging lanes: plane sp, row 8 + sr of the window (and sr when sr < 8)
     const int sp = lane >> 4, sr = lane & 15;
@@ -2108,7 +2114,7 @@ __device__ void deblock_pair_luma(const PicDesc &p, int pair, int wi, int nw, Db
 {
     const int lane = threadIdx.x & 31;
     const int h = lane >> 4, k = lane & 15;
-    const int uw = (int)p.units_w, rows = (int)p.units_h, W = p.W;
+    const int uw = (int)p.units_w, rows = (int)p.units_h, W = p.ys;
     const int row = 2 * pair + h;
     const bool row_ok = row < rows;
     const bool has_second = 2 * pair + 1 < rows;
@@ -2237,7 +2243,7 @@ __device__ void deblock_pair_chroma(const PicDesc &p, int pair, int wi, int nw, 
 {
     const int lane = threadIdx.x & 31;
     const int h = lane >> 4, k = lane & 15, comp = k >> 3, ck = k & 7;
-    const int uw = (int)p.units_w, rows = (int)p.units_h, Wc = p.Wc;
+    const int uw = (int)p.units_w, rows = (int)p.units_h, Wc = p.cs;
     const int row = 2 * pair + h;
     const bool row_ok = row < rows;
     const bool has_second = 2 * pair + 1 < rows;

@@ -95,6 +95,10 @@ extern "C" int h264r_deblock_picture_noalloc(const h264r_picture *pic, uint8_t *
     d.H = d.hmb * 16;
     d.Wc = d.W / 2;
     d.Hc = d.H / 2;
+    d.ys = d.W;
+    d.cs = d.Wc;
+    d.fH = d.H;
+    d.fpic = 0;
     d.mbaff = pic->mbaff;
     d.deblock = 1;
     d.num_mbs = pic->num_mbs;
@@ -111,6 +115,8 @@ extern "C" int h264r_deblock_picture_noalloc(const h264r_picture *pic, uint8_t *
     d.pcm = pic->pcm;
     d.flat_scaling = 1;
     d.dst = planes;
+    d.coff = d.W * d.H;
+    d.cplane = d.Wc * d.Hc;
     d.dpb = planes;
     d.nslots = 1;
     d.bs = s->bs;

@@ -4,6 +4,7 @@
 // arithmetic, no library distributions.
 #include "../../include/h264r_synth.h"
 
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -34,6 +35,7 @@ struct Plan {
     std::vector<int> poc0, poc1;
     int poc;
     int group;
+    int structure = H264R_STRUCT_FRAME;  // field pictures: H264R_STRUCT_TOP / _BOTTOM
 };
 
 inline int clip3(int lo, int hi, int v) { return v < lo ? lo : (v > hi ? hi : v); }
@@ -116,6 +118,47 @@ static void build_plan(h264r_synth *g)
         }
         if (k + 1 < anchors.size()) add_anchor(anchors[k + 1], grp);
     }
+}
+
+// PAFF: frames coded as a top and a bottom field picture (top first) in
+// the same slot.  The fields reference fields of the frames the frame would
+// reference; the second field of a P or B frame may also reference the first
+// (the slot itself, at the front of list 0).  Dependency groups are then
+// recomputed from the slots each picture reads and writes: a picture comes
+// after the writers of what it reads, after the readers and the writer of
+// the slot it writes.
+static void split_fields(h264r_synth *g)
+{
+    const h264r_synth_cfg &c = g->cfg;
+    std::vector<Plan> out;
+    for (const Plan &f : g->plan) {
+        if (!g->rng.pct(c.paff_percent)) {
+            out.push_back(f);
+            continue;
+        }
+        Plan t = f, b = f;
+        t.structure = H264R_STRUCT_TOP;
+        b.structure = H264R_STRUCT_BOTTOM;
+        b.poc = f.poc + 1;
+        if (f.type != PIC_I) {
+            b.l0.insert(b.l0.begin(), f.slot);
+            b.poc0.insert(b.poc0.begin(), f.poc);
+        }
+        out.push_back(t);
+        out.push_back(b);
+    }
+    std::vector<int> writer(g->dpb_slots, -1), reader(g->dpb_slots, -1);
+    for (Plan &p : out) {
+        int grp = std::max(writer[p.slot], reader[p.slot]) + 1;
+        for (int sl : p.l0) grp = std::max(grp, writer[sl] + 1);
+        for (int sl : p.l1) grp = std::max(grp, writer[sl] + 1);
+        for (int sl : p.l0) reader[sl] = std::max(reader[sl], grp);
+        for (int sl : p.l1) reader[sl] = std::max(reader[sl], grp);
+        writer[p.slot] = grp;
+        reader[p.slot] = -1;
+        p.group = grp;
+    }
+    g->plan.swap(out);
 }
 
 // ---- intra mode choice: modes whose neighbours exist (single slice, no CIP)
@@ -210,7 +253,9 @@ static void make_picture(h264r_synth *g, const Plan &pl)
 {
     const h264r_synth_cfg &c = g->cfg;
     Rng &r = g->rng;
-    const int W = c.width_mbs, H = c.height_mbs, n = W * H;
+    // a field picture is a grid of W x H/2 field MBs
+    const bool fpic = pl.structure != H264R_STRUCT_FRAME;
+    const int W = c.width_mbs, H = fpic ? c.height_mbs / 2 : c.height_mbs, n = W * H;
     g->mbs.assign(n, h264r_mb());
     g->slices.clear();
     g->weights.clear();
@@ -232,7 +277,8 @@ static void make_picture(h264r_synth *g, const Plan &pl)
     // further slices every slice_rows MB rows (MB-pair rows for MBAFF), and
     // constrained intra prediction; the extra draws happen only when asked
     // for, so streams without them are unchanged
-    const int unit_rows = c.mbaff ? H / 2 : H;
+    const bool mbaff = c.mbaff != 0 && !fpic;
+    const int unit_rows = mbaff ? H / 2 : H;
     if (c.slice_rows > 0) {
         const int nslices = (unit_rows + c.slice_rows - 1) / c.slice_rows;
         for (int k = 0; k < nslices; k++) {
@@ -300,7 +346,6 @@ static void make_picture(h264r_synth *g, const Plan &pl)
 
     // MBAFF: MBs in pair order (top, bottom); the pair's field decision is
     // taken at its top MB
-    const bool mbaff = c.mbaff != 0;
     bool pair_field = false;
     for (int a = 0; a < n; a++) {
         const int mx = mbaff ? (a / 2) % W : a % W;
@@ -312,6 +357,7 @@ static void make_picture(h264r_synth *g, const Plan &pl)
         if (mbaff && (a & 1) == 0) pair_field = r.pct(c.field_percent);
         const bool field = mbaff && pair_field;
         if (field) m.flags |= H264R_MBF_FIELD;
+        const bool field_refs = field || fpic;  // predicts from fields
         m.qpy = (uint8_t)r.range(c.qp_min, c.qp_max);
         m.slice = (uint16_t)(c.slice_rows > 0 ? (mbaff ? (a / 2) / W : a / W) / c.slice_rows : 0);
         if (cip) m.flags |= H264R_MBF_CIP;
@@ -324,16 +370,33 @@ static void make_picture(h264r_synth *g, const Plan &pl)
             else if (roll < 450) m.type = H264R_MB_I4x4;
             else if (roll < 750) m.type = c.transform8x8 ? H264R_MB_I8x8 : H264R_MB_I4x4;
             else m.type = H264R_MB_I16x16;
-            // MBAFF neighbourhoods depend on the pairs around: DC modes only,
-            // which need no neighbour
             // neighbours usable for intra prediction: same slice, and not an
             // inter MB under constrained intra prediction
             auto usable = [&](int nb) {
                 const h264r_mb &q = g->mbs[nb];
                 return q.slice == m.slice && !(cip && q.type == H264R_MB_INTER);
             };
-            bool A = !mbaff && mx > 0 && usable(a - 1), B = !mbaff && my > 0 && usable(a - W);
-            bool D = !mbaff && mx > 0 && my > 0 && usable(a - W - 1);
+            bool A, B, D;
+            if (!mbaff) {
+                A = mx > 0 && usable(a - 1);
+                B = my > 0 && usable(a - W);
+                D = mx > 0 && my > 0 && usable(a - W - 1);
+            } else {
+                // MBAFF (6.4.12.2, Table 6-4): the left samples lie in the
+                // left pair; the samples above a top MB, or above a field MB,
+                // in the pair above; above a bottom frame MB in the top MB of
+                // its own pair; the corner sample of a bottom frame MB in the
+                // left pair, of any other MB in the pair above-left.  A pair
+                // counts as usable when both its MBs are (under constrained
+                // intra prediction the samples of a frame MB beside a field
+                // pair come from both MBs).
+                const int pa = a / 2, pc = pa % W, pr = pa / W;
+                auto pair_ok = [&](int q) { return usable(2 * q) && usable(2 * q + 1); };
+                const bool upper = (a & 1) == 0 || field;
+                A = pc > 0 && pair_ok(pa - 1);
+                B = upper ? pr > 0 && pair_ok(pa - W) : usable(a - 1);
+                D = upper ? pc > 0 && pr > 0 && pair_ok(pa - W - 1) : A;
+            }
             if (m.type == H264R_MB_IPCM) {
                 m.aux = (uint32_t)(g->pcm.size() / 384);
                 for (int i = 0; i < 384; i++) g->pcm.push_back((uint8_t)r.range(0, 255));
@@ -344,7 +407,7 @@ static void make_picture(h264r_synth *g, const Plan &pl)
                 static const int by[16] = {0, 0, 1, 1, 0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 3, 3};
                 for (int b = 0; b < 16; b++) {
                     bool left = bx[b] > 0 || A, top = by[b] > 0 || B, corner = left && top && (bx[b] > 0 || by[b] > 0 || D);
-                    const int md = mbaff ? 2 : pick4(r, top, left, corner);
+                    const int md = pick4(r, top, left, corner);
                     m.ipred[b >> 3] |= (uint32_t)md << (4 * (b & 7));
                     if (make_block(r, cb, b, 0, 16, dens, 1)) m.nz4x4 |= (uint16_t)(1u << b);
                 }
@@ -353,7 +416,7 @@ static void make_picture(h264r_synth *g, const Plan &pl)
                 for (int b = 0; b < 4; b++) {
                     int x8 = b & 1, y8 = b >> 1;
                     bool left = x8 > 0 || A, top = y8 > 0 || B, corner = left && top && (x8 > 0 || y8 > 0 || D);
-                    const int md = mbaff ? 2 : pick4(r, top, left, corner);
+                    const int md = pick4(r, top, left, corner);
                     m.ipred[0] |= (uint32_t)md << (4 * b);
                     if (make_block(r, cb, b, 0, 64, dens, 4)) m.nz8x8 |= (uint8_t)(1u << b);
                 }
@@ -452,8 +515,10 @@ static void make_picture(h264r_synth *g, const Plan &pl)
                     int slot = l == 0 ? pl.l0[rr[l]] : pl.l1[rr[l]];
                     p.ref[l] = (int8_t)slot;
                     p.dref[l] = (int8_t)slot;
-                    if (field) {  // a field of the reference frame, either parity
-                        p.ref[l] = (int8_t)(slot | H264R_REF_FIELD | (r.pct(50) ? H264R_REF_BOTTOM : 0));
+                    if (field_refs) {  // a field of the reference frame, either parity
+                        // (the first field of the current frame, for a second field)
+                        const bool bot = slot == pl.slot ? false : r.pct(50);
+                        p.ref[l] = (int8_t)(slot | H264R_REF_FIELD | (bot ? H264R_REF_BOTTOM : 0));
                         p.dref[l] = (int8_t)(p.ref[l] & 0x7F);
                     }
                     int mvx, mvy;
@@ -475,7 +540,7 @@ static void make_picture(h264r_synth *g, const Plan &pl)
                         if (side == 3) mvy = ((H - my) * 16 + r.range(0, 48)) * 4;
                         mvx = clip3(-2048, 2047, mvx);
                         mvy = clip3(-512, 511, mvy);
-                        if (field) mvy /= 2;  // field rows
+                        if (field) mvy /= 2;  // field rows (a field picture's grid is in field rows already)
                     } else {
                         mvx = r.range(-c.mv_range, c.mv_range);
                         mvy = r.range(-c.mv_range, c.mv_range);
@@ -518,7 +583,7 @@ static void make_picture(h264r_synth *g, const Plan &pl)
 extern "C" int h264r_synth_create(const h264r_synth_cfg *cfg, h264r_synth **out)
 {
     if (!cfg || !out || cfg->width_mbs == 0 || cfg->height_mbs == 0 || cfg->num_pictures == 0 || cfg->qp_min > cfg->qp_max ||
-        cfg->qp_max > 51 || (cfg->mbaff && (cfg->height_mbs & 1)))
+        cfg->qp_max > 51 || ((cfg->mbaff || cfg->paff_percent) && (cfg->height_mbs & 1)))
         return H264R_ERR_INVALID_ARG;
     h264r_synth *g = new (std::nothrow) h264r_synth();
     if (!g) return H264R_ERR_NO_MEMORY;
@@ -527,6 +592,7 @@ extern "C" int h264r_synth_create(const h264r_synth_cfg *cfg, h264r_synth **out)
     if (g->cfg.num_refs > 4) g->cfg.num_refs = 4;
     g->rng.s = 0x5EED0000ull ^ cfg->seed;
     build_plan(g);
+    if (cfg->paff_percent > 0) split_fields(g);
     *out = g;
     return H264R_OK;
 }
@@ -542,8 +608,8 @@ extern "C" int h264r_synth_next(h264r_synth *g, h264r_picture *pic, int *depende
     memset(pic, 0, sizeof(*pic));
     pic->width_mbs = g->cfg.width_mbs;
     pic->height_mbs = g->cfg.height_mbs;
-    pic->structure = H264R_STRUCT_FRAME;
-    pic->mbaff = g->cfg.mbaff ? 1 : 0;
+    pic->structure = (uint8_t)pl.structure;
+    pic->mbaff = g->cfg.mbaff && pl.structure == H264R_STRUCT_FRAME ? 1 : 0;
     pic->dst_slot = (uint8_t)pl.slot;
     pic->deblock = 1;
     pic->num_slices = (uint16_t)g->slices.size();

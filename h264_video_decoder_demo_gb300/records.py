@@ -191,7 +191,8 @@ class CSynthCfg(ctypes.Structure):
                 ("edge_mv_percent", ctypes.c_uint8), ("mv_range", ctypes.c_int16),
                 ("filter_offset_max", ctypes.c_int8), ("coef_density", ctypes.c_uint8),
                 ("mbaff", ctypes.c_uint8), ("field_percent", ctypes.c_uint8),
-                ("slice_rows", ctypes.c_uint8), ("cip_percent", ctypes.c_uint8)]
+                ("slice_rows", ctypes.c_uint8), ("cip_percent", ctypes.c_uint8),
+                ("paff_percent", ctypes.c_uint8)]
 
 
 class CWriterCfg(ctypes.Structure):

@@ -179,7 +179,11 @@ typedef struct h264r_slice {
 typedef struct h264r_picture {
     uint16_t width_mbs;        /* PicWidthInMbs                              */
     uint16_t height_mbs;       /* FrameHeightInMbs                           */
-    uint8_t  structure;        /* H264R_STRUCT_*                             */
+    uint8_t  structure;        /* H264R_STRUCT_*: a field picture (TOP /
+                                  BOTTOM) writes its field's lines of
+                                  dst_slot, reads fields only (its own slot's
+                                  other field allowed), num_mbs is half the
+                                  frame's, mbaff 0                           */
     uint8_t  mbaff;            /* MbaffFrameFlag                             */
     uint8_t  dst_slot;         /* DPB slot that receives the samples         */
     uint8_t  deblock;          /* 1: run the 8.7 deblocking filter           */

@@ -49,6 +49,10 @@ typedef struct h264r_synth_cfg {
                                    offsets and deblocking mode (0, 1 or 2)    */
     uint8_t  cip_percent;       /* P/B pictures coded with
                                    constrained_intra_pred_flag               */
+    uint8_t  paff_percent;      /* frames coded as two field pictures (PAFF:
+                                   top then bottom, in the frame's slot;
+                                   height_mbs even), the others as frames
+                                   (MBAFF frames when mbaff is set)          */
 } h264r_synth_cfg;
 
 typedef struct h264r_synth h264r_synth;

@@ -75,11 +75,21 @@ static const uint8_t kBlkX[16] = {0, 1, 0, 1, 2, 3, 2, 3, 0, 1, 0, 1, 2, 3, 2, 3
 static const uint8_t kBlkY[16] = {0, 0, 1, 1, 0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 3, 3};
 
 /* ------------------------------------------------------------------------ */
+/* A field picture (PAFF, structure TOP / BOTTOM) is reconstructed and
+   filtered in a view of its field: W x H are the field's size, the planes
+   start on the field's first line and step two frame lines (ys, cs), so MB
+   geometry, neighbours (6.4.12.1) and filtering are those of a frame of the
+   field's size.  Its MBs are field MBs all the same: field scans (8.5.6),
+   field reference views, the chroma vector offset of Table 8-10 and the
+   field rules of the bS derivation (8.7.2.1). */
 typedef struct {
     const h264r_picture *pic;
-    int wmb, hmb;          /* frame size in MBs */
-    int W, H, Wc, Hc;      /* frame size in samples */
-    uint8_t *Y, *Cb, *Cr;  /* destination planes */
+    int wmb, hmb;          /* picture size in MBs (a field picture: its field) */
+    int W, H, Wc, Hc;      /* picture size in samples */
+    int fW, fH;            /* frame size in samples (the DPB slot layout) */
+    int fpic;              /* 0 frame, 1 top field, 2 bottom field */
+    int ys, cs;            /* row strides of the destination view */
+    uint8_t *Y, *Cb, *Cr;  /* destination planes (a field picture: its first line) */
     uint8_t *const *dpb;
     int nslots;
 } octx;
@@ -119,6 +129,9 @@ static int is_field_mb(const octx *c, int addr)
 {
     return c->pic->mbaff && (c->pic->mbs[addr].flags & H264R_MBF_FIELD);
 }
+
+/* field scans and field rules: MBAFF field MBs and every MB of a field picture */
+static int field_coded(const octx *c, int addr) { return is_field_mb(c, addr) || c->fpic != 0; }
 
 static int is_intra_type(int t) { return t == H264R_MB_I4x4 || t == H264R_MB_I8x8 || t == H264R_MB_I16x16; }
 
@@ -333,10 +346,10 @@ static void chroma_dc(const octx *c, const int32_t *lv, int field, int qpc, int 
 }
 
 /* ---- sample access ------------------------------------------------------ */
-static inline uint8_t *lum(const octx *c, int x, int y) { return c->Y + (size_t)y * c->W + x; }
+static inline uint8_t *lum(const octx *c, int x, int y) { return c->Y + (size_t)y * c->ys + x; }
 static inline uint8_t *chr(const octx *c, int pl, int x, int y)
 {
-    return (pl ? c->Cr : c->Cb) + (size_t)y * c->Wc + x;
+    return (pl ? c->Cr : c->Cb) + (size_t)y * c->cs + x;
 }
 
 /* Luma / chroma residual of one MB, added to the prediction already in the
@@ -358,16 +371,16 @@ static void chroma_residual(const octx *c, int addr, const coefs *k, int ls_list
     const h264r_slice *s = &c->pic->slices[m->slice];
     int x, y, dy;
     mb_origin(c, addr, &x, &y, &dy);
-    int field = is_field_mb(c, addr);
+    int field = is_field_mb(c, addr), sf = field_coded(c, addr);
     int xc = x / 2, yc = (y >> 4) * 8 + (y & 1);
     if (c->pic->mbaff && !field) yc = y / 2;
     for (int pl = 0; pl < 2; pl++) {
         int qpc = chroma_qp(m->qpy, s->chroma_qp_offset[pl]);
         int32_t dcC[4];
-        chroma_dc(c, k->cdc[pl], field, qpc, ls_list, dcC);
+        chroma_dc(c, k->cdc[pl], sf, qpc, ls_list, dcC);
         for (int b = 0; b < 4; b++) {
             int32_t r[4][4];
-            residual4x4(c, k->cac[pl][b], field, qpc, ls_list, 1, dcC[b], r);
+            residual4x4(c, k->cac[pl][b], sf, qpc, ls_list, 1, dcC[b], r);
             int bx = (b & 1) * 4, by = (b >> 1) * 4;
             for (int i = 0; i < 4; i++)
                 for (int j = 0; j < 4; j++) {
@@ -828,7 +841,7 @@ static int recon_intra(octx *c, int addr)
     if (rc) return rc;
     int x, y, dy;
     mb_origin(c, addr, &x, &y, &dy);
-    int field = is_field_mb(c, addr);
+    int field = is_field_mb(c, addr), sf = field_coded(c, addr);
     int qp = m->qpy;
     if (m->type == H264R_MB_I4x4) {
         /* transform_decoding_process_for_4x4_luma_residual_blocks (3401) */
@@ -840,7 +853,7 @@ static int recon_intra(octx *c, int addr)
                 for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) *lum(c, bx + j, by + i * dy) = pred[i * 4 + j];
             }
             int32_t r[4][4];
-            residual4x4(c, k.l4[b], field, qp, 0, 0, 0, r);
+            residual4x4(c, k.l4[b], sf, qp, 0, 0, 0, r);
             for (int i = 0; i < 4; i++)
                 for (int j = 0; j < 4; j++) { uint8_t *p = lum(c, bx + j, by + i * dy); *p = (uint8_t)clip1(*p + r[i][j]); }
         }
@@ -854,18 +867,18 @@ static int recon_intra(octx *c, int addr)
                 for (int i = 0; i < 8; i++) for (int j = 0; j < 8; j++) *lum(c, bx + j, by + i * dy) = pred[i * 8 + j];
             }
             int32_t r[8][8];
-            residual8x8(c, k.l8[b], field, qp, 0, r);
+            residual8x8(c, k.l8[b], sf, qp, 0, r);
             for (int i = 0; i < 8; i++)
                 for (int j = 0; j < 8; j++) { uint8_t *p = lum(c, bx + j, by + i * dy); *p = (uint8_t)clip1(*p + r[i][j]); }
         }
     } else {
         /* transform_decoding_process_for_luma_samples_of_Intra_16x16 (3507) */
         int32_t dcY[4][4];
-        luma_dc(c, k.dc, field, qp, dcY);
+        luma_dc(c, k.dc, sf, qp, dcY);
         int32_t rmb[16][16];
         for (int b = 0; b < 16; b++) {
             int32_t r[4][4];
-            residual4x4(c, k.l4[b], field, qp, 0, 1, dcY[kBlkY[b]][kBlkX[b]], r);
+            residual4x4(c, k.l4[b], sf, qp, 0, 1, dcY[kBlkY[b]][kBlkX[b]], r);
             for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) rmb[kBlkY[b] * 4 + i][kBlkX[b] * 4 + j] = r[i][j];
         }
         uint8_t pred[256];
@@ -936,26 +949,30 @@ typedef struct {
 /* Reference plane view.  Frame references: the frame.  Field references of
    MBAFF field MBs: the frame's field view, whose PicWidthInSamples is the
    doubled stride (H264PictureBase.cpp:204-227); the reference clamps x to
-   that doubled width (quirk, H264InterPrediction.cpp:2363, 2504-2507). */
+   that doubled width (quirk, H264InterPrediction.cpp:2363, 2504-2507).
+   Field pictures read fields only, clamped to the picture width as 8.4.2.2
+   has it (the reference decodes no field picture to follow). */
 static int ref_view(const octx *c, int ref, refplanes *rp)
 {
     int slot = H264R_REF_SLOT(ref);
     if (slot >= c->nslots || !c->dpb[slot]) return H264R_ERR_BAD_RECORD;
+    if (c->fpic && !(ref & H264R_REF_FIELD)) return H264R_ERR_BAD_RECORD;
+    const int W = c->fW, H = c->fH, Wc = W / 2, Hc = H / 2;
     const uint8_t *base = c->dpb[slot];
-    const uint8_t *cb = base + (size_t)c->W * c->H, *cr = cb + (size_t)c->Wc * c->Hc;
+    const uint8_t *cb = base + (size_t)W * H, *cr = cb + (size_t)Wc * Hc;
     if (ref & H264R_REF_FIELD) {
         int bot = (ref & H264R_REF_BOTTOM) ? 1 : 0;
-        rp->y = base + bot * c->W;
-        rp->cb = cb + bot * c->Wc;
-        rp->cr = cr + bot * c->Wc;
-        rp->ystride = 2 * c->W;
-        rp->cstride = 2 * c->Wc;
-        rp->xmax = 2 * c->W - 1;
-        rp->xmaxc = 2 * c->Wc - 1;
+        rp->y = base + bot * W;
+        rp->cb = cb + bot * Wc;
+        rp->cr = cr + bot * Wc;
+        rp->ystride = 2 * W;
+        rp->cstride = 2 * Wc;
+        rp->xmax = c->fpic ? W - 1 : 2 * W - 1;
+        rp->xmaxc = c->fpic ? Wc - 1 : 2 * Wc - 1;
     } else {
         rp->y = base; rp->cb = cb; rp->cr = cr;
-        rp->ystride = c->W; rp->cstride = c->Wc;
-        rp->xmax = c->W - 1; rp->xmaxc = c->Wc - 1;
+        rp->ystride = W; rp->cstride = Wc;
+        rp->xmax = W - 1; rp->xmaxc = Wc - 1;
     }
     return 0;
 }
@@ -1046,13 +1063,14 @@ static int recon_inter(octx *c, int addr)
     const h264r_part *parts = (const h264r_part *)(pic->motion + m->aux + 4);
     int x, y, dy;
     mb_origin(c, addr, &x, &y, &dy);
-    const int field = is_field_mb(c, addr);
+    const int field = is_field_mb(c, addr), sf = field_coded(c, addr);
     /* xAL/yAL in the (field) picture the MB predicts from
-       (Inter_prediction_process, H264InterPrediction.cpp:574-580) */
+       (Inter_prediction_process, H264InterPrediction.cpp:574-580); a field
+       picture's view is its field already */
     int yAL0 = field ? ((y - (y & 1)) / 2) : y;
     int ymax = field ? c->H / 2 - 1 : c->H - 1;
     int ymaxc = field ? c->Hc / 2 - 1 : c->Hc - 1;
-    int bottom_mb = c->pic->mbaff ? (addr & 1) : 0;
+    int bottom_mb = c->pic->mbaff ? (addr & 1) : (c->fpic == 2);
     int xc0 = x / 2, yc0 = field ? (((y >> 4) * 8 + (y & 1))) : y / 2;
     for (int b = 0; b < 16; b++) {
         int bx = b & 3, by = b >> 2; /* raster 4x4 */
@@ -1070,7 +1088,7 @@ static int recon_inter(octx *c, int addr)
             if (rc) return rc;
             /* 8.4.1.4 chroma vector, Table 8-10 (H264InterPrediction.cpp:2006-2047) */
             mvcy[l] = p->mv[l][1];
-            if (field) {
+            if (sf) {
                 int refbot = (p->ref[l] & H264R_REF_BOTTOM) ? 1 : 0;
                 if (!refbot && bottom_mb) mvcy[l] += 2;
                 else if (refbot && !bottom_mb) mvcy[l] -= 2;
@@ -1111,7 +1129,7 @@ static int recon_inter(octx *c, int addr)
     if (m->flags & H264R_MBF_T8x8) {
         for (int b = 0; b < 4; b++) {
             int32_t r[8][8];
-            residual8x8(c, k.l8[b], field, qp, 1, r);
+            residual8x8(c, k.l8[b], sf, qp, 1, r);
             int bx = x + (b & 1) * 8, by = y + (b >> 1) * 8 * dy;
             for (int i = 0; i < 8; i++)
                 for (int j = 0; j < 8; j++) { uint8_t *pp = lum(c, bx + j, by + i * dy); *pp = (uint8_t)clip1(*pp + r[i][j]); }
@@ -1119,7 +1137,7 @@ static int recon_inter(octx *c, int addr)
     } else {
         for (int b = 0; b < 16; b++) {
             int32_t r[4][4];
-            residual4x4(c, k.l4[b], field, qp, 3, 0, 0, r);
+            residual4x4(c, k.l4[b], sf, qp, 3, 0, 0, r);
             int bx = x + kBlkX[b] * 4, by = y + kBlkY[b] * 4 * dy;
             for (int i = 0; i < 4; i++)
                 for (int j = 0; j < 4; j++) { uint8_t *pp = lum(c, bx + j, by + i * dy); *pp = (uint8_t)clip1(*pp + r[i][j]); }
@@ -1168,8 +1186,9 @@ static int derive_bs(const octx *c, int mbP, int mbQ, int xp, int yp, int xq, in
 {
     const h264r_picture *pic = c->pic;
     const h264r_mb *P = &pic->mbs[mbP], *Q = &pic->mbs[mbQ];
-    const int mbaff = pic->mbaff;
-    int fP = (P->flags & H264R_MBF_FIELD) && mbaff, fQ = (Q->flags & H264R_MBF_FIELD) && mbaff;
+    const int mbaff = pic->mbaff, fpic = c->fpic != 0;
+    /* every MB of a field picture is a field MB */
+    int fP = ((P->flags & H264R_MBF_FIELD) && mbaff) || fpic, fQ = ((Q->flags & H264R_MBF_FIELD) && mbaff) || fpic;
     int mixed = mbaff && mbP != mbQ && fP != fQ;
     int intraP = is_intra_type(P->type), intraQ = is_intra_type(Q->type);
     int spP = pic->slices[P->slice].slice_type == 3 || pic->slices[P->slice].slice_type == 4;
@@ -1177,7 +1196,7 @@ static int derive_bs(const octx *c, int mbP, int mbQ, int xp, int yp, int xq, in
     /* 994-1310 */
     if (mbP != mbQ) {
         if ((!fP && !fQ && (intraP || intraQ)) || (!fP && !fQ && (spP || spQ)) ||
-            (mbaff && vertical && (intraP || intraQ)) || (mbaff && vertical && (spP || spQ)))
+            ((mbaff || fpic) && vertical && (intraP || intraQ)) || ((mbaff || fpic) && vertical && (spP || spQ)))
             return 4;
     }
     if ((!mixed && (intraP || intraQ)) || (!mixed && (spP || spQ)) ||
@@ -1266,7 +1285,7 @@ static void filter_edge(dbctx *d, int cur, int comp, int vertical, int e, int mb
     const int chroma = comp != 0;
     const int nE = chroma ? 8 : 16;
     uint8_t *plane = comp == 0 ? c->Y : (comp == 1 ? c->Cb : c->Cr);
-    const int stride = chroma ? c->Wc : c->W;
+    const int stride = chroma ? c->cs : c->ys;
     const int ddy = 1 + fieldMode;
     int xI, yI, dyI;
     mb_origin(c, cur, &xI, &yI, &dyI);
@@ -1407,21 +1426,28 @@ static int deblock_picture(octx *c)
 static int setup(octx *c, const h264r_picture *pic, uint8_t *const *dpb, int nslots)
 {
     if (!pic || !dpb) return H264R_ERR_INVALID_ARG;
-    if (pic->structure != H264R_STRUCT_FRAME) return H264R_ERR_UNSUPPORTED;
+    if (pic->structure > H264R_STRUCT_BOTTOM) return H264R_ERR_BAD_RECORD;
     if (pic->dst_slot >= nslots || !dpb[pic->dst_slot]) return H264R_ERR_INVALID_ARG;
     memset(c, 0, sizeof(*c));
     c->pic = pic;
+    c->fpic = pic->structure;
     c->wmb = pic->width_mbs;
-    c->hmb = pic->height_mbs;
+    c->hmb = c->fpic ? pic->height_mbs / 2 : pic->height_mbs;
+    if (c->fpic && (pic->mbaff || (pic->height_mbs & 1))) return H264R_ERR_BAD_RECORD;
     if (pic->num_mbs != (uint32_t)c->wmb * c->hmb) return H264R_ERR_BAD_RECORD;
     if (pic->mbaff && (c->hmb & 1)) return H264R_ERR_BAD_RECORD;
-    c->W = c->wmb * 16;
+    c->fW = c->wmb * 16;
+    c->fH = pic->height_mbs * 16;
+    c->W = c->fW;
     c->H = c->hmb * 16;
     c->Wc = c->W / 2;
     c->Hc = c->H / 2;
-    c->Y = dpb[pic->dst_slot];
-    c->Cb = c->Y + (size_t)c->W * c->H;
-    c->Cr = c->Cb + (size_t)c->Wc * c->Hc;
+    const int bot = c->fpic == H264R_STRUCT_BOTTOM;
+    c->ys = c->fpic ? 2 * c->fW : c->fW;
+    c->cs = c->ys / 2;
+    c->Y = dpb[pic->dst_slot] + (size_t)bot * c->fW;
+    c->Cb = dpb[pic->dst_slot] + (size_t)c->fW * c->fH + (size_t)bot * (c->fW / 2);
+    c->Cr = c->Cb + (size_t)(c->fW / 2) * (c->fH / 2);
     c->dpb = dpb;
     c->nslots = nslots;
     for (uint32_t i = 0; i < pic->num_mbs; i++) {
@@ -1436,9 +1462,19 @@ int h264o_reconstruct(const h264r_picture *pic, uint8_t *const *dpb, int nslots,
     octx c;
     int rc = setup(&c, pic, dpb, nslots);
     if (rc) return rc;
-    size_t planes = (size_t)c.W * c.H * 3 / 2;
-    /* CH264PictureBase::reset clears a reused picture (H264PictureBase.cpp:44-60) */
-    memset(c.Y, 0, planes);
+    size_t planes = (size_t)c.fW * c.fH * 3 / 2;
+    uint8_t *slot = dpb[pic->dst_slot];
+    /* CH264PictureBase::reset clears a reused picture (H264PictureBase.cpp:44-60);
+       a field picture clears its own field's lines */
+    if (!c.fpic) {
+        memset(slot, 0, planes);
+    } else {
+        for (int r = 0; r < c.H; r++) memset(c.Y + (size_t)r * c.ys, 0, (size_t)c.W);
+        for (int r = 0; r < c.Hc; r++) {
+            memset(c.Cb + (size_t)r * c.cs, 0, (size_t)c.Wc);
+            memset(c.Cr + (size_t)r * c.cs, 0, (size_t)c.Wc);
+        }
+    }
     for (uint32_t a = 0; a < pic->num_mbs; a++) {
         const h264r_mb *m = &pic->mbs[a];
         switch (m->type) {
@@ -1449,7 +1485,7 @@ int h264o_reconstruct(const h264r_picture *pic, uint8_t *const *dpb, int nslots,
         }
         if (rc) return rc;
     }
-    if (pre) memcpy(pre, c.Y, planes);
+    if (pre) memcpy(pre, slot, planes);
     if (pic->deblock) rc = deblock_picture(&c);
     return rc;
 }

@@ -178,3 +178,47 @@ def test_mbaff_intra_heavy_matches_oracle(gpu_ctx):
 
 def test_1080i_mbaff_matches_oracle(gpu_ctx):
     assert run_against_oracle(gpu_ctx, h.synth("1080i_mbaff", seed=9), npics=6) == 6
+
+
+# Field pictures (PAFF): the reference decoder aborts on field pictures
+# (tests/golden/paff_probe.json), so these are pinned to the oracle's
+# restatement of the standard, itself pinned to its frame path
+# (tests/test_oracle_paff.py).
+def test_paff_cif_matches_oracle(gpu_ctx):
+    """Every frame coded as a top and a bottom field picture: I, P and B
+    field pairs, second fields that read the first, 8x8 transforms, MVs past
+    the edges, deblocking with the field rules."""
+    g = h.synth("cif_ippp", seed=21, num_pictures=8, paff_percent=100, gop_kind=1, num_refs=2, transform8x8=1,
+                mv_range=128, edge_mv_percent=10, intra_percent=20)
+    assert run_against_oracle(gpu_ctx, g) == 16
+
+
+def test_1080i_mbaff_and_paff_matches_oracle(gpu_ctx):
+    """1080i with half the frames as field pairs and half as MBAFF frames."""
+    g = h.synth("1080i_mbaff", seed=22, paff_percent=50)
+    assert run_against_oracle(gpu_ctx, g, npics=8) == 8
+
+
+def test_paff_batched_matches_oracle(gpu_ctx):
+    """Field pictures of several streams in one batch, by dependency group
+    (a second field comes after its first)."""
+    gens = [h.synth("cif_ippp", seed=30 + i, num_pictures=6, paff_percent=60, gop_kind=1, num_refs=2) for i in range(3)]
+    streams = [list(g) for g in gens]
+    slots = gens[0].dpb_slots
+    w, hh = streams[0][0].width_mbs, streams[0][0].height_mbs
+    dpbs = [OracleDPB(w, hh, slots) for _ in streams]
+    ss = [h.Stream(gpu_ctx, w, hh, slots) for _ in streams]
+    try:
+        ngroups = max(p.group for st in streams for p in st) + 1
+        for grp in range(ngroups):
+            batch = [(i, p) for i, st in enumerate(streams) for p in st if p.group == grp]
+            if not batch:
+                continue
+            gpu_ctx.submit_batch([ss[i] for i, _ in batch], [p for _, p in batch])
+            for i, p in batch:
+                rc, _ = dpbs[i].reconstruct(p)
+                assert rc == 0
+                assert np.array_equal(ss[i].output(p.dst_slot), dpbs[i].planes(p.dst_slot)), (grp, i)
+    finally:
+        for s in ss:
+            s.close()
