@@ -112,6 +112,7 @@ public:
         cv_.notify_all();
         for (auto &t : th_) t.join();
     }
+    int size() const { return (int)th_.size(); }
     // fn(0) .. fn(n-1), on the workers and the calling thread; returns when all are done
     void run(int n, const std::function<void(int)> &fn)
     {
@@ -498,7 +499,8 @@ static uint32_t picture_mbs(const h264r_picture *pic)
     return (uint32_t)pic->width_mbs * rows;
 }
 
-extern "C" int h264r_validate_picture(const h264r_picture *pic, int dpb_slots)
+// Picture-level checks: geometry, parameter tables (everything but the MBs).
+static int validate_header(const h264r_picture *pic, int dpb_slots)
 {
     if (!pic || !pic->mbs || !pic->slices || !pic->weights) return H264R_ERR_INVALID_ARG;
     if (pic->structure > H264R_STRUCT_BOTTOM) return H264R_ERR_BAD_RECORD;
@@ -517,67 +519,100 @@ extern "C" int h264r_validate_picture(const h264r_picture *pic, int dpb_slots)
             pic->slices[i].filter_offset_a < -12 || pic->slices[i].filter_offset_a > 12 ||
             pic->slices[i].filter_offset_b < -12 || pic->slices[i].filter_offset_b > 12)
             return H264R_ERR_BAD_RECORD;
-    for (uint32_t a = 0; a < pic->num_mbs; a++) {
+    return H264R_OK;
+}
+
+// MBs [a0, a1) of a picture whose header passed: ranges, payload offsets and
+// sizes, references.  The significance words of a coefficient payload are
+// counted 64 bits at a time.
+static int validate_mbs(const h264r_picture *pic, int dpb_slots, uint32_t a0, uint32_t a1)
+{
+    const bool fpic = pic->structure != H264R_STRUCT_FRAME;
+    const uint64_t coef_bytes = pic->coef_bytes, motion_bytes = pic->motion_bytes;
+    const uint32_t nslices = pic->num_slices, nweights = pic->num_weights, npcm = pic->num_pcm;
+    const int dst = pic->dst_slot;
+    const bool own_bottom = pic->structure == H264R_STRUCT_BOTTOM;
+    for (uint32_t a = a0; a < a1; a++) {
         const h264r_mb &m = pic->mbs[a];
-        if (m.type > H264R_MB_NONE || m.qpy > 51 || m.slice >= pic->num_slices || m.i16_mode > 3 || m.chroma_mode > 3)
+        if ((m.type > H264R_MB_NONE) | (m.qpy > 51) | (m.slice >= nslices) | (m.i16_mode > 3) | (m.chroma_mode > 3))
             return H264R_ERR_BAD_RECORD;
         if (m.coef != H264R_NONE) {
-            if ((m.coef & 3) || (uint64_t)m.coef + 4 > pic->coef_bytes) return H264R_ERR_BAD_RECORD;
+            if ((m.coef & 3) || (uint64_t)m.coef + 4 > coef_bytes) return H264R_ERR_BAD_RECORD;
+            const uint8_t *c = pic->coef + m.coef;
             uint32_t mask;
-            memcpy(&mask, pic->coef + m.coef, 4);
-            if (mask >> 27) return H264R_ERR_BAD_RECORD;
-            int t8 = (m.flags & H264R_MBF_T8x8) != 0;
-            if (t8 && (mask & 0xFFF0u)) return H264R_ERR_BAD_RECORD;
-            uint64_t nw = __builtin_popcount(mask) + (t8 ? 3 * __builtin_popcount(mask & 15u) : 0);
-            uint64_t voff = (4 + 2 * nw + 3) & ~3ull;
-            if (m.coef + voff > pic->coef_bytes) return H264R_ERR_BAD_RECORD;
-            uint64_t nl = 0;
-            for (uint64_t w = 0; w < nw; w++) {
-                uint16_t s;
-                memcpy(&s, pic->coef + m.coef + 4 + 2 * w, 2);
-                nl += __builtin_popcount(s);
+            memcpy(&mask, c, 4);
+            const int t8 = (m.flags & H264R_MBF_T8x8) != 0;
+            if ((mask >> 27) || (t8 && (mask & 0xFFF0u))) return H264R_ERR_BAD_RECORD;
+            const uint64_t nw = __builtin_popcount(mask) + (t8 ? 3 * __builtin_popcount(mask & 15u) : 0);
+            const uint64_t voff = (4 + 2 * nw + 3) & ~3ull;
+            if (m.coef + voff > coef_bytes) return H264R_ERR_BAD_RECORD;
+            // levels: one per significance bit; whole 64-bit words while they
+            // lie inside the payload buffer, 16-bit words for the rest
+            uint64_t nl = 0, w = 0;
+            const uint64_t room = coef_bytes - m.coef - 4;  // bytes from the first word to the buffer end
+            for (; w + 4 <= nw; w += 4) {
+                uint64_t v;
+                memcpy(&v, c + 4 + 2 * w, 8);
+                nl += __builtin_popcountll(v);
             }
-            if (m.coef + voff + 2 * nl > pic->coef_bytes) return H264R_ERR_BAD_RECORD;
+            if (w < nw && 2 * w + 8 <= room) {
+                uint64_t v;
+                memcpy(&v, c + 4 + 2 * w, 8);
+                nl += __builtin_popcountll(v & (~0ull >> (64 - 16 * (nw - w))));
+            } else {
+                for (; w < nw; w++) {
+                    uint16_t sw;
+                    memcpy(&sw, c + 4 + 2 * w, 2);
+                    nl += __builtin_popcount(sw);
+                }
+            }
+            if (m.coef + voff + 2 * nl > coef_bytes) return H264R_ERR_BAD_RECORD;
             // chroma DC of 4:2:0 has scan positions 0..3 only
             for (int b = 17; b <= 18; b++) {
                 if (!(mask & (1u << b))) continue;
-                uint32_t before = mask & ((1u << b) - 1u);
-                uint64_t w = __builtin_popcount(before) + (t8 ? 3 * __builtin_popcount(before & 15u) : 0);
+                const uint32_t before = mask & ((1u << b) - 1u);
+                const uint64_t wi = __builtin_popcount(before) + (t8 ? 3 * __builtin_popcount(before & 15u) : 0);
                 uint16_t sg;
-                memcpy(&sg, pic->coef + m.coef + 4 + 2 * w, 2);
+                memcpy(&sg, c + 4 + 2 * wi, 2);
                 if (sg & 0xFFF0u) return H264R_ERR_BAD_RECORD;
             }
         }
         if (m.type == H264R_MB_INTER) {
-            if (m.aux == H264R_NONE || (m.aux & 3) || (uint64_t)m.aux + 4 > pic->motion_bytes) return H264R_ERR_BAD_RECORD;
+            if (m.aux == H264R_NONE || (m.aux & 3) || (uint64_t)m.aux + 4 > motion_bytes) return H264R_ERR_BAD_RECORD;
             uint16_t hdr[2];
             memcpy(hdr, pic->motion + m.aux, 4);
-            if (hdr[1] != parts_count(hdr[0]) || (uint64_t)m.aux + 4 + 16ull * hdr[1] > pic->motion_bytes) return H264R_ERR_BAD_RECORD;
+            if (hdr[1] != parts_count(hdr[0]) || (uint64_t)m.aux + 4 + 16ull * hdr[1] > motion_bytes) return H264R_ERR_BAD_RECORD;
+            const bool mb_field = (m.flags & H264R_MBF_FIELD) && pic->mbaff;
             for (int e = 0; e < hdr[1]; e++) {
                 h264r_part p;
                 memcpy(&p, pic->motion + m.aux + 4 + 16 * e, 16);
-                if (p.wt >= pic->num_weights) return H264R_ERR_BAD_RECORD;
+                if (p.wt >= nweights) return H264R_ERR_BAD_RECORD;
                 for (int l = 0; l < 2; l++) {
-                    if (p.ref[l] < 0) continue;
-                    const int slot = H264R_REF_SLOT(p.ref[l]);
-                    const bool fref = (p.ref[l] & H264R_REF_FIELD) != 0, bref = (p.ref[l] & H264R_REF_BOTTOM) != 0;
+                    const int r = p.ref[l];
+                    if (r < 0) continue;
+                    const int slot = H264R_REF_SLOT(r);
+                    const bool fref = (r & H264R_REF_FIELD) != 0, bref = (r & H264R_REF_BOTTOM) != 0;
                     if (slot >= dpb_slots) return H264R_ERR_BAD_RECORD;
                     if (fpic) {
                         // fields only; its own slot only for the opposite
                         // parity (the first field of the frame)
-                        if (!fref) return H264R_ERR_BAD_RECORD;
-                        if (slot == pic->dst_slot && bref == (pic->structure == H264R_STRUCT_BOTTOM)) return H264R_ERR_BAD_RECORD;
-                    } else {
-                        if (slot == pic->dst_slot) return H264R_ERR_BAD_RECORD;
-                        if (fref && !((m.flags & H264R_MBF_FIELD) && pic->mbaff)) return H264R_ERR_BAD_RECORD;
+                        if (!fref || (slot == dst && bref == own_bottom)) return H264R_ERR_BAD_RECORD;
+                    } else if (slot == dst || (fref && !mb_field)) {
+                        return H264R_ERR_BAD_RECORD;
                     }
                 }
             }
         } else if (m.type == H264R_MB_IPCM) {
-            if (m.aux >= pic->num_pcm) return H264R_ERR_BAD_RECORD;
+            if (m.aux >= npcm) return H264R_ERR_BAD_RECORD;
         }
     }
     return H264R_OK;
+}
+
+extern "C" int h264r_validate_picture(const h264r_picture *pic, int dpb_slots)
+{
+    const int r = validate_header(pic, dpb_slots);
+    return r ? r : validate_mbs(pic, dpb_slots, 0, pic->num_mbs);
 }
 
 // ---------------------------------------------------------------- launching
@@ -1400,42 +1435,73 @@ extern "C" int h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *st
     if (rc) return rc;
     rc = ensure(ctx, &b.rec_dev, &b.rec_dev_cap, tot, false);
     if (rc) return rc;
-    // validate and pack the pictures on the host workers
+    // validate and pack the pictures on the host workers: the picture-level
+    // checks here, then every picture in K chunks of MBs and of each record
+    // array, so that all workers stay busy whatever the batch size
     std::vector<h264r_picture> dp(pics, pics + n);
     std::vector<BatchItem> items(n);
-    std::vector<int> prc(n, H264R_OK);
-    ctx->pool->run(n, [&](int i) {
+    for (int i = 0; i < n; i++) {
         const h264r_picture *pic = &pics[i];
-        int r = h264r_validate_picture(pic, streams[i]->cfg.dpb_slots);
+        int r = validate_header(pic, streams[i]->cfg.dpb_slots);
         if (r == H264R_OK && (pic->width_mbs != streams[i]->cfg.width_mbs || pic->height_mbs != streams[i]->cfg.height_mbs))
             r = H264R_ERR_INVALID_ARG;
-        prc[i] = r;
+        if (r) {
+            set_err(ctx, "h264r_submit_batch: picture %d rejected (%d)", i, r);
+            return r;
+        }
+    }
+    const int workers = ctx->pool->size() + 1;
+    int K = 1;
+    while (K < 8 && n * K < 2 * workers) K *= 2;
+    std::vector<int> prc((size_t)n * K, H264R_OK);
+    std::vector<uint8_t> pintra((size_t)n * K, 0);
+    ctx->pool->run(n * K, [&](int t) {
+        const int i = t / K, c = t % K;
+        const h264r_picture *pic = &pics[i];
+        const uint32_t a0 = (uint32_t)((uint64_t)pic->num_mbs * c / K), a1 = (uint32_t)((uint64_t)pic->num_mbs * (c + 1) / K);
+        const int r = validate_mbs(pic, streams[i]->cfg.dpb_slots, a0, a1);
+        prc[t] = r;
         if (r) return;
-        const void *src[6] = {pic->mbs, pic->slices, pic->weights, pic->motion, pic->coef, pic->pcm};
-        uint64_t sz[6] = {sizeof(h264r_mb) * pic->num_mbs, sizeof(h264r_slice) * pic->num_slices,
-                          sizeof(h264r_weight) * pic->num_weights, pic->motion_bytes, pic->coef_bytes, 384ull * pic->num_pcm};
-        for (int k = 0; k < 6; k++)
-            if (sz[k]) memcpy(b.rec_host + offs[i][k], src[k], sz[k]);
-        memcpy(b.rec_host + offs[i][6], pic->scaling4x4, 96);
-        memcpy(b.rec_host + offs[i][6] + 96, pic->scaling8x8, 384);
-        dp[i].mbs = (const h264r_mb *)(b.rec_dev + offs[i][0]);
-        dp[i].slices = (const h264r_slice *)(b.rec_dev + offs[i][1]);
-        dp[i].weights = (const h264r_weight *)(b.rec_dev + offs[i][2]);
-        dp[i].motion = b.rec_dev + offs[i][3];
-        dp[i].coef = b.rec_dev + offs[i][4];
-        dp[i].pcm = b.rec_dev + offs[i][5];
-        items[i].s = streams[i];
-        items[i].pic = &dp[i];
-        items[i].scaling_dev = b.rec_dev + offs[i][6];
-        items[i].has_intra = has_intra_mbs(pic);
+        for (uint32_t a = a0; a < a1; a++) {
+            const int ty = pic->mbs[a].type;
+            if (ty == H264R_MB_I4x4 || ty == H264R_MB_I8x8 || ty == H264R_MB_I16x16) {
+                pintra[t] = 1;
+                break;
+            }
+        }
+        const uint8_t *src[6] = {(const uint8_t *)pic->mbs, (const uint8_t *)pic->slices, (const uint8_t *)pic->weights,
+                                 pic->motion, pic->coef, pic->pcm};
+        const uint64_t sz[6] = {sizeof(h264r_mb) * pic->num_mbs, sizeof(h264r_slice) * pic->num_slices,
+                                sizeof(h264r_weight) * pic->num_weights, pic->motion_bytes, pic->coef_bytes, 384ull * pic->num_pcm};
+        for (int k = 0; k < 6; k++) {
+            const uint64_t b0 = sz[k] * c / K, b1 = sz[k] * (c + 1) / K;
+            if (b1 > b0) memcpy(b.rec_host + offs[i][k] + b0, src[k] + b0, b1 - b0);
+        }
+        if (c == 0) {
+            memcpy(b.rec_host + offs[i][6], pic->scaling4x4, 96);
+            memcpy(b.rec_host + offs[i][6] + 96, pic->scaling8x8, 384);
+            dp[i].mbs = (const h264r_mb *)(b.rec_dev + offs[i][0]);
+            dp[i].slices = (const h264r_slice *)(b.rec_dev + offs[i][1]);
+            dp[i].weights = (const h264r_weight *)(b.rec_dev + offs[i][2]);
+            dp[i].motion = b.rec_dev + offs[i][3];
+            dp[i].coef = b.rec_dev + offs[i][4];
+            dp[i].pcm = b.rec_dev + offs[i][5];
+            items[i].s = streams[i];
+            items[i].pic = &dp[i];
+            items[i].scaling_dev = b.rec_dev + offs[i][6];
+        }
     });
     bool any_intra = false;
-    for (int i = 0; i < n; i++) {
-        if (prc[i]) {
-            set_err(ctx, "h264r_submit_batch: picture %d rejected (%d)", i, prc[i]);
-            return prc[i];
+    for (int t = 0; t < n * K; t++) {
+        if (prc[t]) {
+            set_err(ctx, "h264r_submit_batch: picture %d rejected (%d)", t / K, prc[t]);
+            return prc[t];
         }
-        any_intra = any_intra || items[i].has_intra;
+        any_intra = any_intra || pintra[t];
+    }
+    for (int i = 0; i < n; i++) {
+        items[i].has_intra = false;
+        for (int c = 0; c < K; c++) items[i].has_intra = items[i].has_intra || pintra[(size_t)i * K + c];
     }
     cudaStream_t cs = streams[0]->cs;
     cudaEvent_t ev;

@@ -56,7 +56,8 @@ def test_validator_accepts_reference_records(engine_lib):
 
 
 @pytest.mark.parametrize("mutation", ["qp", "slice", "type", "coef_off", "motion_off", "ref_slot", "self_ref",
-                                      "weight_idx", "mask_bits", "num_mbs", "field_ref_frame_mb"])
+                                      "weight_idx", "mask_bits", "num_mbs", "field_ref_frame_mb", "levels_cut",
+                                      "sig_words_cut"])
 def test_validator_rejects_bad_records(engine_lib, mutation):
     p = _fixture_pic()
     p.mbs = p.mbs.copy()
@@ -91,7 +92,35 @@ def test_validator_rejects_bad_records(engine_lib, mutation):
         p.coef[off + 3] = 0x80
     elif mutation == "num_mbs":
         p.mbs = p.mbs[:-1]
+    elif mutation in ("levels_cut", "sig_words_cut"):
+        # the payload that ends last loses its levels (or most of its
+        # significance words): the counts no longer fit the buffer
+        last = int(np.argmax(np.where(p.mbs["coef"] != R.NONE32, p.mbs["coef"], 0)))
+        off = int(p.mbs[last]["coef"])
+        mask = int(np.frombuffer(p.coef[off:off + 4].tobytes(), "<u4")[0])
+        t8 = bool(p.mbs[last]["flags"] & 4)
+        nw = bin(mask).count("1") + (3 * bin(mask & 15).count("1") if t8 else 0)
+        voff = (4 + 2 * nw + 3) & ~3
+        p.coef = p.coef[:off + voff] if mutation == "levels_cut" else p.coef[:off + 6]
     assert h.validate(p, 16) in (R.ERR_BAD_RECORD, R.ERR_INVALID_ARG)
+
+
+def test_validator_field_pictures(engine_lib):
+    """Field pictures read fields only; their own slot only for the other
+    parity (the first field of the frame)."""
+    g = h.synth("cif_ippp", seed=41, num_pictures=4, paff_percent=100, gop_kind=0)
+    pics = list(g)
+    assert all(h.validate(p, g.dpb_slots) == 0 for p in pics)
+    second = next(p for p in pics if p.structure == 2 and (p.mbs["type"] == 0).any())
+    inter = int(np.nonzero(second.mbs["type"] == 0)[0][0])
+    off = int(second.mbs[inter]["aux"]) + 4
+    for bad in (second.dst_slot | 0x20 | 0x40, 1, second.dst_slot):  # own parity, frame ref, own frame
+        q = R.Picture.from_c(second.to_c())
+        q.motion = q.motion.copy()
+        part = np.frombuffer(q.motion[off:off + 16].tobytes(), R.PART_DTYPE).copy()
+        part["ref"][0, 0] = bad
+        q.motion[off:off + 16] = np.frombuffer(part.tobytes(), np.uint8)
+        assert h.validate(q, g.dpb_slots) == R.ERR_BAD_RECORD, bad
 
 
 def test_synth_is_deterministic(engine_lib):
