@@ -86,6 +86,7 @@ struct LaunchBuf {
     uint64_t rec_dev_cap = 0;
     cudaEvent_t done = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;  // k_bs on the owner's side stream
+    cudaEvent_t uploaded = nullptr;              // host-record upload on the context's upload stream
     bool pending = false;
     GraphEntry graphs[kGraphCache];
     int ngraphs = 0;
@@ -177,6 +178,9 @@ struct h264r_ctx {
     std::vector<std::array<cudaEvent_t, 5>> ev_free, ev_pending;
     std::mutex timing_mu;
     cudaStream_t batch_stream = nullptr;
+    // host-submitted batches upload their records here, so that a batch's
+    // upload overlaps the kernels of the batch before it on the same pipeline
+    cudaStream_t upload_stream = nullptr;
     // launch shapes: the default and the autotuner's choice per geometry mix
     std::mutex tune_mu;
     h264r_tuning tuning{4, 8, 0, 0};
@@ -248,6 +252,7 @@ static void create_events(LaunchBuf &b)
     cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&b.join, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&b.uploaded, cudaEventDisableTiming);
 }
 
 extern "C" int h264r_ctx_create(const h264r_cfg *cfg, h264r_ctx **out)
@@ -268,7 +273,8 @@ extern "C" int h264r_ctx_create(const h264r_cfg *cfg, h264r_ctx **out)
     cudaMemGetInfo(&free_b, &total_b);
     ctx->budget = (cfg && cfg->dpb_budget_bytes) ? cfg->dpb_budget_bytes : (uint64_t)(free_b * 0.9);
     if (cudaMalloc(&ctx->d_error, sizeof(int)) != cudaSuccess || cudaMallocHost(&ctx->h_error, sizeof(int)) != cudaSuccess ||
-        cudaMemset(ctx->d_error, 0, sizeof(int)) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->batch_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaMemset(ctx->d_error, 0, sizeof(int)) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->batch_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->upload_stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete ctx;
         return H264R_ERR_CUDA;
     }
@@ -295,6 +301,7 @@ static void free_buf(LaunchBuf &b)
     if (b.done) cudaEventDestroy(b.done);
     if (b.fork) cudaEventDestroy(b.fork);
     if (b.join) cudaEventDestroy(b.join);
+    if (b.uploaded) cudaEventDestroy(b.uploaded);
     for (int i = 0; i < b.ngraphs; i++)
         if (b.graphs[i].exec) cudaGraphExecDestroy(b.graphs[i].exec);
     b = LaunchBuf();
@@ -305,11 +312,13 @@ extern "C" int h264r_ctx_destroy(h264r_ctx *ctx)
     if (!ctx) return H264R_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->batch_stream);
+    if (ctx->upload_stream) cudaStreamSynchronize(ctx->upload_stream);
     for (auto &b : ctx->batch_ring) free_buf(b);
     for (auto *pool : {&ctx->ev_free, &ctx->ev_pending})
         for (auto &q : *pool)
             for (auto e : q) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->batch_stream);
+    if (ctx->upload_stream) cudaStreamDestroy(ctx->upload_stream);
     cudaFree(ctx->d_error);
     cudaFreeHost(ctx->h_error);
     delete ctx;
@@ -1512,7 +1521,11 @@ extern "C" int h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *st
         cudaStreamWaitEvent(cs, ev, 0);
     }
     rc = H264R_OK;
-    if (cudaMemcpyAsync(b.rec_dev, b.rec_host, tot, cudaMemcpyHostToDevice, cs) != cudaSuccess) {
+    // the upload runs on the upload stream: it overlaps the kernels queued on
+    // cs before this batch; the batch's kernels wait for it (the staging and
+    // device buffers of this ring slot were released by wait_slot)
+    if (cudaMemcpyAsync(b.rec_dev, b.rec_host, tot, cudaMemcpyHostToDevice, ctx->upload_stream) != cudaSuccess ||
+        cudaEventRecord(b.uploaded, ctx->upload_stream) != cudaSuccess || cudaStreamWaitEvent(cs, b.uploaded, 0) != cudaSuccess) {
         set_err(ctx, "h264r_submit_batch: record upload failed");
         rc = H264R_ERR_CUDA;
     }

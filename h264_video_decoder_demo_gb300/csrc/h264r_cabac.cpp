@@ -366,6 +366,16 @@ int cabac_skip_inc(MbDecoder &d)
     return (a >= 0 && !d.P.mbs[a].skip) + (b >= 0 && !d.P.mbs[b].skip);
 }
 
+// mb_field_decoding_flag (9.3.3.1.1.2): the left and upper MB pairs
+// (6.4.10) of the slice that are field pairs
+int cabac_field_inc(MbDecoder &d)
+{
+    const int pair = d.addr >> 1, W = d.W;
+    const int a = pair % W > 0 ? 2 * (pair - 1) : -1, b = pair >= W ? 2 * (pair - W) : -1;
+    const auto fieldpair = [&](int n) { return n >= 0 && d.P.mbs[n].slice == d.sc.index && d.P.mbs[n].field; };
+    return fieldpair(a) + fieldpair(b);
+}
+
 // ---------------------------------------------------------------- motion syntax
 int cabac_sub_mb_type(MbDecoder &d, bool is_b)
 {
@@ -388,14 +398,16 @@ int cabac_sub_mb_type(MbDecoder &d, bool is_b)
 }
 
 // the syntax of the neighbouring partition covering (xN, yN) relative to the
-// current MB: lists its prediction uses, ref_idx and mvd (of list l)
-static bool nb_syntax(const MbDecoder &d, int xN, int yN, int l, int &ref, int mvd[2])
+// current MB: lists its prediction uses, ref_idx and mvd (of list l); *field:
+// the neighbour is a field MB of an MBAFF frame
+static bool nb_syntax(const MbDecoder &d, int xN, int yN, int l, int &ref, int mvd[2], bool *field = nullptr)
 {
     int xW = 0, yW = 0;
     const int n = d.nb_mb(xN, yN, 16, 16, xW, yW);
     ref = 0;
     mvd[0] = mvd[1] = 0;
     if (n < 0) return false;
+    if (field) *field = n == d.addr ? d.fld : (d.mbaff && d.P.mbs[n].field);
     const int bi = (yW >> 2) * 4 + (xW >> 2);
     if (n == d.addr) {
         if (!(d.predl_cur[bi] & (1 << l))) return false;
@@ -412,13 +424,16 @@ static bool nb_syntax(const MbDecoder &d, int xN, int yN, int l, int &ref, int m
     return true;
 }
 
-// ref_idx_lX of the partition at (x, y) (9.3.3.1.1.6, U binarisation)
+// ref_idx_lX of the partition at (x, y) (9.3.3.1.1.6, U binarisation); a
+// field neighbour of a frame MB counts refIdx > 1 (its field index)
 int cabac_ref_idx(MbDecoder &d, int l, int x, int y)
 {
     Cabac &c = *d.cab;
     int ra, rb, mv[2];
-    const int ca = nb_syntax(d, x - 1, y, l, ra, mv) && ra > 0;
-    const int cb = nb_syntax(d, x, y - 1, l, rb, mv) && rb > 0;
+    bool fa = false, fb = false;
+    const bool na = nb_syntax(d, x - 1, y, l, ra, mv, &fa), nb = nb_syntax(d, x, y - 1, l, rb, mv, &fb);
+    const int ca = na && ra > ((!d.fld && fa) ? 1 : 0);
+    const int cb = nb && rb > ((!d.fld && fb) ? 1 : 0);
     if (!c.decision(54 + ca + 2 * cb)) return 0;
     int r = 1;
     int ctx = 58;
@@ -434,9 +449,17 @@ int cabac_mvd(MbDecoder &d, int l, int comp, int x, int y)
 {
     Cabac &c = *d.cab;
     int r, ma[2], mb[2];
-    nb_syntax(d, x - 1, y, l, r, ma);
-    nb_syntax(d, x, y - 1, l, r, mb);
-    const int sum = std::abs(ma[comp]) + std::abs(mb[comp]);
+    bool fa = false, fb = false;
+    nb_syntax(d, x - 1, y, l, r, ma, &fa);
+    nb_syntax(d, x, y - 1, l, r, mb, &fb);
+    // vertical mvd of a neighbour of the other kind (MBAFF frame / field MB)
+    // in the current MB's units
+    auto scaled = [&](int v, bool f) {
+        v = std::abs(v);
+        if (comp == 1 && f != d.fld) v = d.fld ? v / 2 : v * 2;
+        return v;
+    };
+    const int sum = scaled(ma[comp], fa) + scaled(mb[comp], fb);
     const int base = comp ? 47 : 40;
     if (!c.decision(base + (sum < 3 ? 0 : (sum <= 32 ? 1 : 2)))) return 0;
     int v = 1, ctx = 3;

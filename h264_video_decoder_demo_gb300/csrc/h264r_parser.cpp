@@ -55,7 +55,10 @@ void sub_geom(int shape, int sp, int &x, int &y, int &w, int &h)
 int MbDecoder::inter_pred(int mb_type, bool is_b, h264r_mb &r, bool &no_sub_lt8)
 {
     no_sub_lt8 = true;
-    const int nref[2] = {sc.sh.num_ref_idx_active[0], sc.sh.num_ref_idx_active[1]};
+    // a field MB of an MBAFF frame indexes fields: twice the entries, and
+    // ref_idx is present even with one frame in the list (7.3.5.1)
+    const int nref[2] = {ref_limit(0), ref_limit(1)};
+    const bool ref_present[2] = {nref[0] > 1 || fld, nref[1] > 1 || fld};
     parts.clear();
     int shape = 0;
     // read the syntax first (mb_pred / sub_mb_pred, 7.3.5.1 / 7.3.5.2)
@@ -86,9 +89,9 @@ int MbDecoder::inter_pred(int mb_type, bool is_b, h264r_mb &r, bool &no_sub_lt8)
                 if (pred[p] & (1 << l)) {
                     int x0, y0, w4, h4;
                     cover(p, x0, y0, w4, h4);
-                    if (cab) ref[p][l] = nref[l] > 1 ? cabac_ref_idx(*this, l, 4 * x0, 4 * y0) : 0;
-                    else ref[p][l] = nref[l] > 1 ? (int)br.te(nref[l] - 1) : 0;
-                    if (ref[p][l] >= nref[l] || !sc.list[l][ref[p][l]])
+                    if (cab) ref[p][l] = ref_present[l] ? cabac_ref_idx(*this, l, 4 * x0, 4 * y0) : 0;
+                    else ref[p][l] = ref_present[l] ? (int)br.te(nref[l] - 1) : 0;
+                    if (ref[p][l] >= nref[l] || !ref_pic(l, ref[p][l]))
                         return P.fail(H264R_ERR_BAD_RECORD, "ref_idx names no picture (MB %d)", addr);
                     if (cab)
                         for (int j = y0; j < y0 + h4; j++)
@@ -158,9 +161,9 @@ int MbDecoder::inter_pred(int mb_type, bool is_b, h264r_mb &r, bool &no_sub_lt8)
                 ref[q][l] = -1;
                 if (st[q].pred & (1 << l)) {
                     const int qx = (q & 1) * 8, qy = (q >> 1) * 8;
-                    if (cab) ref[q][l] = (!ref0 && nref[l] > 1) ? cabac_ref_idx(*this, l, qx, qy) : 0;
-                    else ref[q][l] = (!ref0 && nref[l] > 1) ? (int)br.te(nref[l] - 1) : 0;
-                    if (ref[q][l] >= nref[l] || !sc.list[l][ref[q][l]])
+                    if (cab) ref[q][l] = (!ref0 && ref_present[l]) ? cabac_ref_idx(*this, l, qx, qy) : 0;
+                    else ref[q][l] = (!ref0 && ref_present[l]) ? (int)br.te(nref[l] - 1) : 0;
+                    if (ref[q][l] >= nref[l] || !ref_pic(l, ref[q][l]))
                         return P.fail(H264R_ERR_BAD_RECORD, "ref_idx names no picture (MB %d)", addr);
                     if (cab)
                         for (int j = qy / 4; j < qy / 4 + 2; j++)
@@ -247,8 +250,9 @@ void MbDecoder::emit_motion(int shape, const std::vector<PartRec> &parts, h264r_
             p.ref[l] = -1;
             p.dref[l] = b.ref[l];  // refIdx for now: the picture-level list resolves it at the end
             if (b.ref[l] >= 0) {
-                const Pic *rp = sc.list[l][b.ref[l]];
+                const Pic *rp = ref_pic(l, b.ref[l]);
                 p.ref[l] = (int8_t)rp->slot;
+                if (fld) p.ref[l] = (int8_t)(rp->slot | H264R_REF_FIELD | (ref_bottom(b.ref[l]) ? H264R_REF_BOTTOM : 0));
             }
         }
         p.wt = weight_index(b.ref[0], b.ref[1]);
@@ -267,7 +271,7 @@ void MbDecoder::store_motion()
             cur->ref[l][i] = (int8_t)r;
             cur->mv[l][i][0] = blk[i].mv[l][0];
             cur->mv[l][i][1] = blk[i].mv[l][1];
-            cur->refpic[l][i] = uid[l][r + 1];
+            cur->refpic[l][i] = uid[l][(fld && r >= 0 ? r >> 1 : r) + 1];
         }
 }
 
@@ -598,6 +602,7 @@ int decode_skip(MbDecoder &d, h264r_mb &r)
 // (CH264SliceData::slice_data, H264SliceData.cpp:64-534)
 int h264r_parser::decode_slice_cabac(SliceCtx &sc, BitReader &br)
 {
+    if (cur_mbaff) return decode_slice_mbaff(sc, br, true);
     const int num_mbs = (int)mbs.size();
     MbDecoder d(*this, sc, br);
     Cabac cab;
@@ -635,10 +640,170 @@ int h264r_parser::decode_slice_cabac(SliceCtx &sc, BitReader &br)
     return H264R_OK;
 }
 
+// slice_data( ) (7.3.4) of an MBAFF frame, CAVLC or CABAC: MB pairs, each
+// with its mb_field_decoding_flag, in the order and with the inference the
+// reference decoder uses (CH264SliceData::slice_data,
+// H264SliceData.cpp:163-521):
+//   - the flag is read before the first coded MB of a pair (the top MB, or
+//     the bottom one when the top is skipped); a skipped top MB takes the
+//     bottom's flag, so it is decoded once that is known: in CAVLC the flag
+//     follows a skip run that ends on a top MB, in CABAC the bottom's
+//     mb_skip_flag (and then the flag) is decoded right after the top's;
+//   - a pair with both MBs skipped infers the flag from the left pair of the
+//     slice, else the pair above, else frame;
+//   - CABAC: the contexts of a top MB's mb_skip_flag see the flag of the
+//     pair decoded last (the pair above for the first pair of a row), the
+//     inference of 7.4.4 as the reference applies it.
+int h264r_parser::decode_slice_mbaff(SliceCtx &sc, BitReader &br, bool cabac)
+{
+    const int num_mbs = (int)mbs.size(), W = width_mbs;
+    MbDecoder d(*this, sc, br);
+    d.mbaff = true;
+    Cabac cab;
+    if (cabac) {
+        cab.br = &br;
+        d.cab = &cab;
+        while (!br.byte_aligned()) br.u(1);
+        cab.init_contexts(sc.sh.slice_type, sc.sh.cabac_init_idc, sc.pps->pic_init_qp + sc.sh.slice_qp_delta);
+        cab.init_engine();
+    }
+    int addr = 2 * sc.sh.first_mb;
+    if (addr >= num_mbs) return fail(H264R_ERR_BAD_RECORD, "first_mb_in_slice %d out of range", sc.sh.first_mb);
+    const bool skips = sc.sh.slice_type != kSliceI;
+    bool field = false;             // mb_field_decoding_flag as the slice decodes it
+    bool prev_skipped = false;      // prevMbSkipped
+    bool flag_read = false;         // the current pair's flag was read ahead
+    int bottom_skip = 0;            // CABAC: the bottom MB's mb_skip_flag, decoded ahead
+    // 7.4.4 inference for a pair whose MBs are both skipped
+    auto infer = [&](int a) {
+        const int pair = a >> 1;
+        if (pair % W > 0 && mbs[a - 2].slice == sc.index) return mbs[a - 2].field;
+        if (pair >= W && mbs[a - 2 * W].slice == sc.index) return mbs[a - 2 * W].field;
+        return false;
+    };
+    auto enter = [&](int a) -> int {
+        if (a >= num_mbs) return fail(H264R_ERR_BAD_RECORD, "slice data past the picture end");
+        if (mbs[a].slice >= 0) return fail(H264R_ERR_BAD_RECORD, "MB %d decoded twice", a);
+        mbs[a].slice = sc.index;
+        mbs[a].skip = false;
+        mbs[a].field = field;
+        d.set_mb(a);
+        return 0;
+    };
+    auto skip_mb = [&](int a) -> int {
+        mbs[a].field = field;
+        d.set_mb(a);
+        if (decode_skip(d, rec[a])) return failed ? H264R_ERR_BAD_RECORD : fail(H264R_ERR_BAD_RECORD, "skip MB %d", a);
+        if (field) rec[a].flags |= H264R_MBF_FIELD;
+        d.prev_qp_nz = false;
+        return 0;
+    };
+    auto coded_mb = [&](int a) -> int {
+        mbs[a].field = field;
+        d.set_mb(a);
+        if (cabac ? d.decode_cabac() : d.decode()) return H264R_ERR_BAD_RECORD;
+        if (field) rec[a].flags |= H264R_MBF_FIELD;
+        return 0;
+    };
+    bool more = true;
+    while (more) {
+        bool skipped = false;
+        if (skips && !cabac) {
+            const uint32_t run = br.ue();
+            if (br.err) return fail(H264R_ERR_BAD_RECORD, "truncated mb_skip_run");
+            prev_skipped = run > 0;
+            for (uint32_t i = 0; i < run; i++) {
+                if (int rc = enter(addr)) return rc;
+                if ((addr & 1) == 0) {
+                    if (i == run - 1) {
+                        // the bottom MB is coded: its flag follows the run
+                        field = br.u(1) != 0;
+                        flag_read = true;
+                    } else {
+                        field = infer(addr);
+                    }
+                }
+                if (int rc = skip_mb(addr)) return rc;
+                addr++;
+            }
+            if (run > 0) more = br.more_rbsp_data();
+            if (!more) break;
+        } else if (skips) {
+            if (int rc = enter(addr)) return rc;
+            if ((addr & 1) == 0) {
+                const int pair = addr >> 1;
+                // the flag the contexts of this pair's mb_skip_flag see
+                if (pair % W == 0 && pair >= W) field = mbs[addr - 2 * W].slice == sc.index ? mbs[addr - 2 * W].field : false;
+                mbs[addr].field = field;
+                d.set_mb(addr);
+            }
+            int sk;
+            if ((addr & 1) && prev_skipped) {
+                sk = bottom_skip;
+            } else {
+                sk = cab.decision((sc.sh.slice_type == kSliceB ? 24 : 11) + cabac_skip_inc(d));
+            }
+            if (sk) {
+                skipped = true;
+                if ((addr & 1) == 0) {
+                    // the bottom MB's mb_skip_flag, and its flag if it is coded,
+                    // decide the pair's kind before the top MB is decoded
+                    mbs[addr].skip = true;
+                    if (addr + 1 >= num_mbs) return fail(H264R_ERR_BAD_RECORD, "MBAFF pair past the picture end");
+                    mbs[addr + 1].slice = sc.index;
+                    mbs[addr + 1].skip = false;
+                    mbs[addr + 1].field = field;
+                    d.set_mb(addr + 1);
+                    bottom_skip = cab.decision((sc.sh.slice_type == kSliceB ? 24 : 11) + cabac_skip_inc(d));
+                    mbs[addr + 1].slice = -1;  // entered again in its turn
+                    if (!bottom_skip) {
+                        field = cab.decision(70 + cabac_field_inc(d)) != 0;
+                        flag_read = true;
+                    } else {
+                        field = infer(addr);
+                    }
+                }
+                if (int rc = skip_mb(addr)) return rc;
+            }
+            prev_skipped = sk != 0;
+        } else if (!cabac) {
+            // I slice, CAVLC
+        }
+        if (!skipped) {
+            if (!skips || !cabac) {
+                if (int rc = enter(addr)) return rc;
+            }
+            if ((addr & 1) == 0 || prev_skipped) {
+                if (!flag_read) {
+                    if (cabac) {
+                        d.set_mb(addr);
+                        field = cab.decision(70 + cabac_field_inc(d)) != 0;
+                    } else {
+                        field = br.u(1) != 0;
+                    }
+                }
+                flag_read = false;
+            }
+            if (int rc = coded_mb(addr)) return rc;
+            if (!cabac) prev_skipped = false;
+        }
+        if (br.err) return fail(H264R_ERR_BAD_RECORD, "truncated slice data (MB %d)", addr);
+        if (cabac) {
+            if ((addr & 1) == 0) more = true;
+            else more = !cab.terminate();
+        } else {
+            more = br.more_rbsp_data();
+        }
+        addr++;
+    }
+    return H264R_OK;
+}
+
 // slice_data( ) (7.3.4), CAVLC
 int h264r_parser::decode_slice(SliceCtx &sc, BitReader &br)
 {
     if (sc.pps->cabac) return decode_slice_cabac(sc, br);
+    if (cur_mbaff) return decode_slice_mbaff(sc, br, false);
     const int num_mbs = (int)mbs.size();
     MbDecoder d(*this, sc, br);
     int addr = sc.sh.first_mb;
@@ -942,7 +1107,7 @@ int h264r_parser::start_picture(const SliceHeader &sh, const Sps &s, const Pps &
     } else if (s.width_mbs != width_mbs || s.frame_height_mbs() != height_mbs) {
         return fail(H264R_ERR_UNSUPPORTED, "picture size change within the stream");
     }
-    if (!s.frame_mbs_only && s.mbaff) return fail(H264R_ERR_UNSUPPORTED, "MBAFF frames");
+    cur_mbaff = sh.mbaff != 0;
     cur = Pic();
     cur.uid = next_uid++;
     // FrameNum of the picture as a reference: the reference decoder assigns
@@ -964,7 +1129,10 @@ int h264r_parser::start_picture(const SliceHeader &sh, const Sps &s, const Pps &
     // same slice (slice >= 0) first, so only that mark is reset per picture
     if ((int)mbs.size() != n) mbs.assign(n, MbState());
     else
-        for (MbState &m : mbs) m.slice = -1;
+        for (MbState &m : mbs) {
+            m.slice = -1;
+            m.field = false;
+        }
     h264r_mb none;
     memset(&none, 0, sizeof(none));
     none.type = H264R_MB_NONE;
@@ -1021,6 +1189,7 @@ int h264r_parser::finish_picture(bool last)
         motion_pool.push_back(mo);
     }
     mo->intra.resize(n);
+    mo->field.assign(n, 0);
     mo->mv.resize((size_t)n * 2 * 16 * 2);
     mo->ref.resize((size_t)n * 2 * 16);
     mo->refpic.resize((size_t)n * 2 * 16);
@@ -1033,6 +1202,7 @@ int h264r_parser::finish_picture(bool last)
         const MbState &m = mbs[a];
         const bool inter = m.slice >= 0 && m.cls == H264R_MB_INTER;
         mo->intra[a] = inter ? 0 : (m.slice >= 0 && m.cls == H264R_MB_IPCM ? 2 : 1);
+        mo->field[a] = cur_mbaff && m.field ? 1 : 0;
         int16_t *mv = &mo->mv[(size_t)a * 64];
         int8_t *ref = &mo->ref[(size_t)a * 32];
         int32_t *rp = &mo->refpic[(size_t)a * 32];
@@ -1075,7 +1245,7 @@ int h264r_parser::finish_picture(bool last)
     d.pic.width_mbs = (uint16_t)width_mbs;
     d.pic.height_mbs = (uint16_t)height_mbs;
     d.pic.structure = H264R_STRUCT_FRAME;
-    d.pic.mbaff = 0;
+    d.pic.mbaff = cur_mbaff ? 1 : 0;
     d.pic.dst_slot = (uint8_t)cur.slot;
     d.pic.deblock = last ? 0 : 1;
     const Pps &q = pps[sh.pps_id];

@@ -42,6 +42,7 @@ inline int median3(int a, int b, int c) { return std::max(std::min(a, b), std::m
 // data for direct prediction, 8.4.1.2.1).
 struct Motion {
     std::vector<uint8_t> intra;   // per MB: 1 intra or undecoded, 2 I_PCM
+    std::vector<uint8_t> field;   // per MB: field MB of an MBAFF frame
     std::vector<int16_t> mv;      // [mb][list][4x4 raster][2]
     std::vector<int8_t> ref;      // [mb][list][4x4 raster], -1: list unused
     std::vector<int32_t> refpic;  // [mb][list][4x4 raster]: uid of the reference picture
@@ -62,6 +63,7 @@ struct MbState {
     int slice = -1;  // slice number, -1 while not decoded
     uint8_t cls = 0; // H264R_MB_*
     bool skip = false;
+    bool field = false;  // MBAFF: mb_field_decoding_flag of the MB's pair
     uint8_t tc[16];        // TotalCoeff per luma4x4BlkIdx
     uint8_t tcc[2][4];     // chroma AC TotalCoeff
     int8_t ipm4[16];       // Intra4x4PredMode per luma4x4BlkIdx
@@ -166,6 +168,7 @@ struct h264r_parser {
     int max_long_term_frame_idx = kNoLongTerm;
     // current picture
     bool in_pic = false;
+    bool cur_mbaff = false;  // MbaffFrameFlag of the current picture
     SliceHeader first_sh;  // first slice of the current picture
     Pic cur;
     int frame_num_offset = 0;
@@ -229,6 +232,7 @@ struct h264r_parser {
     int finish_picture(bool last);
     int decode_slice(SliceCtx &sc, BitReader &br);
     int decode_slice_cabac(SliceCtx &sc, BitReader &br);
+    int decode_slice_mbaff(SliceCtx &sc, BitReader &br, bool cabac);
     int build_lists(SliceCtx &sc);
     void compute_poc(const SliceHeader &sh, const Sps &s);
     int mark_references(const SliceHeader &sh, const Sps &s);
@@ -248,8 +252,13 @@ struct MbDecoder {
     const Sps &sps;
     const Pps &pps;
     int W, addr = 0, qp = 0;
-    int mbx = 0;  // addr % W, set with addr
+    int mbx = 0;  // MB (pair, in MBAFF frames) column of addr, set with addr
     MbState *cur = nullptr;
+    // MBAFF frames: MBs come in pairs (addr 2p top, 2p + 1 bottom) and a
+    // pair is two frame MBs or two field MBs (mb_field_decoding_flag)
+    bool mbaff = false;
+    bool fld = false;   // the current MB is a field MB of an MBAFF frame
+    bool bot = false;   // the current MB is the bottom MB of its pair
     bool decoded4x4[16];  // motion of this 4x4 block already derived
     Blk blk[16];          // motion of the current MB (raster)
     // per-MB scratch, reused across the slice's MBs
@@ -269,10 +278,110 @@ struct MbDecoder {
                 uid[l][i] = (i > 0 && i - 1 < (int)s.list[l].size() && s.list[l][i - 1]) ? s.list[l][i - 1]->uid : -1;
     }
 
+    // the current MB: address, column, state; fld from the MB's state
+    void set_mb(int a)
+    {
+        addr = a;
+        mbx = mbaff ? (a >> 1) % W : a % W;
+        cur = &P.mbs[a];
+        bot = mbaff && (a & 1);
+        fld = mbaff && cur->field;
+    }
+
+    // reference indices of the current MB: a field MB of an MBAFF frame
+    // indexes the fields of the list's frames (8.4.2.1): refIdx >> 1 is the
+    // frame, an even refIdx its field of the MB's parity, an odd one the other
+    int ref_limit(int l) const { return fld ? 2 * sc.sh.num_ref_idx_active[l] : sc.sh.num_ref_idx_active[l]; }
+    const Pic *ref_pic(int l, int ref) const
+    {
+        const int i = fld ? ref >> 1 : ref;
+        return i >= 0 && i < (int)sc.list[l].size() ? sc.list[l][i] : nullptr;
+    }
+    bool ref_bottom(int ref) const { return (ref & 1) ? !bot : bot; }
+    // PicOrderCnt of what refIdx names, and of the current picture or field
+    int ref_poc(int l, int ref) const
+    {
+        const Pic *p = ref_pic(l, ref);
+        return !fld ? p->poc : (ref_bottom(ref) ? p->bottom_poc : p->top_poc);
+    }
+    int cur_poc() const { return !fld ? P.cur.poc : (bot ? P.cur.bottom_poc : P.cur.top_poc); }
+
+    // decoded MB of this slice (or the current MB itself)
+    bool usable(int n) const { return n >= 0 && (n == addr || P.mbs[n].slice == sc.index); }
+
+    // 6.4.12.2 (Table 6-4): the MB of an MBAFF frame holding luma or chroma
+    // location (xN, yN) relative to the current MB, or -1; (xW, yW) inside it
+    int nb_mb_mbaff(int xN, int yN, int maxW, int maxH, int &xW, int &yW) const
+    {
+        const int pair = addr >> 1, px = pair % W;
+        auto pr = [&](int q, bool ok) { return ok && q >= 0 && usable(2 * q) ? 2 * q : -1; };
+        const int A = pr(pair - 1, px > 0), B = pr(pair - W, true), C = pr(pair - W + 1, px + 1 < W),
+                  D = pr(pair - W - 1, px > 0);
+        auto frm = [&](int n) { return !P.mbs[n].field; };
+        const bool frame = !fld, top = !bot;
+        int n = -1, yM = 0;
+        if (xN < 0 && yN < 0) {
+            if (frame) {
+                if (top) { if (D >= 0) { n = D + 1; yM = yN; } }
+                else if (A >= 0) {
+                    if (frm(A)) { n = A; yM = yN; } else { n = A + 1; yM = (yN + maxH) >> 1; }
+                }
+            } else {
+                if (top) {
+                    if (D >= 0) { if (frm(D)) { n = D + 1; yM = 2 * yN; } else { n = D; yM = yN; } }
+                } else if (D >= 0) { n = D + 1; yM = yN; }
+            }
+        } else if (xN < 0 && yN < maxH) {
+            if (A >= 0) {
+                if (frame) {
+                    if (top) {
+                        if (frm(A)) { n = A; yM = yN; } else { n = (yN % 2 == 0) ? A : A + 1; yM = yN >> 1; }
+                    } else {
+                        if (frm(A)) { n = A + 1; yM = yN; } else { n = (yN % 2 == 0) ? A : A + 1; yM = (yN + maxH) >> 1; }
+                    }
+                } else {
+                    if (top) {
+                        if (frm(A)) {
+                            if (yN < maxH / 2) { n = A; yM = yN << 1; } else { n = A + 1; yM = (yN << 1) - maxH; }
+                        } else { n = A; yM = yN; }
+                    } else {
+                        if (frm(A)) {
+                            if (yN < maxH / 2) { n = A; yM = (yN << 1) + 1; } else { n = A + 1; yM = (yN << 1) + 1 - maxH; }
+                        } else { n = A + 1; yM = yN; }
+                    }
+                }
+            }
+        } else if (xN < maxW && yN < 0) {
+            if (frame) {
+                if (top) { if (B >= 0) { n = B + 1; yM = yN; } }
+                else { n = addr - 1; yM = yN; }
+            } else {
+                if (top) {
+                    if (B >= 0) { if (frm(B)) { n = B + 1; yM = 2 * yN; } else { n = B; yM = yN; } }
+                } else if (B >= 0) { n = B + 1; yM = yN; }
+            }
+        } else if (xN < maxW && yN < maxH) {
+            n = addr; yM = yN;
+        } else if (xN >= maxW && yN < 0) {
+            if (frame) {
+                if (top) { if (C >= 0) { n = C + 1; yM = yN; } }
+            } else {
+                if (top) {
+                    if (C >= 0) { if (frm(C)) { n = C + 1; yM = 2 * yN; } else { n = C; yM = yN; } }
+                } else if (C >= 0) { n = C + 1; yM = yN; }
+            }
+        }
+        if (n < 0) return -1;
+        xW = (xN + maxW) & (maxW - 1);
+        yW = (yM + maxH) & (maxH - 1);
+        return n;
+    }
+
     // ---- neighbours (6.4.12.1): the MB holding luma location (xN, yN)
     // relative to the current MB, or -1; (xW, yW) inside it
     int nb_mb(int xN, int yN, int maxW, int maxH, int &xW, int &yW) const
     {
+        if (mbaff) return nb_mb_mbaff(xN, yN, maxW, maxH, xW, yW);
         int n;
         const int x = mbx;
         if (xN < 0 && yN < 0) n = x > 0 ? addr - W - 1 : -1;
@@ -400,6 +509,15 @@ struct MbDecoder {
         if (r.ref >= 0) {
             r.mv[0] = m.mv[list][bi][0];
             r.mv[1] = m.mv[list][bi][1];
+            // 8.4.1.3.2: a neighbour of the other kind (frame / field MB of
+            // an MBAFF frame) in the current MB's units; '/' truncates
+            if (fld && !m.field) {
+                r.mv[1] = r.mv[1] / 2;
+                r.ref *= 2;
+            } else if (!fld && m.field && mbaff) {
+                r.mv[1] *= 2;
+                r.ref /= 2;
+            }
         }
         return r;
     }
@@ -451,7 +569,25 @@ struct MbDecoder {
         const Pic *col = sc.list[1].empty() ? nullptr : sc.list[1][0];
         if (!col || !col->motion) return c;
         const Motion &m = *col->motion;
-        if (m.intra[addr] == 2 && sc.sh.direct_spatial) {
+        int mb = addr;
+        if (mbaff && !m.field.empty()) {
+            // Table 8-8 for an MBAFF frame and an MBAFF co-located frame
+            // (H264InterPrediction.cpp:1173-1215): the co-located pair's kind
+            // picks the MB and the row yM of the co-located block
+            const int xCol = (bi & 3) * 4, yCol = (bi >> 2) * 4;
+            int yM = yCol;
+            const bool col_field = m.field[addr] != 0;
+            if (!fld && col_field) {
+                const int top = std::abs(col->top_poc - P.cur.poc), bottom = std::abs(col->bottom_poc - P.cur.poc);
+                mb = 2 * (addr / 2) + (top < bottom ? 0 : 1);
+                yM = 8 * (addr % 2) + 4 * (yCol / 8);
+            } else if (fld && !col_field) {
+                mb = 2 * (addr / 2) + yCol / 8;
+                yM = (2 * yCol) % 16;
+            }
+            bi = (yM >> 2) * 4 + (xCol >> 2);
+        }
+        if (m.intra[mb] == 2 && sc.sh.direct_spatial) {
             // an I_PCM co-located MB: the reference's intra test does not
             // cover I_PCM (prediction mode Intra_NA), so it reads the MB's
             // cleared motion as list 1, refIdxCol 0 and mvCol (0, 0)
@@ -459,10 +595,10 @@ struct MbDecoder {
             c.ref = 0;
             return c;
         }
-        if (m.intra[addr]) return c;
+        if (m.intra[mb]) return c;
         int l = 0;
-        if (m.ref[(addr * 2 + 0) * 16 + bi] < 0) l = 1;
-        const size_t o = (size_t)(addr * 2 + l) * 16 + bi;
+        if (m.ref[(mb * 2 + 0) * 16 + bi] < 0) l = 1;
+        const size_t o = (size_t)(mb * 2 + l) * 16 + bi;
         c.ref = m.ref[o];
         c.mv[0] = m.mv[o * 2];
         c.mv[1] = m.mv[o * 2 + 1];
@@ -559,42 +695,46 @@ struct MbDecoder {
         if ((st == kSliceP || st == kSliceSP) && pps.weighted_pred && pf0) {
             weighted = true;
             const PredWeights &pw = sc.sh.pw;
+            const int i0 = fld ? ref0 >> 1 : ref0;  // refIdxL0WP
             w.log_wd[0] = (int8_t)pw.luma_log2;
             w.log_wd[1] = w.log_wd[2] = (int8_t)pw.chroma_log2;
-            w.w0[0] = (int16_t)pw.lw[0][ref0];
-            w.o0[0] = (int16_t)pw.lo[0][ref0];
+            w.w0[0] = (int16_t)pw.lw[0][i0];
+            w.o0[0] = (int16_t)pw.lo[0][i0];
             for (int c = 0; c < 2; c++) {
-                w.w0[1 + c] = (int16_t)pw.cw[0][ref0][c];
-                w.o0[1 + c] = (int16_t)pw.co[0][ref0][c];
+                w.w0[1 + c] = (int16_t)pw.cw[0][i0][c];
+                w.o0[1 + c] = (int16_t)pw.co[0][i0][c];
             }
         } else if (st == kSliceB && pps.weighted_bipred_idc == 1 && (pf0 || pf1)) {
             weighted = true;
             const PredWeights &pw = sc.sh.pw;
             w.log_wd[0] = (int8_t)pw.luma_log2;
             w.log_wd[1] = w.log_wd[2] = (int8_t)pw.chroma_log2;
+            const int i0 = fld ? ref0 >> 1 : ref0, i1 = fld ? ref1 >> 1 : ref1;  // refIdxLXWP
             if (pf0) {
-                w.w0[0] = (int16_t)pw.lw[0][ref0];
-                w.o0[0] = (int16_t)pw.lo[0][ref0];
+                w.w0[0] = (int16_t)pw.lw[0][i0];
+                w.o0[0] = (int16_t)pw.lo[0][i0];
                 for (int c = 0; c < 2; c++) {
-                    w.w0[1 + c] = (int16_t)pw.cw[0][ref0][c];
-                    w.o0[1 + c] = (int16_t)pw.co[0][ref0][c];
+                    w.w0[1 + c] = (int16_t)pw.cw[0][i0][c];
+                    w.o0[1 + c] = (int16_t)pw.co[0][i0][c];
                 }
             }
             if (pf1) {
-                w.w1[0] = (int16_t)pw.lw[1][ref1];
-                w.o1[0] = (int16_t)pw.lo[1][ref1];
+                w.w1[0] = (int16_t)pw.lw[1][i1];
+                w.o1[0] = (int16_t)pw.lo[1][i1];
                 for (int c = 0; c < 2; c++) {
-                    w.w1[1 + c] = (int16_t)pw.cw[1][ref1][c];
-                    w.o1[1 + c] = (int16_t)pw.co[1][ref1][c];
+                    w.w1[1 + c] = (int16_t)pw.cw[1][i1][c];
+                    w.o1[1 + c] = (int16_t)pw.co[1][i1][c];
                 }
             }
         } else if (st == kSliceB && pps.weighted_bipred_idc == 2 && pf0 && pf1) {
             weighted = true;
-            const Pic *p0 = sc.list[0][ref0], *p1 = sc.list[1][ref1];
+            // field MBs of MBAFF frames: the POCs of the fields (8.4.2.3.1)
+            const Pic *p0 = ref_pic(0, ref0), *p1 = ref_pic(1, ref1);
             int w0 = 32, w1 = 32;
-            const int td = clip3(-128, 127, p1->poc - p0->poc);
+            const int poc0 = ref_poc(0, ref0), poc1 = ref_poc(1, ref1);
+            const int td = clip3(-128, 127, poc1 - poc0);
             if (td != 0 && !p0->long_ref && !p1->long_ref) {
-                const int tb = clip3(-128, 127, P.cur.poc - p0->poc);
+                const int tb = clip3(-128, 127, cur_poc() - poc0);
                 const int tx = (16384 + std::abs(td / 2)) / td;
                 const int dsf = clip3(-1024, 1023, (tb * tx + 32) >> 6);
                 if (!((dsf >> 2) < -64 || (dsf >> 2) > 128)) {
@@ -637,6 +777,8 @@ struct MbDecoder {
 int decode_skip(MbDecoder &d, h264r_mb &r);
 // ctxIdxInc of mb_skip_flag (9.3.3.1.1.1)
 int cabac_skip_inc(MbDecoder &d);
+// ctxIdxInc of mb_field_decoding_flag (9.3.3.1.1.2): field pairs left / above
+int cabac_field_inc(MbDecoder &d);
 
 }  // namespace pimpl
 }  // namespace h264r
