@@ -42,6 +42,11 @@ const uint8_t kTransLPS[64] = {0,  0,  1,  2,  2,  4,  4,  5,  6,  7,  8,  9,  9
 const uint8_t kSig8x8Frame[63] = {0,  1,  2,  3,  4,  5,  5,  4,  4,  3,  3,  4,  4,  4,  5,  5,  4,  4,  4,  4,  3,
                                   3,  6,  7,  7,  7,  8,  9,  10, 9,  8,  7,  7,  6,  11, 12, 13, 11, 6,  7,  8,  9,
                                   14, 10, 9,  8,  6,  11, 12, 13, 11, 6,  9,  14, 10, 9,  11, 12, 13, 11, 14, 10, 12};
+// ... and of significant_coeff_flag of field coded 8x8 blocks (field MBs of
+// MBAFF frames), by levelListIdx
+const uint8_t kSig8x8Field[63] = {0,  1,  1,  2,  2,  3,  3,  4,  5,  6,  7,  7,  7,  8,  4,  5,  6,  9,  10, 10, 8,
+                                  11, 12, 11, 9,  9,  10, 10, 8,  11, 12, 11, 9,  9,  10, 10, 8,  11, 12, 11, 9,  9,
+                                  10, 10, 8,  13, 13, 9,  9,  10, 10, 8,  13, 13, 9,  9,  10, 10, 14, 14, 14, 14, 14};
 const uint8_t kLast8x8[63] = {0, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2,
                               3, 3, 3, 3, 3, 3, 3, 3, 4, 4, 4, 4, 4, 4, 4, 4, 5, 5, 5, 5, 6, 6, 6, 6, 7, 7, 7, 7, 8, 8, 8};
 
@@ -296,22 +301,25 @@ int cbf_inc(MbDecoder &d, int cat, int blk, int comp)
 
 // residual_block_cabac( ) (7.3.5.3.3, 9.3.3.1.3) of a block of ctxBlockCat
 // cat (0..4, or 5 for 8x8 luma) with max coefficients, the coded_block_flag
-// context increment already derived (ignored for cat 5).  The levels go to
-// lev[] in ascending scan position and their positions to *sig (16-bit
-// word) or *sig64 (8x8).  Returns the number of non-zero levels.
-int block(Cabac &c, int cat, int cbf_ctx_inc, int max, int16_t *lev, uint16_t *sig, uint64_t *sig64)
+// context increment already derived (ignored for cat 5).  Field coded
+// blocks (field MBs of MBAFF frames) take the field significance contexts
+// (Table 9-34: 277 / 338, 436 / 451).  The levels go to lev[] in ascending
+// scan position and their positions to *sig (16-bit word) or *sig64 (8x8).
+// Returns the number of non-zero levels.
+int block(Cabac &c, int cat, int cbf_ctx_inc, int max, int16_t *lev, uint16_t *sig, uint64_t *sig64, bool field)
 {
     if (sig) *sig = 0;
     if (sig64) *sig64 = 0;
     if (cat != 5 && !c.decision(85 + kCbfCatOff[cat] + cbf_ctx_inc)) return 0;
-    const int sig_base = cat == 5 ? 402 : 105 + kSigCatOff[cat];
-    const int last_base = cat == 5 ? 417 : 166 + kSigCatOff[cat];
+    const int sig_base = cat == 5 ? (field ? 436 : 402) : (field ? 277 : 105) + kSigCatOff[cat];
+    const int last_base = cat == 5 ? (field ? 451 : 417) : (field ? 338 : 166) + kSigCatOff[cat];
+    const uint8_t *sig8 = field ? kSig8x8Field : kSig8x8Frame;
     const int abs_base = cat == 5 ? 426 : 227 + kAbsCatOff[cat];
     int pos[64];
     int n = 0;
     int num = max;
     for (int i = 0; i < num - 1; i++) {
-        const int si = cat == 5 ? kSig8x8Frame[i] : (cat == 3 ? std::min(i, 2) : i);
+        const int si = cat == 5 ? sig8[i] : (cat == 3 ? std::min(i, 2) : i);
         if (c.decision(sig_base + si)) {
             pos[n++] = i;
             const int li = cat == 5 ? kLast8x8[i] : (cat == 3 ? std::min(i, 2) : i);
@@ -636,7 +644,7 @@ int MbDecoder::decode_cabac()
         int16_t dc_lev[16];
         int dc_n = 0;
         if (i16) {
-            dc_n = block(c, 0, cbf_inc(*this, 0, 0, 0), 16, dc_lev, &dc_sig, nullptr);
+            dc_n = block(c, 0, cbf_inc(*this, 0, 0, 0), 16, dc_lev, &dc_sig, nullptr, fld);
             if (dc_n) cur->cbf_dc |= 1;
             cur->tc[0] = (uint8_t)dc_n;  // as the reference keeps the DC count in block 0
             if (dc_n) r.nz4x4 = 1;
@@ -645,7 +653,7 @@ int MbDecoder::decode_cabac()
             if (!(cbp_luma & (1 << b8))) continue;
             if (t8) {
                 uint64_t s64 = 0;
-                const int n = block(c, 5, 0, 64, lev, nullptr, &s64);
+                const int n = block(c, 5, 0, 64, lev, nullptr, &s64, fld);
                 cur->cbf_ac[0] |= (uint16_t)(1u << b8);  // inferred coded_block_flag of an 8x8 block
                 if (n) {
                     r.nz8x8 |= (uint8_t)(1u << b8);
@@ -659,10 +667,10 @@ int MbDecoder::decode_cabac()
                 const int b = b8 * 4 + b4;
                 int n;
                 if (i16) {
-                    n = block(c, 1, cbf_inc(*this, 1, b, 0), 15, lev, &s16, nullptr);
+                    n = block(c, 1, cbf_inc(*this, 1, b, 0), 15, lev, &s16, nullptr, fld);
                     s16 = (uint16_t)(s16 << 1);  // AC list position k is scan position k + 1
                 } else {
-                    n = block(c, 2, cbf_inc(*this, 2, b, 0), 16, lev, &s16, nullptr);
+                    n = block(c, 2, cbf_inc(*this, 2, b, 0), 16, lev, &s16, nullptr, fld);
                 }
                 if (n) cur->cbf_ac[0] |= (uint16_t)(1u << b);
                 cur->tc[b] = (uint8_t)n;
@@ -674,7 +682,7 @@ int MbDecoder::decode_cabac()
         if (dc_n) put(dc_sig, dc_lev, dc_n, 16);
         if (cbp_chroma & 3) {
             for (int cc = 0; cc < 2; cc++) {
-                const int n = block(c, 3, cbf_inc(*this, 3, 0, 1 + cc), 4, lev, &s16, nullptr);
+                const int n = block(c, 3, cbf_inc(*this, 3, 0, 1 + cc), 4, lev, &s16, nullptr, fld);
                 if (n) cur->cbf_dc |= (uint8_t)(2 << cc);
                 put(s16, lev, n, 17 + cc);
             }
@@ -682,7 +690,7 @@ int MbDecoder::decode_cabac()
         if (cbp_chroma & 2) {
             for (int cc = 0; cc < 2; cc++)
                 for (int b = 0; b < 4; b++) {
-                    int n = block(c, 4, cbf_inc(*this, 4, b, 1 + cc), 15, lev, &s16, nullptr);
+                    int n = block(c, 4, cbf_inc(*this, 4, b, 1 + cc), 15, lev, &s16, nullptr, fld);
                     s16 = (uint16_t)(s16 << 1);
                     if (n) cur->cbf_ac[1 + cc] |= (uint16_t)(1u << b);
                     cur->tcc[cc][b] = (uint8_t)n;

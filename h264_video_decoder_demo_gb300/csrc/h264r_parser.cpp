@@ -765,9 +765,6 @@ int h264r_parser::decode_slice_mbaff(SliceCtx &sc, BitReader &br, bool cabac)
                 }
                 if (int rc = skip_mb(addr)) return rc;
             }
-            prev_skipped = sk != 0;
-        } else if (!cabac) {
-            // I slice, CAVLC
         }
         if (!skipped) {
             if (!skips || !cabac) {
@@ -785,8 +782,9 @@ int h264r_parser::decode_slice_mbaff(SliceCtx &sc, BitReader &br, bool cabac)
                 flag_read = false;
             }
             if (int rc = coded_mb(addr)) return rc;
-            if (!cabac) prev_skipped = false;
         }
+        // prevMbSkipped: in CABAC the MB just decoded; in CAVLC the last run
+        if (cabac && skips) prev_skipped = skipped;
         if (br.err) return fail(H264R_ERR_BAD_RECORD, "truncated slice data (MB %d)", addr);
         if (cabac) {
             if ((addr & 1) == 0) more = true;

@@ -16,11 +16,13 @@
  * the engine reconstructs, with the DPB slot it writes and the slots that
  * are due for output after it.
  *
- * Scope: progressive (frame) pictures, 4:2:0, 8 bits, CAVLC or CABAC, one
- * slice group, I / P / B slices.  MBAFF and field pictures, SP/SI slices,
- * slice groups and other chroma formats return H264R_ERR_UNSUPPORTED.
+ * Scope: frame pictures, progressive or MBAFF (frame / field MB pairs),
+ * 4:2:0, 8 bits, CAVLC or CABAC, one slice group, I / P / B slices.  Field
+ * pictures (PAFF), SP/SI slices, slice groups and other chroma formats return
+ * H264R_ERR_UNSUPPORTED.
  *
- * Host only; not thread-safe per parser object.
+ * Host only.  A parser object is used by one thread at a time; parsers share
+ * no state, so several streams parse in parallel on their own threads.
  */
 #ifndef H264R_PARSER_H
 #define H264R_PARSER_H

@@ -14,7 +14,7 @@ the first pictures of each stream, in decoding order from the IDR:
                     depth of the SPS) and the POCs in the order its output
                     callback receives them
 
-  <name>.h264       for the two CAVLC and two frame-coded CABAC streams: the stream cut before the first
+  <name>.h264       for the two CAVLC, the two frame-coded CABAC and the MBAFF CABAC streams: the stream cut before the first
                     slice of picture N (parameter sets included), and each
                     stream whole, with
   <name>.frames.json  every picture the reference outputs for that cut stream,
@@ -105,6 +105,7 @@ BITSTREAMS = [
     ("heavyhand_cavlc_b4_6pics", "HeavyHand_1080p.B_frames_4.no_cabac.no_tff.h264", 6),
     ("heavyhand_cabac_p_6pics", "HeavyHand_1080p.no_B_frames.cabac.no_tff.h264", 6),
     ("heavyhand_cabac_ibp_6pics", "HeavyHand_1080p.B_frames.cabac.h264", 6),
+    ("heavyhand_cabac_mbaff_6pics", "HeavyHand_1080p.B_frames_cabac_tff.h264", 6),
     # the two CAVLC streams whole (50 and 76 pictures)
     ("gop121_cavlc_whole", "gop121.naluCnt453.h264", 1 << 20),
     ("heavyhand_cavlc_b4_whole", "HeavyHand_1080p.B_frames_4.no_cabac.no_tff.h264", 1 << 20),

@@ -13,7 +13,8 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 
-BITSTREAMS = ["gop121_cavlc_4pics", "heavyhand_cavlc_b4_6pics", "heavyhand_cabac_p_6pics", "heavyhand_cabac_ibp_6pics"]
+BITSTREAMS = ["gop121_cavlc_4pics", "heavyhand_cavlc_b4_6pics", "heavyhand_cabac_p_6pics", "heavyhand_cabac_ibp_6pics",
+              "heavyhand_cabac_mbaff_6pics"]
 
 
 def _golden(name):

@@ -5,8 +5,9 @@ run the reference built from its own sources (oracle/_ref, `make -C oracle
 ref`); they are skipped where the reference sources are absent.
   - the CAVLC code tables (Tables 9-4, 9-5, 9-7 - 9-10) decode every 16-bit
     window exactly as the reference's own table decoders do;
-  - every record of every picture of the two CAVLC bundled streams equals the
-    reference's (ref_dump at its pre-deblocking hook);
+  - every record of every picture of the two CAVLC bundled streams, and of
+    the first 40 pictures of the three CABAC ones (two frame coded, one
+    MBAFF), equals the reference's (ref_dump at its pre-deblocking hook);
   - decoding order, POC and output order equal the reference's
     (tests/golden/output_order.json);
   - damaged input returns error codes and never crashes.
@@ -32,8 +33,9 @@ PROBE = os.path.join(ORACLE, "_ref", "libref_probe.so")
 DUMPER = os.path.join(ORACLE, "_ref", "ref_dump")
 
 CAVLC_STREAMS = ["gop121.naluCnt453.h264", "HeavyHand_1080p.B_frames_4.no_cabac.no_tff.h264"]
-# the frame-coded CABAC streams (the MBAFF one needs MBAFF slice data)
-CABAC_STREAMS = ["HeavyHand_1080p.no_B_frames.cabac.no_tff.h264", "HeavyHand_1080p.B_frames.cabac.h264"]
+# the CABAC streams: frame coded, and MBAFF (frame / field MB pairs)
+CABAC_STREAMS = ["HeavyHand_1080p.no_B_frames.cabac.no_tff.h264", "HeavyHand_1080p.B_frames.cabac.h264",
+                 "HeavyHand_1080p.B_frames_cabac_tff.h264"]
 
 # The reference's first picture of gop121 ends in a damaged slice: MB 7713
 # fails to parse in both decoders, and the reference's partial non-zero
@@ -199,7 +201,8 @@ def test_unsupported_tools_are_reported(lib):
 
 # ---- committed cut streams (tests/golden/*.h264): no reference needed
 
-BITSTREAMS = ["gop121_cavlc_4pics", "heavyhand_cavlc_b4_6pics", "heavyhand_cabac_p_6pics", "heavyhand_cabac_ibp_6pics"]
+BITSTREAMS = ["gop121_cavlc_4pics", "heavyhand_cavlc_b4_6pics", "heavyhand_cabac_p_6pics", "heavyhand_cabac_ibp_6pics",
+              "heavyhand_cabac_mbaff_6pics"]
 
 
 def _golden_stream(name):
