@@ -130,17 +130,20 @@ struct Writer {
         b.ue((uint32_t)max_refs);
         b.u(1, 0);  // gaps_in_frame_num_value_allowed_flag
         b.ue((uint32_t)(cfg.width_mbs - 1));
-        b.ue((uint32_t)(cfg.height_mbs - 1));
-        b.u(1, 1);  // frame_mbs_only_flag
+        // pic_height_in_map_units: MB pair rows when frame_mbs_only_flag is 0
+        b.ue((uint32_t)((cfg.mbaff ? cfg.height_mbs / 2 : cfg.height_mbs) - 1));
+        b.u(1, cfg.mbaff ? 0 : 1);  // frame_mbs_only_flag
+        if (cfg.mbaff) b.u(1, 1);   // mb_adaptive_frame_field_flag
         b.u(1, 1);  // direct_8x8_inference_flag
-        // a coded height of 1088 for 1080 lines: crop 8 lines (4 in 4:2:0 crop units)
+        // a coded height of 1088 for 1080 lines: crop 8 lines (crop units of
+        // 2 lines in 4:2:0, 4 when frame_mbs_only_flag is 0)
         const bool crop = cfg.height_mbs == 68;
         b.u(1, crop ? 1 : 0);
         if (crop) {
             b.ue(0);
             b.ue(0);
             b.ue(0);
-            b.ue(4);
+            b.ue(cfg.mbaff ? 2 : 4);
         }
         b.u(1, 1);  // vui_parameters_present_flag: bitstream restriction only
         for (int i = 0; i < 8; i++) b.u(1, 0);  // aspect, overscan, signal type, chroma loc, timing, nal/vcl hrd, pic_struct
@@ -162,7 +165,7 @@ struct Writer {
         b.ue(0);    // pic_parameter_set_id
         b.ue(0);    // seq_parameter_set_id
         b.u(1, 0);  // entropy_coding_mode_flag: CAVLC
-        b.u(1, 0);  // bottom_field_pic_order_in_frame_present_flag
+        b.u(1, cfg.mbaff ? 1 : 0);  // bottom_field_pic_order_in_frame_present_flag
         b.ue(0);    // num_slice_groups_minus1
         b.ue((uint32_t)(cfg.num_refs - 1));
         b.ue(0);
@@ -248,12 +251,14 @@ struct Writer {
 
     void write_slice_header(BitWriter &b, const SliceParams &s)
     {
-        b.ue((uint32_t)s.first_mb);
+        b.ue((uint32_t)(cfg.mbaff ? s.first_mb / 2 : s.first_mb));
         b.ue((uint32_t)(s.type == kI ? 2 : s.type == kB ? 1 : 0));
         b.ue(0);  // pic_parameter_set_id
         b.u(log2_max_frame_num, (uint32_t)s.frame_num);
+        if (cfg.mbaff) b.u(1, 0);  // field_pic_flag: a frame (MBAFF)
         if (s.idr) b.ue((uint32_t)(idr_count & 0xFFFF));
         b.u(log2_max_poc_lsb, (uint32_t)s.poc_lsb);
+        if (cfg.mbaff) b.se(1);  // delta_pic_order_cnt_bottom: the fields' POCs differ
         if (s.type == kB) b.u(1, cfg.direct_spatial ? 1 : 0);
         if (s.type != kI) {
             b.u(1, 1);  // num_ref_idx_active_override_flag
@@ -486,9 +491,11 @@ struct Writer {
     }
 
     // target motion vector of a partition at (px, py) (picture luma samples)
+    int pic_h_ = 0;       // height of the picture the current MB predicts from
+    bool field_mb_ = false;  // the current MB is a field MB of an MBAFF frame
     void draw_mv(int px, int py, int w, int h, int mv[2])
     {
-        const int W = cfg.width_mbs * 16, H = cfg.height_mbs * 16;
+        const int W = cfg.width_mbs * 16, H = pic_h_;
         if (rng.pct(cfg.edge_mv_percent)) {
             // the reference block lies wholly or partly past one picture edge
             int rx = px + rng.range(-cfg.mv_range, cfg.mv_range) / 4, ry = py + rng.range(-cfg.mv_range, cfg.mv_range) / 4;
@@ -500,10 +507,15 @@ struct Writer {
             }
             mv[0] = std::max(-8192, std::min(8191, (rx - px) * 4 + rng.range(0, 3)));
             mv[1] = std::max(-8192, std::min(8191, (ry - py) * 4 + rng.range(0, 3)));
-            return;
+        } else {
+            mv[0] = rng.range(-cfg.mv_range, cfg.mv_range);
+            mv[1] = rng.range(-cfg.mv_range, cfg.mv_range);
         }
-        mv[0] = rng.range(-cfg.mv_range, cfg.mv_range);
-        mv[1] = rng.range(-cfg.mv_range, cfg.mv_range);
+        // a field MB reads its reference field with x clamped to the doubled
+        // field-view width (Q3): past the right edge of the last lines the
+        // reference decoder reads beyond its chroma plane, so field MBs keep
+        // their prediction (6-tap and chroma support included) left of the edge
+        if (field_mb_) mv[0] = std::min(mv[0], 4 * (W - 8 - (px + w)));
     }
 
     // derive the partitions' mvd in decoding order, as MbDecoder::inter_pred does
@@ -538,17 +550,34 @@ struct Writer {
     // before it tests it for zero (H264InterPrediction.cpp:2955-2960)
     bool same_picture(const MbDecoder &d, int ref0, int ref1) const
     {
-        return ref0 >= 0 && ref1 >= 0 && d.sc.list[0][ref0] && d.sc.list[1][ref1] &&
-               d.sc.list[0][ref0]->poc == d.sc.list[1][ref1]->poc;
+        return ref0 >= 0 && ref1 >= 0 && d.ref_pic(0, ref0) && d.ref_pic(1, ref1) &&
+               d.ref_poc(0, ref0) == d.ref_poc(1, ref1);
+    }
+
+    // a 4x4 block of a field MB of an MBAFF frame at (bx, by) (4-sample
+    // units) predicts from left of the right picture edge in luma and chroma
+    // (interpolation support included): past it the reference decoder's
+    // doubled-width clamp (Q3) reads beyond its chroma plane on the last lines
+    bool field_block_ok(const MbDecoder &d, int bx, const Blk &b) const
+    {
+        if (!d.fld) return true;
+        const int W = cfg.width_mbs * 16, px = ((d.addr >> 1) % cfg.width_mbs) * 16 + 4 * bx;
+        for (int l = 0; l < 2; l++)
+            if (b.ref[l] >= 0) {
+                const int mvx = b.mv[l][0];
+                if (px + 3 + (mvx >> 2) + 3 > W - 2 || px / 2 + 1 + (mvx >> 3) + 1 > W / 2 - 2) return false;
+            }
+        return true;
     }
 
     // direct blocks the reference decodes as the standard does: explicit
     // weighting never meets a list-1-only block (the reference reads its
     // weights out of range, H264InterPrediction.cpp:2756-2771), implicit
-    // weighting never a bi-predicted block from one picture twice
+    // weighting never a bi-predicted block from one picture twice, a field MB
+    // never reads right of the picture edge
     bool direct_ok(MbDecoder &d, int quadrant_mask)
     {
-        if (cfg.weighted == 0 || (cfg.weighted == 1 && !cfg.direct_spatial)) return true;
+        if (!d.fld && (cfg.weighted == 0 || (cfg.weighted == 1 && !cfg.direct_spatial))) return true;
         for (int q = 0; q < 4; q++) {
             if (!(quadrant_mask & (1 << q))) continue;
             for (int s = 0; s < 4; s++) {
@@ -557,9 +586,27 @@ struct Writer {
                 if (d.direct_block(x >> 2, y >> 2, b)) die("direct prediction failed: %s", P.err.c_str());
                 if (cfg.weighted == 1 && b.ref[0] < 0) return false;
                 if (cfg.weighted == 2 && same_picture(d, b.ref[0], b.ref[1])) return false;
+                if (!field_block_ok(d, x >> 2, b)) return false;
             }
         }
         return true;
+    }
+
+    // P_Skip of a field MB predicts from left of the right picture edge
+    bool p_skip_ok(MbDecoder &d)
+    {
+        if (!d.fld) return true;
+        const MbDecoder::Nb A = d.nb_motion(-1, 0, 0), B = d.nb_motion(0, -1, 0);
+        Blk b;
+        b.ref[0] = 0;
+        b.ref[1] = -1;
+        b.mv[0][0] = b.mv[0][1] = b.mv[1][0] = b.mv[1][1] = 0;
+        if (!(!A.avail || !B.avail || (A.ref == 0 && A.mv[0] == 0 && A.mv[1] == 0) || (B.ref == 0 && B.mv[0] == 0 && B.mv[1] == 0))) {
+            int m[2];
+            d.mvp(0, 0, 16, 0, 0, 0, 0, m);
+            b.mv[0][0] = (int16_t)m[0];
+        }
+        return field_block_ok(d, 3, b);
     }
 
     // reference indices of a partition predicted from lists `pred`
@@ -589,7 +636,18 @@ struct Writer {
     {
         MbState *cur = d.cur;
         cur->cls = H264R_MB_INTER;
-        const int px = (d.addr % cfg.width_mbs) * 16, py = (d.addr / cfg.width_mbs) * 16;
+        // the MB's origin in the picture it predicts from (a field MB: its field)
+        int px, py;
+        if (!d.mbaff) {
+            px = (d.addr % cfg.width_mbs) * 16;
+            py = (d.addr / cfg.width_mbs) * 16;
+        } else {
+            const int pair = d.addr >> 1;
+            px = (pair % cfg.width_mbs) * 16;
+            py = d.fld ? (pair / cfg.width_mbs) * 16 : (pair / cfg.width_mbs) * 32 + (d.addr & 1) * 16;
+        }
+        pic_h_ = d.fld ? cfg.height_mbs * 8 : cfg.height_mbs * 16;
+        field_mb_ = d.fld;
         const bool is_b = st == kB;
         const bool explicit_b = is_b && cfg.weighted == 1;
         std::vector<Part> parts;
@@ -767,10 +825,12 @@ struct Writer {
         }
         if (pp.type != kI && s.nref[0] < 1) die("no reference picture for a %s picture", pp.type == kB ? "B" : "P");
         if (cfg.weighted == 1 && pp.type != kI) draw_weights(s);
-        const int nslices = std::max(1, std::min((int)cfg.slices, nmbs));
+        // slices of whole MB pairs in MBAFF frames
+        const int unit = cfg.mbaff ? 2 : 1, nunits = nmbs / unit;
+        const int nslices = std::max(1, std::min((int)cfg.slices, nunits));
         for (int si = 0; si < nslices; si++) {
-            s.first_mb = (int)((int64_t)nmbs * si / nslices);
-            const int end_mb = (int)((int64_t)nmbs * (si + 1) / nslices);
+            s.first_mb = unit * (int)((int64_t)nunits * si / nslices);
+            const int end_mb = unit * (int)((int64_t)nunits * (si + 1) / nslices);
             s.qp = rng.range(cfg.qp_min, cfg.qp_max);
             s.dbk_alpha = rng.range(-cfg.filter_offset_max, cfg.filter_offset_max);
             s.dbk_beta = rng.range(-cfg.filter_offset_max, cfg.filter_offset_max);
@@ -805,38 +865,67 @@ struct Writer {
         if (rb != 1) die("front end rejected a slice header: %s", P.err.c_str());
         if (hbr.pos != b.nbits) die("slice header length differs (%zu read, %zu written)", hbr.pos, b.nbits);
         MbDecoder d(P, sc, mbr);
+        d.mbaff = cfg.mbaff != 0;
         int skip_run = 0;
         const int W = cfg.width_mbs;
+        bool pair_field = false, top_skipped = false;
+        // the field flag a decoder infers for a pair with both MBs skipped
+        auto inferred = [&](int a) {
+            const int pair = a >> 1;
+            if (pair % W > 0 && P.mbs[a - 2].slice == sc.index) return P.mbs[a - 2].field;
+            if (pair >= W && P.mbs[a - 2 * W].slice == sc.index) return P.mbs[a - 2 * W].field;
+            return false;
+        };
+        bool want_skip[2] = {false, false};
         for (int addr = s.first_mb; addr < end_mb; addr++) {
-            d.addr = addr;
-            d.mbx = addr % W;
-            d.cur = &P.mbs[addr];
-            d.cur->slice = sc.index;
-            d.cur->skip = false;
+            const bool top = d.mbaff && (addr & 1) == 0;
+            if (!d.mbaff) {
+                want_skip[0] = s.type != kI && rng.pct(cfg.skip_percent);
+            } else if (top) {
+                // the pair's kind, and which of its MBs to skip: a pair with
+                // both MBs skipped has the kind a decoder infers (the top MB
+                // is decoded before the bottom one is known)
+                pair_field = rng.pct(cfg.field_percent);
+                want_skip[0] = s.type != kI && rng.pct(cfg.skip_percent);
+                want_skip[1] = s.type != kI && rng.pct(cfg.skip_percent);
+                if (want_skip[0] && want_skip[1]) pair_field = inferred(addr);
+            }
+            P.mbs[addr].slice = sc.index;
+            P.mbs[addr].skip = false;
+            P.mbs[addr].field = pair_field;
+            d.set_mb(addr);
             bool skip = false;
-            if (s.type != kI && rng.pct(cfg.skip_percent)) {
+            if (want_skip[d.mbaff ? (addr & 1) : 0]) {
                 reset_mb_motion(d);
-                skip = s.type == kP || direct_ok(d, 15);
+                skip = s.type == kP ? p_skip_ok(d) : direct_ok(d, 15);
             }
             if (skip) {
                 skip_run++;
                 if (decode_skip(d, P.rec[addr])) die("front end: skipped MB %d: %s", addr, P.err.c_str());
+                if (d.fld) P.rec[addr].flags |= H264R_MBF_FIELD;
+                if (top) top_skipped = true;
                 continue;
             }
             if (s.type != kI) {
                 b.ue((uint32_t)skip_run);
                 skip_run = 0;
             }
+            // mb_field_decoding_flag before the first coded MB of a pair
+            if (d.mbaff && (top || top_skipped)) b.u(1, pair_field ? 1 : 0);
+            if (top) top_skipped = false;
             const size_t start = b.nbits;
             const bool intra = s.type == kI || rng.pct(cfg.intra_percent);
             planned_.clear();
+            const int nref[2] = {d.ref_limit(0), d.ref_limit(1)};
             if (intra) write_intra(b, d, s.type);
-            else write_inter(b, d, s.type, s.nref);
+            else write_inter(b, d, s.type, nref);
             // read the MB back: the front end's state now holds it
             mbr.reset(b.buf.data(), b.buf.size());
             mbr.pos = start;
             d.cur->skip = false;
             if (d.decode()) die("front end rejected MB %d: %s", addr, P.err.c_str());
+            if (d.fld) P.rec[addr].flags |= H264R_MBF_FIELD;
+            top_skipped = false;
             if (mbr.pos != b.nbits) die("MB %d: %zu bits read back, %zu written", addr, mbr.pos - start, b.nbits - start);
             for (const Part &p : planned_) {
                 if (p.pred == 0) continue;
@@ -864,6 +953,7 @@ struct Writer {
         if (cfg.weighted > 2 || cfg.min_partition > 3 || cfg.filter_offset_max > 6 || cfg.chroma_qp_offset_max > 12)
             die("configuration field out of range");
         if (cfg.mv_range > 2048) die("mv_range above 2048 quarter samples");
+        if (cfg.mbaff && (!high || (cfg.height_mbs & 1))) die("MBAFF needs High profile and an even height");
         max_refs = cfg.num_refs;
         chroma_offset[0] = rng.range(-cfg.chroma_qp_offset_max, cfg.chroma_qp_offset_max);
         chroma_offset[1] = high ? rng.range(-cfg.chroma_qp_offset_max, cfg.chroma_qp_offset_max) : chroma_offset[0];

@@ -778,6 +778,15 @@ STREAMS = {
                        num_refs=4, transform8x8=1, weighted=1, direct_spatial=1, min_partition=3, intra_percent=5,
                        skip_percent=10, edge_mv_percent=5, qp_min=22, qp_max=40, filter_offset_max=6,
                        coef_density=40, slices=1, pcm_permille=2, chroma_qp_offset_max=3, mv_range=256),
+    # interlaced 1080i as MBAFF frames (the MBAFF half of the interlaced
+    # configuration): 1920x1088, 20 pictures, GOP 12 with one B picture
+    # between anchors, half the MB pairs field pairs, 2 references, no weighted
+    # prediction, MVs +-128 qpel, CAVLC
+    "1080i_mbaff": dict(width_mbs=120, height_mbs=68, num_pictures=20, profile_idc=100, gop_length=12, b_pictures=1,
+                        num_refs=2, transform8x8=1, weighted=0, direct_spatial=1, min_partition=3, intra_percent=5,
+                        skip_percent=10, edge_mv_percent=5, qp_min=22, qp_max=40, filter_offset_max=6,
+                        coef_density=40, slices=1, pcm_permille=2, chroma_qp_offset_max=3, mv_range=128, mbaff=1,
+                        field_percent=50),
 }
 
 

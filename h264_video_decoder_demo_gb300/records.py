@@ -205,7 +205,8 @@ class CWriterCfg(ctypes.Structure):
                 ("skip_percent", ctypes.c_uint8), ("edge_mv_percent", ctypes.c_uint8), ("qp_min", ctypes.c_uint8),
                 ("qp_max", ctypes.c_uint8), ("filter_offset_max", ctypes.c_uint8), ("coef_density", ctypes.c_uint8),
                 ("slices", ctypes.c_uint8), ("pcm_permille", ctypes.c_uint8),
-                ("chroma_qp_offset_max", ctypes.c_uint8), ("reserved", ctypes.c_uint8 * 3),
+                ("chroma_qp_offset_max", ctypes.c_uint8), ("mbaff", ctypes.c_uint8), ("field_percent", ctypes.c_uint8),
+                ("reserved", ctypes.c_uint8),
                 ("mv_range", ctypes.c_uint16), ("reserved2", ctypes.c_uint16)]
 
 

@@ -8,7 +8,8 @@
  * SPS / PPS / slice headers (7.3.2.1, 7.3.2.2, 7.3.3, pred_weight_table
  * 7.3.3.2), CAVLC slice data with skip runs, I_PCM, Intra 4x4 / 8x8 / 16x16,
  * P and B partitions down to 4x4, direct prediction, explicit or implicit
- * weighted prediction and 8x8 transforms (7.3.4, 7.3.5, 9.2).
+ * weighted prediction and 8x8 transforms (7.3.4, 7.3.5, 9.2), progressive
+ * or MBAFF frames (frame / field MB pairs, mb_field_decoding_flag).
  *
  * The writer chooses syntax elements, not samples: target motion vectors,
  * intra prediction modes, reference indices, coded block patterns, QP and
@@ -20,6 +21,10 @@
  * available; explicit bi-predictive weights keep every pairwise sum within
  * the range 8.4.2.3 allows; explicit weighting never meets a list-1-only
  * partition (the writer avoids it, also for direct blocks).
+ *
+ * MBAFF: a pair whose two MBs are skipped takes the field flag the decoder
+ * infers (left pair, else the pair above, else frame); field MBs index the
+ * fields of the reference frames (twice the entries).
  *
  * Deterministic for a given configuration on every host (own generator, no
  * floating point).  Host only.
@@ -70,7 +75,11 @@ typedef struct h264r_writer_cfg {
     uint8_t  pcm_permille;      /* I_PCM MBs per thousand intra MBs            */
     uint8_t  chroma_qp_offset_max; /* chroma_qp_index_offset (and the second one,
                                    High) uniform in [-max, max]                */
-    uint8_t  reserved[3];
+    uint8_t  mbaff;             /* 1: MBAFF frames (High): MB pairs coded as
+                                   two frame MBs or two field MBs; height_mbs
+                                   even; bottom field POC one above the top   */
+    uint8_t  field_percent;     /* MBAFF: MB pairs coded as field MBs          */
+    uint8_t  reserved;
     uint16_t mv_range;          /* MV components uniform in [-mv_range, mv_range]
                                    quarter samples                            */
     uint16_t reserved2;

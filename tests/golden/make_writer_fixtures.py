@@ -5,7 +5,7 @@ Each case is a configuration of the library's bitstream writer
 benchmark configurations and variants that reach the constructs no bundled
 stream has (explicit bi-predictive weights, motion vectors past the picture
 edges, P sub-partitions down to 4x4, I_PCM, non-IDR I pictures, several
-slices, implicit weights with three B pictures).  For every case the script
+slices, implicit weights with three B pictures, CAVLC MBAFF frames).  For every case the script
 writes the stream, decodes it with the unmodified reference decoder
 (oracle/_ref/ref_dump, built from the reference's own sources by
 `make -C oracle ref`) and records:
@@ -49,6 +49,14 @@ CASES = [
     ("1080p_implicit_b3", "1080p_high", 5, dict(num_pictures=16, weighted=2, b_pictures=3)),
     # no weighted prediction, one B picture, two references
     ("1080p_default_wp_b1", "1080p_high", 6, dict(num_pictures=16, weighted=0, b_pictures=1, num_refs=2)),
+    # MBAFF frames (the MBAFF half of the interlaced configuration): half the
+    # MB pairs field pairs, IBP, two references
+    ("1080i_mbaff", "1080i_mbaff", 7, dict(num_pictures=12)),
+    # MBAFF with explicit bi-predictive weights and four references
+    ("1080i_mbaff_explicit", "1080p_high", 8, dict(num_pictures=8, mbaff=1, field_percent=60)),
+    # CIF MBAFF, High, two slices, I_PCM
+    ("cif_mbaff_2slices_pcm", "cif_ippp", 9, dict(profile_idc=100, mbaff=1, field_percent=50, num_pictures=10,
+                                                  slices=2, pcm_permille=50)),
 ]
 
 
