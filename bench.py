@@ -963,19 +963,26 @@ def run_engine(args, world, rank, local, dist):
         torch.cuda.synchronize()
         ctx.sync()
         host_s[0] = host_s[1] = 0.0
+        hs0 = ctx.host_stats()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             e2e_step()
         drain()
         ctx.sync()
         e2e_dt = time.perf_counter() - t0
+        hs1 = ctx.host_stats()
         e2e = {"value": round(frames_per_step * e2e_steps / e2e_dt, 2), "unit": "frames/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": frames_per_step * FRAME_BYTES,
                "ms_per_step": round(1000.0 * e2e_dt / e2e_steps, 3),
                # wall time the calling thread spent inside the calls (waits for a
                # free launch slot included)
                "submit_ms_per_step": round(1000.0 * host_s[0] / e2e_steps, 3),
-               "copy_out_calls_ms_per_step": round(1000.0 * host_s[1] / e2e_steps, 3)}
+               "copy_out_calls_ms_per_step": round(1000.0 * host_s[1] / e2e_steps, 3),
+               # inside the submit calls: waiting for a free launch slot, validating
+               # and packing the records on the host threads, upload and launch
+               "submit_split_ms_per_step": {k: round(1000.0 * (hs1[i] - hs0[i]) / e2e_steps, 3)
+                                            for i, k in enumerate(("wait_slot", "validate_pack", "upload_launch"))},
+               "pack_threads": int(hs1[3])}
         extra = {"plain_fps": round(plain_fps, 2), "cpu_baseline": cpu, "e2e": e2e, "bit_exact_sample": exact,
                  "bit_exact_vs_reference": ref_exact}
         if args.serve_seconds > 0:

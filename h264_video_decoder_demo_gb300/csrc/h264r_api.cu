@@ -13,8 +13,8 @@
 #include <cstdio>
 #include <cstring>
 #include <functional>
-#include <memory>
 #include <chrono>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <thread>
@@ -167,6 +167,9 @@ private:
 struct h264r_ctx {
     int device = 0;
     std::unique_ptr<WorkerPool> pool;
+    // host time of h264r_submit_batch calls (seconds): waiting for a free
+    // launch slot, validating and packing on the workers, upload and launch
+    double host_s[3] = {0, 0, 0};
     uint64_t budget = 0, used = 0;
     uint32_t max_batch = 64;
     int *d_error = nullptr;
@@ -384,6 +387,15 @@ extern "C" int h264r_ctx_last_timing(h264r_ctx *ctx, float t[3], int *launches)
     return H264R_OK;
 }
 
+extern "C" int h264r_ctx_host_stats(h264r_ctx *ctx, double s[4])
+{
+    if (!ctx || !s) return H264R_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    for (int k = 0; k < 3; k++) s[k] = ctx->host_s[k];
+    s[3] = ctx->pool ? ctx->pool->size() + 1 : 1;
+    return H264R_OK;
+}
+
 extern "C" int h264r_ctx_kernel_timing(h264r_ctx *ctx, float t[4], int *launches)
 {
     if (!ctx || !t) return H264R_ERR_INVALID_ARG;
@@ -488,17 +500,27 @@ extern "C" int h264r_slot_device_ptr(h264r_stream *s, int slot, void **dev_y)
 }
 
 // ---------------------------------------------------------------- validator
-static int parts_count(uint32_t shape)
-{
-    int mp = shape & 3;
-    if (mp == 0) return 1;
-    if (mp != 3) return 2;
-    int n = 0;
-    for (int q = 0; q < 4; q++) {
-        int sc = (shape >> (2 + 2 * q)) & 3;
-        n += (sc == 0) ? 1 : (sc == 3 ? 4 : 2);
+// partitions of a motion payload shape: 1, 2, or per 8x8 quadrant 1 / 2 / 2 / 4
+// (a table over the four 2-bit sub-shapes)
+struct PartsTable {
+    uint8_t n[256];
+    PartsTable()
+    {
+        for (int v = 0; v < 256; v++) {
+            n[v] = 0;
+            for (int q = 0; q < 4; q++) {
+                const int sc = (v >> (2 * q)) & 3;
+                n[v] = (uint8_t)(n[v] + (sc == 0 ? 1 : (sc == 3 ? 4 : 2)));
+            }
+        }
     }
-    return n;
+};
+static const PartsTable kPartsTable;
+
+static inline int parts_count(uint32_t shape)
+{
+    const int mp = shape & 3;
+    return mp == 0 ? 1 : (mp != 3 ? 2 : kPartsTable.n[(shape >> 2) & 255]);
 }
 
 // MBs of a picture: a field picture (PAFF) holds half the frame's MB rows
@@ -592,25 +614,27 @@ static int validate_mbs(const h264r_picture *pic, int dpb_slots, uint32_t a0, ui
             memcpy(hdr, pic->motion + m.aux, 4);
             if (hdr[1] != parts_count(hdr[0]) || (uint64_t)m.aux + 4 + 16ull * hdr[1] > motion_bytes) return H264R_ERR_BAD_RECORD;
             const bool mb_field = (m.flags & H264R_MBF_FIELD) && pic->mbaff;
-            for (int e = 0; e < hdr[1]; e++) {
-                h264r_part p;
-                memcpy(&p, pic->motion + m.aux + 4 + 16 * e, 16);
-                if (p.wt >= nweights) return H264R_ERR_BAD_RECORD;
+            // per reference byte r (>= 0): the slot exists; a field picture
+            // reads fields only and its own slot only for the other parity (the
+            // first field of the frame); a frame picture never its own slot,
+            // and fields only from field MBs of MBAFF frames (branch-free)
+            const uint8_t *pp = pic->motion + m.aux + 4;
+            unsigned bad = 0;
+            for (int e = 0; e < hdr[1]; e++, pp += 16) {
+                uint16_t wt;
+                memcpy(&wt, pp + 12, 2);
+                bad |= wt >= nweights;
                 for (int l = 0; l < 2; l++) {
-                    const int r = p.ref[l];
-                    if (r < 0) continue;
-                    const int slot = H264R_REF_SLOT(r);
-                    const bool fref = (r & H264R_REF_FIELD) != 0, bref = (r & H264R_REF_BOTTOM) != 0;
-                    if (slot >= dpb_slots) return H264R_ERR_BAD_RECORD;
-                    if (fpic) {
-                        // fields only; its own slot only for the opposite
-                        // parity (the first field of the frame)
-                        if (!fref || (slot == dst && bref == own_bottom)) return H264R_ERR_BAD_RECORD;
-                    } else if (slot == dst || (fref && !mb_field)) {
-                        return H264R_ERR_BAD_RECORD;
-                    }
+                    const int r = (int8_t)pp[8 + l];
+                    const int slot = r & 31;
+                    const unsigned fref = (r >> 5) & 1, bref = (r >> 6) & 1;
+                    const unsigned wrong = (slot >= dpb_slots) |
+                                           (fpic ? ((fref ^ 1u) | ((slot == dst) & (bref == (unsigned)own_bottom)))
+                                                 : ((slot == dst) | (fref & (unsigned)!mb_field)));
+                    bad |= (r >= 0) & wrong;
                 }
             }
+            if (bad) return H264R_ERR_BAD_RECORD;
         } else if (m.type == H264R_MB_IPCM) {
             if (m.aux >= npcm) return H264R_ERR_BAD_RECORD;
         }
@@ -1425,8 +1449,11 @@ extern "C" int h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *st
     std::lock_guard<std::mutex> lk(ctx->mu);
     LaunchBuf &b = ctx->batch_ring[ctx->batch_next];
     ctx->batch_next = (ctx->batch_next + 1) % kBatchRing;
+    const auto t0 = std::chrono::steady_clock::now();
     int rc = wait_slot(ctx, b);
     if (rc) return rc;
+    const auto t1 = std::chrono::steady_clock::now();
+    ctx->host_s[0] += std::chrono::duration<double>(t1 - t0).count();
     // layout of the packed records of every picture, then one host -> device copy
     std::vector<std::array<uint64_t, 7>> offs(n);
     uint64_t tot = 0;
@@ -1512,6 +1539,8 @@ extern "C" int h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *st
         items[i].has_intra = false;
         for (int c = 0; c < K; c++) items[i].has_intra = items[i].has_intra || pintra[(size_t)i * K + c];
     }
+    const auto t2 = std::chrono::steady_clock::now();
+    ctx->host_s[1] += std::chrono::duration<double>(t2 - t1).count();
     cudaStream_t cs = streams[0]->cs;
     cudaEvent_t ev;
     cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
@@ -1535,6 +1564,7 @@ extern "C" int h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *st
         for (int i = 1; i < n; i++)
             if (streams[i]->cs != cs) cudaStreamWaitEvent(streams[i]->cs, ev, 0);
     }
+    ctx->host_s[2] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t2).count();
     cudaEventDestroy(ev);
     return rc;
 }

@@ -25,6 +25,7 @@ EXPORTS = [
     "h264r_load_slot", "h264r_slot_device_ptr", "h264r_stream_sync", "h264r_ctx_sync",
     "h264r_stream_cuda_stream", "h264r_stream_output_cuda_stream", "h264r_validate_picture", "h264r_ctx_kernel_launches",
     "h264r_ctx_set_timing", "h264r_ctx_last_timing", "h264r_ctx_kernel_timing", "h264r_ctx_set_wait_test",
+    "h264r_ctx_host_stats",
     "h264r_synth_create", "h264r_synth_dpb_slots", "h264r_synth_next", "h264r_synth_destroy",
     "h264r_submit_batch", "h264r_picture_bytes", "h264r_ctx_cuda_stream",
     "h264r_deblock_picture_noalloc",
@@ -95,6 +96,7 @@ def _load():
         "h264r_ctx_set_timing": (i32, [vp, i32]),
         "h264r_ctx_set_wait_test": (i32, [vp, u64, i32]),
         "h264r_ctx_kernel_timing": (i32, [vp, P(ctypes.c_float), P(i32)]),
+        "h264r_ctx_host_stats": (i32, [vp, P(ctypes.c_double)]),
         "h264r_write_stream": (i32, [P(R.CWriterCfg), P(P(ctypes.c_uint8)), P(ctypes.c_size_t)]),
         "h264r_writer_free": (None, [P(ctypes.c_uint8)]),
         "h264r_writer_last_error": (ctypes.c_char_p, []),
@@ -247,6 +249,13 @@ class Context:
         n = ctypes.c_int()
         self.check(lib().h264r_ctx_kernel_timing(self.h, t, ctypes.byref(n)), "kernel_timing")
         return list(t), n.value
+
+    def host_stats(self):
+        """Host seconds of h264r_submit_batch: (waiting for a launch slot,
+        validating and packing, upload and launch, packing threads)."""
+        s = (ctypes.c_double * 4)()
+        self.check(lib().h264r_ctx_host_stats(self.h, s), "host_stats")
+        return list(s)
 
     def sync(self):
         return self.check(lib().h264r_ctx_sync(self.h), "ctx_sync")

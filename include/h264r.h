@@ -393,6 +393,11 @@ int  h264r_ctx_last_timing(h264r_ctx *ctx, float t[3], int *launches);
  * on the batch's stream (not beside k_inter / k_intra), so that with one
  * launch sequence in flight at a time each kernel is timed alone. */
 int  h264r_ctx_kernel_timing(h264r_ctx *ctx, float t[4], int *launches);
+/* Host time of the context's h264r_submit_batch calls since it was created,
+ * in seconds: s[0] waiting for a free launch slot (the GPU behind), s[1]
+ * validating and packing the records on the host workers, s[2] upload and
+ * kernel launches; s[3] receives the number of threads that pack. */
+int  h264r_ctx_host_stats(h264r_ctx *ctx, double s[4]);
 
 /*
  * Failure-path tests.  The reference's error convention is to print and
