@@ -709,7 +709,9 @@ def run_engine(args, world, rank, local, dist):
     S = args.streams
     streams_pics, slots = gen_written(S, SEED_BASE + 100 * rank, pictures=args.pictures)
     ngroups = max(p.group for ps in streams_pics for p in ps) + 1
-    ctx = h.Context(local, max_batch=4 * S)
+    # the records are uploaded and complete before any step: the strengths of
+    # a batch are derived as soon as it is submitted (H264R_CFG_DEVICE_RECORDS_READY)
+    ctx = h.Context(local, max_batch=4 * S, records_ready=True)
     streams = [h.Stream(ctx, 120, 68, slots[i]) for i in range(S)]
 
     # ---- records resident in HBM

@@ -87,6 +87,7 @@ struct LaunchBuf {
     cudaEvent_t done = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;  // k_bs on the owner's side stream
     cudaEvent_t uploaded = nullptr;              // host-record upload on the context's upload stream
+    bool wait_upload = false;                    // the records of the current use come through `uploaded`
     bool pending = false;
     GraphEntry graphs[kGraphCache];
     int ngraphs = 0;
@@ -170,6 +171,7 @@ struct h264r_ctx {
     // host time of h264r_submit_batch calls (seconds): waiting for a free
     // launch slot, validating and packing on the workers, upload and launch
     double host_s[3] = {0, 0, 0};
+    bool records_ready = false;  // H264R_CFG_DEVICE_RECORDS_READY
     uint64_t budget = 0, used = 0;
     uint32_t max_batch = 64;
     int *d_error = nullptr;
@@ -266,6 +268,7 @@ extern "C" int h264r_ctx_create(const h264r_cfg *cfg, h264r_ctx **out)
     if (!ctx) return H264R_ERR_NO_MEMORY;
     ctx->device = cfg ? cfg->device : 0;
     if (cfg && cfg->max_batch_pictures) ctx->max_batch = cfg->max_batch_pictures;
+    ctx->records_ready = cfg && (cfg->flags & H264R_CFG_DEVICE_RECORDS_READY);
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) {
         fprintf(stderr, "h264r_ctx_create: cudaSetDevice(%d): %s\n", ctx->device, cudaGetErrorString(e));
@@ -746,22 +749,37 @@ struct Seq {
 // Enqueue the descriptor upload and the kernels of one launch sequence on cs
 // (directly, or into a stream capture); *kernels receives how many kernels.
 static int enqueue_sequence(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const Seq &q, cudaStream_t side,
-                            const std::array<cudaEvent_t, 5> *ev, uint32_t *kernels)
+                            const std::array<cudaEvent_t, 5> *ev, uint32_t *kernels, bool early_bs = false)
 {
     uint32_t nk = 0;
-    CUDA_OR(ctx, cudaMemcpyAsync(b.dev, b.host, q.total, cudaMemcpyHostToDevice, cs));
     const unsigned bs_grid = (unsigned)((q.mbs + 3) / 4);
     // The strengths depend on the records alone, so for frame pictures k_bs
     // runs on the side stream of the batch's first stream while k_inter and
     // k_intra fill the device; the deblocking kernels wait for it.  MBAFF
     // strengths cost more and slow the intra wavefront they would share the
     // SMs with (measured: 6 % fewer 1080i frames/s), so they stay in line.
-    if (q.bs_aside) {
-        CUDA_OR(ctx, cudaEventRecord(b.fork, cs));
-        CUDA_OR(ctx, cudaStreamWaitEvent(side, b.fork, 0));
+    // Launched directly (not captured), the side stream also takes the
+    // descriptor upload and starts k_bs right away, without waiting for the
+    // kernels of the batch before on cs: its strengths are ready when this
+    // batch's deblocking starts.  (The descriptors and strength tables of
+    // this launch slot are free: wait_slot saw its last use complete.)
+    if (q.bs_aside && early_bs) {
+        if (b.wait_upload) CUDA_OR(ctx, cudaStreamWaitEvent(side, b.uploaded, 0));
+        CUDA_OR(ctx, cudaMemcpyAsync(b.dev, b.host, q.total, cudaMemcpyHostToDevice, side));
+        CUDA_OR(ctx, cudaEventRecord(b.fork, side));
         h264r::k_bs<<<bs_grid, 128, 0, side>>>(q.dd, q.n, (uint32_t)q.mbs, q.st);
         nk++;
         CUDA_OR(ctx, cudaEventRecord(b.join, side));
+        CUDA_OR(ctx, cudaStreamWaitEvent(cs, b.fork, 0));
+    } else {
+        CUDA_OR(ctx, cudaMemcpyAsync(b.dev, b.host, q.total, cudaMemcpyHostToDevice, cs));
+        if (q.bs_aside) {
+            CUDA_OR(ctx, cudaEventRecord(b.fork, cs));
+            CUDA_OR(ctx, cudaStreamWaitEvent(side, b.fork, 0));
+            h264r::k_bs<<<bs_grid, 128, 0, side>>>(q.dd, q.n, (uint32_t)q.mbs, q.st);
+            nk++;
+            CUDA_OR(ctx, cudaEventRecord(b.join, side));
+        }
     }
     if (ev) cudaEventRecord((*ev)[0], cs);
     const unsigned inter_grid = (unsigned)((q.mbs + q.inter_w - 1) / q.inter_w);
@@ -830,7 +848,10 @@ static GraphEntry *graph_entry(LaunchBuf &b, const GraphKey &key)
     return nullptr;
 }
 
-static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vector<BatchItem> &items, bool any_intra)
+// early_bs: the records are complete, or ordered by b.uploaded
+// (b.wait_upload): k_bs need not wait for the work queued on cs
+static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vector<BatchItem> &items, bool any_intra,
+                  bool early_bs)
 {
     const int n = (int)items.size();
     std::vector<const h264r_picture *> pl(n);
@@ -995,7 +1016,8 @@ static int launch(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const std::vect
     } else {
         std::array<cudaEvent_t, 5> ev{};
         if (ctx->timing) ev = *take_events(ctx);
-        rc = enqueue_sequence(ctx, cs, b, q, side, ctx->timing ? &ev : nullptr, &nk);
+        rc = enqueue_sequence(ctx, cs, b, q, side, ctx->timing ? &ev : nullptr, &nk, early_bs);
+        b.wait_upload = false;
         if (rc) return rc;
         ctx->launches += nk;
     }
@@ -1055,6 +1077,8 @@ extern "C" int h264r_submit_picture(h264r_stream *s, const h264r_picture *pic)
     memcpy(b.rec_host + off[6], pic->scaling4x4, 96);
     memcpy(b.rec_host + off[6] + 96, pic->scaling8x8, 384);
     CUDA_OR(ctx, cudaMemcpyAsync(b.rec_dev, b.rec_host, tot, cudaMemcpyHostToDevice, s->cs));
+    CUDA_OR(ctx, cudaEventRecord(b.uploaded, s->cs));
+    b.wait_upload = true;
     h264r_picture dp = *pic;
     dp.mbs = (const h264r_mb *)(b.rec_dev + off[0]);
     dp.slices = (const h264r_slice *)(b.rec_dev + off[1]);
@@ -1067,7 +1091,7 @@ extern "C" int h264r_submit_picture(h264r_stream *s, const h264r_picture *pic)
     items[0].pic = &dp;
     items[0].scaling_dev = b.rec_dev + off[6];
     items[0].has_intra = has_intra_mbs(pic);
-    return launch(ctx, s->cs, b, items, items[0].has_intra);
+    return launch(ctx, s->cs, b, items, items[0].has_intra, true);
 }
 
 // Device-resident records: the scaling lists are read from the host struct
@@ -1095,7 +1119,7 @@ static int submit_device(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, int n, h
         any_intra = true;
     }
     CUDA_OR(ctx, cudaMemcpyAsync(b.rec_dev, b.rec_host, tot, cudaMemcpyHostToDevice, cs));
-    return launch(ctx, cs, b, items, any_intra);
+    return launch(ctx, cs, b, items, any_intra, ctx->records_ready);
 }
 
 static int check_device_pic(h264r_stream *s, const h264r_picture *pic)
@@ -1558,7 +1582,8 @@ extern "C" int h264r_submit_batch(h264r_ctx *ctx, int n, h264r_stream *const *st
         set_err(ctx, "h264r_submit_batch: record upload failed");
         rc = H264R_ERR_CUDA;
     }
-    if (rc == H264R_OK) rc = launch(ctx, cs, b, items, any_intra);
+    b.wait_upload = true;  // an early k_bs on the side stream waits for it too
+    if (rc == H264R_OK) rc = launch(ctx, cs, b, items, any_intra, true);
     if (rc == H264R_OK) {
         cudaEventRecord(ev, cs);
         for (int i = 1; i < n; i++)

@@ -206,8 +206,10 @@ def validate(pic, dpb_slots):
 class Context:
     """An engine context on one GPU (h264r_ctx)."""
 
-    def __init__(self, device=0, dpb_budget_bytes=0, max_batch=64):
-        cfg = R.CCfg(device, dpb_budget_bytes, max_batch, 0)
+    def __init__(self, device=0, dpb_budget_bytes=0, max_batch=64, records_ready=False):
+        # records_ready: H264R_CFG_DEVICE_RECORDS_READY (device records are
+        # complete when a *_device submit is made)
+        cfg = R.CCfg(device, dpb_budget_bytes, max_batch, 1 if records_ready else 0)
         h = ctypes.c_void_p()
         rc = lib().h264r_ctx_create(ctypes.byref(cfg), ctypes.byref(h))
         if rc != 0:

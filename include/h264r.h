@@ -212,8 +212,16 @@ typedef struct h264r_cfg {
     uint64_t dpb_budget_bytes;   /* admission budget for all stream DPBs;
                                     0 = 90% of free device memory            */
     uint32_t max_batch_pictures; /* pictures per batched launch (0: 64)      */
-    uint32_t flags;              /* reserved, 0                              */
+    uint32_t flags;              /* H264R_CFG_*                              */
 } h264r_cfg;
+
+/* h264r_cfg.flags: device-resident records are complete in device memory
+ * when h264r_submit_*_device is called (they are not produced by work still
+ * queued on the streams).  The boundary strengths of a batch are then derived
+ * on the stream's side stream as soon as the call is made, ahead of the
+ * batches queued before it.  (Host-resident records are uploaded by the
+ * engine itself and get this ordering without the flag.) */
+#define H264R_CFG_DEVICE_RECORDS_READY 0x1u
 
 typedef struct h264r_stream_cfg {
     uint16_t width_mbs;
