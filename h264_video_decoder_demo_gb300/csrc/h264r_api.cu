@@ -752,7 +752,7 @@ static int enqueue_sequence(h264r_ctx *ctx, cudaStream_t cs, LaunchBuf &b, const
                             const std::array<cudaEvent_t, 5> *ev, uint32_t *kernels, bool early_bs = false)
 {
     uint32_t nk = 0;
-    const unsigned bs_grid = (unsigned)((q.mbs + 3) / 4);
+    const unsigned bs_grid = (unsigned)((q.mbs + h264r::kBsMbsPerBlock - 1) / h264r::kBsMbsPerBlock);
     // The strengths depend on the records alone, so for frame pictures k_bs
     // runs on the side stream of the batch's first stream while k_inter and
     // k_intra fill the device; the deblocking kernels wait for it.  MBAFF

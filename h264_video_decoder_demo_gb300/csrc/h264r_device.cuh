@@ -136,6 +136,7 @@ constexpr int kDbWarps = 8;   // MB-row pairs (warps) per frame deblocking block
 constexpr int kDbXRing = 16;  // MBs of a warp's bottom lines kept for the warp below
 constexpr int kMbWarps = 8;   // MB-pair rows (warps) per MBAFF deblocking block
 constexpr int kMbXRing = 8;   // MB pairs of a warp's bottom rows kept for the warp below
+constexpr int kBsMbsPerBlock = 8;  // k_bs: 4 warps of 2 MBs per block
 __host__ __device__ inline uint32_t deblock_units(int mbaff, uint32_t units_h)
 {
     return mbaff ? 2u * ((units_h + kMbWarps - 1u) / kMbWarps) : 0u;

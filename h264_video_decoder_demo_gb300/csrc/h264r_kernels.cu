@@ -1330,198 +1330,259 @@ __device__ __forceinline__ void edge_params(const PicDesc &p, int mbP, int cur, 
     beta = kBeta[indexB];
 }
 
-__global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st)
+// Motion of a 4x4 block for the frame-picture strength rules, with the
+// block's MB-level facts: mv0 / mv1 the list 0 / 1 vectors (x | y << 16);
+// rf: dref[0] | dref[1] << 8 (0xFF: none), bit 16 / 17 list 0 / 1 used,
+// bit 18 the block has non-zero levels, bit 19 its MB is intra (I4x4, I8x8,
+// I16x16), bit 20 its MB was never decoded.  The motion is block_motion's.
+struct BsBlock {
+    uint32_t mv0, mv1, rf;
+};
+
+__device__ __forceinline__ BsBlock bs_block(const PicDesc &p, int type, int flags, int nz4, int nz8, uint32_t aux, int bx, int by)
 {
-    // one warp per MB; 4 MBs per block
-    const uint32_t g = blockIdx.x * 4 + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (g >= total_mbs) return;
-    const int pi = find_pic_by_mb(pics, npics, g);
-    PicDesc *pp = const_cast<PicDesc *>(&pics[pi]);
-    const PicDesc &p = pics[pi];
-    const int cur = (int)(g - p.mb_base);
-    if (!p.deblock) return;
-    EdgeCtl c = edge_ctl(p, cur);
-    uint8_t *out = p.bs + (size_t)cur * kBsBytes;
-    uint32_t mystop = 0xFFFFFFFFu;
-    if (!p.mbaff) {
-        // Frame picture: a strength depends only on the pair of 4x4 blocks
-        // (no field or mixed edges), so lane (dir, e, b) derives edge e of
-        // direction dir for lines 4b..4b+3, and the 4:2:0 chroma strengths
-        // are the luma ones of the same edge at line 2k (the reference
-        // derives them from the luma positions, 994-1310).
-        // The records of the MB and of its left and top neighbours are read
-        // once, and the motion of every block an edge touches once, by one
-        // lane each (0-15 the MB's blocks in raster order, 16-19 column 3
-        // of the left MB, 20-23 row 3 of the MB above); an edge lane takes
-        // its two blocks by shuffles.  The rules are derive_bs's for a frame
-        // picture (no field MBs) or a field picture (all field MBs: bS 3 on
-        // horizontal MB edges of intra MBs, vertical MV limit 2).
-        const int dir = lane >> 4, e = (lane >> 2) & 3, b = lane & 3;
-        const bool on = e == 0 ? (dir ? c.top : c.left) : (c.internal && (e == 2 || !c.t8));
-        const h264r_mb Q = p.mbs[cur];
-        const h264r_mb A = c.mbA >= 0 ? p.mbs[c.mbA] : Q, B = c.mbB >= 0 ? p.mbs[c.mbB] : Q;
-        uint32_t mv0, mv1, rf;  // this lane's block: list 0 / 1 vectors (x | y << 16), refs and flags
-        {
-            const int src = lane < 16 ? 0 : (lane < 20 ? 1 : 2);
-            const int bx = lane < 16 ? (lane & 3) : (lane < 20 ? 3 : (lane < 24 ? lane - 20 : 0));
-            const int by = lane < 16 ? (lane >> 2) : (lane < 20 ? lane - 16 : 3);
-            BlkMotion bm;
-            block_motion(p, src == 0 ? Q.type : (src == 1 ? A.type : B.type), src == 0 ? Q.aux : (src == 1 ? A.aux : B.aux), bx, by, bm);
-            mv0 = ((uint32_t)bm.mv[0][0] & 0xFFFFu) | ((uint32_t)bm.mv[0][1] << 16);
-            mv1 = ((uint32_t)bm.mv[1][0] & 0xFFFFu) | ((uint32_t)bm.mv[1][1] << 16);
-            rf = ((uint32_t)bm.id[0] & 0xFFu) | (((uint32_t)bm.id[1] & 0xFFu) << 8) | ((uint32_t)bm.pf[0] << 16) | ((uint32_t)bm.pf[1] << 17);
-        }
-        const int qsrc = dir == 0 ? b * 4 + e : e * 4 + b;
-        const int psrc = e > 0 ? (dir == 0 ? b * 4 + e - 1 : (e - 1) * 4 + b) : (dir == 0 ? 16 + b : 20 + b);
-        auto unpack = [](uint32_t v0, uint32_t v1, uint32_t r, BlkMotion &o) {
-            o.mv[0][0] = (int16_t)(v0 & 0xFFFFu);
-            o.mv[0][1] = (int16_t)(v0 >> 16);
-            o.mv[1][0] = (int16_t)(v1 & 0xFFFFu);
-            o.mv[1][1] = (int16_t)(v1 >> 16);
-            o.id[0] = (int8_t)(r & 0xFFu);
-            o.id[1] = (int8_t)((r >> 8) & 0xFFu);
-            o.pf[0] = (r >> 16) & 1u;
-            o.pf[1] = (r >> 17) & 1u;
-        };
-        BlkMotion mp, mq;
-        unpack(__shfl_sync(0xffffffffu, mv0, psrc), __shfl_sync(0xffffffffu, mv1, psrc), __shfl_sync(0xffffffffu, rf, psrc), mp);
-        unpack(__shfl_sync(0xffffffffu, mv0, qsrc), __shfl_sync(0xffffffffu, mv1, qsrc), __shfl_sync(0xffffffffu, rf, qsrc), mq);
-        auto sp_of = [&](const h264r_mb &m) -> bool {
-            const int t = p.slices[min((uint32_t)m.slice, p.num_slices - 1)].slice_type;
-            return t == 3 || t == 4;
-        };
-        int bs = 0;
-        if (on) {
-            // an MB edge whose neighbour is not available (another slice
-            // under disable_deblocking_filter_idc 0) takes the MB itself as
-            // its p side, as derive_bs does: no bS 4 there
-            const bool mbedge = e == 0 && (dir == 0 ? c.mbA >= 0 : c.mbB >= 0);
-            const int ptype = mbedge ? (dir == 0 ? A.type : B.type) : Q.type;
-            const bool spP = mbedge ? (dir == 0 ? sp_of(A) : sp_of(B)) : sp_of(Q), spQ = sp_of(Q);
-            if (is_intra_type(ptype) || is_intra_type(Q.type) || spP || spQ) {
-                bs = mbedge && (dir == 0 || !p.fpic) ? 4 : 3;
-            } else {
-                const int qx = dir == 0 ? e : b, qy = dir == 0 ? b : e;
-                const int px = dir == 0 ? (e > 0 ? e - 1 : 3) : b, py = dir == 0 ? b : (e > 0 ? e - 1 : 3);
-                const int pflags = mbedge ? (dir == 0 ? A.flags : B.flags) : Q.flags;
-                const int pnz4 = mbedge ? (dir == 0 ? A.nz4x4 : B.nz4x4) : Q.nz4x4, pnz8 = mbedge ? (dir == 0 ? A.nz8x8 : B.nz8x8) : Q.nz8x8;
-                auto blk4 = [](int x4, int y4) { return 8 * (y4 >> 1) + 4 * (x4 >> 1) + 2 * (y4 & 1) + (x4 & 1); };
-                const int nzP = (pflags & H264R_MBF_T8x8) ? ((pnz8 >> (2 * (py >> 1) + (px >> 1))) & 1) : ((pnz4 >> blk4(px, py)) & 1);
-                const int nzQ = (Q.flags & H264R_MBF_T8x8) ? ((Q.nz8x8 >> (2 * (qy >> 1) + (qx >> 1))) & 1) : ((Q.nz4x4 >> blk4(qx, qy)) & 1);
-                if (nzP || nzQ) bs = 2;
-                else if (ptype == H264R_MB_NONE || Q.type == H264R_MB_NONE) bs = 0xFF;
-                else bs = bs_motion(mp, mq, p.fpic ? 2 : 4);
-            }
-        }
-        if (bs == 0xFF) mystop = stop_key(cur, dir == 0 ? SEQ_LV0 + e : (e == 0 ? SEQ_LH0 : SEQ_LH4 + e - 1), 4 * b);
-        const int k = lane & 15;
-        uint32_t vrow = 0, hrow = 0;
-#pragma unroll
-        for (int e2 = 0; e2 < 4; e2++) {
-            vrow |= (uint32_t)(__shfl_sync(0xffffffffu, bs, e2 * 4 + (k >> 2)) & 255) << (8 * e2);
-            hrow |= (uint32_t)(__shfl_sync(0xffffffffu, bs, 16 + e2 * 4 + (k >> 2)) & 255) << (8 * e2);
-        }
-        *(uint32_t *)(out + (lane < 16 ? bs_lv(0, k) : bs_lh(0, k))) = lane < 16 ? vrow : hrow;
-        // chroma line ck: edges 0 and 4 are luma edges 0 and 8 at luma line 2*ck
-        const int ck = lane & 7;
-        const uint32_t c0 = (uint32_t)(vrow & 255), c1 = (vrow >> 16) & 255;  // lane k = 2*ck holds line 2*ck
-        const uint32_t h0 = (uint32_t)(hrow & 255), h1 = (hrow >> 16) & 255;
-        const uint32_t cvw = __shfl_sync(0xffffffffu, c0 | (c1 << 8), 2 * ck);
-        const uint32_t chw = __shfl_sync(0xffffffffu, h0 | (h1 << 8), 2 * ck);
-        if (lane < 8) *(uint16_t *)(out + bs_cv(0, ck)) = (uint16_t)cvw;
-        else if (lane < 16) *(uint16_t *)(out + bs_ch(0, ck)) = (uint16_t)chw;
-    } else {
-        // MBAFF.  Internal edges join two 4x4 blocks of the same MB (never a
-        // mixed edge), so their strength is uniform over the 4 lines of a
-        // block pair as in frame pictures: lanes 0..23 derive them
-        // (dir, edge 1..3, block), and 4:2:0 chroma takes the luma value of
-        // edge 8 at luma line 2k.  The MB edges (left, top, second top of a
-        // frame MB under a field pair) are derived per line.
-        uint32_t ivrow = 0, ihrow = 0;  // lane k < 16: internal strengths of line / column k, byte e
-        {
-            int bs = 0, dir = 0, ei = 1, b = 0;
-            if (lane < 24) {
-                dir = lane / 12;
-                ei = 1 + (lane % 12) / 4;
-                b = lane & 3;
-                if (c.internal && (ei == 2 || !c.t8))
-                    bs = dir == 0 ? edge_bs(p, cur, 0, 1, 4 * ei, c.mbA, 0, 4 * b) : edge_bs(p, cur, 0, 0, 4 * ei, c.mbB, 0, 4 * b);
-                if (bs == 0xFF) mystop = min(mystop, stop_key(cur, dir == 0 ? SEQ_LV0 + ei : SEQ_LH4 + ei - 1, 4 * b));
-            }
-            const int k = lane & 15;
-#pragma unroll
-            for (int e2 = 1; e2 < 4; e2++) {
-                ivrow |= (uint32_t)(__shfl_sync(0xffffffffu, bs, (e2 - 1) * 4 + (k >> 2)) & 255) << (8 * e2);
-                ihrow |= (uint32_t)(__shfl_sync(0xffffffffu, bs, 12 + (e2 - 1) * 4 + (k >> 2)) & 255) << (8 * e2);
-            }
-        }
-        // MB edges per line: left (0..15), top (16..31), second top (32..47) luma;
-        // chroma left (48..55), top (56..63), second top (64..71)
-        uint32_t lv0 = 0, lh0 = 0;  // lane k < 16: luma left / top strength of line / column k
-        for (int it = lane; it < 72; it += 32) {
-            int bs = 0, seq = 0, k = 0;
-            if (it < 16) {
-                k = it;
-                if (c.left) bs = edge_bs(p, cur, 0, 1, 0, c.mbA, c.leftMixed, k);
-                seq = SEQ_LV0;
-                lv0 = (uint32_t)bs;
-            } else if (it < 32) {
-                k = it - 16;
-                if (c.top) bs = c.topDouble ? edge_bs(p, cur, 0, 0, 0, c.mbB - 1, 0, k) : edge_bs(p, cur, 0, 0, 0, c.mbB, 0, k);
-                seq = SEQ_LH0;
-            } else if (it < 48) {
-                k = it - 32;
-                if (c.top && c.topDouble) bs = edge_bs(p, cur, 0, 0, 1, c.mbB, 0, k);
-                seq = SEQ_LH0B;
-                out[kBsLumaTop2 + k] = (uint8_t)bs;
-            } else if (it < 56) {
-                k = it - 48;
-                if (c.left) bs = edge_bs(p, cur, 1, 1, 0, c.mbA, c.leftMixed, k);
-                seq = SEQ_CBV0;
-                out[bs_cv(0, k)] = (uint8_t)bs;
-            } else if (it < 64) {
-                k = it - 56;
-                if (c.top) bs = edge_bs(p, cur, 1, 0, 0, c.mbB, 0, k);
-                seq = SEQ_CBH0;
-                out[bs_ch(0, k)] = (uint8_t)bs;
-            } else {
-                k = it - 64;
-                if (c.top && c.topDouble) bs = edge_bs(p, cur, 1, 0, 1, c.mbB, 0, k);
-                seq = SEQ_CBH0B;
-                out[kBsChromaTop2 + k] = (uint8_t)bs;
-            }
-            if (it >= 16 && it < 32) lh0 = (uint32_t)bs;
-            if (bs == 0xFF) mystop = min(mystop, stop_key(cur, seq, k));
-        }
-        // lanes 16..31 derived the top edge of column lane-16 in their first item
-        lh0 = __shfl_sync(0xffffffffu, lh0, (lane & 15) + 16);
-        if (lane < 16) {
-            *(uint32_t *)(out + bs_lv(0, lane)) = ivrow | (lv0 & 255);
-            *(uint32_t *)(out + bs_lh(0, lane)) = ihrow | (lh0 & 255);
-        }
-        // chroma internal edge (4): luma edge 8 at luma line / column 2k
-        const int ck = lane & 7;
-        const uint32_t civ = __shfl_sync(0xffffffffu, (ivrow >> 16) & 255, 2 * ck);
-        const uint32_t cih = __shfl_sync(0xffffffffu, (ihrow >> 16) & 255, 2 * ck);
-        if (lane < 8) out[bs_cv(1, ck)] = (uint8_t)civ;
-        else if (lane < 16) out[bs_ch(1, ck)] = (uint8_t)cih;
+    const int nz = (flags & H264R_MBF_T8x8) ? (nz8 >> (2 * (by >> 1) + (bx >> 1))) & 1
+                                            : (nz4 >> (8 * (by >> 1) + 4 * (bx >> 1) + 2 * (by & 1) + (bx & 1))) & 1;
+    BsBlock o;
+    o.mv0 = o.mv1 = 0;
+    o.rf = 0xFFFFu | ((uint32_t)nz << 18) | ((uint32_t)is_intra_type(type) << 19) | ((uint32_t)(type == H264R_MB_NONE) << 20);
+    if (type != H264R_MB_INTER || aux == H264R_NONE || (aux & 3) || (uint64_t)aux + 4 > p.motion_bytes) return o;
+    const uint32_t hdr = *(const uint32_t *)(p.motion + aux);
+    const int e = part_of_block(hdr & 0xFFFF, bx, by);
+    if (e >= (int)(hdr >> 16) || (uint64_t)aux + 4 + 16ull * (e + 1) > p.motion_bytes) return o;
+    // h264r_part: mv[2][2] (8 bytes), ref[2], dref[2]
+    const uint32_t *q = (const uint32_t *)(p.motion + aux + 4 + 16 * e);
+    const uint32_t w = q[2];
+    o.mv0 = q[0];
+    o.mv1 = q[1];
+    o.rf = (o.rf & 0x1C0000u) | (w >> 16) | ((w & 0x80u) ? 0u : 0x10000u) | ((w & 0x8000u) ? 0u : 0x20000u);
+    return o;
+}
+
+// bs_motion on packed blocks: a the p side, b the q side.  Once the two
+// blocks use the same reference pictures in the same number of lists, one
+// list each compares the vectors used; two lists compare the vectors of the
+// same reference picture, or (both lists on one picture) the reference's
+// (A || B) && C || D (H264PictureDeblockingFilterProcess.cpp:1230-1310).
+__device__ __forceinline__ int bs_motion_packed(const BsBlock &a, const BsBlock &b, int lim)
+{
+    const uint32_t ra = a.rf, rb = b.rf;
+    const uint32_t r0p = ra & 255u, r1p = (ra >> 8) & 255u, r0q = rb & 255u, r1q = (rb >> 8) & 255u;
+    const int np = (int)((ra >> 16) & 1u) + (int)((ra >> 17) & 1u), nq = (int)((rb >> 16) & 1u) + (int)((rb >> 17) & 1u);
+    if (!(((r0p == r0q && r1p == r1q) || (r0p == r1q && r1p == r0q)) && np == nq)) return 1;
+    auto diff = [lim](uint32_t u, uint32_t v) {
+        const int dx = abs(((int)(u << 16) >> 16) - ((int)(v << 16) >> 16));
+        const int dy = abs(((int)u >> 16) - ((int)v >> 16));
+        return dx >= 4 || dy >= lim;
+    };
+    if (np == 1) return diff((ra & 0x10000u) ? a.mv0 : a.mv1, (rb & 0x10000u) ? b.mv0 : b.mv1);
+    if (np == 2) {
+        const bool d00 = diff(a.mv0, b.mv0), d11 = diff(a.mv1, b.mv1), d01 = diff(a.mv0, b.mv1), d10 = diff(a.mv1, b.mv0);
+        if (r0p != r1p) return r0q == r0p ? (d00 || d11) : (d10 || d01);
+        return ((d00 || d11) && d01) || d10;
     }
-    // thresholds of each edge class for the frame fast path of k_deblock
-    if (!p.mbaff && lane < 9) {
-        const int comp = lane / 3, kind = lane % 3;  // kind: 0 left, 1 top, 2 internal
-        int mbP = cur;
-        if (kind == 0 && c.mbA >= 0) mbP = c.mbA;
-        if (kind == 1 && c.mbB >= 0) mbP = c.mbB;
-        int iA, al, be;
-        edge_params(p, mbP, cur, comp, iA, al, be);
-        const uint32_t w = (uint32_t)al | ((uint32_t)be << 8) | ((uint32_t)kTc0[0][iA] << 16) |
+    return 0;
+}
+
+// Strengths and thresholds of a frame or field picture's MB (no MBAFF), two
+// MBs per warp: half h of the warp takes MB g, lane j of the half its 4x4
+// block (j & 3, j >> 2), whose left edge (vertical edge j & 3, lines
+// 4(j >> 2)..+3) and top edge (horizontal edge j >> 2, columns 4(j & 3)..+3)
+// it derives.  In a frame picture a strength depends only on the pair of
+// blocks the edge joins (no field or mixed edges); the 4:2:0 chroma
+// strengths are the luma ones of the same edge at line 2k (the reference
+// derives them from the luma positions, 994-1310).  Each lane reads the
+// motion of its block; the lanes of column 3 also read the block left of
+// their row (column 3 of the left MB) and those of row 3 the block above
+// their column (row 3 of the MB above), so that every edge takes its p side
+// in one shuffle.  A neighbour MB is available only in the MB's own slice,
+// so the SP / SI rule reads the MB's slice alone.  The rules are derive_bs's
+// for a frame picture (no field MBs) or a field picture (all field MBs: bS 3
+// on horizontal MB edges of intra MBs, vertical MV limit 2).  All lanes run
+// this; `on` false: the half's MB is not a deblocked frame-picture MB, and
+// nothing is written for it.
+__device__ __forceinline__ void bs_frame_half(const PicDesc *__restrict__ pics, int pi, uint32_t g, bool on)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, j = lane & 15, hb = lane & 16, bx = j & 3, by = j >> 2;
+    const PicDesc &p = pics[pi];
+    const int cur = on ? (int)(g - p.mb_base) : 0;
+    const int W = p.wmb, col = cur % W;
+    const h264r_mb Q = p.mbs[cur];
+    const h264r_mb A0 = p.mbs[col != 0 ? cur - 1 : cur], B0 = p.mbs[cur >= W ? cur - W : cur];
+    const bool hasA = col != 0 && A0.slice == Q.slice, hasB = cur >= W && B0.slice == Q.slice;
+    const h264r_slice sl = p.slices[min((uint32_t)Q.slice, p.num_slices - 1)];
+    const int idc = sl.disable_deblocking_filter_idc;
+    const bool sp = sl.slice_type == 3 || sl.slice_type == 4;
+    const bool t8 = (Q.flags & H264R_MBF_T8x8) != 0;
+    const bool onL = bx == 0 ? !(col == 0 || idc == 1 || (idc == 2 && !hasA)) : (idc != 1 && (bx == 2 || !t8));
+    const bool onT = by == 0 ? !(cur < W || idc == 1 || (idc == 2 && !hasB)) : (idc != 1 && (by == 2 || !t8));
+    // an MB edge whose neighbour is not available (another slice under
+    // disable_deblocking_filter_idc 0) takes the MB itself as its p side
+    const BsBlock own = bs_block(p, Q.type, Q.flags, Q.nz4x4, Q.nz8x8, Q.aux, bx, by);
+    BsBlock sendL = own, sendT = own;
+    if (bx == 3) {
+        sendL = hasA ? bs_block(p, A0.type, A0.flags, A0.nz4x4, A0.nz8x8, A0.aux, 3, by)
+                     : bs_block(p, Q.type, Q.flags, Q.nz4x4, Q.nz8x8, Q.aux, 3, by);
+    }
+    if (by == 3) {
+        sendT = hasB ? bs_block(p, B0.type, B0.flags, B0.nz4x4, B0.nz8x8, B0.aux, bx, 3)
+                     : bs_block(p, Q.type, Q.flags, Q.nz4x4, Q.nz8x8, Q.aux, bx, 3);
+    }
+    const int srcL = hb + (bx > 0 ? j - 1 : 4 * by + 3), srcT = hb + (by > 0 ? j - 4 : 12 + bx);
+    BsBlock pl, pt;
+    pl.mv0 = __shfl_sync(FULL, sendL.mv0, srcL);
+    pl.mv1 = __shfl_sync(FULL, sendL.mv1, srcL);
+    pl.rf = __shfl_sync(FULL, sendL.rf, srcL);
+    pt.mv0 = __shfl_sync(FULL, sendT.mv0, srcT);
+    pt.mv1 = __shfl_sync(FULL, sendT.mv1, srcT);
+    pt.rf = __shfl_sync(FULL, sendT.rf, srcT);
+    const int lim = p.fpic ? 2 : 4;
+    auto strength = [&](const BsBlock &pb, bool edge_on, bool mbedge, bool vertical) -> int {
+        if (!edge_on) return 0;
+        const uint32_t f = pb.rf | own.rf;
+        if ((f & (1u << 19)) || sp) return mbedge && (vertical || !p.fpic) ? 4 : 3;
+        if (f & (1u << 18)) return 2;
+        if (f & (1u << 20)) return 0xFF;
+        return bs_motion_packed(pb, own, lim);
+    };
+    const int bsL = strength(pl, onL, bx == 0 && hasA, true);
+    const int bsT = strength(pt, onT, by == 0 && hasB, false);
+    uint32_t mystop = 0xFFFFFFFFu;
+    if (bsL == 0xFF) mystop = stop_key(cur, SEQ_LV0 + bx, 4 * by);
+    if (bsT == 0xFF) mystop = min(mystop, stop_key(cur, by == 0 ? SEQ_LH0 : SEQ_LH4 + by - 1, 4 * bx));
+    if (__any_sync(FULL, on && mystop != 0xFFFFFFFFu)) {
+        for (int o = 8; o > 0; o >>= 1) mystop = min(mystop, __shfl_xor_sync(FULL, mystop, o));
+        if (on && j == 0 && mystop != 0xFFFFFFFFu) atomicMin(&const_cast<PicDesc *>(&p)->deblock_stop, mystop);
+    }
+    // line / column j (block row / column j >> 2): byte e the strength of
+    // edge e there
+    const int jq = j >> 2;
+    uint32_t vrow = 0, hrow = 0;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        vrow |= (uint32_t)(__shfl_sync(FULL, bsL, hb + 4 * jq + e) & 255) << (8 * e);
+        hrow |= (uint32_t)(__shfl_sync(FULL, bsT, hb + 4 * e + jq) & 255) << (8 * e);
+    }
+    uint8_t *out = p.bs + (size_t)cur * kBsBytes;
+    if (on) {
+        *(uint32_t *)(out + bs_lv(0, j)) = vrow;
+        *(uint32_t *)(out + bs_lh(0, j)) = hrow;
+    }
+    // chroma line / column ck: edges 0 and 4 are luma edges 0 and 8 at luma
+    // line / column 2ck
+    const uint32_t cv = __shfl_sync(FULL, (vrow & 255u) | ((vrow >> 8) & 0xFF00u), hb + 2 * (j & 7));
+    const uint32_t ch = __shfl_sync(FULL, (hrow & 255u) | ((hrow >> 8) & 0xFF00u), hb + 2 * (j & 7));
+    if (on) {
+        if (j < 8) *(uint16_t *)(out + bs_cv(0, j)) = (uint16_t)cv;
+        else *(uint16_t *)(out + bs_ch(0, j - 8)) = (uint16_t)ch;
+    }
+    // thresholds of each edge class for k_deblock_frame: lane j < 9 the
+    // component j / 3 and the class j % 3 (left, top, internal) of edge_params
+    if (on && j < 9) {
+        const int comp = j / 3, kind = j % 3;
+        const bool useA = kind == 0 && hasA, useB = kind == 1 && hasB;
+        const int ptype = useA ? A0.type : (useB ? B0.type : Q.type);
+        const int pqp = useA ? A0.qpy : (useB ? B0.qpy : Q.qpy);
+        int qPp = ptype == H264R_MB_IPCM ? 0 : pqp, qPq = Q.type == H264R_MB_IPCM ? 0 : Q.qpy;
+        if (comp > 0) {
+            const int off = sl.chroma_qp_offset[comp - 1];
+            qPp = chroma_qp(qPp, off);
+            qPq = chroma_qp(qPq, off);
+        }
+        const int qPav = (qPp + qPq + 1) >> 1;
+        const int iA = H264R_CLIP3(0, 51, qPav + sl.filter_offset_a), iB = H264R_CLIP3(0, 51, qPav + sl.filter_offset_b);
+        const uint32_t w = (uint32_t)kAlpha[iA] | ((uint32_t)kBeta[iB] << 8) | ((uint32_t)kTc0[0][iA] << 16) |
                            ((uint32_t)kTc0[1][iA] << 21) | ((uint32_t)kTc0[2][iA] << 26);
         *(uint32_t *)(out + kBsParams + 16 * comp + 4 * kind) = w;
     }
-    // MBAFF pictures: the edge controls of the MB and the thresholds of its
-    // edges, so that the deblocking wavefront reads no records
-    if (p.mbaff && lane < 16) {
+}
+
+// MBAFF pictures: the strengths, edge controls and thresholds of MB cur with
+// the whole warp.
+__device__ __noinline__ void bs_mbaff_mb(const PicDesc &p, PicDesc *pp, int cur)
+{
+    const int lane = threadIdx.x & 31;
+    EdgeCtl c = edge_ctl(p, cur);
+    uint8_t *out = p.bs + (size_t)cur * kBsBytes;
+    uint32_t mystop = 0xFFFFFFFFu;
+    // Internal edges join two 4x4 blocks of the same MB (never a
+    // mixed edge), so their strength is uniform over the 4 lines of a
+    // block pair as in frame pictures: lanes 0..23 derive them
+    // (dir, edge 1..3, block), and 4:2:0 chroma takes the luma value of
+    // edge 8 at luma line 2k.  The MB edges (left, top, second top of a
+    // frame MB under a field pair) are derived per line.
+    uint32_t ivrow = 0, ihrow = 0;  // lane k < 16: internal strengths of line / column k, byte e
+    {
+        int bs = 0, dir = 0, ei = 1, b = 0;
+        if (lane < 24) {
+            dir = lane / 12;
+            ei = 1 + (lane % 12) / 4;
+            b = lane & 3;
+            if (c.internal && (ei == 2 || !c.t8))
+                bs = dir == 0 ? edge_bs(p, cur, 0, 1, 4 * ei, c.mbA, 0, 4 * b) : edge_bs(p, cur, 0, 0, 4 * ei, c.mbB, 0, 4 * b);
+            if (bs == 0xFF) mystop = min(mystop, stop_key(cur, dir == 0 ? SEQ_LV0 + ei : SEQ_LH4 + ei - 1, 4 * b));
+        }
+        const int k = lane & 15;
+#pragma unroll
+        for (int e2 = 1; e2 < 4; e2++) {
+            ivrow |= (uint32_t)(__shfl_sync(0xffffffffu, bs, (e2 - 1) * 4 + (k >> 2)) & 255) << (8 * e2);
+            ihrow |= (uint32_t)(__shfl_sync(0xffffffffu, bs, 12 + (e2 - 1) * 4 + (k >> 2)) & 255) << (8 * e2);
+        }
+    }
+    // MB edges per line: left (0..15), top (16..31), second top (32..47) luma;
+    // chroma left (48..55), top (56..63), second top (64..71)
+    uint32_t lv0 = 0, lh0 = 0;  // lane k < 16: luma left / top strength of line / column k
+    for (int it = lane; it < 72; it += 32) {
+        int bs = 0, seq = 0, k = 0;
+        if (it < 16) {
+            k = it;
+            if (c.left) bs = edge_bs(p, cur, 0, 1, 0, c.mbA, c.leftMixed, k);
+            seq = SEQ_LV0;
+            lv0 = (uint32_t)bs;
+        } else if (it < 32) {
+            k = it - 16;
+            if (c.top) bs = c.topDouble ? edge_bs(p, cur, 0, 0, 0, c.mbB - 1, 0, k) : edge_bs(p, cur, 0, 0, 0, c.mbB, 0, k);
+            seq = SEQ_LH0;
+        } else if (it < 48) {
+            k = it - 32;
+            if (c.top && c.topDouble) bs = edge_bs(p, cur, 0, 0, 1, c.mbB, 0, k);
+            seq = SEQ_LH0B;
+            out[kBsLumaTop2 + k] = (uint8_t)bs;
+        } else if (it < 56) {
+            k = it - 48;
+            if (c.left) bs = edge_bs(p, cur, 1, 1, 0, c.mbA, c.leftMixed, k);
+            seq = SEQ_CBV0;
+            out[bs_cv(0, k)] = (uint8_t)bs;
+        } else if (it < 64) {
+            k = it - 56;
+            if (c.top) bs = edge_bs(p, cur, 1, 0, 0, c.mbB, 0, k);
+            seq = SEQ_CBH0;
+            out[bs_ch(0, k)] = (uint8_t)bs;
+        } else {
+            k = it - 64;
+            if (c.top && c.topDouble) bs = edge_bs(p, cur, 1, 0, 1, c.mbB, 0, k);
+            seq = SEQ_CBH0B;
+            out[kBsChromaTop2 + k] = (uint8_t)bs;
+        }
+        if (it >= 16 && it < 32) lh0 = (uint32_t)bs;
+        if (bs == 0xFF) mystop = min(mystop, stop_key(cur, seq, k));
+    }
+    // lanes 16..31 derived the top edge of column lane-16 in their first item
+    lh0 = __shfl_sync(0xffffffffu, lh0, (lane & 15) + 16);
+    if (lane < 16) {
+        *(uint32_t *)(out + bs_lv(0, lane)) = ivrow | (lv0 & 255);
+        *(uint32_t *)(out + bs_lh(0, lane)) = ihrow | (lh0 & 255);
+    }
+    // chroma internal edge (4): luma edge 8 at luma line / column 2k
+    const int ck = lane & 7;
+    const uint32_t civ = __shfl_sync(0xffffffffu, (ivrow >> 16) & 255, 2 * ck);
+    const uint32_t cih = __shfl_sync(0xffffffffu, (ihrow >> 16) & 255, 2 * ck);
+    if (lane < 8) out[bs_cv(1, ck)] = (uint8_t)civ;
+    else if (lane < 16) out[bs_ch(1, ck)] = (uint8_t)cih;
+    // the edge controls of the MB and the thresholds of its edges, so that
+    // the deblocking wavefront reads no records
+    if (lane < 16) {
         uint32_t w;
         if (lane == 15) {
             w = (c.left ? kDbcLeft : 0u) | (c.top ? kDbcTop : 0u) | (c.internal ? kDbcInternal : 0u) | (c.t8 ? kDbcT8 : 0u) |
@@ -1545,6 +1606,27 @@ __global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, in
     }
     for (int o = 16; o > 0; o >>= 1) mystop = min(mystop, __shfl_xor_sync(0xffffffffu, mystop, o));
     if (lane == 0 && mystop != 0xFFFFFFFFu) atomicMin(&pp->deblock_stop, mystop);
+}
+
+// Boundary strengths of a batch: warp w takes MBs 2w and 2w + 1 (4 warps,
+// 8 MBs per block); frame and field pictures a half-warp per MB, MBAFF
+// pictures the whole warp per MB, one after the other.
+__global__ void __launch_bounds__(128) k_bs(const PicDesc *__restrict__ pics, int npics, uint32_t total_mbs, LaunchState st)
+{
+    const uint32_t w = blockIdx.x * 4 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (2 * w >= total_mbs) return;
+    const uint32_t g = 2 * w + (lane >> 4);
+    const bool in = g < total_mbs;
+    const int pi = find_pic_by_mb(pics, npics, in ? g : 2 * w);
+    const bool frame = in && !pics[pi].mbaff && pics[pi].deblock;
+    if (__any_sync(0xffffffffu, frame)) bs_frame_half(pics, pi, g, frame);
+    for (int h = 0; h < 2; h++) {
+        const int ph = __shfl_sync(0xffffffffu, pi, 16 * h);
+        const bool inh = __shfl_sync(0xffffffffu, in, 16 * h);
+        if (inh && pics[ph].mbaff && pics[ph].deblock)
+            bs_mbaff_mb(pics[ph], const_cast<PicDesc *>(&pics[ph]), (int)(2 * w + h - pics[ph].mb_base));
+    }
 }
 
 // ======================================================================

@@ -140,7 +140,7 @@ extern "C" int h264r_deblock_picture_noalloc(const h264r_picture *pic, uint8_t *
     if (cudaPeekAtLastError() != cudaSuccess) return H264R_ERR_CUDA;
     k_noalloc_init<<<1, 256, 0, cs>>>(d, s);
     if (cudaGetLastError() != cudaSuccess) return H264R_ERR_CUDA;
-    h264r::k_bs<<<(pic->num_mbs + 3) / 4, 128, 0, cs>>>(&s->desc, 1, pic->num_mbs, st);
+    h264r::k_bs<<<(pic->num_mbs + h264r::kBsMbsPerBlock - 1) / h264r::kBsMbsPerBlock, 128, 0, cs>>>(&s->desc, 1, pic->num_mbs, st);
     if (cudaGetLastError() != cudaSuccess) return H264R_ERR_CUDA;
     if (d.dbf_units) {
         h264r::k_deblock_frame<<<d.dbf_units, 32 * h264r::kDbWarps, 0, cs>>>(&s->desc, 1, d.dbf_units, st);
