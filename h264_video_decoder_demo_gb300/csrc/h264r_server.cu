@@ -11,9 +11,12 @@
 //   flight  launched in a batch; done when the event recorded after its
 //           launch (and its output copy) completes
 // Each pass of the scheduler admits waiting streams whose DPB fits the
-// budget, retires finished pictures, uploads queued records, and launches
-// one batch with the next dependency group of every stream that has one
-// uploaded: continuous batching, with at most three batches in flight.
+// budget, retires finished pictures, uploads queued records, and launches,
+// in each lane, one batch with the next dependency group of every stream of
+// the lane that has one uploaded: continuous batching.  The streams are
+// split into lanes by id; a batch waits for the earlier work of its
+// streams, so the batches of one lane follow each other while the lanes'
+// batches run side by side (at most two in flight per lane).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,8 +35,10 @@
 namespace {
 
 constexpr uint64_t kAlign = 256;
-constexpr int kMaxBatchesInFlight = 3;
-constexpr int kMaxGroupsInFlight = 2;  // per stream
+constexpr int kLanes = 3;               // default batch chains over disjoint stream sets
+constexpr int kMaxLanes = 8;
+constexpr int kMaxBatchesInFlight = 2;  // per lane
+constexpr int kMaxGroupsInFlight = 2;   // per stream
 
 uint64_t align_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
 
@@ -97,7 +102,7 @@ struct h264r_server {
     h264r_ctx *ctx = nullptr;
     int device = 0;
     uint64_t budget = 0;
-    int max_batch = 64, depth = 4;
+    int max_batch = 64, depth = 4, lanes = kLanes;
     std::mutex mu;
     std::condition_variable wake, done_cv;
     std::map<int, SStream *> streams;
@@ -105,7 +110,7 @@ struct h264r_server {
     std::deque<h264r_server_done> done_q;
     std::vector<double> lat;
     h264r_server_stats st{};
-    std::deque<cudaEvent_t> batch_done;
+    std::deque<cudaEvent_t> batch_done[kMaxLanes];
     std::vector<cudaEvent_t> ev_pool;
     cudaStream_t up = nullptr;
     std::thread th;
@@ -243,9 +248,11 @@ bool admit(h264r_server *srv)
 bool retire(h264r_server *srv)
 {
     bool progress = false;
-    while (!srv->batch_done.empty() && cudaEventQuery(srv->batch_done.front()) == cudaSuccess) {
-        give_event(srv, srv->batch_done.front());
-        srv->batch_done.pop_front();
+    for (auto &q : srv->batch_done) {
+        while (!q.empty() && cudaEventQuery(q.front()) == cudaSuccess) {
+            give_event(srv, q.front());
+            q.pop_front();
+        }
     }
     for (auto &kv : srv->streams) {
         SStream *S = kv.second;
@@ -321,12 +328,14 @@ bool upload(h264r_server *srv)
     return progress;
 }
 
-bool launch(h264r_server *srv)
+bool launch_lane(h264r_server *srv, int lane)
 {
-    if ((int)srv->batch_done.size() >= kMaxBatchesInFlight) return false;
+    if ((int)srv->batch_done[lane].size() >= kMaxBatchesInFlight) return false;
     std::vector<SStream *> order;
     for (auto &kv : srv->streams)
-        if (kv.second->admitted && !kv.second->finished && !kv.second->status && !kv.second->dev_q.empty()) order.push_back(kv.second);
+        if (kv.first % srv->lanes == lane && kv.second->admitted && !kv.second->finished && !kv.second->status &&
+            !kv.second->dev_q.empty())
+            order.push_back(kv.second);
     if (order.empty()) return false;
     // round robin over the streams so that a full batch does not always
     // leave out the same ones
@@ -379,10 +388,17 @@ bool launch(h264r_server *srv)
     }
     cudaEvent_t be = take_event(srv);
     cudaEventRecord(be, (cudaStream_t)h264r_stream_cuda_stream(ss[0]));
-    srv->batch_done.push_back(be);
+    srv->batch_done[lane].push_back(be);
     srv->st.batches++;
     srv->st.batch_pictures += pics.size();
     return true;
+}
+
+bool launch(h264r_server *srv)
+{
+    bool progress = false;
+    for (int lane = 0; lane < srv->lanes; lane++) progress = launch_lane(srv, lane) || progress;
+    return progress;
 }
 
 void scheduler(h264r_server *srv)
@@ -417,6 +433,7 @@ extern "C" int h264r_server_create(h264r_ctx *ctx, const h264r_server_cfg *cfg, 
     const int ctx_batch = h264r_ctx_max_batch(ctx);
     srv->max_batch = (cfg && cfg->max_batch_pictures) ? (int)std::min<uint32_t>(cfg->max_batch_pictures, ctx_batch) : ctx_batch;
     srv->depth = (cfg && cfg->queue_depth) ? (int)std::min<uint32_t>(cfg->queue_depth, 32) : 4;
+    srv->lanes = (cfg && cfg->lanes) ? (int)std::min<uint32_t>(cfg->lanes, kMaxLanes) : kLanes;
     cudaSetDevice(srv->device);
     if (cudaStreamCreateWithFlags(&srv->up, cudaStreamNonBlocking) != cudaSuccess) {
         delete srv;
@@ -439,7 +456,8 @@ extern "C" int h264r_server_destroy(h264r_server *srv)
     srv->th.join();
     cudaSetDevice(srv->device);
     for (auto &kv : srv->streams) delete kv.second;
-    for (auto e : srv->batch_done) cudaEventDestroy(e);
+    for (auto &q : srv->batch_done)
+        for (auto e : q) cudaEventDestroy(e);
     for (auto e : srv->ev_pool) cudaEventDestroy(e);
     for (auto &kv : srv->pool) cudaFreeHost(kv.second);
     cudaStreamDestroy(srv->up);

@@ -620,10 +620,10 @@ class Server:
     are admitted by the context's DPB budget, pictures pushed as their records
     are complete, finished pictures polled with their latency."""
 
-    def __init__(self, ctx, max_batch=0, queue_depth=0):
+    def __init__(self, ctx, max_batch=0, queue_depth=0, lanes=0):
         self.ctx = ctx
         h = ctypes.c_void_p()
-        cfg = R.CServerCfg(max_batch, queue_depth, 0, 0)
+        cfg = R.CServerCfg(max_batch, queue_depth, 0, lanes)
         ctx.check(lib().h264r_server_create(ctx.h, ctypes.byref(cfg), ctypes.byref(h)), "server_create")
         self.h = h
         self._keep = {}

@@ -213,7 +213,7 @@ class CWriterCfg(ctypes.Structure):
 class CServerCfg(ctypes.Structure):
     """struct h264r_server_cfg (include/h264r_server.h)"""
     _fields_ = [("max_batch_pictures", ctypes.c_uint32), ("queue_depth", ctypes.c_uint32),
-                ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32), ("lanes", ctypes.c_uint32)]
 
 
 class CServerDone(ctypes.Structure):

@@ -38,7 +38,8 @@ typedef struct h264r_server_cfg {
     uint32_t queue_depth;        /* pictures a stream may hold in device memory
                                     (uploaded or in flight), 0: 4             */
     uint32_t flags;              /* reserved, 0                               */
-    uint32_t reserved;
+    uint32_t lanes;              /* batch chains over disjoint stream sets
+                                    (streams split by id; 0: 3, at most 8)    */
 } h264r_server_cfg;
 
 /* One finished picture. */
