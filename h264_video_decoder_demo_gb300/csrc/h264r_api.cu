@@ -186,6 +186,10 @@ struct h264r_ctx {
     // host-submitted batches upload their records here, so that a batch's
     // upload overlaps the kernels of the batch before it on the same pipeline
     cudaStream_t upload_stream = nullptr;
+    // picture buffers of the streams: stream-ordered allocations from a pool
+    // that keeps up to the DPB budget for reuse, so that opening and closing
+    // a stream (a served request) does not wait for the device
+    cudaMemPool_t dpb_pool = nullptr;
     // launch shapes: the default and the autotuner's choice per geometry mix
     std::mutex tune_mu;
     h264r_tuning tuning{4, 8, 0, 0};
@@ -206,6 +210,8 @@ struct h264r_stream {
     h264r_stream_cfg cfg{};
     uint64_t slot_bytes = 0;
     uint8_t *dpb = nullptr;
+    bool pooled = false;        // dpb from the context's pool, cleared on cs
+    bool clear_synced = false;  // h264r_slot_device_ptr waited for that clear
     cudaStream_t cs = nullptr;
     cudaStream_t side = nullptr;  // boundary strengths of launches on cs, beside inter and intra
     // h264r_output_async: copies to the host on their own stream; a launch
@@ -285,6 +291,20 @@ extern "C" int h264r_ctx_create(const h264r_cfg *cfg, h264r_ctx **out)
         return H264R_ERR_CUDA;
     }
     for (auto &b : ctx->batch_ring) create_events(b);
+    {
+        cudaMemPoolProps pp = {};
+        pp.allocType = cudaMemAllocationTypePinned;
+        pp.handleTypes = cudaMemHandleTypeNone;
+        pp.location.type = cudaMemLocationTypeDevice;
+        pp.location.id = ctx->device;
+        if (cudaMemPoolCreate(&ctx->dpb_pool, &pp) == cudaSuccess) {
+            uint64_t keep = ctx->budget;
+            cudaMemPoolSetAttribute(ctx->dpb_pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        } else {
+            ctx->dpb_pool = nullptr;  // plain allocations then
+            cudaGetLastError();
+        }
+    }
     *ctx->h_error = 0;
     const unsigned hw = std::thread::hardware_concurrency();
     ctx->pool.reset(new (std::nothrow) WorkerPool(hw > 2 ? (int)std::min(hw - 1u, 15u) : 0));
@@ -325,6 +345,7 @@ extern "C" int h264r_ctx_destroy(h264r_ctx *ctx)
             for (auto e : q) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->batch_stream);
     if (ctx->upload_stream) cudaStreamDestroy(ctx->upload_stream);
+    if (ctx->dpb_pool) cudaMemPoolDestroy(ctx->dpb_pool);
     cudaFree(ctx->d_error);
     cudaFreeHost(ctx->h_error);
     delete ctx;
@@ -444,25 +465,51 @@ extern "C" int h264r_stream_open(h264r_ctx *ctx, const h264r_stream_cfg *cfg, h2
     s->cfg = *cfg;
     s->slot_bytes = slot_bytes_of(*cfg);
     cudaSetDevice(ctx->device);
-    if (cudaMalloc(&s->dpb, bytes) != cudaSuccess) {
-        set_err(ctx, "h264r_stream_open: cudaMalloc(%llu) failed", (unsigned long long)bytes);
-        delete s;
-        return H264R_ERR_NO_MEMORY;
-    }
-    // the reference starts every picture buffer cleared (H264PictureBase.cpp:162-181)
-    cudaMemset(s->dpb, 0, bytes);
     cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking);
     cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
     cudaStreamCreateWithFlags(&s->out, cudaStreamNonBlocking);
+    // the reference starts every picture buffer cleared (H264PictureBase.cpp:162-181).
+    // From the pool: allocated and cleared in the order of cs, which every
+    // launch and copy touching the stream's slots follows (a batch waits for
+    // the work queued on each of its streams).
+    s->pooled = ctx->dpb_pool && cudaMallocFromPoolAsync((void **)&s->dpb, bytes, ctx->dpb_pool, s->cs) == cudaSuccess &&
+                cudaMemsetAsync(s->dpb, 0, bytes, s->cs) == cudaSuccess;
+    if (!s->pooled) {
+        if (s->dpb) cudaFreeAsync(s->dpb, s->cs);
+        s->dpb = nullptr;
+        cudaGetLastError();
+        if (cudaMalloc(&s->dpb, bytes) != cudaSuccess) {
+            set_err(ctx, "h264r_stream_open: cudaMalloc(%llu) failed", (unsigned long long)bytes);
+            cudaStreamDestroy(s->cs);
+            cudaStreamDestroy(s->side);
+            cudaStreamDestroy(s->out);
+            delete s;
+            return H264R_ERR_NO_MEMORY;
+        }
+        cudaMemset(s->dpb, 0, bytes);
+    }
     cudaEventCreateWithFlags(&s->out_ready, cudaEventDisableTiming);
     s->slot_ev.resize(cfg->dpb_slots);
     for (auto &e : s->slot_ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     s->slot_pending.reset(new std::atomic<uint8_t>[cfg->dpb_slots]);
     for (int i = 0; i < cfg->dpb_slots; i++) s->slot_pending[i] = 0;
     for (auto &b : s->ring) create_events(b);
-    cudaDeviceSynchronize();
+    if (!s->pooled) cudaDeviceSynchronize();  // the legacy-stream clear before any use
+    s->clear_synced = !s->pooled;
     ctx->used += bytes;
     *out = s;
+    return H264R_OK;
+}
+
+extern "C" int h264r_stream_reset(h264r_stream *s)
+{
+    if (!s) return H264R_ERR_INVALID_ARG;
+    h264r_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    CUDA_OR(ctx, cudaStreamSynchronize(s->out));
+    for (int i = 0; i < s->cfg.dpb_slots; i++) s->slot_pending[i] = 0;
+    CUDA_OR(ctx, cudaMemsetAsync(s->dpb, 0, h264r_stream_dpb_bytes(&s->cfg), s->cs));
+    s->clear_synced = false;
     return H264R_OK;
 }
 
@@ -478,10 +525,11 @@ extern "C" int h264r_stream_close(h264r_stream *s)
     cudaStreamSynchronize(s->out);
     for (auto e : s->slot_ev) cudaEventDestroy(e);
     cudaEventDestroy(s->out_ready);
+    if (s->pooled) cudaFreeAsync(s->dpb, s->cs);  // back to the pool once cs is done
     cudaStreamDestroy(s->cs);
     cudaStreamDestroy(s->side);
     cudaStreamDestroy(s->out);
-    cudaFree(s->dpb);
+    if (!s->pooled) cudaFree(s->dpb);
     {
         std::lock_guard<std::mutex> lk(ctx->mu);
         ctx->used -= h264r_stream_dpb_bytes(&s->cfg);
@@ -498,6 +546,13 @@ extern "C" void *h264r_ctx_cuda_stream(h264r_ctx *ctx) { return ctx ? (void *)ct
 extern "C" int h264r_slot_device_ptr(h264r_stream *s, int slot, void **dev_y)
 {
     if (!s || !dev_y || slot < 0 || slot >= s->cfg.dpb_slots) return H264R_ERR_INVALID_ARG;
+    // the caller may use the slot on a stream of its own: the clear queued on
+    // cs at open must be done first
+    if (!s->clear_synced) {
+        cudaSetDevice(s->ctx->device);
+        cudaStreamSynchronize(s->cs);
+        s->clear_synced = true;
+    }
     *dev_y = s->dpb + (uint64_t)slot * s->slot_bytes;
     return H264R_OK;
 }
@@ -1338,9 +1393,13 @@ extern "C" int h264r_output_async(h264r_stream *s, int slot, uint8_t *y, uint8_t
     // after everything enqueued on the stream so far (the picture's batch)
     CUDA_OR(ctx, cudaEventRecord(s->out_ready, s->cs));
     CUDA_OR(ctx, cudaStreamWaitEvent(s->out, s->out_ready, 0));
-    CUDA_OR(ctx, cudaMemcpyAsync(y, base, W * H, cudaMemcpyDeviceToHost, s->out));
-    CUDA_OR(ctx, cudaMemcpyAsync(cb, base + W * H, W * H / 4, cudaMemcpyDeviceToHost, s->out));
-    CUDA_OR(ctx, cudaMemcpyAsync(cr, base + W * H + W * H / 4, W * H / 4, cudaMemcpyDeviceToHost, s->out));
+    if (cb == y + W * H && cr == cb + W * H / 4) {  // one buffer: one copy (the slot's planes follow each other too)
+        CUDA_OR(ctx, cudaMemcpyAsync(y, base, W * H * 3 / 2, cudaMemcpyDeviceToHost, s->out));
+    } else {
+        CUDA_OR(ctx, cudaMemcpyAsync(y, base, W * H, cudaMemcpyDeviceToHost, s->out));
+        CUDA_OR(ctx, cudaMemcpyAsync(cb, base + W * H, W * H / 4, cudaMemcpyDeviceToHost, s->out));
+        CUDA_OR(ctx, cudaMemcpyAsync(cr, base + W * H + W * H / 4, W * H / 4, cudaMemcpyDeviceToHost, s->out));
+    }
     CUDA_OR(ctx, cudaEventRecord(s->slot_ev[slot], s->out));
     s->slot_pending[slot] = 1;
     return H264R_OK;

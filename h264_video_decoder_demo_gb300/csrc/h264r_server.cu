@@ -39,6 +39,7 @@ constexpr int kLanes = 3;               // default batch chains over disjoint st
 constexpr int kMaxLanes = 8;
 constexpr int kMaxBatchesInFlight = 2;  // per lane
 constexpr int kMaxGroupsInFlight = 2;   // per stream
+constexpr size_t kIdleMax = 64;         // engine streams kept for reuse
 
 uint64_t align_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
 
@@ -81,6 +82,7 @@ struct SStream {
     bool admitted = false, ended = false, finished = false;
     int status = 0;
     int pending = 0;  // pushed, not yet polled
+    bool check = false;  // a batch of the stream completed: its finished pictures are looked for
     std::deque<Item *> host_q, dev_q, flight;
     std::vector<Slot> slots;
     int groups_in_flight() const
@@ -106,13 +108,26 @@ struct h264r_server {
     std::mutex mu;
     std::condition_variable wake, done_cv;
     std::map<int, SStream *> streams;
+    std::vector<SStream *> active;  // admitted and not finished: what a scheduler pass visits
+    // engine streams of finished requests by geometry, reused (reset) for the
+    // next request of the same geometry instead of a close and an open
+    std::multimap<uint64_t, h264r_stream *> idle;
     std::deque<SStream *> waiting;
     std::deque<h264r_server_done> done_q;
     std::vector<double> lat;
     h264r_server_stats st{};
-    std::deque<cudaEvent_t> batch_done[kMaxLanes];
+    // per lane, the batches in flight: the event after each and its streams
+    struct Batch {
+        cudaEvent_t done = nullptr;
+        std::vector<SStream *> members;
+    };
+    std::deque<Batch> batch_done[kMaxLanes];
     std::vector<cudaEvent_t> ev_pool;
     cudaStream_t up = nullptr;
+    // device slots for uploaded records: stream-ordered allocations on `up`
+    // from a pool of the server's own, so that a stream's slots come and go
+    // without waiting for the device (nullptr: plain allocations)
+    cudaMemPool_t rec_pool = nullptr;
     std::thread th;
     // pinned buffers for packed records: push packs each picture straight
     // into one (on the caller's thread), the scheduler only enqueues its H2D
@@ -162,6 +177,27 @@ Pinned take_pinned(h264r_server *srv, uint64_t need)
     return p;
 }
 
+// device memory of a record slot, and its release once nothing reads it
+uint8_t *slot_alloc(h264r_server *srv, uint64_t bytes)
+{
+    void *p = nullptr;
+    if (srv->rec_pool) {
+        if (cudaMallocFromPoolAsync(&p, bytes, srv->rec_pool, srv->up) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return (uint8_t *)p;
+    }
+    return cudaMalloc(&p, bytes) == cudaSuccess ? (uint8_t *)p : nullptr;
+}
+
+void slot_free(h264r_server *srv, uint8_t *p)
+{
+    if (!p) return;
+    if (srv->rec_pool) cudaFreeAsync(p, srv->up);
+    else cudaFree(p);
+}
+
 void give_pinned(h264r_server *srv, Pinned &p)
 {
     if (!p.ptr) return;
@@ -202,18 +238,26 @@ void fail_stream(h264r_server *srv, SStream *S, int status)
     }
 }
 
+uint64_t geometry_key(const h264r_stream_cfg &c)
+{
+    return ((uint64_t)c.width_mbs << 32) | ((uint64_t)c.height_mbs << 16) | c.dpb_slots;
+}
+
 void close_stream(h264r_server *srv, SStream *S)
 {
     if (S->s) {
-        const int rc = h264r_stream_sync(S->s);  // device errors of its last work
-        if (rc && !S->status) S->status = rc;
-        h264r_stream_close(S->s);
+        // Every picture of the stream has been reported: its work is done (no
+        // h264r_stream_sync here, whose read of the context's error word
+        // queues behind the output copies of all the other streams).  The
+        // engine stream is kept for the next request of its geometry.
+        if (!S->status && srv->idle.size() < kIdleMax) srv->idle.emplace(geometry_key(S->cfg), S->s);
+        else h264r_stream_close(S->s);
         S->s = nullptr;
         srv->st.dpb_bytes_in_use -= S->dpb;
         srv->st.streams_open--;
     }
-    for (auto &sl : S->slots) {
-        if (sl.dev) cudaFree(sl.dev);
+    for (auto &sl : S->slots) {  // no batch reads them any more (the stream is synchronised)
+        slot_free(srv, sl.dev);
         sl = Slot();
     }
     S->finished = true;
@@ -225,7 +269,25 @@ bool admit(h264r_server *srv)
     bool progress = false;
     while (!srv->waiting.empty()) {
         SStream *S = srv->waiting.front();
-        int rc = h264r_stream_open(srv->ctx, &S->cfg, &S->s);
+        int rc = H264R_ERR_BUDGET;
+        auto f = srv->idle.find(geometry_key(S->cfg));
+        if (f != srv->idle.end()) {
+            S->s = f->second;
+            srv->idle.erase(f);
+            rc = h264r_stream_reset(S->s);
+            if (rc != H264R_OK) {
+                h264r_stream_close(S->s);
+                S->s = nullptr;
+            }
+        }
+        if (!S->s) {
+            rc = h264r_stream_open(srv->ctx, &S->cfg, &S->s);
+            while (rc == H264R_ERR_BUDGET && !srv->idle.empty()) {  // idle streams give their DPBs back
+                h264r_stream_close(srv->idle.begin()->second);
+                srv->idle.erase(srv->idle.begin());
+                rc = h264r_stream_open(srv->ctx, &S->cfg, &S->s);
+            }
+        }
         if (rc == H264R_ERR_BUDGET) break;  // wait for finished streams to free their DPBs
         srv->waiting.pop_front();
         srv->st.streams_waiting--;
@@ -238,6 +300,7 @@ bool admit(h264r_server *srv)
         }
         S->admitted = true;
         S->slots.resize(srv->depth);
+        srv->active.push_back(S);
         srv->st.streams_open++;
         srv->st.dpb_bytes_in_use += S->dpb;
         srv->st.dpb_bytes_peak = std::max(srv->st.dpb_bytes_peak, srv->st.dpb_bytes_in_use);
@@ -248,19 +311,26 @@ bool admit(h264r_server *srv)
 bool retire(h264r_server *srv)
 {
     bool progress = false;
+    // a picture finishes after its batch: only the streams of completed
+    // batches are looked at (one event query per lane otherwise)
     for (auto &q : srv->batch_done) {
-        while (!q.empty() && cudaEventQuery(q.front()) == cudaSuccess) {
-            give_event(srv, q.front());
+        while (!q.empty() && cudaEventQuery(q.front().done) == cudaSuccess) {
+            for (SStream *S : q.front().members) S->check = true;
+            give_event(srv, q.front().done);
             q.pop_front();
         }
     }
-    for (auto &kv : srv->streams) {
-        SStream *S = kv.second;
-        if (!S->admitted || S->finished) continue;
+    for (SStream *S : srv->active) {
+        if (S->finished) continue;
+        if (!S->check && !(S->ended && S->flight.empty())) continue;
+        S->check = false;
         while (!S->flight.empty() && !S->status) {
             Item *it = S->flight.front();
             cudaError_t e = cudaEventQuery(it->done);
-            if (e == cudaErrorNotReady) break;
+            if (e == cudaErrorNotReady) {
+                S->check = true;  // its output copy is still running
+                break;
+            }
             S->flight.pop_front();
             const int status = e == cudaSuccess ? H264R_OK : H264R_ERR_CUDA;
             report(srv, S, it, status);
@@ -275,15 +345,16 @@ bool retire(h264r_server *srv)
             progress = true;
         }
     }
+    srv->active.erase(std::remove_if(srv->active.begin(), srv->active.end(), [](const SStream *S) { return S->finished; }),
+                      srv->active.end());
     return progress;
 }
 
 bool upload(h264r_server *srv)
 {
     bool progress = false;
-    for (auto &kv : srv->streams) {
-        SStream *S = kv.second;
-        if (!S->admitted || S->finished || S->status) continue;
+    for (SStream *S : srv->active) {
+        if (S->finished || S->status) continue;
         while (!S->host_q.empty()) {
             int k = -1;
             for (int i = 0; i < (int)S->slots.size(); i++)
@@ -293,10 +364,10 @@ bool upload(h264r_server *srv)
             Slot &sl = S->slots[k];
             const uint64_t need = it->size;
             if (sl.cap < need) {
-                if (sl.dev) cudaFree(sl.dev);
+                slot_free(srv, sl.dev);  // a free slot: the batch that read it has completed
                 sl = Slot();
                 const uint64_t cap = align_up(need + need / 8, 1 << 16);
-                if (cudaMalloc(&sl.dev, cap) != cudaSuccess) {
+                if (!(sl.dev = slot_alloc(srv, cap))) {
                     sl = Slot();
                     fail_stream(srv, S, H264R_ERR_NO_MEMORY);
                     progress = true;
@@ -328,14 +399,16 @@ bool upload(h264r_server *srv)
     return progress;
 }
 
-bool launch_lane(h264r_server *srv, int lane)
+// The device queues (dev_q, flight), the slots and the engine streams are
+// the scheduler thread's alone; the server lock (held on entry, as `lk`) is
+// released while the batch is submitted and its output copies are queued,
+// so that pushes and polls do not wait for the engine calls.
+bool launch_lane(h264r_server *srv, int lane, std::unique_lock<std::mutex> &lk)
 {
     if ((int)srv->batch_done[lane].size() >= kMaxBatchesInFlight) return false;
     std::vector<SStream *> order;
-    for (auto &kv : srv->streams)
-        if (kv.first % srv->lanes == lane && kv.second->admitted && !kv.second->finished && !kv.second->status &&
-            !kv.second->dev_q.empty())
-            order.push_back(kv.second);
+    for (SStream *S : srv->active)
+        if (S->id % srv->lanes == lane && !S->finished && !S->status && !S->dev_q.empty()) order.push_back(S);
     if (order.empty()) return false;
     // round robin over the streams so that a full batch does not always
     // leave out the same ones
@@ -357,6 +430,7 @@ bool launch_lane(h264r_server *srv, int lane)
         if ((int)pics.size() >= srv->max_batch) break;
     }
     if (pics.empty()) return false;
+    lk.unlock();
     // the records must be on the device before the batch reads them
     for (auto &pr : items)
         cudaStreamWaitEvent((cudaStream_t)h264r_stream_cuda_stream(pr.first->s), pr.second->uploaded, 0);
@@ -381,23 +455,31 @@ bool launch_lane(h264r_server *srv, int lane)
         cudaEventRecord(it->done, cs);
         S->flight.push_back(it);
     }
+    cudaEvent_t be = nullptr;
+    if (rc == H264R_OK) {
+        be = take_event(srv);
+        cudaEventRecord(be, (cudaStream_t)h264r_stream_cuda_stream(ss[0]));
+    }
+    lk.lock();
     if (rc != H264R_OK) {
         for (auto &pr : items)
             if (!pr.first->flight.empty()) fail_stream(srv, pr.first, rc);
         return true;
     }
-    cudaEvent_t be = take_event(srv);
-    cudaEventRecord(be, (cudaStream_t)h264r_stream_cuda_stream(ss[0]));
-    srv->batch_done[lane].push_back(be);
+    h264r_server::Batch bt;
+    bt.done = be;
+    for (auto &pr : items)
+        if (bt.members.empty() || bt.members.back() != pr.first) bt.members.push_back(pr.first);
+    srv->batch_done[lane].push_back(std::move(bt));
     srv->st.batches++;
     srv->st.batch_pictures += pics.size();
     return true;
 }
 
-bool launch(h264r_server *srv)
+bool launch(h264r_server *srv, std::unique_lock<std::mutex> &lk)
 {
     bool progress = false;
-    for (int lane = 0; lane < srv->lanes; lane++) progress = launch_lane(srv, lane) || progress;
+    for (int lane = 0; lane < srv->lanes; lane++) progress = launch_lane(srv, lane, lk) || progress;
     return progress;
 }
 
@@ -409,12 +491,8 @@ void scheduler(h264r_server *srv)
         bool progress = admit(srv);
         progress = retire(srv) || progress;
         progress = upload(srv) || progress;
-        progress = launch(srv) || progress;
-        if (srv->stop && srv->waiting.empty()) {
-            bool all = true;
-            for (auto &kv : srv->streams) all = all && kv.second->finished;
-            if (all) break;
-        }
+        progress = launch(srv, lk) || progress;
+        if (srv->stop && srv->waiting.empty() && srv->active.empty()) break;
         if (!progress) srv->wake.wait_for(lk, std::chrono::microseconds(50));
     }
 }
@@ -439,6 +517,18 @@ extern "C" int h264r_server_create(h264r_ctx *ctx, const h264r_server_cfg *cfg, 
         delete srv;
         return H264R_ERR_CUDA;
     }
+    cudaMemPoolProps pp = {};
+    pp.allocType = cudaMemAllocationTypePinned;
+    pp.handleTypes = cudaMemHandleTypeNone;
+    pp.location.type = cudaMemLocationTypeDevice;
+    pp.location.id = srv->device;
+    if (cudaMemPoolCreate(&srv->rec_pool, &pp) == cudaSuccess) {
+        uint64_t keep = ~0ull;  // freed slots stay in the pool for the next streams
+        cudaMemPoolSetAttribute(srv->rec_pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    } else {
+        srv->rec_pool = nullptr;
+        cudaGetLastError();
+    }
     srv->th = std::thread(scheduler, srv);
     *out = srv;
     return H264R_OK;
@@ -456,10 +546,13 @@ extern "C" int h264r_server_destroy(h264r_server *srv)
     srv->th.join();
     cudaSetDevice(srv->device);
     for (auto &kv : srv->streams) delete kv.second;
+    for (auto &kv : srv->idle) h264r_stream_close(kv.second);
     for (auto &q : srv->batch_done)
-        for (auto e : q) cudaEventDestroy(e);
+        for (auto &b : q) cudaEventDestroy(b.done);
     for (auto e : srv->ev_pool) cudaEventDestroy(e);
     for (auto &kv : srv->pool) cudaFreeHost(kv.second);
+    cudaStreamSynchronize(srv->up);
+    if (srv->rec_pool) cudaMemPoolDestroy(srv->rec_pool);
     cudaStreamDestroy(srv->up);
     delete srv;
     return H264R_OK;

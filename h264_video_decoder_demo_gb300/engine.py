@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libh264r.so
 # h264r_decoder.h declare
 EXPORTS = [
     "h264r_ctx_create", "h264r_ctx_destroy", "h264r_last_error", "h264r_stream_open",
-    "h264r_stream_close", "h264r_stream_dpb_bytes", "h264r_submit_picture",
+    "h264r_stream_close", "h264r_stream_reset", "h264r_stream_dpb_bytes", "h264r_submit_picture",
     "h264r_submit_picture_device", "h264r_submit_batch_device", "h264r_output", "h264r_output_async",
     "h264r_load_slot", "h264r_slot_device_ptr", "h264r_stream_sync", "h264r_ctx_sync",
     "h264r_stream_cuda_stream", "h264r_stream_output_cuda_stream", "h264r_validate_picture", "h264r_ctx_kernel_launches",
@@ -77,6 +77,7 @@ def _load():
         "h264r_last_error": (ctypes.c_char_p, [vp]),
         "h264r_stream_open": (i32, [vp, P(R.CStreamCfg), P(vp)]),
         "h264r_stream_close": (i32, [vp]),
+        "h264r_stream_reset": (i32, [vp]),
         "h264r_stream_dpb_bytes": (u64, [P(R.CStreamCfg)]),
         "h264r_submit_picture": (i32, [vp, P(R.CPicture)]),
         "h264r_submit_picture_device": (i32, [vp, P(R.CPicture)]),
@@ -410,6 +411,10 @@ class Stream:
 
     def sync(self):
         return self.ctx.check(lib().h264r_stream_sync(self.h), "stream_sync")
+
+    def reset(self):
+        """Ready for a new bitstream of the same geometry (buffers cleared)."""
+        return self.ctx.check(lib().h264r_stream_reset(self.h), "stream_reset")
 
     def close(self):
         if self.h:

@@ -248,6 +248,12 @@ const char *h264r_last_error(const h264r_ctx *ctx);
  */
 int  h264r_stream_open(h264r_ctx *ctx, const h264r_stream_cfg *cfg, h264r_stream **out);
 int  h264r_stream_close(h264r_stream *s);
+/* Make an idle stream ready for a new bitstream of the same geometry, as a
+ * freshly opened one: its picture buffers are cleared again (queued on its
+ * CUDA stream, like the clear at open) and its pending output copies are
+ * waited for.  The stream must have no launch in flight.  A server reuses
+ * streams this way instead of closing and opening them per request. */
+int  h264r_stream_reset(h264r_stream *s);
 uint64_t h264r_stream_dpb_bytes(const h264r_stream_cfg *cfg);
 
 /*

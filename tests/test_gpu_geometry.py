@@ -138,3 +138,28 @@ def test_output_async_copies_survive_slot_reuse(gpu_ctx):
             assert np.array_equal(outs[k], expected[k]), k
     finally:
         s.close()
+
+
+@pytest.mark.gpu
+def test_reset_stream_decodes_like_a_new_one(gpu_ctx):
+    """h264r_stream_reset clears the picture buffers as h264r_stream_open
+    does: a P picture decoded first after a reset reads cleared references,
+    exactly as on a freshly opened stream (not the pictures decoded before)."""
+    g = h.synth("cif_ippp", seed=77, num_pictures=4, gop_length=4, gop_kind=0, intra_percent=0, skip_percent=0)
+    pics = list(g)
+    p = next(q for q in pics if q.group > 0)
+    fresh = h.Stream(gpu_ctx, p.width_mbs, p.height_mbs, g.dpb_slots)
+    fresh.submit(p)
+    want = fresh.output(p.dst_slot).copy()
+    fresh.close()
+    s = h.Stream(gpu_ctx, p.width_mbs, p.height_mbs, g.dpb_slots)
+    for q in pics:
+        s.submit(q)
+    s.sync()
+    stale = s.output(p.dst_slot).copy()
+    s.reset()
+    s.submit(p)
+    got = s.output(p.dst_slot).copy()
+    s.close()
+    assert not np.array_equal(stale, want), "the P picture does not depend on its reference"
+    assert np.array_equal(got, want)
