@@ -1206,7 +1206,7 @@ extern "C" int h264r_submit_picture_device(h264r_stream *s, const h264r_picture 
     return submit_device(ctx, s->cs, b, 1, arr, pic);
 }
 
-extern "C" int h264r_submit_batch_device(h264r_ctx *ctx, int n, h264r_stream *const *streams, const h264r_picture *pics)
+static int check_device_batch(h264r_ctx *ctx, int n, h264r_stream *const *streams, const h264r_picture *pics)
 {
     if (!ctx || n <= 0 || !streams || !pics) return H264R_ERR_INVALID_ARG;
     if ((uint32_t)n > ctx->max_batch) {
@@ -1221,11 +1221,33 @@ extern "C" int h264r_submit_batch_device(h264r_ctx *ctx, int n, h264r_stream *co
             return rc;
         }
     }
+    return H264R_OK;
+}
+
+extern "C" int h264r_submit_batch_device_on(h264r_ctx *ctx, void *cuda_stream, int n, h264r_stream *const *streams,
+                                            const h264r_picture *pics)
+{
+    int rc = check_device_batch(ctx, n, streams, pics);
+    if (rc) return rc;
+    if (!cuda_stream) return H264R_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);
     std::lock_guard<std::mutex> lk(ctx->mu);
     LaunchBuf &b = ctx->batch_ring[ctx->batch_next];
     ctx->batch_next = (ctx->batch_next + 1) % kBatchRing;
-    int rc = wait_slot(ctx, b);
+    rc = wait_slot(ctx, b);
+    if (rc) return rc;
+    return submit_device(ctx, (cudaStream_t)cuda_stream, b, n, streams, pics);
+}
+
+extern "C" int h264r_submit_batch_device(h264r_ctx *ctx, int n, h264r_stream *const *streams, const h264r_picture *pics)
+{
+    int rc = check_device_batch(ctx, n, streams, pics);
+    if (rc) return rc;
+    cudaSetDevice(ctx->device);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    LaunchBuf &b = ctx->batch_ring[ctx->batch_next];
+    ctx->batch_next = (ctx->batch_next + 1) % kBatchRing;
+    rc = wait_slot(ctx, b);
     if (rc) return rc;
     // the batch runs on the CUDA stream of its first member, after any work
     // already queued on the other members, which then wait for it
@@ -1401,6 +1423,26 @@ extern "C" int h264r_output_async(h264r_stream *s, int slot, uint8_t *y, uint8_t
         CUDA_OR(ctx, cudaMemcpyAsync(cr, base + W * H + W * H / 4, W * H / 4, cudaMemcpyDeviceToHost, s->out));
     }
     CUDA_OR(ctx, cudaEventRecord(s->slot_ev[slot], s->out));
+    s->slot_pending[slot] = 1;
+    return H264R_OK;
+}
+
+extern "C" int h264r_output_async_on(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *cr, void *cuda_stream)
+{
+    if (!s || slot < 0 || slot >= s->cfg.dpb_slots || !y || !cb || !cr || !cuda_stream) return H264R_ERR_INVALID_ARG;
+    h264r_ctx *ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    const cudaStream_t os = (cudaStream_t)cuda_stream;
+    const uint64_t W = s->cfg.width_mbs * 16ull, H = s->cfg.height_mbs * 16ull;
+    const uint8_t *base = s->dpb + (uint64_t)slot * s->slot_bytes;
+    if (cb == y + W * H && cr == cb + W * H / 4) {
+        CUDA_OR(ctx, cudaMemcpyAsync(y, base, W * H * 3 / 2, cudaMemcpyDeviceToHost, os));
+    } else {
+        CUDA_OR(ctx, cudaMemcpyAsync(y, base, W * H, cudaMemcpyDeviceToHost, os));
+        CUDA_OR(ctx, cudaMemcpyAsync(cb, base + W * H, W * H / 4, cudaMemcpyDeviceToHost, os));
+        CUDA_OR(ctx, cudaMemcpyAsync(cr, base + W * H + W * H / 4, W * H / 4, cudaMemcpyDeviceToHost, os));
+    }
+    CUDA_OR(ctx, cudaEventRecord(s->slot_ev[slot], os));  // a launch rewriting the slot waits for the copy
     s->slot_pending[slot] = 1;
     return H264R_OK;
 }

@@ -71,6 +71,7 @@ struct Item {
     uint8_t *out = nullptr;
     double t_push = 0;
     int slot = -1;
+    uint64_t up_seq = 0;  // order of its upload on the server's upload stream
     cudaEvent_t uploaded = nullptr, done = nullptr;
 };
 
@@ -124,6 +125,11 @@ struct h264r_server {
     std::deque<Batch> batch_done[kMaxLanes];
     std::vector<cudaEvent_t> ev_pool;
     cudaStream_t up = nullptr;
+    uint64_t up_seq = 0;
+    // per lane: the CUDA stream every batch of the lane runs on (so that a
+    // stream's batches follow each other with no per-member events) and the
+    // one its output copies run on
+    cudaStream_t lane_cs[kMaxLanes] = {}, lane_copy[kMaxLanes] = {};
     // device slots for uploaded records: stream-ordered allocations on `up`
     // from a pool of the server's own, so that a stream's slots come and go
     // without waiting for the device (nullptr: plain allocations)
@@ -301,6 +307,12 @@ bool admit(h264r_server *srv)
         S->admitted = true;
         S->slots.resize(srv->depth);
         srv->active.push_back(S);
+        {  // the clear of its buffers (open / reset, on its own CUDA stream) before the lane's batches
+            cudaEvent_t e = take_event(srv);
+            cudaEventRecord(e, (cudaStream_t)h264r_stream_cuda_stream(S->s));
+            cudaStreamWaitEvent(srv->lane_cs[S->id % srv->lanes], e, 0);
+            give_event(srv, e);
+        }
         srv->st.streams_open++;
         srv->st.dpb_bytes_in_use += S->dpb;
         srv->st.dpb_bytes_peak = std::max(srv->st.dpb_bytes_peak, srv->st.dpb_bytes_in_use);
@@ -382,6 +394,7 @@ bool upload(h264r_server *srv)
             }
             it->uploaded = take_event(srv);
             cudaEventRecord(it->uploaded, srv->up);
+            it->up_seq = ++srv->up_seq;
             sl.busy = true;
             it->slot = k;
             uint8_t *d = sl.dev;
@@ -431,10 +444,20 @@ bool launch_lane(h264r_server *srv, int lane, std::unique_lock<std::mutex> &lk)
     }
     if (pics.empty()) return false;
     lk.unlock();
-    // the records must be on the device before the batch reads them
+    // the records must be on the device before the batch reads them: the
+    // upload stream runs in order, so the last upload of the batch covers all
+    const cudaStream_t lcs = srv->lane_cs[lane], lcopy = srv->lane_copy[lane];
+    Item *last = items[0].second;
     for (auto &pr : items)
-        cudaStreamWaitEvent((cudaStream_t)h264r_stream_cuda_stream(pr.first->s), pr.second->uploaded, 0);
-    const int rc = h264r_submit_batch_device(srv->ctx, (int)pics.size(), ss.data(), pics.data());
+        if (pr.second->up_seq > last->up_seq) last = pr.second;
+    cudaStreamWaitEvent(lcs, last->uploaded, 0);
+    const int rc = h264r_submit_batch_device_on(srv->ctx, lcs, (int)pics.size(), ss.data(), pics.data());
+    cudaEvent_t be = nullptr;
+    if (rc == H264R_OK) {
+        be = take_event(srv);
+        cudaEventRecord(be, lcs);
+        cudaStreamWaitEvent(lcopy, be, 0);  // the output copies follow the batch
+    }
     // move the launched pictures from dev_q to flight (same order)
     for (auto &pr : items) {
         SStream *S = pr.first;
@@ -444,21 +467,16 @@ bool launch_lane(h264r_server *srv, int lane, std::unique_lock<std::mutex> &lk)
             S->flight.push_back(it);
             continue;
         }
-        cudaStream_t cs = (cudaStream_t)h264r_stream_cuda_stream(S->s);
+        cudaStream_t cs = lcs;
         if (it->out) {
-            // the copy runs on the stream's copy stream, beside its next batches
+            // the copy runs on the lane's copy stream, beside the lane's next batches
             const uint64_t W = S->cfg.width_mbs * 16ull, H = S->cfg.height_mbs * 16ull;
-            h264r_output_async(S->s, it->pic.dst_slot, it->out, it->out + W * H, it->out + W * H + W * H / 4);
-            cs = (cudaStream_t)h264r_stream_output_cuda_stream(S->s);
+            h264r_output_async_on(S->s, it->pic.dst_slot, it->out, it->out + W * H, it->out + W * H + W * H / 4, lcopy);
+            cs = lcopy;
         }
         it->done = take_event(srv);
         cudaEventRecord(it->done, cs);
         S->flight.push_back(it);
-    }
-    cudaEvent_t be = nullptr;
-    if (rc == H264R_OK) {
-        be = take_event(srv);
-        cudaEventRecord(be, (cudaStream_t)h264r_stream_cuda_stream(ss[0]));
     }
     lk.lock();
     if (rc != H264R_OK) {
@@ -517,6 +535,18 @@ extern "C" int h264r_server_create(h264r_ctx *ctx, const h264r_server_cfg *cfg, 
         delete srv;
         return H264R_ERR_CUDA;
     }
+    for (int l = 0; l < srv->lanes; l++) {
+        if (cudaStreamCreateWithFlags(&srv->lane_cs[l], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&srv->lane_copy[l], cudaStreamNonBlocking) != cudaSuccess) {
+            for (int k = 0; k <= l; k++) {
+                if (srv->lane_cs[k]) cudaStreamDestroy(srv->lane_cs[k]);
+                if (srv->lane_copy[k]) cudaStreamDestroy(srv->lane_copy[k]);
+            }
+            cudaStreamDestroy(srv->up);
+            delete srv;
+            return H264R_ERR_CUDA;
+        }
+    }
     cudaMemPoolProps pp = {};
     pp.allocType = cudaMemAllocationTypePinned;
     pp.handleTypes = cudaMemHandleTypeNone;
@@ -552,6 +582,12 @@ extern "C" int h264r_server_destroy(h264r_server *srv)
     for (auto e : srv->ev_pool) cudaEventDestroy(e);
     for (auto &kv : srv->pool) cudaFreeHost(kv.second);
     cudaStreamSynchronize(srv->up);
+    for (int l = 0; l < srv->lanes; l++) {
+        cudaStreamSynchronize(srv->lane_copy[l]);
+        cudaStreamSynchronize(srv->lane_cs[l]);
+        cudaStreamDestroy(srv->lane_copy[l]);
+        cudaStreamDestroy(srv->lane_cs[l]);
+    }
     if (srv->rec_pool) cudaMemPoolDestroy(srv->rec_pool);
     cudaStreamDestroy(srv->up);
     delete srv;

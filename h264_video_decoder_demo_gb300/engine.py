@@ -21,7 +21,8 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libh264r.so
 EXPORTS = [
     "h264r_ctx_create", "h264r_ctx_destroy", "h264r_last_error", "h264r_stream_open",
     "h264r_stream_close", "h264r_stream_reset", "h264r_stream_dpb_bytes", "h264r_submit_picture",
-    "h264r_submit_picture_device", "h264r_submit_batch_device", "h264r_output", "h264r_output_async",
+    "h264r_submit_picture_device", "h264r_submit_batch_device", "h264r_submit_batch_device_on", "h264r_output",
+    "h264r_output_async", "h264r_output_async_on",
     "h264r_load_slot", "h264r_slot_device_ptr", "h264r_stream_sync", "h264r_ctx_sync",
     "h264r_stream_cuda_stream", "h264r_stream_output_cuda_stream", "h264r_validate_picture", "h264r_ctx_kernel_launches",
     "h264r_ctx_set_timing", "h264r_ctx_last_timing", "h264r_ctx_kernel_timing", "h264r_ctx_set_wait_test",
@@ -82,8 +83,10 @@ def _load():
         "h264r_submit_picture": (i32, [vp, P(R.CPicture)]),
         "h264r_submit_picture_device": (i32, [vp, P(R.CPicture)]),
         "h264r_submit_batch_device": (i32, [vp, i32, P(vp), P(R.CPicture)]),
+        "h264r_submit_batch_device_on": (i32, [vp, vp, i32, P(vp), P(R.CPicture)]),
         "h264r_output": (i32, [vp, i32, vp, vp, vp]),
         "h264r_output_async": (i32, [vp, i32, vp, vp, vp]),
+        "h264r_output_async_on": (i32, [vp, i32, vp, vp, vp, vp]),
         "h264r_stream_output_cuda_stream": (vp, [vp]),
         "h264r_load_slot": (i32, [vp, i32, vp, vp, vp]),
         "h264r_slot_device_ptr": (i32, [vp, i32, P(vp)]),

@@ -284,6 +284,16 @@ int  h264r_submit_picture_device(h264r_stream *s, const h264r_picture *pic);
  */
 int  h264r_submit_batch_device(h264r_ctx *ctx, int n, h264r_stream *const *streams,
                                const h264r_picture *pics);
+/*
+ * The same on a CUDA stream of the caller's, with no ordering against the
+ * member streams' own CUDA streams: all earlier work that touches the
+ * members' picture buffers (earlier batches, the clear of a stream opened
+ * or reset, output copies) must be queued on cuda_stream or ordered before
+ * it.  A server that runs every batch of a set of streams on one CUDA stream
+ * saves the per-member event plumbing this way.
+ */
+int  h264r_submit_batch_device_on(h264r_ctx *ctx, void *cuda_stream, int n, h264r_stream *const *streams,
+                                  const h264r_picture *pics);
 
 /*
  * Batched reconstruction from host-resident records: the records of all n
@@ -320,6 +330,10 @@ int  h264r_output(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *c
  * asynchronous; call h264r_stream_sync before reading them.
  */
 int  h264r_output_async(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *cr);
+/* As h264r_output_async, on a CUDA stream of the caller's that is already
+ * ordered after the picture's batch (a later launch writing the slot still
+ * waits for the copy). */
+int  h264r_output_async_on(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *cr, void *cuda_stream);
 /*
  * Decoded picture (DPB slot) as BGR24 rows of row_bytes bytes (at least
  * 3*width, a multiple of 4, like the reference's bitmap rows), top-down, or
