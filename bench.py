@@ -682,7 +682,7 @@ def run_serving_sweep(args, device, pools, plain_fps):
     """Serving at rising arrival rates (short windows): the highest served
     throughput whose push-to-ready p99 stays under 33 ms."""
     points = []
-    for rate in (80.0, 160.0, 240.0, 320.0, 480.0):
+    for rate in (80.0, 160.0, 240.0, 280.0, 320.0, 480.0):
         r = run_serving(args, device, pools, rate=rate, seconds=args.sweep_seconds, seed=6000 + int(rate))
         points.append({k: r[k] for k in ("arrival_streams_per_s", "fps", "fps_1080p_equivalent", "p50_frame_ms",
                                          "p99_frame_ms", "pictures", "wall_s")})
