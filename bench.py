@@ -306,13 +306,14 @@ def run_mixed(args, device, seed=4000):
     generator puts two B between anchors), the CIF configuration's value
     distributions (MVs +-64 quarter samples, QP 20..36, 10% intra),
     records resident in HBM; every step reconstructs all 1920 pictures, one
-    fused launch per dependency group across all streams.  Reports frames/s
-    and MB/s."""
+    fused launch per dependency group of each of three stream sets.  Reports
+    frames/s and MB/s."""
     sizes = [(22, 18)] * 12 + [(80, 45)] * 12 + [(120, 68)] * 8
     kinds = [("cif_ippp", dict(width_mbs=w, height_mbs=hh)) for w, hh in sizes]
-    out = run_batched(device, kinds, 60, seed, dict(gop_kind=1, gop_length=15))
+    out = run_batched(device, kinds, 60, seed, dict(gop_kind=1, gop_length=15), pipelines=3)
     out["config"] = ("32 streams (12 CIF, 12 720p, 8 1080p) x 60 pictures, IBBP, CIF-configuration distributions, "
-                     "one launch per dependency group across all streams, records in HBM, single pipeline")
+                     "one launch per dependency group of each of 3 pipelines over disjoint stream sets (sizes "
+                     "interleaved), records in HBM")
     return out
 
 
@@ -322,15 +323,17 @@ def run_interlaced(args, device, seed=3000):
     the MB pairs field pairs, field references of either parity), GOP 12
     with B pictures, MVs +-128 quarter samples; 8 streams batched, records in
     HBM.  Frames/s counts a field pair as one frame."""
-    out = run_batched(device, ["1080i_mbaff"] * 8, 20, seed, dict(paff_percent=50))
+    out = run_batched(device, ["1080i_mbaff"] * 8, 20, seed, dict(paff_percent=50), pipelines=2)
     out["config"] = ("8 streams of 1080i x 20 frames: 50% PAFF field pairs, 50% MBAFF frames (50% field MB pairs), "
-                     "one launch per dependency group, records in HBM, single pipeline")
+                     "one launch per dependency group of each of 2 pipelines over disjoint stream sets, records in HBM")
     return out
 
 
-def run_batched(device, kinds, pictures, seed, overrides):
+def run_batched(device, kinds, pictures, seed, overrides, pipelines=1):
     """Frames/s of streams of the given workloads, batched per dependency
-    group across all streams, records resident in HBM (3 timed steps)."""
+    group across the streams of each of `pipelines` disjoint stream sets (the
+    batches of one set run beside the others'), records resident in HBM (3
+    timed steps)."""
     import numpy as np
     import torch
 
@@ -354,16 +357,18 @@ def run_batched(device, kinds, pictures, seed, overrides):
             row.append(c)
         cp.append(row)
     ngroups = max(p.group for ps in pics for p in ps) + 1
+    sets = [list(range(j, len(pics), pipelines)) for j in range(max(1, min(pipelines, len(pics))))]
     batches = []
     for g in range(ngroups):
-        ss, cc = [], []
-        for i, ps in enumerate(pics):
-            for k, p in enumerate(ps):
-                if p.group == g:
-                    ss.append(streams[i])
-                    cc.append(cp[i][k])
-        if ss:
-            batches.append((ss, cc))
+        for idxs in sets:
+            ss, cc = [], []
+            for i in idxs:
+                for k, p in enumerate(pics[i]):
+                    if p.group == g:
+                        ss.append(streams[i])
+                        cc.append(cp[i][k])
+            if ss:
+                batches.append((ss, cc))
     cs = torch.cuda.ExternalStream(streams[0].cuda_stream(), device=dev)
 
     def step():
