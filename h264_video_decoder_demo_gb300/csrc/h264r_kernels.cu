@@ -558,24 +558,28 @@ __device__ __forceinline__ void inter_body(InterWarpSmem (&smem)[W], const PicDe
         const h264r_weight wt = p.weights[pp.wt < p.num_weights ? pp.wt : 0];
         {
             const McWeight mw = mc_weight(wt, 0, use0, use1);
+            const uint32_t wp = mc_weight_pair(mw);
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 const uint32_t a = (i < 2 ? ya0 : ya1) >> (16 * (i & 1)), b = (i < 2 ? yb0 : yb1) >> (16 * (i & 1));
                 const int o = (by * 4 + i) * 16 + bx * 4 + 2 * half;
                 const int2 r = *(const int2 *)&s.res[o];
-                const int v0 = clip1(mc_weigh(mw, a & 255, b & 255) + r.x), v1 = clip1(mc_weigh(mw, (a >> 8) & 255, (b >> 8) & 255) + r.y);
-                *(uint16_t *)&s.out[o] = (uint16_t)(v0 | (v1 << 8));
+                int v0, v1;
+                mc_weigh2(mw, wp, a, b, v0, v1);
+                *(uint16_t *)&s.out[o] = (uint16_t)(clip1(v0 + r.x) | (clip1(v1 + r.y) << 8));
             }
         }
         {
             const McWeight mw = mc_weight(wt, 1 + half, use0, use1);
+            const uint32_t wp = mc_weight_pair(mw);
 #pragma unroll
             for (int i = 0; i < 2; i++) {
                 const uint32_t a = ca >> (16 * i), b = cb >> (16 * i);
                 const int o = 256 + half * 64 + (by * 2 + i) * 8 + bx * 2;
                 const int2 r = *(const int2 *)&s.res[o];
-                const int v0 = clip1(mc_weigh(mw, a & 255, b & 255) + r.x), v1 = clip1(mc_weigh(mw, (a >> 8) & 255, (b >> 8) & 255) + r.y);
-                *(uint16_t *)&s.out[o] = (uint16_t)(v0 | (v1 << 8));
+                int v0, v1;
+                mc_weigh2(mw, wp, a, b, v0, v1);
+                *(uint16_t *)&s.out[o] = (uint16_t)(clip1(v0 + r.x) | (clip1(v1 + r.y) << 8));
             }
         }
     }

@@ -68,6 +68,21 @@ __host__ __device__ __forceinline__ uint32_t mc_prmt(uint32_t a, uint32_t b, uin
 
 __host__ __device__ __forceinline__ int mc_clip1(int v) { return v < 0 ? 0 : (v > 255 ? 255 : v); }
 
+// c + signed 16-bit half 0 of a times unsigned byte 0 (lo) / 2 (hi) of b +
+// signed half 1 of a times byte 1 / 3 of b
+__host__ __device__ __forceinline__ int mc_dp2a(uint32_t a, uint32_t b, int c, bool hi)
+{
+#ifdef __CUDA_ARCH__
+    int d;
+    if (hi) asm("dp2a.hi.s32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    else asm("dp2a.lo.s32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+#else
+    const int sh = hi ? 16 : 0;
+    return c + (int)(int16_t)(a & 0xFFFFu) * (int)((b >> sh) & 255u) + (int)(int16_t)(a >> 16) * (int)((b >> (sh + 8)) & 255u);
+#endif
+}
+
 // per byte (a + b + 1) >> 1
 __host__ __device__ __forceinline__ uint32_t mc_avg4(uint32_t a, uint32_t b) { return (a | b) - (((a ^ b) >> 1) & 0x7F7F7F7Fu); }
 
@@ -204,43 +219,44 @@ struct McWeight {
     int w0, w1, round, shift, offset;
 };
 
+// Branch-free, so that the lanes of a MB mixing one- and two-list
+// partitions do not diverge: default prediction weighs a used list 1 (two
+// lists: round 1, shift 1); explicit weighting takes w / o of the used
+// lists, two lists round 2^logWD and shift logWD + 1 with the mean offset,
+// one list round 2^(logWD-1) and shift logWD when logWD >= 1.
 __host__ __device__ __forceinline__ McWeight mc_weight(const h264r_weight &w, int comp, bool use0, bool use1)
 {
-    McWeight m = {0, 0, 0, 0, 0};
-    if (!use0 && !use1) return m;
-    if (!w.weighted) {
-        if (use0 && use1) {
-            m.w0 = m.w1 = 1;
-            m.round = 1;
-            m.shift = 1;
-        } else {
-            (use0 ? m.w0 : m.w1) = 1;
-        }
-        return m;
-    }
+    McWeight m;
+    const bool wt = w.weighted != 0, bi = use0 && use1, any = use0 || use1;
     const int lw = w.log_wd[comp];
-    if (use0 && use1) {
-        m.w0 = w.w0[comp];
-        m.w1 = w.w1[comp];
-        m.round = 1 << lw;
-        m.shift = lw + 1;
-        m.offset = (w.o0[comp] + w.o1[comp] + 1) >> 1;
-        return m;
-    }
-    const bool first = use0 || comp == 0;
-    const int ww = first ? w.w0[comp] : w.w1[comp];
-    (use0 ? m.w0 : m.w1) = ww;
-    m.offset = first ? w.o0[comp] : w.o1[comp];
-    if (lw >= 1) {
-        m.round = 1 << (lw - 1);
-        m.shift = lw;
-    }
+    const int sw1 = comp == 0 ? w.w0[0] : w.w1[comp];  // list 1 alone: luma takes w0 / o0 (quirk)
+    const int so1 = comp == 0 ? w.o0[0] : w.o1[comp];
+    m.w0 = use0 ? (wt ? (int)w.w0[comp] : 1) : 0;
+    m.w1 = use1 ? (wt ? (bi ? (int)w.w1[comp] : sw1) : 1) : 0;
+    m.offset = (wt && any) ? (bi ? (w.o0[comp] + w.o1[comp] + 1) >> 1 : (use0 ? (int)w.o0[comp] : so1)) : 0;
+    m.shift = any ? (bi ? (wt ? lw + 1 : 1) : ((wt && lw >= 1) ? lw : 0)) : 0;
+    m.round = m.shift ? 1 << (m.shift - 1) : 0;
     return m;
 }
 
 __host__ __device__ __forceinline__ int mc_weigh(const McWeight &m, int p0, int p1)
 {
     return mc_clip1(((p0 * m.w0 + p1 * m.w1 + m.round) >> m.shift) + m.offset);
+}
+
+// mc_weigh of two samples at once: a holds list 0's predictions in bytes 0
+// and 1, b list 1's; w the weights as 16-bit halves (w0 | w1 << 16), so that
+// one byte permute and two dp2a give both weighted sums
+__host__ __device__ __forceinline__ uint32_t mc_weight_pair(const McWeight &m)
+{
+    return ((uint32_t)m.w0 & 0xFFFFu) | ((uint32_t)m.w1 << 16);
+}
+
+__host__ __device__ __forceinline__ void mc_weigh2(const McWeight &m, uint32_t w, uint32_t a, uint32_t b, int &v0, int &v1)
+{
+    const uint32_t src = mc_prmt(a, b, 0x5140u);  // a0 b0 a1 b1
+    v0 = mc_clip1((mc_dp2a(w, src, m.round, false) >> m.shift) + m.offset);
+    v1 = mc_clip1((mc_dp2a(w, src, m.round, true) >> m.shift) + m.offset);
 }
 
 }  // namespace h264r

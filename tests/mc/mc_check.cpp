@@ -194,6 +194,15 @@ int main()
         const int got = mc_weigh(mc_weight(hw, comp, use0, use1), p0, p1);
         if (got != want && bad++ < 5)
             fprintf(stderr, "weight comp %d use %d%d p %d %d: %d != %d\n", comp, use0, use1, p0, p1, got, want);
+        // two samples at once (dp2a form): the second pair of samples differs
+        const int q0 = (int)(rnd() & 255u), q1 = (int)(rnd() & 255u);
+        const McWeight mw = mc_weight(hw, comp, use0, use1);
+        int g0, g1;
+        mc_weigh2(mw, mc_weight_pair(mw), (uint32_t)p0 | ((uint32_t)q0 << 8) | 0xA5000000u,
+                  (uint32_t)p1 | ((uint32_t)q1 << 8) | 0x5A0000u, g0, g1);
+        const int want1 = weigh_ref(hw, comp, use0, use1, q0, q1);
+        if ((g0 != want || g1 != want1) && bad++ < 5)
+            fprintf(stderr, "weight pair comp %d use %d%d: %d %d != %d %d\n", comp, use0, use1, g0, g1, want, want1);
     }
     if (bad) {
         printf("%d mismatches\n", bad);
