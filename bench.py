@@ -238,8 +238,11 @@ def peak_hbm():
 # a side stream beside k_inter and k_intra, so the deblocking stage timed
 # after k_intra is the deblocking kernel alone.
 DRAM_BYTES_PER_MB = {"k_inter": 494, "k_intra": 418, "k_deblock_frame": 669}
-# Warp instructions per MB of k_inter on this mix (ncu smsp__inst_executed per
-# launch / MBs of the launch), for the issue-rate line of the roofline.
+# Warp instructions per MB of k_inter on a batch of nine B pictures of this
+# mix (ncu smsp__inst_executed per launch / MBs of the launch), for the
+# issue-rate line of the roofline: B MBs are the costliest of the step, so the
+# line is an upper bound.  Measured before the weighting rewrite, which took
+# 3.1 % off the instructions of a six-picture batch.
 K_INTER_WARP_INST_PER_MB = 1876
 
 
