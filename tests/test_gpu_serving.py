@@ -212,3 +212,67 @@ def test_server_fed_by_parser_threads_matches_reference():
         # the last picture is output without deblocking
         last_poc = [f for f in c["frames"] if f["yuv_md5"] == got[i][n - 1]]
         assert last_poc, "%s: last picture differs from the reference's output" % nm
+
+
+def test_batches_on_a_callers_stream_match_oracle():
+    """h264r_submit_batch_device_on / h264r_output_async_on (what the server's
+    lanes use): the pictures of two streams batched per dependency group on
+    one CUDA stream of the caller's, with no ordering through the streams' own
+    CUDA streams, and every frame copied out on a second one; a slot rewritten
+    by a later batch waits for its copy.  Every frame equals the oracle's."""
+    import ctypes
+
+    import torch
+
+    from oracle_cpu import OracleDPB
+    gens = [h.synth("cif_ippp", seed=s, num_pictures=14, gop_kind=1, gop_length=14) for s in (21, 22)]  # slots reused
+    pics = [list(g) for g in gens]
+    slots = [g.dpb_slots for g in gens]
+    dev = torch.device("cuda", 0)
+    keep = []
+
+    def to_dev(p):
+        c = p.to_c()
+        for name in R.Picture._ARRAYS:
+            a = np.ascontiguousarray(getattr(p, name)).view(np.uint8).reshape(-1)
+            t = torch.from_numpy(a.copy()).to(dev) if a.size else torch.empty(1, dtype=torch.uint8, device=dev)
+            keep.append(t)
+            setattr(c, name, t.data_ptr())
+        return c
+
+    L = h.engine.lib()
+    with h.Context(0) as ctx:
+        streams = [h.Stream(ctx, ps[0].width_mbs, ps[0].height_mbs, sl) for ps, sl in zip(pics, slots)]
+        cp = [[to_dev(p) for p in ps] for ps in pics]
+        torch.cuda.synchronize()
+        lane, copy = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+        for st in streams:  # the buffer clear queued at open, before the lane
+            ev = torch.cuda.Event()
+            ev.record(torch.cuda.ExternalStream(st.cuda_stream(), device=dev))
+            lane.wait_event(ev)
+        outs = {}
+        for g in range(max(p.group for ps in pics for p in ps) + 1):
+            items = [(i, k, p) for i, ps in enumerate(pics) for k, p in enumerate(ps) if p.group == g]
+            n = len(items)
+            arr = (ctypes.c_void_p * n)(*[streams[i].h.value for i, _, _ in items])
+            pa = (R.CPicture * n)(*[cp[i][k] for i, k, _ in items])
+            assert L.h264r_submit_batch_device_on(ctx.h, ctypes.c_void_p(lane.cuda_stream), n, arr, pa) == 0
+            ev = torch.cuda.Event()
+            ev.record(lane)
+            copy.wait_event(ev)
+            for i, k, p in items:
+                buf = torch.empty(p.plane_bytes, dtype=torch.uint8, pin_memory=True).numpy()
+                y, wh = buf.ctypes.data, p.width_mbs * p.height_mbs * 256
+                assert L.h264r_output_async_on(streams[i].h, p.dst_slot, y, y + wh, y + wh + wh // 4,
+                                               ctypes.c_void_p(copy.cuda_stream)) == 0
+                outs[(i, k)] = buf
+        copy.synchronize()
+        lane.synchronize()
+        for st in streams:
+            st.close()
+    for i, ps in enumerate(pics):
+        dpb = OracleDPB(ps[0].width_mbs, ps[0].height_mbs, slots[i])
+        for k, p in enumerate(ps):
+            rc, _ = dpb.reconstruct(p)
+            assert rc == 0
+            assert np.array_equal(outs[(i, k)], dpb.planes(p.dst_slot)), "stream %d picture %d" % (i, k)
