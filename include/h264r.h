@@ -252,7 +252,8 @@ int  h264r_stream_close(h264r_stream *s);
  * freshly opened one: its picture buffers are cleared again (queued on its
  * CUDA stream, like the clear at open) and its pending output copies are
  * waited for.  The stream must have no launch in flight.  A server reuses
- * streams this way instead of closing and opening them per request. */
+ * streams this way instead of closing and opening them per request.  No
+ * counterpart in the reference, which decodes one bitstream per decoder. */
 int  h264r_stream_reset(h264r_stream *s);
 uint64_t h264r_stream_dpb_bytes(const h264r_stream_cfg *cfg);
 
@@ -290,7 +291,8 @@ int  h264r_submit_batch_device(h264r_ctx *ctx, int n, h264r_stream *const *strea
  * members' picture buffers (earlier batches, the clear of a stream opened
  * or reset, output copies) must be queued on cuda_stream or ordered before
  * it.  A server that runs every batch of a set of streams on one CUDA stream
- * saves the per-member event plumbing this way.
+ * saves the per-member event plumbing this way.  No counterpart in the
+ * reference (one bitstream, one thread).
  */
 int  h264r_submit_batch_device_on(h264r_ctx *ctx, void *cuda_stream, int n, h264r_stream *const *streams,
                                   const h264r_picture *pics);
@@ -332,7 +334,9 @@ int  h264r_output(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *c
 int  h264r_output_async(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *cr);
 /* As h264r_output_async, on a CUDA stream of the caller's that is already
  * ordered after the picture's batch (a later launch writing the slot still
- * waits for the copy). */
+ * waits for the copy).  Replaces, like h264r_output, the reference's hand-off
+ * of a decoded picture (H264VideoDecoder.cpp:383-435), for callers that order
+ * their own streams. */
 int  h264r_output_async_on(h264r_stream *s, int slot, uint8_t *y, uint8_t *cb, uint8_t *cr, void *cuda_stream);
 /*
  * Decoded picture (DPB slot) as BGR24 rows of row_bytes bytes (at least
