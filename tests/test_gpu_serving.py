@@ -19,8 +19,12 @@ from h264_video_decoder_demo_gb300 import records as R
 
 pytestmark = pytest.mark.gpu
 
+# (generator, seed, pictures[, overrides]): progressive streams of three sizes,
+# a stream of field pictures (every frame a top and a bottom field, each its
+# own dependency group) and one of MBAFF frames
 MIX = [("cif_ippp", 11, 8), ("1080p_high", 31, 6), ("720p_high", 21, 6), ("cif_ippp", 12, 8),
-       ("1080p_high", 32, 6), ("720p_high", 22, 6), ("cif_ippp", 13, 8)]
+       ("1080p_high", 32, 6), ("720p_high", 22, 6), ("cif_ippp", 13, 8),
+       ("cif_ippp", 41, 5, dict(paff_percent=100)), ("1080i_mbaff", 42, 6, dict(width_mbs=22, height_mbs=18))]
 
 
 def md5(a):
@@ -29,8 +33,8 @@ def md5(a):
 
 def make_streams():
     out = []
-    for name, seed, n in MIX:
-        g = h.synth(name, seed=seed, num_pictures=n)
+    for name, seed, n, *over in MIX:
+        g = h.synth(name, seed=seed, num_pictures=n, **(over[0] if over else {}))
         pics = list(g)
         out.append((pics, g.dpb_slots))
         g.close()
