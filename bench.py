@@ -244,6 +244,10 @@ DRAM_BYTES_PER_MB = {"k_inter": 494, "k_intra": 418, "k_deblock_frame": 669}
 # line is an upper bound.  Measured before the weighting rewrite, which took
 # 3.1 % off the instructions of a six-picture batch.
 K_INTER_WARP_INST_PER_MB = 1876
+# The same for k_bs (a 1080p P picture) and the frame deblocking kernel (a
+# 1080p picture, its wavefront waits included), from their ncu summaries.
+K_BS_WARP_INST_PER_MB = 407
+K_DEBLOCK_WARP_INST_PER_MB = 784
 
 
 def dist_setup(args):
@@ -884,6 +888,13 @@ def run_engine(args, world, rank, local, dist):
                 "per_kernel": per_kernel,
                 "k_inter_issue": {"warp_inst_per_mb": K_INTER_WARP_INST_PER_MB, "mb_per_s": round(inter_mb_per_s, 1),
                                   "frac_of_issue_peak": round(K_INTER_WARP_INST_PER_MB * inter_mb_per_s / issue_peak, 4)},
+                # the issue rate of the other two MB-parallel and wavefront kernels, on the same
+                # footing: warp instructions per MB x MBs per second of their serialised time
+                "issue": {nm: {"warp_inst_per_mb": ipm,
+                               "frac_of_issue_peak": round(ipm * (mbs_step / (ktimes[k] / kt_steps / 1000.0)) / issue_peak, 4)
+                               if ktimes[k] > 0 else None}
+                          for nm, k, ipm in (("k_bs", 2, K_BS_WARP_INST_PER_MB),
+                                             ("k_deblock_frame", 3, K_DEBLOCK_WARP_INST_PER_MB))},
                 "kernel_timing": "%d steps after the timed region, one launch sequence in flight at a time, "
                                  "k_bs in line, CUDA events per kernel" % kt_steps}
 
