@@ -46,7 +46,7 @@ static_assert(sizeof(h264r_slice) == 8, "h264r_slice layout");
 namespace {
 
 constexpr int kRing = 4;                 // in-flight launches per stream
-constexpr int kBatchRing = 8;            // in-flight batched launches per context (all pipelines)
+constexpr int kBatchRing = 16;           // in-flight batched launches per context (all pipelines, server lanes)
 constexpr uint64_t kAlign = 256;
 constexpr unsigned long long kSpinLimit = 1ull << 25;  // ~ seconds of 64 ns sleeps
 

@@ -35,8 +35,8 @@
 namespace {
 
 constexpr uint64_t kAlign = 256;
-constexpr int kLanes = 4;               // default batch chains over disjoint stream sets
-                                        // (x 2 in flight: within the engine's launch ring of 8)
+constexpr int kLanes = 6;               // default batch chains over disjoint stream sets
+                                        // (x 2 in flight: within the engine's launch ring of 16)
 constexpr int kMaxLanes = 8;
 constexpr int kMaxBatchesInFlight = 2;  // per lane
 constexpr int kMaxGroupsInFlight = 2;   // per stream

@@ -39,7 +39,7 @@ typedef struct h264r_server_cfg {
                                     (uploaded or in flight), 0: 4             */
     uint32_t flags;              /* reserved, 0                               */
     uint32_t lanes;              /* batch chains over disjoint stream sets
-                                    (streams split by id; 0: 4, at most 8)    */
+                                    (streams split by id; 0: 6, at most 8)    */
 } h264r_server_cfg;
 
 /* One finished picture. */
